@@ -1,0 +1,109 @@
+// Device-side layout of the brick cache, shared by the cache kernels and the
+// ray caster.
+//
+// HBM layout (one allocation each, all 256-byte aligned):
+//   mrpd   uint4[mx*my*mz]   page directory, levels packed along x
+//                            (MultiResolutionPageDirectory.hpp:88-125): entry
+//                            {cacheX, cacheY, cacheZ, flag 0|1|2}
+//   req    uint32[mx*my*mz]  request timestamps, same indexing (CacheManager.hpp:239-249)
+//   usage  uint32[nslots]    last-use timestamp per pool slot (CacheDevice.hpp:133)
+//   order  uint32[nslots]x2  LRU order as slot ids (ping-pong); the reference
+//                            moves 28-byte LruContent records instead
+//   slot_level / slot_vpos   per-slot LruContent payload (level, volumePosition)
+//   pool   bytes             slot-major bricks: slot s = x + y*sx + z*sx*sy holds
+//                            B^3 voxels x-fastest (the reference uses a cudaArray
+//                            of (sx*B, sy*B, sz*B) voxels)
+#pragma once
+
+#include <cstdint>
+
+#include "gc_gb300.h"
+
+namespace gc {
+
+struct LevelTables {
+    uint32_t nlevels;
+    uint32_t off[GC_MAX_LEVELS];        // MRPD x offset of each level
+    uint32_t nb[GC_MAX_LEVELS][3];      // bricks per axis (MRPD level dimensions)
+    uint32_t vvox[GC_MAX_LEVELS][3];    // virtualized voxels per axis (= real sizes)
+    float ior[GC_MAX_LEVELS][3];        // initial / real size (CacheManager.hpp:271-285)
+};
+
+struct CacheView {
+    uint4 *mrpd;
+    uint32_t *req;
+    uint32_t *usage;
+    const uint8_t *pool;
+    uint32_t mx, my, mz;
+    uint32_t sx, sy, sz;
+    uint32_t B, c, Beff, eb;
+    uint32_t ts;
+};
+
+// Per-launch ray-caster parameters of one view.
+struct ViewParams {
+    float m[12];
+    uint32_t W, H;
+    float bmin[3], bmax[3];
+    float tstep, focal, early;
+    uint32_t mode, sampler;
+    uint32_t tfw;
+    const float *tf;
+    uint32_t *rgba;
+    float *tbuf;
+    float *state;
+    // LOD tables (display_volume_raycaster, VolumeRayCaster.cu:146-161)
+    float inv_size[GC_MAX_LEVELS][3];   // bboxSizeMin / initial level size
+    float step[GC_MAX_LEVELS];          // LODStepSize
+    float kexp[GC_MAX_LEVELS];          // LODStepSize / tstep (opacity correction exponent)
+    uint32_t tiles_x;                   // 8x4 warp tiles per row
+    uint32_t tile_begin;                // first global tile index of this view
+};
+
+// Scan control block shared by the decoupled look-back kernels.
+struct ScanCtl {
+    uint32_t ticket;
+    uint32_t done;
+    uint32_t err;
+    uint32_t total;     // result: flagged items of the last scan
+};
+
+constexpr uint32_t kErrLookback = 1u;   // a look-back wait ran out
+constexpr uint32_t kErrRender = 2u;     // render work-queue wait ran out
+
+// Host launchers (cache_kernels.cu).
+void launch_lru_count(const uint32_t *usage, uint32_t nslots, uint32_t ts, uint32_t *count, cudaStream_t s);
+void launch_lru_partition(const uint32_t *order_in, uint32_t *order_out, const uint32_t *usage, uint32_t ts,
+                          uint32_t nslots, const uint32_t *count, uint64_t *status, ScanCtl *ctl,
+                          uint32_t epoch, cudaStream_t s);
+void launch_miss_compact(const uint32_t *req, uint64_t nscan, uint32_t ts, uint32_t maxreq, uint4 *list,
+                         const LevelTables &lt, uint32_t mx, uint32_t my, uint64_t *status, ScanCtl *ctl,
+                         uint32_t epoch, cudaStream_t s);
+uint32_t lookback_tiles(uint64_t n);
+
+struct InstallArgs {
+    uint4 *mrpd;
+    uint32_t mx, my;
+    const uint32_t *order;     // current LRU order
+    uint32_t nslots;
+    uint32_t *slot_level;
+    float4 *slot_vpos;
+    uint8_t *pool;
+    uint32_t sx, sy;
+    uint32_t B, Beff, eb;
+    uint32_t BB[3];
+    const uint4 *asked;        // partitioned asked list: non-empty first
+    const uint32_t *big_index; // per non-empty brick
+    const uint4 *big_coord;    // per loaded big brick
+    const uint8_t *staging;    // loaded big bricks
+    uint32_t n, n_nonempty;
+};
+void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s);
+void launch_completude(const float4 *slot_vpos, uint32_t nslots, uint32_t *count, cudaStream_t s);
+
+// Ray caster (render.cu).
+void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams *views_dev,
+                   const ViewParams *views_host, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
+                   uint32_t *err, cudaStream_t s);
+
+}  // namespace gc

@@ -1,0 +1,393 @@
+// Per-frame cache kernels: LRU update, miss-list compaction, brick install,
+// completude.
+//
+// LRU update.  The reference builds a bool mask (create_usage_mask,
+// GcCore/src/cuda/libGPUCache/CacheManagerKernels.cu:8-29) and runs two
+// thrust::copy_if over 28-byte LruContent records into a freshly allocated
+// device_vector (CacheDevice.hpp:200-219): a stable partition, used slots
+// first.  That is one stable 1-bit radix pass on the key "used this frame"
+// (usage[slot] == timestamp).  Here the order is a list of 4-byte slot ids:
+//   lru_count      : total_used = #slots with usage == ts (one read of usage)
+//   lru_partition  : per 4096-item tile, ballot/popc + block scan of the used
+//                    flags, decoupled look-back for the tile's exclusive
+//                    prefix P, then used id -> out[P + rank], unused id at
+//                    global index i -> out[total_used + i - used_before(i)].
+// Miss list.  The reference compacts indexes i in [0, size - 1) with
+// req[i] == ts with thrust::copy_if over a counting iterator into a full-size
+// size_t vector, keeps the first 50 and decodes them with coord_1D_to_3D
+// (CacheManager.hpp:409-474, CacheManagerKernels.cu:32-72).  miss_compact
+// does the scan, cap and decode in one pass with the same look-back scan.
+// Every look-back wait is bounded; on expiry the kernel sets ScanCtl::err.
+#include <algorithm>
+
+#include "cache.cuh"
+#include "gc_internal.h"
+
+namespace gc {
+
+constexpr int kThreads = 256;
+constexpr int kItems = 16;
+constexpr uint32_t kTile = kThreads * kItems;
+constexpr uint32_t kMaxSpins = 1u << 22;
+
+__device__ __forceinline__ void st_release(uint64_t *p, uint64_t v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t ld_acquire(const uint64_t *p) {
+    uint64_t v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Exclusive scan of one value per thread over a 256-thread block.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &total) {
+    __shared__ uint32_t warp_tot[kThreads / 32];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= static_cast<uint32_t>(o)) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    uint32_t pre = 0, tot = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < kThreads / 32; ++w) {
+        const uint32_t t = warp_tot[w];
+        pre += (w < warp) ? t : 0u;
+        tot += t;
+    }
+    __syncthreads();
+    total = tot;
+    return pre + x - v;
+}
+
+// Decoupled look-back (single thread).  Status word: [63:62] flag
+// (1 aggregate, 2 inclusive prefix), [61:32] launch epoch, [31:0] value.
+__device__ uint32_t lookback(uint64_t *status, uint32_t tile, uint32_t agg, uint32_t epoch, uint32_t *err) {
+    const uint32_t ep = epoch & 0x3FFFFFFFu;
+    const uint64_t E = static_cast<uint64_t>(ep) << 32;
+    if (tile == 0) {
+        st_release(&status[0], (2ull << 62) | E | agg);
+        return 0;
+    }
+    st_release(&status[tile], (1ull << 62) | E | agg);
+    uint32_t excl = 0;
+    int64_t j = static_cast<int64_t>(tile) - 1;
+    uint32_t spins = 0;
+    while (j >= 0) {
+        const uint64_t s = ld_acquire(&status[j]);
+        const uint32_t flag = static_cast<uint32_t>(s >> 62);
+        const uint32_t sep = static_cast<uint32_t>(s >> 32) & 0x3FFFFFFFu;
+        if (sep != ep || flag == 0) {
+            if (++spins > kMaxSpins) {
+                atomicOr(err, kErrLookback);
+                break;
+            }
+            __nanosleep(64);
+            continue;
+        }
+        excl += static_cast<uint32_t>(s);
+        if (flag == 2) break;
+        --j;
+    }
+    st_release(&status[tile], (2ull << 62) | E | (excl + agg));
+    return excl;
+}
+
+// The last block of a launch resets the ticket so the next launch needs no memset.
+__device__ __forceinline__ void finish_tile(ScanCtl *ctl) {
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&ctl->done, 1u) == gridDim.x - 1) {
+            ctl->ticket = 0;
+            ctl->done = 0;
+            __threadfence();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) lru_count_kernel(const uint32_t *__restrict__ usage, uint32_t n,
+                                                        uint32_t ts, uint32_t *__restrict__ count) {
+    uint32_t c = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        c += (usage[i] == ts) ? 1u : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+__global__ void __launch_bounds__(kThreads) lru_partition_kernel(const uint32_t *__restrict__ order_in,
+                                                                 uint32_t *__restrict__ order_out,
+                                                                 const uint32_t *__restrict__ usage,
+                                                                 uint32_t ts, uint32_t n,
+                                                                 const uint32_t *__restrict__ count,
+                                                                 uint64_t *status, ScanCtl *ctl,
+                                                                 uint32_t epoch) {
+    __shared__ uint32_t s_tile, s_excl;
+    if (threadIdx.x == 0) s_tile = atomicAdd(&ctl->ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t base = static_cast<uint64_t>(tile) * kTile + threadIdx.x * kItems;
+    uint32_t ids[kItems];
+    uint32_t flags = 0;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const uint64_t i = base + k;
+        ids[k] = 0;
+        if (i < n) {
+            ids[k] = order_in[i];
+            flags |= (usage[ids[k]] == ts ? 1u : 0u) << k;
+        }
+    }
+    uint32_t tile_total;
+    const uint32_t excl_thread = block_exclusive_scan(__popc(flags), tile_total);
+    if (threadIdx.x == 0) s_excl = lookback(status, tile, tile_total, epoch, &ctl->err);
+    __syncthreads();
+    const uint32_t total_used = *count;
+    uint32_t used_before = s_excl + excl_thread;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const uint64_t i = base + k;
+        if (i < n) {
+            if ((flags >> k) & 1u)
+                order_out[used_before++] = ids[k];
+            else
+                order_out[total_used + static_cast<uint32_t>(i) - used_before] = ids[k];
+        }
+    }
+    finish_tile(ctl);
+}
+
+__device__ __forceinline__ uint4 decode_request(uint64_t i, uint32_t mx, uint32_t my, const LevelTables &lt) {
+    const uint64_t xy = static_cast<uint64_t>(mx) * my;
+    const uint32_t z = static_cast<uint32_t>(i / xy);
+    const uint64_t r = i - static_cast<uint64_t>(z) * xy;
+    const uint32_t y = static_cast<uint32_t>(r / mx);
+    const uint32_t x = static_cast<uint32_t>(r - static_cast<uint64_t>(y) * mx);
+    uint32_t sum = 0, level = 0;
+    for (level = 0; level < lt.nlevels; ++level) {
+        sum += lt.nb[level][0];
+        if (x < sum) break;
+    }
+    if (level >= lt.nlevels) level = lt.nlevels - 1;
+    return make_uint4(x - (sum - lt.nb[level][0]), y, z, level);
+}
+
+__global__ void __launch_bounds__(kThreads) miss_compact_kernel(const uint32_t *__restrict__ req, uint64_t nscan,
+                                                                uint32_t ts, uint32_t maxreq,
+                                                                uint4 *__restrict__ list, const LevelTables lt,
+                                                                uint32_t mx, uint32_t my, uint64_t *status,
+                                                                ScanCtl *ctl, uint32_t epoch) {
+    __shared__ uint32_t s_tile, s_excl;
+    if (threadIdx.x == 0) s_tile = atomicAdd(&ctl->ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t base = static_cast<uint64_t>(tile) * kTile + threadIdx.x * kItems;
+    uint32_t flags = 0;
+    if (base + kItems <= nscan) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(req + base);
+#pragma unroll
+        for (int q = 0; q < kItems / 4; ++q) {
+            const uint4 v = __ldcs(p + q);
+            flags |= ((v.x == ts) ? 1u : 0u) << (4 * q);
+            flags |= ((v.y == ts) ? 1u : 0u) << (4 * q + 1);
+            flags |= ((v.z == ts) ? 1u : 0u) << (4 * q + 2);
+            flags |= ((v.w == ts) ? 1u : 0u) << (4 * q + 3);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kItems; ++k)
+            if (base + k < nscan) flags |= ((req[base + k] == ts) ? 1u : 0u) << k;
+    }
+    uint32_t tile_total;
+    const uint32_t excl_thread = block_exclusive_scan(__popc(flags), tile_total);
+    if (threadIdx.x == 0) s_excl = lookback(status, tile, tile_total, epoch, &ctl->err);
+    __syncthreads();
+    uint32_t rank = s_excl + excl_thread;
+    if (flags && rank < maxreq) {
+        for (int k = 0; k < kItems && rank < maxreq; ++k) {
+            if ((flags >> k) & 1u) list[rank++] = decode_request(base + k, mx, my, lt);
+        }
+    }
+    if (threadIdx.x == 0 && tile == gridDim.x - 1) ctl->total = s_excl + tile_total;
+    finish_tile(ctl);
+}
+
+// ---------------------------------------------------------------------------
+// Brick install (CacheManager::load_new_bricks, CacheManager.hpp:502-632).
+
+// MRPD coordinate of a normalized brick origin (K_MultiResolutionPageDirectory::set,
+// K_MultiResolutionPageDirectory.hpp:193-205).
+__device__ __forceinline__ uint64_t mrpd_index(const LevelTables &lt, uint32_t level, float vx, float vy, float vz,
+                                               uint32_t mx, uint32_t my) {
+    const uint32_t x = lt.off[level] + static_cast<uint32_t>(__fmul_rn(vx, static_cast<float>(lt.nb[level][0])));
+    const uint32_t y = static_cast<uint32_t>(__fmul_rn(vy, static_cast<float>(lt.nb[level][1])));
+    const uint32_t z = static_cast<uint32_t>(__fmul_rn(vz, static_cast<float>(lt.nb[level][2])));
+    return x + static_cast<uint64_t>(y) * mx + static_cast<uint64_t>(z) * mx * my;
+}
+
+// compute_volume_position (CacheManagerKernels.cu:75-86):
+// x / (V.x * (1 / (B - 2c))) + FLT_EPSILON.
+__device__ __forceinline__ float4 brick_origin(const LevelTables &lt, uint4 b, float one_over_beff) {
+    const float eps = 1.1920928955078125e-7f;
+    float4 v;
+    v.x = __fadd_rn(__fdiv_rn(static_cast<float>(b.x), __fmul_rn(static_cast<float>(lt.vvox[b.w][0]), one_over_beff)), eps);
+    v.y = __fadd_rn(__fdiv_rn(static_cast<float>(b.y), __fmul_rn(static_cast<float>(lt.vvox[b.w][1]), one_over_beff)), eps);
+    v.z = __fadd_rn(__fdiv_rn(static_cast<float>(b.z), __fmul_rn(static_cast<float>(lt.vvox[b.w][2]), one_over_beff)), eps);
+    v.w = 0.f;
+    return v;
+}
+
+// dereference_old_bricks (CacheManagerKernels.hpp:115-145) for the LRU tail.
+__global__ void install_evict_kernel(InstallArgs a, const LevelTables lt) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n_nonempty) return;
+    const uint32_t slot = a.order[a.nslots - a.n_nonempty + i];
+    const float4 vp = a.slot_vpos[slot];
+    if (vp.x < 0.f) return;  // slot never held a brick
+    a.mrpd[mrpd_index(lt, a.slot_level[slot], vp.x, vp.y, vp.z, a.mx, a.my)] = make_uint4(0, 0, 0, 0);
+}
+
+// compute_lru_volume_position + copy_lru_position + write_brick
+// (CacheManagerKernels.cu:90-114, CacheManagerKernels.hpp:59-107): one block
+// per non-empty brick copies B^3 voxels from the staged big brick into the
+// LRU-tail slot, 16 bytes at a time when rows allow it.
+__global__ void __launch_bounds__(256) install_place_kernel(InstallArgs a, const LevelTables lt, float one_over_beff) {
+    const uint32_t i = blockIdx.x;
+    if (i >= a.n_nonempty) return;
+    const uint4 b = a.asked[i];
+    const uint32_t slot = a.order[a.nslots - a.n_nonempty + i];
+    if (threadIdx.x == 0) {
+        a.slot_level[slot] = b.w;
+        a.slot_vpos[slot] = brick_origin(lt, b, one_over_beff);
+    }
+    const uint32_t B = a.B, eb = a.eb;
+    const uint32_t bvx = a.BB[0] * B, bvy = a.BB[1] * B, bvz = a.BB[2] * B;
+    const uint64_t big_bytes = static_cast<uint64_t>(bvx) * bvy * bvz * eb;
+    const uint32_t bi = a.big_index[i];
+    const uint4 bc = a.big_coord[bi];
+    const uint32_t ox = (b.x - bc.x * a.BB[0]) * B, oy = (b.y - bc.y * a.BB[1]) * B, oz = (b.z - bc.z * a.BB[2]) * B;
+    const uint8_t *src = a.staging + bi * big_bytes;
+    uint8_t *dst = a.pool + static_cast<uint64_t>(slot) * B * B * B * eb;
+    const uint32_t row_bytes = B * eb;
+    const uint32_t rows = B * B;
+    if (row_bytes % 16 == 0 && (reinterpret_cast<uintptr_t>(src) % 16 == 0) && ((bvx * eb) % 16 == 0)) {
+        const uint32_t vec_per_row = row_bytes / 16;
+        for (uint32_t v = threadIdx.x; v < rows * vec_per_row; v += blockDim.x) {
+            const uint32_t r = v / vec_per_row, q = v % vec_per_row;
+            const uint32_t ly = r % B, lz = r / B;
+            const uint64_t soff = ((static_cast<uint64_t>(oz + lz) * bvy + (oy + ly)) * bvx + ox) * eb + q * 16;
+            const uint4 val = __ldcs(reinterpret_cast<const uint4 *>(src + soff));
+            reinterpret_cast<uint4 *>(dst + static_cast<uint64_t>(r) * row_bytes)[q] = val;
+        }
+    } else {
+        const uint32_t nbytes = rows * row_bytes;
+        for (uint32_t v = threadIdx.x; v < nbytes; v += blockDim.x) {
+            const uint32_t r = v / row_bytes, q = v % row_bytes;
+            const uint32_t ly = r % B, lz = r / B;
+            const uint64_t soff = ((static_cast<uint64_t>(oz + lz) * bvy + (oy + ly)) * bvx + ox) * eb + q;
+            dst[v] = src[soff];
+        }
+    }
+}
+
+// reference_new_bricks (CacheManagerKernels.hpp:308-357) for the MRPD-only
+// hierarchy: in list order (non-empty first), an unmapped entry becomes
+// {slot position, 1} or {0, 0, 0, 2} for an empty brick; an entry that is
+// already mapped or empty is left alone.  The reference walks the list in one
+// thread; here each brick is one thread and a brick whose MRPD entry also
+// belongs to an earlier list element yields to it, which is the serial order.
+__global__ void __launch_bounds__(1024) install_reference_kernel(InstallArgs a, const LevelTables lt,
+                                                                 float one_over_beff) {
+    extern __shared__ uint64_t s_coord[];
+    for (uint32_t i = threadIdx.x; i < a.n; i += blockDim.x) {
+        const uint4 b = a.asked[i];
+        const float4 v = brick_origin(lt, b, one_over_beff);
+        s_coord[i] = mrpd_index(lt, b.w, v.x, v.y, v.z, a.mx, a.my);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < a.n; i += blockDim.x) {
+        const uint64_t c = s_coord[i];
+        bool dup = false;
+        for (uint32_t j = 0; j < i; ++j)
+            if (s_coord[j] == c) {
+                dup = true;
+                break;
+            }
+        if (dup) continue;
+        const uint4 e = a.mrpd[c];
+        if (e.w >= 1) continue;
+        if (i < a.n_nonempty) {
+            const uint32_t slot = a.order[a.nslots - a.n_nonempty + i];
+            const uint32_t sx = slot % a.sx, sy = (slot / a.sx) % a.sy, sz = slot / (a.sx * a.sy);
+            a.mrpd[c] = make_uint4(sx * a.B, sy * a.B, sz * a.B, 1u);
+        } else {
+            a.mrpd[c] = make_uint4(0, 0, 0, 2u);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) completude_kernel(const float4 *__restrict__ vpos, uint32_t n,
+                                                         uint32_t *__restrict__ count) {
+    uint32_t c = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        c += (vpos[i].x != -1.f) ? 1u : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+// ---------------------------------------------------------------------------
+uint32_t lookback_tiles(uint64_t n) { return static_cast<uint32_t>(std::max<uint64_t>(1, (n + kTile - 1) / kTile)); }
+
+void launch_lru_count(const uint32_t *usage, uint32_t nslots, uint32_t ts, uint32_t *count, cudaStream_t s) {
+    GC_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), s));
+    const uint32_t grid = std::min<uint32_t>(div_up(nslots, 256), static_cast<uint32_t>(sm_count()) * 4);
+    lru_count_kernel<<<std::max(1u, grid), 256, 0, s>>>(usage, nslots, ts, count);
+    GC_CUDA(cudaGetLastError());
+}
+
+void launch_lru_partition(const uint32_t *order_in, uint32_t *order_out, const uint32_t *usage, uint32_t ts,
+                          uint32_t nslots, const uint32_t *count, uint64_t *status, ScanCtl *ctl,
+                          uint32_t epoch, cudaStream_t s) {
+    lru_partition_kernel<<<lookback_tiles(nslots), kThreads, 0, s>>>(order_in, order_out, usage, ts, nslots,
+                                                                     count, status, ctl, epoch);
+    GC_CUDA(cudaGetLastError());
+}
+
+void launch_miss_compact(const uint32_t *req, uint64_t nscan, uint32_t ts, uint32_t maxreq, uint4 *list,
+                         const LevelTables &lt, uint32_t mx, uint32_t my, uint64_t *status, ScanCtl *ctl,
+                         uint32_t epoch, cudaStream_t s) {
+    miss_compact_kernel<<<lookback_tiles(nscan), kThreads, 0, s>>>(req, nscan, ts, maxreq, list, lt, mx, my,
+                                                                   status, ctl, epoch);
+    GC_CUDA(cudaGetLastError());
+}
+
+void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s) {
+    if (a.n == 0) return;
+    const float one_over_beff = 1.0f / static_cast<float>(a.Beff);
+    if (a.n_nonempty) {
+        install_evict_kernel<<<div_up(a.n_nonempty, 128), 128, 0, s>>>(a, lt);
+        GC_CUDA(cudaGetLastError());
+        install_place_kernel<<<a.n_nonempty, 256, 0, s>>>(a, lt, one_over_beff);
+        GC_CUDA(cudaGetLastError());
+    }
+    const size_t smem = static_cast<size_t>(a.n) * sizeof(uint64_t);
+    GC_REQUIRE(smem <= 200 * 1024, "too many bricks in one install");
+    if (smem > 48 * 1024)
+        GC_CUDA(cudaFuncSetAttribute(install_reference_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+    install_reference_kernel<<<1, 1024, smem, s>>>(a, lt, one_over_beff);
+    GC_CUDA(cudaGetLastError());
+}
+
+void launch_completude(const float4 *slot_vpos, uint32_t nslots, uint32_t *count, cudaStream_t s) {
+    GC_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), s));
+    const uint32_t grid = std::min<uint32_t>(div_up(nslots, 256), static_cast<uint32_t>(sm_count()) * 4);
+    completude_kernel<<<std::max(1u, grid), 256, 0, s>>>(slot_vpos, nslots, count);
+    GC_CUDA(cudaGetLastError());
+}
+
+}  // namespace gc

@@ -1,0 +1,714 @@
+// Host side of the brick cache: the per-frame state machine of
+// CacheManager<T>::update (GcCore/include/GcCore/cuda/libGPUCache/CacheManager.hpp:318-354),
+// the request handler (RequestHandler.hpp:157-372) and the brick sources
+// (BricksManager::get_brick, GcCore/src/libData/BricksManager.cpp:48-78).
+//
+// Frame protocol (timestamp ts, starting at 1):
+//   render(ts)                 rays stamp usage[slot] = ts and req[brick] = ts
+//   update():
+//     LRU update               used slots first, stable        (always)
+//     loader busy              -> ts++, return false           (async mode only)
+//     a load finished          -> install it, return false
+//     otherwise                -> scan requests; none -> return true,
+//                                 else hand up to max_requests misses to the
+//                                 loader, return false
+//     ts++
+// With GC_CACHE_SYNC_LOADER the loader finishes inside update(), which gives
+// the reference's request -> install alternation deterministically.  Without
+// it a loader thread resolves bricks while later frames render, as the
+// reference's RequestHandler thread does; bricks then go up through a pinned
+// staging buffer with cudaMemcpyAsync on a side stream, and the install waits
+// on that copy's event instead of reading mapped host memory from the kernel.
+#include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <cstring>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "cache.cuh"
+#include "gc_internal.h"
+
+namespace gc {
+
+struct LruRecord {  // LruContent (LruContent.hpp:10-15)
+    uint32_t cx, cy, cz, level;
+    float vx, vy, vz;
+};
+static_assert(sizeof(LruRecord) == 28, "LruContent is 28 bytes");
+
+template <class T>
+static T *dalloc(size_t count, const char *what) {
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(count * sizeof(T), 16));
+    if (e != cudaSuccess) fail(GC_ERR_NOMEM, std::string("cudaMalloc failed for ") + what + ": " + cudaGetErrorString(e));
+    return static_cast<T *>(p);
+}
+template <class T>
+static T *halloc(size_t count) {
+    void *p = nullptr;
+    GC_CUDA(cudaHostAlloc(&p, std::max<size_t>(count * sizeof(T), 16), cudaHostAllocDefault));
+    return static_cast<T *>(p);
+}
+
+__global__ void init_slots_kernel(uint32_t *order, uint32_t *level, float4 *vpos, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        order[i] = i;
+        level[i] = 0;
+        vpos[i] = make_float4(-1.f, -1.f, -1.f, 0.f);
+    }
+}
+
+struct Source {
+    int kind = 0;  // 0 none, 1 host store, 2 callback
+    const uint8_t *host = nullptr;
+    std::vector<uint64_t> level_off;
+    gc_brick_loader_fn fn = nullptr;
+    void *user = nullptr;
+    std::unordered_set<uint64_t> empty;
+};
+
+}  // namespace gc
+
+struct gc_cache {
+    gc_cache_desc d;
+    gc::LevelTables lt;
+    uint32_t mx = 0, my = 0, mz = 0, nslots = 0, B = 0, c = 0, Beff = 0, eb = 0;
+    uint64_t nentries = 0, brick_bytes = 0, big_bytes = 0;
+    int device = 0;
+    // device buffers
+    uint4 *mrpd = nullptr;
+    uint32_t *req = nullptr, *usage = nullptr, *order[2] = {nullptr, nullptr}, *slot_level = nullptr;
+    float4 *slot_vpos = nullptr;
+    uint8_t *pool = nullptr;
+    uint64_t *status_lru = nullptr, *status_miss = nullptr;
+    gc::ScanCtl *ctl_lru = nullptr, *ctl_miss = nullptr;
+    uint32_t *d_count = nullptr, *d_misc = nullptr, *d_queue = nullptr;
+    uint4 *d_list = nullptr, *d_asked = nullptr, *d_big_coord = nullptr;
+    uint32_t *d_big_index = nullptr;
+    uint8_t *d_staging = nullptr;
+    gc::ViewParams *d_views = nullptr;
+    uint32_t max_views = 256;
+    // pinned host buffers
+    uint4 *h_list = nullptr, *h_asked = nullptr, *h_big_coord = nullptr;
+    uint32_t *h_total = nullptr, *h_big_index = nullptr, *h_misc = nullptr;
+    uint8_t *h_staging = nullptr;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_list = nullptr, ev_upload = nullptr;
+    int cur = 0;
+    uint32_t ts = 1, epoch_lru = 0, epoch_miss = 0;
+    // loader
+    gc::Source src;
+    std::thread th;
+    std::mutex mu;
+    std::condition_variable cv;
+    bool stop = false, has_request = false, busy = false, done = false, last_converged = false;
+    uint32_t pend_n = 0, pend_nonempty = 0;
+    std::string loader_error;
+    gc_cache_stats stats;
+
+    bool sync_mode() const { return (d.flags & GC_CACHE_SYNC_LOADER) != 0; }
+};
+
+namespace gc {
+
+static void build_tables(gc_cache *C) {
+    const gc_layout &L = C->d.layout;
+    LevelTables &lt = C->lt;
+    std::memset(&lt, 0, sizeof(lt));
+    lt.nlevels = L.nb_levels;
+    uint32_t off = 0;
+    C->mx = 0;
+    C->my = 0;
+    C->mz = 0;
+    for (uint32_t l = 0; l < L.nb_levels; ++l) {
+        lt.off[l] = off;
+        for (int a = 0; a < 3; ++a) {
+            lt.nb[l][a] = L.nb_bricks[l][a];
+            lt.vvox[l][a] = L.nb_bricks[l][a] * C->Beff;
+            lt.ior[l][a] = static_cast<float>(L.initial[l][a]) / static_cast<float>(L.real[l][a]);
+        }
+        off += L.nb_bricks[l][0];
+        C->my = std::max(C->my, L.nb_bricks[l][1]);
+        C->mz = std::max(C->mz, L.nb_bricks[l][2]);
+    }
+    C->mx = off;
+}
+
+// Resolve the asked bricks: RequestHandler::handle_request (RequestHandler.hpp:277-372).
+// Returns the number of bricks to install (non-empty first), or 0.
+static void resolve_and_upload(gc_cache *C, uint32_t n) {
+    const gc_volume_desc &v = C->d.volume;
+    const uint32_t BB[3] = {v.big_brick_size[0], v.big_brick_size[1], v.big_brick_size[2]};
+    std::unordered_map<uint64_t, int32_t> asked;
+    std::vector<int> kind(n, 0);  // 0 non-empty, 1 empty, 2 unknown (dropped)
+    uint32_t n_nonempty = 0, nbig = 0;
+    std::vector<uint32_t> big_index;
+    big_index.reserve(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint4 b = C->h_list[i];
+        const uint32_t gx = b.x / BB[0], gy = b.y / BB[1], gz = b.z / BB[2];
+        const uint64_t key = gc_brick_key(b.w, gx, gy, gz);
+        auto it = asked.find(key);
+        if (it != asked.end()) {
+            if (it->second == -1)
+                kind[i] = 1;
+            else if (it->second == -2)
+                kind[i] = 2;
+            else {
+                kind[i] = 0;
+                big_index.push_back(static_cast<uint32_t>(it->second));
+                ++n_nonempty;
+            }
+            continue;
+        }
+        int status = GC_BRICK_UNKNOWN;
+        if (C->src.empty.count(key)) {
+            status = GC_BRICK_EMPTY;
+        } else if (C->src.kind == 1) {
+            const gc_layout &L = C->d.layout;
+            if (b.w < L.nb_levels && gx < L.nb_big_bricks[b.w][0] && gy < L.nb_big_bricks[b.w][1] &&
+                gz < L.nb_big_bricks[b.w][2]) {
+                const uint64_t idx =
+                    (static_cast<uint64_t>(gz) * L.nb_big_bricks[b.w][1] + gy) * L.nb_big_bricks[b.w][0] + gx;
+                std::memcpy(C->h_staging + static_cast<uint64_t>(nbig) * C->big_bytes,
+                            C->src.host + C->src.level_off[b.w] + idx * C->big_bytes, C->big_bytes);
+                status = GC_BRICK_SUCCESS;
+            }
+        } else if (C->src.kind == 2) {
+            status = C->src.fn(C->src.user, b.w, gx, gy, gz,
+                               C->h_staging + static_cast<uint64_t>(nbig) * C->big_bytes, C->big_bytes);
+        }
+        if (status == GC_BRICK_SUCCESS) {
+            asked[key] = static_cast<int32_t>(nbig);
+            C->h_big_coord[nbig] = make_uint4(gx, gy, gz, b.w);
+            big_index.push_back(nbig);
+            ++nbig;
+            ++n_nonempty;
+            kind[i] = 0;
+        } else if (status == GC_BRICK_EMPTY) {
+            asked[key] = -1;
+            kind[i] = 1;
+        } else {
+            // The reference asserts here (RequestHandler.hpp:348-350).  The
+            // brick stays unmapped and is requested again by a later frame.
+            asked[key] = -2;
+            kind[i] = 2;
+            C->stats.load_errors++;
+        }
+    }
+    // stable partition: non-empty first, then empty (RequestHandler.hpp:354-369)
+    uint32_t k = 0;
+    for (uint32_t i = 0; i < n; ++i)
+        if (kind[i] == 0) C->h_asked[k++] = C->h_list[i];
+    for (uint32_t i = 0; i < n; ++i)
+        if (kind[i] == 1) C->h_asked[k++] = C->h_list[i];
+    std::memcpy(C->h_big_index, big_index.data(), big_index.size() * sizeof(uint32_t));
+    C->pend_n = k;
+    C->pend_nonempty = n_nonempty;
+    if (k == 0) return;
+    cudaStream_t s = C->side;
+    if (nbig)
+        GC_CUDA(cudaMemcpyAsync(C->d_staging, C->h_staging, static_cast<size_t>(nbig) * C->big_bytes,
+                                cudaMemcpyHostToDevice, s));
+    GC_CUDA(cudaMemcpyAsync(C->d_asked, C->h_asked, k * sizeof(uint4), cudaMemcpyHostToDevice, s));
+    if (n_nonempty) {
+        GC_CUDA(cudaMemcpyAsync(C->d_big_index, C->h_big_index, n_nonempty * sizeof(uint32_t),
+                                cudaMemcpyHostToDevice, s));
+        GC_CUDA(cudaMemcpyAsync(C->d_big_coord, C->h_big_coord, std::max(1u, nbig) * sizeof(uint4),
+                                cudaMemcpyHostToDevice, s));
+    }
+    GC_CUDA(cudaEventRecord(C->ev_upload, s));
+    C->stats.bytes_h2d += static_cast<uint64_t>(nbig) * C->big_bytes;
+    C->stats.requests_served += n;
+}
+
+// Waits for the miss list of the last scan and resolves it.  Returns true when
+// bricks are pending for install.
+static bool serve_request(gc_cache *C) {
+    GC_CUDA(cudaSetDevice(C->device));
+    GC_CUDA(cudaEventSynchronize(C->ev_list));
+    const uint32_t total = *C->h_total;
+    const uint32_t n = std::min(total, C->d.max_requests);
+    C->stats.last_requests = total;
+    C->stats.requests_raised += total;
+    if (n == 0) return false;
+    resolve_and_upload(C, n);
+    return C->pend_n > 0;
+}
+
+static void loader_main(gc_cache *C) {
+    std::unique_lock<std::mutex> lk(C->mu);
+    for (;;) {
+        C->cv.wait(lk, [&] { return C->stop || C->has_request; });
+        if (C->stop) return;
+        C->has_request = false;
+        lk.unlock();
+        bool pending = false, converged = false;
+        std::string err;
+        try {
+            pending = serve_request(C);
+            converged = (C->stats.last_requests == 0);
+        } catch (const std::exception &e) {
+            err = e.what();
+        }
+        lk.lock();
+        C->done = pending;
+        C->last_converged = converged;
+        if (!err.empty()) C->loader_error = err;
+        C->busy = false;
+        C->cv.notify_all();
+    }
+}
+
+static CacheView cache_view(const gc_cache *C) {
+    CacheView cv;
+    cv.mrpd = C->mrpd;
+    cv.req = C->req;
+    cv.usage = C->usage;
+    cv.pool = C->pool;
+    cv.mx = C->mx;
+    cv.my = C->my;
+    cv.mz = C->mz;
+    cv.sx = C->d.cache_size[0];
+    cv.sy = C->d.cache_size[1];
+    cv.sz = C->d.cache_size[2];
+    cv.B = C->B;
+    cv.c = C->c;
+    cv.Beff = C->Beff;
+    cv.eb = C->eb;
+    cv.ts = C->ts;
+    return cv;
+}
+
+static void lru_update(gc_cache *C, cudaStream_t s) {
+    launch_lru_count(C->usage, C->nslots, C->ts, C->d_count, s);
+    launch_lru_partition(C->order[C->cur], C->order[C->cur ^ 1], C->usage, C->ts, C->nslots, C->d_count,
+                         C->status_lru, C->ctl_lru, ++C->epoch_lru, s);
+    C->cur ^= 1;
+}
+
+static void install(gc_cache *C, cudaStream_t s) {
+    if (C->pend_n == 0) return;
+    GC_CUDA(cudaStreamWaitEvent(s, C->ev_upload, 0));
+    InstallArgs a;
+    a.mrpd = C->mrpd;
+    a.mx = C->mx;
+    a.my = C->my;
+    a.order = C->order[C->cur];
+    a.nslots = C->nslots;
+    a.slot_level = C->slot_level;
+    a.slot_vpos = C->slot_vpos;
+    a.pool = C->pool;
+    a.sx = C->d.cache_size[0];
+    a.sy = C->d.cache_size[1];
+    a.B = C->B;
+    a.Beff = C->Beff;
+    a.eb = C->eb;
+    for (int i = 0; i < 3; ++i) a.BB[i] = C->d.volume.big_brick_size[i];
+    a.asked = C->d_asked;
+    a.big_index = C->d_big_index;
+    a.big_coord = C->d_big_coord;
+    a.staging = C->d_staging;
+    a.n = C->pend_n;
+    a.n_nonempty = std::min(C->pend_nonempty, C->nslots);
+    launch_install(a, C->lt, s);
+    C->stats.bricks_installed += a.n_nonempty;
+    C->stats.bricks_empty += a.n - C->pend_nonempty;
+    C->pend_n = 0;
+    C->pend_nonempty = 0;
+}
+
+static void scan_requests(gc_cache *C, cudaStream_t s) {
+    launch_miss_compact(C->req, C->nentries - 1, C->ts, C->d.max_requests, C->d_list, C->lt, C->mx, C->my,
+                        C->status_miss, C->ctl_miss, ++C->epoch_miss, s);
+    GC_CUDA(cudaMemcpyAsync(C->h_list, C->d_list, C->d.max_requests * sizeof(uint4), cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaMemcpyAsync(C->h_total, &C->ctl_miss->total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaEventRecord(C->ev_list, s));
+}
+
+static bool update(gc_cache *C, cudaStream_t s) {
+    GC_CUDA(cudaSetDevice(C->device));
+    lru_update(C, s);
+    bool converged = false;
+    if (C->sync_mode()) {
+        if (C->done) {
+            install(C, s);
+            C->done = false;
+        } else {
+            scan_requests(C, s);
+            C->done = serve_request(C);
+            converged = (C->stats.last_requests == 0);
+        }
+    } else {
+        std::unique_lock<std::mutex> lk(C->mu);
+        if (!C->loader_error.empty()) {
+            std::string e = C->loader_error;
+            C->loader_error.clear();
+            fail(GC_ERR_IO, "brick loader: " + e);
+        }
+        if (C->busy) {
+            C->ts++;
+            C->stats.frames++;
+            return false;
+        }
+        if (C->done) {
+            lk.unlock();
+            install(C, s);
+            lk.lock();
+            C->done = false;
+        } else {
+            lk.unlock();
+            scan_requests(C, s);
+            lk.lock();
+            C->busy = true;
+            C->has_request = true;
+            C->cv.notify_all();
+            converged = C->last_converged;
+        }
+    }
+    C->ts++;
+    C->stats.frames++;
+    return converged;
+}
+
+static void destroy(gc_cache *C) {
+    if (C->th.joinable()) {
+        {
+            std::lock_guard<std::mutex> g(C->mu);
+            C->stop = true;
+            C->cv.notify_all();
+        }
+        C->th.join();
+    }
+    cudaSetDevice(C->device);
+    cudaDeviceSynchronize();
+    void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool,
+                   C->status_lru, C->status_miss, C->ctl_lru, C->ctl_miss, C->d_count, C->d_misc, C->d_queue,
+                   C->d_list, C->d_asked, C->d_big_coord, C->d_big_index, C->d_staging, C->d_views};
+    for (void *p : dev)
+        if (p) cudaFree(p);
+    void *host[] = {C->h_list, C->h_asked, C->h_big_coord, C->h_total, C->h_big_index, C->h_misc, C->h_staging};
+    for (void *p : host)
+        if (p) cudaFreeHost(p);
+    if (C->ev_list) cudaEventDestroy(C->ev_list);
+    if (C->ev_upload) cudaEventDestroy(C->ev_upload);
+    if (C->side) cudaStreamDestroy(C->side);
+    delete C;
+}
+
+// LOD tables of display_volume_raycaster (VolumeRayCaster.cu:136-161).
+static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
+    GC_REQUIRE(in.width > 0 && in.height > 0, "view size must be > 0");
+    GC_REQUIRE(in.rgba && in.tbuf && in.state, "view buffers must be set");
+    GC_REQUIRE(in.tf && in.tf_width >= 1, "transfer function must be set");
+    GC_REQUIRE(in.tstep > 0.f, "tstep must be > 0");
+    GC_REQUIRE(in.mode == GC_MODE_DVR || in.mode == GC_MODE_MOP, "bad compositing mode");
+    GC_REQUIRE(in.sampler == GC_SAMPLER_REFERENCE || in.sampler == GC_SAMPLER_TRILINEAR, "bad sampler");
+    GC_REQUIRE(C->c >= 1 || in.sampler == GC_SAMPLER_REFERENCE || true, "");
+    std::memset(&out, 0, sizeof(out));
+    std::memcpy(out.m, in.inv_view, sizeof(out.m));
+    out.W = in.width;
+    out.H = in.height;
+    for (int a = 0; a < 3; ++a) {
+        out.bmin[a] = in.bbox_min[a];
+        out.bmax[a] = in.bbox_max[a];
+    }
+    out.tstep = in.tstep;
+    out.focal = in.focal;
+    out.early = in.early_alpha;
+    out.mode = in.mode;
+    out.sampler = in.sampler;
+    out.tfw = in.tf_width;
+    out.tf = in.tf;
+    out.rgba = in.rgba;
+    out.tbuf = in.tbuf;
+    out.state = in.state;
+    const float bsx = in.bbox_max[0] - in.bbox_min[0];
+    const float bsy = in.bbox_max[1] - in.bbox_min[1];
+    const float bsz = in.bbox_max[2] - in.bbox_min[2];
+    const float bmin = std::min(bsx, std::min(bsy, bsz));
+    const gc_layout &L = C->d.layout;
+    for (uint32_t l = 0; l < L.nb_levels; ++l) {
+        for (int a = 0; a < 3; ++a) out.inv_size[l][a] = bmin / static_cast<float>(L.initial[l][a]);
+        const uint32_t mn = std::min(L.initial[l][0], std::min(L.initial[l][1], L.initial[l][2]));
+        out.step[l] = (bmin / static_cast<float>(mn)) / 2.f;
+        out.kexp[l] = out.step[l] / in.tstep;
+    }
+    out.tiles_x = div_up(in.width, 8);
+}
+
+static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s) {
+    GC_REQUIRE(views && n >= 1, "no views");
+    GC_REQUIRE(n <= C->max_views, "too many views in one batch");
+    GC_REQUIRE(C->d.volume.channels == 1, "the ray caster renders single-channel volumes");
+    GC_CUDA(cudaSetDevice(C->device));
+    std::vector<ViewParams> vp(n);
+    uint32_t tiles = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        fill_view(C, views[i], vp[i]);
+        vp[i].tile_begin = tiles;
+        tiles += vp[i].tiles_x * div_up(views[i].height, 4);
+    }
+    // pageable source: the call returns once the data is staged
+    GC_CUDA(cudaMemcpyAsync(C->d_views, vp.data(), n * sizeof(ViewParams), cudaMemcpyHostToDevice, s));
+    launch_render(cache_view(C), C->lt, C->d_views, vp.data(), n, tiles, C->d_queue, nullptr, s);
+}
+
+}  // namespace gc
+
+using namespace gc;
+
+extern "C" {
+
+int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out) {
+    gc_cache *C = nullptr;
+    int rc = guard([&] {
+        GC_REQUIRE(desc && out, "null argument");
+        validate_volume(desc->volume);
+        const gc_layout &L = desc->layout;
+        GC_REQUIRE(L.nb_levels >= 1 && L.nb_levels <= GC_MAX_LEVELS, "bad layout");
+        GC_REQUIRE(desc->max_requests >= 1 && desc->max_requests <= 16384, "max_requests must be in [1, 16384]");
+        for (int a = 0; a < 3; ++a) GC_REQUIRE(desc->cache_size[a] >= 1, "cache size must be >= 1");
+        C = new gc_cache();
+        std::memset(&C->stats, 0, sizeof(C->stats));
+        C->d = *desc;
+        C->device = desc->gpu;
+        GC_CUDA(cudaSetDevice(C->device));
+        C->B = desc->volume.brick_size;
+        C->c = desc->volume.covering;
+        C->Beff = C->B - 2 * C->c;
+        C->eb = desc->volume.encoded_bytes;
+        const uint64_t nslots = static_cast<uint64_t>(desc->cache_size[0]) * desc->cache_size[1] * desc->cache_size[2];
+        GC_REQUIRE(nslots < (1ull << 31), "too many pool slots");
+        C->nslots = static_cast<uint32_t>(nslots);
+        build_tables(C);
+        C->nentries = static_cast<uint64_t>(C->mx) * C->my * C->mz;
+        GC_REQUIRE(C->nentries >= 2, "page directory too small");
+        GC_REQUIRE(C->nentries < (1ull << 32), "page directory too large");
+        C->brick_bytes = static_cast<uint64_t>(C->B) * C->B * C->B * C->eb;
+        C->big_bytes = C->brick_bytes * desc->volume.big_brick_size[0] * desc->volume.big_brick_size[1] *
+                       desc->volume.big_brick_size[2];
+        const uint32_t maxr = desc->max_requests;
+        C->mrpd = dalloc<uint4>(C->nentries, "page directory");
+        C->req = dalloc<uint32_t>(C->nentries, "request buffer");
+        C->usage = dalloc<uint32_t>(C->nslots, "usage buffer");
+        C->order[0] = dalloc<uint32_t>(C->nslots, "LRU");
+        C->order[1] = dalloc<uint32_t>(C->nslots, "LRU");
+        C->slot_level = dalloc<uint32_t>(C->nslots, "slot levels");
+        C->slot_vpos = dalloc<float4>(C->nslots, "slot positions");
+        C->pool = dalloc<uint8_t>(C->nslots * C->brick_bytes, "brick pool");
+        C->status_lru = dalloc<uint64_t>(lookback_tiles(C->nslots), "scan status");
+        C->status_miss = dalloc<uint64_t>(lookback_tiles(C->nentries), "scan status");
+        C->ctl_lru = dalloc<ScanCtl>(1, "scan control");
+        C->ctl_miss = dalloc<ScanCtl>(1, "scan control");
+        C->d_count = dalloc<uint32_t>(1, "counter");
+        C->d_misc = dalloc<uint32_t>(1, "counter");
+        C->d_queue = dalloc<uint32_t>(4, "work queue");
+        C->d_list = dalloc<uint4>(maxr, "miss list");
+        C->d_asked = dalloc<uint4>(maxr, "asked list");
+        C->d_big_coord = dalloc<uint4>(maxr, "big brick coords");
+        C->d_big_index = dalloc<uint32_t>(maxr, "big brick indexes");
+        C->d_staging = dalloc<uint8_t>(maxr * C->big_bytes, "staging");
+        C->d_views = dalloc<ViewParams>(C->max_views, "views");
+        C->h_list = halloc<uint4>(maxr);
+        C->h_asked = halloc<uint4>(maxr);
+        C->h_big_coord = halloc<uint4>(maxr);
+        C->h_big_index = halloc<uint32_t>(maxr);
+        C->h_total = halloc<uint32_t>(1);
+        C->h_misc = halloc<uint32_t>(1);
+        C->h_staging = halloc<uint8_t>(maxr * C->big_bytes);
+        GC_CUDA(cudaMemset(C->mrpd, 0, C->nentries * sizeof(uint4)));
+        GC_CUDA(cudaMemset(C->req, 0, C->nentries * sizeof(uint32_t)));
+        GC_CUDA(cudaMemset(C->usage, 0, C->nslots * sizeof(uint32_t)));
+        GC_CUDA(cudaMemset(C->pool, 0, C->nslots * C->brick_bytes));
+        GC_CUDA(cudaMemset(C->status_lru, 0, lookback_tiles(C->nslots) * sizeof(uint64_t)));
+        GC_CUDA(cudaMemset(C->status_miss, 0, lookback_tiles(C->nentries) * sizeof(uint64_t)));
+        GC_CUDA(cudaMemset(C->ctl_lru, 0, sizeof(ScanCtl)));
+        GC_CUDA(cudaMemset(C->ctl_miss, 0, sizeof(ScanCtl)));
+        GC_CUDA(cudaMemset(C->d_queue, 0, 4 * sizeof(uint32_t)));
+        init_slots_kernel<<<std::min<uint32_t>(div_up(C->nslots, 256), 4096), 256>>>(C->order[0], C->slot_level,
+                                                                                    C->slot_vpos, C->nslots);
+        GC_CUDA(cudaGetLastError());
+        GC_CUDA(cudaStreamCreateWithFlags(&C->side, cudaStreamNonBlocking));
+        GC_CUDA(cudaEventCreateWithFlags(&C->ev_list, cudaEventDisableTiming));
+        GC_CUDA(cudaEventCreateWithFlags(&C->ev_upload, cudaEventDisableTiming));
+        GC_CUDA(cudaDeviceSynchronize());
+        if (!C->sync_mode()) C->th = std::thread(loader_main, C);
+        *out = C;
+    });
+    if (rc != GC_OK && C) destroy(C);
+    return rc;
+}
+
+int gc_cache_destroy(gc_cache_t cache) {
+    if (cache) destroy(cache);
+    return GC_OK;
+}
+
+int gc_cache_set_source_host(gc_cache_t C, const void *bricks, const uint64_t *level_offsets,
+                             const uint64_t *empty_keys, size_t n_empty) {
+    return guard([&] {
+        GC_REQUIRE(C && bricks && level_offsets, "null argument");
+        std::lock_guard<std::mutex> g(C->mu);
+        GC_REQUIRE(!C->busy, "the loader is busy");
+        C->src = Source();
+        C->src.kind = 1;
+        C->src.host = static_cast<const uint8_t *>(bricks);
+        C->src.level_off.assign(level_offsets, level_offsets + C->d.layout.nb_levels);
+        for (size_t i = 0; i < n_empty; ++i) C->src.empty.insert(empty_keys[i]);
+    });
+}
+
+int gc_cache_set_source_callback(gc_cache_t C, gc_brick_loader_fn fn, void *user, const uint64_t *empty_keys,
+                                 size_t n_empty) {
+    return guard([&] {
+        GC_REQUIRE(C && fn, "null argument");
+        std::lock_guard<std::mutex> g(C->mu);
+        GC_REQUIRE(!C->busy, "the loader is busy");
+        C->src = Source();
+        C->src.kind = 2;
+        C->src.fn = fn;
+        C->src.user = user;
+        for (size_t i = 0; i < n_empty; ++i) C->src.empty.insert(empty_keys[i]);
+    });
+}
+
+int gc_cache_update(gc_cache_t C, void *stream, int *converged) {
+    return guard([&] {
+        GC_REQUIRE(C, "null cache");
+        GC_REQUIRE(C->src.kind != 0, "no brick source set");
+        const bool r = update(C, as_stream(stream));
+        if (converged) *converged = r ? 1 : 0;
+    });
+}
+
+int gc_cache_completude(gc_cache_t C, void *stream, float *fraction) {
+    return guard([&] {
+        GC_REQUIRE(C && fraction, "null argument");
+        GC_CUDA(cudaSetDevice(C->device));
+        cudaStream_t s = as_stream(stream);
+        launch_completude(C->slot_vpos, C->nslots, C->d_misc, s);
+        GC_CUDA(cudaMemcpyAsync(C->h_misc, C->d_misc, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        GC_CUDA(cudaStreamSynchronize(s));
+        *fraction = static_cast<float>(*C->h_misc) / static_cast<float>(C->nslots);
+    });
+}
+
+int gc_cache_timestamp(gc_cache_t C, uint32_t *ts) {
+    return guard([&] {
+        GC_REQUIRE(C && ts, "null argument");
+        *ts = C->ts;
+    });
+}
+
+int gc_cache_info_get(gc_cache_t C, gc_cache_info *out) {
+    return guard([&] {
+        GC_REQUIRE(C && out, "null argument");
+        std::memset(out, 0, sizeof(*out));
+        out->mrpd_dims[0] = C->mx;
+        out->mrpd_dims[1] = C->my;
+        out->mrpd_dims[2] = C->mz;
+        out->nb_slots = C->nslots;
+        out->slot_voxels = C->B * C->B * C->B;
+        for (uint32_t l = 0; l < C->lt.nlevels; ++l) out->level_offset[l] = C->lt.off[l];
+        out->pool_bytes = static_cast<uint64_t>(C->nslots) * C->brick_bytes;
+    });
+}
+
+int gc_cache_stats_get(gc_cache_t C, gc_cache_stats *out) {
+    return guard([&] {
+        GC_REQUIRE(C && out, "null argument");
+        GC_CUDA(cudaSetDevice(C->device));
+        ScanCtl a, b;
+        GC_CUDA(cudaMemcpy(&a, C->ctl_lru, sizeof(a), cudaMemcpyDeviceToHost));
+        GC_CUDA(cudaMemcpy(&b, C->ctl_miss, sizeof(b), cudaMemcpyDeviceToHost));
+        std::lock_guard<std::mutex> g(C->mu);
+        *out = C->stats;
+        out->device_error = a.err | b.err;
+    });
+}
+
+int gc_cache_dump(gc_cache_t C, int what, void *dst, size_t bytes) {
+    return guard([&] {
+        GC_REQUIRE(C && dst, "null argument");
+        GC_CUDA(cudaSetDevice(C->device));
+        GC_CUDA(cudaDeviceSynchronize());
+        switch (what) {
+            case GC_DUMP_MRPD:
+                GC_REQUIRE(bytes == C->nentries * sizeof(uint4), "wrong size for the page directory");
+                GC_CUDA(cudaMemcpy(dst, C->mrpd, bytes, cudaMemcpyDeviceToHost));
+                break;
+            case GC_DUMP_REQUESTS:
+                GC_REQUIRE(bytes == C->nentries * sizeof(uint32_t), "wrong size for the request buffer");
+                GC_CUDA(cudaMemcpy(dst, C->req, bytes, cudaMemcpyDeviceToHost));
+                break;
+            case GC_DUMP_USAGE:
+                GC_REQUIRE(bytes == C->nslots * sizeof(uint32_t), "wrong size for the usage buffer");
+                GC_CUDA(cudaMemcpy(dst, C->usage, bytes, cudaMemcpyDeviceToHost));
+                break;
+            case GC_DUMP_POOL:
+                GC_REQUIRE(bytes == C->nslots * C->brick_bytes, "wrong size for the pool");
+                GC_CUDA(cudaMemcpy(dst, C->pool, bytes, cudaMemcpyDeviceToHost));
+                break;
+            case GC_DUMP_LRU: {
+                GC_REQUIRE(bytes == C->nslots * sizeof(LruRecord), "wrong size for the LRU");
+                std::vector<uint32_t> order(C->nslots), level(C->nslots);
+                std::vector<float4> vpos(C->nslots);
+                GC_CUDA(cudaMemcpy(order.data(), C->order[C->cur], C->nslots * 4, cudaMemcpyDeviceToHost));
+                GC_CUDA(cudaMemcpy(level.data(), C->slot_level, C->nslots * 4, cudaMemcpyDeviceToHost));
+                GC_CUDA(cudaMemcpy(vpos.data(), C->slot_vpos, C->nslots * 16, cudaMemcpyDeviceToHost));
+                LruRecord *r = static_cast<LruRecord *>(dst);
+                const uint32_t sx = C->d.cache_size[0], sy = C->d.cache_size[1];
+                for (uint32_t i = 0; i < C->nslots; ++i) {
+                    const uint32_t s = order[i];
+                    r[i].cx = (s % sx) * C->B;
+                    r[i].cy = ((s / sx) % sy) * C->B;
+                    r[i].cz = (s / (sx * sy)) * C->B;
+                    r[i].level = level[s];
+                    r[i].vx = vpos[s].x;
+                    r[i].vy = vpos[s].y;
+                    r[i].vz = vpos[s].z;
+                }
+                break;
+            }
+            default: fail(GC_ERR_INVALID, "unknown dump selector");
+        }
+    });
+}
+
+int gc_cache_load_buffer(gc_cache_t C, int what, const void *src, size_t bytes) {
+    return guard([&] {
+        GC_REQUIRE(C && src, "null argument");
+        GC_CUDA(cudaSetDevice(C->device));
+        GC_CUDA(cudaDeviceSynchronize());
+        if (what == GC_DUMP_USAGE) {
+            GC_REQUIRE(bytes == C->nslots * sizeof(uint32_t), "wrong size for the usage buffer");
+            GC_CUDA(cudaMemcpy(C->usage, src, bytes, cudaMemcpyHostToDevice));
+        } else if (what == GC_DUMP_REQUESTS) {
+            GC_REQUIRE(bytes == C->nentries * sizeof(uint32_t), "wrong size for the request buffer");
+            GC_CUDA(cudaMemcpy(C->req, src, bytes, cudaMemcpyHostToDevice));
+        } else {
+            fail(GC_ERR_INVALID, "only the usage and request buffers can be loaded");
+        }
+    });
+}
+
+int gc_render(gc_cache_t C, const gc_view *view, void *stream) {
+    return guard([&] {
+        GC_REQUIRE(C && view, "null argument");
+        render(C, view, 1, as_stream(stream));
+    });
+}
+
+int gc_render_batch(gc_cache_t C, const gc_view *views, uint32_t n, void *stream) {
+    return guard([&] {
+        GC_REQUIRE(C && views, "null argument");
+        render(C, views, n, as_stream(stream));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,353 @@
+// Preprocessor kernels: mip pyramid (2x2x2 box reduction), bricking with a
+// covering border, and empty-brick flags.  Everything stays resident in HBM;
+// the reference streams 512 MB chunks through cudaMalloc/H2D/kernel/D2H/free
+// per chunk (GcCore/src/cuda/libPreprocessor/Mipmapper.cu:401-578) and bricks
+// on the CPU with one seek+read per brick row
+// (GcCore/src/libPreprocessor/Bricker_v2.cpp:79-252).
+#include <cstring>
+
+#include "gc_internal.h"
+
+namespace gc {
+
+// ---------------------------------------------------------------------------
+// mip_reduce: one 2x2x2 pass.
+//
+// Reference arithmetic (down_sampling_inner, Mipmapper.cu:29-105):
+//   8-bit channels : uint64 sum of the 8 inputs, integer division by 8;
+//   16-bit, 1 ch.  : double sum (its initial value is uninitialised in the
+//                    reference; zero here), / 8.0, truncating conversion;
+//                    the sum of 8 u16 is exact so this is floor(sum / 8);
+//   f32            : double sum in (z, y, x) loop order, / 8.0, rounded to float.
+// The reference handles interleaved channels only on the 8-bit path; here every
+// integer channel width uses the per-channel floor mean.
+//
+// Vector kernel: one thread per 16-byte chunk of each of the 4 input rows
+// (y0,z0), (y1,z0), (y0,z1), (y1,z1); it writes the 8 output bytes that chunk
+// reduces to.  Every input byte is read once, with 128-bit loads.
+template <int CB, int NC>
+__device__ inline void reduce_chunk(const uint4 (&r)[4], uint2 &out) {
+    if constexpr (CB == 1) {
+        const uint8_t *b0 = reinterpret_cast<const uint8_t *>(&r[0]);
+        const uint8_t *b1 = reinterpret_cast<const uint8_t *>(&r[1]);
+        const uint8_t *b2 = reinterpret_cast<const uint8_t *>(&r[2]);
+        const uint8_t *b3 = reinterpret_cast<const uint8_t *>(&r[3]);
+        uint8_t *o = reinterpret_cast<uint8_t *>(&out);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int i = j / NC, c = j % NC;
+            const int a = (2 * i) * NC + c, b = (2 * i + 1) * NC + c;
+            uint32_t s = b0[a] + b0[b] + b1[a] + b1[b] + b2[a] + b2[b] + b3[a] + b3[b];
+            o[j] = static_cast<uint8_t>(s / 8u);
+        }
+    } else if constexpr (CB == 2) {
+        const uint16_t *h0 = reinterpret_cast<const uint16_t *>(&r[0]);
+        const uint16_t *h1 = reinterpret_cast<const uint16_t *>(&r[1]);
+        const uint16_t *h2 = reinterpret_cast<const uint16_t *>(&r[2]);
+        const uint16_t *h3 = reinterpret_cast<const uint16_t *>(&r[3]);
+        uint16_t *o = reinterpret_cast<uint16_t *>(&out);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int i = j / NC, c = j % NC;
+            const int a = (2 * i) * NC + c, b = (2 * i + 1) * NC + c;
+            uint32_t s = h0[a] + h0[b] + h1[a] + h1[b] + h2[a] + h2[b] + h3[a] + h3[b];
+            o[j] = static_cast<uint16_t>(s / 8u);
+        }
+    } else {
+        const float *f0 = reinterpret_cast<const float *>(&r[0]);
+        const float *f1 = reinterpret_cast<const float *>(&r[1]);
+        const float *f2 = reinterpret_cast<const float *>(&r[2]);
+        const float *f3 = reinterpret_cast<const float *>(&r[3]);
+        float *o = reinterpret_cast<float *>(&out);
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            double s = 0.0;
+            s += f0[2 * i];
+            s += f0[2 * i + 1];
+            s += f1[2 * i];
+            s += f1[2 * i + 1];
+            s += f2[2 * i];
+            s += f2[2 * i + 1];
+            s += f3[2 * i];
+            s += f3[2 * i + 1];
+            o[i] = static_cast<float>(s / 8.0);
+        }
+    }
+}
+
+struct MipParams {
+    uint32_t X, Y, Z;            // source dims
+    uint32_t oX, oY, oZ;         // output dims
+    uint64_t in_row, out_row;    // bytes per row
+    uint32_t chunks;             // 16-byte chunks per input row that produce output
+    uint64_t total;              // chunks * oY * oZ
+};
+
+template <int CB, int NC>
+__global__ void __launch_bounds__(256) mip_vec_kernel(const uint8_t *__restrict__ src,
+                                                      uint8_t *__restrict__ dst, MipParams p) {
+    for (uint64_t t = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; t < p.total;
+         t += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint32_t chunk = static_cast<uint32_t>(t % p.chunks);
+        const uint64_t orow = t / p.chunks;
+        const uint32_t oy = static_cast<uint32_t>(orow % p.oY), oz = static_cast<uint32_t>(orow / p.oY);
+        const uint64_t r00 = (static_cast<uint64_t>(2 * oz) * p.Y + 2 * oy) * p.in_row;
+        const uint64_t plane = static_cast<uint64_t>(p.Y) * p.in_row;
+        const uint64_t off = static_cast<uint64_t>(chunk) * 16;
+        uint4 r[4];
+        r[0] = __ldcs(reinterpret_cast<const uint4 *>(src + r00 + off));
+        r[1] = __ldcs(reinterpret_cast<const uint4 *>(src + r00 + p.in_row + off));
+        r[2] = __ldcs(reinterpret_cast<const uint4 *>(src + r00 + plane + off));
+        r[3] = __ldcs(reinterpret_cast<const uint4 *>(src + r00 + plane + p.in_row + off));
+        uint2 o;
+        reduce_chunk<CB, NC>(r, o);
+        *reinterpret_cast<uint2 *>(dst + (static_cast<uint64_t>(oz) * p.oY + oy) * p.out_row + chunk * 8) = o;
+    }
+}
+
+// Generic path (any width, odd sizes): one thread per output channel value.
+__global__ void mip_scalar_kernel(const uint8_t *__restrict__ src, uint8_t *__restrict__ dst,
+                                  MipParams p, uint32_t cb, uint32_t nc) {
+    const uint64_t n = static_cast<uint64_t>(p.oX) * p.oY * p.oZ * nc;
+    for (uint64_t t = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; t < n;
+         t += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint32_t c = static_cast<uint32_t>(t % nc);
+        const uint64_t v = t / nc;
+        const uint32_t ox = static_cast<uint32_t>(v % p.oX);
+        const uint64_t r = v / p.oX;
+        const uint32_t oy = static_cast<uint32_t>(r % p.oY), oz = static_cast<uint32_t>(r / p.oY);
+        const uint64_t eb = static_cast<uint64_t>(cb) * nc;
+        uint64_t isum = 0;
+        double dsum = 0.0;
+        for (int dz = 0; dz < 2; ++dz)
+            for (int dy = 0; dy < 2; ++dy)
+                for (int dx = 0; dx < 2; ++dx) {
+                    const uint64_t vox = (static_cast<uint64_t>(2 * oz + dz) * p.Y + (2 * oy + dy)) * p.X + (2 * ox + dx);
+                    const uint8_t *ptr = src + vox * eb + c * cb;
+                    if (cb == 1)
+                        isum += *ptr;
+                    else if (cb == 2)
+                        isum += *reinterpret_cast<const uint16_t *>(ptr);
+                    else
+                        dsum += *reinterpret_cast<const float *>(ptr);
+                }
+        uint8_t *o = dst + ((static_cast<uint64_t>(oz) * p.oY + oy) * p.oX + ox) * eb + c * cb;
+        if (cb == 1)
+            *o = static_cast<uint8_t>(isum / 8u);
+        else if (cb == 2)
+            *reinterpret_cast<uint16_t *>(o) = static_cast<uint16_t>(isum / 8u);
+        else
+            *reinterpret_cast<float *>(o) = static_cast<float>(dsum / 8.0);
+    }
+}
+
+static void launch_mip(const void *src, void *dst, const uint32_t d[3], uint32_t eb, uint32_t nc,
+                       cudaStream_t s) {
+    GC_REQUIRE(eb % nc == 0, "encoded bytes must be a multiple of channels");
+    const uint32_t cb = eb / nc;
+    GC_REQUIRE(cb == 1 || cb == 2 || cb == 4, "bytes per channel must be 1, 2 or 4");
+    MipParams p;
+    p.X = d[0];
+    p.Y = d[1];
+    p.Z = d[2];
+    p.oX = d[0] / 2;
+    p.oY = d[1] / 2;
+    p.oZ = d[2] / 2;
+    GC_REQUIRE(p.oX && p.oY && p.oZ, "level too small to down-sample");
+    p.in_row = static_cast<uint64_t>(p.X) * eb;
+    p.out_row = static_cast<uint64_t>(p.oX) * eb;
+    const int grid = sm_count() * 8;
+    const bool aligned = (reinterpret_cast<uintptr_t>(src) % 16 == 0) &&
+                         (reinterpret_cast<uintptr_t>(dst) % 8 == 0) && (p.X % 2 == 0) &&
+                         (p.in_row % 16 == 0);
+    if (aligned) {
+        p.chunks = static_cast<uint32_t>(p.in_row / 16);
+        p.total = static_cast<uint64_t>(p.chunks) * p.oY * p.oZ;
+        auto *in = static_cast<const uint8_t *>(src);
+        auto *out = static_cast<uint8_t *>(dst);
+        if (cb == 1 && nc == 1)
+            mip_vec_kernel<1, 1><<<grid, 256, 0, s>>>(in, out, p);
+        else if (cb == 1 && nc == 2)
+            mip_vec_kernel<1, 2><<<grid, 256, 0, s>>>(in, out, p);
+        else if (cb == 1 && nc == 4)
+            mip_vec_kernel<1, 4><<<grid, 256, 0, s>>>(in, out, p);
+        else if (cb == 2 && nc == 1)
+            mip_vec_kernel<2, 1><<<grid, 256, 0, s>>>(in, out, p);
+        else if (cb == 2 && nc == 2)
+            mip_vec_kernel<2, 2><<<grid, 256, 0, s>>>(in, out, p);
+        else if (cb == 4 && nc == 1)
+            mip_vec_kernel<4, 1><<<grid, 256, 0, s>>>(in, out, p);
+        else
+            mip_scalar_kernel<<<grid, 256, 0, s>>>(in, out, p, cb, nc);
+    } else {
+        mip_scalar_kernel<<<grid, 256, 0, s>>>(static_cast<const uint8_t *>(src),
+                                                static_cast<uint8_t *>(dst), p, cb, nc);
+    }
+    GC_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// Bricking: small brick (bx, by, bz) of level dims D covers voxels
+// [b * (B - 2c) - c, b * (B - 2c) - c + B) per axis; voxels outside the level
+// are zero (Bricker_v2.cpp:145-200), and so is every small brick whose start
+// b * (B - 2c) is outside the level on some axis.  Output layout: big bricks in (z, y, x)
+// raster order, each (BB*B)^3 voxels x-fastest; small brick (i, j, k) of a big
+// brick at voxel offset (i*B, j*B, k*B) (Bricker_v2.cpp:149-152, 295-299).
+struct BrickParams {
+    uint32_t D[3];
+    uint32_t B, c, Beff;
+    uint32_t BB[3];
+    uint32_t nbig[3];     // big bricks per axis
+    uint32_t eb;
+    uint64_t nsmall;      // small bricks in the level
+};
+
+__global__ void __launch_bounds__(256) brick_kernel(const uint8_t *__restrict__ level,
+                                                    uint8_t *__restrict__ out, BrickParams p) {
+    const uint32_t B = p.B;
+    const uint32_t bvx = p.BB[0] * B, bvy = p.BB[1] * B;
+    const uint64_t big_bytes = static_cast<uint64_t>(bvx) * bvy * (p.BB[2] * B) * p.eb;
+    for (uint64_t sb = blockIdx.x; sb < p.nsmall; sb += gridDim.x) {
+        // small brick grid = nbig * BB per axis, x fastest
+        const uint32_t nsx = p.nbig[0] * p.BB[0], nsy = p.nbig[1] * p.BB[1];
+        const uint32_t sx = static_cast<uint32_t>(sb % nsx);
+        const uint32_t sy = static_cast<uint32_t>((sb / nsx) % nsy);
+        const uint32_t sz = static_cast<uint32_t>(sb / (static_cast<uint64_t>(nsx) * nsy));
+        const uint32_t gx = sx / p.BB[0], gy = sy / p.BB[1], gz = sz / p.BB[2];
+        const uint32_t ix = sx % p.BB[0], iy = sy % p.BB[1], iz = sz % p.BB[2];
+        const uint64_t big = (static_cast<uint64_t>(gz) * p.nbig[1] + gy) * p.nbig[0] + gx;
+        uint8_t *bbase = out + big * big_bytes;
+        const int64_t ox = static_cast<int64_t>(sx) * p.Beff - p.c;
+        const int64_t oy = static_cast<int64_t>(sy) * p.Beff - p.c;
+        const int64_t oz = static_cast<int64_t>(sz) * p.Beff - p.c;
+        // The reference visits a small brick only if its start lies inside the
+        // level on every axis (Bricker_v2.cpp:203-221); the others stay zero even
+        // where their covering border reaches into the volume.
+        const bool visited = static_cast<uint64_t>(sx) * p.Beff < p.D[0] &&
+                             static_cast<uint64_t>(sy) * p.Beff < p.D[1] && static_cast<uint64_t>(sz) * p.Beff < p.D[2];
+        const uint32_t nvox = B * B * B;
+        for (uint32_t v = threadIdx.x; v < nvox; v += blockDim.x) {
+            const uint32_t lx = v % B, ly = (v / B) % B, lz = v / (B * B);
+            const int64_t gx_ = ox + lx, gy_ = oy + ly, gz_ = oz + lz;
+            uint8_t *dptr = bbase + ((static_cast<uint64_t>(iz * B + lz) * bvy + (iy * B + ly)) * bvx + (ix * B + lx)) * p.eb;
+            const bool inside = visited && gx_ >= 0 && gy_ >= 0 && gz_ >= 0 && gx_ < p.D[0] && gy_ < p.D[1] &&
+                                gz_ < p.D[2];
+            const uint8_t *sptr = level + ((static_cast<uint64_t>(gz_) * p.D[1] + gy_) * p.D[0] + gx_) * p.eb;
+            switch (p.eb) {
+                case 1: *dptr = inside ? __ldg(sptr) : 0; break;
+                case 2:
+                    *reinterpret_cast<uint16_t *>(dptr) = inside ? __ldg(reinterpret_cast<const uint16_t *>(sptr)) : 0;
+                    break;
+                case 4:
+                    *reinterpret_cast<uint32_t *>(dptr) = inside ? __ldg(reinterpret_cast<const uint32_t *>(sptr)) : 0;
+                    break;
+                default:
+                    for (uint32_t b = 0; b < p.eb; ++b) dptr[b] = inside ? sptr[b] : 0;
+            }
+        }
+    }
+}
+
+// Empty flags: 1 if every channel value of the big brick is < threshold
+// (DefaultBrickProcessorPredicate: (float)value < threshold).
+__global__ void __launch_bounds__(256) empty_kernel(const uint8_t *__restrict__ bricks, uint64_t nbig,
+                                                    uint64_t big_values, uint32_t cb, float threshold,
+                                                    uint8_t *__restrict__ flags) {
+    __shared__ int s_nonempty;
+    for (uint64_t b = blockIdx.x; b < nbig; b += gridDim.x) {
+        if (threadIdx.x == 0) s_nonempty = 0;
+        __syncthreads();
+        const uint8_t *base = bricks + b * big_values * cb;
+        int nonempty = 0;
+        for (uint64_t i = threadIdx.x; i < big_values && !nonempty; i += blockDim.x) {
+            float v;
+            if (cb == 1)
+                v = static_cast<float>(base[i]);
+            else if (cb == 2)
+                v = static_cast<float>(reinterpret_cast<const uint16_t *>(base)[i]);
+            else
+                v = reinterpret_cast<const float *>(base)[i];
+            if (!(v < threshold)) nonempty = 1;
+        }
+        if (__syncthreads_or(nonempty) && threadIdx.x == 0) s_nonempty = 1;
+        __syncthreads();
+        if (threadIdx.x == 0) flags[b] = s_nonempty ? 0 : 1;
+        __syncthreads();
+    }
+}
+
+}  // namespace gc
+
+using namespace gc;
+
+extern "C" {
+
+int gc_mip_level(const void *src, void *dst, const uint32_t src_dims[3], uint32_t encoded_bytes,
+                 uint32_t channels, void *stream) {
+    return guard([&] {
+        GC_REQUIRE(src && dst && src_dims, "null argument");
+        GC_REQUIRE(channels >= 1, "channels must be >= 1");
+        launch_mip(src, dst, src_dims, encoded_bytes, channels, as_stream(stream));
+    });
+}
+
+int gc_mip_build(void *pyramid, const gc_layout *layout, const uint64_t *level_offsets,
+                 uint32_t encoded_bytes, uint32_t channels, void *stream) {
+    return guard([&] {
+        GC_REQUIRE(pyramid && layout && level_offsets, "null argument");
+        GC_REQUIRE(layout->nb_levels >= 1 && layout->nb_levels <= GC_MAX_LEVELS, "bad layout");
+        GC_REQUIRE(level_offsets[0] == 0, "level 0 must start at offset 0");
+        uint8_t *base = static_cast<uint8_t *>(pyramid);
+        for (uint32_t l = 1; l < layout->nb_levels; ++l) {
+            const uint32_t *d = layout->mip[l - 1];
+            for (int a = 0; a < 3; ++a)
+                GC_REQUIRE(layout->mip[l][a] == d[a] / 2,
+                           "level sizes that stop halving (dimension <= 2) are not supported");
+            launch_mip(base + level_offsets[l - 1], base + level_offsets[l], d, encoded_bytes, channels,
+                       as_stream(stream));
+        }
+    });
+}
+
+int gc_bricks_build(const void *level, const uint32_t level_dims[3], const gc_volume_desc *vol,
+                    const uint32_t nb_big_bricks[3], void *out, void *stream) {
+    return guard([&] {
+        GC_REQUIRE(level && level_dims && vol && nb_big_bricks && out, "null argument");
+        validate_volume(*vol);
+        BrickParams p;
+        for (int a = 0; a < 3; ++a) {
+            p.D[a] = level_dims[a];
+            p.BB[a] = vol->big_brick_size[a];
+            p.nbig[a] = nb_big_bricks[a];
+            GC_REQUIRE(p.nbig[a] > 0, "nb_big_bricks must be > 0");
+        }
+        p.B = vol->brick_size;
+        p.c = vol->covering;
+        p.Beff = p.B - 2 * p.c;
+        p.eb = vol->encoded_bytes;
+        p.nsmall = static_cast<uint64_t>(p.nbig[0] * p.BB[0]) * (p.nbig[1] * p.BB[1]) * (p.nbig[2] * p.BB[2]);
+        const uint64_t grid = std::min<uint64_t>(p.nsmall, static_cast<uint64_t>(sm_count()) * 16);
+        brick_kernel<<<static_cast<unsigned>(grid), 256, 0, as_stream(stream)>>>(
+            static_cast<const uint8_t *>(level), static_cast<uint8_t *>(out), p);
+        GC_CUDA(cudaGetLastError());
+    });
+}
+
+int gc_bricks_empty(const void *bricks, uint64_t nb_big_bricks, const gc_volume_desc *vol,
+                    float threshold, uint8_t *flags, void *stream) {
+    return guard([&] {
+        GC_REQUIRE(bricks && vol && flags, "null argument");
+        validate_volume(*vol);
+        const uint64_t B = vol->brick_size;
+        const uint64_t values = B * B * B * vol->big_brick_size[0] * vol->big_brick_size[1] *
+                                vol->big_brick_size[2] * vol->channels;
+        if (nb_big_bricks == 0) return;
+        const uint64_t grid = std::min<uint64_t>(nb_big_bricks, static_cast<uint64_t>(sm_count()) * 16);
+        empty_kernel<<<static_cast<unsigned>(grid), 256, 0, as_stream(stream)>>>(
+            static_cast<const uint8_t *>(bricks), nb_big_bricks, values, channel_bytes(*vol), threshold,
+            flags);
+        GC_CUDA(cudaGetLastError());
+    });
+}
+
+}  // extern "C"

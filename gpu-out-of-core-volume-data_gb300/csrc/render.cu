@@ -1,0 +1,442 @@
+// dvr_march: the out-of-core DVR / MIP ray caster.
+//
+// Per-ray method of RayCastDVRImpl / RayCastMOPImpl
+// (Applications/DVR-ray-caster/src/RayCasters.cu:35-349): eye ray from the
+// 3x4 camera matrix, slab test against the bounding box, front-to-back march
+// with a per-sample LOD from the projected pixel footprint (compute_LOD,
+// RayCasters.cu:551-567), page-directory walk and brick sampling through the
+// cache (K_CacheManager::get_normalized, K_CacheManager.hpp:265-361;
+// K_CacheDevice::compute_element_position, K_CacheDevice.hpp:314-336),
+// transfer function, opacity correction 1 - (1 - a)^(LODStep / tstep),
+// premultiplied compositing, early termination, progressive resume through the
+// t / colour-state buffers, truncating RGBA8 pack (RayCasters.cu:528-536).
+//
+// This translation unit is compiled with -fmad=false: every float expression
+// below is a sequence of IEEE-rounded operations in source order, so the host
+// oracle evaluates the same values.  Where the reference calls approximate
+// device functions, this kernel uses exactly-rounded ones:
+//   normalize: v * (1 / sqrtf(v.v))           (reference: rsqrtf)
+//   powf:      gc_pow, series log2/exp2 below (reference: CUDA powf)
+//   texture:   explicit loads and FP32 lerps  (reference: texture unit with
+//                                              8-bit fractional weights)
+//
+// GB300 mapping: persistent warps pull 8x4-pixel tiles from a global queue
+// (one queue across every view of a batch), so neighbouring rays of a warp
+// walk the same bricks; each thread caches its last page-directory entry and
+// stamps the usage word only when the entry changes; brick voxels are read
+// through the read-only path from the slot-major HBM pool.
+#include <algorithm>
+#include <climits>
+
+#include "cache.cuh"
+#include "gc_internal.h"
+
+namespace gc {
+
+constexpr uint32_t kRenderThreads = 128;
+
+struct V3 {
+    float x, y, z;
+};
+__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float length(V3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ V3 normalize(V3 a) {
+    const float inv = 1.0f / sqrtf(dot(a, a));
+    return a * inv;
+}
+__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+    return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float clampf(float f, float a, float b) { return fmaxf(a, fminf(f, b)); }
+__device__ __forceinline__ float saturate(float x) { return (x != x) ? 0.0f : fminf(fmaxf(x, 0.0f), 1.0f); }
+
+// log2 for normal x > 0: x = m 2^e, m in [sqrt(1/2), sqrt(2)), then
+// ln m = 2 atanh(s), s = (m - 1)/(m + 1), by its odd series to s^9.
+__device__ __forceinline__ float gc_log2(float x) {
+    const uint32_t bits = __float_as_uint(x);
+    int e = static_cast<int>((bits >> 23) & 0xffu) - 126;
+    float m = __uint_as_float((bits & 0x807fffffu) | (126u << 23));  // [0.5, 1)
+    if (m < 0.70710678f) {
+        m = m * 2.0f;
+        e -= 1;
+    }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    float p = s2 * 0.11111111f + 0.14285715f;
+    p = p * s2 + 0.2f;
+    p = p * s2 + 0.33333334f;
+    p = p * s2 + 1.0f;
+    const float ln = (2.0f * s) * p;
+    return static_cast<float>(e) + ln * 1.44269504f;
+}
+// exp2 for y <= 0: y = n + f, f in [-1/2, 1/2], e^(f ln 2) by Taylor to degree 7.
+__device__ __forceinline__ float gc_exp2(float y) {
+    if (y < -125.0f) return 0.0f;
+    const float n = floorf(y + 0.5f);
+    const float t = (y - n) * 0.69314718f;
+    float p = t * 0.00019841270f + 0.0013888889f;
+    p = p * t + 0.0083333333f;
+    p = p * t + 0.041666668f;
+    p = p * t + 0.16666667f;
+    p = p * t + 0.5f;
+    p = p * t + 1.0f;
+    p = p * t + 1.0f;
+    const float scale = __uint_as_float(static_cast<uint32_t>(static_cast<int>(n) + 127) << 23);
+    return p * scale;
+}
+__device__ __forceinline__ float gc_pow(float x, float k) {
+    if (!(x > 0.0f)) return 0.0f;
+    if (x == 1.0f) return 1.0f;
+    return gc_exp2(k * gc_log2(x));
+}
+
+__device__ __forceinline__ float4 tf_lookup(const float *__restrict__ tf, uint32_t w, float s) {
+    const float xb = s * static_cast<float>(w) - 0.5f;
+    const float fl = floorf(xb);
+    const float a = xb - fl;
+    int i0 = static_cast<int>(fl);
+    int i1 = i0 + 1;
+    const int hi = static_cast<int>(w) - 1;
+    i0 = i0 < 0 ? 0 : (i0 > hi ? hi : i0);
+    i1 = i1 < 0 ? 0 : (i1 > hi ? hi : i1);
+    const float4 t0 = __ldg(reinterpret_cast<const float4 *>(tf) + i0);
+    const float4 t1 = __ldg(reinterpret_cast<const float4 *>(tf) + i1);
+    return make_float4(t0.x + (t1.x - t0.x) * a, t0.y + (t1.y - t0.y) * a, t0.z + (t1.z - t0.z) * a,
+                       t0.w + (t1.w - t0.w) * a);
+}
+
+template <typename T>
+struct VoxelTraits;
+template <>
+struct VoxelTraits<uint8_t> {
+    static constexpr float kSum8 = 2040.0f;
+    static constexpr float kMax = 255.0f;
+};
+template <>
+struct VoxelTraits<uint16_t> {
+    static constexpr float kSum8 = 524280.0f;
+    static constexpr float kMax = 65535.0f;
+};
+template <>
+struct VoxelTraits<float> {
+    static constexpr float kSum8 = 8.0f;
+    static constexpr float kMax = 1.0f;
+};
+
+// Reference sampler: normalized linear read at the integer voxel corner e =
+// (lx, ly, lz) of the slot = mean of voxels {e-1, e} per axis.
+template <typename T>
+__device__ __forceinline__ float sample_corner(const T *__restrict__ b, uint32_t B, uint32_t lx, uint32_t ly,
+                                               uint32_t lz) {
+    const uint32_t i0 = ((lz - 1) * B + (ly - 1)) * B + (lx - 1);
+    const uint32_t BB = B * B;
+    if constexpr (sizeof(T) < 4) {
+        const uint32_t s = static_cast<uint32_t>(__ldg(b + i0)) + __ldg(b + i0 + 1) + __ldg(b + i0 + B) +
+                           __ldg(b + i0 + B + 1) + __ldg(b + i0 + BB) + __ldg(b + i0 + BB + 1) +
+                           __ldg(b + i0 + BB + B) + __ldg(b + i0 + BB + B + 1);
+        return static_cast<float>(s) / VoxelTraits<T>::kSum8;
+    } else {
+        const float s = ((__ldg(b + i0) + __ldg(b + i0 + 1)) + (__ldg(b + i0 + B) + __ldg(b + i0 + B + 1))) +
+                        ((__ldg(b + i0 + BB) + __ldg(b + i0 + BB + 1)) +
+                         (__ldg(b + i0 + BB + B) + __ldg(b + i0 + BB + B + 1)));
+        return s * 0.125f;
+    }
+}
+
+// Trilinear sampler at the fractional position f (voxels of the level).
+__device__ __forceinline__ void tri_axis(float f, uint32_t c, uint32_t beff, uint32_t &i0, float &w) {
+    const uint32_t m = static_cast<uint32_t>(f);
+    const float fr = f - static_cast<float>(m);
+    const uint32_t l = c + m % beff;
+    if (fr >= 0.5f) {
+        i0 = l;
+        w = fr - 0.5f;
+    } else {
+        i0 = l - 1;
+        w = fr + 0.5f;
+    }
+}
+template <typename T>
+__device__ __forceinline__ float ldv(const T *__restrict__ b, uint32_t i) {
+    return static_cast<float>(__ldg(b + i));
+}
+template <typename T>
+__device__ __forceinline__ float sample_trilinear(const T *__restrict__ b, uint32_t B, uint32_t x0, uint32_t y0,
+                                                  uint32_t z0, float wx, float wy, float wz) {
+    const uint32_t i = (z0 * B + y0) * B + x0, BB = B * B;
+    const float c00 = ldv(b, i) + (ldv(b, i + 1) - ldv(b, i)) * wx;
+    const float c10 = ldv(b, i + B) + (ldv(b, i + B + 1) - ldv(b, i + B)) * wx;
+    const float c01 = ldv(b, i + BB) + (ldv(b, i + BB + 1) - ldv(b, i + BB)) * wx;
+    const float c11 = ldv(b, i + BB + B) + (ldv(b, i + BB + B + 1) - ldv(b, i + BB + B)) * wx;
+    const float c0 = c00 + (c10 - c00) * wy;
+    const float c1 = c01 + (c11 - c01) * wy;
+    return (c0 + (c1 - c0) * wz) / VoxelTraits<T>::kMax;
+}
+
+enum Status { kMapped = 0, kUnmapped = 1, kEmpty = 2 };
+
+// Per-thread page-walk state (K_CacheManager::_previousCoords / _previousEntries).
+struct Walk {
+    uint32_t pcx, pcy, pcz;
+    uint4 entry;
+};
+
+template <typename T>
+__device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt, uint32_t sampler, uint32_t lod,
+                                     V3 np, Walk &w, float &sample) {
+    const float px = np.x * lt.ior[lod][0];
+    const float py = np.y * lt.ior[lod][1];
+    const float pz = np.z * lt.ior[lod][2];
+    const uint32_t cx = lt.off[lod] + static_cast<uint32_t>(px * static_cast<float>(lt.nb[lod][0]));
+    const uint32_t cy = static_cast<uint32_t>(py * static_cast<float>(lt.nb[lod][1]));
+    const uint32_t cz = static_cast<uint32_t>(pz * static_cast<float>(lt.nb[lod][2]));
+    const uint64_t idx = cx + static_cast<uint64_t>(cy) * cv.mx + static_cast<uint64_t>(cz) * cv.mx * cv.my;
+    bool fresh = false;
+    if (cx != w.pcx || cy != w.pcy || cz != w.pcz) {
+        w.entry = __ldg(cv.mrpd + idx);
+        w.pcx = cx;
+        w.pcy = cy;
+        w.pcz = cz;
+        fresh = true;
+    }
+    const uint4 e = w.entry;
+    if (e.w == 1u) {
+        const uint32_t B = cv.B;
+        const uint32_t slot = e.x / B + (e.y / B) * cv.sx + (e.z / B) * cv.sx * cv.sy;
+        if (fresh) {
+            uint32_t *u = cv.usage + slot;
+            if (*u != cv.ts) *u = cv.ts;
+        }
+        const T *b = reinterpret_cast<const T *>(cv.pool) + static_cast<uint64_t>(slot) * B * B * B;
+        const float fx = px * static_cast<float>(lt.vvox[lod][0]);
+        const float fy = py * static_cast<float>(lt.vvox[lod][1]);
+        const float fz = pz * static_cast<float>(lt.vvox[lod][2]);
+        if (sampler == GC_SAMPLER_REFERENCE) {
+            const uint32_t lx = cv.c + static_cast<uint32_t>(fx) % cv.Beff;
+            const uint32_t ly = cv.c + static_cast<uint32_t>(fy) % cv.Beff;
+            const uint32_t lz = cv.c + static_cast<uint32_t>(fz) % cv.Beff;
+            sample = sample_corner<T>(b, B, lx, ly, lz);
+        } else {
+            uint32_t x0, y0, z0;
+            float wx, wy, wz;
+            tri_axis(fx, cv.c, cv.Beff, x0, wx);
+            tri_axis(fy, cv.c, cv.Beff, y0, wy);
+            tri_axis(fz, cv.c, cv.Beff, z0, wz);
+            sample = sample_trilinear<T>(b, B, x0, y0, z0, wx, wy, wz);
+        }
+        return kMapped;
+    }
+    if (e.w == 0u) {
+        // raise_brick_request (K_CacheManager.hpp:364-396): same coordinates
+        uint32_t *r = cv.req + idx;
+        if (*r != cv.ts) *r = cv.ts;
+        return kUnmapped;
+    }
+    return kEmpty;
+}
+
+template <typename T>
+__device__ void march(const CacheView &cv, const LevelTables &lt, const ViewParams &vp, uint32_t x, uint32_t y) {
+    const uint32_t W = vp.W, H = vp.H;
+    uint32_t xN = x + 1;
+    if (xN > W) xN = x - 1;
+    uint32_t yN = y + 1;
+    if (yN > H) yN = y - 1;
+    const float fW = static_cast<float>(W), fH = static_cast<float>(H);
+    const float u = ((static_cast<float>(x) + 0.5f) / fW) * 2.0f - 1.0f;
+    const float uN = ((static_cast<float>(xN) + 0.5f) / fW) * 2.0f - 1.0f;
+    const float v = ((static_cast<float>(y) + 0.5f) / fH) * 2.0f - 1.0f;
+    const float vN = ((static_cast<float>(yN) + 0.5f) / fH) * 2.0f - 1.0f;
+    const float *m = vp.m;
+    // mul(M, float4(0,0,0,1)) and mul(M, float3) (RayCasters.cu:484-503)
+    const V3 origin = v3(0.0f * m[0] + 0.0f * m[1] + 0.0f * m[2] + 1.0f * m[3],
+                         0.0f * m[4] + 0.0f * m[5] + 0.0f * m[6] + 1.0f * m[7],
+                         0.0f * m[8] + 0.0f * m[9] + 0.0f * m[10] + 1.0f * m[11]);
+    const V3 r0 = v3(m[0], m[1], m[2]), r1 = v3(m[4], m[5], m[6]), r2 = v3(m[8], m[9], m[10]);
+    auto rot = [&](V3 d) { return v3(dot(d, r0), dot(d, r1), dot(d, r2)); };
+    const V3 dir = rot(normalize(v3(u, v, -vp.focal)));
+    const V3 dirXN = rot(normalize(v3(uN, v, -vp.focal)));
+    const V3 dirYN = rot(normalize(v3(u, vN, -vp.focal)));
+    const V3 dirLeft = normalize(cross(dir, dirYN));
+    const V3 dirUp = normalize(cross(dir, dirXN));
+
+    // intersectBox (RayCasters.cu:506-525)
+    const V3 invR = v3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+    const V3 tbot = invR * (v3(vp.bmin[0], vp.bmin[1], vp.bmin[2]) - origin);
+    const V3 ttop = invR * (v3(vp.bmax[0], vp.bmax[1], vp.bmax[2]) - origin);
+    const V3 tmin = v3(fminf(ttop.x, tbot.x), fminf(ttop.y, tbot.y), fminf(ttop.z, tbot.z));
+    const V3 tmax = v3(fmaxf(ttop.x, tbot.x), fmaxf(ttop.y, tbot.y), fmaxf(ttop.z, tbot.z));
+    float tnear = fmaxf(fmaxf(tmin.x, tmin.y), fmaxf(tmin.x, tmin.z));
+    const float tfar = fminf(fminf(tmax.x, tmax.y), fminf(tmax.x, tmax.z));
+    const bool hit = tfar > tnear;
+
+    const uint32_t i = y * W + x;
+    tnear = fmaxf(tnear, vp.tbuf[i]);
+    float4 *state = reinterpret_cast<float4 *>(vp.state);
+    const bool dvr = vp.mode == GC_MODE_DVR;
+    float4 fc = dvr ? state[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!hit) {
+        fc.x = 0.f;
+        fc.y = 0.f;
+        fc.z = 0.f;
+    } else {
+        if (tnear < 0.f) tnear = 0.f;
+        float t = tnear;
+        V3 pos = origin + dir * tnear;
+        const float endX = fabsf(dot(dir - dirXN, dirLeft) * tfar);
+        const float endY = fabsf(dot(dir - dirYN, dirUp) * tfar);
+        const uint32_t nl = lt.nlevels;
+        uint32_t lod = 0;
+        float sL = 0.f, sU = 0.f;  // spacings of level lod + 1
+        if (nl > 1) {
+            const V3 n1 = v3(vp.inv_size[1][0], vp.inv_size[1][1], vp.inv_size[1][2]);
+            sL = length(dirLeft * n1);
+            sU = length(dirUp * n1);
+        }
+        Walk w;
+        w.pcx = w.pcy = w.pcz = UINT_MAX;
+        w.entry = make_uint4(0, 0, 0, 0);
+        bool unm = false;
+        float maxOp = dvr ? 0.f : state[i].x;
+        while ((!dvr || fc.w < vp.early) && t < tfar) {
+            const float alpha = t / tfar;
+            const float pX = endX * alpha;
+            const float pY = endY * alpha;
+            V3 tp = pos * 0.495f + v3(0.495f, 0.495f, 0.495f);
+            tp.z = 1.0f - tp.z;
+            const V3 np = v3(clampf(tp.x, 0.f, 0.99f), clampf(tp.y, 0.f, 0.99f), clampf(tp.z, 0.f, 0.99f));
+            // compute_LOD: the level only grows along a ray because the pixel
+            // footprint grows with t, so the scan resumes at the current level.
+            while (lod + 1 < nl && !(sL >= pX || sU >= pY)) {
+                ++lod;
+                if (lod + 1 < nl) {
+                    const V3 nn = v3(vp.inv_size[lod + 1][0], vp.inv_size[lod + 1][1], vp.inv_size[lod + 1][2]);
+                    sL = length(dirLeft * nn);
+                    sU = length(dirUp * nn);
+                }
+            }
+            float sample = 0.f;
+            const int st = fetch<T>(cv, lt, vp.sampler, lod, np, w, sample);
+            if (st != kMapped) {
+                if (st == kUnmapped) {
+                    if (!unm) {
+                        vp.tbuf[i] = t;
+                        if (dvr)
+                            state[i] = fc;
+                        else
+                            vp.state[4 * i] = maxOp;
+                    }
+                    unm = true;
+                    break;
+                }
+                t += vp.tstep;
+                if (t > tfar) break;
+                pos = pos + dir * vp.tstep;
+                continue;
+            }
+            if (dvr) {
+                float4 col = tf_lookup(vp.tf, vp.tfw, sample);
+                col.w = 1.0f - gc_pow(1.0f - col.w, vp.kexp[lod]);
+                if (col.w > 0.001f) {
+                    col.x *= col.w;
+                    col.y *= col.w;
+                    col.z *= col.w;
+                    const float r = 1.0f - fc.w;
+                    fc.x = fc.x + col.x * r;
+                    fc.y = fc.y + col.y * r;
+                    fc.z = fc.z + col.z * r;
+                    fc.w = fc.w + col.w * r;
+                }
+            } else {
+                maxOp = fmaxf(maxOp, sample);
+            }
+            t += vp.step[lod];
+            pos = pos + dir * vp.step[lod];
+        }
+        if (!unm) {
+            vp.tbuf[i] = t;
+            if (dvr)
+                state[i] = fc;
+            else
+                vp.state[4 * i] = maxOp;
+        }
+        if (!dvr) fc = tf_lookup(vp.tf, vp.tfw, maxOp);
+    }
+    const uint32_t R = static_cast<uint32_t>(saturate(fc.x) * 255.0f);
+    const uint32_t G = static_cast<uint32_t>(saturate(fc.y) * 255.0f);
+    const uint32_t Bc = static_cast<uint32_t>(saturate(fc.z) * 255.0f);
+    const uint32_t A = static_cast<uint32_t>(saturate(fc.w) * 255.0f);
+    vp.rgba[i] = (A << 24) | (Bc << 16) | (G << 8) | R;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRenderThreads) render_kernel(const CacheView cv, const LevelTables lt,
+                                                                const ViewParams *__restrict__ views,
+                                                                uint32_t nviews, uint32_t total_tiles,
+                                                                uint32_t *queue, uint32_t nwarps) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(queue, 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= total_tiles) break;
+        uint32_t v = 0;
+        {
+            uint32_t lo = 0, hi = nviews - 1;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (views[mid].tile_begin <= t)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            v = lo;
+        }
+        const ViewParams &vp = views[v];
+        const uint32_t local = t - vp.tile_begin;
+        const uint32_t ty = local / vp.tiles_x, tx = local - ty * vp.tiles_x;
+        const uint32_t x = tx * 8 + (lane & 7u), y = ty * 4 + (lane >> 3);
+        if (x < vp.W && y < vp.H) march<T>(cv, lt, vp, x, y);
+    }
+    if (lane == 0) {
+        __threadfence();
+        if (atomicAdd(queue + 1, 1u) == nwarps - 1) {
+            queue[0] = 0;
+            queue[1] = 0;
+            __threadfence();
+        }
+    }
+}
+
+void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams *views_dev,
+                   const ViewParams * /*views_host*/, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
+                   uint32_t * /*err*/, cudaStream_t s) {
+    if (total_tiles == 0) return;
+    static int blocks_per_sm[3] = {0, 0, 0};
+    auto launch = [&](auto kernel, int slot) {
+        if (!blocks_per_sm[slot]) {
+            int b = 0;
+            GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kRenderThreads, 0));
+            blocks_per_sm[slot] = std::max(1, b);
+        }
+        const uint32_t max_blocks = static_cast<uint32_t>(sm_count() * blocks_per_sm[slot]);
+        const uint32_t want = div_up(total_tiles, kRenderThreads / 32);
+        const uint32_t grid = std::max(1u, std::min(max_blocks, want));
+        kernel<<<grid, kRenderThreads, 0, s>>>(cv, lt, views_dev, nviews, total_tiles, queue,
+                                               grid * (kRenderThreads / 32));
+        GC_CUDA(cudaGetLastError());
+    };
+    switch (cv.eb) {
+        case 1: launch(render_kernel<uint8_t>, 0); break;
+        case 2: launch(render_kernel<uint16_t>, 1); break;
+        case 4: launch(render_kernel<float>, 2); break;
+        default: fail(GC_ERR_UNSUPPORTED, "the ray caster supports one channel of 1, 2 or 4 bytes");
+    }
+}
+
+}  // namespace gc

@@ -1,0 +1,377 @@
+"""Python host mirror of the GB300 out-of-core volume path.
+
+Binds the C ABI of libgcgb300.so (include/gc_gb300.h) with ctypes and wraps it
+in classes named after the reference's interface:
+
+  Configuration          GcCore/include/GcCore/libData/Configuration.hpp:18-87
+  compute_layout         Mipmapper::fill_metaData + init_meta_data
+  Mipmapper              GcCore/include/GcCore/cuda/libPreprocessor/Mipmapper.hpp:35-108
+  process_bricking       GcCore/include/GcCore/libPreprocessor/Bricker_v2.hpp:13-41
+  CacheManager           GcCore/include/GcCore/cuda/libGPUCache/CacheManager.hpp:38-128
+  TransferFunction       Applications/DVR-ray-caster/src/TransferFunction.cpp:16-157
+
+Device memory, streams and events come from PyTorch (plumbing only): every
+function takes raw device pointers (int) and a cudaStream_t (int, 0 = legacy
+stream).  Errors raise GcError with the library's message.  There is no
+fallback: if the shared library is missing, importing this module fails.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgcgb300.so")
+
+MAX_LEVELS = 16
+OK = 0
+BRICK_SUCCESS, BRICK_UNKNOWN, BRICK_EMPTY = 0, 1, 2
+MODE_DVR, MODE_MOP = 0, 1
+SAMPLER_REFERENCE, SAMPLER_TRILINEAR = 0, 1
+CACHE_SYNC_LOADER = 1
+DUMP_MRPD, DUMP_LRU, DUMP_USAGE, DUMP_REQUESTS, DUMP_POOL = 0, 1, 2, 3, 4
+
+U3 = C.c_uint32 * 3
+L3 = (C.c_uint32 * 3) * MAX_LEVELS
+
+
+class VolumeDesc(C.Structure):
+    _fields_ = [("size", U3), ("brick_size", C.c_uint32), ("big_brick_size", U3), ("covering", C.c_uint32),
+                ("encoded_bytes", C.c_uint32), ("channels", C.c_uint32), ("downscale", U3)]
+
+
+class Layout(C.Structure):
+    _fields_ = [("nb_levels", C.c_uint32), ("initial", L3), ("real", L3), ("nb_bricks", L3),
+                ("nb_big_bricks", L3), ("mip", L3)]
+
+
+class Blob(C.Structure):
+    _fields_ = [("cx", C.c_int32), ("cy", C.c_int32), ("cz", C.c_int32), ("k", C.c_uint64 * 3),
+                ("r", C.c_int32 * 3), ("amplitude", C.c_int32)]
+
+
+class Generator(C.Structure):
+    _fields_ = [("size", U3), ("bytes_per_channel", C.c_uint32), ("channels", C.c_uint32),
+                ("channel", C.c_uint32), ("field", C.c_uint32), ("seed", C.c_uint32),
+                ("noise_amplitude", C.c_int32), ("nblobs", C.c_uint32), ("blobs", C.POINTER(Blob))]
+
+
+class CacheDesc(C.Structure):
+    _fields_ = [("volume", VolumeDesc), ("layout", Layout), ("cache_size", U3), ("max_requests", C.c_uint32),
+                ("flags", C.c_uint32), ("gpu", C.c_int32)]
+
+
+class CacheInfo(C.Structure):
+    _fields_ = [("mrpd_dims", U3), ("nb_slots", C.c_uint32), ("slot_voxels", C.c_uint32),
+                ("level_offset", C.c_uint32 * MAX_LEVELS), ("pool_bytes", C.c_uint64)]
+
+
+class CacheStats(C.Structure):
+    _fields_ = [("frames", C.c_uint64), ("requests_raised", C.c_uint64), ("requests_served", C.c_uint64),
+                ("bricks_installed", C.c_uint64), ("bricks_empty", C.c_uint64), ("bytes_h2d", C.c_uint64),
+                ("load_errors", C.c_uint64), ("last_requests", C.c_uint32), ("device_error", C.c_uint32)]
+
+
+class View(C.Structure):
+    _fields_ = [("inv_view", C.c_float * 12), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3), ("tstep", C.c_float),
+                ("focal", C.c_float), ("early_alpha", C.c_float), ("mode", C.c_uint32), ("sampler", C.c_uint32),
+                ("tf_width", C.c_uint32), ("tf", C.c_void_p), ("rgba", C.c_void_p), ("tbuf", C.c_void_p),
+                ("state", C.c_void_p)]
+
+
+class TfPoint(C.Structure):
+    _fields_ = [("value", C.c_float), ("alpha", C.c_float), ("r", C.c_float), ("g", C.c_float), ("b", C.c_float)]
+
+
+LOADER_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p,
+                        C.c_size_t)
+
+vp = C.c_void_p
+P = C.POINTER
+# name -> argtypes (restype is int unless listed in _RESTYPES)
+_SIGS = {
+    "gc_last_error": [], "gc_version": [], "gc_device_count": [P(C.c_int)],
+    "gc_config_create": [P(vp)], "gc_config_destroy": [vp], "gc_config_load": [vp, C.c_char_p],
+    "gc_config_set": [vp, C.c_char_p, C.c_char_p], "gc_config_get": [vp, C.c_char_p, C.c_char_p, C.c_size_t],
+    "gc_config_volume_desc": [vp, P(VolumeDesc)], "gc_layout_compute": [P(VolumeDesc), P(Layout)],
+    "gc_pool_dims": [P(VolumeDesc), C.c_uint64, P(C.c_uint32)],
+    "gc_generator_blobs": [C.c_uint32, C.c_uint32, P(C.c_uint32), C.c_float, C.c_float, C.c_int32, C.c_int32,
+                           P(Blob)],
+    "gc_generate_volume": [P(Generator), vp, vp],
+    "gc_mip_level": [vp, vp, P(C.c_uint32), C.c_uint32, C.c_uint32, vp],
+    "gc_mip_build": [vp, P(Layout), P(C.c_uint64), C.c_uint32, C.c_uint32, vp],
+    "gc_bricks_build": [vp, P(C.c_uint32), P(VolumeDesc), P(C.c_uint32), vp, vp],
+    "gc_bricks_empty": [vp, C.c_uint64, P(VolumeDesc), C.c_float, vp, vp],
+    "gc_brick_key": [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32],
+    "gc_cache_create": [P(CacheDesc), P(vp)], "gc_cache_destroy": [vp],
+    "gc_cache_set_source_host": [vp, vp, P(C.c_uint64), P(C.c_uint64), C.c_size_t],
+    "gc_cache_set_source_callback": [vp, LOADER_FN, vp, P(C.c_uint64), C.c_size_t],
+    "gc_cache_update": [vp, vp, P(C.c_int)], "gc_cache_completude": [vp, vp, P(C.c_float)],
+    "gc_cache_timestamp": [vp, P(C.c_uint32)], "gc_cache_info_get": [vp, P(CacheInfo)],
+    "gc_cache_stats_get": [vp, P(CacheStats)], "gc_cache_dump": [vp, C.c_int, vp, C.c_size_t],
+    "gc_cache_load_buffer": [vp, C.c_int, vp, C.c_size_t],
+    "gc_view_matrix": [P(C.c_float), P(C.c_float), P(C.c_float)],
+    "gc_look_at": [P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_float)],
+    "gc_tf_build": [P(TfPoint), C.c_uint32, C.c_uint32, P(C.c_float)],
+    "gc_render": [vp, P(View), vp], "gc_render_batch": [vp, P(View), C.c_uint32, vp],
+}
+_RESTYPES = {"gc_last_error": C.c_char_p, "gc_version": C.c_char_p, "gc_brick_key": C.c_uint64}
+
+
+class GcError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[gc error {code}] {msg}")
+        self.code = code
+
+
+def load(path=LIB_PATH):
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is not built; run __graft_entry__.build()")
+    lib = C.CDLL(path)
+    for name, args in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _RESTYPES.get(name, C.c_int)
+    return lib
+
+
+lib = load()
+
+
+def check(rc):
+    if rc != OK:
+        raise GcError(rc, lib.gc_last_error().decode())
+    return rc
+
+
+def u3(v):
+    return U3(*[int(x) for x in v])
+
+
+# ---------------------------------------------------------------------------
+class Configuration:
+    """Key/value configuration (Configuration::get_field / add_field)."""
+
+    def __init__(self, path=None):
+        self._h = vp()
+        check(lib.gc_config_create(C.byref(self._h)))
+        if path:
+            self.load(path)
+
+    def load(self, path):
+        check(lib.gc_config_load(self._h, str(path).encode()))
+
+    def add_field(self, key, value):
+        check(lib.gc_config_set(self._h, key.encode(), str(value).encode()))
+
+    def get_field(self, key):
+        buf = C.create_string_buffer(4096)
+        rc = lib.gc_config_get(self._h, key.encode(), buf, len(buf))
+        return buf.value.decode() if rc == OK else None
+
+    def volume_desc(self):
+        d = VolumeDesc()
+        check(lib.gc_config_volume_desc(self._h, C.byref(d)))
+        return d
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib.gc_config_destroy(self._h)
+            self._h = None
+
+
+def volume_desc(size, brick_size=16, covering=1, encoded_bytes=1, channels=1, big_brick=(1, 1, 1)):
+    return VolumeDesc(u3(size), brick_size, u3(big_brick), covering, encoded_bytes, channels, u3((2, 2, 2)))
+
+
+def compute_layout(vol):
+    L = Layout()
+    check(lib.gc_layout_compute(C.byref(vol), C.byref(L)))
+    return L
+
+
+def pool_dims(vol, pool_bytes):
+    out = U3()
+    check(lib.gc_pool_dims(C.byref(vol), int(pool_bytes), out))
+    return tuple(out)
+
+
+def brick_key(level, x, y, z):
+    return int(lib.gc_brick_key(level, x, y, z))
+
+
+def generator_blobs(seed, nblobs, size, sigma_min, sigma_max, amp_min, amp_max):
+    arr = (Blob * max(1, nblobs))()
+    check(lib.gc_generator_blobs(seed, nblobs, u3(size), sigma_min, sigma_max, amp_min, amp_max, arr))
+    return arr
+
+
+def make_generator(size, bytes_per_channel, seed, blobs, noise_amplitude, channels=1, channel=0, field=0):
+    g = Generator(u3(size), bytes_per_channel, channels, channel, field, seed, noise_amplitude, len(blobs),
+                  C.cast(blobs, P(Blob)))
+    g._keep = blobs
+    return g
+
+
+def generate_volume(gen, dst_ptr, stream=0):
+    check(lib.gc_generate_volume(C.byref(gen), vp(dst_ptr), vp(stream)))
+
+
+# ---------------------------------------------------------------------------
+class Mipmapper:
+    """Device-resident mip pyramid (Mipmapper::process)."""
+
+    @staticmethod
+    def down_scale(src_ptr, dst_ptr, dims, encoded_bytes, channels, stream=0):
+        check(lib.gc_mip_level(vp(src_ptr), vp(dst_ptr), u3(dims), encoded_bytes, channels, vp(stream)))
+
+    @staticmethod
+    def process(pyramid_ptr, layout, level_offsets, encoded_bytes, channels, stream=0):
+        offs = (C.c_uint64 * MAX_LEVELS)(*[int(o) for o in level_offsets])
+        check(lib.gc_mip_build(vp(pyramid_ptr), C.byref(layout), offs, encoded_bytes, channels, vp(stream)))
+
+
+def process_bricking(level_ptr, level_dims, vol, nb_big_bricks, out_ptr, stream=0):
+    """Bricks one level on the device (process_bricking)."""
+    check(lib.gc_bricks_build(vp(level_ptr), u3(level_dims), C.byref(vol), u3(nb_big_bricks), vp(out_ptr),
+                              vp(stream)))
+
+
+def process_empty(bricks_ptr, nb_big, vol, threshold, flags_ptr, stream=0):
+    check(lib.gc_bricks_empty(vp(bricks_ptr), int(nb_big), C.byref(vol), float(threshold), vp(flags_ptr),
+                              vp(stream)))
+
+
+def pyramid_offsets(layout, encoded_bytes, align=256):
+    """Byte offsets of each level in one device buffer (level 0 first)."""
+    offs, off = [], 0
+    for l in range(layout.nb_levels):
+        offs.append(off)
+        n = layout.mip[l][0] * layout.mip[l][1] * layout.mip[l][2] * encoded_bytes
+        off += (n + align - 1) // align * align
+    return offs, off
+
+
+def brick_store_offsets(layout, vol):
+    """Byte offsets of each level's big bricks in a flat brick store."""
+    B = vol.brick_size
+    big = B ** 3 * vol.big_brick_size[0] * vol.big_brick_size[1] * vol.big_brick_size[2] * vol.encoded_bytes
+    offs, off = [], 0
+    for l in range(layout.nb_levels):
+        offs.append(off)
+        nb = layout.nb_big_bricks[l]
+        off += nb[0] * nb[1] * nb[2] * big
+    return offs, off, big
+
+
+# ---------------------------------------------------------------------------
+def view_matrix(rotation_deg, translation):
+    out = (C.c_float * 12)()
+    check(lib.gc_view_matrix((C.c_float * 2)(*rotation_deg), (C.c_float * 3)(*translation), out))
+    return list(out)
+
+
+def look_at(eye, target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0)):
+    out = (C.c_float * 12)()
+    check(lib.gc_look_at((C.c_float * 3)(*eye), (C.c_float * 3)(*target), (C.c_float * 3)(*up), out))
+    return list(out)
+
+
+class TransferFunction:
+    """Piecewise-linear RGBA transfer function (TransferFunction::getSample)."""
+
+    @staticmethod
+    def build(points, samples):
+        arr = (TfPoint * max(1, len(points)))(*[TfPoint(*p) for p in points])
+        out = (C.c_float * (4 * samples))()
+        check(lib.gc_tf_build(arr, len(points), samples, out))
+        return list(out)
+
+    @staticmethod
+    def defaultColorful(samples=128):
+        return TransferFunction.build([(0.20, 0.10, 0, 0, 1), (0.35, 0.70, 0, 1, 1), (0.45, 1.0, 0, 1, 0),
+                                       (0.70, 1.0, 1, 1, 0), (1.0, 1.0, 1, 0, 0)], samples)
+
+    @staticmethod
+    def greyRamp(samples=128):
+        return TransferFunction.build([(0.0, 0.0, 0, 0, 0), (1.0, 1.0, 1, 1, 1)], samples)
+
+
+def make_view(inv_view, width, height, tf_ptr, tf_width, rgba_ptr, tbuf_ptr, state_ptr, tstep=2.0 / 256.0,
+              focal=2.0, early_alpha=0.95, mode=MODE_DVR, sampler=SAMPLER_REFERENCE,
+              bbox_min=(-1.0, -1.0, -1.0), bbox_max=(1.0, 1.0, 1.0)):
+    return View((C.c_float * 12)(*inv_view), width, height, (C.c_float * 3)(*bbox_min), (C.c_float * 3)(*bbox_max),
+                tstep, focal, early_alpha, mode, sampler, tf_width, vp(tf_ptr), vp(rgba_ptr), vp(tbuf_ptr),
+                vp(state_ptr))
+
+
+# ---------------------------------------------------------------------------
+class CacheManager:
+    """GPU brick cache + ray caster entry (CacheManager<T> + RayCastDVR)."""
+
+    def __init__(self, vol, layout, cache_size, max_requests=50, sync_loader=True, gpu=0):
+        self.desc = CacheDesc(vol, layout, u3(cache_size), max_requests, CACHE_SYNC_LOADER if sync_loader else 0, gpu)
+        self._h = vp()
+        check(lib.gc_cache_create(C.byref(self.desc), C.byref(self._h)))
+        info = CacheInfo()
+        check(lib.gc_cache_info_get(self._h, C.byref(info)))
+        self.info = info
+        self._keep = []
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_source_host(self, bricks_ptr, level_offsets, empty_keys=()):
+        offs = (C.c_uint64 * MAX_LEVELS)(*[int(o) for o in level_offsets])
+        keys = (C.c_uint64 * max(1, len(empty_keys)))(*[int(k) for k in empty_keys])
+        self._keep.append((offs, keys))
+        check(lib.gc_cache_set_source_host(self._h, vp(bricks_ptr), offs, keys, len(empty_keys)))
+
+    def set_source_callback(self, fn, empty_keys=()):
+        cb = LOADER_FN(fn)
+        keys = (C.c_uint64 * max(1, len(empty_keys)))(*[int(k) for k in empty_keys])
+        self._keep.append((cb, keys))
+        check(lib.gc_cache_set_source_callback(self._h, cb, None, keys, len(empty_keys)))
+
+    def update(self, stream=0):
+        conv = C.c_int()
+        check(lib.gc_cache_update(self._h, vp(stream), C.byref(conv)))
+        return bool(conv.value)
+
+    def completude(self, stream=0):
+        f = C.c_float()
+        check(lib.gc_cache_completude(self._h, vp(stream), C.byref(f)))
+        return f.value
+
+    def timestamp(self):
+        t = C.c_uint32()
+        check(lib.gc_cache_timestamp(self._h, C.byref(t)))
+        return t.value
+
+    def stats(self):
+        s = CacheStats()
+        check(lib.gc_cache_stats_get(self._h, C.byref(s)))
+        return s
+
+    def dump(self, what, buf):
+        """Copies one state buffer into a writable host buffer (numpy array)."""
+        check(lib.gc_cache_dump(self._h, what, vp(buf.ctypes.data), buf.nbytes))
+        return buf
+
+    def load_buffer(self, what, buf):
+        check(lib.gc_cache_load_buffer(self._h, what, vp(buf.ctypes.data), buf.nbytes))
+
+    def render(self, view, stream=0):
+        check(lib.gc_render(self._h, C.byref(view), vp(stream)))
+
+    def render_batch(self, views, stream=0):
+        arr = (View * len(views))(*views)
+        check(lib.gc_render_batch(self._h, arr, len(views), vp(stream)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.gc_cache_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

@@ -1,0 +1,312 @@
+/*
+ * gc_gb300.h -- C ABI of the GB300-native out-of-core volume path.
+ *
+ * This is the drop-in boundary for GcCore's out-of-core volume path
+ * (ftilde/GPU-Out-of-Core-Volume-Data).  The reference exposes that path as a
+ * C++ template library (CacheManager<T>, K_CacheManager<T>, Mipmapper,
+ * process_bricking, RayCastDVR); its only C linkage is the bricker shim
+ * GcCore/include/GcCore/libPython/Py_Bricker.hpp:8-49.  Every entry point
+ * below names the reference interface it replaces.
+ *
+ * Conventions
+ *  - plain pointers and sizes only; no C++ or torch types cross the boundary;
+ *  - every call returns an int status (GC_OK == 0); gc_last_error() returns
+ *    a thread-local, human-readable message for the last failing call;
+ *  - device pointers are CUDA device addresses on the cache's GPU; `stream`
+ *    arguments are cudaStream_t values passed as void* (0 = legacy stream);
+ *  - a gc_cache handle is not thread-safe: drive it from one host thread,
+ *    like the reference's CacheManager (CacheManager.hpp:38-128).
+ */
+#ifndef GC_GB300_H
+#define GC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GC_MAX_LEVELS 16
+
+/* status codes */
+#define GC_OK 0
+#define GC_ERR_INVALID 1    /* bad argument or configuration                 */
+#define GC_ERR_CUDA 2       /* a CUDA runtime call failed                     */
+#define GC_ERR_IO 3         /* file or brick-source failure                   */
+#define GC_ERR_TIMEOUT 4    /* a bounded device-side or host-side wait ran out */
+#define GC_ERR_NOMEM 5      /* allocation failed                              */
+#define GC_ERR_UNSUPPORTED 6
+
+/* brick status, as BricksManager::BrickStatus (BricksManager.hpp:321-326) */
+#define GC_BRICK_SUCCESS 0
+#define GC_BRICK_UNKNOWN 1
+#define GC_BRICK_EMPTY 2
+
+/* compositing, as CompositingMode DVR|MOP (VolumeRayCaster.cu:91-99) */
+#define GC_MODE_DVR 0
+#define GC_MODE_MOP 1
+
+/* sampler: GC_SAMPLER_REFERENCE reproduces the reference's normalized
+ * texture read at the integer voxel corner (K_CacheDevice.hpp:193-200), i.e.
+ * the mean of the 2x2x2 voxels (e-1,e) per axis; GC_SAMPLER_TRILINEAR
+ * interpolates at the fractional position inside the brick using the
+ * covering border. */
+#define GC_SAMPLER_REFERENCE 0
+#define GC_SAMPLER_TRILINEAR 1
+
+/* cache flags */
+#define GC_CACHE_SYNC_LOADER 1u   /* loader completes inside update(): deterministic
+                                     request -> install alternation            */
+
+/* ------------------------------------------------------------------------ */
+/* Volume description: the reference's config surface (config_skull.cfg:1-24,
+ * VolumeConfiguration.hpp:14-31).  encoded_bytes is bytes per voxel over all
+ * channels (MetaData.cpp:21-32); bytes per channel = encoded_bytes/channels. */
+typedef struct gc_volume_desc {
+    uint32_t size[3];            /* size_X/Y/Z                      */
+    uint32_t brick_size;         /* BrickSize (cubic)               */
+    uint32_t big_brick_size[3];  /* BigBrickSizeX/Y/Z               */
+    uint32_t covering;           /* VoxelCovering                   */
+    uint32_t encoded_bytes;      /* NumberEncodedBytes              */
+    uint32_t channels;           /* NumberChannels                  */
+    uint32_t downscale[3];       /* downScale_X/Y/Z (only 2 is supported) */
+} gc_volume_desc;
+
+/* Per-level geometry: Mipmapper::fill_metaData (Mipmapper.cu:583-597) and
+ * init_meta_data (Bricker_v2.cpp:45-76). */
+typedef struct gc_layout {
+    uint32_t nb_levels;
+    uint32_t initial[GC_MAX_LEVELS][3];        /* mip level sizes (voxels)        */
+    uint32_t real[GC_MAX_LEVELS][3];           /* nb_bricks * (B - 2c)            */
+    uint32_t nb_bricks[GC_MAX_LEVELS][3];      /* small bricks per axis           */
+    uint32_t nb_big_bricks[GC_MAX_LEVELS][3];  /* big bricks per axis             */
+    uint32_t mip[GC_MAX_LEVELS][3];            /* sizes of the mip data actually
+                                                  produced (== initial for the
+                                                  supported power-of-two volumes) */
+} gc_layout;
+
+/* ------------------------------------------------------------------------ */
+/* Errors and version. */
+const char *gc_last_error(void);
+const char *gc_version(void);
+int gc_device_count(int *count);
+
+/* ------------------------------------------------------------------------ */
+/* Configuration: Configuration::load<TDNSConfigurationParser> +
+ * get_field/add_field (Configuration.cpp:30-186, ConfigurationPolicies.cpp:16-44),
+ * load_volume_configuration's config part (VolumeConfiguration.cpp:14-50). */
+typedef struct gc_config *gc_config_t;
+int gc_config_create(gc_config_t *out);
+int gc_config_destroy(gc_config_t cfg);
+/* parses the reference's <Fields><Field key="" value=""/></Fields> file */
+int gc_config_load(gc_config_t cfg, const char *path);
+int gc_config_set(gc_config_t cfg, const char *key, const char *value);
+/* copies the value (NUL-terminated) into buf; GC_ERR_INVALID if missing */
+int gc_config_get(gc_config_t cfg, const char *key, char *buf, size_t buflen);
+/* fills a volume description from BrickSize, BigBrickSize{X,Y,Z},
+ * VoxelCovering, NumberEncodedBytes, NumberChannels, size_{X,Y,Z},
+ * downScale_{X,Y,Z}; missing required keys are GC_ERR_INVALID with the key
+ * named, like the reference's runtime_error messages. */
+int gc_config_volume_desc(gc_config_t cfg, gc_volume_desc *out);
+
+/* Level geometry (fill_metaData + init_meta_data + levelMax at
+ * Mipmapper.cu:441-443). */
+int gc_layout_compute(const gc_volume_desc *vol, gc_layout *out);
+
+/* Pool sizing of Application.cu:79-93: the cube of slots that holds
+ * pool_bytes / (B^3 * encoded_bytes) bricks, grown round-robin per axis. */
+int gc_pool_dims(const gc_volume_desc *vol, uint64_t pool_bytes, uint32_t out_dims[3]);
+
+/* ------------------------------------------------------------------------ */
+/* Synthetic volume (seeded blobs + value noise, integer arithmetic so that
+ * every device and host evaluation is bit-identical).  Writes X*Y*Z voxels
+ * (x fastest) of `bytes_per_channel` (1 or 2) to `dst` on the device.
+ * Channel `channel` selects an independent field (0: blobs+noise,
+ * 1: noise only); `stride_channels` interleaves into a multi-channel volume. */
+typedef struct gc_blob {
+    int32_t cx, cy, cz;        /* centre (voxels)                         */
+    uint64_t k[3];             /* per-axis 2^38 / (9 sigma^2)             */
+    int32_t r[3];              /* bounding half-extent (voxels)           */
+    int32_t amplitude;         /* value units                              */
+} gc_blob;
+
+typedef struct gc_generator {
+    uint32_t size[3];
+    uint32_t bytes_per_channel;    /* 1 or 2                                */
+    uint32_t channels;             /* interleave stride                      */
+    uint32_t channel;              /* which channel to write                 */
+    uint32_t field;                /* 0: blobs + noise, 1: noise only        */
+    uint32_t seed;
+    int32_t noise_amplitude;       /* value units                            */
+    uint32_t nblobs;
+    const gc_blob *blobs;          /* host array                             */
+} gc_generator;
+
+/* Draws blob parameters from a seeded splitmix64 stream (the same function
+ * runs in the oracle). */
+int gc_generator_blobs(uint32_t seed, uint32_t nblobs, const uint32_t size[3],
+                       float sigma_min, float sigma_max, int32_t amp_min,
+                       int32_t amp_max, gc_blob *out);
+int gc_generate_volume(const gc_generator *gen, void *dst, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Preprocessor.
+ * gc_mip_level: one 2x2x2 down-sampling pass (Mipmapper::down_scale,
+ * Mipmapper.cu:528-578, kernel down_sampling_inner Mipmapper.cu:29-105):
+ * output voxel = floor(sum / 8) for integer channels (u8 via the integer
+ * path, u16 via the double path whose sum is exact), (float)(sum_double / 8)
+ * for f32.  src/dst are device pointers, dims are the source level sizes. */
+int gc_mip_level(const void *src, void *dst, const uint32_t src_dims[3],
+                 uint32_t encoded_bytes, uint32_t channels, void *stream);
+
+/* gc_mip_build: the whole pyramid (Mipmapper::process, Mipmapper.cu:401-525)
+ * kept resident on the device.  `pyramid` holds level 0 at offset 0 and
+ * receives levels 1..nb_levels-1 at level_offsets[l] (bytes). */
+int gc_mip_build(void *pyramid, const gc_layout *layout, const uint64_t *level_offsets,
+                 uint32_t encoded_bytes, uint32_t channels, void *stream);
+
+/* gc_bricks_build: cuts one level into covered bricks (process_bricking,
+ * Bricker_v2.cpp:79-252).  Output holds the level's big bricks in
+ * (z, y, x) raster order, each (BB*B)^3 voxels x-fastest (Bricker_v2.cpp:295-299);
+ * voxels outside the level are zero. */
+int gc_bricks_build(const void *level, const uint32_t level_dims[3],
+                    const gc_volume_desc *vol, const uint32_t nb_big_bricks[3],
+                    void *out, void *stream);
+
+/* gc_bricks_empty: per big brick, 1 if every channel value < threshold
+ * (BrickProcessor::process_empty + DefaultBrickProcessorPredicate,
+ * BrickProcessor.hpp:91-162, BrickProcessorPredicate.hpp:11-46). */
+int gc_bricks_empty(const void *bricks, uint64_t nb_big_bricks, const gc_volume_desc *vol,
+                    float threshold, uint8_t *flags, void *stream);
+
+/* Brick key: 4 x uint16 {level, x, y, z} packed little-endian into a uint64
+ * (get_key, BrickKey.cpp:15-25). */
+uint64_t gc_brick_key(uint32_t level, uint32_t x, uint32_t y, uint32_t z);
+
+/* ------------------------------------------------------------------------ */
+/* GPU brick cache: CacheManager<T> (CacheManager.hpp:38-670) with its
+ * MultiResolutionPageDirectory (MultiResolutionPageDirectory.hpp:88-125),
+ * CacheDevice (CacheDevice.hpp:122-219) and RequestHandler
+ * (RequestHandler.hpp:29-372). */
+typedef struct gc_cache *gc_cache_t;
+
+typedef struct gc_cache_desc {
+    gc_volume_desc volume;
+    gc_layout layout;
+    uint32_t cache_size[3];   /* pool slots per axis (CacheConfiguration::CacheSize[0]) */
+    uint32_t max_requests;    /* reference: 50 (CacheManager.hpp:263)              */
+    uint32_t flags;           /* GC_CACHE_*                                        */
+    int32_t gpu;              /* gpuID                                             */
+} gc_cache_desc;
+
+/* Brick source callback: copy the big brick (level, x, y, z) -- (BB*B)^3
+ * voxels of encoded_bytes -- into dst and return a GC_BRICK_* status.  Called
+ * from the cache's loader thread (BricksManager::get_brick,
+ * BricksManager.cpp:48-78). */
+typedef int (*gc_brick_loader_fn)(void *user, uint32_t level, uint32_t x, uint32_t y,
+                                  uint32_t z, void *dst, size_t bytes);
+
+int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out);
+int gc_cache_destroy(gc_cache_t cache);
+/* In-memory brick store: all big bricks of every level, level l starting at
+ * byte offset level_offsets[l] in (z, y, x) raster order.  The memory must
+ * outlive the cache.  empty_keys lists gc_brick_key()s reported as Empty
+ * (bricks.xml <EmptyBricks>, MetaData.cpp:65-77). */
+int gc_cache_set_source_host(gc_cache_t cache, const void *bricks, const uint64_t *level_offsets,
+                             const uint64_t *empty_keys, size_t n_empty);
+int gc_cache_set_source_callback(gc_cache_t cache, gc_brick_loader_fn fn, void *user,
+                                 const uint64_t *empty_keys, size_t n_empty);
+/* CacheManager::update (CacheManager.hpp:318-354).  *converged = 1 when the
+ * request list was empty this frame. */
+int gc_cache_update(gc_cache_t cache, void *stream, int *converged);
+/* CacheManager::completude (CacheManager.hpp:357-383). */
+int gc_cache_completude(gc_cache_t cache, void *stream, float *fraction);
+int gc_cache_timestamp(gc_cache_t cache, uint32_t *ts);
+
+typedef struct gc_cache_info {
+    uint32_t mrpd_dims[3];        /* (sum_l nb_bricks.x, max y, max z)        */
+    uint32_t nb_slots;
+    uint32_t slot_voxels;         /* B^3                                      */
+    uint32_t level_offset[GC_MAX_LEVELS];
+    uint64_t pool_bytes;
+} gc_cache_info;
+int gc_cache_info_get(gc_cache_t cache, gc_cache_info *out);
+
+typedef struct gc_cache_stats {
+    uint64_t frames;
+    uint64_t requests_raised;     /* bricks flagged in the request buffer      */
+    uint64_t requests_served;     /* bricks handed to the loader               */
+    uint64_t bricks_installed;    /* non-empty bricks written to the pool      */
+    uint64_t bricks_empty;        /* empty bricks referenced (flag 2)          */
+    uint64_t bytes_h2d;           /* brick bytes copied host -> device         */
+    uint64_t load_errors;         /* GC_BRICK_UNKNOWN answers from the source  */
+    uint32_t last_requests;       /* misses found in the last request scan     */
+    uint32_t device_error;        /* sticky device-side error word (0 = none)  */
+} gc_cache_stats;
+int gc_cache_stats_get(gc_cache_t cache, gc_cache_stats *out);
+
+/* State dumps for parity checks (host destinations, sizes in bytes):
+ *  GC_DUMP_MRPD     uint32[4] per entry (cacheX, cacheY, cacheZ, flag)
+ *  GC_DUMP_LRU      LruContent[] in LRU order: {uint32 cx,cy,cz,level; float vx,vy,vz}
+ *                   (LruContent.hpp:10-15)
+ *  GC_DUMP_USAGE    uint32 per slot (x fastest)
+ *  GC_DUMP_REQUESTS uint32 per MRPD entry
+ *  GC_DUMP_POOL     B^3 * encoded_bytes per slot, slot-major (x fastest)
+ */
+#define GC_DUMP_MRPD 0
+#define GC_DUMP_LRU 1
+#define GC_DUMP_USAGE 2
+#define GC_DUMP_REQUESTS 3
+#define GC_DUMP_POOL 4
+int gc_cache_dump(gc_cache_t cache, int what, void *dst, size_t bytes);
+/* Overwrite the usage or request buffer (GC_DUMP_USAGE / GC_DUMP_REQUESTS)
+ * from the host: used to replay recorded frames through the update path. */
+int gc_cache_load_buffer(gc_cache_t cache, int what, const void *src, size_t bytes);
+
+/* ------------------------------------------------------------------------ */
+/* Ray caster: RayCastDVR / RayCastMOP (RayCasters.cu:35-468) with the LOD
+ * tables of display_volume_raycaster (VolumeRayCaster.cu:141-175) and the
+ * camera of update_CUDA_inv_view_model_matrix (RayCasters.cu:587-590). */
+typedef struct gc_view {
+    float inv_view[12];       /* 3x4 row-major: d_invModelViewMatrix           */
+    uint32_t width, height;   /* screenSize                                    */
+    float bbox_min[3];
+    float bbox_max[3];
+    float tstep;              /* marchingStep (reference 2/256)                */
+    float focal;              /* ray direction (u, v, -focal); reference 2     */
+    float early_alpha;        /* reference 0.95                                */
+    uint32_t mode;            /* GC_MODE_*                                     */
+    uint32_t sampler;         /* GC_SAMPLER_*                                  */
+    uint32_t tf_width;        /* transfer-function entries                     */
+    const float *tf;          /* device: tf_width RGBA float entries           */
+    uint32_t *rgba;           /* device: width*height RGBA8 (R in low byte)    */
+    float *tbuf;              /* device: width*height progressive t            */
+    float *state;             /* device: width*height float4 colour state      */
+} gc_view;
+
+/* Camera of updateViewMatrix (Display_helper.cpp:93-118): the rows of
+ * glRotatef(-rx,1,0,0) * glRotatef(-ry,0,1,0) * glTranslatef(-t), computed in
+ * double and rounded to float. */
+int gc_view_matrix(const float rotation_deg[2], const float translation[3], float out[12]);
+/* Camera placed at `eye` looking at `target`: columns (right, up, -forward, eye). */
+int gc_look_at(const float eye[3], const float target[3], const float up[3], float out[12]);
+
+/* Transfer function: TransferFunction::getSample / regenerateSamples
+ * (TransferFunction.cpp:121-157): piecewise-linear RGBA between control
+ * points sorted by value; sample i is taken at i / samples. */
+typedef struct gc_tf_point {
+    float value, alpha, r, g, b;
+} gc_tf_point;
+int gc_tf_build(const gc_tf_point *points, uint32_t n, uint32_t samples, float *out_rgba);
+
+/* One view per launch, like get_frame (VolumeRayCaster.cu:356-429). */
+int gc_render(gc_cache_t cache, const gc_view *view, void *stream);
+/* Many views of uneven sizes in one persistent launch sharing the cache's
+ * request buffer (one frame for the cache). */
+int gc_render_batch(gc_cache_t cache, const gc_view *views, uint32_t n, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GC_GB300_H */
