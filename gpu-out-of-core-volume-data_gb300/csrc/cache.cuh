@@ -84,6 +84,7 @@ uint32_t lookback_tiles(uint64_t n);
 struct InstallArgs {
     uint4 *mrpd;
     uint32_t mx, my;
+    uint64_t nentries;
     const uint32_t *order;     // current LRU order
     uint32_t nslots;
     uint32_t *slot_level;

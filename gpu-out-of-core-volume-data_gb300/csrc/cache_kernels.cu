@@ -147,16 +147,21 @@ __global__ void __launch_bounds__(kThreads) lru_partition_kernel(const uint32_t 
     __syncthreads();
     const uint32_t total_used = *count;
     uint32_t used_before = s_excl + excl_thread;
+    bool bad = false;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         const uint64_t i = base + k;
         if (i < n) {
-            if ((flags >> k) & 1u)
-                order_out[used_before++] = ids[k];
+            const uint64_t dst = ((flags >> k) & 1u) ? used_before
+                                                     : static_cast<uint64_t>(total_used) + i - used_before;
+            if ((flags >> k) & 1u) ++used_before;
+            if (dst < n)
+                order_out[dst] = ids[k];
             else
-                order_out[total_used + static_cast<uint32_t>(i) - used_before] = ids[k];
+                bad = true;  // only after a failed look-back
         }
     }
+    if (bad) atomicOr(&ctl->err, kErrLookback);
     finish_tile(ctl);
 }
 
@@ -247,7 +252,8 @@ __global__ void install_evict_kernel(InstallArgs a, const LevelTables lt) {
     const uint32_t slot = a.order[a.nslots - a.n_nonempty + i];
     const float4 vp = a.slot_vpos[slot];
     if (vp.x < 0.f) return;  // slot never held a brick
-    a.mrpd[mrpd_index(lt, a.slot_level[slot], vp.x, vp.y, vp.z, a.mx, a.my)] = make_uint4(0, 0, 0, 0);
+    const uint64_t e = mrpd_index(lt, a.slot_level[slot], vp.x, vp.y, vp.z, a.mx, a.my);
+    if (e < a.nentries) a.mrpd[e] = make_uint4(0, 0, 0, 0);
 }
 
 // compute_lru_volume_position + copy_lru_position + write_brick
@@ -316,7 +322,7 @@ __global__ void __launch_bounds__(1024) install_reference_kernel(InstallArgs a, 
                 dup = true;
                 break;
             }
-        if (dup) continue;
+        if (dup || c >= a.nentries) continue;
         const uint4 e = a.mrpd[c];
         if (e.w >= 1) continue;
         if (i < a.n_nonempty) {
@@ -347,6 +353,7 @@ void launch_lru_count(const uint32_t *usage, uint32_t nslots, uint32_t ts, uint3
     const uint32_t grid = std::min<uint32_t>(div_up(nslots, 256), static_cast<uint32_t>(sm_count()) * 4);
     lru_count_kernel<<<std::max(1u, grid), 256, 0, s>>>(usage, nslots, ts, count);
     GC_CUDA(cudaGetLastError());
+        count_launch();
 }
 
 void launch_lru_partition(const uint32_t *order_in, uint32_t *order_out, const uint32_t *usage, uint32_t ts,
@@ -355,6 +362,7 @@ void launch_lru_partition(const uint32_t *order_in, uint32_t *order_out, const u
     lru_partition_kernel<<<lookback_tiles(nslots), kThreads, 0, s>>>(order_in, order_out, usage, ts, nslots,
                                                                      count, status, ctl, epoch);
     GC_CUDA(cudaGetLastError());
+        count_launch();
 }
 
 void launch_miss_compact(const uint32_t *req, uint64_t nscan, uint32_t ts, uint32_t maxreq, uint4 *list,
@@ -363,6 +371,7 @@ void launch_miss_compact(const uint32_t *req, uint64_t nscan, uint32_t ts, uint3
     miss_compact_kernel<<<lookback_tiles(nscan), kThreads, 0, s>>>(req, nscan, ts, maxreq, list, lt, mx, my,
                                                                    status, ctl, epoch);
     GC_CUDA(cudaGetLastError());
+        count_launch();
 }
 
 void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s) {
@@ -371,8 +380,10 @@ void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s)
     if (a.n_nonempty) {
         install_evict_kernel<<<div_up(a.n_nonempty, 128), 128, 0, s>>>(a, lt);
         GC_CUDA(cudaGetLastError());
+        count_launch();
         install_place_kernel<<<a.n_nonempty, 256, 0, s>>>(a, lt, one_over_beff);
         GC_CUDA(cudaGetLastError());
+        count_launch();
     }
     const size_t smem = static_cast<size_t>(a.n) * sizeof(uint64_t);
     GC_REQUIRE(smem <= 200 * 1024, "too many bricks in one install");
@@ -381,6 +392,7 @@ void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s)
                                      static_cast<int>(smem)));
     install_reference_kernel<<<1, 1024, smem, s>>>(a, lt, one_over_beff);
     GC_CUDA(cudaGetLastError());
+        count_launch();
 }
 
 void launch_completude(const float4 *slot_vpos, uint32_t nslots, uint32_t *count, cudaStream_t s) {
@@ -388,6 +400,7 @@ void launch_completude(const float4 *slot_vpos, uint32_t nslots, uint32_t *count
     const uint32_t grid = std::min<uint32_t>(div_up(nslots, 256), static_cast<uint32_t>(sm_count()) * 4);
     completude_kernel<<<std::max(1u, grid), 256, 0, s>>>(slot_vpos, nslots, count);
     GC_CUDA(cudaGetLastError());
+        count_launch();
 }
 
 }  // namespace gc

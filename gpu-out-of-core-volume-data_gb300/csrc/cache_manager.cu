@@ -298,6 +298,7 @@ static void install(gc_cache *C, cudaStream_t s) {
     a.mrpd = C->mrpd;
     a.mx = C->mx;
     a.my = C->my;
+    a.nentries = C->nentries;
     a.order = C->order[C->cur];
     a.nslots = C->nslots;
     a.slot_level = C->slot_level;
@@ -484,6 +485,7 @@ int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out) {
         C->eb = desc->volume.encoded_bytes;
         const uint64_t nslots = static_cast<uint64_t>(desc->cache_size[0]) * desc->cache_size[1] * desc->cache_size[2];
         GC_REQUIRE(nslots < (1ull << 31), "too many pool slots");
+        GC_REQUIRE(desc->max_requests <= nslots, "max_requests must not exceed the number of pool slots");
         C->nslots = static_cast<uint32_t>(nslots);
         build_tables(C);
         C->nentries = static_cast<uint64_t>(C->mx) * C->my * C->mz;
@@ -521,6 +523,8 @@ int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out) {
         C->h_total = halloc<uint32_t>(1);
         C->h_misc = halloc<uint32_t>(1);
         C->h_staging = halloc<uint8_t>(maxr * C->big_bytes);
+        *C->h_total = 0;
+        *C->h_misc = 0;
         GC_CUDA(cudaMemset(C->mrpd, 0, C->nentries * sizeof(uint4)));
         GC_CUDA(cudaMemset(C->req, 0, C->nentries * sizeof(uint32_t)));
         GC_CUDA(cudaMemset(C->usage, 0, C->nslots * sizeof(uint32_t)));
@@ -533,6 +537,7 @@ int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out) {
         init_slots_kernel<<<std::min<uint32_t>(div_up(C->nslots, 256), 4096), 256>>>(C->order[0], C->slot_level,
                                                                                     C->slot_vpos, C->nslots);
         GC_CUDA(cudaGetLastError());
+        count_launch();
         GC_CUDA(cudaStreamCreateWithFlags(&C->side, cudaStreamNonBlocking));
         GC_CUDA(cudaEventCreateWithFlags(&C->ev_list, cudaEventDisableTiming));
         GC_CUDA(cudaEventCreateWithFlags(&C->ev_upload, cudaEventDisableTiming));
@@ -627,8 +632,11 @@ int gc_cache_stats_get(gc_cache_t C, gc_cache_stats *out) {
         GC_CUDA(cudaMemcpy(&a, C->ctl_lru, sizeof(a), cudaMemcpyDeviceToHost));
         GC_CUDA(cudaMemcpy(&b, C->ctl_miss, sizeof(b), cudaMemcpyDeviceToHost));
         std::lock_guard<std::mutex> g(C->mu);
+        uint32_t used = 0;
+        GC_CUDA(cudaMemcpy(&used, C->d_count, sizeof(used), cudaMemcpyDeviceToHost));
         *out = C->stats;
         out->device_error = a.err | b.err;
+        out->last_used = used;
     });
 }
 
@@ -677,6 +685,22 @@ int gc_cache_dump(gc_cache_t C, int what, void *dst, size_t bytes) {
             }
             default: fail(GC_ERR_INVALID, "unknown dump selector");
         }
+    });
+}
+
+int gc_cache_last_misses(gc_cache_t C, uint32_t *out4, uint32_t max, uint32_t *count, uint32_t *total) {
+    return guard([&] {
+        GC_REQUIRE(C && out4 && count && total, "null argument");
+        GC_CUDA(cudaSetDevice(C->device));
+        {
+            std::unique_lock<std::mutex> lk(C->mu);
+            C->cv.wait(lk, [&] { return !C->busy; });
+        }
+        GC_CUDA(cudaEventSynchronize(C->ev_list));
+        const uint32_t n = std::min(std::min(*C->h_total, C->d.max_requests), max);
+        std::memcpy(out4, C->h_list, static_cast<size_t>(n) * sizeof(uint4));
+        *count = n;
+        *total = *C->h_total;
     });
 }
 

@@ -9,6 +9,7 @@
 //    (GcCore/src/cuda/libPreprocessor/Mipmapper.cu:441-443, 583-597) and
 //    init_meta_data (GcCore/src/libPreprocessor/Bricker_v2.cpp:45-76).
 //  - gc_pool_dims: pool sizing of Applications/DVR-ray-caster/src/Application.cu:79-93.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <fstream>
@@ -21,6 +22,9 @@
 namespace gc {
 
 static thread_local std::string g_last_error;
+static std::atomic<uint64_t> g_launches{0};
+
+void count_launch(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 void set_error(const std::string &msg) { g_last_error = msg; }
 void clear_error() { g_last_error.clear(); }
@@ -111,6 +115,8 @@ extern "C" {
 const char *gc_last_error(void) { return g_last_error.c_str(); }
 
 const char *gc_version(void) { return "gcgb300 0.1 (sm_103a)"; }
+
+uint64_t gc_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int gc_device_count(int *count) {
     return guard([&] {

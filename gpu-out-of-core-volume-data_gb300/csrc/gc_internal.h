@@ -56,6 +56,9 @@ inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s
 
 inline uint32_t div_up(uint64_t a, uint64_t b) { return static_cast<uint32_t>((a + b - 1) / b); }
 
+// Counts kernel launches (gc_kernel_launches).
+void count_launch(uint32_t n = 1);
+
 // Number of SMs of the current device (cached per process for device 0..7).
 int sm_count();
 

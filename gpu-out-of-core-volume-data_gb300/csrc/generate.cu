@@ -210,6 +210,7 @@ int gc_generate_volume(const gc_generator *gen, void *dst, void *stream) {
         GC_REQUIRE(grid.y <= 65535, "volume too wide");
         generate_kernel<<<grid, block, 0, s>>>(dst, p);
         GC_CUDA(cudaGetLastError());
+        count_launch();
         // the constant bank is reused by the next call: keep calls ordered
         if (gen->nblobs) GC_CUDA(cudaStreamSynchronize(s));
     });

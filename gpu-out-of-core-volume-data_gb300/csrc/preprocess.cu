@@ -184,6 +184,7 @@ static void launch_mip(const void *src, void *dst, const uint32_t d[3], uint32_t
                                                 static_cast<uint8_t *>(dst), p, cb, nc);
     }
     GC_CUDA(cudaGetLastError());
+        count_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -234,13 +235,24 @@ __global__ void __launch_bounds__(256) brick_kernel(const uint8_t *__restrict__ 
                                 gz_ < p.D[2];
             const uint8_t *sptr = level + ((static_cast<uint64_t>(gz_) * p.D[1] + gy_) * p.D[0] + gx_) * p.eb;
             switch (p.eb) {
-                case 1: *dptr = inside ? __ldg(sptr) : 0; break;
-                case 2:
-                    *reinterpret_cast<uint16_t *>(dptr) = inside ? __ldg(reinterpret_cast<const uint16_t *>(sptr)) : 0;
+                case 1: {
+                    uint8_t v = 0;
+                    if (inside) v = __ldg(sptr);
+                    *dptr = v;
                     break;
-                case 4:
-                    *reinterpret_cast<uint32_t *>(dptr) = inside ? __ldg(reinterpret_cast<const uint32_t *>(sptr)) : 0;
+                }
+                case 2: {
+                    uint16_t v = 0;
+                    if (inside) v = __ldg(reinterpret_cast<const uint16_t *>(sptr));
+                    *reinterpret_cast<uint16_t *>(dptr) = v;
                     break;
+                }
+                case 4: {
+                    uint32_t v = 0;
+                    if (inside) v = __ldg(reinterpret_cast<const uint32_t *>(sptr));
+                    *reinterpret_cast<uint32_t *>(dptr) = v;
+                    break;
+                }
                 default:
                     for (uint32_t b = 0; b < p.eb; ++b) dptr[b] = inside ? sptr[b] : 0;
             }
@@ -330,6 +342,7 @@ int gc_bricks_build(const void *level, const uint32_t level_dims[3], const gc_vo
         brick_kernel<<<static_cast<unsigned>(grid), 256, 0, as_stream(stream)>>>(
             static_cast<const uint8_t *>(level), static_cast<uint8_t *>(out), p);
         GC_CUDA(cudaGetLastError());
+        count_launch();
     });
 }
 
@@ -347,6 +360,7 @@ int gc_bricks_empty(const void *bricks, uint64_t nb_big_bricks, const gc_volume_
             static_cast<const uint8_t *>(bricks), nb_big_bricks, values, channel_bytes(*vol), threshold,
             flags);
         GC_CUDA(cudaGetLastError());
+        count_launch();
     });
 }
 

@@ -130,9 +130,15 @@ struct VoxelTraits<float> {
 
 // Reference sampler: normalized linear read at the integer voxel corner e =
 // (lx, ly, lz) of the slot = mean of voxels {e-1, e} per axis.
+// With covering >= 1 both voxels lie in the brick; with covering 0 the lower
+// one is clamped to the brick edge (the reference then reads the neighbouring
+// slot of its texture).
 template <typename T>
 __device__ __forceinline__ float sample_corner(const T *__restrict__ b, uint32_t B, uint32_t lx, uint32_t ly,
                                                uint32_t lz) {
+    lx = lx > 0 ? lx : 1u;
+    ly = ly > 0 ? ly : 1u;
+    lz = lz > 0 ? lz : 1u;
     const uint32_t i0 = ((lz - 1) * B + (ly - 1)) * B + (lx - 1);
     const uint32_t BB = B * B;
     if constexpr (sizeof(T) < 4) {
@@ -148,8 +154,9 @@ __device__ __forceinline__ float sample_corner(const T *__restrict__ b, uint32_t
     }
 }
 
-// Trilinear sampler at the fractional position f (voxels of the level).
-__device__ __forceinline__ void tri_axis(float f, uint32_t c, uint32_t beff, uint32_t &i0, float &w) {
+// Trilinear sampler at the fractional position f (voxels of the level); the
+// pair (i0, i0 + 1) is clamped to the brick (only reachable with covering 0).
+__device__ __forceinline__ void tri_axis(float f, uint32_t c, uint32_t beff, uint32_t B, uint32_t &i0, float &w) {
     const uint32_t m = static_cast<uint32_t>(f);
     const float fr = f - static_cast<float>(m);
     const uint32_t l = c + m % beff;
@@ -157,8 +164,12 @@ __device__ __forceinline__ void tri_axis(float f, uint32_t c, uint32_t beff, uin
         i0 = l;
         w = fr - 0.5f;
     } else {
-        i0 = l - 1;
-        w = fr + 0.5f;
+        i0 = l > 0 ? l - 1 : 0u;
+        w = l > 0 ? fr + 0.5f : 0.0f;
+    }
+    if (i0 + 1 >= B) {
+        i0 = B - 2;
+        w = 1.0f;
     }
 }
 template <typename T>
@@ -224,9 +235,9 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
         } else {
             uint32_t x0, y0, z0;
             float wx, wy, wz;
-            tri_axis(fx, cv.c, cv.Beff, x0, wx);
-            tri_axis(fy, cv.c, cv.Beff, y0, wy);
-            tri_axis(fz, cv.c, cv.Beff, z0, wz);
+            tri_axis(fx, cv.c, cv.Beff, B, x0, wx);
+            tri_axis(fy, cv.c, cv.Beff, B, y0, wy);
+            tri_axis(fz, cv.c, cv.Beff, B, z0, wz);
             sample = sample_trilinear<T>(b, B, x0, y0, z0, wx, wy, wz);
         }
         return kMapped;
@@ -430,6 +441,7 @@ void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams 
         kernel<<<grid, kRenderThreads, 0, s>>>(cv, lt, views_dev, nviews, total_tiles, queue,
                                                grid * (kRenderThreads / 32));
         GC_CUDA(cudaGetLastError());
+        count_launch();
     };
     switch (cv.eb) {
         case 1: launch(render_kernel<uint8_t>, 0); break;

@@ -67,7 +67,8 @@ class CacheInfo(C.Structure):
 class CacheStats(C.Structure):
     _fields_ = [("frames", C.c_uint64), ("requests_raised", C.c_uint64), ("requests_served", C.c_uint64),
                 ("bricks_installed", C.c_uint64), ("bricks_empty", C.c_uint64), ("bytes_h2d", C.c_uint64),
-                ("load_errors", C.c_uint64), ("last_requests", C.c_uint32), ("device_error", C.c_uint32)]
+                ("load_errors", C.c_uint64), ("last_requests", C.c_uint32), ("last_used", C.c_uint32),
+                ("device_error", C.c_uint32)]
 
 
 class View(C.Structure):
@@ -89,7 +90,7 @@ vp = C.c_void_p
 P = C.POINTER
 # name -> argtypes (restype is int unless listed in _RESTYPES)
 _SIGS = {
-    "gc_last_error": [], "gc_version": [], "gc_device_count": [P(C.c_int)],
+    "gc_last_error": [], "gc_version": [], "gc_device_count": [P(C.c_int)], "gc_kernel_launches": [],
     "gc_config_create": [P(vp)], "gc_config_destroy": [vp], "gc_config_load": [vp, C.c_char_p],
     "gc_config_set": [vp, C.c_char_p, C.c_char_p], "gc_config_get": [vp, C.c_char_p, C.c_char_p, C.c_size_t],
     "gc_config_volume_desc": [vp, P(VolumeDesc)], "gc_layout_compute": [P(VolumeDesc), P(Layout)],
@@ -109,12 +110,14 @@ _SIGS = {
     "gc_cache_timestamp": [vp, P(C.c_uint32)], "gc_cache_info_get": [vp, P(CacheInfo)],
     "gc_cache_stats_get": [vp, P(CacheStats)], "gc_cache_dump": [vp, C.c_int, vp, C.c_size_t],
     "gc_cache_load_buffer": [vp, C.c_int, vp, C.c_size_t],
+    "gc_cache_last_misses": [vp, P(C.c_uint32), C.c_uint32, P(C.c_uint32), P(C.c_uint32)],
     "gc_view_matrix": [P(C.c_float), P(C.c_float), P(C.c_float)],
     "gc_look_at": [P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_float)],
     "gc_tf_build": [P(TfPoint), C.c_uint32, C.c_uint32, P(C.c_float)],
     "gc_render": [vp, P(View), vp], "gc_render_batch": [vp, P(View), C.c_uint32, vp],
 }
-_RESTYPES = {"gc_last_error": C.c_char_p, "gc_version": C.c_char_p, "gc_brick_key": C.c_uint64}
+_RESTYPES = {"gc_last_error": C.c_char_p, "gc_version": C.c_char_p, "gc_brick_key": C.c_uint64,
+             "gc_kernel_launches": C.c_uint64}
 
 
 class GcError(RuntimeError):
@@ -195,6 +198,10 @@ def pool_dims(vol, pool_bytes):
     return tuple(out)
 
 
+def kernel_launches():
+    return int(lib.gc_kernel_launches())
+
+
 def brick_key(level, x, y, z):
     return int(lib.gc_brick_key(level, x, y, z))
 
@@ -261,6 +268,55 @@ def brick_store_offsets(layout, vol):
         nb = layout.nb_big_bricks[l]
         off += nb[0] * nb[1] * nb[2] * big
     return offs, off, big
+
+
+def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host", pin=False):
+    """Application::pre_process (Applications/DVR-ray-caster/src/Application.cu:148-197)
+    run on the device: mip pyramid, bricking of every level and empty flags.
+
+    level0 is a CUDA tensor holding the level-0 voxels (any dtype, contiguous).
+    Returns (bricks, level_offsets, empty_keys): the big bricks of every level in
+    one uint8 tensor (host memory unless store == "device"; pinned when pin),
+    their per-level byte offsets, and the gc_brick_key of every big brick whose
+    values are all below empty_threshold (none when it is None, like the
+    reference's default threshold 0).
+    """
+    import torch
+
+    eb, nc = vol.encoded_bytes, vol.channels
+    for l in range(layout.nb_levels):
+        if tuple(layout.mip[l]) != tuple(layout.initial[l]):
+            raise GcError(1, "mip level sizes differ from the metadata sizes (dimension <= 2)")
+    offs, total = pyramid_offsets(layout, eb)
+    dev = level0.device
+    pyr = torch.empty(total, dtype=torch.uint8, device=dev)
+    n0 = level0.numel() * level0.element_size()
+    pyr[:n0].copy_(level0.reshape(-1).view(torch.uint8))
+    Mipmapper.process(pyr.data_ptr(), layout, offs, eb, nc, stream)
+    soffs, stotal, big = brick_store_offsets(layout, vol)
+    bricks = torch.empty(stotal, dtype=torch.uint8, device=dev)
+    for l in range(layout.nb_levels):
+        process_bricking(pyr.data_ptr() + offs[l], layout.initial[l], vol, layout.nb_big_bricks[l],
+                         bricks.data_ptr() + soffs[l], stream)
+    empty_keys = []
+    if empty_threshold is not None:
+        for l in range(layout.nb_levels):
+            nb = layout.nb_big_bricks[l]
+            n = nb[0] * nb[1] * nb[2]
+            flags = torch.empty(n, dtype=torch.uint8, device=dev)
+            process_empty(bricks.data_ptr() + soffs[l], n, vol, empty_threshold, flags.data_ptr(), stream)
+            torch.cuda.synchronize(dev)
+            for i in torch.nonzero(flags).flatten().tolist():
+                x, y, z = i % nb[0], (i // nb[0]) % nb[1], i // (nb[0] * nb[1])
+                empty_keys.append(brick_key(l, x, y, z))
+    torch.cuda.synchronize(dev)
+    del pyr
+    if store == "device":
+        return bricks, soffs, empty_keys
+    host = torch.empty(stotal, dtype=torch.uint8, pin_memory=pin)
+    host.copy_(bricks)
+    del bricks
+    return host, soffs, empty_keys
 
 
 # ---------------------------------------------------------------------------
@@ -357,6 +413,16 @@ class CacheManager:
         """Copies one state buffer into a writable host buffer (numpy array)."""
         check(lib.gc_cache_dump(self._h, what, vp(buf.ctypes.data), buf.nbytes))
         return buf
+
+    def last_misses(self, max_entries=None):
+        """(total flagged, list of (x, y, z, level)) of the last request scan."""
+        import numpy as np
+
+        m = max_entries or self.desc.max_requests
+        out = np.zeros((m, 4), dtype=np.uint32)
+        n, tot = C.c_uint32(), C.c_uint32()
+        check(lib.gc_cache_last_misses(self._h, out.ctypes.data_as(P(C.c_uint32)), m, C.byref(n), C.byref(tot)))
+        return tot.value, out[: n.value]
 
     def load_buffer(self, what, buf):
         check(lib.gc_cache_load_buffer(self._h, what, vp(buf.ctypes.data), buf.nbytes))

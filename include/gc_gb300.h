@@ -91,6 +91,8 @@ typedef struct gc_layout {
 const char *gc_last_error(void);
 const char *gc_version(void);
 int gc_device_count(int *count);
+/* Number of CUDA kernels this library has launched in this process. */
+uint64_t gc_kernel_launches(void);
 
 /* ------------------------------------------------------------------------ */
 /* Configuration: Configuration::load<TDNSConfigurationParser> +
@@ -242,6 +244,7 @@ typedef struct gc_cache_stats {
     uint64_t bytes_h2d;           /* brick bytes copied host -> device         */
     uint64_t load_errors;         /* GC_BRICK_UNKNOWN answers from the source  */
     uint32_t last_requests;       /* misses found in the last request scan     */
+    uint32_t last_used;           /* slots stamped by the last rendered frame   */
     uint32_t device_error;        /* sticky device-side error word (0 = none)  */
 } gc_cache_stats;
 int gc_cache_stats_get(gc_cache_t cache, gc_cache_stats *out);
@@ -260,6 +263,10 @@ int gc_cache_stats_get(gc_cache_t cache, gc_cache_stats *out);
 #define GC_DUMP_REQUESTS 3
 #define GC_DUMP_POOL 4
 int gc_cache_dump(gc_cache_t cache, int what, void *dst, size_t bytes);
+/* Miss list of the last request scan (coord_1D_to_3D output: x, y, z, level
+ * per brick, CacheManagerKernels.cu:32-72), at most `max` entries; *total is
+ * the number of bricks flagged in the scan.  Waits for the scan to finish. */
+int gc_cache_last_misses(gc_cache_t cache, uint32_t *out4, uint32_t max, uint32_t *count, uint32_t *total);
 /* Overwrite the usage or request buffer (GC_DUMP_USAGE / GC_DUMP_REQUESTS)
  * from the host: used to replay recorded frames through the update path. */
 int gc_cache_load_buffer(gc_cache_t cache, int what, const void *src, size_t bytes);

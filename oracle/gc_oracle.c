@@ -805,7 +805,7 @@ static float voxel_value(const orc_cache *c, const uint8_t *slot, uint32_t idx) 
     return ((const float *)slot)[idx];
 }
 
-static void tri_axis(float f, uint32_t cov, uint32_t beff, uint32_t *i0, float *w) {
+static void tri_axis(float f, uint32_t cov, uint32_t beff, uint32_t B, uint32_t *i0, float *w) {
     uint32_t m = (uint32_t)f;
     float fr = f - (float)m;
     uint32_t l = cov + m % beff;
@@ -813,8 +813,12 @@ static void tri_axis(float f, uint32_t cov, uint32_t beff, uint32_t *i0, float *
         *i0 = l;
         *w = fr - 0.5f;
     } else {
-        *i0 = l - 1;
-        *w = fr + 0.5f;
+        *i0 = l > 0 ? l - 1 : 0u;
+        *w = l > 0 ? fr + 0.5f : 0.0f;
+    }
+    if (*i0 + 1 >= B) {
+        *i0 = B - 2;
+        *w = 1.0f;
     }
 }
 
@@ -845,6 +849,9 @@ static int fetch32(orc_cache *c, uint32_t sampler, uint32_t lod, f3 np, walk *w,
         if (sampler == GC_SAMPLER_REFERENCE) {
             uint32_t lx = c->c + (uint32_t)fx % c->Beff, ly = c->c + (uint32_t)fy % c->Beff,
                      lz = c->c + (uint32_t)fz % c->Beff;
+            if (lx == 0) lx = 1;
+            if (ly == 0) ly = 1;
+            if (lz == 0) lz = 1;
             uint32_t i0 = ((lz - 1) * B + (ly - 1)) * B + (lx - 1), BB2 = B * B;
             if (c->eb < 4) {
                 uint32_t s = 0;
@@ -861,9 +868,9 @@ static int fetch32(orc_cache *c, uint32_t sampler, uint32_t lod, f3 np, walk *w,
         } else {
             uint32_t x0, y0, z0;
             float wx, wy, wz;
-            tri_axis(fx, c->c, c->Beff, &x0, &wx);
-            tri_axis(fy, c->c, c->Beff, &y0, &wy);
-            tri_axis(fz, c->c, c->Beff, &z0, &wz);
+            tri_axis(fx, c->c, c->Beff, B, &x0, &wx);
+            tri_axis(fy, c->c, c->Beff, B, &y0, &wy);
+            tri_axis(fz, c->c, c->Beff, B, &z0, &wz);
             uint32_t i = (z0 * B + y0) * B + x0, BB2 = B * B;
 #define LV(k) voxel_value(c, sb, (k))
             float c00 = LV(i) + (LV(i + 1) - LV(i)) * wx;
@@ -1132,6 +1139,9 @@ static void march64(orc_cache *c, const gc_view *v, const float *tf, uint32_t x,
                 if (v->sampler == GC_SAMPLER_REFERENCE) {
                     uint32_t lx = c->c + (uint32_t)fx % c->Beff, ly = c->c + (uint32_t)fy % c->Beff,
                              lz = c->c + (uint32_t)fz % c->Beff;
+                    if (lx == 0) lx = 1;
+                    if (ly == 0) ly = 1;
+                    if (lz == 0) lz = 1;
                     double s = 0;
                     for (int dz = 0; dz < 2; ++dz)
                         for (int dyy = 0; dyy < 2; ++dyy)
@@ -1149,8 +1159,12 @@ static void march64(orc_cache *c, const gc_view *v, const float *tf, uint32_t x,
                             i0[a] = l;
                             wt[a] = fr - 0.5;
                         } else {
-                            i0[a] = l - 1;
-                            wt[a] = fr + 0.5;
+                            i0[a] = l > 0 ? l - 1 : 0u;
+                            wt[a] = l > 0 ? fr + 0.5 : 0.0;
+                        }
+                        if (i0[a] + 1 >= B) {
+                            i0[a] = B - 2;
+                            wt[a] = 1.0;
                         }
                     }
                     double s = 0;

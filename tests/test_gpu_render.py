@@ -1,0 +1,191 @@
+"""Ray caster parity: the CUDA render + update loop against the oracle's FP32
+restatement of RayCastDVR/RayCastMOP and CacheManager::update, frame by frame.
+
+Tolerances (per RGBA channel, in 1/255 units):
+  CUDA vs FP32 oracle : 0   (same operation sequence; cache state bit-exact)
+  CUDA vs FP64 oracle : 1   (the double-precision restatement of the method)
+"""
+import numpy as np
+import pytest
+
+import scenario
+
+pytestmark = pytest.mark.gpu
+
+RGBA_TOL_FP32 = 0
+RGBA_TOL_FP64 = 1
+
+
+class Scene:
+    def __init__(self, gc, orc, torch, size, bpc, B, c, bb, pool, maxreq, seed=21, nblobs=6, sync=True):
+        self.gc, self.orc, self.torch = gc, orc, torch
+        self.vol = gc.volume_desc(size, B, c, bpc, 1, bb)
+        self.layout = gc.compute_layout(self.vol)
+        d = scenario.gpu_volume(gc, torch, size, bpc, seed, nblobs)
+        self.store, self.offs, _ = gc.pre_process(self.vol, self.layout, d)
+        o = scenario.orc_volume(orc, size, bpc, seed, nblobs)
+        ref, roffs = scenario.orc_store(orc, gc, o.reshape(-1).view(np.uint8), self.vol, self.layout)
+        assert np.array_equal(self.store.numpy(), ref)
+        self.ref = ref
+        self.cm = gc.CacheManager(self.vol, self.layout, pool, max_requests=maxreq, sync_loader=sync)
+        self.cm.set_source_host(self.store.data_ptr(), self.offs)
+        self.oc = orc.Cache(self.cm.desc)
+        self.oc.set_source(ref, roffs)
+
+    def buffers(self, W, H):
+        t = self.torch
+        g = (t.zeros(W * H, dtype=t.int32, device="cuda"), t.zeros(W * H, dtype=t.float32, device="cuda"),
+             t.zeros(W * H * 4, dtype=t.float32, device="cuda"))
+        o = (np.zeros(W * H, np.uint32), np.zeros(W * H, np.float32), np.zeros(W * H * 4, np.float32))
+        return g, o
+
+    def view(self, m, W, H, tf_dev, tfw, g, **kw):
+        return self.gc.make_view(m, W, H, tf_dev.data_ptr(), tfw, g[0].data_ptr(), g[1].data_ptr(), g[2].data_ptr(),
+                                 **kw)
+
+    def compare_cache(self, tag):
+        gc, oc, cm = self.gc, self.oc, self.cm
+        lru = np.zeros(oc.nslots, dtype=oc.lru().dtype)
+        cm.dump(gc.DUMP_LRU, lru)
+        assert np.array_equal(lru, oc.lru()), tag
+        for what, ref in ((gc.DUMP_USAGE, oc.usage()), (gc.DUMP_REQUESTS, oc.requests())):
+            a = np.zeros_like(ref)
+            cm.dump(what, a)
+            assert np.array_equal(a, ref), (tag, what)
+        mrpd = np.zeros((oc.nentries, 4), np.uint32)
+        cm.dump(gc.DUMP_MRPD, mrpd)
+        assert np.array_equal(mrpd, oc.mrpd()), tag
+        pool = np.zeros(oc.pool_bytes, np.uint8)
+        cm.dump(gc.DUMP_POOL, pool)
+        assert np.array_equal(pool, oc.pool()), tag
+
+
+def rgba_diff(a, b):
+    return np.abs(a.view(np.uint8).astype(np.int32) - b.view(np.uint8).astype(np.int32))
+
+
+LOOP_CASES = {
+    # size, bpc, B, c, big brick, pool, maxreq, W, H, view kwargs
+    "u8_dvr_ref": ((64, 64, 64), 1, 16, 1, (1, 1, 1), (4, 4, 4), 50, 56, 48, dict()),
+    "u16_mop_tri": ((48, 48, 48), 2, 8, 1, (2, 1, 1), (5, 5, 5), 64, 40, 36,
+                    dict(mode=1, sampler=1, early_alpha=0.99, focal=2.4142137)),
+    "u8_dvr_tri_wide": ((80, 64, 48), 1, 16, 2, (1, 1, 1), (6, 5, 5), 300, 77, 45,
+                        dict(sampler=1, early_alpha=0.99)),
+}
+
+
+@pytest.mark.parametrize("case", sorted(LOOP_CASES))
+def test_render_update_loop_matches_oracle(gc, orc, torch_cuda, case):
+    size, bpc, B, c, bb, pool, maxreq, W, H, kw = LOOP_CASES[case]
+    s = Scene(gc, orc, torch_cuda, size, bpc, B, c, bb, pool, maxreq)
+    tf = scenario.ramp_tf() if "dvr" in case else scenario.bumps_tf(3)
+    tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
+    g, o = s.buffers(W, H)
+    for f in range(16):
+        m = scenario.orbit_camera(gc, f // 4, 12, 2.6 + 0.3 * (f // 4))
+        if f % 4 == 0:  # camera moved: restart the progressive buffers
+            for x in g:
+                x.zero_()
+            for x in o:
+                x[:] = 0
+        v = s.view(m, W, H, tf_dev, 256, g, **kw)
+        s.cm.render(v)
+        s.oc.render(v, tf, *o)
+        torch_cuda.cuda.synchronize()
+        d = rgba_diff(g[0].cpu().numpy(), o[0])
+        assert d.max() <= RGBA_TOL_FP32, f"frame {f}: max {d.max()} at {np.argmax(d)}"
+        assert np.array_equal(g[1].cpu().numpy(), o[1]), f"frame {f}: t buffer"
+        assert np.array_equal(g[2].cpu().numpy(), o[2]), f"frame {f}: colour state"
+        c1, c2 = s.cm.update(), s.oc.update()
+        assert c1 == c2, f"frame {f}"
+        s.compare_cache(f"frame {f}")
+    st = s.cm.stats()
+    assert st.bricks_installed > 0 and st.device_error == 0
+
+
+def test_batch_matches_sequential_oracle(gc, orc, torch_cuda):
+    """Three views of different sizes in one persistent launch (one cache
+    frame) equal the oracle rendering them one after the other."""
+    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 4096)
+    tf = scenario.ramp_tf()
+    tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
+    sizes = [(64, 48), (33, 17), (96, 80)]
+    bufs = [s.buffers(W, H) for W, H in sizes]
+    for f in range(6):
+        views = []
+        for i, (W, H) in enumerate(sizes):
+            m = scenario.orbit_camera(gc, i * 3 + 1, 12, 3.0)
+            views.append(s.view(m, W, H, tf_dev, 256, bufs[i][0]))
+        s.cm.render_batch(views)
+        for i in range(len(sizes)):
+            s.oc.render(views[i], tf, *bufs[i][1])
+        torch_cuda.cuda.synchronize()
+        for i in range(len(sizes)):
+            d = rgba_diff(bufs[i][0][0].cpu().numpy(), bufs[i][1][0])
+            assert d.max() <= RGBA_TOL_FP32, (f, i)
+        assert s.cm.update() == s.oc.update()
+        s.compare_cache(f"frame {f}")
+
+
+def test_converged_image_vs_fp64_oracle(gc, orc, torch_cuda):
+    """After convergence the FP32 CUDA image is within 1/255 of the
+    double-precision restatement of the same method."""
+    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 4096)
+    tf = scenario.ramp_tf()
+    tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
+    W, H = 160, 128
+    g, o = s.buffers(W, H)
+    m = scenario.orbit_camera(gc, 3, 36, 3.2)
+    for mode, sampler in ((0, 0), (0, 1), (1, 0)):
+        v = s.view(m, W, H, tf_dev, 256, g, mode=mode, sampler=sampler)
+        for f in range(12):
+            for x in g:
+                x.zero_()
+            s.cm.render(v)
+            conv = s.cm.update()
+            if conv and f >= 1:
+                break
+        assert conv
+        for x in g:
+            x.zero_()
+        s.cm.render(v)
+        torch_cuda.cuda.synchronize()
+        s.cm.update()
+        r64 = np.zeros(W * H, np.uint32)
+        scratch_u = np.zeros(s.oc.nslots, np.uint32)
+        scratch_r = np.zeros(s.oc.nentries, np.uint32)
+        # the oracle reads the GPU's converged page directory and pool
+        s.cm.dump(gc.DUMP_MRPD, s.oc.mrpd())
+        s.cm.dump(gc.DUMP_POOL, s.oc.pool())
+        s.oc.render_f64(v, tf, r64, np.zeros(W * H), np.zeros(W * H * 4), scratch_u, scratch_r)
+        d = rgba_diff(g[0].cpu().numpy(), r64)
+        assert d.max() <= RGBA_TOL_FP64, (mode, sampler, d.max())
+        assert (g[0].cpu().numpy() >> 24).astype(bool).mean() > 0.05  # the image is not empty
+
+
+def test_async_loader_converges_to_same_image(gc, orc, torch_cuda):
+    """The asynchronous loader (bricks resolved on a host thread, uploaded by
+    cudaMemcpyAsync on a side stream) reaches the image of the synchronous one."""
+    imgs = []
+    for sync in (True, False):
+        s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 4096, sync=sync)
+        tf = scenario.ramp_tf()
+        tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
+        g, _ = s.buffers(96, 80)
+        v = s.view(scenario.orbit_camera(gc, 2, 12, 3.0), 96, 80, tf_dev, 256, g)
+        conv = False
+        for f in range(200):
+            for x in g:
+                x.zero_()
+            s.cm.render(v)
+            conv = s.cm.update()
+            if conv and f > 2:
+                break
+        assert conv
+        for x in g:
+            x.zero_()
+        s.cm.render(v)
+        torch_cuda.cuda.synchronize()
+        imgs.append(g[0].cpu().numpy())
+        s.cm.close()
+    assert np.array_equal(imgs[0], imgs[1])
