@@ -69,7 +69,7 @@ LOOP_CASES = {
     "u8_dvr_ref": ((64, 64, 64), 1, 16, 1, (1, 1, 1), (4, 4, 4), 50, 56, 48, dict()),
     "u16_mop_tri": ((48, 48, 48), 2, 8, 1, (2, 1, 1), (5, 5, 5), 64, 40, 36,
                     dict(mode=1, sampler=1, early_alpha=0.99, focal=2.4142137)),
-    "u8_dvr_tri_wide": ((80, 64, 48), 1, 16, 2, (1, 1, 1), (6, 5, 5), 300, 77, 45,
+    "u8_dvr_tri_wide": ((80, 64, 48), 1, 16, 2, (1, 1, 1), (6, 5, 5), 150, 77, 45,
                         dict(sampler=1, early_alpha=0.99)),
 }
 
@@ -106,7 +106,7 @@ def test_render_update_loop_matches_oracle(gc, orc, torch_cuda, case):
 def test_batch_matches_sequential_oracle(gc, orc, torch_cuda):
     """Three views of different sizes in one persistent launch (one cache
     frame) equal the oracle rendering them one after the other."""
-    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 4096)
+    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 216)
     tf = scenario.ramp_tf()
     tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
     sizes = [(64, 48), (33, 17), (96, 80)]
@@ -130,7 +130,7 @@ def test_batch_matches_sequential_oracle(gc, orc, torch_cuda):
 def test_converged_image_vs_fp64_oracle(gc, orc, torch_cuda):
     """After convergence the FP32 CUDA image is within 1/255 of the
     double-precision restatement of the same method."""
-    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 4096)
+    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 216)
     tf = scenario.ramp_tf()
     tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
     W, H = 160, 128
@@ -168,7 +168,7 @@ def test_async_loader_converges_to_same_image(gc, orc, torch_cuda):
     cudaMemcpyAsync on a side stream) reaches the image of the synchronous one."""
     imgs = []
     for sync in (True, False):
-        s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 4096, sync=sync)
+        s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 216, sync=sync)
         tf = scenario.ramp_tf()
         tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
         g, _ = s.buffers(96, 80)
