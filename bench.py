@@ -1,23 +1,35 @@
 """Benchmark of the out-of-core volume path on one GB300.
 
-Metric: Mrays/s (primary rays W*H per view per frame) with p50/p99 frame
-latency, plain per-view path; the batched form is reported beside it.
+Metric: Mrays/s of converged views (W*H primary rays per view) with p50/p99
+view latency, for the plain per-view path (value, e2e) and the batched form.
 
-  python bench.py [--config c2] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py [--steps K] [--warmup W] [--impl ours|reference] [--config c2]
+
+A step renders one view to convergence, the way the reference's own benchmark
+counts time until "Frame done" (ref:bench.sh:39-55): restart the progressive
+buffers (the camera moved), then repeat {render, cache update} until the
+update reports an empty miss list.  Each iteration pages the missing bricks in
+from host memory (miss scan -> loader -> pinned staging -> cudaMemcpyAsync ->
+install).  Rays are counted once per converged view.
 
 Workloads (seeded synthetic volumes with the shapes of the benchmark configs;
 no public dataset is used):
-  c1  256^3 u8, BrickSize 16, covering 1, 512^2 views orbiting at 2x the
-      diagonal, fov 45 deg, TF ramp (alpha 0 at 40 -> 0.6 at 255), early alpha 0.99
-  c2  2048^3 u16 (16 GiB), BrickSize 16, covering 1, 2 GiB pool, 1024^2 views
-      on a fly-through zooming from 3.0x to 0.3x the diagonal, TF with 3
-      Gaussian alpha bumps
-A step is one frame: render (camera parameters go host -> device with the
-call), cache update (LRU update, miss scan or brick install; missed bricks go
-up from pinned host memory on a side stream), and for e2e the RGBA frame read
-back into pinned host memory.  Inputs larger than L2 (the pool and the page
-directory) are touched every frame.
+  c2  (plain, the bench line's value)  2048^3 u16 (16 GiB), BrickSize 16,
+      covering 1, 2 GiB pool, 1024^2 views along a fly-through zooming from 3.0x
+      to 0.3x the diagonal, fov 45 deg, TF with 3 Gaussian alpha bumps,
+      early termination at alpha 0.99.
+  c3  (batched, reported under "batched")  the same volume with BrickSize 32
+      and a 4 GiB pool; batches of 64 views on a sphere at 0.5-3.0x the
+      diagonal with sizes uniform over {256^2, 512^2, 1024^2, 1920x1080}, all
+      views of a batch in one persistent launch sharing the cache's miss list;
+      the same views are also rendered one at a time (plain) for the ratio.
+  c1  256^3 u8 (small; used for profiling).
+The pool and page directory exceed L2 (129 MB) for c2/c3.
 
+value  : views rendered into device buffers.
+e2e    : the same through the C ABI with the converged RGBA frame read back
+         into pinned host memory inside the timed region; brick bytes paged in
+         (H2D) and the frame (D2H) are counted per step.
 --impl reference runs the CPU port of the same method (the oracle's FP32
 ray-march + cache state machine, all host threads) on a bounded sample.
 """
@@ -29,7 +41,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -40,15 +51,20 @@ for _p in (ROOT, PKG):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
+VOL2048 = dict(size=(2048, 2048, 2048), bpc=2, nblobs=32, sigma=(40.0, 300.0), amp=(60 * 257, 200 * 257),
+               noise=20 * 257, seed=2)
 CONFIGS = {
     "c1": dict(size=(256, 256, 256), bpc=1, nblobs=8, sigma=(10.0, 40.0), amp=(60, 200), noise=20, seed=1, B=16,
                c=1, pool_bytes=None, pool_slots=(21, 21, 21), W=512, H=512, frames=36, path="orbit",
                dist=(2.0, 2.0), tf="ramp", early=0.99, fov=45.0),
-    "c2": dict(size=(2048, 2048, 2048), bpc=2, nblobs=32, sigma=(40.0, 300.0), amp=(60 * 257, 200 * 257),
-               noise=20 * 257, seed=2, B=16, c=1, pool_bytes=2 << 30, pool_slots=None, W=1024, H=1024, frames=120,
-               path="fly", dist=(3.0, 0.3), tf="bumps", early=0.99, fov=45.0),
+    "c2": dict(VOL2048, B=16, c=1, pool_bytes=2 << 30, pool_slots=None, W=1024, H=1024, frames=120, path="fly",
+               dist=(3.0, 0.3), tf="bumps", early=0.99, fov=45.0),
+    "c3": dict(VOL2048, B=32, c=1, pool_bytes=4 << 30, pool_slots=None, batch=64,
+               sizes=((256, 256), (512, 512), (1024, 1024), (1920, 1080)), dist=(0.5, 3.0), tf="bumps",
+               early=0.99, fov=45.0),
 }
 DIAG = 2.0 * math.sqrt(3.0)
+PIXEL_BYTES = 44  # RGBA 4 + t 4+4 + colour state 16+16 per pixel and launch
 
 
 def log(*a):
@@ -57,11 +73,11 @@ def log(*a):
 
 def tf_table(kind, seed=3):
     x = np.linspace(0.0, 1.0, 256)
-    if kind == "ramp":
+    if kind == "ramp":  # alpha 0 up to value 40, ramp to 0.6 at 255
         v = x * 255.0
         a = np.where(v <= 40, 0.0, 0.6 * np.clip((v - 40) / 215.0, 0, 1))
         rgb = np.stack([np.clip(0.2 + 1.2 * x, 0, 1), 0.3 + 1.2 * x * (1 - x), 1.0 - x], 1)
-    else:
+    else:  # three seeded Gaussian alpha bumps
         rng = np.random.default_rng(seed)
         a = np.zeros_like(x)
         for _ in range(3):
@@ -71,14 +87,13 @@ def tf_table(kind, seed=3):
     return np.concatenate([rgb, np.clip(a, 0, 1)[:, None]], 1).astype(np.float32)
 
 
-def camera(gc, cfg, f, rank=0):
+def path_camera(gc, cfg, f, rank=0):
     n = cfg["frames"]
     t = (f % n) / max(1, n - 1)
     if cfg["path"] == "orbit":
         ang = 2 * math.pi * ((f + rank * 7) % n) / n
         d = cfg["dist"][0] * DIAG
-        eye = (d * math.sin(ang) * math.cos(0.3), d * math.sin(0.3), d * math.cos(ang) * math.cos(0.3))
-        return gc.look_at(eye)
+        return gc.look_at((d * math.sin(ang) * math.cos(0.3), d * math.sin(0.3), d * math.cos(ang) * math.cos(0.3)))
     d = (cfg["dist"][0] + (cfg["dist"][1] - cfg["dist"][0]) * t) * DIAG
     ang = 0.6 * t + 0.4 * rank
     dirv = (math.sin(ang) * 0.8, 0.35, math.cos(ang))
@@ -88,12 +103,25 @@ def camera(gc, cfg, f, rank=0):
     return gc.look_at(eye, target)
 
 
+def batch_views(gc, cfg, seed, n):
+    """n seeded (matrix, W, H): cameras on a sphere looking at the centre."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        v = rng.standard_normal(3)
+        v /= np.linalg.norm(v)
+        d = rng.uniform(*cfg["dist"]) * DIAG
+        up = (0.0, 1.0, 0.0) if abs(v[1]) < 0.95 else (1.0, 0.0, 0.0)
+        W, H = cfg["sizes"][int(rng.integers(0, len(cfg["sizes"])))]
+        out.append((gc.look_at(tuple(float(c) * d for c in v), (0.0, 0.0, 0.0), up), W, H))
+    return out
+
+
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
     def __init__(self):
-        self.proc = None
-        self.path = None
+        self.proc, self.path = None, None
 
     def start(self):
         try:
@@ -102,9 +130,10 @@ class ClockSampler:
             q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
-            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                          "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
-                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0"
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-i",
+                                          dev, "-lms", "100"], stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
         except (OSError, ValueError):
             self.proc = None
 
@@ -113,18 +142,22 @@ class ClockSampler:
             return None
         self.proc.terminate()
         self.proc.wait(timeout=5)
-        rows = []
-        for line in open(self.path):
-            parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 9:
-                rows.append(parts)
+        rows = [[p.strip() for p in line.split(",")] for line in open(self.path)]
+        rows = [r for r in rows if len(r) >= 9]
         os.remove(self.path)
         if not rows:
             return None
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [v for v in (num(r[1]) for r in rows) if v is not None]
+        mx = [v for v in (num(r[2]) for r in rows) if v is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows)}
 
@@ -137,7 +170,9 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def build_scene(gc, torch, cfg, max_requests, sync):
+def make_store(gc, torch, cfg):
+    """Synthetic volume generated on the device, pre-processed (mip + bricks) on
+    the device, brick store moved to host memory (the out-of-core source)."""
     size, bpc = cfg["size"], cfg["bpc"]
     vol = gc.volume_desc(size, cfg["B"], cfg["c"], bpc, 1)
     layout = gc.compute_layout(vol)
@@ -152,15 +187,98 @@ def build_scene(gc, torch, cfg, max_requests, sync):
     del dev
     torch.cuda.empty_cache()
     t2 = time.time()
-    log(f"volume {size} generated in {t1 - t0:.2f}s, pre-processed ({store.numel() / 2**30:.2f} GiB bricks) "
-        f"in {t2 - t1:.2f}s")
-    pool = cfg["pool_slots"] or gc.pool_dims(vol, cfg["pool_bytes"])
-    cm = gc.CacheManager(vol, layout, pool, max_requests=max_requests, sync_loader=sync)
-    cm.set_source_host(store.data_ptr(), offs)
-    return vol, layout, store, offs, cm, pool, (t2 - t0)
+    log(f"volume {size} B{cfg['B']}: generated {t1 - t0:.2f}s, pre-processed "
+        f"({store.numel() / 2**30:.2f} GiB of bricks) {t2 - t1:.2f}s")
+    return vol, layout, store, offs, t2 - t0
 
 
-def run_ours(args, cfg):
+class Session:
+    """One cache + the buffers of its views, driven through the C ABI."""
+
+    def __init__(self, gc, torch, cfg, vol, layout, store, offs, max_requests, sync=True):
+        self.gc, self.torch, self.cfg = gc, torch, cfg
+        self.pool = cfg["pool_slots"] or gc.pool_dims(vol, cfg["pool_bytes"])
+        self.cm = gc.CacheManager(vol, layout, self.pool, max_requests=max_requests, sync_loader=sync)
+        self.cm.set_source_host(store.data_ptr(), offs)
+        self.vol = vol
+        self.tf = torch.from_numpy(tf_table(cfg["tf"]).reshape(-1)).cuda()
+        self.stream = torch.cuda.Stream()
+        self.sp = self.stream.cuda_stream
+        self.focal = 1.0 / math.tan(math.radians(cfg["fov"]) / 2)
+        self.bufs = {}
+
+    def buffers(self, i, W, H):
+        key = (i, W, H)
+        if key not in self.bufs:
+            t = self.torch
+            self.bufs[key] = (t.zeros(W * H, dtype=t.int32, device="cuda"),
+                              t.zeros(W * H, dtype=t.float32, device="cuda"),
+                              t.zeros(W * H * 4, dtype=t.float32, device="cuda"),
+                              t.empty(W * H, dtype=t.int32, pin_memory=True))
+        return self.bufs[key]
+
+    def views(self, specs):
+        out, bufs = [], []
+        for i, (m, W, H) in enumerate(specs):
+            b = self.buffers(i, W, H)
+            bufs.append(b)
+            out.append(self.gc.make_view(m, W, H, self.tf.data_ptr(), 256, b[0].data_ptr(), b[1].data_ptr(),
+                                         b[2].data_ptr(), tstep=2.0 / 256.0, focal=self.focal,
+                                         early_alpha=self.cfg["early"]))
+        return out, bufs
+
+    def converge(self, specs, e2e=False, cap=64, render_events=None):
+        """Render the views to convergence; returns (iterations, converged)."""
+        torch = self.torch
+        views, bufs = self.views(specs)
+        it, conv = 0, False
+        with torch.cuda.stream(self.stream):
+            for b in bufs:  # camera moved: restart progressive rendering (VolumeRayCaster.cu:320-329)
+                b[1].zero_()
+                b[2].zero_()
+            while not conv and it < cap:
+                if render_events is not None:
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(self.stream)
+                if len(views) == 1:
+                    self.cm.render(views[0], self.sp)
+                else:
+                    self.cm.render_batch(views, self.sp)
+                if render_events is not None:
+                    e1.record(self.stream)
+                    render_events.append((e0, e1))
+                conv = self.cm.update(self.sp)
+                it += 1
+            if e2e:
+                for b in bufs:
+                    b[3].copy_(b[0], non_blocking=True)
+        return it, conv
+
+    def close(self):
+        self.cm.close()
+
+
+def timed(torch, stream, fn, steps):
+    """Per-step latencies (CUDA events on the launch stream) and wall time."""
+    lat, info = [], []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        info.append(fn(i))
+        b.record(stream)
+        lat.append((a, b))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    return wall, [x.elapsed_time(y) for x, y in lat], info
+
+
+def pct(v, q):
+    return round(float(np.percentile(v, q)), 4)
+
+
+def run_ours(args):
     import torch
 
     import gcgb300 as gc
@@ -172,163 +290,178 @@ def run_ours(args, cfg):
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-    vol, layout, store, offs, cm, pool, prep_s = build_scene(gc, torch, cfg, args.max_requests, sync=False)
+    cfg = CONFIGS[args.config]
+    vol, layout, store, offs, prep_s = make_store(gc, torch, cfg)
+    S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
     W, H = cfg["W"], cfg["H"]
-    tf = torch.from_numpy(tf_table(cfg["tf"]).reshape(-1)).cuda()
-    rgba = torch.zeros(W * H, dtype=torch.int32, device="cuda")
-    tbuf = torch.zeros(W * H, dtype=torch.float32, device="cuda")
-    state = torch.zeros(W * H * 4, dtype=torch.float32, device="cuda")
-    host_rgba = torch.empty(W * H, dtype=torch.int32, pin_memory=True)
-    stream = torch.cuda.Stream()
-    sp = stream.cuda_stream
-    focal = 1.0 / math.tan(math.radians(cfg["fov"]) / 2)
-
-    def view(f):
-        return gc.make_view(camera(gc, cfg, f, rank), W, H, tf.data_ptr(), 256, rgba.data_ptr(), tbuf.data_ptr(),
-                            state.data_ptr(), tstep=2.0 / 256.0, focal=focal, early_alpha=cfg["early"])
-
-    def frame(f, e2e, ev):
-        with torch.cuda.stream(stream):
-            ev[0].record(stream)
-            tbuf.zero_()   # camera moved: restart progressive rendering (VolumeRayCaster.cu:320-329)
-            state.zero_()
-            ev[1].record(stream)
-            cm.render(view(f), sp)
-            ev[2].record(stream)
-            cm.update(sp)
-            if e2e:
-                host_rgba.copy_(rgba, non_blocking=True)
-            ev[3].record(stream)
-
-    def loop(k, start, e2e):
-        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(k)]
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for i in range(k):
-            frame(start + i, e2e, evs[i])
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-        lat = [evs[i][0].elapsed_time(evs[i][3]) for i in range(k)]
-        rend = [evs[i][1].elapsed_time(evs[i][2]) for i in range(k)]
-        return wall, lat, rend
+    spec = lambda f: [(path_camera(gc, cfg, f, rank), W, H)]  # noqa: E731
 
     for f in range(args.warmup):
-        frame(f, True, [torch.cuda.Event(enable_timing=True) for _ in range(4)])
-    torch.cuda.synchronize()
-    s0 = cm.stats()
-    launches0 = gc.kernel_launches()
+        S.converge(spec(f))
+    s0, l0 = S.cm.stats(), gc.kernel_launches()
     clocks = ClockSampler()
     clocks.start()
-    wall_dev, lat_dev, rend_dev = loop(args.steps, args.warmup, e2e=False)
-    launches_dev = gc.kernel_launches() - launches0
-    s1 = cm.stats()
-    wall_e2e, lat_e2e, rend_e2e = loop(args.steps, args.warmup + args.steps, e2e=True)
-    s2 = cm.stats()
+    rev = []
+    wall, lat, info = timed(torch, S.stream, lambda i: S.converge(spec(args.warmup + i), render_events=rev),
+                            args.steps)
+    launches = gc.kernel_launches() - l0
+    s1 = S.cm.stats()
+    wall_e, lat_e, _ = timed(torch, S.stream, lambda i: S.converge(spec(args.warmup + args.steps + i), e2e=True),
+                             args.steps)
+    s2 = S.cm.stats()
     clk = clocks.stop()
     if world > 1:
-        t = torch.tensor([wall_dev, wall_e2e], device="cuda")
+        t = torch.tensor([wall, wall_e], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        wall_dev, wall_e2e = t.tolist()
+        wall, wall_e = t.tolist()
     rays = W * H * args.steps * world
-    value = rays / wall_dev / 1e6
-    e2e = rays / wall_e2e / 1e6
+    iters = [i for i, _ in info]
+    conv = sum(1 for _, c in info if c)
 
-    # roofline of the dominant kernel (dvr_march): compulsory bytes per launch =
-    # touched bricks * B^3 * bytes + W*H * (4 RGBA + 20 state read + 20 state write)
-    frame(args.warmup + 2 * args.steps, False, [torch.cuda.Event(enable_timing=True) for _ in range(4)])
+    # Roofline of the dominant kernel on a converged view: full work per launch.
+    last = spec(args.warmup + 2 * args.steps - 1)
+    ev = []
+    for _ in range(5):
+        views, bufs = S.views(last)
+        with torch.cuda.stream(S.stream):
+            bufs[0][1].zero_()
+            bufs[0][2].zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(S.stream)
+            S.cm.render(views[0], S.sp)
+            e1.record(S.stream)
+            ev.append((e0, e1))
+            S.cm.update(S.sp)
     torch.cuda.synchronize()
-    touched = cm.stats().last_used
-    algo_bytes = touched * cfg["B"] ** 3 * vol.encoded_bytes + W * H * 44
-    avg_render_s = statistics.mean(rend_dev) / 1e3
+    touched = S.cm.stats().last_used
+    render_ms = statistics.median([a.elapsed_time(b) for a, b in ev])
+    algo = touched * cfg["B"] ** 3 * vol.encoded_bytes + W * H * PIXEL_BYTES
     peak, peak_kind = measured_peak()
-    achieved = algo_bytes / avg_render_s / 1e9
-    gather = None
+    achieved = algo / (render_ms / 1e3) / 1e9
 
     out = {
-        "metric": "Mrays/s", "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(1e3 * wall_dev / args.steps, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u16" if cfg["bpc"] == 2 else "u8",
-        "data": "synthetic (seeded blobs + value noise, benchmark-config shapes)",
-        "config": {"workload": f"{args.config}: plain per-view out-of-core frame loop", "volume": list(cfg["size"]),
-                   "bytes_per_voxel": cfg["bpc"], "brick_size": cfg["B"], "covering": cfg["c"],
-                   "pool_slots": list(pool), "view": [W, H], "frames_in_path": cfg["frames"],
-                   "max_requests": args.max_requests, "loader": "async", "l2": "pool and page directory > L2",
+        "metric": "Mrays/s", "value": round(rays / wall / 1e6, 3), "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * wall / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
+        "data": "synthetic (seeded blobs + value noise, 2048^3 u16; no public dataset)",
+        "config": {"workload": "c2: 2048^3 u16 out-of-core, plain per-view path, 1024^2 views along a 120-view "
+                               "fly-through, each rendered to convergence",
+                   "brick_size": cfg["B"], "covering": cfg["c"], "pool_slots": list(S.pool), "pool_gib": 2,
+                   "view": [W, H], "max_requests": args.max_requests, "loader": "sync",
+                   "l2": "inputs > L2 (2 GiB pool, 103 MB page directory, 28 GiB host brick store)",
                    "preprocess_s": round(prep_s, 2)},
-        "latency_ms": {"p50": round(statistics.median(lat_dev), 4),
-                       "p99": round(float(np.percentile(lat_dev, 99)), 4)},
-        "e2e": {"value": round(e2e, 3), "unit": "Mrays/s",
+        "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+        "iterations_per_view": {"mean": round(statistics.mean(iters), 2), "max": max(iters)},
+        "converged_views": f"{conv}/{args.steps}",
+        "e2e": {"value": round(rays / wall_e / 1e6, 3), "unit": "Mrays/s",
                 "h2d_bytes_per_step": int((s2.bytes_h2d - s1.bytes_h2d) / args.steps) + 700,
-                "d2h_bytes_per_step": W * H * 4,
-                "latency_ms": {"p50": round(statistics.median(lat_e2e), 4),
-                               "p99": round(float(np.percentile(lat_e2e, 99)), 4)}},
+                "d2h_bytes_per_step": W * H * 4, "latency_ms": {"p50": pct(lat_e, 50), "p99": pct(lat_e, 99)}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 5), "traffic": None,
-                     "kernel": "render_kernel (dvr_march)", "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": int(algo_bytes), "avg_launch_ms": round(avg_render_s * 1e3, 4),
-                     "touched_bricks": int(touched)},
-        "gpu_launches": int(launches_dev),
+                     "frac": round(achieved / peak, 5), "traffic": None, "kernel": "render_kernel (dvr_march)",
+                     "peak_kind": peak_kind, "algorithmic_bytes_per_launch": int(algo),
+                     "launch_ms": round(render_ms, 4), "touched_bricks": int(touched),
+                     "note": "converged 1024^2 view of c2; compulsory bytes = touched bricks x B^3 x 2 B + 44 B/pixel"},
+        "gpu_launches": int(launches),
         "cache": {"bricks_installed": int(s1.bricks_installed - s0.bricks_installed),
-                  "requests_raised": int(s1.requests_raised - s0.requests_raised),
                   "brick_h2d_bytes": int(s1.bytes_h2d - s0.bytes_h2d), "device_error": int(s2.device_error)},
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(gc, cm, cfg, vol, layout, store, offs, tf, args)
+        out["cpu_baseline"] = cpu_baseline(gc, S, cfg, spec(args.warmup + 2 * args.steps - 1), args)
+    S.close()
+    del store
+    if rank == 0 and not args.no_batched:
+        out["batched"] = run_batched(gc, torch, args)
     if rank == 0:
         print(json.dumps(out), flush=True)
-    cm.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
-def cpu_baseline(gc, cm, cfg, vol, layout, store, offs, tf, args):
-    """The oracle's FP32 ray-march (all host threads) on a bounded sample of the
-    same frames, reading a snapshot of the GPU's cache state."""
+def run_batched(gc, torch, args):
+    """c3: the same views rendered batched (64 per persistent launch) and plain
+    (one per launch), each on a fresh cache, to convergence."""
+    cfg = CONFIGS["c3"]
+    vol, layout, store, offs, prep_s = make_store(gc, torch, cfg)
+    nb = args.batches
+    specs = [batch_views(gc, cfg, 100 + b, cfg["batch"]) for b in range(nb + 1)]
+    res = {}
+    for form in ("batched", "plain"):
+        S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
+        if form == "batched":
+            S.converge(specs[nb], cap=args.batch_cap)  # warm-up batch (not timed)
+            wall, lat, info = timed(torch, S.stream, lambda i: S.converge(specs[i], cap=args.batch_cap), nb)
+            rays = sum(W * H for b in specs[:nb] for _, W, H in b)
+            conv = sum(1 for _, c in info if c)
+            res[form] = {"value": round(rays / wall / 1e6, 3), "batch_latency_ms": {"p50": pct(lat, 50),
+                                                                                    "p99": pct(lat, 99)},
+                         "iterations_per_batch": [i for i, _ in info], "converged_batches": f"{conv}/{nb}"}
+        else:
+            flat = [v for b in specs[:nb] for v in b]
+            S.converge([specs[nb][0]])
+            wall, lat, info = timed(torch, S.stream, lambda i: S.converge([flat[i]]), len(flat))
+            rays = sum(W * H for _, W, H in flat)
+            res[form] = {"value": round(rays / wall / 1e6, 3), "view_latency_ms": {"p50": pct(lat, 50),
+                                                                                   "p99": pct(lat, 99)},
+                         "converged_views": f"{sum(1 for _, c in info if c)}/{len(flat)}"}
+        st = S.cm.stats()
+        res[form]["device_error"] = int(st.device_error)
+        S.close()
+    return {"config": {"workload": f"c3: {nb} batches of {cfg['batch']} views, sizes {list(cfg['sizes'])}, "
+                                   f"cameras at 0.5-3.0x diagonal; BrickSize 32, 4 GiB pool",
+                       "preprocess_s": round(prep_s, 2), "rays_per_batch_mean": int(
+                           np.mean([sum(W * H for _, W, H in b) for b in specs[:nb]]))},
+            "unit": "Mrays/s", "batched": res["batched"], "plain_same_views": res["plain"],
+            "ratio": round(res["batched"]["value"] / res["plain"]["value"], 3)}
+
+
+def cpu_baseline(gc, S, cfg, spec, args):
+    """The oracle's FP32 ray-march (all host threads) on a bounded sample of
+    converged c2 views, reading a snapshot of the GPU's cache state."""
     from oracle import oracle as orc
 
-    W, H = cfg["W"], cfg["H"]
-    oc = orc.Cache(cm.desc)
-    cm.dump(gc.DUMP_MRPD, oc.mrpd())
-    cm.dump(gc.DUMP_POOL, oc.pool())
-    tf_np = tf.cpu().numpy()
-    focal = 1.0 / math.tan(math.radians(cfg["fov"]) / 2)
+    (m, W, H), = spec
+    oc = orc.Cache(S.cm.desc)
+    S.cm.dump(gc.DUMP_MRPD, oc.mrpd())
+    S.cm.dump(gc.DUMP_POOL, oc.pool())
+    tf_np = S.tf.cpu().numpy()
     rgba = np.zeros(W * H, np.uint32)
     tb = np.zeros(W * H, np.float32)
     st = np.zeros(W * H * 4, np.float32)
+    v = gc.make_view(m, W, H, 0, 256, 0, 0, 0, tstep=2.0 / 256.0, focal=S.focal, early_alpha=cfg["early"])
     frames = 0
     t0 = time.perf_counter()
     while True:
-        v = gc.make_view(camera(gc, cfg, frames), W, H, 0, 256, 0, 0, 0, focal=focal, early_alpha=cfg["early"])
         tb[:] = 0
         st[:] = 0
         oc.render(v, tf_np, rgba, tb, st)
         frames += 1
         el = time.perf_counter() - t0
-        if el > args.cpu_seconds or frames >= cfg["frames"]:
+        if el > args.cpu_seconds:
             break
     oc.close()
     return {"value": round(W * H * frames / el / 1e6, 4), "unit": "Mrays/s", "cores": os.cpu_count(),
-            "kind": "port", "sample": f"{frames} frames of {W}x{H} on the GPU's converged-so-far cache state "
-                                      f"(FP32 ray-march of the oracle, {os.cpu_count()} threads)"}
+            "kind": "port", "sample": f"{frames} renders of one converged {W}x{H} c2 view from the GPU's cache "
+                                      f"snapshot (oracle FP32 ray-march, {os.cpu_count()} threads)"}
 
 
-def run_reference(args, cfg):
-    """CPU port of the whole frame loop (render + cache update) on the host."""
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+def run_reference(args):
+    """CPU port of the plain path: each view rendered to convergence by the
+    oracle's ray-march + cache state machine on the host cores."""
+    if int(os.environ.get("RANK", "0")) != 0:
         return
     import torch
 
     import gcgb300 as gc
     from oracle import oracle as orc
 
-    # inputs: the same brick store (built on the device; bytes identical to the
-    # oracle's own mip + bricker, see tests/test_gpu_preprocess.py)
-    vol, layout, store, offs, cm, pool, prep_s = build_scene(gc, torch, cfg, args.max_requests, sync=True)
-    oc = orc.Cache(cm.desc)
-    cm.close()
+    cfg = CONFIGS[args.config]
+    # inputs: the brick store (built on the device; bytes identical to the
+    # oracle's own mip + bricker, tests/test_gpu_preprocess.py)
+    vol, layout, store, offs, prep_s = make_store(gc, torch, cfg)
+    pool = cfg["pool_slots"] or gc.pool_dims(vol, cfg["pool_bytes"])
+    desc = gc.CacheDesc(vol, layout, gc.u3(pool), args.max_requests, gc.CACHE_SYNC_LOADER, 0)
+    oc = orc.Cache(desc)
     st_np = store.numpy()
     oc.set_source(st_np, offs)
     W, H = cfg["W"], cfg["H"]
@@ -338,33 +471,37 @@ def run_reference(args, cfg):
     tb = np.zeros(W * H, np.float32)
     st = np.zeros(W * H * 4, np.float32)
 
-    def frame(f):
-        v = gc.make_view(camera(gc, cfg, f), W, H, 0, 256, 0, 0, 0, focal=focal, early_alpha=cfg["early"])
+    def view_to_convergence(f):
+        v = gc.make_view(path_camera(gc, cfg, f), W, H, 0, 256, 0, 0, 0, tstep=2.0 / 256.0, focal=focal,
+                         early_alpha=cfg["early"])
         tb[:] = 0
         st[:] = 0
-        oc.render(v, tf, rgba, tb, st)
-        oc.update()
+        for it in range(64):
+            oc.render(v, tf, rgba, tb, st)
+            if oc.update():
+                return it + 1
 
     for f in range(args.warmup):
-        frame(f)
+        view_to_convergence(f)
     lat = []
     t0 = time.perf_counter()
     for i in range(args.steps):
         a = time.perf_counter()
-        frame(args.warmup + i)
+        view_to_convergence(args.warmup + i)
         lat.append(1e3 * (time.perf_counter() - a))
     el = time.perf_counter() - t0
     value = W * H * args.steps / el / 1e6
     out = {"impl": "reference", "metric": "Mrays/s", "value": round(value, 4), "unit": "Mrays/s", "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * el / args.steps, 3),
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "u16" if cfg["bpc"] == 2 else "u8", "data": "synthetic",
-           "config": {"workload": f"{args.config}: plain per-view out-of-core frame loop on host cores",
-                      "volume": list(cfg["size"]), "view": [W, H], "max_requests": args.max_requests},
-           "latency_ms": {"p50": round(statistics.median(lat), 3), "p99": round(float(np.percentile(lat, 99)), 3)},
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
+           "data": "synthetic (seeded blobs + value noise, 2048^3 u16; no public dataset)",
+           "config": {"workload": "c2: 2048^3 u16 out-of-core, plain per-view path, 1024^2 views along a 120-view "
+                                  "fly-through, each rendered to convergence (CPU port on host cores)",
+                      "view": [W, H], "max_requests": args.max_requests, "pool_slots": list(pool)},
+           "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
-                            "sample": f"{args.steps} frames of {W}x{H}: oracle FP32 ray-march + cache update, "
-                                      f"{os.cpu_count()} threads"},
+                            "sample": f"{args.steps} views after {args.warmup} warm-up views: oracle FP32 "
+                                      f"ray-march + cache update, {os.cpu_count()} threads"},
            "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
     oc.close()
@@ -374,23 +511,25 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None)
-    ap.add_argument("--warmup", type=int, default=None)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=sorted(CONFIGS), default="c2")
+    ap.add_argument("--config", choices=["c1", "c2"], default="c2")
     ap.add_argument("--max-requests", type=int, default=8192)
+    ap.add_argument("--batches", type=int, default=3)
+    ap.add_argument("--batch-cap", type=int, default=48)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
-    cfg = CONFIGS[args.config]
     if args.steps is None:
-        args.steps = cfg["frames"] if args.impl == "ours" else 3
-    if args.warmup is None:
-        args.warmup = 3
+        args.steps = 40 if args.impl == "ours" else 2
     args.warmup = max(3, args.warmup)
+    if args.config != "c2":
+        args.no_batched = True
     if args.impl == "reference":
-        run_reference(args, cfg)
+        run_reference(args)
     else:
-        run_ours(args, cfg)
+        run_ours(args)
 
 
 if __name__ == "__main__":
