@@ -292,23 +292,25 @@ def run_ours(args):
         dist.init_process_group("nccl")
     cfg = CONFIGS[args.config]
     vol, layout, store, offs, prep_s = make_store(gc, torch, cfg)
-    S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
     W, H = cfg["W"], cfg["H"]
     spec = lambda f: [(path_camera(gc, cfg, f, rank), W, H)]  # noqa: E731
 
-    for f in range(args.warmup):
-        S.converge(spec(f))
-    s0, l0 = S.cm.stats(), gc.kernel_launches()
+    def plain_pass(e2e):
+        """Fresh cache; warm-up views, then the timed views (same views for value and e2e)."""
+        S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
+        for f in range(args.warmup):
+            S.converge(spec(f))
+        s0, l0 = S.cm.stats(), gc.kernel_launches()
+        wall, lat, info = timed(torch, S.stream, lambda i: S.converge(spec(args.warmup + i), e2e=e2e), args.steps)
+        launches = gc.kernel_launches() - l0
+        s1 = S.cm.stats()
+        return S, wall, lat, info, launches, s0, s1
+
     clocks = ClockSampler()
     clocks.start()
-    rev = []
-    wall, lat, info = timed(torch, S.stream, lambda i: S.converge(spec(args.warmup + i), render_events=rev),
-                            args.steps)
-    launches = gc.kernel_launches() - l0
-    s1 = S.cm.stats()
-    wall_e, lat_e, _ = timed(torch, S.stream, lambda i: S.converge(spec(args.warmup + args.steps + i), e2e=True),
-                             args.steps)
-    s2 = S.cm.stats()
+    S_e, wall_e, lat_e, _, _, s0_e, s1_e = plain_pass(True)
+    S_e.close()
+    S, wall, lat, info, launches, s0, s1 = plain_pass(False)
     clk = clocks.stop()
     if world > 1:
         t = torch.tensor([wall, wall_e], device="cuda")
@@ -319,7 +321,7 @@ def run_ours(args):
     conv = sum(1 for _, c in info if c)
 
     # Roofline of the dominant kernel on a converged view: full work per launch.
-    last = spec(args.warmup + 2 * args.steps - 1)
+    last = spec(args.warmup + args.steps - 1)
     ev = []
     for _ in range(5):
         views, bufs = S.views(last)
@@ -354,7 +356,7 @@ def run_ours(args):
         "iterations_per_view": {"mean": round(statistics.mean(iters), 2), "max": max(iters)},
         "converged_views": f"{conv}/{args.steps}",
         "e2e": {"value": round(rays / wall_e / 1e6, 3), "unit": "Mrays/s",
-                "h2d_bytes_per_step": int((s2.bytes_h2d - s1.bytes_h2d) / args.steps) + 700,
+                "h2d_bytes_per_step": int((s1_e.bytes_h2d - s0_e.bytes_h2d) / args.steps) + 700,
                 "d2h_bytes_per_step": W * H * 4, "latency_ms": {"p50": pct(lat_e, 50), "p99": pct(lat_e, 99)}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 5), "traffic": None, "kernel": "render_kernel (dvr_march)",
@@ -363,11 +365,11 @@ def run_ours(args):
                      "note": "converged 1024^2 view of c2; compulsory bytes = touched bricks x B^3 x 2 B + 44 B/pixel"},
         "gpu_launches": int(launches),
         "cache": {"bricks_installed": int(s1.bricks_installed - s0.bricks_installed),
-                  "brick_h2d_bytes": int(s1.bytes_h2d - s0.bytes_h2d), "device_error": int(s2.device_error)},
+                  "brick_h2d_bytes": int(s1.bytes_h2d - s0.bytes_h2d), "device_error": int(s1.device_error)},
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(gc, S, cfg, spec(args.warmup + 2 * args.steps - 1), args)
+        out["cpu_baseline"] = cpu_baseline(gc, S, cfg, last, args)
     S.close()
     del store
     if rank == 0 and not args.no_batched:
@@ -379,38 +381,62 @@ def run_ours(args):
 
 
 def run_batched(gc, torch, args):
-    """c3: the same views rendered batched (64 per persistent launch) and plain
-    (one per launch), each on a fresh cache, to convergence."""
+    """c3: the same views rendered batched (continuous batching, all active
+    views in one persistent launch per tick) and plain (one view per launch,
+    to convergence), each on a fresh cache."""
     cfg = CONFIGS["c3"]
     vol, layout, store, offs, prep_s = make_store(gc, torch, cfg)
     nb = args.batches
-    specs = [batch_views(gc, cfg, 100 + b, cfg["batch"]) for b in range(nb + 1)]
+    views = [v for b in range(nb) for v in batch_views(gc, cfg, 100 + b, cfg["batch"])]
+    warm = batch_views(gc, cfg, 99, 8)
+    rays = sum(W * H for _, W, H in views)
     res = {}
-    for form in ("batched", "plain"):
-        S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
-        if form == "batched":
-            S.converge(specs[nb], cap=args.batch_cap)  # warm-up batch (not timed)
-            wall, lat, info = timed(torch, S.stream, lambda i: S.converge(specs[i], cap=args.batch_cap), nb)
-            rays = sum(W * H for b in specs[:nb] for _, W, H in b)
-            conv = sum(1 for _, c in info if c)
-            res[form] = {"value": round(rays / wall / 1e6, 3), "batch_latency_ms": {"p50": pct(lat, 50),
-                                                                                    "p99": pct(lat, 99)},
-                         "iterations_per_batch": [i for i, _ in info], "converged_batches": f"{conv}/{nb}"}
-        else:
-            flat = [v for b in specs[:nb] for v in b]
-            S.converge([specs[nb][0]])
-            wall, lat, info = timed(torch, S.stream, lambda i: S.converge([flat[i]]), len(flat))
-            rays = sum(W * H for _, W, H in flat)
-            res[form] = {"value": round(rays / wall / 1e6, 3), "view_latency_ms": {"p50": pct(lat, 50),
-                                                                                   "p99": pct(lat, 99)},
-                         "converged_views": f"{sum(1 for _, c in info if c)}/{len(flat)}"}
-        st = S.cm.stats()
-        res[form]["device_error"] = int(st.device_error)
-        S.close()
-    return {"config": {"workload": f"c3: {nb} batches of {cfg['batch']} views, sizes {list(cfg['sizes'])}, "
-                                   f"cameras at 0.5-3.0x diagonal; BrickSize 32, 4 GiB pool",
-                       "preprocess_s": round(prep_s, 2), "rays_per_batch_mean": int(
-                           np.mean([sum(W * H for _, W, H in b) for b in specs[:nb]]))},
+
+    # batched
+    S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
+    B = gc.Batch(S.cm, max_views=cfg["batch"], max_pixels=args.batch_pixels, max_passes=args.batch_cap)
+
+    def run_all(vs, base):
+        for i, (m, W, H) in enumerate(vs):
+            b = S.buffers(base + i, W, H)
+            B.submit(gc.make_view(m, W, H, S.tf.data_ptr(), 256, b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr(),
+                                  tstep=2.0 / 256.0, focal=S.focal, early_alpha=cfg["early"]), base + i)
+        out, ticks = [], 0
+        while len(out) < len(vs):
+            B.tick(S.sp)
+            out += B.poll()
+            ticks += 1
+        return out, ticks
+
+    run_all(warm, 10000)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out, ticks = run_all(views, 0)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    lat = [r[3] for r in out]
+    res["batched"] = {"value": round(rays / wall / 1e6, 3), "wall_s": round(wall, 4), "ticks": ticks,
+                      "view_latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+                      "passes_per_view": round(statistics.mean(r[1] for r in out), 2),
+                      "converged_views": f"{sum(1 for r in out if r[2])}/{len(views)}",
+                      "device_error": int(S.cm.stats().device_error)}
+    B.close()
+    S.close()
+
+    # plain on the same views
+    S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
+    for i, v in enumerate(warm):
+        S.converge([v], cap=args.batch_cap)
+    wall, lat, info = timed(torch, S.stream, lambda i: S.converge([views[i]], cap=args.batch_cap), len(views))
+    res["plain"] = {"value": round(rays / wall / 1e6, 3), "wall_s": round(wall, 4),
+                    "view_latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+                    "converged_views": f"{sum(1 for _, c in info if c)}/{len(views)}",
+                    "device_error": int(S.cm.stats().device_error)}
+    S.close()
+    return {"config": {"workload": f"c3: {len(views)} views ({nb} x {cfg['batch']}), sizes {list(cfg['sizes'])}, "
+                                   f"cameras at 0.5-3.0x diagonal; BrickSize 32, 4 GiB pool; all submitted at t0, "
+                                   f"continuous batching with a {args.batch_pixels} pixel admission budget",
+                       "preprocess_s": round(prep_s, 2), "rays": int(rays)},
             "unit": "Mrays/s", "batched": res["batched"], "plain_same_views": res["plain"],
             "ratio": round(res["batched"]["value"] / res["plain"]["value"], 3)}
 
@@ -516,7 +542,8 @@ def main():
     ap.add_argument("--config", choices=["c1", "c2"], default="c2")
     ap.add_argument("--max-requests", type=int, default=8192)
     ap.add_argument("--batches", type=int, default=3)
-    ap.add_argument("--batch-cap", type=int, default=48)
+    ap.add_argument("--batch-cap", type=int, default=256)
+    ap.add_argument("--batch-pixels", type=int, default=16 << 20)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")

@@ -52,6 +52,7 @@ struct ViewParams {
     uint32_t *rgba;
     float *tbuf;
     float *state;
+    uint32_t *status;                   // optional per-view "met an unmapped brick" word
     // LOD tables (display_volume_raycaster, VolumeRayCaster.cu:146-161)
     float inv_size[GC_MAX_LEVELS][3];   // bboxSizeMin / initial level size
     float step[GC_MAX_LEVELS];          // LODStepSize

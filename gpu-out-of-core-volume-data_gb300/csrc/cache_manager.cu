@@ -148,6 +148,11 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     uint32_t n_nonempty = 0, nbig = 0;
     std::vector<uint32_t> big_index;
     big_index.reserve(n);
+    struct Copy {
+        const uint8_t *src;
+        uint8_t *dst;
+    };
+    std::vector<Copy> copies;
     for (uint32_t i = 0; i < n; ++i) {
         const uint4 b = C->h_list[i];
         const uint32_t gx = b.x / BB[0], gy = b.y / BB[1], gz = b.z / BB[2];
@@ -174,8 +179,8 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
                 gz < L.nb_big_bricks[b.w][2]) {
                 const uint64_t idx =
                     (static_cast<uint64_t>(gz) * L.nb_big_bricks[b.w][1] + gy) * L.nb_big_bricks[b.w][0] + gx;
-                std::memcpy(C->h_staging + static_cast<uint64_t>(nbig) * C->big_bytes,
-                            C->src.host + C->src.level_off[b.w] + idx * C->big_bytes, C->big_bytes);
+                copies.push_back({C->src.host + C->src.level_off[b.w] + idx * C->big_bytes,
+                                  C->h_staging + static_cast<uint64_t>(nbig) * C->big_bytes});
                 status = GC_BRICK_SUCCESS;
             }
         } else if (C->src.kind == 2) {
@@ -198,6 +203,25 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
             asked[key] = -2;
             kind[i] = 2;
             C->stats.load_errors++;
+        }
+    }
+    // Host-store bricks are copied into the pinned staging buffer by up to 8
+    // threads (one memcpy stream saturates well below the host's bandwidth).
+    if (!copies.empty()) {
+        const size_t bytes = copies.size() * C->big_bytes;
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const unsigned nt = static_cast<unsigned>(
+            std::min<size_t>(std::min(8u, hw), std::max<size_t>(1, bytes >> 21)));  // >= 2 MiB per thread
+        auto work = [&](unsigned t) {
+            for (size_t i = t; i < copies.size(); i += nt) std::memcpy(copies[i].dst, copies[i].src, C->big_bytes);
+        };
+        if (nt <= 1) {
+            work(0);
+        } else {
+            std::vector<std::thread> pool;
+            for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work, t);
+            work(0);
+            for (auto &th : pool) th.join();
         }
     }
     // stable partition: non-empty first, then empty (RequestHandler.hpp:354-369)
@@ -428,6 +452,7 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
     out.rgba = in.rgba;
     out.tbuf = in.tbuf;
     out.state = in.state;
+    out.status = in.status;
     const float bsx = in.bbox_max[0] - in.bbox_min[0];
     const float bsy = in.bbox_max[1] - in.bbox_min[1];
     const float bsz = in.bbox_max[2] - in.bbox_min[2];
@@ -732,6 +757,147 @@ int gc_render_batch(gc_cache_t C, const gc_view *views, uint32_t n, void *stream
     return guard([&] {
         GC_REQUIRE(C && views, "null argument");
         render(C, views, n, as_stream(stream));
+    });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Continuous batching (gc_batch_*).
+#include <chrono>
+#include <deque>
+
+struct gc_batch {
+    gc_cache *cache = nullptr;
+    gc_batch_desc d;
+    struct Item {
+        gc_view view;
+        uint64_t tag;
+        uint32_t passes;
+        std::chrono::steady_clock::time_point submitted;
+    };
+    std::deque<Item> queue;
+    std::vector<Item> active;
+    std::deque<gc_batch_result> done;
+    uint32_t *d_status = nullptr;
+    uint32_t *h_status = nullptr;
+    cudaEvent_t ev = nullptr;
+};
+
+namespace gc {
+static void batch_destroy(gc_batch *b) {
+    if (!b) return;
+    if (b->d_status) cudaFree(b->d_status);
+    if (b->h_status) cudaFreeHost(b->h_status);
+    if (b->ev) cudaEventDestroy(b->ev);
+    delete b;
+}
+}  // namespace gc
+
+extern "C" {
+
+int gc_batch_create(gc_cache_t C, const gc_batch_desc *desc, gc_batch_t *out) {
+    gc_batch *b = nullptr;
+    int rc = guard([&] {
+        GC_REQUIRE(C && desc && out, "null argument");
+        GC_REQUIRE(desc->max_views >= 1 && desc->max_views <= C->max_views, "max_views must be in [1, 256]");
+        GC_REQUIRE(desc->max_pixels >= 1, "max_pixels must be >= 1");
+        GC_CUDA(cudaSetDevice(C->device));
+        b = new gc_batch();
+        b->cache = C;
+        b->d = *desc;
+        b->d_status = dalloc<uint32_t>(desc->max_views, "batch status");
+        b->h_status = halloc<uint32_t>(desc->max_views);
+        GC_CUDA(cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming));
+        *out = b;
+    });
+    if (rc != GC_OK) batch_destroy(b);
+    return rc;
+}
+
+int gc_batch_destroy(gc_batch_t b) {
+    batch_destroy(b);
+    return GC_OK;
+}
+
+int gc_batch_submit(gc_batch_t b, const gc_view *view, uint64_t tag) {
+    return guard([&] {
+        GC_REQUIRE(b && view, "null argument");
+        ViewParams check;
+        fill_view(b->cache, *view, check);  // validates the view now, not at admission
+        b->queue.push_back({*view, tag, 0, std::chrono::steady_clock::now()});
+    });
+}
+
+int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_queued) {
+    return guard([&] {
+        GC_REQUIRE(b, "null batch");
+        gc_cache *C = b->cache;
+        GC_REQUIRE(C->src.kind != 0, "no brick source set");
+        GC_CUDA(cudaSetDevice(C->device));
+        cudaStream_t s = as_stream(stream);
+        // admission: views in arrival order while the budgets allow (at least one)
+        uint64_t pixels = 0;
+        for (auto &it : b->active) pixels += static_cast<uint64_t>(it.view.width) * it.view.height;
+        while (!b->queue.empty() && b->active.size() < b->d.max_views) {
+            const gc_view &v = b->queue.front().view;
+            const uint64_t px = static_cast<uint64_t>(v.width) * v.height;
+            if (!b->active.empty() && pixels + px > b->d.max_pixels) break;
+            GC_CUDA(cudaMemsetAsync(v.tbuf, 0, px * sizeof(float), s));
+            GC_CUDA(cudaMemsetAsync(v.state, 0, px * 4 * sizeof(float), s));
+            pixels += px;
+            b->active.push_back(b->queue.front());
+            b->queue.pop_front();
+        }
+        const uint32_t n = static_cast<uint32_t>(b->active.size());
+        if (n_active) *n_active = n;
+        if (n == 0) {
+            if (n_queued) *n_queued = static_cast<uint32_t>(b->queue.size());
+            return;
+        }
+        std::vector<gc_view> views(n);
+        for (uint32_t i = 0; i < n; ++i) {
+            views[i] = b->active[i].view;
+            views[i].status = b->d_status + i;
+        }
+        GC_CUDA(cudaMemsetAsync(b->d_status, 0, n * sizeof(uint32_t), s));
+        render(C, views.data(), n, s);
+        GC_CUDA(cudaMemcpyAsync(b->h_status, b->d_status, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        GC_CUDA(cudaEventRecord(b->ev, s));
+        update(C, s);
+        GC_CUDA(cudaEventSynchronize(b->ev));
+        const auto now = std::chrono::steady_clock::now();
+        std::vector<gc_batch::Item> keep;
+        keep.reserve(n);
+        for (uint32_t i = 0; i < n; ++i) {
+            auto &it = b->active[i];
+            it.passes++;
+            const bool conv = (b->h_status[i] & 1u) == 0;
+            if (conv || (b->d.max_passes && it.passes >= b->d.max_passes)) {
+                gc_batch_result r;
+                r.tag = it.tag;
+                r.passes = it.passes;
+                r.converged = conv ? 1u : 0u;
+                r.latency_ms = std::chrono::duration<double, std::milli>(now - it.submitted).count();
+                b->done.push_back(r);
+            } else {
+                keep.push_back(it);
+            }
+        }
+        b->active.swap(keep);
+        if (n_queued) *n_queued = static_cast<uint32_t>(b->queue.size());
+    });
+}
+
+int gc_batch_poll(gc_batch_t b, gc_batch_result *out, uint32_t max, uint32_t *n) {
+    return guard([&] {
+        GC_REQUIRE(b && n && (out || max == 0), "null argument");
+        uint32_t k = 0;
+        while (k < max && !b->done.empty()) {
+            out[k++] = b->done.front();
+            b->done.pop_front();
+        }
+        *n = k;
     });
 }
 

@@ -251,8 +251,9 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
     return kEmpty;
 }
 
+// Returns true when the ray stopped at an unmapped brick.
 template <typename T>
-__device__ void march(const CacheView &cv, const LevelTables &lt, const ViewParams &vp, uint32_t x, uint32_t y) {
+__device__ bool march(const CacheView &cv, const LevelTables &lt, const ViewParams &vp, uint32_t x, uint32_t y) {
     const uint32_t W = vp.W, H = vp.H;
     uint32_t xN = x + 1;
     if (xN > W) xN = x - 1;
@@ -290,6 +291,7 @@ __device__ void march(const CacheView &cv, const LevelTables &lt, const ViewPara
     tnear = fmaxf(tnear, vp.tbuf[i]);
     float4 *state = reinterpret_cast<float4 *>(vp.state);
     const bool dvr = vp.mode == GC_MODE_DVR;
+    bool unmapped = false;
     float4 fc = dvr ? state[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     if (!hit) {
         fc.x = 0.f;
@@ -376,6 +378,7 @@ __device__ void march(const CacheView &cv, const LevelTables &lt, const ViewPara
             else
                 vp.state[4 * i] = maxOp;
         }
+        unmapped = unm;
         if (!dvr) fc = tf_lookup(vp.tf, vp.tfw, maxOp);
     }
     const uint32_t R = static_cast<uint32_t>(saturate(fc.x) * 255.0f);
@@ -383,6 +386,7 @@ __device__ void march(const CacheView &cv, const LevelTables &lt, const ViewPara
     const uint32_t Bc = static_cast<uint32_t>(saturate(fc.z) * 255.0f);
     const uint32_t A = static_cast<uint32_t>(saturate(fc.w) * 255.0f);
     vp.rgba[i] = (A << 24) | (Bc << 16) | (G << 8) | R;
+    return unmapped;
 }
 
 template <typename T>
@@ -412,7 +416,10 @@ __global__ void __launch_bounds__(kRenderThreads) render_kernel(const CacheView 
         const uint32_t local = t - vp.tile_begin;
         const uint32_t ty = local / vp.tiles_x, tx = local - ty * vp.tiles_x;
         const uint32_t x = tx * 8 + (lane & 7u), y = ty * 4 + (lane >> 3);
-        if (x < vp.W && y < vp.H) march<T>(cv, lt, vp, x, y);
+        bool unm = false;
+        if (x < vp.W && y < vp.H) unm = march<T>(cv, lt, vp, x, y);
+        const uint32_t any = __ballot_sync(0xffffffffu, unm);
+        if (any && lane == 0 && vp.status) atomicOr(vp.status, 1u);
     }
     if (lane == 0) {
         __threadfence();

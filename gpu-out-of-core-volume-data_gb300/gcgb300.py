@@ -76,7 +76,15 @@ class View(C.Structure):
                 ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3), ("tstep", C.c_float),
                 ("focal", C.c_float), ("early_alpha", C.c_float), ("mode", C.c_uint32), ("sampler", C.c_uint32),
                 ("tf_width", C.c_uint32), ("tf", C.c_void_p), ("rgba", C.c_void_p), ("tbuf", C.c_void_p),
-                ("state", C.c_void_p)]
+                ("state", C.c_void_p), ("status", C.c_void_p)]
+
+
+class BatchDesc(C.Structure):
+    _fields_ = [("max_views", C.c_uint32), ("max_pixels", C.c_uint64), ("max_passes", C.c_uint32)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("tag", C.c_uint64), ("passes", C.c_uint32), ("converged", C.c_uint32), ("latency_ms", C.c_double)]
 
 
 class TfPoint(C.Structure):
@@ -115,6 +123,9 @@ _SIGS = {
     "gc_look_at": [P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_float)],
     "gc_tf_build": [P(TfPoint), C.c_uint32, C.c_uint32, P(C.c_float)],
     "gc_render": [vp, P(View), vp], "gc_render_batch": [vp, P(View), C.c_uint32, vp],
+    "gc_batch_create": [vp, P(BatchDesc), P(vp)], "gc_batch_destroy": [vp],
+    "gc_batch_submit": [vp, P(View), C.c_uint64], "gc_batch_tick": [vp, vp, P(C.c_uint32), P(C.c_uint32)],
+    "gc_batch_poll": [vp, P(BatchResult), C.c_uint32, P(C.c_uint32)],
 }
 _RESTYPES = {"gc_last_error": C.c_char_p, "gc_version": C.c_char_p, "gc_brick_key": C.c_uint64,
              "gc_kernel_launches": C.c_uint64}
@@ -354,10 +365,10 @@ class TransferFunction:
 
 def make_view(inv_view, width, height, tf_ptr, tf_width, rgba_ptr, tbuf_ptr, state_ptr, tstep=2.0 / 256.0,
               focal=2.0, early_alpha=0.95, mode=MODE_DVR, sampler=SAMPLER_REFERENCE,
-              bbox_min=(-1.0, -1.0, -1.0), bbox_max=(1.0, 1.0, 1.0)):
+              bbox_min=(-1.0, -1.0, -1.0), bbox_max=(1.0, 1.0, 1.0), status_ptr=0):
     return View((C.c_float * 12)(*inv_view), width, height, (C.c_float * 3)(*bbox_min), (C.c_float * 3)(*bbox_max),
                 tstep, focal, early_alpha, mode, sampler, tf_width, vp(tf_ptr), vp(rgba_ptr), vp(tbuf_ptr),
-                vp(state_ptr))
+                vp(state_ptr), vp(status_ptr or None))
 
 
 # ---------------------------------------------------------------------------
@@ -437,6 +448,38 @@ class CacheManager:
     def close(self):
         if getattr(self, "_h", None):
             lib.gc_cache_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Batch:
+    """Continuous batching of views over one cache (gc_batch_*)."""
+
+    def __init__(self, cache, max_views=64, max_pixels=1 << 24, max_passes=0):
+        self.cache = cache
+        self._h = vp()
+        check(lib.gc_batch_create(cache.handle, C.byref(BatchDesc(max_views, max_pixels, max_passes)),
+                                  C.byref(self._h)))
+
+    def submit(self, view, tag):
+        check(lib.gc_batch_submit(self._h, C.byref(view), int(tag)))
+
+    def tick(self, stream=0):
+        a, q = C.c_uint32(), C.c_uint32()
+        check(lib.gc_batch_tick(self._h, vp(stream), C.byref(a), C.byref(q)))
+        return a.value, q.value
+
+    def poll(self, max_results=4096):
+        arr = (BatchResult * max_results)()
+        n = C.c_uint32()
+        check(lib.gc_batch_poll(self._h, arr, max_results, C.byref(n)))
+        return [(r.tag, r.passes, bool(r.converged), r.latency_ms) for r in arr[: n.value]]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.gc_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -290,6 +290,10 @@ typedef struct gc_view {
     uint32_t *rgba;           /* device: width*height RGBA8 (R in low byte)    */
     float *tbuf;              /* device: width*height progressive t            */
     float *state;             /* device: width*height float4 colour state      */
+    uint32_t *status;         /* optional device word: bit 0 is set when a ray
+                                 of this view met an unmapped brick in this
+                                 pass (the view is not converged); the caller
+                                 clears it before the pass                      */
 } gc_view;
 
 /* Camera of updateViewMatrix (Display_helper.cpp:93-118): the rows of
@@ -312,6 +316,37 @@ int gc_render(gc_cache_t cache, const gc_view *view, void *stream);
 /* Many views of uneven sizes in one persistent launch sharing the cache's
  * request buffer (one frame for the cache). */
 int gc_render_batch(gc_cache_t cache, const gc_view *views, uint32_t n, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Continuous batching of views over one cache (the batched and served forms;
+ * no counterpart in the reference, whose frame loop renders one view per
+ * launch, VolumeRayCaster.cu:261-330).  Views are queued with their own
+ * buffers; each tick admits queued views within the budgets, renders every
+ * active view in one persistent launch sharing the cache's miss list, runs one
+ * cache update, and retires the views none of whose rays met an unmapped brick
+ * in that pass (or that reached max_passes).  A retired view's buffers hold its
+ * final image. */
+typedef struct gc_batch *gc_batch_t;
+typedef struct gc_batch_desc {
+    uint32_t max_views;      /* active views per launch (<= 256)              */
+    uint64_t max_pixels;     /* admission budget: sum of W*H of active views  */
+    uint32_t max_passes;     /* retire unconverged after this many passes (0: never) */
+} gc_batch_desc;
+typedef struct gc_batch_result {
+    uint64_t tag;
+    uint32_t passes;         /* render passes the view took                   */
+    uint32_t converged;      /* 1 if its last pass met no unmapped brick      */
+    double latency_ms;       /* submit -> retirement, host clock              */
+} gc_batch_result;
+int gc_batch_create(gc_cache_t cache, const gc_batch_desc *desc, gc_batch_t *out);
+int gc_batch_destroy(gc_batch_t batch);
+/* Queue a view; its tbuf and state are cleared when it is admitted.  The
+ * view's status field is managed by the batch. */
+int gc_batch_submit(gc_batch_t batch, const gc_view *view, uint64_t tag);
+/* One tick.  Outputs (optional): views active during the tick, views queued after it. */
+int gc_batch_tick(gc_batch_t batch, void *stream, uint32_t *active, uint32_t *queued);
+/* Retrieve up to max retired views (oldest first). */
+int gc_batch_poll(gc_batch_t batch, gc_batch_result *out, uint32_t max, uint32_t *n);
 
 #ifdef __cplusplus
 }

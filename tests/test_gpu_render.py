@@ -5,6 +5,8 @@ Tolerances (per RGBA channel, in 1/255 units):
   CUDA vs FP32 oracle : 0   (same operation sequence; cache state bit-exact)
   CUDA vs FP64 oracle : 1   (the double-precision restatement of the method)
 """
+import time
+
 import numpy as np
 import pytest
 
@@ -174,13 +176,19 @@ def test_async_loader_converges_to_same_image(gc, orc, torch_cuda):
         g, _ = s.buffers(96, 80)
         v = s.view(scenario.orbit_camera(gc, 2, 12, 3.0), 96, 80, tf_dev, 256, g)
         conv = False
-        for f in range(200):
+        # the loader runs on its own thread: bound the loop by wall time, not frames
+        t_end = time.time() + 20.0
+        f = 0
+        while time.time() < t_end:
             for x in g:
                 x.zero_()
             s.cm.render(v)
             conv = s.cm.update()
-            if conv and f > 2:
+            f += 1
+            if conv and f > 3:
                 break
+            torch_cuda.cuda.synchronize()
+            time.sleep(0.001)
         assert conv
         for x in g:
             x.zero_()
@@ -189,3 +197,51 @@ def test_async_loader_converges_to_same_image(gc, orc, torch_cuda):
         imgs.append(g[0].cpu().numpy())
         s.cm.close()
     assert np.array_equal(imgs[0], imgs[1])
+
+
+def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda):
+    """Continuous batching (admission by pixel budget, one persistent launch
+    per tick, retirement on convergence) gives every view the image it gets
+    when rendered alone to convergence; the per-view status word reports
+    convergence exactly."""
+    specs = [((64, 48), 1), ((33, 17), 4), ((96, 80), 7), ((40, 40), 10), ((80, 24), 5)]
+    tf = scenario.ramp_tf()
+    single = []
+    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 64)
+    tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
+    status = torch_cuda.zeros(1, dtype=torch_cuda.int32, device="cuda")
+    for (W, H), cam in specs:
+        g, _ = s.buffers(W, H)
+        v = s.view(scenario.orbit_camera(gc, cam, 12, 3.0), W, H, tf_dev, 256, g)
+        v.status = status.data_ptr()
+        for it in range(64):
+            status.zero_()
+            s.cm.render(v)
+            s.cm.update()
+            if int(status.item()) == 0:
+                break
+        assert int(status.item()) == 0
+        single.append(g[0].cpu().numpy())
+    s.cm.close()
+
+    s2 = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 64)
+    b = gc.Batch(s2.cm, max_views=3, max_pixels=96 * 80 + 64 * 48)
+    bufs = []
+    for i, ((W, H), cam) in enumerate(specs):
+        g, _ = s2.buffers(W, H)
+        bufs.append(g)
+        b.submit(s2.view(scenario.orbit_camera(gc, cam, 12, 3.0), W, H, tf_dev, 256, g), tag=100 + i)
+    results = []
+    for tick in range(400):
+        active, queued = b.tick()
+        assert active <= 3
+        results += b.poll()
+        if len(results) == len(specs):
+            break
+    assert sorted(r[0] for r in results) == [100 + i for i in range(len(specs))]
+    assert all(r[2] for r in results)
+    torch_cuda.cuda.synchronize()
+    for i in range(len(specs)):
+        assert np.array_equal(bufs[i][0].cpu().numpy(), single[i]), i
+    b.close()
+    assert s2.cm.stats().device_error == 0
