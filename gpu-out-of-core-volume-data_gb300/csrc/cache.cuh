@@ -57,7 +57,8 @@ struct ViewParams {
     float inv_size[GC_MAX_LEVELS][3];   // bboxSizeMin / initial level size
     float step[GC_MAX_LEVELS];          // LODStepSize
     float kexp[GC_MAX_LEVELS];          // LODStepSize / tstep (opacity correction exponent)
-    uint32_t tiles_x;                   // 8x4 warp tiles per row
+    uint32_t tiles_x;                   // warp tiles per row
+    uint32_t tile_shift;                // log2 of the tile width
     uint32_t tile_begin;                // first global tile index of this view
 };
 
@@ -103,7 +104,16 @@ struct InstallArgs {
 void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s);
 void launch_completude(const float4 *slot_vpos, uint32_t nslots, uint32_t *count, cudaStream_t s);
 
-// Ray caster (render.cu).
+// Ray caster (render.cu).  Launch configuration of the ray caster, process
+// wide: scheduler 0 = one 8x4 tile per warp, 1 = per-lane pixel refill;
+// threads per block; blocks per SM cap (0 = occupancy limit).
+struct RenderTuning {
+    uint32_t scheduler = 1;
+    uint32_t threads = 128;
+    uint32_t blocks_per_sm = 0;
+    uint32_t tile_w = 8;  // ray tile of one warp: tile_w x (32 / tile_w) pixels
+};
+RenderTuning &render_tuning();
 void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams *views_dev,
                    const ViewParams *views_host, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
                    uint32_t *err, cudaStream_t s);

@@ -464,7 +464,9 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
         out.step[l] = (bmin / static_cast<float>(mn)) / 2.f;
         out.kexp[l] = out.step[l] / in.tstep;
     }
-    out.tiles_x = div_up(in.width, 8);
+    const uint32_t tw = render_tuning().tile_w;
+    out.tiles_x = div_up(in.width, tw);
+    out.tile_shift = static_cast<uint32_t>(__builtin_ctz(tw));
 }
 
 static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s) {
@@ -477,7 +479,7 @@ static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s
     for (uint32_t i = 0; i < n; ++i) {
         fill_view(C, views[i], vp[i]);
         vp[i].tile_begin = tiles;
-        tiles += vp[i].tiles_x * div_up(views[i].height, 4);
+        tiles += vp[i].tiles_x * div_up(views[i].height, 32u >> vp[i].tile_shift);
     }
     // pageable source: the call returns once the data is staged
     GC_CUDA(cudaMemcpyAsync(C->d_views, vp.data(), n * sizeof(ViewParams), cudaMemcpyHostToDevice, s));
@@ -780,7 +782,8 @@ struct gc_batch {
     std::vector<Item> active;
     std::deque<gc_batch_result> done;
     uint32_t *d_status = nullptr;
-    uint32_t *h_status = nullptr;
+    uint32_t *h_status = nullptr;   // [max_views] status words + [1] used slots
+    uint32_t last_used = 0;
     cudaEvent_t ev = nullptr;
 };
 
@@ -807,7 +810,7 @@ int gc_batch_create(gc_cache_t C, const gc_batch_desc *desc, gc_batch_t *out) {
         b->cache = C;
         b->d = *desc;
         b->d_status = dalloc<uint32_t>(desc->max_views, "batch status");
-        b->h_status = halloc<uint32_t>(desc->max_views);
+        b->h_status = halloc<uint32_t>(desc->max_views + 1);
         GC_CUDA(cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming));
         *out = b;
     });
@@ -836,13 +839,21 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         GC_REQUIRE(C->src.kind != 0, "no brick source set");
         GC_CUDA(cudaSetDevice(C->device));
         cudaStream_t s = as_stream(stream);
-        // admission: views in arrival order while the budgets allow (at least one)
+        // admission: views in arrival order while the budgets allow (at least
+        // one active view); by cache memory: no admission while the last tick
+        // used more than max_occupancy of the pool slots
         uint64_t pixels = 0;
         for (auto &it : b->active) pixels += static_cast<uint64_t>(it.view.width) * it.view.height;
+        const bool occ_ok = b->d.max_occupancy <= 0.f ||
+                            static_cast<double>(b->last_used) <= b->d.max_occupancy * static_cast<double>(C->nslots);
+        uint32_t admitted = 0;
         while (!b->queue.empty() && b->active.size() < b->d.max_views) {
             const gc_view &v = b->queue.front().view;
             const uint64_t px = static_cast<uint64_t>(v.width) * v.height;
-            if (!b->active.empty() && pixels + px > b->d.max_pixels) break;
+            if (!b->active.empty() &&
+                (pixels + px > b->d.max_pixels || !occ_ok || (b->d.max_admit && admitted >= b->d.max_admit)))
+                break;
+            ++admitted;
             GC_CUDA(cudaMemsetAsync(v.tbuf, 0, px * sizeof(float), s));
             GC_CUDA(cudaMemsetAsync(v.state, 0, px * 4 * sizeof(float), s));
             pixels += px;
@@ -863,9 +874,12 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         GC_CUDA(cudaMemsetAsync(b->d_status, 0, n * sizeof(uint32_t), s));
         render(C, views.data(), n, s);
         GC_CUDA(cudaMemcpyAsync(b->h_status, b->d_status, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        GC_CUDA(cudaEventRecord(b->ev, s));
         update(C, s);
+        GC_CUDA(cudaMemcpyAsync(b->h_status + b->d.max_views, C->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                s));
+        GC_CUDA(cudaEventRecord(b->ev, s));
         GC_CUDA(cudaEventSynchronize(b->ev));
+        b->last_used = b->h_status[b->d.max_views];
         const auto now = std::chrono::steady_clock::now();
         std::vector<gc_batch::Item> keep;
         keep.reserve(n);

@@ -33,7 +33,6 @@
 
 namespace gc {
 
-constexpr uint32_t kRenderThreads = 128;
 
 struct V3 {
     float x, y, z;
@@ -251,9 +250,25 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
     return kEmpty;
 }
 
-// Returns true when the ray stopped at an unmapped brick.
+// Per-ray state between samples.  The method is split into ray_setup /
+// ray_step / ray_finish so that both schedulers below run the same code.
+struct Ray {
+    const ViewParams *vp;
+    uint32_t i;
+    V3 pos, dir, dirLeft, dirUp;
+    float t, tfar, endX, endY, sL, sU, maxOp;
+    float4 fc;
+    uint32_t lod;
+    Walk w;
+    bool unm, dvr;
+};
+
+// Eye ray, box intersection and progressive resume.  Returns false when the
+// ray has nothing to march (the pixel is then already written).
 template <typename T>
-__device__ bool march(const CacheView &cv, const LevelTables &lt, const ViewParams &vp, uint32_t x, uint32_t y) {
+__device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParams *vpp, uint32_t x, uint32_t y,
+                                          Ray &r) {
+    const ViewParams &vp = *vpp;
     const uint32_t W = vp.W, H = vp.H;
     uint32_t xN = x + 1;
     if (xN > W) xN = x - 1;
@@ -289,139 +304,146 @@ __device__ bool march(const CacheView &cv, const LevelTables &lt, const ViewPara
 
     const uint32_t i = y * W + x;
     tnear = fmaxf(tnear, vp.tbuf[i]);
-    float4 *state = reinterpret_cast<float4 *>(vp.state);
-    const bool dvr = vp.mode == GC_MODE_DVR;
-    bool unmapped = false;
-    float4 fc = dvr ? state[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 *state = reinterpret_cast<const float4 *>(vp.state);
+    r.vp = vpp;
+    r.i = i;
+    r.dvr = vp.mode == GC_MODE_DVR;
+    r.unm = false;
+    r.fc = r.dvr ? state[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     if (!hit) {
-        fc.x = 0.f;
-        fc.y = 0.f;
-        fc.z = 0.f;
-    } else {
-        if (tnear < 0.f) tnear = 0.f;
-        float t = tnear;
-        V3 pos = origin + dir * tnear;
-        const float endX = fabsf(dot(dir - dirXN, dirLeft) * tfar);
-        const float endY = fabsf(dot(dir - dirYN, dirUp) * tfar);
-        const uint32_t nl = lt.nlevels;
-        uint32_t lod = 0;
-        float sL = 0.f, sU = 0.f;  // spacings of level lod + 1
-        if (nl > 1) {
-            const V3 n1 = v3(vp.inv_size[1][0], vp.inv_size[1][1], vp.inv_size[1][2]);
-            sL = length(dirLeft * n1);
-            sU = length(dirUp * n1);
-        }
-        Walk w;
-        w.pcx = w.pcy = w.pcz = UINT_MAX;
-        w.entry = make_uint4(0, 0, 0, 0);
-        bool unm = false;
-        float maxOp = dvr ? 0.f : state[i].x;
-        while ((!dvr || fc.w < vp.early) && t < tfar) {
-            const float alpha = t / tfar;
-            const float pX = endX * alpha;
-            const float pY = endY * alpha;
-            V3 tp = pos * 0.495f + v3(0.495f, 0.495f, 0.495f);
-            tp.z = 1.0f - tp.z;
-            const V3 np = v3(clampf(tp.x, 0.f, 0.99f), clampf(tp.y, 0.f, 0.99f), clampf(tp.z, 0.f, 0.99f));
-            // compute_LOD: the level only grows along a ray because the pixel
-            // footprint grows with t, so the scan resumes at the current level.
-            while (lod + 1 < nl && !(sL >= pX || sU >= pY)) {
-                ++lod;
-                if (lod + 1 < nl) {
-                    const V3 nn = v3(vp.inv_size[lod + 1][0], vp.inv_size[lod + 1][1], vp.inv_size[lod + 1][2]);
-                    sL = length(dirLeft * nn);
-                    sU = length(dirUp * nn);
-                }
-            }
-            float sample = 0.f;
-            const int st = fetch<T>(cv, lt, vp.sampler, lod, np, w, sample);
-            if (st != kMapped) {
-                if (st == kUnmapped) {
-                    if (!unm) {
-                        vp.tbuf[i] = t;
-                        if (dvr)
-                            state[i] = fc;
-                        else
-                            vp.state[4 * i] = maxOp;
-                    }
-                    unm = true;
-                    break;
-                }
-                t += vp.tstep;
-                if (t > tfar) break;
-                pos = pos + dir * vp.tstep;
-                continue;
-            }
-            if (dvr) {
-                float4 col = tf_lookup(vp.tf, vp.tfw, sample);
-                col.w = 1.0f - gc_pow(1.0f - col.w, vp.kexp[lod]);
-                if (col.w > 0.001f) {
-                    col.x *= col.w;
-                    col.y *= col.w;
-                    col.z *= col.w;
-                    const float r = 1.0f - fc.w;
-                    fc.x = fc.x + col.x * r;
-                    fc.y = fc.y + col.y * r;
-                    fc.z = fc.z + col.z * r;
-                    fc.w = fc.w + col.w * r;
-                }
-            } else {
-                maxOp = fmaxf(maxOp, sample);
-            }
-            t += vp.step[lod];
-            pos = pos + dir * vp.step[lod];
-        }
-        if (!unm) {
-            vp.tbuf[i] = t;
-            if (dvr)
-                state[i] = fc;
-            else
-                vp.state[4 * i] = maxOp;
-        }
-        unmapped = unm;
-        if (!dvr) fc = tf_lookup(vp.tf, vp.tfw, maxOp);
+        r.fc.x = 0.f;
+        r.fc.y = 0.f;
+        r.fc.z = 0.f;
+        const float4 fc = r.fc;
+        const uint32_t R = static_cast<uint32_t>(saturate(fc.x) * 255.0f);
+        const uint32_t G = static_cast<uint32_t>(saturate(fc.y) * 255.0f);
+        const uint32_t Bc = static_cast<uint32_t>(saturate(fc.z) * 255.0f);
+        const uint32_t A = static_cast<uint32_t>(saturate(fc.w) * 255.0f);
+        vp.rgba[i] = (A << 24) | (Bc << 16) | (G << 8) | R;
+        return false;
     }
+    if (tnear < 0.f) tnear = 0.f;
+    r.t = tnear;
+    r.tfar = tfar;
+    r.pos = origin + dir * tnear;
+    r.dir = dir;
+    r.dirLeft = dirLeft;
+    r.dirUp = dirUp;
+    r.endX = fabsf(dot(dir - dirXN, dirLeft) * tfar);
+    r.endY = fabsf(dot(dir - dirYN, dirUp) * tfar);
+    r.lod = 0;
+    r.sL = 0.f;  // spacings of level lod + 1
+    r.sU = 0.f;
+    if (lt.nlevels > 1) {
+        const V3 n1 = v3(vp.inv_size[1][0], vp.inv_size[1][1], vp.inv_size[1][2]);
+        r.sL = length(dirLeft * n1);
+        r.sU = length(dirUp * n1);
+    }
+    r.w.pcx = r.w.pcy = r.w.pcz = UINT_MAX;
+    r.w.entry = make_uint4(0, 0, 0, 0);
+    r.maxOp = r.dvr ? 0.f : vp.state[4 * i];
+    return true;
+}
+
+// One iteration of the march loop (RayCasters.cu:122-188).  Returns false
+// when the loop ends.
+template <typename T>
+__device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables &lt, Ray &r) {
+    const ViewParams &vp = *r.vp;
+    if (!((!r.dvr || r.fc.w < vp.early) && r.t < r.tfar)) return false;
+    const float alpha = r.t / r.tfar;
+    const float pX = r.endX * alpha;
+    const float pY = r.endY * alpha;
+    V3 tp = r.pos * 0.495f + v3(0.495f, 0.495f, 0.495f);
+    tp.z = 1.0f - tp.z;
+    const V3 np = v3(clampf(tp.x, 0.f, 0.99f), clampf(tp.y, 0.f, 0.99f), clampf(tp.z, 0.f, 0.99f));
+    // compute_LOD: the level only grows along a ray because the pixel
+    // footprint grows with t, so the scan resumes at the current level.
+    const uint32_t nl = lt.nlevels;
+    while (r.lod + 1 < nl && !(r.sL >= pX || r.sU >= pY)) {
+        ++r.lod;
+        if (r.lod + 1 < nl) {
+            const V3 nn = v3(vp.inv_size[r.lod + 1][0], vp.inv_size[r.lod + 1][1], vp.inv_size[r.lod + 1][2]);
+            r.sL = length(r.dirLeft * nn);
+            r.sU = length(r.dirUp * nn);
+        }
+    }
+    const uint32_t lod = r.lod;
+    float sample = 0.f;
+    const int st = fetch<T>(cv, lt, vp.sampler, lod, np, r.w, sample);
+    if (st != kMapped) {
+        if (st == kUnmapped) {
+            vp.tbuf[r.i] = r.t;
+            if (r.dvr)
+                reinterpret_cast<float4 *>(vp.state)[r.i] = r.fc;
+            else
+                vp.state[4 * r.i] = r.maxOp;
+            r.unm = true;
+            return false;
+        }
+        r.t += vp.tstep;
+        if (r.t > r.tfar) return false;
+        r.pos = r.pos + r.dir * vp.tstep;
+        return true;
+    }
+    if (r.dvr) {
+        float4 col = tf_lookup(vp.tf, vp.tfw, sample);
+        col.w = 1.0f - gc_pow(1.0f - col.w, vp.kexp[lod]);
+        if (col.w > 0.001f) {
+            col.x *= col.w;
+            col.y *= col.w;
+            col.z *= col.w;
+            const float rr = 1.0f - r.fc.w;
+            r.fc.x = r.fc.x + col.x * rr;
+            r.fc.y = r.fc.y + col.y * rr;
+            r.fc.z = r.fc.z + col.z * rr;
+            r.fc.w = r.fc.w + col.w * rr;
+        }
+    } else {
+        r.maxOp = fmaxf(r.maxOp, sample);
+    }
+    r.t += vp.step[lod];
+    r.pos = r.pos + r.dir * vp.step[lod];
+    return true;
+}
+
+// Progressive state, MIP classification and the truncating RGBA8 pack
+// (RayCasters.cu:189-197, 528-536).  Returns true when the ray stopped at an
+// unmapped brick.
+__device__ __forceinline__ bool ray_finish(Ray &r) {
+    const ViewParams &vp = *r.vp;
+    if (!r.unm) {
+        vp.tbuf[r.i] = r.t;
+        if (r.dvr)
+            reinterpret_cast<float4 *>(vp.state)[r.i] = r.fc;
+        else
+            vp.state[4 * r.i] = r.maxOp;
+    }
+    float4 fc = r.fc;
+    if (!r.dvr) fc = tf_lookup(vp.tf, vp.tfw, r.maxOp);
     const uint32_t R = static_cast<uint32_t>(saturate(fc.x) * 255.0f);
     const uint32_t G = static_cast<uint32_t>(saturate(fc.y) * 255.0f);
     const uint32_t Bc = static_cast<uint32_t>(saturate(fc.z) * 255.0f);
     const uint32_t A = static_cast<uint32_t>(saturate(fc.w) * 255.0f);
-    vp.rgba[i] = (A << 24) | (Bc << 16) | (G << 8) | R;
-    return unmapped;
+    vp.rgba[r.i] = (A << 24) | (Bc << 16) | (G << 8) | R;
+    return r.unm;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kRenderThreads) render_kernel(const CacheView cv, const LevelTables lt,
-                                                                const ViewParams *__restrict__ views,
-                                                                uint32_t nviews, uint32_t total_tiles,
-                                                                uint32_t *queue, uint32_t nwarps) {
-    const uint32_t lane = threadIdx.x & 31u;
-    for (;;) {
-        uint32_t t = 0;
-        if (lane == 0) t = atomicAdd(queue, 1u);
-        t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= total_tiles) break;
-        uint32_t v = 0;
-        {
-            uint32_t lo = 0, hi = nviews - 1;
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi + 1) >> 1;
-                if (views[mid].tile_begin <= t)
-                    lo = mid;
-                else
-                    hi = mid - 1;
-            }
-            v = lo;
-        }
-        const ViewParams &vp = views[v];
-        const uint32_t local = t - vp.tile_begin;
-        const uint32_t ty = local / vp.tiles_x, tx = local - ty * vp.tiles_x;
-        const uint32_t x = tx * 8 + (lane & 7u), y = ty * 4 + (lane >> 3);
-        bool unm = false;
-        if (x < vp.W && y < vp.H) unm = march<T>(cv, lt, vp, x, y);
-        const uint32_t any = __ballot_sync(0xffffffffu, unm);
-        if (any && lane == 0 && vp.status) atomicOr(vp.status, 1u);
+__device__ __forceinline__ uint32_t find_view(const ViewParams *__restrict__ views, uint32_t nviews, uint32_t t) {
+    uint32_t lo = 0, hi = nviews - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (views[mid].tile_begin <= t)
+            lo = mid;
+        else
+            hi = mid - 1;
     }
-    if (lane == 0) {
+    return lo;
+}
+
+// The last warp of a launch resets the work queue for the next launch.
+__device__ __forceinline__ void retire_warp(uint32_t *queue, uint32_t nwarps) {
+    if ((threadIdx.x & 31u) == 0) {
         __threadfence();
         if (atomicAdd(queue + 1, 1u) == nwarps - 1) {
             queue[0] = 0;
@@ -431,29 +453,150 @@ __global__ void __launch_bounds__(kRenderThreads) render_kernel(const CacheView 
     }
 }
 
+// Tile scheduler: a warp takes one tile (tile_w x 32/tile_w pixels) at a time
+// from the queue and marches its 32 rays to completion.
+template <typename T>
+__global__ void __launch_bounds__(256) render_kernel(const CacheView cv, const LevelTables lt,
+                                                     const ViewParams *__restrict__ views, uint32_t nviews,
+                                                     uint32_t total_tiles, uint32_t *queue, uint32_t nwarps) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(queue, 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= total_tiles) break;
+        const ViewParams *vp = views + find_view(views, nviews, t);
+        const uint32_t local = t - vp->tile_begin;
+        const uint32_t ty = local / vp->tiles_x, tx = local - ty * vp->tiles_x;
+        const uint32_t sh = vp->tile_shift, tw = 1u << sh;
+        const uint32_t x = (tx << sh) + (lane & (tw - 1u)), y = ty * (32u >> sh) + (lane >> sh);
+        bool unm = false;
+        if (x < vp->W && y < vp->H) {
+            Ray r;
+            if (ray_setup<T>(lt, vp, x, y, r)) {
+                while (ray_step<T>(cv, lt, r)) {
+                }
+                unm = ray_finish(r);
+            }
+        }
+        const uint32_t any = __ballot_sync(0xffffffffu, unm);
+        if (any && lane == 0 && vp->status) atomicOr(vp->status, 1u);
+    }
+    retire_warp(queue, nwarps);
+}
+
+// Pixel scheduler: every lane keeps its own ray; lanes whose ray ended take
+// the next pixels of the queue (one warp-aggregated atomic), so a warp never
+// waits for its slowest ray.  Pixels are enumerated tile by tile, which keeps
+// consecutive grabs spatially close.
+template <typename T>
+__global__ void __launch_bounds__(256) render_pixels_kernel(const CacheView cv, const LevelTables lt,
+                                                            const ViewParams *__restrict__ views, uint32_t nviews,
+                                                            uint32_t total_tiles, uint32_t *queue, uint32_t nwarps) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t total = total_tiles * 32u;
+    Ray r;
+    bool active = false, exhausted = false;
+    for (;;) {
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (idle && !exhausted) {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (static_cast<int>(lane) == leader) base = atomicAdd(queue, static_cast<uint32_t>(__popc(idle)));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base >= total) exhausted = true;
+            if (!active) {
+                const uint32_t p = base + __popc(idle & ((1u << lane) - 1u));
+                if (p < total) {
+                    const uint32_t t = p >> 5, k = p & 31u;
+                    const ViewParams *vp = views + find_view(views, nviews, t);
+                    const uint32_t local = t - vp->tile_begin;
+                    const uint32_t ty = local / vp->tiles_x, tx = local - ty * vp->tiles_x;
+                    const uint32_t sh = vp->tile_shift, tw = 1u << sh;
+                    const uint32_t x = (tx << sh) + (k & (tw - 1u)), y = ty * (32u >> sh) + (k >> sh);
+                    if (x < vp->W && y < vp->H) active = ray_setup<T>(lt, vp, x, y, r);
+                }
+            }
+        }
+        if (active && !ray_step<T>(cv, lt, r)) {
+            active = false;
+            if (ray_finish(r) && r.vp->status && *r.vp->status == 0u) atomicOr(r.vp->status, 1u);
+        }
+        if (exhausted && !__any_sync(0xffffffffu, active)) break;
+    }
+    retire_warp(queue, nwarps);
+}
+
+RenderTuning &render_tuning() {
+    static RenderTuning t;
+    return t;
+}
+
+}  // namespace gc
+
+extern "C" {
+int gc_render_tuning_set(uint32_t scheduler, uint32_t tile_w, uint32_t threads, uint32_t blocks_per_sm) {
+    return gc::guard([&] {
+        GC_REQUIRE(scheduler <= 1, "scheduler must be 0 (tile) or 1 (pixel)");
+        GC_REQUIRE(tile_w == 4 || tile_w == 8 || tile_w == 16 || tile_w == 32, "tile width must be 4, 8, 16 or 32");
+        GC_REQUIRE(threads == 64 || threads == 128 || threads == 256, "threads must be 64, 128 or 256");
+        gc::RenderTuning &t = gc::render_tuning();
+        t.scheduler = scheduler;
+        t.tile_w = tile_w;
+        t.threads = threads;
+        t.blocks_per_sm = blocks_per_sm;
+    });
+}
+int gc_render_tuning_get(uint32_t out[4]) {
+    return gc::guard([&] {
+        GC_REQUIRE(out, "null argument");
+        const gc::RenderTuning &t = gc::render_tuning();
+        out[0] = t.scheduler;
+        out[1] = t.tile_w;
+        out[2] = t.threads;
+        out[3] = t.blocks_per_sm;
+    });
+}
+}  // extern "C"
+
+namespace gc {
+
 void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams *views_dev,
                    const ViewParams * /*views_host*/, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
                    uint32_t * /*err*/, cudaStream_t s) {
     if (total_tiles == 0) return;
-    static int blocks_per_sm[3] = {0, 0, 0};
-    auto launch = [&](auto kernel, int slot) {
-        if (!blocks_per_sm[slot]) {
+    const RenderTuning tune = render_tuning();
+    const uint32_t threads = tune.threads;
+    GC_REQUIRE(threads == 64 || threads == 128 || threads == 256, "render threads must be 64, 128 or 256");
+    static int occupancy[2][3][3] = {};
+    const int tslot = threads == 64 ? 0 : (threads == 128 ? 1 : 2);
+    auto launch = [&](auto kernel, int sched, int slot) {
+        int &occ = occupancy[sched][slot][tslot];
+        if (!occ) {
             int b = 0;
-            GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kRenderThreads, 0));
-            blocks_per_sm[slot] = std::max(1, b);
+            GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, static_cast<int>(threads), 0));
+            occ = std::max(1, b);
         }
-        const uint32_t max_blocks = static_cast<uint32_t>(sm_count() * blocks_per_sm[slot]);
-        const uint32_t want = div_up(total_tiles, kRenderThreads / 32);
+        int per_sm = occ;
+        if (tune.blocks_per_sm > 0) per_sm = std::min(per_sm, static_cast<int>(tune.blocks_per_sm));
+        const uint32_t max_blocks = static_cast<uint32_t>(sm_count() * per_sm);
+        const uint32_t want = div_up(total_tiles, threads / 32);
         const uint32_t grid = std::max(1u, std::min(max_blocks, want));
-        kernel<<<grid, kRenderThreads, 0, s>>>(cv, lt, views_dev, nviews, total_tiles, queue,
-                                               grid * (kRenderThreads / 32));
+        kernel<<<grid, threads, 0, s>>>(cv, lt, views_dev, nviews, total_tiles, queue, grid * (threads / 32));
         GC_CUDA(cudaGetLastError());
         count_launch();
     };
+    const bool pix = tune.scheduler == 1;
     switch (cv.eb) {
-        case 1: launch(render_kernel<uint8_t>, 0); break;
-        case 2: launch(render_kernel<uint16_t>, 1); break;
-        case 4: launch(render_kernel<float>, 2); break;
+        case 1:
+            pix ? launch(render_pixels_kernel<uint8_t>, 1, 0) : launch(render_kernel<uint8_t>, 0, 0);
+            break;
+        case 2:
+            pix ? launch(render_pixels_kernel<uint16_t>, 1, 1) : launch(render_kernel<uint16_t>, 0, 1);
+            break;
+        case 4:
+            pix ? launch(render_pixels_kernel<float>, 1, 2) : launch(render_kernel<float>, 0, 2);
+            break;
         default: fail(GC_ERR_UNSUPPORTED, "the ray caster supports one channel of 1, 2 or 4 bytes");
     }
 }

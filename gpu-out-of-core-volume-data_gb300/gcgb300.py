@@ -80,7 +80,8 @@ class View(C.Structure):
 
 
 class BatchDesc(C.Structure):
-    _fields_ = [("max_views", C.c_uint32), ("max_pixels", C.c_uint64), ("max_passes", C.c_uint32)]
+    _fields_ = [("max_views", C.c_uint32), ("max_pixels", C.c_uint64), ("max_passes", C.c_uint32),
+                ("max_occupancy", C.c_float), ("max_admit", C.c_uint32)]
 
 
 class BatchResult(C.Structure):
@@ -126,6 +127,8 @@ _SIGS = {
     "gc_batch_create": [vp, P(BatchDesc), P(vp)], "gc_batch_destroy": [vp],
     "gc_batch_submit": [vp, P(View), C.c_uint64], "gc_batch_tick": [vp, vp, P(C.c_uint32), P(C.c_uint32)],
     "gc_batch_poll": [vp, P(BatchResult), C.c_uint32, P(C.c_uint32)],
+    "gc_render_tuning_set": [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32],
+    "gc_render_tuning_get": [P(C.c_uint32)],
 }
 _RESTYPES = {"gc_last_error": C.c_char_p, "gc_version": C.c_char_p, "gc_brick_key": C.c_uint64,
              "gc_kernel_launches": C.c_uint64}
@@ -207,6 +210,16 @@ def pool_dims(vol, pool_bytes):
     out = U3()
     check(lib.gc_pool_dims(C.byref(vol), int(pool_bytes), out))
     return tuple(out)
+
+
+def render_tuning(scheduler=None, tile_w=None, threads=None, blocks_per_sm=None):
+    """Reads, and optionally sets, the ray caster's launch configuration."""
+    cur = (C.c_uint32 * 4)()
+    check(lib.gc_render_tuning_get(cur))
+    new = [cur[0] if scheduler is None else scheduler, cur[1] if tile_w is None else tile_w,
+           cur[2] if threads is None else threads, cur[3] if blocks_per_sm is None else blocks_per_sm]
+    check(lib.gc_render_tuning_set(*new))
+    return tuple(new)
 
 
 def kernel_launches():
@@ -457,11 +470,11 @@ class CacheManager:
 class Batch:
     """Continuous batching of views over one cache (gc_batch_*)."""
 
-    def __init__(self, cache, max_views=64, max_pixels=1 << 24, max_passes=0):
+    def __init__(self, cache, max_views=64, max_pixels=1 << 24, max_passes=0, max_occupancy=0.0, max_admit=0):
         self.cache = cache
         self._h = vp()
-        check(lib.gc_batch_create(cache.handle, C.byref(BatchDesc(max_views, max_pixels, max_passes)),
-                                  C.byref(self._h)))
+        d = BatchDesc(max_views, max_pixels, max_passes, max_occupancy, max_admit)
+        check(lib.gc_batch_create(cache.handle, C.byref(d), C.byref(self._h)))
 
     def submit(self, view, tag):
         check(lib.gc_batch_submit(self._h, C.byref(view), int(tag)))
@@ -484,3 +497,61 @@ class Batch:
 
     def __del__(self):
         self.close()
+
+
+AUTOTUNE_CANDIDATES = [(sched, tw, th, bps) for sched in (1, 0) for tw in (8, 4, 16) for th in (128, 64, 256)
+                       for bps in (0, 4)]
+
+
+def autotune_render(cache, views, clear, stream=0, candidates=None, repeats=3, cache_file=None, key=None):
+    """Chooses the ray caster's launch configuration (scheduler, ray-tile
+    shape, threads per block, blocks per SM) by timing `views` (a list of View
+    whose bricks are resident) under each candidate, applies the fastest and
+    returns (best, timings).  `clear()` restarts the views' progressive buffers
+    before each timed render.  With cache_file and key, a previous choice for
+    the same key is reused without timing.  Images do not depend on the choice."""
+    import json
+    import torch
+
+    if cache_file and key and os.path.exists(cache_file):
+        try:
+            with open(cache_file) as f:
+                known = json.load(f)
+            if key in known:
+                best = tuple(known[key]["best"])
+                render_tuning(*best)
+                return best, known[key].get("timings_ms", {})
+        except (OSError, ValueError, KeyError):
+            pass
+    arr = (View * len(views))(*views)
+    s = torch.cuda.ExternalStream(stream) if stream else torch.cuda.current_stream()
+    timings = {}
+    for cand in candidates or AUTOTUNE_CANDIDATES:
+        render_tuning(*cand)
+        ms = []
+        for r in range(repeats + 1):
+            clear()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            check(lib.gc_render_batch(cache.handle, arr, len(views), vp(stream)))
+            b.record(s)
+            b.synchronize()
+            if r:
+                ms.append(a.elapsed_time(b))
+        timings[str(cand)] = sorted(ms)[len(ms) // 2]
+    best = min(timings, key=timings.get)
+    best = tuple(int(x) for x in best.strip("()").split(","))
+    render_tuning(*best)
+    if cache_file and key:
+        try:
+            known = {}
+            if os.path.exists(cache_file):
+                with open(cache_file) as f:
+                    known = json.load(f)
+            known[key] = {"best": list(best), "timings_ms": timings}
+            os.makedirs(os.path.dirname(os.path.abspath(cache_file)), exist_ok=True)
+            with open(cache_file, "w") as f:
+                json.dump(known, f, indent=1)
+        except (OSError, ValueError):
+            pass
+    return best, timings

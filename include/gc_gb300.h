@@ -317,6 +317,15 @@ int gc_render(gc_cache_t cache, const gc_view *view, void *stream);
  * request buffer (one frame for the cache). */
 int gc_render_batch(gc_cache_t cache, const gc_view *views, uint32_t n, void *stream);
 
+/* Launch configuration of the ray caster (process-wide; results do not
+ * depend on it): scheduler 0 = a warp marches one ray tile at a time,
+ * 1 = each lane refills from the pixel queue when its ray ends; tile width
+ * 4, 8, 16 or 32 (a warp tile is tile_w x 32/tile_w pixels); threads per
+ * block 64, 128 or 256; blocks per SM cap (0 = occupancy limit).  Chosen by
+ * the autotuner of the Python host (gcgb300.autotune_render). */
+int gc_render_tuning_set(uint32_t scheduler, uint32_t tile_w, uint32_t threads, uint32_t blocks_per_sm);
+int gc_render_tuning_get(uint32_t out[4]);
+
 /* ------------------------------------------------------------------------ */
 /* Continuous batching of views over one cache (the batched and served forms;
  * no counterpart in the reference, whose frame loop renders one view per
@@ -331,6 +340,10 @@ typedef struct gc_batch_desc {
     uint32_t max_views;      /* active views per launch (<= 256)              */
     uint64_t max_pixels;     /* admission budget: sum of W*H of active views  */
     uint32_t max_passes;     /* retire unconverged after this many passes (0: never) */
+    float max_occupancy;     /* admission by cache memory: no view is admitted
+                                while the last tick used more than this
+                                fraction of the pool slots (<= 0: no limit)    */
+    uint32_t max_admit;      /* views admitted per tick (0: no limit)          */
 } gc_batch_desc;
 typedef struct gc_batch_result {
     uint64_t tag;
