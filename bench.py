@@ -258,6 +258,23 @@ class Session:
         self.cm.close()
 
 
+def autotune(gc, torch, S, specs, args):
+    """Autotunes the ray caster's launch configuration on converged views."""
+    S.converge(specs)
+    views, bufs = S.views(specs)
+
+    def clear():
+        for b in bufs:
+            b[1].zero_()
+            b[2].zero_()
+
+    with torch.cuda.stream(S.stream):
+        best, timings = gc.autotune_render(S.cm, views, clear, stream=S.sp, repeats=3)
+    log(f"autotune: best {best} of {len(timings)} ({min(timings.values()):.3f} ms vs default "
+        f"{timings.get(str((1, 8, 128, 0)), float('nan')):.3f} ms)")
+    return best, timings
+
+
 def timed(torch, stream, fn, steps):
     """Per-step latencies (CUDA events on the launch stream) and wall time."""
     lat, info = [], []
@@ -300,12 +317,15 @@ def run_ours(args):
         S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
         for f in range(args.warmup):
             S.converge(spec(f))
+        if not tuned:
+            tuned.append(autotune(gc, torch, S, spec(args.warmup - 1), args))
         s0, l0 = S.cm.stats(), gc.kernel_launches()
         wall, lat, info = timed(torch, S.stream, lambda i: S.converge(spec(args.warmup + i), e2e=e2e), args.steps)
         launches = gc.kernel_launches() - l0
         s1 = S.cm.stats()
         return S, wall, lat, info, launches, s0, s1
 
+    tuned = []
     clocks = ClockSampler()
     clocks.start()
     S_e, wall_e, lat_e, _, _, s0_e, s1_e = plain_pass(True)
@@ -363,6 +383,8 @@ def run_ours(args):
                      "peak_kind": peak_kind, "algorithmic_bytes_per_launch": int(algo),
                      "launch_ms": round(render_ms, 4), "touched_bricks": int(touched),
                      "note": "converged 1024^2 view of c2; compulsory bytes = touched bricks x B^3 x 2 B + 44 B/pixel"},
+        "render_tuning": {"scheduler_tile_threads_bps": list(tuned[0][0]) if tuned else None,
+                          "candidates_timed": len(tuned[0][1]) if tuned else 0},
         "gpu_launches": int(launches),
         "cache": {"bricks_installed": int(s1.bricks_installed - s0.bricks_installed),
                   "brick_h2d_bytes": int(s1.bytes_h2d - s0.bytes_h2d), "device_error": int(s1.device_error)},
@@ -392,9 +414,10 @@ def run_batched(gc, torch, args):
     rays = sum(W * H for _, W, H in views)
     res = {}
 
-    # batched
-    S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
-    B = gc.Batch(S.cm, max_views=cfg["batch"], max_pixels=args.batch_pixels, max_passes=args.batch_cap)
+    # batched: asynchronous loader, admission by pixel budget and cache occupancy
+    S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests, sync=False)
+    B = gc.Batch(S.cm, max_views=cfg["batch"], max_pixels=args.batch_pixels, max_passes=args.batch_cap,
+                 max_occupancy=args.occupancy, max_admit=args.admit)
 
     def run_all(vs, base):
         for i, (m, W, H) in enumerate(vs):
@@ -435,7 +458,9 @@ def run_batched(gc, torch, args):
     S.close()
     return {"config": {"workload": f"c3: {len(views)} views ({nb} x {cfg['batch']}), sizes {list(cfg['sizes'])}, "
                                    f"cameras at 0.5-3.0x diagonal; BrickSize 32, 4 GiB pool; all submitted at t0, "
-                                   f"continuous batching with a {args.batch_pixels} pixel admission budget",
+                                   f"continuous batching with a {args.batch_pixels} pixel budget, admission "
+                                   f"while the last tick used <= {args.occupancy} of the pool, <= {args.admit} "
+                                   f"admissions per tick, asynchronous loader",
                        "preprocess_s": round(prep_s, 2), "rays": int(rays)},
             "unit": "Mrays/s", "batched": res["batched"], "plain_same_views": res["plain"],
             "ratio": round(res["batched"]["value"] / res["plain"]["value"], 3)}
@@ -544,6 +569,8 @@ def main():
     ap.add_argument("--batches", type=int, default=3)
     ap.add_argument("--batch-cap", type=int, default=256)
     ap.add_argument("--batch-pixels", type=int, default=16 << 20)
+    ap.add_argument("--occupancy", type=float, default=0.6)
+    ap.add_argument("--admit", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
