@@ -19,6 +19,9 @@
 // does the scan, cap and decode in one pass with the same look-back scan.
 // Every look-back wait is bounded; on expiry the kernel sets ScanCtl::err.
 #include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <mutex>
 
 #include "cache.cuh"
 #include "gc_internal.h"
@@ -404,3 +407,88 @@ void launch_completude(const float4 *slot_vpos, uint32_t nslots, uint32_t *count
 }
 
 }  // namespace gc
+
+// ---------------------------------------------------------------------------
+// Miss list without allocation.
+//
+// Some callers cannot allocate device memory at the moment they need the miss
+// list: a host that records its frame into a CUDA graph (memory allocation is
+// not allowed while a stream is being captured), a render loop with a hard
+// frame deadline that must not block in the allocator (cudaMalloc can wait for
+// the device), or a plug-in whose host application owns every byte of device
+// memory and hands it only input and output buffers.  For them the scan's
+// scratch -- one look-back status word per 4096-entry tile and the scan
+// control block -- lives in this file-scope device array instead of memory
+// obtained from cudaMalloc.  Every GPU that loads the library holds it until
+// the process exits.
+namespace gc {
+
+constexpr uint32_t kNoAllocMaxTiles = 2048;  // request buffers of up to 2048 * 4096 entries
+constexpr uint64_t kNoAllocMaxEntries = static_cast<uint64_t>(kNoAllocMaxTiles) * kTile;
+
+// words [0, kNoAllocMaxTiles): look-back status; the last two words: ScanCtl
+constexpr uint32_t kNoAllocWords = kNoAllocMaxTiles + sizeof(ScanCtl) / sizeof(uint64_t);
+static_assert(sizeof(ScanCtl) == 2 * sizeof(uint64_t), "ScanCtl must fill two scratch words");
+static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocWords];  // 16 KiB + 16 B
+
+// Host code cannot use g_noalloc_scratch as a device address (the name is a
+// host-side stand-in); the device address is looked up once per device, with
+// that device current.
+constexpr int kNoAllocMaxDevices = 64;
+static uint64_t *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+static std::mutex g_noalloc_mu;
+
+static uint64_t *noalloc_scratch() {
+    int dev = 0;
+    GC_CUDA(cudaGetDevice(&dev));
+    GC_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, "device index out of range");
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        uint64_t *p = nullptr;
+        GC_CUDA(cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_noalloc_scratch));
+        g_noalloc_ptr[dev] = p;
+    }
+    return g_noalloc_ptr[dev];
+}
+
+}  // namespace gc
+
+extern "C" int gc_miss_list_noalloc(const uint32_t *requests, uint64_t n_entries, uint32_t timestamp,
+                                    const gc_layout *layout, uint32_t max_requests, uint32_t *out_list,
+                                    uint32_t *out_total, void *stream) {
+    using namespace gc;
+    return guard([&] {
+        GC_REQUIRE(requests && layout && out_list && out_total, "null argument");
+        GC_REQUIRE(n_entries >= 2, "the request buffer needs at least 2 entries");
+        GC_REQUIRE(n_entries - 1 <= kNoAllocMaxEntries,
+                   "request buffer too large for the allocation-free scan: at most 8388609 entries "
+                   "(2048 tiles of 4096) are supported");
+        GC_REQUIRE(max_requests >= 1, "max_requests must be >= 1");
+        GC_REQUIRE(layout->nb_levels >= 1 && layout->nb_levels <= GC_MAX_LEVELS, "bad layout");
+        // level tables of the page directory (levels packed along x)
+        LevelTables lt;
+        std::memset(&lt, 0, sizeof(lt));
+        lt.nlevels = layout->nb_levels;
+        uint32_t mx = 0, my = 0, mz = 0;
+        for (uint32_t l = 0; l < layout->nb_levels; ++l) {
+            lt.off[l] = mx;
+            for (int a = 0; a < 3; ++a) lt.nb[l][a] = layout->nb_bricks[l][a];
+            mx += layout->nb_bricks[l][0];
+            my = std::max(my, layout->nb_bricks[l][1]);
+            mz = std::max(mz, layout->nb_bricks[l][2]);
+        }
+        GC_REQUIRE(static_cast<uint64_t>(mx) * my * mz == n_entries,
+                   "n_entries does not match the page directory of the layout");
+        cudaStream_t s = as_stream(stream);
+        uint64_t *status = noalloc_scratch();
+        ScanCtl *ctl = reinterpret_cast<ScanCtl *>(status + kNoAllocMaxTiles);
+        // The scratch keeps the previous call's contents: clear the control block
+        // and the status words this scan uses.
+        GC_CUDA(cudaMemsetAsync(ctl, 0, sizeof(ScanCtl), s));
+        GC_CUDA(cudaMemsetAsync(status, 0, lookback_tiles(n_entries - 1) * sizeof(uint64_t), s));
+        static std::atomic<uint32_t> epoch{0};
+        launch_miss_compact(requests, n_entries - 1, timestamp, max_requests, reinterpret_cast<uint4 *>(out_list),
+                            lt, mx, my, status, ctl, epoch.fetch_add(1) + 1, s);
+        GC_CUDA(cudaMemcpyAsync(out_total, &ctl->total, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+    });
+}

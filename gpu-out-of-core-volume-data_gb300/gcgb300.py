@@ -127,6 +127,7 @@ _SIGS = {
     "gc_batch_create": [vp, P(BatchDesc), P(vp)], "gc_batch_destroy": [vp],
     "gc_batch_submit": [vp, P(View), C.c_uint64], "gc_batch_tick": [vp, vp, P(C.c_uint32), P(C.c_uint32)],
     "gc_batch_poll": [vp, P(BatchResult), C.c_uint32, P(C.c_uint32)],
+    "gc_miss_list_noalloc": [vp, C.c_uint64, C.c_uint32, P(Layout), C.c_uint32, vp, vp, vp],
     "gc_render_tuning_set": [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32],
     "gc_render_tuning_get": [P(C.c_uint32)],
 }
@@ -220,6 +221,15 @@ def render_tuning(scheduler=None, tile_w=None, threads=None, blocks_per_sm=None)
            cur[2] if threads is None else threads, cur[3] if blocks_per_sm is None else blocks_per_sm]
     check(lib.gc_render_tuning_set(*new))
     return tuple(new)
+
+
+def miss_list_noalloc(requests_ptr, n_entries, timestamp, layout, max_requests, out_list_ptr, out_total_ptr,
+                      stream=0):
+    """Miss list of a request buffer without any device allocation (for
+    callers that cannot allocate: stream capture, hard frame deadlines, hosts
+    that own all device memory).  See gc_miss_list_noalloc for the limits."""
+    check(lib.gc_miss_list_noalloc(vp(requests_ptr), int(n_entries), int(timestamp), C.byref(layout),
+                                   int(max_requests), vp(out_list_ptr), vp(out_total_ptr), vp(stream)))
 
 
 def kernel_launches():

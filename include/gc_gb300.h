@@ -267,6 +267,25 @@ int gc_cache_dump(gc_cache_t cache, int what, void *dst, size_t bytes);
  * per brick, CacheManagerKernels.cu:32-72), at most `max` entries; *total is
  * the number of bricks flagged in the scan.  Waits for the scan to finish. */
 int gc_cache_last_misses(gc_cache_t cache, uint32_t *out4, uint32_t max, uint32_t *count, uint32_t *total);
+/* Miss list without device allocation.  No counterpart in the reference.
+ * The same scan, cap and decode as the miss list built inside
+ * gc_cache_update, on a caller's request buffer (device, n_entries uint32 laid
+ * out like the cache's page directory for `layout`): entries with value
+ * `timestamp` in [0, n_entries - 1), the first max_requests of them written
+ * to out_list (device, 4 x uint32 per brick: x, y, z, level) and their total
+ * count to out_total (device uint32).  It calls no cudaMalloc or cudaFree: its
+ * scratch is a fixed array in device memory that every GPU loading the
+ * library keeps until exit, so it suits callers that cannot allocate (stream
+ * capture, hard frame deadlines, hosts that own all device memory).  Limits:
+ * n_entries - 1 <= 8,388,608 (2048 scan tiles of 4096); larger buffers are
+ * rejected with GC_ERR_INVALID.  The first call on a device looks the array's
+ * address up (cudaGetSymbolAddress): make that first call before any stream
+ * capture.  All calls share the array: calls whose work overlaps on the GPU
+ * (other streams, other host threads) race and corrupt each other's results;
+ * order them on one stream. */
+int gc_miss_list_noalloc(const uint32_t *requests, uint64_t n_entries, uint32_t timestamp,
+                         const gc_layout *layout, uint32_t max_requests, uint32_t *out_list,
+                         uint32_t *out_total, void *stream);
 /* Overwrite the usage or request buffer (GC_DUMP_USAGE / GC_DUMP_REQUESTS)
  * from the host: used to replay recorded frames through the update path. */
 int gc_cache_load_buffer(gc_cache_t cache, int what, const void *src, size_t bytes);
