@@ -67,6 +67,21 @@ DIAG = 2.0 * math.sqrt(3.0)
 PIXEL_BYTES = 44  # RGBA 4 + t 4+4 + colour state 16+16 per pixel and launch
 
 
+def workload(name, cfg):
+    """(workload text, voxel dtype, data text) of a plain per-view config."""
+    n = cfg["size"][0]
+    dt = "u8" if cfg["bpc"] == 1 else "u16"
+    vol = f"{n}^3 {dt}"
+    if cfg["path"] == "orbit":
+        how = f"{cfg['W']}^2 views on a {cfg['frames']}-view orbit at {cfg['dist'][0]}x the diagonal"
+    else:
+        how = (f"{cfg['W']}^2 views along a {cfg['frames']}-view fly-through from {cfg['dist'][0]}x to "
+               f"{cfg['dist'][1]}x the diagonal")
+    core = "in-core" if cfg["pool_slots"] else "out-of-core"
+    return (f"{name}: {vol} {core}, plain per-view path, {how}, each rendered to convergence", dt,
+            f"synthetic (seeded blobs + value noise, {vol}; no public dataset)")
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -343,6 +358,7 @@ def run_ours(args):
     # Roofline of the dominant kernel on a converged view: full work per launch.
     last = spec(args.warmup + args.steps - 1)
     ev = []
+    torch.cuda.nvtx.range_push("roofline")
     for _ in range(5):
         views, bufs = S.views(last)
         with torch.cuda.stream(S.stream):
@@ -355,22 +371,24 @@ def run_ours(args):
             ev.append((e0, e1))
             S.cm.update(S.sp)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     touched = S.cm.stats().last_used
     render_ms = statistics.median([a.elapsed_time(b) for a, b in ev])
     algo = touched * cfg["B"] ** 3 * vol.encoded_bytes + W * H * PIXEL_BYTES
     peak, peak_kind = measured_peak()
     achieved = algo / (render_ms / 1e3) / 1e9
 
+    wl, dt, data_txt = workload(args.config, cfg)
+    pool_bytes = S.cm.info.pool_bytes
     out = {
         "metric": "Mrays/s", "value": round(rays / wall / 1e6, 3), "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * wall / args.steps, 4),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
-        "data": "synthetic (seeded blobs + value noise, 2048^3 u16; no public dataset)",
-        "config": {"workload": "c2: 2048^3 u16 out-of-core, plain per-view path, 1024^2 views along a 120-view "
-                               "fly-through, each rendered to convergence",
-                   "brick_size": cfg["B"], "covering": cfg["c"], "pool_slots": list(S.pool), "pool_gib": 2,
-                   "view": [W, H], "max_requests": args.max_requests, "loader": "sync",
-                   "l2": "inputs > L2 (2 GiB pool, 103 MB page directory, 28 GiB host brick store)",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dt, "data": data_txt,
+        "config": {"workload": wl, "brick_size": cfg["B"], "covering": cfg["c"], "pool_slots": list(S.pool),
+                   "pool_gib": round(pool_bytes / 2**30, 3), "view": [W, H], "max_requests": args.max_requests,
+                   "loader": "sync",
+                   "l2": "inputs > L2 (2 GiB pool, 103 MB page directory, 28 GiB host brick store)"
+                   if args.config == "c2" else "in-core volume; L2 not flushed (the c1 case is for profiling)",
                    "preprocess_s": round(prep_s, 2)},
         "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
         "iterations_per_view": {"mean": round(statistics.mean(iters), 2), "max": max(iters)},
@@ -379,15 +397,16 @@ def run_ours(args):
                 "h2d_bytes_per_step": int((s1_e.bytes_h2d - s0_e.bytes_h2d) / args.steps) + 700,
                 "d2h_bytes_per_step": W * H * 4, "latency_ms": {"p50": pct(lat_e, 50), "p99": pct(lat_e, 99)}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 5), "traffic": None, "kernel": "render_kernel (dvr_march)",
+                     "frac": round(achieved / peak, 5), "traffic": None,
+                     "kernel": "render_pixels_kernel" if gc.render_tuning()[0] == 1 else "render_kernel",
                      "peak_kind": peak_kind, "algorithmic_bytes_per_launch": int(algo),
                      "launch_ms": round(render_ms, 4), "touched_bricks": int(touched),
-                     "note": "converged 1024^2 view of c2; compulsory bytes = touched bricks x B^3 x 2 B + 44 B/pixel"},
+                     "note": f"converged {W}x{H} view of {args.config}; compulsory bytes = touched bricks x B^3 x "
+                             f"{vol.encoded_bytes} B + {PIXEL_BYTES} B/pixel"},
         "render_tuning": {"scheduler_tile_threads_bps": list(tuned[0][0]) if tuned else None,
                           "candidates_timed": len(tuned[0][1]) if tuned else 0},
         "gpu_launches": int(launches),
-        "cache": {"bricks_installed": int(s1.bricks_installed - s0.bricks_installed),
-                  "brick_h2d_bytes": int(s1.bytes_h2d - s0.bytes_h2d), "device_error": int(s1.device_error)},
+        "cache": cache_delta(s0, s1),
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -402,22 +421,25 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def run_batched(gc, torch, args):
-    """c3: the same views rendered batched (continuous batching, all active
-    views in one persistent launch per tick) and plain (one view per launch,
-    to convergence), each on a fresh cache."""
-    cfg = CONFIGS["c3"]
-    vol, layout, store, offs, prep_s = make_store(gc, torch, cfg)
-    nb = args.batches
-    views = [v for b in range(nb) for v in batch_views(gc, cfg, 100 + b, cfg["batch"])]
-    warm = batch_views(gc, cfg, 99, 8)
-    rays = sum(W * H for _, W, H in views)
-    res = {}
+def cache_delta(s0, s1):
+    """Loader and upload figures between two gc_cache_stats snapshots."""
+    up_ms = (s1.upload_ns - s0.upload_ns) / 1e6
+    nbytes = s1.bytes_h2d - s0.bytes_h2d
+    return {"bricks_installed": int(s1.bricks_installed - s0.bricks_installed), "brick_h2d_bytes": int(nbytes),
+            "load_cycles": int(s1.load_cycles - s0.load_cycles),
+            "loader_host_ms": round((s1.loader_host_ns - s0.loader_host_ns) / 1e6, 2),
+            "upload_ms": round(up_ms, 2), "upload_gbs": round(nbytes / (up_ms / 1e3) / 1e9, 1) if up_ms > 0 else None,
+            "device_error": int(s1.device_error)}
 
-    # batched: asynchronous loader, admission by pixel budget and cache occupancy
+
+def batched_pass(gc, torch, cfg, data, views, warm, args):
+    """The batched form over `views`: continuous batching with the
+    asynchronous loader on a fresh cache.  Returns (result dict, wall s)."""
+    vol, layout, store, offs = data
+    rays = sum(W * H for _, W, H in views)
     S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests, sync=False)
     B = gc.Batch(S.cm, max_views=cfg["batch"], max_pixels=args.batch_pixels, max_passes=args.batch_cap,
-                 max_occupancy=args.occupancy, max_admit=args.admit)
+                 max_occupancy=args.occupancy, max_admit=args.admit, lookahead=args.lookahead)
 
     def run_all(vs, base):
         for i, (m, W, H) in enumerate(vs):
@@ -433,37 +455,69 @@ def run_batched(gc, torch, args):
 
     run_all(warm, 10000)
     torch.cuda.synchronize()
+    s0 = S.cm.stats()
     t0 = time.perf_counter()
     out, ticks = run_all(views, 0)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
+    s1 = S.cm.stats()
     lat = [r[3] for r in out]
-    res["batched"] = {"value": round(rays / wall / 1e6, 3), "wall_s": round(wall, 4), "ticks": ticks,
-                      "view_latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
-                      "passes_per_view": round(statistics.mean(r[1] for r in out), 2),
-                      "converged_views": f"{sum(1 for r in out if r[2])}/{len(views)}",
-                      "device_error": int(S.cm.stats().device_error)}
+    res = {"value": round(rays / wall / 1e6, 3), "wall_s": round(wall, 4), "ticks": ticks,
+           "view_latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+           "passes_per_view": round(statistics.mean(r[1] for r in out), 2),
+           "converged_views": f"{sum(1 for r in out if r[2])}/{len(views)}",
+           "cache": cache_delta(s0, s1)}
     B.close()
     S.close()
+    return res, wall
 
-    # plain on the same views
+
+def plain_views_pass(gc, torch, cfg, data, views, warm, args):
+    """The plain per-view loop (synchronous loader, one view per launch, each
+    to convergence) over the same views on a fresh cache."""
+    vol, layout, store, offs = data
+    rays = sum(W * H for _, W, H in views)
     S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
-    for i, v in enumerate(warm):
+    for v in warm:
         S.converge([v], cap=args.batch_cap)
+    s0 = S.cm.stats()
     wall, lat, info = timed(torch, S.stream, lambda i: S.converge([views[i]], cap=args.batch_cap), len(views))
-    res["plain"] = {"value": round(rays / wall / 1e6, 3), "wall_s": round(wall, 4),
-                    "view_latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
-                    "converged_views": f"{sum(1 for _, c in info if c)}/{len(views)}",
-                    "device_error": int(S.cm.stats().device_error)}
+    s1 = S.cm.stats()
+    res = {"value": round(rays / wall / 1e6, 3), "wall_s": round(wall, 4),
+           "view_latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+           "converged_views": f"{sum(1 for _, c in info if c)}/{len(views)}",
+           "iterations_per_view": round(statistics.mean(i for i, _ in info), 2),
+           "cache": cache_delta(s0, s1)}
     S.close()
-    return {"config": {"workload": f"c3: {len(views)} views ({nb} x {cfg['batch']}), sizes {list(cfg['sizes'])}, "
-                                   f"cameras at 0.5-3.0x diagonal; BrickSize 32, 4 GiB pool; all submitted at t0, "
-                                   f"continuous batching with a {args.batch_pixels} pixel budget, admission "
-                                   f"while the last tick used <= {args.occupancy} of the pool, <= {args.admit} "
-                                   f"admissions per tick, asynchronous loader",
+    return res, wall
+
+
+def c3_views(gc, cfg, nb):
+    views = [v for b in range(nb) for v in batch_views(gc, cfg, 100 + b, cfg["batch"])]
+    return views, batch_views(gc, cfg, 99, 8)
+
+
+def run_batched(gc, torch, args):
+    """c3: the same views rendered batched (continuous batching, all views
+    that can progress in one persistent launch per tick) and plain (one view
+    per launch, to convergence), each on a fresh cache."""
+    cfg = CONFIGS["c3"]
+    vol, layout, store, offs, prep_s = make_store(gc, torch, cfg)
+    data = (vol, layout, store, offs)
+    views, warm = c3_views(gc, cfg, args.batches)
+    rays = sum(W * H for _, W, H in views)
+    batched, _ = batched_pass(gc, torch, cfg, data, views, warm, args)
+    plain, _ = plain_views_pass(gc, torch, cfg, data, views, warm, args)
+    la = "all bricks to the ray's end" if args.lookahead >= 1 << 20 else f"{args.lookahead} bricks"
+    return {"config": {"workload": f"c3: {len(views)} views ({args.batches} x {cfg['batch']}), sizes "
+                                   f"{list(cfg['sizes'])}, cameras at 0.5-3.0x diagonal; BrickSize 32, 4 GiB pool; "
+                                   f"all submitted at t0, continuous batching with a {args.batch_pixels} pixel "
+                                   f"budget, admission while demand (used + missing) <= {args.occupancy} of the "
+                                   f"pool, <= {args.admit} admissions per tick, request lookahead {la}, "
+                                   f"asynchronous loader",
                        "preprocess_s": round(prep_s, 2), "rays": int(rays)},
-            "unit": "Mrays/s", "batched": res["batched"], "plain_same_views": res["plain"],
-            "ratio": round(res["batched"]["value"] / res["plain"]["value"], 3)}
+            "unit": "Mrays/s", "batched": batched, "plain_same_views": plain,
+            "ratio": round(batched["value"] / plain["value"], 3)}
 
 
 def cpu_baseline(gc, S, cfg, spec, args):
@@ -544,10 +598,9 @@ def run_reference(args):
     value = W * H * args.steps / el / 1e6
     out = {"impl": "reference", "metric": "Mrays/s", "value": round(value, 4), "unit": "Mrays/s", "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * el / args.steps, 3),
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
-           "data": "synthetic (seeded blobs + value noise, 2048^3 u16; no public dataset)",
-           "config": {"workload": "c2: 2048^3 u16 out-of-core, plain per-view path, 1024^2 views along a 120-view "
-                                  "fly-through, each rendered to convergence (CPU port on host cores)",
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": workload(args.config, cfg)[1],
+           "data": workload(args.config, cfg)[2],
+           "config": {"workload": workload(args.config, cfg)[0] + " (CPU port on host cores)",
                       "view": [W, H], "max_requests": args.max_requests, "pool_slots": list(pool)},
            "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
@@ -571,6 +624,8 @@ def main():
     ap.add_argument("--batch-pixels", type=int, default=16 << 20)
     ap.add_argument("--occupancy", type=float, default=0.6)
     ap.add_argument("--admit", type=int, default=4)
+    ap.add_argument("--lookahead", type=int, default=1 << 20,
+                    help="batched request policy: further missing bricks a stopped ray requests")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")

@@ -60,6 +60,7 @@ struct ViewParams {
     uint32_t tiles_x;                   // warp tiles per row
     uint32_t tile_shift;                // log2 of the tile width
     uint32_t tile_begin;                // first global tile index of this view
+    uint32_t lookahead;                 // extra missing bricks a stopped ray requests (0: none)
 };
 
 // Scan control block shared by the decoupled look-back kernels.

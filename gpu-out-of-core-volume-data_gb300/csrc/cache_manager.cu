@@ -21,6 +21,7 @@
 // on that copy's event instead of reading mapped host memory from the kernel.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <mutex>
@@ -97,7 +98,8 @@ struct gc_cache {
     uint32_t *h_total = nullptr, *h_big_index = nullptr, *h_misc = nullptr;
     uint8_t *h_staging = nullptr;
     cudaStream_t side = nullptr;
-    cudaEvent_t ev_list = nullptr, ev_upload = nullptr;
+    cudaEvent_t ev_list = nullptr, ev_upload = nullptr, ev_upload_begin = nullptr;
+    bool upload_timed = false;  // ev_upload_begin/ev_upload bracket an upload not yet counted
     int cur = 0;
     uint32_t ts = 1, epoch_lru = 0, epoch_miss = 0;
     // loader
@@ -141,6 +143,7 @@ static void build_tables(gc_cache *C) {
 // Resolve the asked bricks: RequestHandler::handle_request (RequestHandler.hpp:277-372).
 // Returns the number of bricks to install (non-empty first), or 0.
 static void resolve_and_upload(gc_cache *C, uint32_t n) {
+    const auto t_begin = std::chrono::steady_clock::now();
     const gc_volume_desc &v = C->d.volume;
     const uint32_t BB[3] = {v.big_brick_size[0], v.big_brick_size[1], v.big_brick_size[2]};
     std::unordered_map<uint64_t, int32_t> asked;
@@ -233,8 +236,12 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     std::memcpy(C->h_big_index, big_index.data(), big_index.size() * sizeof(uint32_t));
     C->pend_n = k;
     C->pend_nonempty = n_nonempty;
+    C->stats.load_cycles++;
+    C->stats.loader_host_ns += static_cast<uint64_t>(
+        std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t_begin).count());
     if (k == 0) return;
     cudaStream_t s = C->side;
+    GC_CUDA(cudaEventRecord(C->ev_upload_begin, s));
     if (nbig)
         GC_CUDA(cudaMemcpyAsync(C->d_staging, C->h_staging, static_cast<size_t>(nbig) * C->big_bytes,
                                 cudaMemcpyHostToDevice, s));
@@ -246,6 +253,7 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
                                 cudaMemcpyHostToDevice, s));
     }
     GC_CUDA(cudaEventRecord(C->ev_upload, s));
+    C->upload_timed = true;
     C->stats.bytes_h2d += static_cast<uint64_t>(nbig) * C->big_bytes;
     C->stats.requests_served += n;
 }
@@ -255,6 +263,16 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
 static bool serve_request(gc_cache *C) {
     GC_CUDA(cudaSetDevice(C->device));
     GC_CUDA(cudaEventSynchronize(C->ev_list));
+    // The previous upload has normally completed (its install ran before this
+    // scan); waiting on it also keeps the staging buffers from being refilled
+    // under a copy when the caller switches streams between frames.
+    if (C->upload_timed) {
+        GC_CUDA(cudaEventSynchronize(C->ev_upload));
+        float ms = 0.f;
+        GC_CUDA(cudaEventElapsedTime(&ms, C->ev_upload_begin, C->ev_upload));
+        C->stats.upload_ns += static_cast<uint64_t>(static_cast<double>(ms) * 1e6);
+        C->upload_timed = false;
+    }
     const uint32_t total = *C->h_total;
     const uint32_t n = std::min(total, C->d.max_requests);
     C->stats.last_requests = total;
@@ -421,6 +439,7 @@ static void destroy(gc_cache *C) {
         if (p) cudaFreeHost(p);
     if (C->ev_list) cudaEventDestroy(C->ev_list);
     if (C->ev_upload) cudaEventDestroy(C->ev_upload);
+    if (C->ev_upload_begin) cudaEventDestroy(C->ev_upload_begin);
     if (C->side) cudaStreamDestroy(C->side);
     delete C;
 }
@@ -469,7 +488,7 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
     out.tile_shift = static_cast<uint32_t>(__builtin_ctz(tw));
 }
 
-static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s) {
+static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s, uint32_t lookahead = 0) {
     GC_REQUIRE(views && n >= 1, "no views");
     GC_REQUIRE(n <= C->max_views, "too many views in one batch");
     GC_REQUIRE(C->d.volume.channels == 1, "the ray caster renders single-channel volumes");
@@ -478,6 +497,7 @@ static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s
     uint32_t tiles = 0;
     for (uint32_t i = 0; i < n; ++i) {
         fill_view(C, views[i], vp[i]);
+        vp[i].lookahead = lookahead;
         vp[i].tile_begin = tiles;
         tiles += vp[i].tiles_x * div_up(views[i].height, 32u >> vp[i].tile_shift);
     }
@@ -567,7 +587,8 @@ int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out) {
         count_launch();
         GC_CUDA(cudaStreamCreateWithFlags(&C->side, cudaStreamNonBlocking));
         GC_CUDA(cudaEventCreateWithFlags(&C->ev_list, cudaEventDisableTiming));
-        GC_CUDA(cudaEventCreateWithFlags(&C->ev_upload, cudaEventDisableTiming));
+        GC_CUDA(cudaEventCreate(&C->ev_upload));
+        GC_CUDA(cudaEventCreate(&C->ev_upload_begin));
         GC_CUDA(cudaDeviceSynchronize());
         if (!C->sync_mode()) C->th = std::thread(loader_main, C);
         *out = C;
@@ -769,6 +790,82 @@ int gc_render_batch(gc_cache_t C, const gc_view *views, uint32_t n, void *stream
 #include <chrono>
 #include <deque>
 
+namespace gc {
+
+// The batched tick runs the cache steps in the order install -> render ->
+// LRU update -> scan, so that one tick carries a whole request cycle: the
+// scan sees the requests of a render that already used the bricks installed
+// at the start of the same tick.  (The plain frame loop keeps the reference's
+// update(), where install and scan fall in different frames.)
+
+// Installs what the loader finished.  Returns true when bricks were installed.
+static bool batch_install(gc_cache *C, cudaStream_t s) {
+    if (C->sync_mode()) {
+        if (!C->done) return false;
+        const bool any = C->pend_n > 0;
+        install(C, s);
+        C->done = false;
+        return any;
+    }
+    std::unique_lock<std::mutex> lk(C->mu);
+    if (!C->loader_error.empty()) {
+        std::string e = C->loader_error;
+        C->loader_error.clear();
+        fail(GC_ERR_IO, "brick loader: " + e);
+    }
+    if (C->busy || !C->done) return false;
+    lk.unlock();
+    const bool any = C->pend_n > 0;
+    install(C, s);
+    lk.lock();
+    C->done = false;
+    return any;
+}
+
+// True when no load is in flight and none waits for its install.
+static bool loader_idle(gc_cache *C) {
+    if (C->sync_mode()) return !C->done;
+    std::lock_guard<std::mutex> g(C->mu);
+    return !C->busy && !C->done;
+}
+
+// End of a rendered tick: LRU update and, with the loader idle, the scan.
+// Returns true when a scan was issued (its miss count lands in h_total).
+static bool batch_update(gc_cache *C, cudaStream_t s) {
+    lru_update(C, s);
+    bool scanned = false;
+    if (C->sync_mode()) {
+        if (!C->done) {
+            scan_requests(C, s);
+            C->done = serve_request(C);
+            scanned = true;
+        }
+    } else {
+        std::unique_lock<std::mutex> lk(C->mu);
+        if (!C->busy && !C->done) {
+            lk.unlock();
+            scan_requests(C, s);
+            lk.lock();
+            C->busy = true;
+            C->has_request = true;
+            C->cv.notify_all();
+            scanned = true;
+        }
+    }
+    C->ts++;
+    C->stats.frames++;
+    return scanned;
+}
+
+// Waits (bounded) for the asynchronous loader to finish its load.
+static void wait_loader(gc_cache *C, int ms) {
+    if (C->sync_mode()) return;
+    std::unique_lock<std::mutex> lk(C->mu);
+    C->cv.wait_for(lk, std::chrono::milliseconds(ms), [&] { return !C->busy; });
+}
+
+}  // namespace gc
+
 struct gc_batch {
     gc_cache *cache = nullptr;
     gc_batch_desc d;
@@ -776,14 +873,18 @@ struct gc_batch {
         gc_view view;
         uint64_t tag;
         uint32_t passes;
+        uint64_t epoch;  // install count at the view's last pass (kNever before the first)
         std::chrono::steady_clock::time_point submitted;
     };
+    static constexpr uint64_t kNever = ~0ull;
+    uint64_t installs = 0;  // ticks that installed bricks
     std::deque<Item> queue;
     std::vector<Item> active;
     std::deque<gc_batch_result> done;
     uint32_t *d_status = nullptr;
     uint32_t *h_status = nullptr;   // [max_views] status words + [1] used slots
-    uint32_t last_used = 0;
+    uint32_t last_used = 0;         // slots stamped by the last pass over all active views
+    uint32_t last_misses = 0;       // missing bricks requested by the last scan (uncapped)
     cudaEvent_t ev = nullptr;
 };
 
@@ -828,7 +929,7 @@ int gc_batch_submit(gc_batch_t b, const gc_view *view, uint64_t tag) {
         GC_REQUIRE(b && view, "null argument");
         ViewParams check;
         fill_view(b->cache, *view, check);  // validates the view now, not at admission
-        b->queue.push_back({*view, tag, 0, std::chrono::steady_clock::now()});
+        b->queue.push_back({*view, tag, 0, gc_batch::kNever, std::chrono::steady_clock::now()});
     });
 }
 
@@ -839,19 +940,26 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         GC_REQUIRE(C->src.kind != 0, "no brick source set");
         GC_CUDA(cudaSetDevice(C->device));
         cudaStream_t s = as_stream(stream);
+        if (batch_install(C, s)) b->installs++;
+        // Every active view is rendered when bricks were just installed or the
+        // loader is idle; only then are views admitted, so that a new view's
+        // first pass feeds the scan that ends the tick.
+        const bool all = loader_idle(C);
         // admission: views in arrival order while the budgets allow (at least
-        // one active view); by cache memory: no admission while the last tick
-        // used more than max_occupancy of the pool slots
+        // one active view).  By cache memory: the demand of the active views
+        // -- slots their last full pass used plus the missing bricks the last
+        // scan found -- must stay within max_occupancy of the pool slots.
         uint64_t pixels = 0;
         for (auto &it : b->active) pixels += static_cast<uint64_t>(it.view.width) * it.view.height;
-        const bool occ_ok = b->d.max_occupancy <= 0.f ||
-                            static_cast<double>(b->last_used) <= b->d.max_occupancy * static_cast<double>(C->nslots);
+        const double demand = static_cast<double>(b->last_used) + static_cast<double>(b->last_misses);
+        const bool occ_ok =
+            b->d.max_occupancy <= 0.f || demand <= b->d.max_occupancy * static_cast<double>(C->nslots);
         uint32_t admitted = 0;
         while (!b->queue.empty() && b->active.size() < b->d.max_views) {
             const gc_view &v = b->queue.front().view;
             const uint64_t px = static_cast<uint64_t>(v.width) * v.height;
-            if (!b->active.empty() &&
-                (pixels + px > b->d.max_pixels || !occ_ok || (b->d.max_admit && admitted >= b->d.max_admit)))
+            if (!b->active.empty() && (!all || pixels + px > b->d.max_pixels || !occ_ok ||
+                                       (b->d.max_admit && admitted >= b->d.max_admit)))
                 break;
             ++admitted;
             GC_CUDA(cudaMemsetAsync(v.tbuf, 0, px * sizeof(float), s));
@@ -860,33 +968,42 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
             b->active.push_back(b->queue.front());
             b->queue.pop_front();
         }
-        const uint32_t n = static_cast<uint32_t>(b->active.size());
-        if (n_active) *n_active = n;
-        if (n == 0) {
-            if (n_queued) *n_queued = static_cast<uint32_t>(b->queue.size());
+        const uint32_t na = static_cast<uint32_t>(b->active.size());
+        if (n_active) *n_active = na;
+        if (n_queued) *n_queued = static_cast<uint32_t>(b->queue.size());
+        // Views that can progress: never rendered, or bricks were installed
+        // since their last pass.
+        std::vector<uint32_t> sel;
+        sel.reserve(na);
+        for (uint32_t i = 0; i < na; ++i)
+            if (all || b->active[i].epoch != b->installs) sel.push_back(i);
+        if (sel.empty()) {
+            if (na) wait_loader(C, 5);
             return;
         }
+        const uint32_t n = static_cast<uint32_t>(sel.size());
         std::vector<gc_view> views(n);
-        for (uint32_t i = 0; i < n; ++i) {
-            views[i] = b->active[i].view;
-            views[i].status = b->d_status + i;
+        for (uint32_t k = 0; k < n; ++k) {
+            views[k] = b->active[sel[k]].view;
+            views[k].status = b->d_status + k;
         }
         GC_CUDA(cudaMemsetAsync(b->d_status, 0, n * sizeof(uint32_t), s));
-        render(C, views.data(), n, s);
+        render(C, views.data(), n, s, b->d.lookahead);
         GC_CUDA(cudaMemcpyAsync(b->h_status, b->d_status, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        update(C, s);
+        const bool scanned = batch_update(C, s);
         GC_CUDA(cudaMemcpyAsync(b->h_status + b->d.max_views, C->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                 s));
         GC_CUDA(cudaEventRecord(b->ev, s));
         GC_CUDA(cudaEventSynchronize(b->ev));
-        b->last_used = b->h_status[b->d.max_views];
+        if (all) b->last_used = b->h_status[b->d.max_views];
+        if (scanned) b->last_misses = *C->h_total;  // copied on this stream before the event
         const auto now = std::chrono::steady_clock::now();
-        std::vector<gc_batch::Item> keep;
-        keep.reserve(n);
-        for (uint32_t i = 0; i < n; ++i) {
-            auto &it = b->active[i];
+        std::vector<char> gone(na, 0);
+        for (uint32_t k = 0; k < n; ++k) {
+            auto &it = b->active[sel[k]];
             it.passes++;
-            const bool conv = (b->h_status[i] & 1u) == 0;
+            it.epoch = b->installs;
+            const bool conv = (b->h_status[k] & 1u) == 0;
             if (conv || (b->d.max_passes && it.passes >= b->d.max_passes)) {
                 gc_batch_result r;
                 r.tag = it.tag;
@@ -894,12 +1011,14 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
                 r.converged = conv ? 1u : 0u;
                 r.latency_ms = std::chrono::duration<double, std::milli>(now - it.submitted).count();
                 b->done.push_back(r);
-            } else {
-                keep.push_back(it);
+                gone[sel[k]] = 1;
             }
         }
+        std::vector<gc_batch::Item> keep;
+        keep.reserve(na);
+        for (uint32_t i = 0; i < na; ++i)
+            if (!gone[i]) keep.push_back(b->active[i]);
         b->active.swap(keep);
-        if (n_queued) *n_queued = static_cast<uint32_t>(b->queue.size());
     });
 }
 

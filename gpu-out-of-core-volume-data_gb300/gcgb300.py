@@ -68,7 +68,8 @@ class CacheStats(C.Structure):
     _fields_ = [("frames", C.c_uint64), ("requests_raised", C.c_uint64), ("requests_served", C.c_uint64),
                 ("bricks_installed", C.c_uint64), ("bricks_empty", C.c_uint64), ("bytes_h2d", C.c_uint64),
                 ("load_errors", C.c_uint64), ("last_requests", C.c_uint32), ("last_used", C.c_uint32),
-                ("device_error", C.c_uint32)]
+                ("device_error", C.c_uint32), ("load_cycles", C.c_uint64), ("loader_host_ns", C.c_uint64),
+                ("upload_ns", C.c_uint64)]
 
 
 class View(C.Structure):
@@ -81,7 +82,7 @@ class View(C.Structure):
 
 class BatchDesc(C.Structure):
     _fields_ = [("max_views", C.c_uint32), ("max_pixels", C.c_uint64), ("max_passes", C.c_uint32),
-                ("max_occupancy", C.c_float), ("max_admit", C.c_uint32)]
+                ("max_occupancy", C.c_float), ("max_admit", C.c_uint32), ("lookahead", C.c_uint32)]
 
 
 class BatchResult(C.Structure):
@@ -480,10 +481,11 @@ class CacheManager:
 class Batch:
     """Continuous batching of views over one cache (gc_batch_*)."""
 
-    def __init__(self, cache, max_views=64, max_pixels=1 << 24, max_passes=0, max_occupancy=0.0, max_admit=0):
+    def __init__(self, cache, max_views=64, max_pixels=1 << 24, max_passes=0, max_occupancy=0.0, max_admit=0,
+                 lookahead=0):
         self.cache = cache
         self._h = vp()
-        d = BatchDesc(max_views, max_pixels, max_passes, max_occupancy, max_admit)
+        d = BatchDesc(max_views, max_pixels, max_passes, max_occupancy, max_admit, lookahead)
         check(lib.gc_batch_create(cache.handle, C.byref(d), C.byref(self._h)))
 
     def submit(self, view, tag):

@@ -246,6 +246,9 @@ typedef struct gc_cache_stats {
     uint32_t last_requests;       /* misses found in the last request scan     */
     uint32_t last_used;           /* slots stamped by the last rendered frame   */
     uint32_t device_error;        /* sticky device-side error word (0 = none)  */
+    uint64_t load_cycles;         /* request lists the loader resolved         */
+    uint64_t loader_host_ns;      /* host time resolving + staging bricks      */
+    uint64_t upload_ns;           /* device time of the side-stream H2D copies */
 } gc_cache_stats;
 int gc_cache_stats_get(gc_cache_t cache, gc_cache_stats *out);
 
@@ -349,24 +352,41 @@ int gc_render_tuning_get(uint32_t out[4]);
 /* Continuous batching of views over one cache (the batched and served forms;
  * no counterpart in the reference, whose frame loop renders one view per
  * launch, VolumeRayCaster.cu:261-330).  Views are queued with their own
- * buffers; each tick admits queued views within the budgets, renders every
- * active view in one persistent launch sharing the cache's miss list, runs one
- * cache update, and retires the views none of whose rays met an unmapped brick
- * in that pass (or that reached max_passes).  A retired view's buffers hold its
- * final image. */
+ * buffers.  A tick (1) installs the bricks the loader finished, (2) when
+ * bricks were installed or the loader is idle, admits queued views within
+ * the budgets, (3) renders in one persistent launch every
+ * view that can progress -- the newly admitted ones, and all active views
+ * when bricks were installed or the loader is idle; a view whose rays wait on
+ * missing bricks cannot progress before the next install, so its pass is
+ * skipped -- (4) updates the LRU order and, when the loader is idle, scans the
+ * shared request buffer and hands the miss list to the loader, and (5)
+ * retires the rendered views none of whose rays met an unmapped brick (or
+ * that reached max_passes).  When nothing can be rendered it waits for the
+ * loader (a few milliseconds at most).  A retired view's buffers hold its
+ * final image, the one the plain per-view loop converges to.  The batch
+ * requires the cache's asynchronous loader or its synchronous one alike. */
 typedef struct gc_batch *gc_batch_t;
 typedef struct gc_batch_desc {
     uint32_t max_views;      /* active views per launch (<= 256)              */
     uint64_t max_pixels;     /* admission budget: sum of W*H of active views  */
     uint32_t max_passes;     /* retire unconverged after this many passes (0: never) */
     float max_occupancy;     /* admission by cache memory: no view is admitted
-                                while the last tick used more than this
-                                fraction of the pool slots (<= 0: no limit)    */
+                                while the active views' demand -- slots their
+                                last full pass used plus the missing bricks
+                                the last scan found -- exceeds this fraction
+                                of the pool slots (<= 0: no limit).  With a
+                                lookahead the first pass of a view requests
+                                its whole working set, so the demand is
+                                known one tick after admission.               */
     uint32_t max_admit;      /* views admitted per tick (0: no limit)          */
+    uint32_t lookahead;      /* request policy: a ray that stops at a missing
+                                brick also requests up to this many further
+                                missing bricks along its path (0: only the
+                                first, as the plain method does)               */
 } gc_batch_desc;
 typedef struct gc_batch_result {
     uint64_t tag;
-    uint32_t passes;         /* render passes the view took                   */
+    uint32_t passes;         /* render passes the view took (skipped ones not counted) */
     uint32_t converged;      /* 1 if its last pass met no unmapped brick      */
     double latency_ms;       /* submit -> retirement, host clock              */
 } gc_batch_result;

@@ -199,11 +199,14 @@ def test_async_loader_converges_to_same_image(gc, orc, torch_cuda):
     assert np.array_equal(imgs[0], imgs[1])
 
 
-def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda):
+@pytest.mark.parametrize("lookahead,sync", [(0, True), (0, False), (1 << 20, True), (3, False)])
+def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, lookahead, sync):
     """Continuous batching (admission by pixel budget, one persistent launch
-    per tick, retirement on convergence) gives every view the image it gets
-    when rendered alone to convergence; the per-view status word reports
-    convergence exactly."""
+    per tick, skipped passes for views that cannot progress, retirement on
+    convergence) gives every view the image it gets when rendered alone to
+    convergence, with the synchronous or the asynchronous loader and with the
+    first-miss or the lookahead request policy; the per-view status word
+    reports convergence exactly."""
     specs = [((64, 48), 1), ((33, 17), 4), ((96, 80), 7), ((40, 40), 10), ((80, 24), 5)]
     tf = scenario.ramp_tf()
     single = []
@@ -224,15 +227,15 @@ def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda):
         single.append(g[0].cpu().numpy())
     s.cm.close()
 
-    s2 = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 64)
-    b = gc.Batch(s2.cm, max_views=3, max_pixels=96 * 80 + 64 * 48)
+    s2 = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 64, sync=sync)
+    b = gc.Batch(s2.cm, max_views=3, max_pixels=96 * 80 + 64 * 48, lookahead=lookahead)
     bufs = []
     for i, ((W, H), cam) in enumerate(specs):
         g, _ = s2.buffers(W, H)
         bufs.append(g)
         b.submit(s2.view(scenario.orbit_camera(gc, cam, 12, 3.0), W, H, tf_dev, 256, g), tag=100 + i)
     results = []
-    for tick in range(400):
+    for tick in range(4000):
         active, queued = b.tick()
         assert active <= 3
         results += b.poll()
