@@ -210,11 +210,14 @@ def make_store(gc, torch, cfg):
 class Session:
     """One cache + the buffers of its views, driven through the C ABI."""
 
+    staged = False  # GC_CACHE_STAGED_UPLOAD for every session (--upload staged)
+
     def __init__(self, gc, torch, cfg, vol, layout, store, offs, max_requests, sync=True):
         self.gc, self.torch, self.cfg = gc, torch, cfg
         self.pool = cfg["pool_slots"] or gc.pool_dims(vol, cfg["pool_bytes"])
-        self.cm = gc.CacheManager(vol, layout, self.pool, max_requests=max_requests, sync_loader=sync)
-        self.cm.set_source_host(store.data_ptr(), offs)
+        self.cm = gc.CacheManager(vol, layout, self.pool, max_requests=max_requests, sync_loader=sync,
+                                  staged_upload=Session.staged)
+        self.cm.set_source_host(store, offs)
         self.vol = vol
         self.tf = torch.from_numpy(tf_table(cfg["tf"]).reshape(-1)).cuda()
         self.stream = torch.cuda.Stream()
@@ -386,7 +389,8 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dt, "data": data_txt,
         "config": {"workload": wl, "brick_size": cfg["B"], "covering": cfg["c"], "pool_slots": list(S.pool),
                    "pool_gib": round(pool_bytes / 2**30, 3), "view": [W, H], "max_requests": args.max_requests,
-                   "loader": "sync",
+                   "loader": "sync", "upload": "gather kernel reading the host store"
+                   if S.cm.stats().upload_direct else "staged host copies + cudaMemcpyAsync",
                    "l2": "inputs > L2 (2 GiB pool, 103 MB page directory, 28 GiB host brick store)"
                    if args.config == "c2" else "in-core volume; L2 not flushed (the c1 case is for profiling)",
                    "preprocess_s": round(prep_s, 2)},
@@ -429,6 +433,7 @@ def cache_delta(s0, s1):
             "load_cycles": int(s1.load_cycles - s0.load_cycles),
             "loader_host_ms": round((s1.loader_host_ns - s0.loader_host_ns) / 1e6, 2),
             "upload_ms": round(up_ms, 2), "upload_gbs": round(nbytes / (up_ms / 1e3) / 1e9, 1) if up_ms > 0 else None,
+            "upload_route": "gather" if s1.upload_direct else "staged",
             "device_error": int(s1.device_error)}
 
 
@@ -439,7 +444,8 @@ def batched_pass(gc, torch, cfg, data, views, warm, args):
     rays = sum(W * H for _, W, H in views)
     S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests, sync=False)
     B = gc.Batch(S.cm, max_views=cfg["batch"], max_pixels=args.batch_pixels, max_passes=args.batch_cap,
-                 max_occupancy=args.occupancy, max_admit=args.admit, lookahead=args.lookahead)
+                 max_occupancy=args.occupancy, max_admit=args.admit, lookahead=args.lookahead,
+                 reorder_window=args.reorder)
 
     def run_all(vs, base):
         for i, (m, W, H) in enumerate(vs):
@@ -456,16 +462,26 @@ def batched_pass(gc, torch, cfg, data, views, warm, args):
     run_all(warm, 10000)
     torch.cuda.synchronize()
     s0 = S.cm.stats()
+    b0 = B.stats()
+    torch.cuda.nvtx.range_push("batched")
     t0 = time.perf_counter()
     out, ticks = run_all(views, 0)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
+    torch.cuda.nvtx.range_pop()
     s1 = S.cm.stats()
+    b1 = B.stats()
     lat = [r[3] for r in out]
     res = {"value": round(rays / wall / 1e6, 3), "wall_s": round(wall, 4), "ticks": ticks,
            "view_latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
            "passes_per_view": round(statistics.mean(r[1] for r in out), 2),
            "converged_views": f"{sum(1 for r in out if r[2])}/{len(views)}",
+           "ticks_detail": {"render_ticks": b1.render_ticks - b0.render_ticks,
+                            "install_ticks": b1.install_ticks - b0.install_ticks,
+                            "view_passes": b1.view_passes - b0.view_passes,
+                            "render_ms": round(b1.render_ms - b0.render_ms, 2),
+                            "tick_host_ms": round(b1.tick_ms - b0.tick_ms, 2),
+                            "loader_wait_ms": round(b1.wait_ms - b0.wait_ms, 2)},
            "cache": cache_delta(s0, s1)}
     B.close()
     S.close()
@@ -495,6 +511,38 @@ def plain_views_pass(gc, torch, cfg, data, views, warm, args):
 def c3_views(gc, cfg, nb):
     views = [v for b in range(nb) for v in batch_views(gc, cfg, 100 + b, cfg["batch"])]
     return views, batch_views(gc, cfg, 99, 8)
+
+
+def run_c3(args):
+    """`--config c3` alone: the batched form over the c3 views (and, unless
+    --no-plain, the plain loop over the same views), one JSON line."""
+    import torch
+
+    import gcgb300 as gc
+
+    cfg = CONFIGS["c3"]
+    vol, layout, store, offs, prep_s = make_store(gc, torch, cfg)
+    data = (vol, layout, store, offs)
+    views, warm = c3_views(gc, cfg, args.batches)
+    rays = sum(W * H for _, W, H in views)
+    S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
+    best, _ = autotune(gc, torch, S, warm[:4], args)
+    S.close()
+    batched, wall = batched_pass(gc, torch, cfg, data, views, warm, args)
+    out = {"metric": "Mrays/s", "value": batched["value"], "unit": "Mrays/s", "n_gpus": 1, "steps": len(views),
+           "warmup": len(warm), "ms_per_step": round(1e3 * wall / len(views), 4), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "u16",
+           "data": "synthetic (seeded blobs + value noise, 2048^3 u16; no public dataset)",
+           "config": {"workload": f"c3: {len(views)} views, batched (continuous batching), each to convergence",
+                      "rays": int(rays), "reorder": args.reorder, "occupancy": args.occupancy,
+                      "admit": args.admit, "lookahead": args.lookahead, "render_tuning": list(best),
+                      "preprocess_s": round(prep_s, 2)},
+           "batched": batched}
+    if not args.no_plain:
+        plain, _ = plain_views_pass(gc, torch, cfg, data, views, warm, args)
+        out["plain_same_views"] = plain
+        out["ratio"] = round(batched["value"] / plain["value"], 3)
+    print(json.dumps(out), flush=True)
 
 
 def run_batched(gc, torch, args):
@@ -617,26 +665,40 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=["c1", "c2"], default="c2")
+    ap.add_argument("--config", choices=["c1", "c2", "c3"], default="c2",
+                    help="c2: the plain out-of-core line (+ the c3 batched object); c1: small in-core plain case; "
+                         "c3: the batched form alone")
     ap.add_argument("--max-requests", type=int, default=8192)
     ap.add_argument("--batches", type=int, default=3)
     ap.add_argument("--batch-cap", type=int, default=256)
     ap.add_argument("--batch-pixels", type=int, default=16 << 20)
     ap.add_argument("--occupancy", type=float, default=0.6)
     ap.add_argument("--admit", type=int, default=4)
-    ap.add_argument("--lookahead", type=int, default=1 << 20,
+    ap.add_argument("--upload", choices=["auto", "staged"], default="auto",
+                    help="brick upload route: auto = gather kernel reading the host store where the device can, "
+                         "staged = host copies into pinned staging + cudaMemcpyAsync")
+    ap.add_argument("--reorder", type=int, default=192,
+                    help="batched admission: locality window over queued views (0: arrival order)")
+    ap.add_argument("--lookahead", type=int, default=0,
                     help="batched request policy: further missing bricks a stopped ray requests")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="c3: skip the plain loop over the same views")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 40 if args.impl == "ours" else 2
     args.warmup = max(3, args.warmup)
+    Session.staged = args.upload == "staged"
     if args.config != "c2":
         args.no_batched = True
-    if args.impl == "reference":
+    if args.impl == "reference" and args.config == "c3":
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm covers the plain configs "
+                                                              "(c1, c2); c3 is the batched form"}), flush=True)
+    elif args.impl == "reference":
         run_reference(args)
+    elif args.config == "c3":
+        run_c3(args)
     else:
         run_ours(args)
 

@@ -61,6 +61,8 @@ struct ViewParams {
     uint32_t tile_shift;                // log2 of the tile width
     uint32_t tile_begin;                // first global tile index of this view
     uint32_t lookahead;                 // extra missing bricks a stopped ray requests (0: none)
+    uint32_t mark_done;                 // batched passes: a finished ray leaves -1 - t in tbuf and
+                                        // later passes skip its pixel (rgba already final)
 };
 
 // Scan control block shared by the decoupled look-back kernels.
@@ -103,6 +105,11 @@ struct InstallArgs {
     uint32_t n, n_nonempty;
 };
 void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s);
+// Copies n blocks of `bytes` bytes from src + off[i] (device-readable host
+// memory) to dst + i * bytes; vec16: src, every offset and bytes are
+// multiples of 16.
+void launch_gather_bricks(const uint8_t *src, const uint64_t *off, uint32_t n, uint64_t bytes, uint8_t *dst,
+                          bool vec16, cudaStream_t s);
 void launch_completude(const float4 *slot_vpos, uint32_t nslots, uint32_t *count, cudaStream_t s);
 
 // Ray caster (render.cu).  Launch configuration of the ray caster, process

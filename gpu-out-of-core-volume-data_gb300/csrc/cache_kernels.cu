@@ -356,7 +356,7 @@ void launch_lru_count(const uint32_t *usage, uint32_t nslots, uint32_t ts, uint3
     const uint32_t grid = std::min<uint32_t>(div_up(nslots, 256), static_cast<uint32_t>(sm_count()) * 4);
     lru_count_kernel<<<std::max(1u, grid), 256, 0, s>>>(usage, nslots, ts, count);
     GC_CUDA(cudaGetLastError());
-        count_launch();
+    count_launch();
 }
 
 void launch_lru_partition(const uint32_t *order_in, uint32_t *order_out, const uint32_t *usage, uint32_t ts,
@@ -365,7 +365,7 @@ void launch_lru_partition(const uint32_t *order_in, uint32_t *order_out, const u
     lru_partition_kernel<<<lookback_tiles(nslots), kThreads, 0, s>>>(order_in, order_out, usage, ts, nslots,
                                                                      count, status, ctl, epoch);
     GC_CUDA(cudaGetLastError());
-        count_launch();
+    count_launch();
 }
 
 void launch_miss_compact(const uint32_t *req, uint64_t nscan, uint32_t ts, uint32_t maxreq, uint4 *list,
@@ -374,7 +374,7 @@ void launch_miss_compact(const uint32_t *req, uint64_t nscan, uint32_t ts, uint3
     miss_compact_kernel<<<lookback_tiles(nscan), kThreads, 0, s>>>(req, nscan, ts, maxreq, list, lt, mx, my,
                                                                    status, ctl, epoch);
     GC_CUDA(cudaGetLastError());
-        count_launch();
+    count_launch();
 }
 
 void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s) {
@@ -395,7 +395,52 @@ void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s)
                                      static_cast<int>(smem)));
     install_reference_kernel<<<1, 1024, smem, s>>>(a, lt, one_over_beff);
     GC_CUDA(cudaGetLastError());
-        count_launch();
+    count_launch();
+}
+
+// Brick gather from device-readable host memory (the direct upload route):
+// block-strided over bricks, each brick copied by the whole block with
+// 16-byte loads when aligned.  The reads travel over the host link; the
+// writes land in the device staging buffer the install kernels read.
+// Four independent loads per thread are in flight before their stores: the
+// host link's latency (microseconds) needs many bytes in flight per SM.
+template <typename W>
+__global__ void gather_bricks_kernel(const uint8_t *__restrict__ src, const uint64_t *__restrict__ off, uint32_t n,
+                                     uint64_t words, uint8_t *__restrict__ dst) {
+    constexpr uint32_t kIlp = 4;
+    for (uint32_t b = blockIdx.x; b < n; b += gridDim.x) {
+        const W *sp = reinterpret_cast<const W *>(src + off[b]);
+        W *dp = reinterpret_cast<W *>(dst) + static_cast<uint64_t>(b) * words;
+        const uint64_t stride = static_cast<uint64_t>(blockDim.x) * kIlp;
+        for (uint64_t i0 = threadIdx.x; i0 < words; i0 += stride) {
+            W v[kIlp];
+#pragma unroll
+            for (uint32_t k = 0; k < kIlp; ++k) {
+                const uint64_t i = i0 + static_cast<uint64_t>(k) * blockDim.x;
+                if (i < words) v[k] = sp[i];
+            }
+#pragma unroll
+            for (uint32_t k = 0; k < kIlp; ++k) {
+                const uint64_t i = i0 + static_cast<uint64_t>(k) * blockDim.x;
+                if (i < words) dp[i] = v[k];
+            }
+        }
+    }
+}
+
+void launch_gather_bricks(const uint8_t *src, const uint64_t *off, uint32_t n, uint64_t bytes, uint8_t *dst,
+                          bool vec16, cudaStream_t s) {
+    if (n == 0) return;
+    // one block of 256 per SM (four 16-byte loads in flight per thread)
+    // saturates the host link; more would only take SM slots from the ray
+    // caster running beside it
+    const uint32_t grid = std::min<uint32_t>(n, static_cast<uint32_t>(sm_count()));
+    if (vec16)
+        gather_bricks_kernel<uint4><<<grid, 256, 0, s>>>(src, off, n, bytes / 16, dst);
+    else
+        gather_bricks_kernel<uint8_t><<<grid, 256, 0, s>>>(src, off, n, bytes, dst);
+    GC_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void launch_completude(const float4 *slot_vpos, uint32_t nslots, uint32_t *count, cudaStream_t s) {
@@ -403,7 +448,7 @@ void launch_completude(const float4 *slot_vpos, uint32_t nslots, uint32_t *count
     const uint32_t grid = std::min<uint32_t>(div_up(nslots, 256), static_cast<uint32_t>(sm_count()) * 4);
     completude_kernel<<<std::max(1u, grid), 256, 0, s>>>(slot_vpos, nslots, count);
     GC_CUDA(cudaGetLastError());
-        count_launch();
+    count_launch();
 }
 
 }  // namespace gc

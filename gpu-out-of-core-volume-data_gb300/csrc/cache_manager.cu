@@ -16,9 +16,11 @@
 // With GC_CACHE_SYNC_LOADER the loader finishes inside update(), which gives
 // the reference's request -> install alternation deterministically.  Without
 // it a loader thread resolves bricks while later frames render, as the
-// reference's RequestHandler thread does; bricks then go up through a pinned
-// staging buffer with cudaMemcpyAsync on a side stream, and the install waits
-// on that copy's event instead of reading mapped host memory from the kernel.
+// reference's RequestHandler thread does.  Either way the bricks go up on a
+// side stream and the install waits on that upload's event: a gather kernel
+// reading the host store directly where the device can (page-locked store, or
+// pageable memory on a coherent Grace-Blackwell link), else host copies into
+// a pinned staging buffer and one cudaMemcpyAsync.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -66,6 +68,10 @@ __global__ void init_slots_kernel(uint32_t *order, uint32_t *level, float4 *vpos
 struct Source {
     int kind = 0;  // 0 none, 1 host store, 2 callback
     const uint8_t *host = nullptr;
+    uint64_t bytes = 0;
+    bool direct = false;          // the device reads the store (gather kernel)
+    bool vec16 = false;           // store, offsets and big-brick bytes 16-byte aligned
+    const uint8_t *dev = nullptr;  // device-usable address of the store
     std::vector<uint64_t> level_off;
     gc_brick_loader_fn fn = nullptr;
     void *user = nullptr;
@@ -90,14 +96,17 @@ struct gc_cache {
     uint32_t *d_count = nullptr, *d_misc = nullptr, *d_queue = nullptr;
     uint4 *d_list = nullptr, *d_asked = nullptr, *d_big_coord = nullptr;
     uint32_t *d_big_index = nullptr;
+    uint64_t *d_src_off = nullptr;
     uint8_t *d_staging = nullptr;
     gc::ViewParams *d_views = nullptr;
     uint32_t max_views = 256;
     // pinned host buffers
     uint4 *h_list = nullptr, *h_asked = nullptr, *h_big_coord = nullptr;
     uint32_t *h_total = nullptr, *h_big_index = nullptr, *h_misc = nullptr;
+    uint64_t *h_src_off = nullptr;
     uint8_t *h_staging = nullptr;
     cudaStream_t side = nullptr;
+    cudaStream_t frame_stream = nullptr;  // stream of the update in progress (synchronous loader)
     cudaEvent_t ev_list = nullptr, ev_upload = nullptr, ev_upload_begin = nullptr;
     bool upload_timed = false;  // ev_upload_begin/ev_upload bracket an upload not yet counted
     int cur = 0;
@@ -182,8 +191,11 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
                 gz < L.nb_big_bricks[b.w][2]) {
                 const uint64_t idx =
                     (static_cast<uint64_t>(gz) * L.nb_big_bricks[b.w][1] + gy) * L.nb_big_bricks[b.w][0] + gx;
-                copies.push_back({C->src.host + C->src.level_off[b.w] + idx * C->big_bytes,
-                                  C->h_staging + static_cast<uint64_t>(nbig) * C->big_bytes});
+                const uint64_t off = C->src.level_off[b.w] + idx * C->big_bytes;  // inside the store (checked)
+                if (C->src.direct)
+                    C->h_src_off[nbig] = off;
+                else
+                    copies.push_back({C->src.host + off, C->h_staging + static_cast<uint64_t>(nbig) * C->big_bytes});
                 status = GC_BRICK_SUCCESS;
             }
         } else if (C->src.kind == 2) {
@@ -240,11 +252,20 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     C->stats.loader_host_ns += static_cast<uint64_t>(
         std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t_begin).count());
     if (k == 0) return;
-    cudaStream_t s = C->side;
+    // With the synchronous loader a gather upload goes on the caller's stream,
+    // ahead of the next frame's render: on a side stream it can wait behind a
+    // persistent ray-caster launch that holds every SM.  Staged copies (copy
+    // engine) and the asynchronous loader use the high-priority side stream.
+    const bool gather = C->src.kind == 1 && C->src.direct;
+    cudaStream_t s = C->sync_mode() && gather ? C->frame_stream : C->side;
     GC_CUDA(cudaEventRecord(C->ev_upload_begin, s));
-    if (nbig)
+    if (nbig && gather) {
+        GC_CUDA(cudaMemcpyAsync(C->d_src_off, C->h_src_off, nbig * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+        launch_gather_bricks(C->src.dev, C->d_src_off, nbig, C->big_bytes, C->d_staging, C->src.vec16, s);
+    } else if (nbig) {
         GC_CUDA(cudaMemcpyAsync(C->d_staging, C->h_staging, static_cast<size_t>(nbig) * C->big_bytes,
                                 cudaMemcpyHostToDevice, s));
+    }
     GC_CUDA(cudaMemcpyAsync(C->d_asked, C->h_asked, k * sizeof(uint4), cudaMemcpyHostToDevice, s));
     if (n_nonempty) {
         GC_CUDA(cudaMemcpyAsync(C->d_big_index, C->h_big_index, n_nonempty * sizeof(uint32_t),
@@ -375,6 +396,7 @@ static void scan_requests(gc_cache *C, cudaStream_t s) {
 
 static bool update(gc_cache *C, cudaStream_t s) {
     GC_CUDA(cudaSetDevice(C->device));
+    C->frame_stream = s;
     lru_update(C, s);
     bool converged = false;
     if (C->sync_mode()) {
@@ -431,10 +453,11 @@ static void destroy(gc_cache *C) {
     cudaDeviceSynchronize();
     void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool,
                    C->status_lru, C->status_miss, C->ctl_lru, C->ctl_miss, C->d_count, C->d_misc, C->d_queue,
-                   C->d_list, C->d_asked, C->d_big_coord, C->d_big_index, C->d_staging, C->d_views};
+                   C->d_list, C->d_asked, C->d_big_coord, C->d_big_index, C->d_src_off, C->d_staging, C->d_views};
     for (void *p : dev)
         if (p) cudaFree(p);
-    void *host[] = {C->h_list, C->h_asked, C->h_big_coord, C->h_total, C->h_big_index, C->h_misc, C->h_staging};
+    void *host[] = {C->h_list,  C->h_asked, C->h_big_coord, C->h_total,
+                    C->h_big_index, C->h_misc, C->h_src_off, C->h_staging};
     for (void *p : host)
         if (p) cudaFreeHost(p);
     if (C->ev_list) cudaEventDestroy(C->ev_list);
@@ -488,7 +511,8 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
     out.tile_shift = static_cast<uint32_t>(__builtin_ctz(tw));
 }
 
-static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s, uint32_t lookahead = 0) {
+static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s, uint32_t lookahead = 0,
+                   bool mark_done = false) {
     GC_REQUIRE(views && n >= 1, "no views");
     GC_REQUIRE(n <= C->max_views, "too many views in one batch");
     GC_REQUIRE(C->d.volume.channels == 1, "the ray caster renders single-channel volumes");
@@ -498,6 +522,7 @@ static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s
     for (uint32_t i = 0; i < n; ++i) {
         fill_view(C, views[i], vp[i]);
         vp[i].lookahead = lookahead;
+        vp[i].mark_done = mark_done ? 1u : 0u;
         vp[i].tile_begin = tiles;
         tiles += vp[i].tiles_x * div_up(views[i].height, 32u >> vp[i].tile_shift);
     }
@@ -561,12 +586,14 @@ int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out) {
         C->d_asked = dalloc<uint4>(maxr, "asked list");
         C->d_big_coord = dalloc<uint4>(maxr, "big brick coords");
         C->d_big_index = dalloc<uint32_t>(maxr, "big brick indexes");
+        C->d_src_off = dalloc<uint64_t>(maxr, "brick source offsets");
         C->d_staging = dalloc<uint8_t>(maxr * C->big_bytes, "staging");
         C->d_views = dalloc<ViewParams>(C->max_views, "views");
         C->h_list = halloc<uint4>(maxr);
         C->h_asked = halloc<uint4>(maxr);
         C->h_big_coord = halloc<uint4>(maxr);
         C->h_big_index = halloc<uint32_t>(maxr);
+        C->h_src_off = halloc<uint64_t>(maxr);
         C->h_total = halloc<uint32_t>(1);
         C->h_misc = halloc<uint32_t>(1);
         C->h_staging = halloc<uint8_t>(maxr * C->big_bytes);
@@ -585,7 +612,9 @@ int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out) {
                                                                                     C->slot_vpos, C->nslots);
         GC_CUDA(cudaGetLastError());
         count_launch();
-        GC_CUDA(cudaStreamCreateWithFlags(&C->side, cudaStreamNonBlocking));
+        int least = 0, greatest = 0;
+        GC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        GC_CUDA(cudaStreamCreateWithPriority(&C->side, cudaStreamNonBlocking, greatest));
         GC_CUDA(cudaEventCreateWithFlags(&C->ev_list, cudaEventDisableTiming));
         GC_CUDA(cudaEventCreate(&C->ev_upload));
         GC_CUDA(cudaEventCreate(&C->ev_upload_begin));
@@ -602,16 +631,51 @@ int gc_cache_destroy(gc_cache_t cache) {
     return GC_OK;
 }
 
-int gc_cache_set_source_host(gc_cache_t C, const void *bricks, const uint64_t *level_offsets,
+int gc_cache_set_source_host(gc_cache_t C, const void *bricks, uint64_t bytes, const uint64_t *level_offsets,
                              const uint64_t *empty_keys, size_t n_empty) {
     return guard([&] {
-        GC_REQUIRE(C && bricks && level_offsets, "null argument");
+        GC_REQUIRE(C && bricks && level_offsets && (empty_keys || n_empty == 0), "null argument");
+        GC_CUDA(cudaSetDevice(C->device));
+        const gc_layout &L = C->d.layout;
+        bool aligned = C->big_bytes % 16 == 0;
+        for (uint32_t l = 0; l < L.nb_levels; ++l) {
+            const uint64_t nbig =
+                static_cast<uint64_t>(L.nb_big_bricks[l][0]) * L.nb_big_bricks[l][1] * L.nb_big_bricks[l][2];
+            GC_REQUIRE(level_offsets[l] <= bytes && nbig <= (bytes - level_offsets[l]) / C->big_bytes,
+                       "brick store: level " + std::to_string(l) + " does not fit in the store's bytes");
+            aligned = aligned && level_offsets[l] % 16 == 0;
+        }
+        // Can the device read the store?  Page-locked memory has a device
+        // address; any host memory can be read where the device accesses
+        // pageable memory coherently.
+        bool direct = false;
+        const uint8_t *dev = nullptr;
+        if (!(C->d.flags & GC_CACHE_STAGED_UPLOAD)) {
+            cudaPointerAttributes at;
+            if (cudaPointerGetAttributes(&at, bricks) == cudaSuccess && at.type == cudaMemoryTypeHost &&
+                at.devicePointer) {
+                direct = true;
+                dev = static_cast<const uint8_t *>(at.devicePointer);
+            } else {
+                (void)cudaGetLastError();
+                int pageable = 0;
+                GC_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, C->device));
+                if (pageable) {
+                    direct = true;
+                    dev = static_cast<const uint8_t *>(bricks);
+                }
+            }
+        }
         std::lock_guard<std::mutex> g(C->mu);
         GC_REQUIRE(!C->busy, "the loader is busy");
         C->src = Source();
         C->src.kind = 1;
         C->src.host = static_cast<const uint8_t *>(bricks);
-        C->src.level_off.assign(level_offsets, level_offsets + C->d.layout.nb_levels);
+        C->src.bytes = bytes;
+        C->src.direct = direct;
+        C->src.dev = dev;
+        C->src.vec16 = aligned && reinterpret_cast<uintptr_t>(dev) % 16 == 0;
+        C->src.level_off.assign(level_offsets, level_offsets + L.nb_levels);
         for (size_t i = 0; i < n_empty; ++i) C->src.empty.insert(empty_keys[i]);
     });
 }
@@ -684,6 +748,7 @@ int gc_cache_stats_get(gc_cache_t C, gc_cache_stats *out) {
         GC_CUDA(cudaMemcpy(&used, C->d_count, sizeof(used), cudaMemcpyDeviceToHost));
         *out = C->stats;
         out->device_error = a.err | b.err;
+        out->upload_direct = C->src.kind == 1 && C->src.direct ? 1u : 0u;
         out->last_used = used;
     });
 }
@@ -832,6 +897,7 @@ static bool loader_idle(gc_cache *C) {
 // End of a rendered tick: LRU update and, with the loader idle, the scan.
 // Returns true when a scan was issued (its miss count lands in h_total).
 static bool batch_update(gc_cache *C, cudaStream_t s) {
+    C->frame_stream = s;
     lru_update(C, s);
     bool scanned = false;
     if (C->sync_mode()) {
@@ -874,8 +940,11 @@ struct gc_batch {
         uint64_t tag;
         uint32_t passes;
         uint64_t epoch;  // install count at the view's last pass (kNever before the first)
+        uint32_t skipped;  // times a later view was admitted before it
         std::chrono::steady_clock::time_point submitted;
     };
+    float last_cam[3] = {0.f, 0.f, 0.f};  // camera of the last admitted view
+    bool have_cam = false;
     static constexpr uint64_t kNever = ~0ull;
     uint64_t installs = 0;  // ticks that installed bricks
     std::deque<Item> queue;
@@ -885,7 +954,8 @@ struct gc_batch {
     uint32_t *h_status = nullptr;   // [max_views] status words + [1] used slots
     uint32_t last_used = 0;         // slots stamped by the last pass over all active views
     uint32_t last_misses = 0;       // missing bricks requested by the last scan (uncapped)
-    cudaEvent_t ev = nullptr;
+    cudaEvent_t ev = nullptr, ev_r0 = nullptr, ev_r1 = nullptr;
+    gc_batch_stats st;
 };
 
 namespace gc {
@@ -894,6 +964,8 @@ static void batch_destroy(gc_batch *b) {
     if (b->d_status) cudaFree(b->d_status);
     if (b->h_status) cudaFreeHost(b->h_status);
     if (b->ev) cudaEventDestroy(b->ev);
+    if (b->ev_r0) cudaEventDestroy(b->ev_r0);
+    if (b->ev_r1) cudaEventDestroy(b->ev_r1);
     delete b;
 }
 }  // namespace gc
@@ -913,6 +985,9 @@ int gc_batch_create(gc_cache_t C, const gc_batch_desc *desc, gc_batch_t *out) {
         b->d_status = dalloc<uint32_t>(desc->max_views, "batch status");
         b->h_status = halloc<uint32_t>(desc->max_views + 1);
         GC_CUDA(cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming));
+        GC_CUDA(cudaEventCreate(&b->ev_r0));
+        GC_CUDA(cudaEventCreate(&b->ev_r1));
+        std::memset(&b->st, 0, sizeof(b->st));
         *out = b;
     });
     if (rc != GC_OK) batch_destroy(b);
@@ -929,7 +1004,7 @@ int gc_batch_submit(gc_batch_t b, const gc_view *view, uint64_t tag) {
         GC_REQUIRE(b && view, "null argument");
         ViewParams check;
         fill_view(b->cache, *view, check);  // validates the view now, not at admission
-        b->queue.push_back({*view, tag, 0, gc_batch::kNever, std::chrono::steady_clock::now()});
+        b->queue.push_back({*view, tag, 0, gc_batch::kNever, 0, std::chrono::steady_clock::now()});
     });
 }
 
@@ -940,7 +1015,19 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         GC_REQUIRE(C->src.kind != 0, "no brick source set");
         GC_CUDA(cudaSetDevice(C->device));
         cudaStream_t s = as_stream(stream);
-        if (batch_install(C, s)) b->installs++;
+        const auto t_tick = std::chrono::steady_clock::now();
+        struct TickClock {  // adds the host time of this tick on every exit
+            gc_batch *b;
+            std::chrono::steady_clock::time_point t0;
+            ~TickClock() {
+                b->st.ticks++;
+                b->st.tick_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            }
+        } tick_clock{b, t_tick};
+        if (batch_install(C, s)) {
+            b->installs++;
+            b->st.install_ticks++;
+        }
         // Every active view is rendered when bricks were just installed or the
         // loader is idle; only then are views admitted, so that a new view's
         // first pass feeds the scan that ends the tick.
@@ -955,8 +1042,25 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         const bool occ_ok =
             b->d.max_occupancy <= 0.f || demand <= b->d.max_occupancy * static_cast<double>(C->nslots);
         uint32_t admitted = 0;
+        auto cam_dist = [&](const gc_view &v) {  // camera = translation column of the view matrix
+            const float dx = v.inv_view[3] - b->last_cam[0], dy = v.inv_view[7] - b->last_cam[1],
+                        dz = v.inv_view[11] - b->last_cam[2];
+            return dx * dx + dy * dy + dz * dz;
+        };
         while (!b->queue.empty() && b->active.size() < b->d.max_views) {
-            const gc_view &v = b->queue.front().view;
+            size_t pick = 0;
+            if (b->d.reorder_window > 1 && b->have_cam && b->queue.front().skipped < b->d.reorder_window) {
+                const size_t w = std::min<size_t>(b->queue.size(), b->d.reorder_window);
+                float best = cam_dist(b->queue[0].view);
+                for (size_t k = 1; k < w; ++k) {
+                    const float d = cam_dist(b->queue[k].view);
+                    if (d < best) {
+                        best = d;
+                        pick = k;
+                    }
+                }
+            }
+            const gc_view &v = b->queue[pick].view;
             const uint64_t px = static_cast<uint64_t>(v.width) * v.height;
             if (!b->active.empty() && (!all || pixels + px > b->d.max_pixels || !occ_ok ||
                                        (b->d.max_admit && admitted >= b->d.max_admit)))
@@ -965,8 +1069,13 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
             GC_CUDA(cudaMemsetAsync(v.tbuf, 0, px * sizeof(float), s));
             GC_CUDA(cudaMemsetAsync(v.state, 0, px * 4 * sizeof(float), s));
             pixels += px;
-            b->active.push_back(b->queue.front());
-            b->queue.pop_front();
+            b->last_cam[0] = v.inv_view[3];
+            b->last_cam[1] = v.inv_view[7];
+            b->last_cam[2] = v.inv_view[11];
+            b->have_cam = true;
+            if (pick) b->queue.front().skipped++;
+            b->active.push_back(b->queue[pick]);
+            b->queue.erase(b->queue.begin() + static_cast<std::ptrdiff_t>(pick));
         }
         const uint32_t na = static_cast<uint32_t>(b->active.size());
         if (n_active) *n_active = na;
@@ -978,7 +1087,11 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         for (uint32_t i = 0; i < na; ++i)
             if (all || b->active[i].epoch != b->installs) sel.push_back(i);
         if (sel.empty()) {
-            if (na) wait_loader(C, 5);
+            if (na) {
+                const auto t0 = std::chrono::steady_clock::now();
+                wait_loader(C, 5);
+                b->st.wait_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            }
             return;
         }
         const uint32_t n = static_cast<uint32_t>(sel.size());
@@ -988,7 +1101,9 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
             views[k].status = b->d_status + k;
         }
         GC_CUDA(cudaMemsetAsync(b->d_status, 0, n * sizeof(uint32_t), s));
-        render(C, views.data(), n, s, b->d.lookahead);
+        GC_CUDA(cudaEventRecord(b->ev_r0, s));
+        render(C, views.data(), n, s, b->d.lookahead, true);
+        GC_CUDA(cudaEventRecord(b->ev_r1, s));
         GC_CUDA(cudaMemcpyAsync(b->h_status, b->d_status, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         const bool scanned = batch_update(C, s);
         GC_CUDA(cudaMemcpyAsync(b->h_status + b->d.max_views, C->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost,
@@ -996,6 +1111,11 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         GC_CUDA(cudaEventRecord(b->ev, s));
         GC_CUDA(cudaEventSynchronize(b->ev));
         if (all) b->last_used = b->h_status[b->d.max_views];
+        float rms = 0.f;
+        GC_CUDA(cudaEventElapsedTime(&rms, b->ev_r0, b->ev_r1));
+        b->st.render_ms += rms;
+        b->st.render_ticks++;
+        b->st.view_passes += n;
         if (scanned) b->last_misses = *C->h_total;  // copied on this stream before the event
         const auto now = std::chrono::steady_clock::now();
         std::vector<char> gone(na, 0);
@@ -1019,6 +1139,13 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         for (uint32_t i = 0; i < na; ++i)
             if (!gone[i]) keep.push_back(b->active[i]);
         b->active.swap(keep);
+    });
+}
+
+int gc_batch_stats_get(gc_batch_t b, gc_batch_stats *out) {
+    return guard([&] {
+        GC_REQUIRE(b && out, "null argument");
+        *out = b->st;
     });
 }
 

@@ -301,6 +301,8 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
                                           Ray &r) {
     const ViewParams &vp = *vpp;
     const uint32_t W = vp.W, H = vp.H;
+    // a batched pass skips a pixel whose ray finished in an earlier pass
+    if (vp.mark_done && vp.tbuf[y * W + x] < 0.f) return false;
     uint32_t xN = x + 1;
     if (xN > W) xN = x - 1;
     uint32_t yN = y + 1;
@@ -351,6 +353,7 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
         const uint32_t Bc = static_cast<uint32_t>(saturate(fc.z) * 255.0f);
         const uint32_t A = static_cast<uint32_t>(saturate(fc.w) * 255.0f);
         vp.rgba[i] = (A << 24) | (Bc << 16) | (G << 8) | R;
+        if (vp.mark_done) vp.tbuf[i] = -1.0f;
         return false;
     }
     if (tnear < 0.f) tnear = 0.f;
@@ -483,11 +486,15 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
 __device__ __forceinline__ bool ray_finish(Ray &r) {
     const ViewParams &vp = *r.vp;
     if (!r.unm) {
-        vp.tbuf[r.i] = r.t;
-        if (r.dvr)
-            reinterpret_cast<float4 *>(vp.state)[r.i] = r.fc;
-        else
-            vp.state[4 * r.i] = r.maxOp;
+        if (vp.mark_done) {
+            vp.tbuf[r.i] = -1.0f - r.t;  // t >= 0: the mark is < 0; the state is not read again
+        } else {
+            vp.tbuf[r.i] = r.t;
+            if (r.dvr)
+                reinterpret_cast<float4 *>(vp.state)[r.i] = r.fc;
+            else
+                vp.state[4 * r.i] = r.maxOp;
+        }
     }
     float4 fc = r.fc;
     if (!r.dvr) fc = tf_lookup(vp.tf, vp.tfw, r.maxOp);

@@ -27,6 +27,7 @@ BRICK_SUCCESS, BRICK_UNKNOWN, BRICK_EMPTY = 0, 1, 2
 MODE_DVR, MODE_MOP = 0, 1
 SAMPLER_REFERENCE, SAMPLER_TRILINEAR = 0, 1
 CACHE_SYNC_LOADER = 1
+CACHE_STAGED_UPLOAD = 2
 DUMP_MRPD, DUMP_LRU, DUMP_USAGE, DUMP_REQUESTS, DUMP_POOL = 0, 1, 2, 3, 4
 
 U3 = C.c_uint32 * 3
@@ -69,7 +70,7 @@ class CacheStats(C.Structure):
                 ("bricks_installed", C.c_uint64), ("bricks_empty", C.c_uint64), ("bytes_h2d", C.c_uint64),
                 ("load_errors", C.c_uint64), ("last_requests", C.c_uint32), ("last_used", C.c_uint32),
                 ("device_error", C.c_uint32), ("load_cycles", C.c_uint64), ("loader_host_ns", C.c_uint64),
-                ("upload_ns", C.c_uint64)]
+                ("upload_ns", C.c_uint64), ("upload_direct", C.c_uint32)]
 
 
 class View(C.Structure):
@@ -82,7 +83,14 @@ class View(C.Structure):
 
 class BatchDesc(C.Structure):
     _fields_ = [("max_views", C.c_uint32), ("max_pixels", C.c_uint64), ("max_passes", C.c_uint32),
-                ("max_occupancy", C.c_float), ("max_admit", C.c_uint32), ("lookahead", C.c_uint32)]
+                ("max_occupancy", C.c_float), ("max_admit", C.c_uint32), ("lookahead", C.c_uint32),
+                ("reorder_window", C.c_uint32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("ticks", C.c_uint64), ("render_ticks", C.c_uint64), ("view_passes", C.c_uint64),
+                ("install_ticks", C.c_uint64), ("render_ms", C.c_double), ("tick_ms", C.c_double),
+                ("wait_ms", C.c_double)]
 
 
 class BatchResult(C.Structure):
@@ -114,7 +122,7 @@ _SIGS = {
     "gc_bricks_empty": [vp, C.c_uint64, P(VolumeDesc), C.c_float, vp, vp],
     "gc_brick_key": [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32],
     "gc_cache_create": [P(CacheDesc), P(vp)], "gc_cache_destroy": [vp],
-    "gc_cache_set_source_host": [vp, vp, P(C.c_uint64), P(C.c_uint64), C.c_size_t],
+    "gc_cache_set_source_host": [vp, vp, C.c_uint64, P(C.c_uint64), P(C.c_uint64), C.c_size_t],
     "gc_cache_set_source_callback": [vp, LOADER_FN, vp, P(C.c_uint64), C.c_size_t],
     "gc_cache_update": [vp, vp, P(C.c_int)], "gc_cache_completude": [vp, vp, P(C.c_float)],
     "gc_cache_timestamp": [vp, P(C.c_uint32)], "gc_cache_info_get": [vp, P(CacheInfo)],
@@ -126,7 +134,7 @@ _SIGS = {
     "gc_tf_build": [P(TfPoint), C.c_uint32, C.c_uint32, P(C.c_float)],
     "gc_render": [vp, P(View), vp], "gc_render_batch": [vp, P(View), C.c_uint32, vp],
     "gc_batch_create": [vp, P(BatchDesc), P(vp)], "gc_batch_destroy": [vp],
-    "gc_batch_submit": [vp, P(View), C.c_uint64], "gc_batch_tick": [vp, vp, P(C.c_uint32), P(C.c_uint32)],
+    "gc_batch_submit": [vp, P(View), C.c_uint64], "gc_batch_stats_get": [vp, P(BatchStats)], "gc_batch_tick": [vp, vp, P(C.c_uint32), P(C.c_uint32)],
     "gc_batch_poll": [vp, P(BatchResult), C.c_uint32, P(C.c_uint32)],
     "gc_miss_list_noalloc": [vp, C.c_uint64, C.c_uint32, P(Layout), C.c_uint32, vp, vp, vp],
     "gc_render_tuning_set": [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32],
@@ -399,8 +407,9 @@ def make_view(inv_view, width, height, tf_ptr, tf_width, rgba_ptr, tbuf_ptr, sta
 class CacheManager:
     """GPU brick cache + ray caster entry (CacheManager<T> + RayCastDVR)."""
 
-    def __init__(self, vol, layout, cache_size, max_requests=50, sync_loader=True, gpu=0):
-        self.desc = CacheDesc(vol, layout, u3(cache_size), max_requests, CACHE_SYNC_LOADER if sync_loader else 0, gpu)
+    def __init__(self, vol, layout, cache_size, max_requests=50, sync_loader=True, gpu=0, staged_upload=False):
+        flags = (CACHE_SYNC_LOADER if sync_loader else 0) | (CACHE_STAGED_UPLOAD if staged_upload else 0)
+        self.desc = CacheDesc(vol, layout, u3(cache_size), max_requests, flags, gpu)
         self._h = vp()
         check(lib.gc_cache_create(C.byref(self.desc), C.byref(self._h)))
         info = CacheInfo()
@@ -412,11 +421,21 @@ class CacheManager:
     def handle(self):
         return self._h
 
-    def set_source_host(self, bricks_ptr, level_offsets, empty_keys=()):
+    def set_source_host(self, store, level_offsets, empty_keys=(), nbytes=None):
+        """`store`: a host torch tensor or numpy array holding the brick store
+        (or a raw address, with `nbytes`).  The store must outlive the cache."""
+        if hasattr(store, "data_ptr"):
+            ptr, size = store.data_ptr(), store.numel() * store.element_size()
+        elif hasattr(store, "ctypes"):
+            ptr, size = store.ctypes.data, store.nbytes
+        else:
+            if nbytes is None:
+                raise ValueError("nbytes is required with a raw store address")
+            ptr, size = int(store), int(nbytes)
         offs = (C.c_uint64 * MAX_LEVELS)(*[int(o) for o in level_offsets])
         keys = (C.c_uint64 * max(1, len(empty_keys)))(*[int(k) for k in empty_keys])
-        self._keep.append((offs, keys))
-        check(lib.gc_cache_set_source_host(self._h, vp(bricks_ptr), offs, keys, len(empty_keys)))
+        self._keep.append((offs, keys, store))
+        check(lib.gc_cache_set_source_host(self._h, vp(ptr), size, offs, keys, len(empty_keys)))
 
     def set_source_callback(self, fn, empty_keys=()):
         cb = LOADER_FN(fn)
@@ -482,10 +501,10 @@ class Batch:
     """Continuous batching of views over one cache (gc_batch_*)."""
 
     def __init__(self, cache, max_views=64, max_pixels=1 << 24, max_passes=0, max_occupancy=0.0, max_admit=0,
-                 lookahead=0):
+                 lookahead=0, reorder_window=0):
         self.cache = cache
         self._h = vp()
-        d = BatchDesc(max_views, max_pixels, max_passes, max_occupancy, max_admit, lookahead)
+        d = BatchDesc(max_views, max_pixels, max_passes, max_occupancy, max_admit, lookahead, reorder_window)
         check(lib.gc_batch_create(cache.handle, C.byref(d), C.byref(self._h)))
 
     def submit(self, view, tag):
@@ -501,6 +520,11 @@ class Batch:
         n = C.c_uint32()
         check(lib.gc_batch_poll(self._h, arr, max_results, C.byref(n)))
         return [(r.tag, r.passes, bool(r.converged), r.latency_ms) for r in arr[: n.value]]
+
+    def stats(self):
+        st = BatchStats()
+        check(lib.gc_batch_stats_get(self._h, C.byref(st)))
+        return st
 
     def close(self):
         if getattr(self, "_h", None):

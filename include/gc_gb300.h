@@ -58,6 +58,9 @@ extern "C" {
 /* cache flags */
 #define GC_CACHE_SYNC_LOADER 1u   /* loader completes inside update(): deterministic
                                      request -> install alternation            */
+#define GC_CACHE_STAGED_UPLOAD 2u /* host-store bricks always go through the pinned
+                                     staging buffer + cudaMemcpyAsync, even when
+                                     the device can read the store directly     */
 
 /* ------------------------------------------------------------------------ */
 /* Volume description: the reference's config surface (config_skull.cfg:1-24,
@@ -211,11 +214,19 @@ typedef int (*gc_brick_loader_fn)(void *user, uint32_t level, uint32_t x, uint32
 
 int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out);
 int gc_cache_destroy(gc_cache_t cache);
-/* In-memory brick store: all big bricks of every level, level l starting at
- * byte offset level_offsets[l] in (z, y, x) raster order.  The memory must
- * outlive the cache.  empty_keys lists gc_brick_key()s reported as Empty
- * (bricks.xml <EmptyBricks>, MetaData.cpp:65-77). */
-int gc_cache_set_source_host(gc_cache_t cache, const void *bricks, const uint64_t *level_offsets,
+/* In-memory brick store of `bytes` bytes: all big bricks of every level,
+ * level l starting at byte offset level_offsets[l] in (z, y, x) raster order;
+ * every level must lie inside the store (checked, GC_ERR_INVALID otherwise).
+ * The memory must outlive the cache.  empty_keys lists gc_brick_key()s
+ * reported as Empty (bricks.xml <EmptyBricks>, MetaData.cpp:65-77).
+ * Upload route: when the device can read the store -- page-locked memory
+ * (cudaHostAlloc / cudaHostRegister), or any host memory on a system whose
+ * device reports cudaDevAttrPageableMemoryAccess (Grace-Blackwell over
+ * NVLink-C2C) -- a kernel on the loader's side stream gathers the missing
+ * bricks from it straight into device memory and the host only resolves the
+ * request list; otherwise, or with GC_CACHE_STAGED_UPLOAD, host threads copy
+ * the bricks into pinned staging memory and cudaMemcpyAsync uploads them. */
+int gc_cache_set_source_host(gc_cache_t cache, const void *bricks, uint64_t bytes, const uint64_t *level_offsets,
                              const uint64_t *empty_keys, size_t n_empty);
 int gc_cache_set_source_callback(gc_cache_t cache, gc_brick_loader_fn fn, void *user,
                                  const uint64_t *empty_keys, size_t n_empty);
@@ -249,6 +260,8 @@ typedef struct gc_cache_stats {
     uint64_t load_cycles;         /* request lists the loader resolved         */
     uint64_t loader_host_ns;      /* host time resolving + staging bricks      */
     uint64_t upload_ns;           /* device time of the side-stream H2D copies */
+    uint32_t upload_direct;       /* 1: host-store bricks are gathered by a kernel
+                                     reading the store; 0: staged copies         */
 } gc_cache_stats;
 int gc_cache_stats_get(gc_cache_t cache, gc_cache_stats *out);
 
@@ -383,6 +396,13 @@ typedef struct gc_batch_desc {
                                 brick also requests up to this many further
                                 missing bricks along its path (0: only the
                                 first, as the plain method does)               */
+    uint32_t reorder_window; /* locality-aware admission: pick, among the first
+                                reorder_window queued views, the one whose
+                                camera is nearest the last admitted view's
+                                (views that look at the same bricks share
+                                them in the cache); the oldest queued view is
+                                admitted once passed over reorder_window
+                                times.  0 or 1: arrival order.                 */
 } gc_batch_desc;
 typedef struct gc_batch_result {
     uint64_t tag;
@@ -393,12 +413,25 @@ typedef struct gc_batch_result {
 int gc_batch_create(gc_cache_t cache, const gc_batch_desc *desc, gc_batch_t *out);
 int gc_batch_destroy(gc_batch_t batch);
 /* Queue a view; its tbuf and state are cleared when it is admitted.  The
- * view's status field is managed by the batch. */
+ * view's status field is managed by the batch.  While batched, tbuf and
+ * state are the batch's scratch: a finished ray leaves -1 - t in tbuf so
+ * that later passes skip its pixel; rgba holds the image. */
 int gc_batch_submit(gc_batch_t batch, const gc_view *view, uint64_t tag);
 /* One tick.  Outputs (optional): views active during the tick, views queued after it. */
 int gc_batch_tick(gc_batch_t batch, void *stream, uint32_t *active, uint32_t *queued);
 /* Retrieve up to max retired views (oldest first). */
 int gc_batch_poll(gc_batch_t batch, gc_batch_result *out, uint32_t max, uint32_t *n);
+/* Counters since the batch was created. */
+typedef struct gc_batch_stats {
+    uint64_t ticks;           /* gc_batch_tick calls                           */
+    uint64_t render_ticks;    /* ticks that rendered (one launch each)         */
+    uint64_t view_passes;     /* views rendered, summed over ticks             */
+    uint64_t install_ticks;   /* ticks that installed bricks                   */
+    double render_ms;         /* device time of the render launches            */
+    double tick_ms;           /* host time inside gc_batch_tick                */
+    double wait_ms;           /* host time waiting for the loader              */
+} gc_batch_stats;
+int gc_batch_stats_get(gc_batch_t batch, gc_batch_stats *out);
 
 #ifdef __cplusplus
 }

@@ -35,15 +35,40 @@ def compare_state(gc, cm, oc, tag):
     assert cm.completude() == pytest.approx(oc.completude(), abs=0)
 
 
-@pytest.mark.parametrize("maxreq", [50, 700])
-def test_update_replay_with_installs(gc, orc, torch_cuda, maxreq):
+def device_reads_pageable(torch):
+    """cudaDevAttrPageableMemoryAccess of device 0 (Grace-Blackwell: 1)."""
+    import ctypes as C
+
+    rt = None
+    for name in ("libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"):
+        try:
+            rt = C.CDLL(name)
+            break
+        except OSError:
+            pass
+    assert rt is not None, "CUDA runtime library not found"
+    v = C.c_int(0)
+    assert rt.cudaDeviceGetAttribute(C.byref(v), 88, 0) == 0  # cudaDevAttrPageableMemoryAccess
+    return bool(v.value)
+
+
+# upload routes: "pageable" = numpy store (gathered by a kernel where the
+# device reads pageable memory, else staged), "pinned" = page-locked store
+# (always gathered), "staged" = GC_CACHE_STAGED_UPLOAD (host copies + one
+# cudaMemcpyAsync)
+@pytest.mark.parametrize("maxreq,route", [(50, "pageable"), (700, "pageable"), (700, "pinned"), (50, "staged")])
+def test_update_replay_with_installs(gc, orc, torch_cuda, maxreq, route):
     size = (256, 256, 256)
     vol = gc.volume_desc(size, 16, 1, 1, 1)
     layout = gc.compute_layout(vol)
     o = scenario.orc_volume(orc, (256, 256, 256), 1, 1, 8)
     store, offs = scenario.orc_store(orc, gc, o.reshape(-1).view(np.uint8), vol, layout)
-    cm = gc.CacheManager(vol, layout, (10, 10, 10), max_requests=maxreq, sync_loader=True)
-    cm.set_source_host(store.ctypes.data, offs)
+    cm = gc.CacheManager(vol, layout, (10, 10, 10), max_requests=maxreq, sync_loader=True,
+                         staged_upload=route == "staged")
+    src = torch_cuda.from_numpy(store).pin_memory() if route == "pinned" else store
+    cm.set_source_host(src, offs)
+    expect_direct = route == "pinned" or (route == "pageable" and device_reads_pageable(torch_cuda))
+    assert cm.stats().upload_direct == int(expect_direct)
     oc = orc.Cache(cm.desc)
     oc.set_source(store, offs)
     mx, my, _ = oc.mrpd_dims
@@ -63,6 +88,22 @@ def test_update_replay_with_installs(gc, orc, torch_cuda, maxreq):
         compare_state(gc, cm, oc, f"frame {f}")
     st = cm.stats()
     assert st.bricks_installed > 0 and st.device_error == 0
+
+
+def test_store_size_is_checked(gc, orc, torch_cuda):
+    """Every level of the brick store must lie inside the bytes given: the
+    upload kernel reads the store directly, so a short store is rejected up
+    front instead of being read past its end."""
+    size = (64, 64, 64)
+    vol = gc.volume_desc(size, 16, 1, 1, 1)
+    layout = gc.compute_layout(vol)
+    o = scenario.orc_volume(orc, size, 1, 4, 5)
+    store, offs = scenario.orc_store(orc, gc, o.reshape(-1).view(np.uint8), vol, layout)
+    cm = gc.CacheManager(vol, layout, (6, 6, 6), max_requests=50, sync_loader=True)
+    with pytest.raises(gc.GcError, match="does not fit"):
+        cm.set_source_host(store[: store.size - 1], offs)
+    cm.set_source_host(store, offs)
+    cm.close()
 
 
 def test_update_replay_large_geometry(gc, orc, torch_cuda):

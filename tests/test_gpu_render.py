@@ -30,7 +30,7 @@ class Scene:
         assert np.array_equal(self.store.numpy(), ref)
         self.ref = ref
         self.cm = gc.CacheManager(self.vol, self.layout, pool, max_requests=maxreq, sync_loader=sync)
-        self.cm.set_source_host(self.store.data_ptr(), self.offs)
+        self.cm.set_source_host(self.store, self.offs)
         self.oc = orc.Cache(self.cm.desc)
         self.oc.set_source(ref, roffs)
 
@@ -199,14 +199,16 @@ def test_async_loader_converges_to_same_image(gc, orc, torch_cuda):
     assert np.array_equal(imgs[0], imgs[1])
 
 
-@pytest.mark.parametrize("lookahead,sync", [(0, True), (0, False), (1 << 20, True), (3, False)])
-def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, lookahead, sync):
+@pytest.mark.parametrize("lookahead,sync,reorder", [(0, True, 0), (0, False, 0), (1 << 20, True, 0), (3, False, 4),
+                                                    (0, True, 3)])
+def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, lookahead, sync, reorder):
     """Continuous batching (admission by pixel budget, one persistent launch
     per tick, skipped passes for views that cannot progress, retirement on
     convergence) gives every view the image it gets when rendered alone to
-    convergence, with the synchronous or the asynchronous loader and with the
-    first-miss or the lookahead request policy; the per-view status word
-    reports convergence exactly."""
+    convergence, with the synchronous or the asynchronous loader, with the
+    first-miss or the lookahead request policy and with arrival-order or
+    locality-ordered admission; the per-view status word reports convergence
+    exactly."""
     specs = [((64, 48), 1), ((33, 17), 4), ((96, 80), 7), ((40, 40), 10), ((80, 24), 5)]
     tf = scenario.ramp_tf()
     single = []
@@ -228,7 +230,7 @@ def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, lookahead, sy
     s.cm.close()
 
     s2 = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 64, sync=sync)
-    b = gc.Batch(s2.cm, max_views=3, max_pixels=96 * 80 + 64 * 48, lookahead=lookahead)
+    b = gc.Batch(s2.cm, max_views=3, max_pixels=96 * 80 + 64 * 48, lookahead=lookahead, reorder_window=reorder)
     bufs = []
     for i, ((W, H), cam) in enumerate(specs):
         g, _ = s2.buffers(W, H)
