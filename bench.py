@@ -478,6 +478,7 @@ def batched_pass(gc, torch, cfg, data, views, warm, args):
            "converged_views": f"{sum(1 for r in out if r[2])}/{len(views)}",
            "ticks_detail": {"render_ticks": b1.render_ticks - b0.render_ticks,
                             "install_ticks": b1.install_ticks - b0.install_ticks,
+                            "graph_replays": b1.graph_replays - b0.graph_replays,
                             "view_passes": b1.view_passes - b0.view_passes,
                             "render_ms": round(b1.render_ms - b0.render_ms, 2),
                             "tick_host_ms": round(b1.tick_ms - b0.tick_ms, 2),

@@ -126,4 +126,22 @@ void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams 
                    const ViewParams *views_host, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
                    uint32_t *err, cudaStream_t s);
 
+// An executable CUDA graph of the batched launch (view-table copy + ray caster).
+struct RenderGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t copy = nullptr, kern = nullptr;
+    void *func = nullptr;
+    uint32_t threads = 0;
+    uint64_t replays = 0;
+    RenderGraph() = default;
+    RenderGraph(const RenderGraph &) = delete;
+    RenderGraph &operator=(const RenderGraph &) = delete;
+    ~RenderGraph();
+    void reset();
+};
+void launch_render_graph(RenderGraph &g, const CacheView &cv, const LevelTables &lt, ViewParams *views_dev,
+                         const ViewParams *views_pinned, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
+                         cudaStream_t s);
+
 }  // namespace gc

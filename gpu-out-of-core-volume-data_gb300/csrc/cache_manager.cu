@@ -511,8 +511,10 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
     out.tile_shift = static_cast<uint32_t>(__builtin_ctz(tw));
 }
 
+// graph + pinned view table: the batched form replays a CUDA graph instead
+// of launching (launch_render_graph)
 static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s, uint32_t lookahead = 0,
-                   bool mark_done = false) {
+                   bool mark_done = false, RenderGraph *graph = nullptr, ViewParams *pinned = nullptr) {
     GC_REQUIRE(views && n >= 1, "no views");
     GC_REQUIRE(n <= C->max_views, "too many views in one batch");
     GC_REQUIRE(C->d.volume.channels == 1, "the ray caster renders single-channel volumes");
@@ -525,6 +527,11 @@ static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s
         vp[i].mark_done = mark_done ? 1u : 0u;
         vp[i].tile_begin = tiles;
         tiles += vp[i].tiles_x * div_up(views[i].height, 32u >> vp[i].tile_shift);
+    }
+    if (graph) {
+        std::memcpy(pinned, vp.data(), n * sizeof(ViewParams));
+        launch_render_graph(*graph, cache_view(C), C->lt, C->d_views, pinned, n, tiles, C->d_queue, s);
+        return;
     }
     // pageable source: the call returns once the data is staged
     GC_CUDA(cudaMemcpyAsync(C->d_views, vp.data(), n * sizeof(ViewParams), cudaMemcpyHostToDevice, s));
@@ -956,6 +963,8 @@ struct gc_batch {
     uint32_t last_misses = 0;       // missing bricks requested by the last scan (uncapped)
     cudaEvent_t ev = nullptr, ev_r0 = nullptr, ev_r1 = nullptr;
     gc_batch_stats st;
+    gc::RenderGraph graph;                // the replayed launch
+    gc::ViewParams *h_views = nullptr;    // pinned view table the graph copies
 };
 
 namespace gc {
@@ -963,6 +972,7 @@ static void batch_destroy(gc_batch *b) {
     if (!b) return;
     if (b->d_status) cudaFree(b->d_status);
     if (b->h_status) cudaFreeHost(b->h_status);
+    if (b->h_views) cudaFreeHost(b->h_views);
     if (b->ev) cudaEventDestroy(b->ev);
     if (b->ev_r0) cudaEventDestroy(b->ev_r0);
     if (b->ev_r1) cudaEventDestroy(b->ev_r1);
@@ -984,6 +994,7 @@ int gc_batch_create(gc_cache_t C, const gc_batch_desc *desc, gc_batch_t *out) {
         b->d = *desc;
         b->d_status = dalloc<uint32_t>(desc->max_views, "batch status");
         b->h_status = halloc<uint32_t>(desc->max_views + 1);
+        b->h_views = halloc<ViewParams>(desc->max_views);
         GC_CUDA(cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming));
         GC_CUDA(cudaEventCreate(&b->ev_r0));
         GC_CUDA(cudaEventCreate(&b->ev_r1));
@@ -1102,7 +1113,7 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         }
         GC_CUDA(cudaMemsetAsync(b->d_status, 0, n * sizeof(uint32_t), s));
         GC_CUDA(cudaEventRecord(b->ev_r0, s));
-        render(C, views.data(), n, s, b->d.lookahead, true);
+        render(C, views.data(), n, s, b->d.lookahead, true, &b->graph, b->h_views);
         GC_CUDA(cudaEventRecord(b->ev_r1, s));
         GC_CUDA(cudaMemcpyAsync(b->h_status, b->d_status, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         const bool scanned = batch_update(C, s);
@@ -1146,6 +1157,7 @@ int gc_batch_stats_get(gc_batch_t b, gc_batch_stats *out) {
     return guard([&] {
         GC_REQUIRE(b && out, "null argument");
         *out = b->st;
+        out->graph_replays = b->graph.replays;
     });
 }
 

@@ -638,16 +638,20 @@ int gc_render_tuning_get(uint32_t out[4]) {
 
 namespace gc {
 
-void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams *views_dev,
-                   const ViewParams * /*views_host*/, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
-                   uint32_t * /*err*/, cudaStream_t s) {
-    if (total_tiles == 0) return;
+// Kernel, grid and block of one ray-caster launch under the current tuning:
+// a persistent grid of at most (SMs x resident blocks) that takes its work
+// from the launch's tile queue.
+struct RenderLaunch {
+    void *func;
+    uint32_t grid, threads;
+};
+static RenderLaunch render_launch_config(uint32_t eb, uint32_t total_tiles) {
     const RenderTuning tune = render_tuning();
     const uint32_t threads = tune.threads;
     GC_REQUIRE(threads == 64 || threads == 128 || threads == 256, "render threads must be 64, 128 or 256");
     static int occupancy[2][3][3] = {};
     const int tslot = threads == 64 ? 0 : (threads == 128 ? 1 : 2);
-    auto launch = [&](auto kernel, int sched, int slot) {
+    auto config = [&](auto kernel, int sched, int slot) {
         int &occ = occupancy[sched][slot][tslot];
         if (!occ) {
             int b = 0;
@@ -658,24 +662,78 @@ void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams 
         if (tune.blocks_per_sm > 0) per_sm = std::min(per_sm, static_cast<int>(tune.blocks_per_sm));
         const uint32_t max_blocks = static_cast<uint32_t>(sm_count() * per_sm);
         const uint32_t want = div_up(total_tiles, threads / 32);
-        const uint32_t grid = std::max(1u, std::min(max_blocks, want));
-        kernel<<<grid, threads, 0, s>>>(cv, lt, views_dev, nviews, total_tiles, queue, grid * (threads / 32));
-        GC_CUDA(cudaGetLastError());
-        count_launch();
+        return RenderLaunch{reinterpret_cast<void *>(kernel), std::max(1u, std::min(max_blocks, want)), threads};
     };
     const bool pix = tune.scheduler == 1;
-    switch (cv.eb) {
-        case 1:
-            pix ? launch(render_pixels_kernel<uint8_t>, 1, 0) : launch(render_kernel<uint8_t>, 0, 0);
-            break;
-        case 2:
-            pix ? launch(render_pixels_kernel<uint16_t>, 1, 1) : launch(render_kernel<uint16_t>, 0, 1);
-            break;
-        case 4:
-            pix ? launch(render_pixels_kernel<float>, 1, 2) : launch(render_kernel<float>, 0, 2);
-            break;
+    switch (eb) {
+        case 1: return pix ? config(render_pixels_kernel<uint8_t>, 1, 0) : config(render_kernel<uint8_t>, 0, 0);
+        case 2: return pix ? config(render_pixels_kernel<uint16_t>, 1, 1) : config(render_kernel<uint16_t>, 0, 1);
+        case 4: return pix ? config(render_pixels_kernel<float>, 1, 2) : config(render_kernel<float>, 0, 2);
         default: fail(GC_ERR_UNSUPPORTED, "the ray caster supports one channel of 1, 2 or 4 bytes");
     }
+}
+
+void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams *views_dev,
+                   const ViewParams * /*views_host*/, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
+                   uint32_t * /*err*/, cudaStream_t s) {
+    if (total_tiles == 0) return;
+    const RenderLaunch L = render_launch_config(cv.eb, total_tiles);
+    uint32_t nwarps = L.grid * (L.threads / 32);
+    void *args[] = {const_cast<CacheView *>(&cv), const_cast<LevelTables *>(&lt), &views_dev, &nviews, &total_tiles,
+                    &queue, &nwarps};
+    GC_CUDA(cudaLaunchKernel(L.func, dim3(L.grid), dim3(L.threads), args, 0, s));
+    count_launch();
+}
+
+RenderGraph::~RenderGraph() { reset(); }
+
+void RenderGraph::reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    func = nullptr;
+}
+
+// The batched form's launch: an instantiated graph of two nodes -- the copy of
+// the view table from pinned host memory and the persistent ray caster -- is
+// replayed every tick; only the kernel's arguments (timestamp, view and tile
+// counts, grid) and the copy's size change, through the executable graph's
+// node-update calls.  The graph is rebuilt when the tuning changes the kernel.
+void launch_render_graph(RenderGraph &g, const CacheView &cv, const LevelTables &lt, ViewParams *views_dev,
+                         const ViewParams *views_pinned, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
+                         cudaStream_t s) {
+    if (total_tiles == 0) return;
+    const RenderLaunch L = render_launch_config(cv.eb, total_tiles);
+    uint32_t nwarps = L.grid * (L.threads / 32);
+    const ViewParams *vd = views_dev;
+    void *args[] = {const_cast<CacheView *>(&cv), const_cast<LevelTables *>(&lt), &vd, &nviews, &total_tiles,
+                    &queue, &nwarps};
+    cudaKernelNodeParams kp = {};
+    kp.func = L.func;
+    kp.gridDim = dim3(L.grid);
+    kp.blockDim = dim3(L.threads);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    const size_t bytes = static_cast<size_t>(nviews) * sizeof(ViewParams);
+    if (g.exec && (g.func != L.func || g.threads != L.threads)) g.reset();
+    if (!g.exec) {
+        GC_CUDA(cudaGraphCreate(&g.graph, 0));
+        GC_CUDA(cudaGraphAddMemcpyNode1D(&g.copy, g.graph, nullptr, 0, views_dev, views_pinned, bytes,
+                                         cudaMemcpyHostToDevice));
+        GC_CUDA(cudaGraphAddKernelNode(&g.kern, g.graph, &g.copy, 1, &kp));
+        GC_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
+        g.func = L.func;
+        g.threads = L.threads;
+    } else {
+        GC_CUDA(cudaGraphExecMemcpyNodeSetParams1D(g.exec, g.copy, views_dev, views_pinned, bytes,
+                                                   cudaMemcpyHostToDevice));
+        GC_CUDA(cudaGraphExecKernelNodeSetParams(g.exec, g.kern, &kp));
+    }
+    GC_CUDA(cudaGraphLaunch(g.exec, s));
+    g.replays++;
+    count_launch();
 }
 
 }  // namespace gc

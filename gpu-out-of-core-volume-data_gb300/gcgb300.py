@@ -89,7 +89,8 @@ class BatchDesc(C.Structure):
 
 class BatchStats(C.Structure):
     _fields_ = [("ticks", C.c_uint64), ("render_ticks", C.c_uint64), ("view_passes", C.c_uint64),
-                ("install_ticks", C.c_uint64), ("render_ms", C.c_double), ("tick_ms", C.c_double),
+                ("install_ticks", C.c_uint64), ("graph_replays", C.c_uint64), ("render_ms", C.c_double),
+                ("tick_ms", C.c_double),
                 ("wait_ms", C.c_double)]
 
 

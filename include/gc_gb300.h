@@ -417,7 +417,9 @@ int gc_batch_destroy(gc_batch_t batch);
  * state are the batch's scratch: a finished ray leaves -1 - t in tbuf so
  * that later passes skip its pixel; rgba holds the image. */
 int gc_batch_submit(gc_batch_t batch, const gc_view *view, uint64_t tag);
-/* One tick.  Outputs (optional): views active during the tick, views queued after it. */
+/* One tick.  The render of a tick replays the batch's instantiated CUDA graph
+ * (its view-table copy and persistent ray-caster nodes updated in place).
+ * Outputs (optional): views active during the tick, views queued after it. */
 int gc_batch_tick(gc_batch_t batch, void *stream, uint32_t *active, uint32_t *queued);
 /* Retrieve up to max retired views (oldest first). */
 int gc_batch_poll(gc_batch_t batch, gc_batch_result *out, uint32_t max, uint32_t *n);
@@ -427,6 +429,8 @@ typedef struct gc_batch_stats {
     uint64_t render_ticks;    /* ticks that rendered (one launch each)         */
     uint64_t view_passes;     /* views rendered, summed over ticks             */
     uint64_t install_ticks;   /* ticks that installed bricks                   */
+    uint64_t graph_replays;   /* render launches replayed from the batch's CUDA
+                                 graph (view-table copy + persistent ray caster) */
     double render_ms;         /* device time of the render launches            */
     double tick_ms;           /* host time inside gc_batch_tick                */
     double wait_ms;           /* host time waiting for the loader              */

@@ -248,5 +248,7 @@ def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, lookahead, sy
     torch_cuda.cuda.synchronize()
     for i in range(len(specs)):
         assert np.array_equal(bufs[i][0].cpu().numpy(), single[i]), i
+    st = b.stats()
+    assert st.graph_replays == st.render_ticks > 0  # every batched render replayed the graph
     b.close()
     assert s2.cm.stats().device_error == 0
