@@ -21,12 +21,20 @@
 
 namespace gc {
 
+// Levels of every volume the cache holds, concatenated (volume 0's levels
+// first): a cache over several volumes is one page directory whose levels
+// are those of all of its volumes, with one pool, one LRU and one request
+// scan (the serving form's shared pool).
+constexpr uint32_t kMaxCacheLevels = 4 * GC_MAX_LEVELS;
+
 struct LevelTables {
     uint32_t nlevels;
-    uint32_t off[GC_MAX_LEVELS];        // MRPD x offset of each level
-    uint32_t nb[GC_MAX_LEVELS][3];      // bricks per axis (MRPD level dimensions)
-    uint32_t vvox[GC_MAX_LEVELS][3];    // virtualized voxels per axis (= real sizes)
-    float ior[GC_MAX_LEVELS][3];        // initial / real size (CacheManager.hpp:271-285)
+    uint32_t off[kMaxCacheLevels];        // MRPD x offset of each level
+    uint32_t nb[kMaxCacheLevels][3];      // bricks per axis (MRPD level dimensions)
+    uint32_t vvox[kMaxCacheLevels][3];    // virtualized voxels per axis (= real sizes)
+    float ior[kMaxCacheLevels][3];        // initial / real size (CacheManager.hpp:271-285)
+    uint32_t eb[kMaxCacheLevels];         // bytes per voxel of the level's volume
+    uint32_t bb[kMaxCacheLevels][3];      // big-brick size (in bricks) of the level's volume
 };
 
 struct CacheView {
@@ -36,7 +44,9 @@ struct CacheView {
     const uint8_t *pool;
     uint32_t mx, my, mz;
     uint32_t sx, sy, sz;
-    uint32_t B, c, Beff, eb;
+    uint32_t B, c, Beff;
+    uint32_t eb;          // bytes per voxel of every volume, 0 when the volumes differ
+    uint64_t slot_bytes;  // pool slot stride: B^3 x the widest voxel
     uint32_t ts;
 };
 
@@ -60,6 +70,9 @@ struct ViewParams {
     uint32_t tiles_x;                   // warp tiles per row
     uint32_t tile_shift;                // log2 of the tile width
     uint32_t tile_begin;                // first global tile index of this view
+    uint32_t level_base;                // first cache level of the view's volume
+    uint32_t nlevels;                   // levels of the view's volume
+    uint32_t eb;                        // bytes per voxel of the view's volume
     uint32_t lookahead;                 // extra missing bricks a stopped ray requests (0: none)
     uint32_t mark_done;                 // batched passes: a finished ray leaves -1 - t in tbuf and
                                         // later passes skip its pixel (rgba already final)
@@ -95,9 +108,10 @@ struct InstallArgs {
     uint32_t *slot_level;
     float4 *slot_vpos;
     uint8_t *pool;
+    uint64_t slot_bytes;       // pool slot stride
+    uint64_t big_stride;       // staging stride of one big brick
     uint32_t sx, sy;
-    uint32_t B, Beff, eb;
-    uint32_t BB[3];
+    uint32_t B, Beff;
     const uint4 *asked;        // partitioned asked list: non-empty first
     const uint32_t *big_index; // per non-empty brick
     const uint4 *big_coord;    // per loaded big brick
@@ -105,11 +119,11 @@ struct InstallArgs {
     uint32_t n, n_nonempty;
 };
 void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s);
-// Copies n blocks of `bytes` bytes from src + off[i] (device-readable host
-// memory) to dst + i * bytes; vec16: src, every offset and bytes are
-// multiples of 16.
-void launch_gather_bricks(const uint8_t *src, const uint64_t *off, uint32_t n, uint64_t bytes, uint8_t *dst,
-                          bool vec16, cudaStream_t s);
+// Copies brick i (src[i] = {device-readable host address, bytes}) to
+// dst + i * stride; vec16: every address, size and the stride are multiples
+// of 16.
+void launch_gather_bricks(const ulonglong2 *src, uint32_t n, uint64_t stride, uint8_t *dst, bool vec16,
+                          cudaStream_t s);
 void launch_completude(const float4 *slot_vpos, uint32_t nslots, uint32_t *count, cudaStream_t s);
 
 // Ray caster (render.cu).  Launch configuration of the ray caster, process

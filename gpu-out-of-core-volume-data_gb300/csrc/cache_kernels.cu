@@ -272,14 +272,15 @@ __global__ void __launch_bounds__(256) install_place_kernel(InstallArgs a, const
         a.slot_level[slot] = b.w;
         a.slot_vpos[slot] = brick_origin(lt, b, one_over_beff);
     }
-    const uint32_t B = a.B, eb = a.eb;
-    const uint32_t bvx = a.BB[0] * B, bvy = a.BB[1] * B, bvz = a.BB[2] * B;
-    const uint64_t big_bytes = static_cast<uint64_t>(bvx) * bvy * bvz * eb;
+    // the brick's volume: voxel width and big-brick shape of its level
+    const uint32_t B = a.B, eb = lt.eb[b.w];
+    const uint32_t *BB = lt.bb[b.w];
+    const uint32_t bvx = BB[0] * B, bvy = BB[1] * B;
     const uint32_t bi = a.big_index[i];
     const uint4 bc = a.big_coord[bi];
-    const uint32_t ox = (b.x - bc.x * a.BB[0]) * B, oy = (b.y - bc.y * a.BB[1]) * B, oz = (b.z - bc.z * a.BB[2]) * B;
-    const uint8_t *src = a.staging + bi * big_bytes;
-    uint8_t *dst = a.pool + static_cast<uint64_t>(slot) * B * B * B * eb;
+    const uint32_t ox = (b.x - bc.x * BB[0]) * B, oy = (b.y - bc.y * BB[1]) * B, oz = (b.z - bc.z * BB[2]) * B;
+    const uint8_t *src = a.staging + bi * a.big_stride;
+    uint8_t *dst = a.pool + static_cast<uint64_t>(slot) * a.slot_bytes;
     const uint32_t row_bytes = B * eb;
     const uint32_t rows = B * B;
     if (row_bytes % 16 == 0 && (reinterpret_cast<uintptr_t>(src) % 16 == 0) && ((bvx * eb) % 16 == 0)) {
@@ -405,12 +406,14 @@ void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s)
 // Four independent loads per thread are in flight before their stores: the
 // host link's latency (microseconds) needs many bytes in flight per SM.
 template <typename W>
-__global__ void gather_bricks_kernel(const uint8_t *__restrict__ src, const uint64_t *__restrict__ off, uint32_t n,
-                                     uint64_t words, uint8_t *__restrict__ dst) {
+__global__ void gather_bricks_kernel(const ulonglong2 *__restrict__ src, uint32_t n, uint64_t stride,
+                                     uint8_t *__restrict__ dst) {
     constexpr uint32_t kIlp = 4;
     for (uint32_t b = blockIdx.x; b < n; b += gridDim.x) {
-        const W *sp = reinterpret_cast<const W *>(src + off[b]);
-        W *dp = reinterpret_cast<W *>(dst) + static_cast<uint64_t>(b) * words;
+        const ulonglong2 e = src[b];  // {address, bytes}
+        const W *sp = reinterpret_cast<const W *>(e.x);
+        W *dp = reinterpret_cast<W *>(dst + static_cast<uint64_t>(b) * stride);
+        const uint64_t words = e.y / sizeof(W);
         const uint64_t stride = static_cast<uint64_t>(blockDim.x) * kIlp;
         for (uint64_t i0 = threadIdx.x; i0 < words; i0 += stride) {
             W v[kIlp];
@@ -428,17 +431,17 @@ __global__ void gather_bricks_kernel(const uint8_t *__restrict__ src, const uint
     }
 }
 
-void launch_gather_bricks(const uint8_t *src, const uint64_t *off, uint32_t n, uint64_t bytes, uint8_t *dst,
-                          bool vec16, cudaStream_t s) {
+void launch_gather_bricks(const ulonglong2 *src, uint32_t n, uint64_t stride, uint8_t *dst, bool vec16,
+                          cudaStream_t s) {
     if (n == 0) return;
     // one block of 256 per SM (four 16-byte loads in flight per thread)
     // saturates the host link; more would only take SM slots from the ray
     // caster running beside it
     const uint32_t grid = std::min<uint32_t>(n, static_cast<uint32_t>(sm_count()));
     if (vec16)
-        gather_bricks_kernel<uint4><<<grid, 256, 0, s>>>(src, off, n, bytes / 16, dst);
+        gather_bricks_kernel<uint4><<<grid, 256, 0, s>>>(src, n, stride, dst);
     else
-        gather_bricks_kernel<uint8_t><<<grid, 256, 0, s>>>(src, off, n, bytes, dst);
+        gather_bricks_kernel<uint8_t><<<grid, 256, 0, s>>>(src, n, stride, dst);
     GC_CUDA(cudaGetLastError());
     count_launch();
 }

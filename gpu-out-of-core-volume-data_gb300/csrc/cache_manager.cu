@@ -78,13 +78,28 @@ struct Source {
     std::unordered_set<uint64_t> empty;
 };
 
+// One volume of the cache: its levels are cache levels
+// [level_base, level_base + layout.nb_levels).
+struct Volume {
+    gc_volume_desc desc;
+    gc_layout layout;
+    uint32_t level_base = 0;
+    uint64_t brick_bytes = 0, big_bytes = 0;
+    Source src;
+};
+
 }  // namespace gc
 
 struct gc_cache {
-    gc_cache_desc d;
+    gc_cache_desc d;                  // d.volume / d.layout: volume 0
+    std::vector<gc::Volume> vols;
+    std::vector<uint32_t> level_volume;  // volume of each cache level
     gc::LevelTables lt;
-    uint32_t mx = 0, my = 0, mz = 0, nslots = 0, B = 0, c = 0, Beff = 0, eb = 0;
-    uint64_t nentries = 0, brick_bytes = 0, big_bytes = 0;
+    uint32_t mx = 0, my = 0, mz = 0, nslots = 0, B = 0, c = 0, Beff = 0;
+    uint32_t eb = 0;                  // voxel bytes of every volume, 0 when they differ
+    uint64_t nentries = 0;
+    uint64_t slot_bytes = 0;          // pool slot: B^3 x the widest voxel
+    uint64_t big_stride = 0;          // staging stride: the largest big brick
     int device = 0;
     // device buffers
     uint4 *mrpd = nullptr;
@@ -96,14 +111,14 @@ struct gc_cache {
     uint32_t *d_count = nullptr, *d_misc = nullptr, *d_queue = nullptr;
     uint4 *d_list = nullptr, *d_asked = nullptr, *d_big_coord = nullptr;
     uint32_t *d_big_index = nullptr;
-    uint64_t *d_src_off = nullptr;
+    ulonglong2 *d_src = nullptr;      // gather list: {host address, bytes} per big brick
     uint8_t *d_staging = nullptr;
     gc::ViewParams *d_views = nullptr;
     uint32_t max_views = 256;
     // pinned host buffers
     uint4 *h_list = nullptr, *h_asked = nullptr, *h_big_coord = nullptr;
     uint32_t *h_total = nullptr, *h_big_index = nullptr, *h_misc = nullptr;
-    uint64_t *h_src_off = nullptr;
+    ulonglong2 *h_src = nullptr;
     uint8_t *h_staging = nullptr;
     cudaStream_t side = nullptr;
     cudaStream_t frame_stream = nullptr;  // stream of the update in progress (synchronous loader)
@@ -112,7 +127,8 @@ struct gc_cache {
     int cur = 0;
     uint32_t ts = 1, epoch_lru = 0, epoch_miss = 0;
     // loader
-    gc::Source src;
+    bool gather = false;              // every host-store volume is read by the gather kernel
+    bool vec16 = false;
     std::thread th;
     std::mutex mu;
     std::condition_variable cv;
@@ -127,25 +143,33 @@ struct gc_cache {
 namespace gc {
 
 static void build_tables(gc_cache *C) {
-    const gc_layout &L = C->d.layout;
     LevelTables &lt = C->lt;
     std::memset(&lt, 0, sizeof(lt));
-    lt.nlevels = L.nb_levels;
-    uint32_t off = 0;
+    C->level_volume.clear();
+    uint32_t off = 0, l = 0;
     C->mx = 0;
     C->my = 0;
     C->mz = 0;
-    for (uint32_t l = 0; l < L.nb_levels; ++l) {
-        lt.off[l] = off;
-        for (int a = 0; a < 3; ++a) {
-            lt.nb[l][a] = L.nb_bricks[l][a];
-            lt.vvox[l][a] = L.nb_bricks[l][a] * C->Beff;
-            lt.ior[l][a] = static_cast<float>(L.initial[l][a]) / static_cast<float>(L.real[l][a]);
+    for (uint32_t v = 0; v < C->vols.size(); ++v) {
+        Volume &V = C->vols[v];
+        const gc_layout &L = V.layout;
+        V.level_base = l;
+        for (uint32_t k = 0; k < L.nb_levels; ++k, ++l) {
+            lt.off[l] = off;
+            for (int a = 0; a < 3; ++a) {
+                lt.nb[l][a] = L.nb_bricks[k][a];
+                lt.vvox[l][a] = L.nb_bricks[k][a] * C->Beff;
+                lt.ior[l][a] = static_cast<float>(L.initial[k][a]) / static_cast<float>(L.real[k][a]);
+                lt.bb[l][a] = V.desc.big_brick_size[a];
+            }
+            lt.eb[l] = V.desc.encoded_bytes;
+            off += L.nb_bricks[k][0];
+            C->my = std::max(C->my, L.nb_bricks[k][1]);
+            C->mz = std::max(C->mz, L.nb_bricks[k][2]);
+            C->level_volume.push_back(v);
         }
-        off += L.nb_bricks[l][0];
-        C->my = std::max(C->my, L.nb_bricks[l][1]);
-        C->mz = std::max(C->mz, L.nb_bricks[l][2]);
     }
+    lt.nlevels = l;
     C->mx = off;
 }
 
@@ -153,8 +177,6 @@ static void build_tables(gc_cache *C) {
 // Returns the number of bricks to install (non-empty first), or 0.
 static void resolve_and_upload(gc_cache *C, uint32_t n) {
     const auto t_begin = std::chrono::steady_clock::now();
-    const gc_volume_desc &v = C->d.volume;
-    const uint32_t BB[3] = {v.big_brick_size[0], v.big_brick_size[1], v.big_brick_size[2]};
     std::unordered_map<uint64_t, int32_t> asked;
     std::vector<int> kind(n, 0);  // 0 non-empty, 1 empty, 2 unknown (dropped)
     uint32_t n_nonempty = 0, nbig = 0;
@@ -163,10 +185,15 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     struct Copy {
         const uint8_t *src;
         uint8_t *dst;
+        uint64_t bytes;
     };
     std::vector<Copy> copies;
+    uint64_t bytes_up = 0;
     for (uint32_t i = 0; i < n; ++i) {
-        const uint4 b = C->h_list[i];
+        const uint4 b = C->h_list[i];  // (x, y, z, cache level)
+        const Volume &V = C->vols[C->level_volume[b.w < C->lt.nlevels ? b.w : 0]];
+        const uint32_t lvl = b.w - V.level_base;  // level within the volume
+        const uint32_t *BB = V.desc.big_brick_size;
         const uint32_t gx = b.x / BB[0], gy = b.y / BB[1], gz = b.z / BB[2];
         const uint64_t key = gc_brick_key(b.w, gx, gy, gz);
         auto it = asked.find(key);
@@ -183,26 +210,28 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
             continue;
         }
         int status = GC_BRICK_UNKNOWN;
-        if (C->src.empty.count(key)) {
+        const Source &src = V.src;
+        uint8_t *stage = C->h_staging + static_cast<uint64_t>(nbig) * C->big_stride;
+        if (src.empty.count(gc_brick_key(lvl, gx, gy, gz))) {  // the volume's own brick keys
             status = GC_BRICK_EMPTY;
-        } else if (C->src.kind == 1) {
-            const gc_layout &L = C->d.layout;
-            if (b.w < L.nb_levels && gx < L.nb_big_bricks[b.w][0] && gy < L.nb_big_bricks[b.w][1] &&
-                gz < L.nb_big_bricks[b.w][2]) {
+        } else if (src.kind == 1) {
+            const gc_layout &L = V.layout;
+            if (lvl < L.nb_levels && gx < L.nb_big_bricks[lvl][0] && gy < L.nb_big_bricks[lvl][1] &&
+                gz < L.nb_big_bricks[lvl][2]) {
                 const uint64_t idx =
-                    (static_cast<uint64_t>(gz) * L.nb_big_bricks[b.w][1] + gy) * L.nb_big_bricks[b.w][0] + gx;
-                const uint64_t off = C->src.level_off[b.w] + idx * C->big_bytes;  // inside the store (checked)
-                if (C->src.direct)
-                    C->h_src_off[nbig] = off;
+                    (static_cast<uint64_t>(gz) * L.nb_big_bricks[lvl][1] + gy) * L.nb_big_bricks[lvl][0] + gx;
+                const uint64_t off = src.level_off[lvl] + idx * V.big_bytes;  // inside the store (checked)
+                if (C->gather)
+                    C->h_src[nbig] = make_ulonglong2(reinterpret_cast<uint64_t>(src.dev + off), V.big_bytes);
                 else
-                    copies.push_back({C->src.host + off, C->h_staging + static_cast<uint64_t>(nbig) * C->big_bytes});
+                    copies.push_back({src.host + off, stage, V.big_bytes});
                 status = GC_BRICK_SUCCESS;
             }
-        } else if (C->src.kind == 2) {
-            status = C->src.fn(C->src.user, b.w, gx, gy, gz,
-                               C->h_staging + static_cast<uint64_t>(nbig) * C->big_bytes, C->big_bytes);
+        } else if (src.kind == 2) {
+            status = src.fn(src.user, lvl, gx, gy, gz, stage, V.big_bytes);
         }
         if (status == GC_BRICK_SUCCESS) {
+            bytes_up += V.big_bytes;
             asked[key] = static_cast<int32_t>(nbig);
             C->h_big_coord[nbig] = make_uint4(gx, gy, gz, b.w);
             big_index.push_back(nbig);
@@ -223,12 +252,12 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     // Host-store bricks are copied into the pinned staging buffer by up to 8
     // threads (one memcpy stream saturates well below the host's bandwidth).
     if (!copies.empty()) {
-        const size_t bytes = copies.size() * C->big_bytes;
+        const size_t bytes = copies.size() * C->big_stride;
         const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
         const unsigned nt = static_cast<unsigned>(
             std::min<size_t>(std::min(8u, hw), std::max<size_t>(1, bytes >> 21)));  // >= 2 MiB per thread
         auto work = [&](unsigned t) {
-            for (size_t i = t; i < copies.size(); i += nt) std::memcpy(copies[i].dst, copies[i].src, C->big_bytes);
+            for (size_t i = t; i < copies.size(); i += nt) std::memcpy(copies[i].dst, copies[i].src, copies[i].bytes);
         };
         if (nt <= 1) {
             work(0);
@@ -256,14 +285,14 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     // ahead of the next frame's render: on a side stream it can wait behind a
     // persistent ray-caster launch that holds every SM.  Staged copies (copy
     // engine) and the asynchronous loader use the high-priority side stream.
-    const bool gather = C->src.kind == 1 && C->src.direct;
+    const bool gather = C->gather;
     cudaStream_t s = C->sync_mode() && gather ? C->frame_stream : C->side;
     GC_CUDA(cudaEventRecord(C->ev_upload_begin, s));
     if (nbig && gather) {
-        GC_CUDA(cudaMemcpyAsync(C->d_src_off, C->h_src_off, nbig * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
-        launch_gather_bricks(C->src.dev, C->d_src_off, nbig, C->big_bytes, C->d_staging, C->src.vec16, s);
+        GC_CUDA(cudaMemcpyAsync(C->d_src, C->h_src, nbig * sizeof(ulonglong2), cudaMemcpyHostToDevice, s));
+        launch_gather_bricks(C->d_src, nbig, C->big_stride, C->d_staging, C->vec16, s);
     } else if (nbig) {
-        GC_CUDA(cudaMemcpyAsync(C->d_staging, C->h_staging, static_cast<size_t>(nbig) * C->big_bytes,
+        GC_CUDA(cudaMemcpyAsync(C->d_staging, C->h_staging, static_cast<size_t>(nbig) * C->big_stride,
                                 cudaMemcpyHostToDevice, s));
     }
     GC_CUDA(cudaMemcpyAsync(C->d_asked, C->h_asked, k * sizeof(uint4), cudaMemcpyHostToDevice, s));
@@ -275,7 +304,7 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     }
     GC_CUDA(cudaEventRecord(C->ev_upload, s));
     C->upload_timed = true;
-    C->stats.bytes_h2d += static_cast<uint64_t>(nbig) * C->big_bytes;
+    C->stats.bytes_h2d += bytes_up;
     C->stats.requests_served += n;
 }
 
@@ -343,6 +372,7 @@ static CacheView cache_view(const gc_cache *C) {
     cv.c = C->c;
     cv.Beff = C->Beff;
     cv.eb = C->eb;
+    cv.slot_bytes = C->slot_bytes;
     cv.ts = C->ts;
     return cv;
 }
@@ -371,8 +401,8 @@ static void install(gc_cache *C, cudaStream_t s) {
     a.sy = C->d.cache_size[1];
     a.B = C->B;
     a.Beff = C->Beff;
-    a.eb = C->eb;
-    for (int i = 0; i < 3; ++i) a.BB[i] = C->d.volume.big_brick_size[i];
+    a.slot_bytes = C->slot_bytes;
+    a.big_stride = C->big_stride;
     a.asked = C->d_asked;
     a.big_index = C->d_big_index;
     a.big_coord = C->d_big_coord;
@@ -453,11 +483,11 @@ static void destroy(gc_cache *C) {
     cudaDeviceSynchronize();
     void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool,
                    C->status_lru, C->status_miss, C->ctl_lru, C->ctl_miss, C->d_count, C->d_misc, C->d_queue,
-                   C->d_list, C->d_asked, C->d_big_coord, C->d_big_index, C->d_src_off, C->d_staging, C->d_views};
+                   C->d_list, C->d_asked, C->d_big_coord, C->d_big_index, C->d_src, C->d_staging, C->d_views};
     for (void *p : dev)
         if (p) cudaFree(p);
     void *host[] = {C->h_list,  C->h_asked, C->h_big_coord, C->h_total,
-                    C->h_big_index, C->h_misc, C->h_src_off, C->h_staging};
+                    C->h_big_index, C->h_misc, C->h_src, C->h_staging};
     for (void *p : host)
         if (p) cudaFreeHost(p);
     if (C->ev_list) cudaEventDestroy(C->ev_list);
@@ -475,7 +505,9 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
     GC_REQUIRE(in.tstep > 0.f, "tstep must be > 0");
     GC_REQUIRE(in.mode == GC_MODE_DVR || in.mode == GC_MODE_MOP, "bad compositing mode");
     GC_REQUIRE(in.sampler == GC_SAMPLER_REFERENCE || in.sampler == GC_SAMPLER_TRILINEAR, "bad sampler");
-    GC_REQUIRE(C->c >= 1 || in.sampler == GC_SAMPLER_REFERENCE || true, "");
+    GC_REQUIRE(in.volume < C->vols.size(), "the view's volume is not in this cache");
+    const Volume &V = C->vols[in.volume];
+    GC_REQUIRE(V.desc.channels == 1, "the ray caster renders single-channel volumes");
     std::memset(&out, 0, sizeof(out));
     std::memcpy(out.m, in.inv_view, sizeof(out.m));
     out.W = in.width;
@@ -499,7 +531,10 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
     const float bsy = in.bbox_max[1] - in.bbox_min[1];
     const float bsz = in.bbox_max[2] - in.bbox_min[2];
     const float bmin = std::min(bsx, std::min(bsy, bsz));
-    const gc_layout &L = C->d.layout;
+    const gc_layout &L = V.layout;
+    out.level_base = V.level_base;
+    out.nlevels = L.nb_levels;
+    out.eb = V.desc.encoded_bytes;
     for (uint32_t l = 0; l < L.nb_levels; ++l) {
         for (int a = 0; a < 3; ++a) out.inv_size[l][a] = bmin / static_cast<float>(L.initial[l][a]);
         const uint32_t mn = std::min(L.initial[l][0], std::min(L.initial[l][1], L.initial[l][2]));
@@ -517,7 +552,6 @@ static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s
                    bool mark_done = false, RenderGraph *graph = nullptr, ViewParams *pinned = nullptr) {
     GC_REQUIRE(views && n >= 1, "no views");
     GC_REQUIRE(n <= C->max_views, "too many views in one batch");
-    GC_REQUIRE(C->d.volume.channels == 1, "the ray caster renders single-channel volumes");
     GC_CUDA(cudaSetDevice(C->device));
     std::vector<ViewParams> vp(n);
     uint32_t tiles = 0;
@@ -538,6 +572,78 @@ static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s
     launch_render(cache_view(C), C->lt, C->d_views, vp.data(), n, tiles, C->d_queue, nullptr, s);
 }
 
+// Upload route of the cache: the gather kernel when every volume with a host
+// store can be read by the device and no volume loads through a callback
+// (callbacks fill the pinned staging buffer); staged copies otherwise.
+static void update_upload_route(gc_cache *C) {
+    bool any = false, all = true, vec16 = C->big_stride % 16 == 0;
+    for (const Volume &V : C->vols) {
+        if (V.src.kind == 2) all = false;
+        if (V.src.kind == 1) {
+            any = true;
+            all = all && V.src.direct;
+            vec16 = vec16 && V.src.vec16;
+        }
+    }
+    C->gather = any && all;
+    C->vec16 = vec16;
+}
+
+static bool has_source(const gc_cache *C) {
+    for (const Volume &V : C->vols)
+        if (V.src.kind != 0) return true;
+    return false;
+}
+
+// A cache over n volumes (the first one described by desc): one page
+// directory holding the levels of all of them, one pool, one LRU.
+static gc_cache *create_cache(const gc_cache_desc *desc, const gc_volume_desc *vols, const gc_layout *layouts,
+                              uint32_t n) {
+    GC_REQUIRE(n >= 1 && n <= kMaxCacheLevels / GC_MAX_LEVELS, "a cache holds 1 to 4 volumes");
+    uint32_t total_levels = 0;
+    for (uint32_t v = 0; v < n; ++v) {
+        validate_volume(vols[v]);
+        GC_REQUIRE(layouts[v].nb_levels >= 1 && layouts[v].nb_levels <= GC_MAX_LEVELS, "bad layout");
+        GC_REQUIRE(vols[v].brick_size == vols[0].brick_size && vols[v].covering == vols[0].covering,
+                   "volumes sharing a pool need the same BrickSize and VoxelCovering");
+        total_levels += layouts[v].nb_levels;
+    }
+    GC_REQUIRE(total_levels <= kMaxCacheLevels, "too many levels in one cache");
+    GC_REQUIRE(desc->max_requests >= 1 && desc->max_requests <= 16384, "max_requests must be in [1, 16384]");
+    for (int a = 0; a < 3; ++a) GC_REQUIRE(desc->cache_size[a] >= 1, "cache size must be >= 1");
+    gc_cache *C = new gc_cache();
+    try {
+        std::memset(&C->stats, 0, sizeof(C->stats));
+        C->d = *desc;
+        C->d.volume = vols[0];
+        C->d.layout = layouts[0];
+        C->device = desc->gpu;
+        GC_CUDA(cudaSetDevice(C->device));
+        C->B = vols[0].brick_size;
+        C->c = vols[0].covering;
+        C->Beff = C->B - 2 * C->c;
+        C->eb = vols[0].encoded_bytes;
+        uint32_t eb_max = 0;
+        C->vols.resize(n);
+        for (uint32_t v = 0; v < n; ++v) {
+            Volume &V = C->vols[v];
+            V.desc = vols[v];
+            V.layout = layouts[v];
+            V.brick_bytes = static_cast<uint64_t>(C->B) * C->B * C->B * vols[v].encoded_bytes;
+            V.big_bytes = V.brick_bytes * vols[v].big_brick_size[0] * vols[v].big_brick_size[1] *
+                          vols[v].big_brick_size[2];
+            eb_max = std::max(eb_max, vols[v].encoded_bytes);
+            if (vols[v].encoded_bytes != C->eb) C->eb = 0;  // mixed voxel widths
+            C->big_stride = std::max(C->big_stride, V.big_bytes);
+        }
+        C->slot_bytes = static_cast<uint64_t>(C->B) * C->B * C->B * eb_max;
+    } catch (...) {
+        delete C;
+        throw;
+    }
+    return C;
+}
+
 }  // namespace gc
 
 using namespace gc;
@@ -545,23 +651,16 @@ using namespace gc;
 extern "C" {
 
 int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out) {
+    if (!desc) return guard([] { fail(GC_ERR_INVALID, "null argument"); });
+    return gc_cache_create_shared(desc, &desc->volume, &desc->layout, 1, out);
+}
+
+int gc_cache_create_shared(const gc_cache_desc *desc, const gc_volume_desc *volumes, const gc_layout *layouts,
+                           uint32_t n_volumes, gc_cache_t *out) {
     gc_cache *C = nullptr;
     int rc = guard([&] {
-        GC_REQUIRE(desc && out, "null argument");
-        validate_volume(desc->volume);
-        const gc_layout &L = desc->layout;
-        GC_REQUIRE(L.nb_levels >= 1 && L.nb_levels <= GC_MAX_LEVELS, "bad layout");
-        GC_REQUIRE(desc->max_requests >= 1 && desc->max_requests <= 16384, "max_requests must be in [1, 16384]");
-        for (int a = 0; a < 3; ++a) GC_REQUIRE(desc->cache_size[a] >= 1, "cache size must be >= 1");
-        C = new gc_cache();
-        std::memset(&C->stats, 0, sizeof(C->stats));
-        C->d = *desc;
-        C->device = desc->gpu;
-        GC_CUDA(cudaSetDevice(C->device));
-        C->B = desc->volume.brick_size;
-        C->c = desc->volume.covering;
-        C->Beff = C->B - 2 * C->c;
-        C->eb = desc->volume.encoded_bytes;
+        GC_REQUIRE(desc && volumes && layouts && out, "null argument");
+        C = create_cache(desc, volumes, layouts, n_volumes);
         const uint64_t nslots = static_cast<uint64_t>(desc->cache_size[0]) * desc->cache_size[1] * desc->cache_size[2];
         GC_REQUIRE(nslots < (1ull << 31), "too many pool slots");
         GC_REQUIRE(desc->max_requests <= nslots, "max_requests must not exceed the number of pool slots");
@@ -570,9 +669,6 @@ int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out) {
         C->nentries = static_cast<uint64_t>(C->mx) * C->my * C->mz;
         GC_REQUIRE(C->nentries >= 2, "page directory too small");
         GC_REQUIRE(C->nentries < (1ull << 32), "page directory too large");
-        C->brick_bytes = static_cast<uint64_t>(C->B) * C->B * C->B * C->eb;
-        C->big_bytes = C->brick_bytes * desc->volume.big_brick_size[0] * desc->volume.big_brick_size[1] *
-                       desc->volume.big_brick_size[2];
         const uint32_t maxr = desc->max_requests;
         C->mrpd = dalloc<uint4>(C->nentries, "page directory");
         C->req = dalloc<uint32_t>(C->nentries, "request buffer");
@@ -581,7 +677,7 @@ int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out) {
         C->order[1] = dalloc<uint32_t>(C->nslots, "LRU");
         C->slot_level = dalloc<uint32_t>(C->nslots, "slot levels");
         C->slot_vpos = dalloc<float4>(C->nslots, "slot positions");
-        C->pool = dalloc<uint8_t>(C->nslots * C->brick_bytes, "brick pool");
+        C->pool = dalloc<uint8_t>(C->nslots * C->slot_bytes, "brick pool");
         C->status_lru = dalloc<uint64_t>(lookback_tiles(C->nslots), "scan status");
         C->status_miss = dalloc<uint64_t>(lookback_tiles(C->nentries), "scan status");
         C->ctl_lru = dalloc<ScanCtl>(1, "scan control");
@@ -593,23 +689,23 @@ int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out) {
         C->d_asked = dalloc<uint4>(maxr, "asked list");
         C->d_big_coord = dalloc<uint4>(maxr, "big brick coords");
         C->d_big_index = dalloc<uint32_t>(maxr, "big brick indexes");
-        C->d_src_off = dalloc<uint64_t>(maxr, "brick source offsets");
-        C->d_staging = dalloc<uint8_t>(maxr * C->big_bytes, "staging");
+        C->d_src = dalloc<ulonglong2>(maxr, "brick gather list");
+        C->d_staging = dalloc<uint8_t>(maxr * C->big_stride, "staging");
         C->d_views = dalloc<ViewParams>(C->max_views, "views");
         C->h_list = halloc<uint4>(maxr);
         C->h_asked = halloc<uint4>(maxr);
         C->h_big_coord = halloc<uint4>(maxr);
         C->h_big_index = halloc<uint32_t>(maxr);
-        C->h_src_off = halloc<uint64_t>(maxr);
+        C->h_src = halloc<ulonglong2>(maxr);
         C->h_total = halloc<uint32_t>(1);
         C->h_misc = halloc<uint32_t>(1);
-        C->h_staging = halloc<uint8_t>(maxr * C->big_bytes);
+        C->h_staging = halloc<uint8_t>(maxr * C->big_stride);
         *C->h_total = 0;
         *C->h_misc = 0;
         GC_CUDA(cudaMemset(C->mrpd, 0, C->nentries * sizeof(uint4)));
         GC_CUDA(cudaMemset(C->req, 0, C->nentries * sizeof(uint32_t)));
         GC_CUDA(cudaMemset(C->usage, 0, C->nslots * sizeof(uint32_t)));
-        GC_CUDA(cudaMemset(C->pool, 0, C->nslots * C->brick_bytes));
+        GC_CUDA(cudaMemset(C->pool, 0, C->nslots * C->slot_bytes));
         GC_CUDA(cudaMemset(C->status_lru, 0, lookback_tiles(C->nslots) * sizeof(uint64_t)));
         GC_CUDA(cudaMemset(C->status_miss, 0, lookback_tiles(C->nentries) * sizeof(uint64_t)));
         GC_CUDA(cudaMemset(C->ctl_lru, 0, sizeof(ScanCtl)));
@@ -638,17 +734,19 @@ int gc_cache_destroy(gc_cache_t cache) {
     return GC_OK;
 }
 
-int gc_cache_set_source_host(gc_cache_t C, const void *bricks, uint64_t bytes, const uint64_t *level_offsets,
-                             const uint64_t *empty_keys, size_t n_empty) {
+int gc_cache_set_volume_source_host(gc_cache_t C, uint32_t volume, const void *bricks, uint64_t bytes,
+                                    const uint64_t *level_offsets, const uint64_t *empty_keys, size_t n_empty) {
     return guard([&] {
         GC_REQUIRE(C && bricks && level_offsets && (empty_keys || n_empty == 0), "null argument");
+        GC_REQUIRE(volume < C->vols.size(), "no such volume in this cache");
         GC_CUDA(cudaSetDevice(C->device));
-        const gc_layout &L = C->d.layout;
-        bool aligned = C->big_bytes % 16 == 0;
+        const Volume &V = C->vols[volume];
+        const gc_layout &L = V.layout;
+        bool aligned = V.big_bytes % 16 == 0;
         for (uint32_t l = 0; l < L.nb_levels; ++l) {
             const uint64_t nbig =
                 static_cast<uint64_t>(L.nb_big_bricks[l][0]) * L.nb_big_bricks[l][1] * L.nb_big_bricks[l][2];
-            GC_REQUIRE(level_offsets[l] <= bytes && nbig <= (bytes - level_offsets[l]) / C->big_bytes,
+            GC_REQUIRE(level_offsets[l] <= bytes && nbig <= (bytes - level_offsets[l]) / V.big_bytes,
                        "brick store: level " + std::to_string(l) + " does not fit in the store's bytes");
             aligned = aligned && level_offsets[l] % 16 == 0;
         }
@@ -675,36 +773,51 @@ int gc_cache_set_source_host(gc_cache_t C, const void *bricks, uint64_t bytes, c
         }
         std::lock_guard<std::mutex> g(C->mu);
         GC_REQUIRE(!C->busy, "the loader is busy");
-        C->src = Source();
-        C->src.kind = 1;
-        C->src.host = static_cast<const uint8_t *>(bricks);
-        C->src.bytes = bytes;
-        C->src.direct = direct;
-        C->src.dev = dev;
-        C->src.vec16 = aligned && reinterpret_cast<uintptr_t>(dev) % 16 == 0;
-        C->src.level_off.assign(level_offsets, level_offsets + L.nb_levels);
-        for (size_t i = 0; i < n_empty; ++i) C->src.empty.insert(empty_keys[i]);
+        Source &src = C->vols[volume].src;
+        src = Source();
+        src.kind = 1;
+        src.host = static_cast<const uint8_t *>(bricks);
+        src.bytes = bytes;
+        src.direct = direct;
+        src.dev = dev;
+        src.vec16 = aligned && reinterpret_cast<uintptr_t>(dev) % 16 == 0;
+        src.level_off.assign(level_offsets, level_offsets + L.nb_levels);
+        for (size_t i = 0; i < n_empty; ++i) src.empty.insert(empty_keys[i]);
+        update_upload_route(C);
     });
+}
+
+int gc_cache_set_volume_source_callback(gc_cache_t C, uint32_t volume, gc_brick_loader_fn fn, void *user,
+                                        const uint64_t *empty_keys, size_t n_empty) {
+    return guard([&] {
+        GC_REQUIRE(C && fn && (empty_keys || n_empty == 0), "null argument");
+        GC_REQUIRE(volume < C->vols.size(), "no such volume in this cache");
+        std::lock_guard<std::mutex> g(C->mu);
+        GC_REQUIRE(!C->busy, "the loader is busy");
+        Source &src = C->vols[volume].src;
+        src = Source();
+        src.kind = 2;
+        src.fn = fn;
+        src.user = user;
+        for (size_t i = 0; i < n_empty; ++i) src.empty.insert(empty_keys[i]);
+        update_upload_route(C);
+    });
+}
+
+int gc_cache_set_source_host(gc_cache_t C, const void *bricks, uint64_t bytes, const uint64_t *level_offsets,
+                             const uint64_t *empty_keys, size_t n_empty) {
+    return gc_cache_set_volume_source_host(C, 0, bricks, bytes, level_offsets, empty_keys, n_empty);
 }
 
 int gc_cache_set_source_callback(gc_cache_t C, gc_brick_loader_fn fn, void *user, const uint64_t *empty_keys,
                                  size_t n_empty) {
-    return guard([&] {
-        GC_REQUIRE(C && fn, "null argument");
-        std::lock_guard<std::mutex> g(C->mu);
-        GC_REQUIRE(!C->busy, "the loader is busy");
-        C->src = Source();
-        C->src.kind = 2;
-        C->src.fn = fn;
-        C->src.user = user;
-        for (size_t i = 0; i < n_empty; ++i) C->src.empty.insert(empty_keys[i]);
-    });
+    return gc_cache_set_volume_source_callback(C, 0, fn, user, empty_keys, n_empty);
 }
 
 int gc_cache_update(gc_cache_t C, void *stream, int *converged) {
     return guard([&] {
         GC_REQUIRE(C, "null cache");
-        GC_REQUIRE(C->src.kind != 0, "no brick source set");
+        GC_REQUIRE(has_source(C), "no brick source set");
         const bool r = update(C, as_stream(stream));
         if (converged) *converged = r ? 1 : 0;
     });
@@ -719,6 +832,15 @@ int gc_cache_completude(gc_cache_t C, void *stream, float *fraction) {
         GC_CUDA(cudaMemcpyAsync(C->h_misc, C->d_misc, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         GC_CUDA(cudaStreamSynchronize(s));
         *fraction = static_cast<float>(*C->h_misc) / static_cast<float>(C->nslots);
+    });
+}
+
+int gc_cache_volume_levels(gc_cache_t C, uint32_t volume, uint32_t *level_base, uint32_t *n_levels) {
+    return guard([&] {
+        GC_REQUIRE(C && level_base && n_levels, "null argument");
+        GC_REQUIRE(volume < C->vols.size(), "no such volume in this cache");
+        *level_base = C->vols[volume].level_base;
+        *n_levels = C->vols[volume].layout.nb_levels;
     });
 }
 
@@ -738,8 +860,10 @@ int gc_cache_info_get(gc_cache_t C, gc_cache_info *out) {
         out->mrpd_dims[2] = C->mz;
         out->nb_slots = C->nslots;
         out->slot_voxels = C->B * C->B * C->B;
-        for (uint32_t l = 0; l < C->lt.nlevels; ++l) out->level_offset[l] = C->lt.off[l];
-        out->pool_bytes = static_cast<uint64_t>(C->nslots) * C->brick_bytes;
+        // the first GC_MAX_LEVELS cache levels (a shared cache: gc_cache_volume_levels)
+        for (uint32_t l = 0; l < std::min<uint32_t>(C->lt.nlevels, GC_MAX_LEVELS); ++l)
+            out->level_offset[l] = C->lt.off[l];
+        out->pool_bytes = static_cast<uint64_t>(C->nslots) * C->slot_bytes;
     });
 }
 
@@ -755,7 +879,7 @@ int gc_cache_stats_get(gc_cache_t C, gc_cache_stats *out) {
         GC_CUDA(cudaMemcpy(&used, C->d_count, sizeof(used), cudaMemcpyDeviceToHost));
         *out = C->stats;
         out->device_error = a.err | b.err;
-        out->upload_direct = C->src.kind == 1 && C->src.direct ? 1u : 0u;
+        out->upload_direct = C->gather ? 1u : 0u;
         out->last_used = used;
     });
 }
@@ -779,7 +903,7 @@ int gc_cache_dump(gc_cache_t C, int what, void *dst, size_t bytes) {
                 GC_CUDA(cudaMemcpy(dst, C->usage, bytes, cudaMemcpyDeviceToHost));
                 break;
             case GC_DUMP_POOL:
-                GC_REQUIRE(bytes == C->nslots * C->brick_bytes, "wrong size for the pool");
+                GC_REQUIRE(bytes == C->nslots * C->slot_bytes, "wrong size for the pool");
                 GC_CUDA(cudaMemcpy(dst, C->pool, bytes, cudaMemcpyDeviceToHost));
                 break;
             case GC_DUMP_LRU: {
@@ -1023,7 +1147,7 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
     return guard([&] {
         GC_REQUIRE(b, "null batch");
         gc_cache *C = b->cache;
-        GC_REQUIRE(C->src.kind != 0, "no brick source set");
+        GC_REQUIRE(has_source(C), "no brick source set");
         GC_CUDA(cudaSetDevice(C->device));
         cudaStream_t s = as_stream(stream);
         const auto t_tick = std::chrono::steady_clock::now();

@@ -196,15 +196,48 @@ struct Walk {
     uint4 entry;
 };
 
+// Voxel sampling of one brick (slot base address), typed by T; MixedVoxel
+// picks the type from the view's voxel width (caches whose volumes differ).
+struct MixedVoxel {};
+
 template <typename T>
-__device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt, uint32_t sampler, uint32_t lod,
-                                     V3 np, Walk &w, float &sample) {
-    const float px = np.x * lt.ior[lod][0];
-    const float py = np.y * lt.ior[lod][1];
-    const float pz = np.z * lt.ior[lod][2];
-    const uint32_t cx = lt.off[lod] + static_cast<uint32_t>(px * static_cast<float>(lt.nb[lod][0]));
-    const uint32_t cy = static_cast<uint32_t>(py * static_cast<float>(lt.nb[lod][1]));
-    const uint32_t cz = static_cast<uint32_t>(pz * static_cast<float>(lt.nb[lod][2]));
+__device__ __forceinline__ float sample_slot(const uint8_t *base, uint32_t /*eb*/, const CacheView &cv,
+                                             uint32_t sampler, float fx, float fy, float fz) {
+    const T *b = reinterpret_cast<const T *>(base);
+    const uint32_t B = cv.B;
+    if (sampler == GC_SAMPLER_REFERENCE) {
+        const uint32_t lx = cv.c + static_cast<uint32_t>(fx) % cv.Beff;
+        const uint32_t ly = cv.c + static_cast<uint32_t>(fy) % cv.Beff;
+        const uint32_t lz = cv.c + static_cast<uint32_t>(fz) % cv.Beff;
+        return sample_corner<T>(b, B, lx, ly, lz);
+    }
+    uint32_t x0, y0, z0;
+    float wx, wy, wz;
+    tri_axis(fx, cv.c, cv.Beff, B, x0, wx);
+    tri_axis(fy, cv.c, cv.Beff, B, y0, wy);
+    tri_axis(fz, cv.c, cv.Beff, B, z0, wz);
+    return sample_trilinear<T>(b, B, x0, y0, z0, wx, wy, wz);
+}
+template <>
+__device__ __forceinline__ float sample_slot<MixedVoxel>(const uint8_t *base, uint32_t eb, const CacheView &cv,
+                                                         uint32_t sampler, float fx, float fy, float fz) {
+    if (eb == 1) return sample_slot<uint8_t>(base, eb, cv, sampler, fx, fy, fz);
+    if (eb == 2) return sample_slot<uint16_t>(base, eb, cv, sampler, fx, fy, fz);
+    return sample_slot<float>(base, eb, cv, sampler, fx, fy, fz);
+}
+
+// Page walk + sample at the normalized position np of cache level lvl (the
+// view's level base + its LOD): K_CacheManager::get_normalized
+// (K_CacheManager.hpp:265-361).
+template <typename T>
+__device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt, uint32_t sampler, uint32_t eb,
+                                     uint32_t lvl, V3 np, Walk &w, float &sample) {
+    const float px = np.x * lt.ior[lvl][0];
+    const float py = np.y * lt.ior[lvl][1];
+    const float pz = np.z * lt.ior[lvl][2];
+    const uint32_t cx = lt.off[lvl] + static_cast<uint32_t>(px * static_cast<float>(lt.nb[lvl][0]));
+    const uint32_t cy = static_cast<uint32_t>(py * static_cast<float>(lt.nb[lvl][1]));
+    const uint32_t cz = static_cast<uint32_t>(pz * static_cast<float>(lt.nb[lvl][2]));
     const uint64_t idx = cx + static_cast<uint64_t>(cy) * cv.mx + static_cast<uint64_t>(cz) * cv.mx * cv.my;
     bool fresh = false;
     if (cx != w.pcx || cy != w.pcy || cz != w.pcz) {
@@ -222,23 +255,10 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
             uint32_t *u = cv.usage + slot;
             if (*u != cv.ts) *u = cv.ts;
         }
-        const T *b = reinterpret_cast<const T *>(cv.pool) + static_cast<uint64_t>(slot) * B * B * B;
-        const float fx = px * static_cast<float>(lt.vvox[lod][0]);
-        const float fy = py * static_cast<float>(lt.vvox[lod][1]);
-        const float fz = pz * static_cast<float>(lt.vvox[lod][2]);
-        if (sampler == GC_SAMPLER_REFERENCE) {
-            const uint32_t lx = cv.c + static_cast<uint32_t>(fx) % cv.Beff;
-            const uint32_t ly = cv.c + static_cast<uint32_t>(fy) % cv.Beff;
-            const uint32_t lz = cv.c + static_cast<uint32_t>(fz) % cv.Beff;
-            sample = sample_corner<T>(b, B, lx, ly, lz);
-        } else {
-            uint32_t x0, y0, z0;
-            float wx, wy, wz;
-            tri_axis(fx, cv.c, cv.Beff, B, x0, wx);
-            tri_axis(fy, cv.c, cv.Beff, B, y0, wy);
-            tri_axis(fz, cv.c, cv.Beff, B, z0, wz);
-            sample = sample_trilinear<T>(b, B, x0, y0, z0, wx, wy, wz);
-        }
+        const float fx = px * static_cast<float>(lt.vvox[lvl][0]);
+        const float fy = py * static_cast<float>(lt.vvox[lvl][1]);
+        const float fz = pz * static_cast<float>(lt.vvox[lvl][2]);
+        sample = sample_slot<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, eb, cv, sampler, fx, fy, fz);
         return kMapped;
     }
     if (e.w == 0u) {
@@ -254,14 +274,14 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
 // a new brick, stamps the usage of a resident one (the ray will sample it once
 // its first missing brick is in) and raises the request of a missing one.
 // Returns the entry's status, or kMapped when the brick did not change.
-__device__ __forceinline__ int probe(const CacheView &cv, const LevelTables &lt, uint32_t lod, V3 np, Walk &w,
+__device__ __forceinline__ int probe(const CacheView &cv, const LevelTables &lt, uint32_t lvl, V3 np, Walk &w,
                                      bool &raised) {
-    const float px = np.x * lt.ior[lod][0];  // the brick arithmetic of fetch()
-    const float py = np.y * lt.ior[lod][1];
-    const float pz = np.z * lt.ior[lod][2];
-    const uint32_t cx = lt.off[lod] + static_cast<uint32_t>(px * static_cast<float>(lt.nb[lod][0]));
-    const uint32_t cy = static_cast<uint32_t>(py * static_cast<float>(lt.nb[lod][1]));
-    const uint32_t cz = static_cast<uint32_t>(pz * static_cast<float>(lt.nb[lod][2]));
+    const float px = np.x * lt.ior[lvl][0];  // the brick arithmetic of fetch()
+    const float py = np.y * lt.ior[lvl][1];
+    const float pz = np.z * lt.ior[lvl][2];
+    const uint32_t cx = lt.off[lvl] + static_cast<uint32_t>(px * static_cast<float>(lt.nb[lvl][0]));
+    const uint32_t cy = static_cast<uint32_t>(py * static_cast<float>(lt.nb[lvl][1]));
+    const uint32_t cz = static_cast<uint32_t>(pz * static_cast<float>(lt.nb[lvl][2]));
     raised = false;
     if (cx == w.pcx && cy == w.pcy && cz == w.pcz) return static_cast<int>(w.entry.w);
     const uint64_t idx = cx + static_cast<uint64_t>(cy) * cv.mx + static_cast<uint64_t>(cz) * cv.mx * cv.my;
@@ -368,7 +388,7 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
     r.lod = 0;
     r.sL = 0.f;  // spacings of level lod + 1
     r.sU = 0.f;
-    if (lt.nlevels > 1) {
+    if (vp.nlevels > 1) {
         const V3 n1 = v3(vp.inv_size[1][0], vp.inv_size[1][1], vp.inv_size[1][2]);
         r.sL = length(dirLeft * n1);
         r.sU = length(dirUp * n1);
@@ -392,7 +412,7 @@ __device__ __noinline__ void lookahead_walk(const CacheView &cv, const LevelTabl
     const ViewParams &vp = *r.vp;
     r.t += vp.step[r.lod];  // the stop sample's brick is requested already
     r.pos = r.pos + r.dir * vp.step[r.lod];
-    const uint32_t nl = lt.nlevels;
+    const uint32_t nl = vp.nlevels;
     while (r.t < r.tfar) {
         const float alpha = r.t / r.tfar;
         const float pX = r.endX * alpha;
@@ -409,7 +429,7 @@ __device__ __noinline__ void lookahead_walk(const CacheView &cv, const LevelTabl
             }
         }
         bool raised = false;
-        const int st = probe(cv, lt, r.lod, np, r.w, raised);
+        const int st = probe(cv, lt, vp.level_base + r.lod, np, r.w, raised);
         if (raised && --budget == 0) return;
         const float dt = st == kEmpty ? vp.tstep : vp.step[r.lod];
         r.t += dt;
@@ -431,7 +451,7 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
     const V3 np = v3(clampf(tp.x, 0.f, 0.99f), clampf(tp.y, 0.f, 0.99f), clampf(tp.z, 0.f, 0.99f));
     // compute_LOD: the level only grows along a ray because the pixel
     // footprint grows with t, so the scan resumes at the current level.
-    const uint32_t nl = lt.nlevels;
+    const uint32_t nl = vp.nlevels;
     while (r.lod + 1 < nl && !(r.sL >= pX || r.sU >= pY)) {
         ++r.lod;
         if (r.lod + 1 < nl) {
@@ -442,7 +462,7 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
     }
     const uint32_t lod = r.lod;
     float sample = 0.f;
-    const int st = fetch<T>(cv, lt, vp.sampler, lod, np, r.w, sample);
+    const int st = fetch<T>(cv, lt, vp.sampler, vp.eb, vp.level_base + lod, np, r.w, sample);
     if (st != kMapped) {
         if (st == kUnmapped) {
             vp.tbuf[r.i] = r.t;
@@ -649,7 +669,7 @@ static RenderLaunch render_launch_config(uint32_t eb, uint32_t total_tiles) {
     const RenderTuning tune = render_tuning();
     const uint32_t threads = tune.threads;
     GC_REQUIRE(threads == 64 || threads == 128 || threads == 256, "render threads must be 64, 128 or 256");
-    static int occupancy[2][3][3] = {};
+    static int occupancy[2][4][3] = {};
     const int tslot = threads == 64 ? 0 : (threads == 128 ? 1 : 2);
     auto config = [&](auto kernel, int sched, int slot) {
         int &occ = occupancy[sched][slot][tslot];
@@ -669,6 +689,8 @@ static RenderLaunch render_launch_config(uint32_t eb, uint32_t total_tiles) {
         case 1: return pix ? config(render_pixels_kernel<uint8_t>, 1, 0) : config(render_kernel<uint8_t>, 0, 0);
         case 2: return pix ? config(render_pixels_kernel<uint16_t>, 1, 1) : config(render_kernel<uint16_t>, 0, 1);
         case 4: return pix ? config(render_pixels_kernel<float>, 1, 2) : config(render_kernel<float>, 0, 2);
+        case 0:  // volumes of different voxel widths share the cache
+            return pix ? config(render_pixels_kernel<MixedVoxel>, 1, 3) : config(render_kernel<MixedVoxel>, 0, 3);
         default: fail(GC_ERR_UNSUPPORTED, "the ray caster supports one channel of 1, 2 or 4 bytes");
     }
 }

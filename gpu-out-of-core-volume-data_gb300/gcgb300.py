@@ -78,7 +78,7 @@ class View(C.Structure):
                 ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3), ("tstep", C.c_float),
                 ("focal", C.c_float), ("early_alpha", C.c_float), ("mode", C.c_uint32), ("sampler", C.c_uint32),
                 ("tf_width", C.c_uint32), ("tf", C.c_void_p), ("rgba", C.c_void_p), ("tbuf", C.c_void_p),
-                ("state", C.c_void_p), ("status", C.c_void_p)]
+                ("state", C.c_void_p), ("status", C.c_void_p), ("volume", C.c_uint32)]
 
 
 class BatchDesc(C.Structure):
@@ -125,6 +125,10 @@ _SIGS = {
     "gc_cache_create": [P(CacheDesc), P(vp)], "gc_cache_destroy": [vp],
     "gc_cache_set_source_host": [vp, vp, C.c_uint64, P(C.c_uint64), P(C.c_uint64), C.c_size_t],
     "gc_cache_set_source_callback": [vp, LOADER_FN, vp, P(C.c_uint64), C.c_size_t],
+    "gc_cache_set_volume_source_host": [vp, C.c_uint32, vp, C.c_uint64, P(C.c_uint64), P(C.c_uint64), C.c_size_t],
+    "gc_cache_set_volume_source_callback": [vp, C.c_uint32, LOADER_FN, vp, P(C.c_uint64), C.c_size_t],
+    "gc_cache_create_shared": [P(CacheDesc), P(VolumeDesc), P(Layout), C.c_uint32, P(vp)],
+    "gc_cache_volume_levels": [vp, C.c_uint32, P(C.c_uint32), P(C.c_uint32)],
     "gc_cache_update": [vp, vp, P(C.c_int)], "gc_cache_completude": [vp, vp, P(C.c_float)],
     "gc_cache_timestamp": [vp, P(C.c_uint32)], "gc_cache_info_get": [vp, P(CacheInfo)],
     "gc_cache_stats_get": [vp, P(CacheStats)], "gc_cache_dump": [vp, C.c_int, vp, C.c_size_t],
@@ -398,21 +402,29 @@ class TransferFunction:
 
 def make_view(inv_view, width, height, tf_ptr, tf_width, rgba_ptr, tbuf_ptr, state_ptr, tstep=2.0 / 256.0,
               focal=2.0, early_alpha=0.95, mode=MODE_DVR, sampler=SAMPLER_REFERENCE,
-              bbox_min=(-1.0, -1.0, -1.0), bbox_max=(1.0, 1.0, 1.0), status_ptr=0):
+              bbox_min=(-1.0, -1.0, -1.0), bbox_max=(1.0, 1.0, 1.0), status_ptr=0, volume=0):
     return View((C.c_float * 12)(*inv_view), width, height, (C.c_float * 3)(*bbox_min), (C.c_float * 3)(*bbox_max),
                 tstep, focal, early_alpha, mode, sampler, tf_width, vp(tf_ptr), vp(rgba_ptr), vp(tbuf_ptr),
-                vp(state_ptr), vp(status_ptr or None))
+                vp(state_ptr), vp(status_ptr or None), volume)
 
 
 # ---------------------------------------------------------------------------
 class CacheManager:
     """GPU brick cache + ray caster entry (CacheManager<T> + RayCastDVR)."""
 
-    def __init__(self, vol, layout, cache_size, max_requests=50, sync_loader=True, gpu=0, staged_upload=False):
+    def __init__(self, vol, layout, cache_size, max_requests=50, sync_loader=True, gpu=0, staged_upload=False,
+                 shared=None):
+        """shared: [(volume_desc, layout), ...] for one cache over several
+        volumes sharing the pool (vol/layout are then the first of them)."""
         flags = (CACHE_SYNC_LOADER if sync_loader else 0) | (CACHE_STAGED_UPLOAD if staged_upload else 0)
         self.desc = CacheDesc(vol, layout, u3(cache_size), max_requests, flags, gpu)
         self._h = vp()
-        check(lib.gc_cache_create(C.byref(self.desc), C.byref(self._h)))
+        if shared:
+            vols = (VolumeDesc * len(shared))(*[v for v, _ in shared])
+            lays = (Layout * len(shared))(*[l for _, l in shared])
+            check(lib.gc_cache_create_shared(C.byref(self.desc), vols, lays, len(shared), C.byref(self._h)))
+        else:
+            check(lib.gc_cache_create(C.byref(self.desc), C.byref(self._h)))
         info = CacheInfo()
         check(lib.gc_cache_info_get(self._h, C.byref(info)))
         self.info = info
@@ -422,7 +434,12 @@ class CacheManager:
     def handle(self):
         return self._h
 
-    def set_source_host(self, store, level_offsets, empty_keys=(), nbytes=None):
+    def volume_levels(self, volume):
+        base, n = C.c_uint32(), C.c_uint32()
+        check(lib.gc_cache_volume_levels(self._h, volume, C.byref(base), C.byref(n)))
+        return base.value, n.value
+
+    def set_source_host(self, store, level_offsets, empty_keys=(), nbytes=None, volume=0):
         """`store`: a host torch tensor or numpy array holding the brick store
         (or a raw address, with `nbytes`).  The store must outlive the cache."""
         if hasattr(store, "data_ptr"):
@@ -436,13 +453,13 @@ class CacheManager:
         offs = (C.c_uint64 * MAX_LEVELS)(*[int(o) for o in level_offsets])
         keys = (C.c_uint64 * max(1, len(empty_keys)))(*[int(k) for k in empty_keys])
         self._keep.append((offs, keys, store))
-        check(lib.gc_cache_set_source_host(self._h, vp(ptr), size, offs, keys, len(empty_keys)))
+        check(lib.gc_cache_set_volume_source_host(self._h, volume, vp(ptr), size, offs, keys, len(empty_keys)))
 
-    def set_source_callback(self, fn, empty_keys=()):
+    def set_source_callback(self, fn, empty_keys=(), volume=0):
         cb = LOADER_FN(fn)
         keys = (C.c_uint64 * max(1, len(empty_keys)))(*[int(k) for k in empty_keys])
         self._keep.append((cb, keys))
-        check(lib.gc_cache_set_source_callback(self._h, cb, None, keys, len(empty_keys)))
+        check(lib.gc_cache_set_volume_source_callback(self._h, volume, cb, None, keys, len(empty_keys)))
 
     def update(self, stream=0):
         conv = C.c_int()

@@ -213,6 +213,20 @@ typedef int (*gc_brick_loader_fn)(void *user, uint32_t level, uint32_t x, uint32
                                   uint32_t z, void *dst, size_t bytes);
 
 int gc_cache_create(const gc_cache_desc *desc, gc_cache_t *out);
+/* One cache over several volumes sharing one brick pool (the serving form;
+ * no counterpart in the reference, whose CacheManager holds one volume).
+ * The page directory holds the levels of all n_volumes volumes one after
+ * the other (volume 0 first; gc_cache_volume_levels gives each volume's
+ * range), the LRU order, usage and request scan run over the whole pool,
+ * and a view names its volume in gc_view.volume.  The volumes need the same
+ * BrickSize and VoxelCovering; their voxel widths and big-brick sizes may
+ * differ (a pool slot then holds B^3 voxels of the widest type).  desc gives
+ * the pool size, max_requests, flags and device; its volume/layout fields
+ * are ignored.  1 to 4 volumes, at most 64 levels in all. */
+int gc_cache_create_shared(const gc_cache_desc *desc, const gc_volume_desc *volumes, const gc_layout *layouts,
+                           uint32_t n_volumes, gc_cache_t *out);
+/* First cache level and level count of one volume of the cache. */
+int gc_cache_volume_levels(gc_cache_t cache, uint32_t volume, uint32_t *level_base, uint32_t *n_levels);
 int gc_cache_destroy(gc_cache_t cache);
 /* In-memory brick store of `bytes` bytes: all big bricks of every level,
  * level l starting at byte offset level_offsets[l] in (z, y, x) raster order;
@@ -230,6 +244,12 @@ int gc_cache_set_source_host(gc_cache_t cache, const void *bricks, uint64_t byte
                              const uint64_t *empty_keys, size_t n_empty);
 int gc_cache_set_source_callback(gc_cache_t cache, gc_brick_loader_fn fn, void *user,
                                  const uint64_t *empty_keys, size_t n_empty);
+/* The same for one volume of a shared cache (the calls above set volume 0).
+ * Level numbers, brick keys and empty keys are the volume's own. */
+int gc_cache_set_volume_source_host(gc_cache_t cache, uint32_t volume, const void *bricks, uint64_t bytes,
+                                    const uint64_t *level_offsets, const uint64_t *empty_keys, size_t n_empty);
+int gc_cache_set_volume_source_callback(gc_cache_t cache, uint32_t volume, gc_brick_loader_fn fn, void *user,
+                                        const uint64_t *empty_keys, size_t n_empty);
 /* CacheManager::update (CacheManager.hpp:318-354).  *converged = 1 when the
  * request list was empty this frame. */
 int gc_cache_update(gc_cache_t cache, void *stream, int *converged);
@@ -329,6 +349,8 @@ typedef struct gc_view {
                                  of this view met an unmapped brick in this
                                  pass (the view is not converged); the caller
                                  clears it before the pass                      */
+    uint32_t volume;          /* volume of a shared cache (gc_cache_create_shared);
+                                 0 for a single-volume cache                    */
 } gc_view;
 
 /* Camera of updateViewMatrix (Display_helper.cpp:93-118): the rows of
