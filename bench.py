@@ -62,6 +62,14 @@ CONFIGS = {
     "c3": dict(VOL2048, B=32, c=1, pool_bytes=4 << 30, pool_slots=None, batch=64,
                sizes=((256, 256), (512, 512), (1024, 1024), (1920, 1080)), dist=(0.5, 3.0), tf="bumps",
                early=0.99, fov=45.0),
+    # serving: three resident volumes sharing one 24 GiB pool, Poisson requests
+    "c4": dict(B=16, c=1, pool_bytes=24 << 30, rate=200.0, duration=6.0, batch=64,
+               sizes=((256, 256), (512, 512), (1024, 1024), (1920, 1080)), dist=(0.5, 3.0), early=0.99, fov=45.0,
+               volumes=(dict(size=(1024, 1024, 1024), bpc=1, nblobs=16, sigma=(20.0, 150.0), amp=(60, 200),
+                             noise=20, seed=11),
+                        dict(VOL2048, seed=12),
+                        dict(size=(4096, 4096, 2048), bpc=1, nblobs=48, sigma=(80.0, 600.0), amp=(60, 200),
+                             noise=20, seed=13))),
 }
 DIAG = 2.0 * math.sqrt(3.0)
 PIXEL_BYTES = 44  # RGBA 4 + t 4+4 + colour state 16+16 per pixel and launch
@@ -185,6 +193,9 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+PIN_STORES = False  # --pin-stores: brick stores in page-locked host memory
+
+
 def make_store(gc, torch, cfg):
     """Synthetic volume generated on the device, pre-processed (mip + bricks) on
     the device, brick store moved to host memory (the out-of-core source)."""
@@ -198,7 +209,7 @@ def make_store(gc, torch, cfg):
     gc.generate_volume(gc.make_generator(size, bpc, cfg["seed"], blobs, cfg["noise"]), dev.data_ptr())
     torch.cuda.synchronize()
     t1 = time.time()
-    store, offs, _ = gc.pre_process(vol, layout, dev)
+    store, offs, _ = gc.pre_process(vol, layout, dev, pin=PIN_STORES)
     del dev
     torch.cuda.empty_cache()
     t2 = time.time()
@@ -444,7 +455,7 @@ def batched_pass(gc, torch, cfg, data, views, warm, args):
     rays = sum(W * H for _, W, H in views)
     S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests, sync=False)
     B = gc.Batch(S.cm, max_views=cfg["batch"], max_pixels=args.batch_pixels, max_passes=args.batch_cap,
-                 max_occupancy=args.occupancy, max_admit=args.admit, lookahead=args.lookahead,
+                 max_occupancy=args.occupancy, max_admit=args.admit, park_above=args.park,
                  reorder_window=args.reorder)
 
     def run_all(vs, base):
@@ -536,7 +547,7 @@ def run_c3(args):
            "data": "synthetic (seeded blobs + value noise, 2048^3 u16; no public dataset)",
            "config": {"workload": f"c3: {len(views)} views, batched (continuous batching), each to convergence",
                       "rays": int(rays), "reorder": args.reorder, "occupancy": args.occupancy,
-                      "admit": args.admit, "lookahead": args.lookahead, "render_tuning": list(best),
+                      "admit": args.admit, "park_above": args.park, "render_tuning": list(best),
                       "preprocess_s": round(prep_s, 2)},
            "batched": batched}
     if not args.no_plain:
@@ -544,6 +555,125 @@ def run_c3(args):
         out["plain_same_views"] = plain
         out["ratio"] = round(batched["value"] / plain["value"], 3)
     print(json.dumps(out), flush=True)
+
+
+def run_c4(args):
+    """`--config c4`: the serving form.  Three volumes are generated and
+    pre-processed on the device and kept as host brick stores; one cache holds
+    all three in a shared 24 GiB pool.  Requests arrive as a Poisson stream
+    (seeded) over `duration` seconds, each with a random volume, camera,
+    resolution and one of 4 transfer functions; each is submitted to the
+    continuous batch at its arrival time and retired when converged.  Latency =
+    arrival -> retirement; Mrays/s = rays of all requests / time to the last
+    retirement."""
+    import torch
+
+    import gcgb300 as gc
+
+    cfg = CONFIGS["c4"]
+    vols, stores, prep = c4_stores(gc, torch, cfg)
+    out = c4_serve(gc, torch, cfg, vols, stores, args)
+    out["config"]["preprocess_s"] = round(prep, 2)
+    print(json.dumps(out), flush=True)
+
+
+def c4_stores(gc, torch, cfg):
+    """The three c4 volumes generated and pre-processed on the device; host stores."""
+    vols, stores = [], []
+    prep = 0.0
+    for vc in cfg["volumes"]:
+        vcfg = dict(vc, B=cfg["B"], c=cfg["c"])
+        vol, layout, store, offs, prep_s = make_store(gc, torch, vcfg)
+        vols.append((vol, layout))
+        stores.append((store, offs))
+        prep += prep_s
+    return vols, stores, prep
+
+
+def c4_serve(gc, torch, cfg, vols, stores, args):
+    """One serving run over a fresh shared cache; returns the JSON object."""
+    widest = max(vols, key=lambda v: v[0].encoded_bytes)[0]
+    pool = gc.pool_dims(widest, cfg["pool_bytes"])
+    cm = gc.CacheManager(vols[0][0], vols[0][1], pool, max_requests=args.max_requests, sync_loader=False,
+                         shared=vols, staged_upload=args.upload == "staged")
+    for k, (store, offs) in enumerate(stores):
+        cm.set_source_host(store, offs, volume=k)
+    tfs = [torch.from_numpy(tf_table(kind, seed).reshape(-1)).cuda()
+           for kind, seed in (("ramp", 0), ("bumps", 3), ("bumps", 4), ("bumps", 5))]
+    focal = 1.0 / math.tan(math.radians(cfg["fov"]) / 2)
+    rng = np.random.default_rng(2026)
+    reqs, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / args.rate)
+        if t > args.duration:
+            break
+        v = rng.standard_normal(3)
+        v /= np.linalg.norm(v)
+        d = rng.uniform(*cfg["dist"]) * DIAG
+        up = (0.0, 1.0, 0.0) if abs(v[1]) < 0.95 else (1.0, 0.0, 0.0)
+        W, H = cfg["sizes"][int(rng.integers(0, len(cfg["sizes"])))]
+        reqs.append((t, int(rng.integers(0, len(vols))), gc.look_at(tuple(float(c) * d for c in v), (0.0, 0.0, 0.0),
+                                                                    up), W, H, int(rng.integers(0, len(tfs)))))
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    B = gc.Batch(cm, max_views=cfg["batch"], max_pixels=args.batch_pixels, max_passes=args.batch_cap,
+                 max_occupancy=args.occupancy, max_admit=args.admit, reorder_window=args.reorder,
+                 park_above=args.park)
+    bufs, lat, passes, conv, rays_done = {}, [], [], 0, 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    nxt = 0
+    torch.cuda.nvtx.range_push("serving")
+    while len(lat) < len(reqs):
+        now = time.perf_counter() - t0
+        while nxt < len(reqs) and reqs[nxt][0] <= now:  # arrivals so far
+            _, vol_i, m, W, H, tf_i = reqs[nxt]
+            with torch.cuda.stream(stream):
+                b = (torch.empty(W * H, dtype=torch.int32, device="cuda"),
+                     torch.empty(W * H, dtype=torch.float32, device="cuda"),
+                     torch.empty(W * H * 4, dtype=torch.float32, device="cuda"))
+            bufs[nxt] = b
+            B.submit(gc.make_view(m, W, H, tfs[tf_i].data_ptr(), 256, b[0].data_ptr(), b[1].data_ptr(),
+                                  b[2].data_ptr(), tstep=2.0 / 256.0, focal=focal, early_alpha=cfg["early"],
+                                  volume=vol_i), nxt)
+            nxt += 1
+        active, queued = B.tick(sp)
+        for tag, npass, ok, _ in B.poll():
+            _, _, _, W, H, _ = reqs[tag]
+            lat.append(1e3 * (time.perf_counter() - t0 - reqs[tag][0]))  # arrival -> retirement
+            passes.append(npass)
+            conv += int(ok)
+            rays_done += W * H
+            del bufs[tag]
+        if active == 0 and queued == 0 and nxt < len(reqs):
+            time.sleep(max(0.0, min(0.002, reqs[nxt][0] - (time.perf_counter() - t0))))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    torch.cuda.nvtx.range_pop()
+    st, bs = cm.stats(), B.stats()
+    rays = sum(W * H for _, _, _, W, H, _ in reqs)
+    out = {"metric": "Mrays/s", "value": round(rays / wall / 1e6, 3), "unit": "Mrays/s", "n_gpus": 1,
+           "steps": len(reqs), "warmup": 0, "ms_per_step": round(1e3 * wall / len(reqs), 4),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8+u16",
+           "data": "synthetic (seeded blobs + value noise; 1024^3 u8, 2048^3 u16, 4096x4096x2048 u8)",
+           "config": {"workload": f"c4: serving, {len(reqs)} Poisson requests at {args.rate}/s over "
+                                  f"{args.duration} s, 3 volumes in one shared pool {list(pool)} "
+                                  f"({cm.info.pool_bytes / 2**30:.1f} GiB), sizes {list(cfg['sizes'])}, 4 TFs",
+                      "offered_mrays_per_s": round(rays / args.duration / 1e6, 2), "reorder": args.reorder,
+                      "occupancy": args.occupancy, "admit": args.admit, "park_above": args.park,
+                      "upload": "staged" if args.upload == "staged" else "gather",
+                      "stores": "pinned" if PIN_STORES else "pageable",
+                      "max_passes": args.batch_cap},
+           "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+           "passes_per_request": round(statistics.mean(passes), 2), "converged": f"{conv}/{len(reqs)}",
+           "ticks": {"render_ticks": bs.render_ticks, "graph_replays": bs.graph_replays, "parked": bs.parked,
+                     "render_ms": round(bs.render_ms, 1), "loader_wait_ms": round(bs.wait_ms, 1)},
+           "cache": {"bricks_installed": int(st.bricks_installed), "brick_h2d_bytes": int(st.bytes_h2d),
+                     "upload_gbs": round(st.bytes_h2d / (st.upload_ns / 1e9) / 1e9, 1) if st.upload_ns else None,
+                     "device_error": int(st.device_error)}}
+    B.close()
+    cm.close()
+    return out
 
 
 def run_batched(gc, torch, args):
@@ -557,12 +687,11 @@ def run_batched(gc, torch, args):
     rays = sum(W * H for _, W, H in views)
     batched, _ = batched_pass(gc, torch, cfg, data, views, warm, args)
     plain, _ = plain_views_pass(gc, torch, cfg, data, views, warm, args)
-    la = "all bricks to the ray's end" if args.lookahead >= 1 << 20 else f"{args.lookahead} bricks"
     return {"config": {"workload": f"c3: {len(views)} views ({args.batches} x {cfg['batch']}), sizes "
                                    f"{list(cfg['sizes'])}, cameras at 0.5-3.0x diagonal; BrickSize 32, 4 GiB pool; "
                                    f"all submitted at t0, continuous batching with a {args.batch_pixels} pixel "
                                    f"budget, admission while demand (used + missing) <= {args.occupancy} of the "
-                                   f"pool, <= {args.admit} admissions per tick, request lookahead {la}, "
+                                   f"pool, <= {args.admit} admissions per tick, "
                                    f"asynchronous loader",
                        "preprocess_s": round(prep_s, 2), "rays": int(rays)},
             "unit": "Mrays/s", "batched": batched, "plain_same_views": plain,
@@ -666,9 +795,11 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=["c1", "c2", "c3"], default="c2",
+    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4"], default="c2",
                     help="c2: the plain out-of-core line (+ the c3 batched object); c1: small in-core plain case; "
-                         "c3: the batched form alone")
+                         "c3: the batched form alone; c4: serving (three volumes, shared pool, Poisson requests)")
+    ap.add_argument("--rate", type=float, default=200.0, help="c4: request arrivals per second")
+    ap.add_argument("--duration", type=float, default=6.0, help="c4: seconds of arrivals")
     ap.add_argument("--max-requests", type=int, default=8192)
     ap.add_argument("--batches", type=int, default=3)
     ap.add_argument("--batch-cap", type=int, default=256)
@@ -680,8 +811,11 @@ def main():
                          "staged = host copies into pinned staging + cudaMemcpyAsync")
     ap.add_argument("--reorder", type=int, default=192,
                     help="batched admission: locality window over queued views (0: arrival order)")
-    ap.add_argument("--lookahead", type=int, default=0,
-                    help="batched request policy: further missing bricks a stopped ray requests")
+    ap.add_argument("--pin-stores", action="store_true",
+                    help="keep the host brick stores in page-locked memory (read by the gather kernel "
+                         "through the device's own mappings)")
+    ap.add_argument("--park", type=float, default=0.0,
+                    help="batched/serving: park the newest view while demand exceeds this fraction of the pool")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
@@ -691,15 +825,19 @@ def main():
         args.steps = 40 if args.impl == "ours" else 2
     args.warmup = max(3, args.warmup)
     Session.staged = args.upload == "staged"
+    global PIN_STORES
+    PIN_STORES = args.pin_stores
     if args.config != "c2":
         args.no_batched = True
-    if args.impl == "reference" and args.config == "c3":
+    if args.impl == "reference" and args.config in ("c3", "c4"):
         print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm covers the plain configs "
                                                               "(c1, c2); c3 is the batched form"}), flush=True)
     elif args.impl == "reference":
         run_reference(args)
     elif args.config == "c3":
         run_c3(args)
+    elif args.config == "c4":
+        run_c4(args)
     else:
         run_ours(args)
 

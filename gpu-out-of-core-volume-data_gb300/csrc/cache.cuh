@@ -73,7 +73,6 @@ struct ViewParams {
     uint32_t level_base;                // first cache level of the view's volume
     uint32_t nlevels;                   // levels of the view's volume
     uint32_t eb;                        // bytes per voxel of the view's volume
-    uint32_t lookahead;                 // extra missing bricks a stopped ray requests (0: none)
     uint32_t mark_done;                 // batched passes: a finished ray leaves -1 - t in tbuf and
                                         // later passes skip its pixel (rgba already final)
 };

@@ -548,8 +548,8 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
 
 // graph + pinned view table: the batched form replays a CUDA graph instead
 // of launching (launch_render_graph)
-static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s, uint32_t lookahead = 0,
-                   bool mark_done = false, RenderGraph *graph = nullptr, ViewParams *pinned = nullptr) {
+static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s, bool mark_done = false,
+                   RenderGraph *graph = nullptr, ViewParams *pinned = nullptr) {
     GC_REQUIRE(views && n >= 1, "no views");
     GC_REQUIRE(n <= C->max_views, "too many views in one batch");
     GC_CUDA(cudaSetDevice(C->device));
@@ -557,7 +557,6 @@ static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s
     uint32_t tiles = 0;
     for (uint32_t i = 0; i < n; ++i) {
         fill_view(C, views[i], vp[i]);
-        vp[i].lookahead = lookahead;
         vp[i].mark_done = mark_done ? 1u : 0u;
         vp[i].tile_begin = tiles;
         tiles += vp[i].tiles_x * div_up(views[i].height, 32u >> vp[i].tile_shift);
@@ -1073,8 +1072,12 @@ struct gc_batch {
         uint64_t epoch;  // install count at the view's last pass (kNever before the first)
         uint32_t skipped;  // times a later view was admitted before it
         std::chrono::steady_clock::time_point submitted;
+        bool started;      // progressive buffers cleared (first admission)
+        uint64_t seq;      // admission sequence number (the newest is parked first)
     };
+    uint64_t admissions = 0;
     float last_cam[3] = {0.f, 0.f, 0.f};  // camera of the last admitted view
+    uint32_t last_volume = 0;             // and its volume
     bool have_cam = false;
     static constexpr uint64_t kNever = ~0ull;
     uint64_t installs = 0;  // ticks that installed bricks
@@ -1139,7 +1142,7 @@ int gc_batch_submit(gc_batch_t b, const gc_view *view, uint64_t tag) {
         GC_REQUIRE(b && view, "null argument");
         ViewParams check;
         fill_view(b->cache, *view, check);  // validates the view now, not at admission
-        b->queue.push_back({*view, tag, 0, gc_batch::kNever, 0, std::chrono::steady_clock::now()});
+        b->queue.push_back({*view, tag, 0, gc_batch::kNever, 0, std::chrono::steady_clock::now(), false, 0});
     });
 }
 
@@ -1180,7 +1183,8 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         auto cam_dist = [&](const gc_view &v) {  // camera = translation column of the view matrix
             const float dx = v.inv_view[3] - b->last_cam[0], dy = v.inv_view[7] - b->last_cam[1],
                         dz = v.inv_view[11] - b->last_cam[2];
-            return dx * dx + dy * dy + dz * dz;
+            // views of another volume share no bricks: farther than any camera
+            return dx * dx + dy * dy + dz * dz + (v.volume != b->last_volume ? 1e30f : 0.f);
         };
         while (!b->queue.empty() && b->active.size() < b->d.max_views) {
             size_t pick = 0;
@@ -1201,12 +1205,17 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
                                        (b->d.max_admit && admitted >= b->d.max_admit)))
                 break;
             ++admitted;
-            GC_CUDA(cudaMemsetAsync(v.tbuf, 0, px * sizeof(float), s));
-            GC_CUDA(cudaMemsetAsync(v.state, 0, px * 4 * sizeof(float), s));
+            if (!b->queue[pick].started) {  // a parked view resumes with its progress
+                GC_CUDA(cudaMemsetAsync(v.tbuf, 0, px * sizeof(float), s));
+                GC_CUDA(cudaMemsetAsync(v.state, 0, px * 4 * sizeof(float), s));
+                b->queue[pick].started = true;
+            }
+            b->queue[pick].seq = b->admissions++;
             pixels += px;
             b->last_cam[0] = v.inv_view[3];
             b->last_cam[1] = v.inv_view[7];
             b->last_cam[2] = v.inv_view[11];
+            b->last_volume = v.volume;
             b->have_cam = true;
             if (pick) b->queue.front().skipped++;
             b->active.push_back(b->queue[pick]);
@@ -1237,7 +1246,7 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         }
         GC_CUDA(cudaMemsetAsync(b->d_status, 0, n * sizeof(uint32_t), s));
         GC_CUDA(cudaEventRecord(b->ev_r0, s));
-        render(C, views.data(), n, s, b->d.lookahead, true, &b->graph, b->h_views);
+        render(C, views.data(), n, s, true, &b->graph, b->h_views);
         GC_CUDA(cudaEventRecord(b->ev_r1, s));
         GC_CUDA(cudaMemcpyAsync(b->h_status, b->d_status, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         const bool scanned = batch_update(C, s);
@@ -1274,6 +1283,22 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         for (uint32_t i = 0; i < na; ++i)
             if (!gone[i]) keep.push_back(b->active[i]);
         b->active.swap(keep);
+        // Memory-pressure parking: the working sets of the active views do not
+        // fit the pool -- the newest view leaves for the queue's front (its
+        // buffers keep its progress) so that the others stop evicting each
+        // other's bricks.
+        const double demand_now = static_cast<double>(b->last_used) + static_cast<double>(b->last_misses);
+        if (all && b->d.park_above > 0.f && b->active.size() > 1 &&
+            demand_now > b->d.park_above * static_cast<double>(C->nslots)) {
+            size_t newest = 0;
+            for (size_t i = 1; i < b->active.size(); ++i)
+                if (b->active[i].seq > b->active[newest].seq) newest = i;
+            gc_batch::Item it = b->active[newest];
+            it.epoch = gc_batch::kNever;  // render it when it resumes
+            b->active.erase(b->active.begin() + static_cast<std::ptrdiff_t>(newest));
+            b->queue.push_front(it);
+            b->st.parked++;
+        }
     });
 }
 

@@ -270,37 +270,6 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
     return kEmpty;
 }
 
-// Page-table probe for the lookahead walk: loads the entry when the ray enters
-// a new brick, stamps the usage of a resident one (the ray will sample it once
-// its first missing brick is in) and raises the request of a missing one.
-// Returns the entry's status, or kMapped when the brick did not change.
-__device__ __forceinline__ int probe(const CacheView &cv, const LevelTables &lt, uint32_t lvl, V3 np, Walk &w,
-                                     bool &raised) {
-    const float px = np.x * lt.ior[lvl][0];  // the brick arithmetic of fetch()
-    const float py = np.y * lt.ior[lvl][1];
-    const float pz = np.z * lt.ior[lvl][2];
-    const uint32_t cx = lt.off[lvl] + static_cast<uint32_t>(px * static_cast<float>(lt.nb[lvl][0]));
-    const uint32_t cy = static_cast<uint32_t>(py * static_cast<float>(lt.nb[lvl][1]));
-    const uint32_t cz = static_cast<uint32_t>(pz * static_cast<float>(lt.nb[lvl][2]));
-    raised = false;
-    if (cx == w.pcx && cy == w.pcy && cz == w.pcz) return static_cast<int>(w.entry.w);
-    const uint64_t idx = cx + static_cast<uint64_t>(cy) * cv.mx + static_cast<uint64_t>(cz) * cv.mx * cv.my;
-    w.entry = __ldg(cv.mrpd + idx);
-    w.pcx = cx;
-    w.pcy = cy;
-    w.pcz = cz;
-    if (w.entry.w == 1u) {
-        const uint32_t B = cv.B;
-        uint32_t *u = cv.usage + (w.entry.x / B + (w.entry.y / B) * cv.sx + (w.entry.z / B) * cv.sx * cv.sy);
-        if (*u != cv.ts) *u = cv.ts;
-    } else if (w.entry.w == 0u) {
-        uint32_t *r = cv.req + idx;
-        if (*r != cv.ts) *r = cv.ts;
-        raised = true;
-    }
-    return static_cast<int>(w.entry.w);
-}
-
 // Per-ray state between samples.  The method is split into ray_setup /
 // ray_step / ray_finish so that both schedulers below run the same code.
 struct Ray {
@@ -399,44 +368,6 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
     return true;
 }
 
-// Request walk of a ray that stopped at a missing brick (batched form only;
-// the plain method requests the first missing brick alone).  The walk
-// continues from the stop with the march's own positions, level choice and
-// step sizes -- as if every missing brick were resident -- and requests up to
-// `budget` further missing bricks, so that one load cycle brings in most of
-// what the ray needs instead of one brick per cycle.  Nothing is sampled or
-// composited and the saved progressive state is already written: the image
-// is the one the first-miss policy converges to.  Rays that would terminate
-// early ask for some bricks they never sample.
-__device__ __noinline__ void lookahead_walk(const CacheView &cv, const LevelTables &lt, Ray r, uint32_t budget) {
-    const ViewParams &vp = *r.vp;
-    r.t += vp.step[r.lod];  // the stop sample's brick is requested already
-    r.pos = r.pos + r.dir * vp.step[r.lod];
-    const uint32_t nl = vp.nlevels;
-    while (r.t < r.tfar) {
-        const float alpha = r.t / r.tfar;
-        const float pX = r.endX * alpha;
-        const float pY = r.endY * alpha;
-        V3 tp = r.pos * 0.495f + v3(0.495f, 0.495f, 0.495f);
-        tp.z = 1.0f - tp.z;
-        const V3 np = v3(clampf(tp.x, 0.f, 0.99f), clampf(tp.y, 0.f, 0.99f), clampf(tp.z, 0.f, 0.99f));
-        while (r.lod + 1 < nl && !(r.sL >= pX || r.sU >= pY)) {
-            ++r.lod;
-            if (r.lod + 1 < nl) {
-                const V3 nn = v3(vp.inv_size[r.lod + 1][0], vp.inv_size[r.lod + 1][1], vp.inv_size[r.lod + 1][2]);
-                r.sL = length(r.dirLeft * nn);
-                r.sU = length(r.dirUp * nn);
-            }
-        }
-        bool raised = false;
-        const int st = probe(cv, lt, vp.level_base + r.lod, np, r.w, raised);
-        if (raised && --budget == 0) return;
-        const float dt = st == kEmpty ? vp.tstep : vp.step[r.lod];
-        r.t += dt;
-        r.pos = r.pos + r.dir * dt;
-    }
-}
-
 // One iteration of the march loop (RayCasters.cu:122-188).  Returns false
 // when the loop ends.
 template <typename T>
@@ -471,7 +402,6 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
             else
                 vp.state[4 * r.i] = r.maxOp;
             r.unm = true;
-            if (vp.lookahead) lookahead_walk(cv, lt, r, vp.lookahead);
             return false;
         }
         r.t += vp.tstep;

@@ -409,15 +409,14 @@ typedef struct gc_batch_desc {
                                 while the active views' demand -- slots their
                                 last full pass used plus the missing bricks
                                 the last scan found -- exceeds this fraction
-                                of the pool slots (<= 0: no limit).  With a
-                                lookahead the first pass of a view requests
-                                its whole working set, so the demand is
-                                known one tick after admission.               */
+                                of the pool slots (<= 0: no limit)             */
     uint32_t max_admit;      /* views admitted per tick (0: no limit)          */
-    uint32_t lookahead;      /* request policy: a ray that stops at a missing
-                                brick also requests up to this many further
-                                missing bricks along its path (0: only the
-                                first, as the plain method does)               */
+    float park_above;        /* memory-pressure parking: while that demand
+                                exceeds this fraction of the pool slots and
+                                more than one view is active, the most recently
+                                admitted view leaves the batch for the front of
+                                the queue with its progressive state kept, and
+                                resumes when admission allows (<= 0: never)    */
     uint32_t reorder_window; /* locality-aware admission: pick, among the first
                                 reorder_window queued views, the one whose
                                 camera is nearest the last admitted view's
@@ -453,6 +452,7 @@ typedef struct gc_batch_stats {
     uint64_t install_ticks;   /* ticks that installed bricks                   */
     uint64_t graph_replays;   /* render launches replayed from the batch's CUDA
                                  graph (view-table copy + persistent ray caster) */
+    uint64_t parked;          /* views parked under memory pressure            */
     double render_ms;         /* device time of the render launches            */
     double tick_ms;           /* host time inside gc_batch_tick                */
     double wait_ms;           /* host time waiting for the loader              */

@@ -199,15 +199,16 @@ def test_async_loader_converges_to_same_image(gc, orc, torch_cuda):
     assert np.array_equal(imgs[0], imgs[1])
 
 
-@pytest.mark.parametrize("lookahead,sync,reorder", [(0, True, 0), (0, False, 0), (1 << 20, True, 0), (3, False, 4),
-                                                    (0, True, 3)])
-def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, lookahead, sync, reorder):
+@pytest.mark.parametrize("park,sync,reorder", [(0.0, True, 0), (0.0, False, 0), (0.05, True, 0), (0.05, False, 4),
+                                               (0.0, True, 3)])
+def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, park, sync, reorder):
     """Continuous batching (admission by pixel budget, one persistent launch
     per tick, skipped passes for views that cannot progress, retirement on
     convergence) gives every view the image it gets when rendered alone to
-    convergence, with the synchronous or the asynchronous loader, with the
-    first-miss or the lookahead request policy and with arrival-order or
-    locality-ordered admission; the per-view status word reports convergence
+    convergence, with the synchronous or the asynchronous loader, with
+    arrival-order or locality-ordered admission and with views parked under
+    memory pressure (a low park threshold parks views often; they resume from
+    their progressive state); the per-view status word reports convergence
     exactly."""
     specs = [((64, 48), 1), ((33, 17), 4), ((96, 80), 7), ((40, 40), 10), ((80, 24), 5)]
     tf = scenario.ramp_tf()
@@ -230,7 +231,7 @@ def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, lookahead, sy
     s.cm.close()
 
     s2 = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 64, sync=sync)
-    b = gc.Batch(s2.cm, max_views=3, max_pixels=96 * 80 + 64 * 48, lookahead=lookahead, reorder_window=reorder)
+    b = gc.Batch(s2.cm, max_views=3, max_pixels=96 * 80 + 64 * 48, park_above=park, reorder_window=reorder)
     bufs = []
     for i, ((W, H), cam) in enumerate(specs):
         g, _ = s2.buffers(W, H)
@@ -250,5 +251,7 @@ def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, lookahead, sy
         assert np.array_equal(bufs[i][0].cpu().numpy(), single[i]), i
     st = b.stats()
     assert st.graph_replays == st.render_ticks > 0  # every batched render replayed the graph
+    if park > 0:
+        assert st.parked > 0
     b.close()
     assert s2.cm.stats().device_error == 0
