@@ -9,8 +9,8 @@ A step renders one view to convergence, the way the reference's own benchmark
 counts time until "Frame done" (ref:bench.sh:39-55): restart the progressive
 buffers (the camera moved), then repeat {render, cache update} until the
 update reports an empty miss list.  Each iteration pages the missing bricks in
-from host memory (miss scan -> loader -> pinned staging -> cudaMemcpyAsync ->
-install).  Rays are counted once per converged view.
+from host memory (miss scan -> loader -> upload on a side stream -> install).
+Rays are counted once per converged view.
 
 Workloads (seeded synthetic volumes with the shapes of the benchmark configs;
 no public dataset is used):
@@ -24,7 +24,13 @@ no public dataset is used):
       views of a batch in one persistent launch sharing the cache's miss list;
       the same views are also rendered one at a time (plain) for the ratio.
   c1  256^3 u8 (small; used for profiling).
-The pool and page directory exceed L2 (129 MB) for c2/c3.
+  c4  (serving, --config c4)  three volumes (1024^3 u8, 2048^3 u16,
+      4096x4096x2048 u8) in one 24 GiB shared pool; Poisson requests at 200/s
+      with a random volume, camera, size and one of 4 transfer functions;
+      latency from arrival to retirement.
+The pool and page directory exceed L2 (129 MB) for c2/c3/c4.  Bricks are paged
+in by a gather kernel reading the host store over the host link where the
+device can (--upload staged: host copies + cudaMemcpyAsync).
 
 value  : views rendered into device buffers.
 e2e    : the same through the C ABI with the converged RGBA frame read back
