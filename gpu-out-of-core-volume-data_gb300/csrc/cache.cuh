@@ -46,6 +46,7 @@ struct CacheView {
     uint32_t sx, sy, sz;
     uint32_t B, c, Beff;
     uint32_t eb;          // bytes per voxel of every volume, 0 when the volumes differ
+    uint32_t nc;          // channels per voxel (1, or 2 for two 8-bit channels)
     uint64_t slot_bytes;  // pool slot stride: B^3 x the widest voxel
     uint32_t ts;
 };
@@ -58,6 +59,7 @@ struct ViewParams {
     float tstep, focal, early;
     uint32_t mode, sampler;
     uint32_t tfw;
+    uint32_t tfh;                       // 2D transfer function rows (two-channel volumes)
     const float *tf;
     uint32_t *rgba;
     float *tbuf;

@@ -97,6 +97,7 @@ struct gc_cache {
     gc::LevelTables lt;
     uint32_t mx = 0, my = 0, mz = 0, nslots = 0, B = 0, c = 0, Beff = 0;
     uint32_t eb = 0;                  // voxel bytes of every volume, 0 when they differ
+    uint32_t nc = 1;                  // channels per voxel (the same for every volume)
     uint64_t nentries = 0;
     uint64_t slot_bytes = 0;          // pool slot: B^3 x the widest voxel
     uint64_t big_stride = 0;          // staging stride: the largest big brick
@@ -372,6 +373,7 @@ static CacheView cache_view(const gc_cache *C) {
     cv.c = C->c;
     cv.Beff = C->Beff;
     cv.eb = C->eb;
+    cv.nc = C->nc;
     cv.slot_bytes = C->slot_bytes;
     cv.ts = C->ts;
     return cv;
@@ -507,7 +509,12 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
     GC_REQUIRE(in.sampler == GC_SAMPLER_REFERENCE || in.sampler == GC_SAMPLER_TRILINEAR, "bad sampler");
     GC_REQUIRE(in.volume < C->vols.size(), "the view's volume is not in this cache");
     const Volume &V = C->vols[in.volume];
-    GC_REQUIRE(V.desc.channels == 1, "the ray caster renders single-channel volumes");
+    GC_REQUIRE(V.desc.channels == 1 || (V.desc.channels == 2 && V.desc.encoded_bytes == 2),
+               "the ray caster renders one channel (8, 16 or 32 bit) or two 8-bit channels");
+    if (V.desc.channels == 2)
+        GC_REQUIRE(in.tf_height >= 1, "a two-channel volume needs a 2D transfer function (tf_height >= 1)");
+    else
+        GC_REQUIRE(in.tf_height <= 1, "a 2D transfer function needs a two-channel volume");
     std::memset(&out, 0, sizeof(out));
     std::memcpy(out.m, in.inv_view, sizeof(out.m));
     out.W = in.width;
@@ -522,6 +529,7 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
     out.mode = in.mode;
     out.sampler = in.sampler;
     out.tfw = in.tf_width;
+    out.tfh = in.tf_height > 0 ? in.tf_height : 1;
     out.tf = in.tf;
     out.rgba = in.rgba;
     out.tbuf = in.tbuf;
@@ -605,6 +613,7 @@ static gc_cache *create_cache(const gc_cache_desc *desc, const gc_volume_desc *v
         GC_REQUIRE(layouts[v].nb_levels >= 1 && layouts[v].nb_levels <= GC_MAX_LEVELS, "bad layout");
         GC_REQUIRE(vols[v].brick_size == vols[0].brick_size && vols[v].covering == vols[0].covering,
                    "volumes sharing a pool need the same BrickSize and VoxelCovering");
+        GC_REQUIRE(vols[v].channels == vols[0].channels, "volumes sharing a pool need the same NumberChannels");
         total_levels += layouts[v].nb_levels;
     }
     GC_REQUIRE(total_levels <= kMaxCacheLevels, "too many levels in one cache");
@@ -622,6 +631,7 @@ static gc_cache *create_cache(const gc_cache_desc *desc, const gc_volume_desc *v
         C->c = vols[0].covering;
         C->Beff = C->B - 2 * C->c;
         C->eb = vols[0].encoded_bytes;
+        C->nc = vols[0].channels;
         uint32_t eb_max = 0;
         C->vols.resize(n);
         for (uint32_t v = 0; v < n; ++v) {

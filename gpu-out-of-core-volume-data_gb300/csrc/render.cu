@@ -27,6 +27,7 @@
 // through the read-only path from the slot-major HBM pool.
 #include <algorithm>
 #include <climits>
+#include <type_traits>
 
 #include "cache.cuh"
 #include "gc_internal.h"
@@ -107,6 +108,31 @@ __device__ __forceinline__ float4 tf_lookup(const float *__restrict__ tf, uint32
     const float4 t1 = __ldg(reinterpret_cast<const float4 *>(tf) + i1);
     return make_float4(t0.x + (t1.x - t0.x) * a, t0.y + (t1.y - t0.y) * a, t0.z + (t1.z - t0.z) * a,
                        t0.w + (t1.w - t0.w) * a);
+}
+
+// 2D transfer function (two-channel volumes): a w x h table of RGBA, channel
+// 0 along w and channel 1 along h, read with the 1D lookup's rule on each
+// axis (bilinear, edge-clamped).
+__device__ __forceinline__ float4 tf2d_lookup(const float *__restrict__ tf, uint32_t w, uint32_t h, float s0,
+                                              float s1) {
+    const float xb = s0 * static_cast<float>(w) - 0.5f, yb = s1 * static_cast<float>(h) - 0.5f;
+    const float flx = floorf(xb), fly = floorf(yb);
+    const float ax = xb - flx, ay = yb - fly;
+    const int hx = static_cast<int>(w) - 1, hy = static_cast<int>(h) - 1;
+    int i0 = static_cast<int>(flx), i1 = i0 + 1, j0 = static_cast<int>(fly), j1 = j0 + 1;
+    i0 = i0 < 0 ? 0 : (i0 > hx ? hx : i0);
+    i1 = i1 < 0 ? 0 : (i1 > hx ? hx : i1);
+    j0 = j0 < 0 ? 0 : (j0 > hy ? hy : j0);
+    j1 = j1 < 0 ? 0 : (j1 > hy ? hy : j1);
+    const float4 *t = reinterpret_cast<const float4 *>(tf);
+    const float4 t00 = __ldg(t + j0 * static_cast<int>(w) + i0), t10 = __ldg(t + j0 * static_cast<int>(w) + i1);
+    const float4 t01 = __ldg(t + j1 * static_cast<int>(w) + i0), t11 = __ldg(t + j1 * static_cast<int>(w) + i1);
+    const float4 r0 = make_float4(t00.x + (t10.x - t00.x) * ax, t00.y + (t10.y - t00.y) * ax,
+                                  t00.z + (t10.z - t00.z) * ax, t00.w + (t10.w - t00.w) * ax);
+    const float4 r1 = make_float4(t01.x + (t11.x - t01.x) * ax, t01.y + (t11.y - t01.y) * ax,
+                                  t01.z + (t11.z - t01.z) * ax, t01.w + (t11.w - t01.w) * ax);
+    return make_float4(r0.x + (r1.x - r0.x) * ay, r0.y + (r1.y - r0.y) * ay, r0.z + (r1.z - r0.z) * ay,
+                       r0.w + (r1.w - r0.w) * ay);
 }
 
 template <typename T>
@@ -197,8 +223,25 @@ struct Walk {
 };
 
 // Voxel sampling of one brick (slot base address), typed by T; MixedVoxel
-// picks the type from the view's voxel width (caches whose volumes differ).
+// picks the type from the view's voxel width (caches whose volumes differ);
+// TwoU8 samples two interleaved 8-bit channels (NumberChannels 2) into a
+// float2 for the 2D transfer function.
 struct MixedVoxel {};
+struct TwoU8 {};
+template <typename T>
+struct SampleOf {
+    using type = float;
+};
+template <>
+struct SampleOf<TwoU8> {
+    using type = float2;
+};
+__device__ __forceinline__ float first_channel(float s) { return s; }
+__device__ __forceinline__ float first_channel(float2 s) { return s.x; }
+__device__ __forceinline__ float4 classify(const ViewParams &vp, float s) { return tf_lookup(vp.tf, vp.tfw, s); }
+__device__ __forceinline__ float4 classify(const ViewParams &vp, float2 s) {
+    return tf2d_lookup(vp.tf, vp.tfw, vp.tfh, s.x, s.y);
+}
 
 template <typename T>
 __device__ __forceinline__ float sample_slot(const uint8_t *base, uint32_t /*eb*/, const CacheView &cv,
@@ -225,13 +268,64 @@ __device__ __forceinline__ float sample_slot<MixedVoxel>(const uint8_t *base, ui
     if (eb == 2) return sample_slot<uint16_t>(base, eb, cv, sampler, fx, fy, fz);
     return sample_slot<float>(base, eb, cv, sampler, fx, fy, fz);
 }
+// Two interleaved u8 channels: each channel sampled with the one-channel
+// rule (corner mean of 8 voxels, or trilinear), voxel i channel k at byte 2i+k.
+__device__ __forceinline__ float2 sample_slot_two(const uint8_t *__restrict__ b, const CacheView &cv,
+                                                  uint32_t sampler, float fx, float fy, float fz) {
+    const uint32_t B = cv.B, BB = B * B;
+    if (sampler == GC_SAMPLER_REFERENCE) {
+        uint32_t lx = cv.c + static_cast<uint32_t>(fx) % cv.Beff;
+        uint32_t ly = cv.c + static_cast<uint32_t>(fy) % cv.Beff;
+        uint32_t lz = cv.c + static_cast<uint32_t>(fz) % cv.Beff;
+        lx = lx > 0 ? lx : 1u;
+        ly = ly > 0 ? ly : 1u;
+        lz = lz > 0 ? lz : 1u;
+        const uint32_t i0 = ((lz - 1) * B + (ly - 1)) * B + (lx - 1);
+        const uint32_t id[8] = {i0, i0 + 1, i0 + B, i0 + B + 1, i0 + BB, i0 + BB + 1, i0 + BB + B, i0 + BB + B + 1};
+        uint32_t s0 = 0, s1 = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uchar2 v = __ldg(reinterpret_cast<const uchar2 *>(b) + id[k]);
+            s0 += v.x;
+            s1 += v.y;
+        }
+        return make_float2(static_cast<float>(s0) / 2040.0f, static_cast<float>(s1) / 2040.0f);
+    }
+    uint32_t x0, y0, z0;
+    float wx, wy, wz;
+    tri_axis(fx, cv.c, cv.Beff, B, x0, wx);
+    tri_axis(fy, cv.c, cv.Beff, B, y0, wy);
+    tri_axis(fz, cv.c, cv.Beff, B, z0, wz);
+    const uint32_t i = (z0 * B + y0) * B + x0;
+    float out[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        auto lv = [&](uint32_t j) { return static_cast<float>(__ldg(b + 2 * j + k)); };
+        const float c00 = lv(i) + (lv(i + 1) - lv(i)) * wx;
+        const float c10 = lv(i + B) + (lv(i + B + 1) - lv(i + B)) * wx;
+        const float c01 = lv(i + BB) + (lv(i + BB + 1) - lv(i + BB)) * wx;
+        const float c11 = lv(i + BB + B) + (lv(i + BB + B + 1) - lv(i + BB + B)) * wx;
+        const float c0 = c00 + (c10 - c00) * wy;
+        const float c1 = c01 + (c11 - c01) * wy;
+        out[k] = (c0 + (c1 - c0) * wz) / 255.0f;
+    }
+    return make_float2(out[0], out[1]);
+}
+template <typename T>
+__device__ __forceinline__ typename SampleOf<T>::type sample_any(const uint8_t *base, uint32_t eb, const CacheView &cv,
+                                                                 uint32_t sampler, float fx, float fy, float fz) {
+    if constexpr (std::is_same<T, TwoU8>::value)
+        return sample_slot_two(base, cv, sampler, fx, fy, fz);
+    else
+        return sample_slot<T>(base, eb, cv, sampler, fx, fy, fz);
+}
 
 // Page walk + sample at the normalized position np of cache level lvl (the
 // view's level base + its LOD): K_CacheManager::get_normalized
 // (K_CacheManager.hpp:265-361).
 template <typename T>
 __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt, uint32_t sampler, uint32_t eb,
-                                     uint32_t lvl, V3 np, Walk &w, float &sample) {
+                                     uint32_t lvl, V3 np, Walk &w, typename SampleOf<T>::type &sample) {
     const float px = np.x * lt.ior[lvl][0];
     const float py = np.y * lt.ior[lvl][1];
     const float pz = np.z * lt.ior[lvl][2];
@@ -258,7 +352,7 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
         const float fx = px * static_cast<float>(lt.vvox[lvl][0]);
         const float fy = py * static_cast<float>(lt.vvox[lvl][1]);
         const float fz = pz * static_cast<float>(lt.vvox[lvl][2]);
-        sample = sample_slot<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, eb, cv, sampler, fx, fy, fz);
+        sample = sample_any<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, eb, cv, sampler, fx, fy, fz);
         return kMapped;
     }
     if (e.w == 0u) {
@@ -392,7 +486,7 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
         }
     }
     const uint32_t lod = r.lod;
-    float sample = 0.f;
+    typename SampleOf<T>::type sample{};
     const int st = fetch<T>(cv, lt, vp.sampler, vp.eb, vp.level_base + lod, np, r.w, sample);
     if (st != kMapped) {
         if (st == kUnmapped) {
@@ -410,7 +504,7 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
         return true;
     }
     if (r.dvr) {
-        float4 col = tf_lookup(vp.tf, vp.tfw, sample);
+        float4 col = classify(vp, sample);
         col.w = 1.0f - gc_pow(1.0f - col.w, vp.kexp[lod]);
         if (col.w > 0.001f) {
             col.x *= col.w;
@@ -423,7 +517,7 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
             r.fc.w = r.fc.w + col.w * rr;
         }
     } else {
-        r.maxOp = fmaxf(r.maxOp, sample);
+        r.maxOp = fmaxf(r.maxOp, first_channel(sample));
     }
     r.t += vp.step[lod];
     r.pos = r.pos + r.dir * vp.step[lod];
@@ -595,11 +689,16 @@ struct RenderLaunch {
     void *func;
     uint32_t grid, threads;
 };
+// Voxel kind of a cache: its voxel width (1, 2, 4), 0 when its volumes'
+// widths differ, kTwoChannelU8 for two 8-bit channels.
+constexpr uint32_t kTwoChannelU8 = 0x202;
+static uint32_t voxel_kind(const CacheView &cv) { return cv.nc == 2 ? kTwoChannelU8 : cv.eb; }
+
 static RenderLaunch render_launch_config(uint32_t eb, uint32_t total_tiles) {
     const RenderTuning tune = render_tuning();
     const uint32_t threads = tune.threads;
     GC_REQUIRE(threads == 64 || threads == 128 || threads == 256, "render threads must be 64, 128 or 256");
-    static int occupancy[2][4][3] = {};
+    static int occupancy[2][5][3] = {};
     const int tslot = threads == 64 ? 0 : (threads == 128 ? 1 : 2);
     auto config = [&](auto kernel, int sched, int slot) {
         int &occ = occupancy[sched][slot][tslot];
@@ -621,6 +720,8 @@ static RenderLaunch render_launch_config(uint32_t eb, uint32_t total_tiles) {
         case 4: return pix ? config(render_pixels_kernel<float>, 1, 2) : config(render_kernel<float>, 0, 2);
         case 0:  // volumes of different voxel widths share the cache
             return pix ? config(render_pixels_kernel<MixedVoxel>, 1, 3) : config(render_kernel<MixedVoxel>, 0, 3);
+        case kTwoChannelU8:  // two 8-bit channels per voxel (2D transfer function)
+            return pix ? config(render_pixels_kernel<TwoU8>, 1, 4) : config(render_kernel<TwoU8>, 0, 4);
         default: fail(GC_ERR_UNSUPPORTED, "the ray caster supports one channel of 1, 2 or 4 bytes");
     }
 }
@@ -629,7 +730,7 @@ void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams 
                    const ViewParams * /*views_host*/, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
                    uint32_t * /*err*/, cudaStream_t s) {
     if (total_tiles == 0) return;
-    const RenderLaunch L = render_launch_config(cv.eb, total_tiles);
+    const RenderLaunch L = render_launch_config(voxel_kind(cv), total_tiles);
     uint32_t nwarps = L.grid * (L.threads / 32);
     void *args[] = {const_cast<CacheView *>(&cv), const_cast<LevelTables *>(&lt), &views_dev, &nviews, &total_tiles,
                     &queue, &nwarps};
@@ -656,7 +757,7 @@ void launch_render_graph(RenderGraph &g, const CacheView &cv, const LevelTables 
                          const ViewParams *views_pinned, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
                          cudaStream_t s) {
     if (total_tiles == 0) return;
-    const RenderLaunch L = render_launch_config(cv.eb, total_tiles);
+    const RenderLaunch L = render_launch_config(voxel_kind(cv), total_tiles);
     uint32_t nwarps = L.grid * (L.threads / 32);
     const ViewParams *vd = views_dev;
     void *args[] = {const_cast<CacheView *>(&cv), const_cast<LevelTables *>(&lt), &vd, &nviews, &total_tiles,

@@ -351,6 +351,12 @@ typedef struct gc_view {
                                  clears it before the pass                      */
     uint32_t volume;          /* volume of a shared cache (gc_cache_create_shared);
                                  0 for a single-volume cache                    */
+    uint32_t tf_height;       /* two-channel volumes (NumberChannels 2, 8 bits
+                                 each): tf is a 2D table of tf_height rows of
+                                 tf_width RGBA entries, channel 0 along a row,
+                                 channel 1 across rows, read bilinearly; MIP
+                                 classifies the maximum of channel 0 with row 0.
+                                 0 or 1 for one-channel volumes                 */
 } gc_view;
 
 /* Camera of updateViewMatrix (Display_helper.cpp:93-118): the rows of

@@ -777,6 +777,32 @@ static f4 tf_lookup(const float *tf, uint32_t w, float s) {
     return r;
 }
 
+/* 2D transfer function of two-channel volumes: bilinear over a w x h table,
+   channel 0 along a row, channel 1 across rows (no counterpart in the
+   reference, whose ray caster reads one channel; same rule as tf_lookup on
+   each axis). */
+static f4 tf2d_lookup(const float *tf, uint32_t w, uint32_t h, float s0, float s1) {
+    float xb = s0 * (float)w - 0.5f, yb = s1 * (float)h - 0.5f;
+    float flx = floorf(xb), fly = floorf(yb);
+    float ax = xb - flx, ay = yb - fly;
+    int hx = (int)w - 1, hy = (int)h - 1;
+    int i0 = (int)flx, i1 = i0 + 1, j0 = (int)fly, j1 = j0 + 1;
+    i0 = i0 < 0 ? 0 : (i0 > hx ? hx : i0);
+    i1 = i1 < 0 ? 0 : (i1 > hx ? hx : i1);
+    j0 = j0 < 0 ? 0 : (j0 > hy ? hy : j0);
+    j1 = j1 < 0 ? 0 : (j1 > hy ? hy : j1);
+    const float *t00 = tf + 4 * (j0 * (int)w + i0), *t10 = tf + 4 * (j0 * (int)w + i1);
+    const float *t01 = tf + 4 * (j1 * (int)w + i0), *t11 = tf + 4 * (j1 * (int)w + i1);
+    float r0[4], r1[4];
+    for (int k = 0; k < 4; ++k) {
+        r0[k] = t00[k] + (t10[k] - t00[k]) * ax;
+        r1[k] = t01[k] + (t11[k] - t01[k]) * ax;
+    }
+    f4 r = {r0[0] + (r1[0] - r0[0]) * ay, r0[1] + (r1[1] - r0[1]) * ay, r0[2] + (r1[2] - r0[2]) * ay,
+            r0[3] + (r1[3] - r0[3]) * ay};
+    return r;
+}
+
 typedef struct {
     float inv_size[GC_MAX_LEVELS][3];
     float step[GC_MAX_LEVELS];
@@ -828,6 +854,7 @@ typedef struct {
     uint32_t e[4];
 } walk;
 
+/* sample[0] (and sample[1] for two 8-bit channels, voxel i channel k at byte 2i+k) */
 static int fetch32(orc_cache *c, uint32_t sampler, uint32_t lod, f3 np, walk *w, float *sample) {
     float px = np.x * c->ior[lod][0], py = np.y * c->ior[lod][1], pz = np.z * c->ior[lod][2];
     uint32_t cx = c->off[lod] + (uint32_t)(px * (float)c->nb[lod][0]);
@@ -846,6 +873,43 @@ static int fetch32(orc_cache *c, uint32_t sampler, uint32_t lod, f3 np, walk *w,
         __atomic_store_n(&c->usage[slot], c->ts, __ATOMIC_RELAXED);
         const uint8_t *sb = c->pool + (uint64_t)slot * c->brick_bytes;
         float fx = px * (float)c->vvox[lod][0], fy = py * (float)c->vvox[lod][1], fz = pz * (float)c->vvox[lod][2];
+        if (c->d.volume.channels == 2) {
+            uint32_t BB2 = B * B;
+            if (sampler == GC_SAMPLER_REFERENCE) {
+                uint32_t lx = c->c + (uint32_t)fx % c->Beff, ly = c->c + (uint32_t)fy % c->Beff,
+                         lz = c->c + (uint32_t)fz % c->Beff;
+                if (lx == 0) lx = 1;
+                if (ly == 0) ly = 1;
+                if (lz == 0) lz = 1;
+                uint32_t i0 = ((lz - 1) * B + (ly - 1)) * B + (lx - 1);
+                uint32_t ids[8] = {i0, i0 + 1, i0 + B, i0 + B + 1, i0 + BB2, i0 + BB2 + 1, i0 + BB2 + B, i0 + BB2 + B + 1};
+                uint32_t s0 = 0, s1 = 0;
+                for (int k = 0; k < 8; ++k) {
+                    s0 += sb[2 * ids[k]];
+                    s1 += sb[2 * ids[k] + 1];
+                }
+                sample[0] = (float)s0 / 2040.0f;
+                sample[1] = (float)s1 / 2040.0f;
+            } else {
+                uint32_t x0, y0, z0;
+                float wx, wy, wz;
+                tri_axis(fx, c->c, c->Beff, B, &x0, &wx);
+                tri_axis(fy, c->c, c->Beff, B, &y0, &wy);
+                tri_axis(fz, c->c, c->Beff, B, &z0, &wz);
+                uint32_t i = (z0 * B + y0) * B + x0;
+                for (int k = 0; k < 2; ++k) {
+#define LV2(j) ((float)sb[2 * (j) + k])
+                    float c00 = LV2(i) + (LV2(i + 1) - LV2(i)) * wx;
+                    float c10 = LV2(i + B) + (LV2(i + B + 1) - LV2(i + B)) * wx;
+                    float c01 = LV2(i + BB2) + (LV2(i + BB2 + 1) - LV2(i + BB2)) * wx;
+                    float c11 = LV2(i + BB2 + B) + (LV2(i + BB2 + B + 1) - LV2(i + BB2 + B)) * wx;
+#undef LV2
+                    float c0 = c00 + (c10 - c00) * wy, c1 = c01 + (c11 - c01) * wy;
+                    sample[k] = (c0 + (c1 - c0) * wz) / 255.0f;
+                }
+            }
+            return 0;
+        }
         if (sampler == GC_SAMPLER_REFERENCE) {
             uint32_t lx = c->c + (uint32_t)fx % c->Beff, ly = c->c + (uint32_t)fy % c->Beff,
                      lz = c->c + (uint32_t)fz % c->Beff;
@@ -945,6 +1009,7 @@ static void march32(orc_cache *c, const gc_view *v, const float *tf, const lod_t
         int unm = 0;
         float maxOp = dvr ? 0.f : state[4 * i];
         uint32_t nl = c->nl;
+        int two = c->d.volume.channels == 2;
         while ((!dvr || fc.w < v->early_alpha) && t < tfar) {
             float alpha = t / tfar;
             float pX = endX * alpha, pY = endY * alpha;
@@ -958,8 +1023,9 @@ static void march32(orc_cache *c, const gc_view *v, const float *tf, const lod_t
                 float sl = len3(mulv(dirLeft, ns)), su = len3(mulv(dirUp, ns));
                 if (sl >= pX * 1.0f || su >= pY * 1.0f) break;
             }
-            float sample = 0.f;
-            int st = fetch32(c, v->sampler, lod, np, &w, &sample);
+            float smp[2] = {0.f, 0.f};
+            int st = fetch32(c, v->sampler, lod, np, &w, smp);
+            float sample = smp[0];
             if (st != 0) {
                 if (st == 1) {
                     if (!unm) {
@@ -981,7 +1047,8 @@ static void march32(orc_cache *c, const gc_view *v, const float *tf, const lod_t
                 continue;
             }
             if (dvr) {
-                f4 col = tf_lookup(tf, v->tf_width, sample);
+                f4 col = two ? tf2d_lookup(tf, v->tf_width, v->tf_height, smp[0], smp[1])
+                             : tf_lookup(tf, v->tf_width, sample);
                 col.w = 1.0f - orc_pow(1.0f - col.w, T->kexp[lod]);
                 if (col.w > 0.001f) {
                     col.x *= col.w;

@@ -83,3 +83,18 @@ def bumps_tf(seed, width=256, nbumps=3):
         a += h * np.exp(-0.5 * ((x - c) / w) ** 2)
     tf = np.stack([np.clip(0.3 + x, 0, 1), np.clip(1.2 - x, 0, 1), 0.5 + 0.5 * np.sin(6 * x), np.clip(a, 0, 1)], 1)
     return tf.astype(np.float32)
+
+
+def tf2d(seed, width=64, height=48):
+    """2D RGBA table for two-channel volumes (row-major, height rows of width
+    entries): alpha from seeded bumps over channel 0, modulated along channel 1."""
+    rng = np.random.default_rng(seed)
+    x = np.linspace(0.0, 1.0, width)[None, :]
+    y = np.linspace(0.0, 1.0, height)[:, None]
+    a = np.zeros((height, width))
+    for _ in range(3):
+        c, w, h = rng.uniform(0.2, 0.9), rng.uniform(0.04, 0.1), rng.uniform(0.2, 0.7)
+        a = a + h * np.exp(-0.5 * ((x - c) / w) ** 2) * (0.3 + 0.7 * y)
+    rgb = np.stack([np.broadcast_to(np.clip(0.2 + x, 0, 1), a.shape), np.broadcast_to(np.clip(1.0 - y, 0, 1), a.shape),
+                    0.5 + 0.5 * np.sin(5 * x + 3 * y)], -1)
+    return np.concatenate([rgb, np.clip(a, 0, 1)[..., None]], -1).astype(np.float32)

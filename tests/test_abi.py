@@ -135,3 +135,46 @@ def test_layout_product_equals_oracle(gc, orc):
         v = gc.volume_desc(size, B, c, eb, nc, bb)
         a, b = gc.compute_layout(v), orc.layout(v)
         assert bytes(a) == bytes(b)
+
+
+# ctypes mirrors of the C structs (product binding, and the oracle's copies)
+STRUCTS = {"gc_volume_desc": "VolumeDesc", "gc_layout": "Layout", "gc_blob": "Blob", "gc_generator": "Generator",
+           "gc_cache_desc": "CacheDesc", "gc_cache_info": "CacheInfo", "gc_cache_stats": "CacheStats",
+           "gc_view": "View", "gc_batch_desc": "BatchDesc", "gc_batch_stats": "BatchStats",
+           "gc_batch_result": "BatchResult", "gc_tf_point": "TfPoint"}
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Every ctypes structure has the size and field offsets the C compiler
+    gives the header's struct (a mismatch would pass garbage through the ABI)."""
+    import ctypes
+    import shutil
+    import subprocess
+
+    import gcgb300 as gc
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "gc_gb300.h"', "int main(void) {"]
+    for cname, pyname in STRUCTS.items():
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for field, _ in getattr(gc, pyname)._fields_:
+            lines.append(f'printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = os.path.join(ROOT, "include")
+    subprocess.run(["gcc", "-I", inc, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    c_layout = {(a, b): int(c) for a, b, c in (l.split() for l in out if l)}
+    for cname, pyname in STRUCTS.items():
+        cls = getattr(gc, pyname)
+        assert ctypes.sizeof(cls) == c_layout[(cname, "sizeof")], cname
+        for field, _ in cls._fields_:
+            assert getattr(cls, field).offset == c_layout[(cname, field)], (cname, field)
+    from oracle import oracle as orc
+
+    for cname, pyname in (("gc_view", "View"), ("gc_cache_desc", "CacheDesc"), ("gc_volume_desc", "VolumeDesc"),
+                          ("gc_layout", "Layout")):
+        assert ctypes.sizeof(getattr(orc, pyname)) == c_layout[(cname, "sizeof")], ("oracle", cname)

@@ -19,13 +19,13 @@ RGBA_TOL_FP64 = 1
 
 
 class Scene:
-    def __init__(self, gc, orc, torch, size, bpc, B, c, bb, pool, maxreq, seed=21, nblobs=6, sync=True):
+    def __init__(self, gc, orc, torch, size, bpc, B, c, bb, pool, maxreq, seed=21, nblobs=6, sync=True, channels=1):
         self.gc, self.orc, self.torch = gc, orc, torch
-        self.vol = gc.volume_desc(size, B, c, bpc, 1, bb)
+        self.vol = gc.volume_desc(size, B, c, bpc * channels, channels, bb)
         self.layout = gc.compute_layout(self.vol)
-        d = scenario.gpu_volume(gc, torch, size, bpc, seed, nblobs)
+        d = scenario.gpu_volume(gc, torch, size, bpc, seed, nblobs, channels=channels)
         self.store, self.offs, _ = gc.pre_process(self.vol, self.layout, d)
-        o = scenario.orc_volume(orc, size, bpc, seed, nblobs)
+        o = scenario.orc_volume(orc, size, bpc, seed, nblobs, channels=channels)
         ref, roffs = scenario.orc_store(orc, gc, o.reshape(-1).view(np.uint8), self.vol, self.layout)
         assert np.array_equal(self.store.numpy(), ref)
         self.ref = ref
@@ -103,6 +103,39 @@ def test_render_update_loop_matches_oracle(gc, orc, torch_cuda, case):
         s.compare_cache(f"frame {f}")
     st = s.cm.stats()
     assert st.bricks_installed > 0 and st.device_error == 0
+
+
+@pytest.mark.parametrize("mode,sampler", [(0, 0), (0, 1), (1, 0)])
+def test_two_channel_2d_tf_loop_matches_oracle(gc, orc, torch_cuda, mode, sampler):
+    """Two 8-bit channels (blob field + independent noise field, interleaved)
+    rendered with a 2D transfer function, covering 2 and big bricks 2^3 (the
+    c5 brick layout): RGBA, t buffer and colour state bit-exact vs the FP32
+    oracle every frame, cache state bit-exact.  (No reference counterpart:
+    the reference ray caster reads one channel.)"""
+    s = Scene(gc, orc, torch_cuda, (72, 64, 56), 1, 16, 2, (2, 2, 2), (6, 6, 6), 100, channels=2, seed=33)
+    tf = scenario.tf2d(5)
+    th, tw = tf.shape[:2]
+    tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
+    W, H = 61, 47
+    g, o = s.buffers(W, H)
+    for f in range(12):
+        m = scenario.orbit_camera(gc, f // 4, 12, 2.7)
+        if f % 4 == 0:
+            for x in g:
+                x.zero_()
+            for x in o:
+                x[:] = 0
+        v = s.view(m, W, H, tf_dev, tw, g, tf_height=th, mode=mode, sampler=sampler, early_alpha=0.99)
+        s.cm.render(v)
+        s.oc.render(v, tf.reshape(-1), *o)
+        torch_cuda.cuda.synchronize()
+        d = rgba_diff(g[0].cpu().numpy(), o[0])
+        assert d.max() <= RGBA_TOL_FP32, f"frame {f}: max {d.max()}"
+        assert np.array_equal(g[1].cpu().numpy(), o[1]), f"frame {f}: t buffer"
+        assert np.array_equal(g[2].cpu().numpy(), o[2]), f"frame {f}: colour state"
+        assert s.cm.update() == s.oc.update()
+        s.compare_cache(f"frame {f}")
+    assert (g[0].cpu().numpy() >> 24).astype(bool).mean() > 0.05  # not an empty image
 
 
 def test_batch_matches_sequential_oracle(gc, orc, torch_cuda):
