@@ -68,6 +68,12 @@ CONFIGS = {
     "c3": dict(VOL2048, B=32, c=1, pool_bytes=4 << 30, pool_slots=None, batch=64,
                sizes=((256, 256), (512, 512), (1024, 1024), (1920, 1080)), dist=(0.5, 3.0), tf="bumps",
                early=0.99, fov=45.0),
+    # large stress, scaled to the box (4096^3 x 2 channels with covering 2 needs ~300 GB of host brick
+    # store; the box has 197 GB of RAM): two u8 channels (blob field + independent noise field),
+    # covering 2, big bricks 2^3, 8 GiB pool, 2048^2 views on a path through the interior, 2D TF
+    "c5": dict(size=(2048, 2048, 2048), bpc=1, channels=2, nblobs=32, sigma=(40.0, 300.0), amp=(60, 200), noise=20,
+               seed=5, B=16, c=2, bb=(2, 2, 2), pool_bytes=8 << 30, pool_slots=None, W=2048, H=2048, frames=240,
+               path="cross", dist=(0.0, 0.0), tf="2d", early=0.99, fov=45.0, cap=256),
     # serving: three resident volumes sharing one 24 GiB pool, Poisson requests
     "c4": dict(B=16, c=1, pool_bytes=24 << 30, rate=200.0, duration=6.0, batch=64,
                sizes=((256, 256), (512, 512), (1024, 1024), (1920, 1080)), dist=(0.5, 3.0), early=0.99, fov=45.0,
@@ -85,9 +91,15 @@ def workload(name, cfg):
     """(workload text, voxel dtype, data text) of a plain per-view config."""
     n = cfg["size"][0]
     dt = "u8" if cfg["bpc"] == 1 else "u16"
+    nc = cfg.get("channels", 1)
+    if nc > 1:
+        dt = f"{dt}x{nc}"
     vol = f"{n}^3 {dt}"
     if cfg["path"] == "orbit":
         how = f"{cfg['W']}^2 views on a {cfg['frames']}-view orbit at {cfg['dist'][0]}x the diagonal"
+    elif cfg["path"] == "cross":
+        how = (f"{cfg['W']}^2 views along a {cfg['frames']}-view path through the interior, 2D transfer function, "
+               f"covering {cfg['c']}, big bricks {cfg.get('bb')}")
     else:
         how = (f"{cfg['W']}^2 views along a {cfg['frames']}-view fly-through from {cfg['dist'][0]}x to "
                f"{cfg['dist'][1]}x the diagonal")
@@ -98,6 +110,21 @@ def workload(name, cfg):
 
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
+
+
+def tf2d_table(seed=5, width=64, height=64):
+    """2D RGBA table (height rows of width entries) for two-channel volumes:
+    alpha from seeded bumps over channel 0, modulated along channel 1."""
+    rng = np.random.default_rng(seed)
+    x = np.linspace(0.0, 1.0, width)[None, :]
+    y = np.linspace(0.0, 1.0, height)[:, None]
+    a = np.zeros((height, width))
+    for _ in range(3):
+        c, w, h = rng.uniform(0.2, 0.9), rng.uniform(0.04, 0.1), rng.uniform(0.2, 0.7)
+        a = a + h * np.exp(-0.5 * ((x - c) / w) ** 2) * (0.3 + 0.7 * y)
+    rgb = np.stack([np.broadcast_to(np.clip(0.2 + x, 0, 1), a.shape), np.broadcast_to(np.clip(1.0 - y, 0, 1), a.shape),
+                    0.5 + 0.5 * np.sin(5 * x + 3 * y)], -1)
+    return np.concatenate([rgb, np.clip(a, 0, 1)[..., None]], -1).astype(np.float32)
 
 
 def tf_table(kind, seed=3):
@@ -119,6 +146,11 @@ def tf_table(kind, seed=3):
 def path_camera(gc, cfg, f, rank=0):
     n = cfg["frames"]
     t = (f % n) / max(1, n - 1)
+    if cfg["path"] == "cross":  # through the interior, looking ahead along the path
+        a, b = (-0.85, -0.25, -0.8), (0.85, 0.3, 0.8)
+        eye = tuple(p + (q - p) * t for p, q in zip(a, b))
+        ahead = tuple(e + (q - p) * 0.5 for e, p, q in zip(eye, a, b))
+        return gc.look_at(eye, ahead)
     if cfg["path"] == "orbit":
         ang = 2 * math.pi * ((f + rank * 7) % n) / n
         d = cfg["dist"][0] * DIAG
@@ -206,13 +238,18 @@ def make_store(gc, torch, cfg):
     """Synthetic volume generated on the device, pre-processed (mip + bricks) on
     the device, brick store moved to host memory (the out-of-core source)."""
     size, bpc = cfg["size"], cfg["bpc"]
-    vol = gc.volume_desc(size, cfg["B"], cfg["c"], bpc, 1)
+    nc = cfg.get("channels", 1)
+    vol = gc.volume_desc(size, cfg["B"], cfg["c"], bpc * nc, nc, cfg.get("bb", (1, 1, 1)))
     layout = gc.compute_layout(vol)
     t0 = time.time()
     blobs = gc.generator_blobs(cfg["seed"], cfg["nblobs"], size, cfg["sigma"][0], cfg["sigma"][1], cfg["amp"][0],
                                cfg["amp"][1])
-    dev = torch.empty(size[0] * size[1] * size[2] * bpc, dtype=torch.uint8, device="cuda")
-    gc.generate_volume(gc.make_generator(size, bpc, cfg["seed"], blobs, cfg["noise"]), dev.data_ptr())
+    dev = torch.empty(size[0] * size[1] * size[2] * bpc * nc, dtype=torch.uint8, device="cuda")
+    gc.generate_volume(gc.make_generator(size, bpc, cfg["seed"], blobs, cfg["noise"], channels=nc, channel=0,
+                                         field=0), dev.data_ptr())
+    for ch in range(1, nc):  # further channels: an independent noise field
+        gc.generate_volume(gc.make_generator(size, bpc, cfg["seed"] + ch, blobs, cfg["noise"] * 4, channels=nc,
+                                             channel=ch, field=1), dev.data_ptr())
     torch.cuda.synchronize()
     t1 = time.time()
     store, offs, _ = gc.pre_process(vol, layout, dev, pin=PIN_STORES)
@@ -236,7 +273,9 @@ class Session:
                                   staged_upload=Session.staged)
         self.cm.set_source_host(store, offs)
         self.vol = vol
-        self.tf = torch.from_numpy(tf_table(cfg["tf"]).reshape(-1)).cuda()
+        tf = tf2d_table() if cfg["tf"] == "2d" else tf_table(cfg["tf"])
+        self.tfh, self.tfw = (tf.shape[0], tf.shape[1]) if tf.ndim == 3 else (0, tf.shape[0])
+        self.tf = torch.from_numpy(tf.reshape(-1)).cuda()
         self.stream = torch.cuda.Stream()
         self.sp = self.stream.cuda_stream
         self.focal = 1.0 / math.tan(math.radians(cfg["fov"]) / 2)
@@ -257,9 +296,9 @@ class Session:
         for i, (m, W, H) in enumerate(specs):
             b = self.buffers(i, W, H)
             bufs.append(b)
-            out.append(self.gc.make_view(m, W, H, self.tf.data_ptr(), 256, b[0].data_ptr(), b[1].data_ptr(),
+            out.append(self.gc.make_view(m, W, H, self.tf.data_ptr(), self.tfw, b[0].data_ptr(), b[1].data_ptr(),
                                          b[2].data_ptr(), tstep=2.0 / 256.0, focal=self.focal,
-                                         early_alpha=self.cfg["early"]))
+                                         early_alpha=self.cfg["early"], tf_height=self.tfh))
         return out, bufs
 
     def converge(self, specs, e2e=False, cap=64, render_events=None):
@@ -295,7 +334,7 @@ class Session:
 
 def autotune(gc, torch, S, specs, args):
     """Autotunes the ray caster's launch configuration on converged views."""
-    S.converge(specs)
+    S.converge(specs, cap=S.cfg.get("cap", 64))
     views, bufs = S.views(specs)
 
     def clear():
@@ -351,11 +390,12 @@ def run_ours(args):
         """Fresh cache; warm-up views, then the timed views (same views for value and e2e)."""
         S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
         for f in range(args.warmup):
-            S.converge(spec(f))
+            S.converge(spec(f), cap=cfg.get("cap", 64))
         if not tuned:
             tuned.append(autotune(gc, torch, S, spec(args.warmup - 1), args))
         s0, l0 = S.cm.stats(), gc.kernel_launches()
-        wall, lat, info = timed(torch, S.stream, lambda i: S.converge(spec(args.warmup + i), e2e=e2e), args.steps)
+        wall, lat, info = timed(torch, S.stream, lambda i: S.converge(spec(args.warmup + i), e2e=e2e,
+                                                                      cap=cfg.get("cap", 64)), args.steps)
         launches = gc.kernel_launches() - l0
         s1 = S.cm.stats()
         return S, wall, lat, info, launches, s0, s1
@@ -409,7 +449,9 @@ def run_ours(args):
                    "loader": "sync", "upload": "gather kernel reading the host store"
                    if S.cm.stats().upload_direct else "staged host copies + cudaMemcpyAsync",
                    "l2": "inputs > L2 (2 GiB pool, 103 MB page directory, 28 GiB host brick store)"
-                   if args.config == "c2" else "in-core volume; L2 not flushed (the c1 case is for profiling)",
+                   if args.config == "c2" else ("inputs > L2 (8 GiB pool, 43 GiB host brick store)"
+                                                if args.config == "c5" else
+                                                "in-core volume; L2 not flushed (the c1 case is for profiling)"),
                    "preprocess_s": round(prep_s, 2)},
         "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
         "iterations_per_view": {"mean": round(statistics.mean(iters), 2), "max": max(iters)},
@@ -717,7 +759,8 @@ def cpu_baseline(gc, S, cfg, spec, args):
     rgba = np.zeros(W * H, np.uint32)
     tb = np.zeros(W * H, np.float32)
     st = np.zeros(W * H * 4, np.float32)
-    v = gc.make_view(m, W, H, 0, 256, 0, 0, 0, tstep=2.0 / 256.0, focal=S.focal, early_alpha=cfg["early"])
+    v = gc.make_view(m, W, H, 0, S.tfw, 0, 0, 0, tstep=2.0 / 256.0, focal=S.focal, early_alpha=cfg["early"],
+                     tf_height=S.tfh)
     frames = 0
     t0 = time.perf_counter()
     while True:
@@ -730,7 +773,7 @@ def cpu_baseline(gc, S, cfg, spec, args):
             break
     oc.close()
     return {"value": round(W * H * frames / el / 1e6, 4), "unit": "Mrays/s", "cores": os.cpu_count(),
-            "kind": "port", "sample": f"{frames} renders of one converged {W}x{H} c2 view from the GPU's cache "
+            "kind": "port", "sample": f"{frames} renders of one converged {W}x{H} {args.config} view from the GPU's cache "
                                       f"snapshot (oracle FP32 ray-march, {os.cpu_count()} threads)"}
 
 
@@ -801,9 +844,10 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4"], default="c2",
+    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default="c2",
                     help="c2: the plain out-of-core line (+ the c3 batched object); c1: small in-core plain case; "
-                         "c3: the batched form alone; c4: serving (three volumes, shared pool, Poisson requests)")
+                         "c3: the batched form alone; c4: serving (three volumes, shared pool, Poisson requests); "
+                         "c5: two-channel 2D-TF stress (plain loop)")
     ap.add_argument("--rate", type=float, default=200.0, help="c4: request arrivals per second")
     ap.add_argument("--duration", type=float, default=6.0, help="c4: seconds of arrivals")
     ap.add_argument("--max-requests", type=int, default=8192)
