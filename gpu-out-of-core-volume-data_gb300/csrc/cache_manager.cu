@@ -21,6 +21,8 @@
 // reading the host store directly where the device can (page-locked store, or
 // pageable memory on a coherent Grace-Blackwell link), else host copies into
 // a pinned staging buffer and one cudaMemcpyAsync.
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -32,6 +34,7 @@
 #include <unordered_set>
 #include <vector>
 
+#include "brickfiles.h"
 #include "cache.cuh"
 #include "gc_internal.h"
 
@@ -66,7 +69,9 @@ __global__ void init_slots_kernel(uint32_t *order, uint32_t *level, float4 *vpos
 }
 
 struct Source {
-    int kind = 0;  // 0 none, 1 host store, 2 callback
+    int kind = 0;  // 0 none, 1 host store, 2 callback, 3 brick files
+    std::string dir;       // brick files: the volume directory (with '/')
+    uint32_t threads = 0;  // brick files: reader threads
     const uint8_t *host = nullptr;
     uint64_t bytes = 0;
     bool direct = false;          // the device reads the store (gather kernel)
@@ -189,6 +194,13 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
         uint64_t bytes;
     };
     std::vector<Copy> copies;
+    struct FileRead {
+        std::string path;
+        uint8_t *dst;
+        uint64_t bytes;
+    };
+    std::vector<FileRead> reads;
+    uint32_t read_threads = 1;
     uint64_t bytes_up = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const uint4 b = C->h_list[i];  // (x, y, z, cache level)
@@ -230,6 +242,14 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
             }
         } else if (src.kind == 2) {
             status = src.fn(src.user, lvl, gx, gy, gz, stage, V.big_bytes);
+        } else if (src.kind == 3) {
+            std::string p = brick_file_path(src.dir, V.desc.brick_size, lvl, gx, gy, gz);
+            struct stat st;
+            if (::stat(p.c_str(), &st) == 0) {  // BricksManager::load_brick: a missing file is Unknown
+                reads.push_back({std::move(p), stage, V.big_bytes});
+                read_threads = std::max(read_threads, src.threads ? src.threads : 8u);
+                status = GC_BRICK_SUCCESS;
+            }
         }
         if (status == GC_BRICK_SUCCESS) {
             bytes_up += V.big_bytes;
@@ -268,6 +288,27 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
             work(0);
             for (auto &th : pool) th.join();
         }
+    }
+    // Brick files: read and decompressed by worker threads into the staging slots.
+    if (!reads.empty()) {
+        std::atomic<size_t> next{0};
+        std::atomic<bool> bad{false};
+        std::string bad_path;
+        std::mutex bad_mu;
+        auto work = [&] {
+            for (size_t i = next++; i < reads.size(); i = next++)
+                if (read_brick_file(reads[i].path, reads[i].dst, reads[i].bytes) != 0) {
+                    std::lock_guard<std::mutex> g(bad_mu);
+                    bad = true;
+                    bad_path = reads[i].path;
+                }
+        };
+        const unsigned nt = static_cast<unsigned>(std::min<size_t>(read_threads, reads.size()));
+        std::vector<std::thread> pool;
+        for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+        work();
+        for (auto &th : pool) th.join();
+        if (bad) fail(GC_ERR_IO, "unreadable brick file " + bad_path);
     }
     // stable partition: non-empty first, then empty (RequestHandler.hpp:354-369)
     uint32_t k = 0;
@@ -585,7 +626,7 @@ static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s
 static void update_upload_route(gc_cache *C) {
     bool any = false, all = true, vec16 = C->big_stride % 16 == 0;
     for (const Volume &V : C->vols) {
-        if (V.src.kind == 2) all = false;
+        if (V.src.kind == 2 || V.src.kind == 3) all = false;
         if (V.src.kind == 1) {
             any = true;
             all = all && V.src.direct;
@@ -791,6 +832,26 @@ int gc_cache_set_volume_source_host(gc_cache_t C, uint32_t volume, const void *b
         src.dev = dev;
         src.vec16 = aligned && reinterpret_cast<uintptr_t>(dev) % 16 == 0;
         src.level_off.assign(level_offsets, level_offsets + L.nb_levels);
+        for (size_t i = 0; i < n_empty; ++i) src.empty.insert(empty_keys[i]);
+        update_upload_route(C);
+    });
+}
+
+int gc_cache_set_volume_source_files(gc_cache_t C, uint32_t volume, const char *volume_dir,
+                                     const uint64_t *empty_keys, size_t n_empty, uint32_t threads) {
+    return guard([&] {
+        GC_REQUIRE(C && volume_dir && (empty_keys || n_empty == 0), "null argument");
+        GC_REQUIRE(volume < C->vols.size(), "no such volume in this cache");
+        std::string why;
+        if (!lz4_available(&why)) fail(GC_ERR_UNSUPPORTED, why);
+        std::lock_guard<std::mutex> g(C->mu);
+        GC_REQUIRE(!C->busy, "the loader is busy");
+        Source &src = C->vols[volume].src;
+        src = Source();
+        src.kind = 3;
+        src.dir = volume_dir;
+        if (!src.dir.empty() && src.dir.back() != '/') src.dir += '/';
+        src.threads = threads;
         for (size_t i = 0; i < n_empty; ++i) src.empty.insert(empty_keys[i]);
         update_upload_route(C);
     });

@@ -29,7 +29,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 EXTRA = {
     "render.cu": ["-fmad=false"],
 }
-SOURCES = ["config.cpp", "generate.cu", "preprocess.cu", "cache_kernels.cu", "cache_manager.cu", "render.cu"]
+SOURCES = ["config.cpp", "generate.cu", "preprocess.cu", "cache_kernels.cu", "cache_manager.cu", "render.cu",
+           "brickfiles.cpp"]
 
 
 def nvcc():
@@ -74,7 +75,7 @@ def build(verbose=False, force=False):
     objs = [o for o, _ in results]
     rebuilt = any(r for _, r in results)
     if rebuilt or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread", "-ldl"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -129,6 +129,13 @@ _SIGS = {
     "gc_cache_set_volume_source_host": [vp, C.c_uint32, vp, C.c_uint64, P(C.c_uint64), P(C.c_uint64), C.c_size_t],
     "gc_cache_set_volume_source_callback": [vp, C.c_uint32, LOADER_FN, vp, P(C.c_uint64), C.c_size_t],
     "gc_cache_create_shared": [P(CacheDesc), P(VolumeDesc), P(Layout), C.c_uint32, P(vp)],
+    "gc_cache_set_volume_source_files": [vp, C.c_uint32, C.c_char_p, P(C.c_uint64), C.c_size_t, C.c_uint32],
+    "gc_lz4_available": [],
+    "gc_brick_files_write": [C.c_char_p, P(VolumeDesc), P(Layout), vp, C.c_uint64, P(C.c_uint64), C.c_uint32],
+    "gc_brick_files_read": [C.c_char_p, P(VolumeDesc), P(Layout), vp, C.c_uint64, P(C.c_uint64), C.c_uint32],
+    "gc_bricks_xml_write": [C.c_char_p, P(VolumeDesc), P(Layout), P(C.c_uint64), C.c_size_t],
+    "gc_bricks_xml_read": [C.c_char_p, P(C.c_uint32), P(C.c_uint32 * 3), P(C.c_uint32 * 3), P(C.c_uint64),
+                           C.c_size_t, P(C.c_size_t)],
     "gc_cache_volume_levels": [vp, C.c_uint32, P(C.c_uint32), P(C.c_uint32)],
     "gc_cache_update": [vp, vp, P(C.c_int)], "gc_cache_completude": [vp, vp, P(C.c_float)],
     "gc_cache_timestamp": [vp, P(C.c_uint32)], "gc_cache_info_get": [vp, P(CacheInfo)],
@@ -409,6 +416,52 @@ def make_view(inv_view, width, height, tf_ptr, tf_width, rgba_ptr, tbuf_ptr, sta
                 vp(state_ptr), vp(status_ptr or None), volume, tf_height)
 
 
+def lz4_available():
+    """True when liblz4 (the codec of the reference's brick files) can be loaded."""
+    return bool(lib.gc_lz4_available())
+
+
+def _store_ptr(store, nbytes):
+    if hasattr(store, "data_ptr"):
+        return store.data_ptr(), store.numel() * store.element_size()
+    if hasattr(store, "ctypes"):
+        return store.ctypes.data, store.nbytes
+    return int(store), int(nbytes)
+
+
+def write_brick_files(volume_dir, vol, layout, store, level_offsets, threads=0, nbytes=None):
+    """BricksManager::write_brick for every big brick of the store (LZ4 HC 9)."""
+    ptr, size = _store_ptr(store, nbytes)
+    offs = (C.c_uint64 * MAX_LEVELS)(*[int(o) for o in level_offsets])
+    check(lib.gc_brick_files_write(str(volume_dir).encode(), C.byref(vol), C.byref(layout), vp(ptr), size, offs,
+                                   threads))
+
+
+def read_brick_files(volume_dir, vol, layout, store, level_offsets, threads=0, nbytes=None):
+    """BricksManager::load_brick for every big brick, into the store."""
+    ptr, size = _store_ptr(store, nbytes)
+    offs = (C.c_uint64 * MAX_LEVELS)(*[int(o) for o in level_offsets])
+    check(lib.gc_brick_files_read(str(volume_dir).encode(), C.byref(vol), C.byref(layout), vp(ptr), size, offs,
+                                  threads))
+
+
+def write_bricks_xml(volume_dir, vol, layout, empty_keys=()):
+    keys = (C.c_uint64 * max(1, len(empty_keys)))(*[int(k) for k in empty_keys])
+    check(lib.gc_bricks_xml_write(str(volume_dir).encode(), C.byref(vol), C.byref(layout), keys, len(empty_keys)))
+
+
+def read_bricks_xml(path, max_empty=1 << 20):
+    """(level initial sizes, level real sizes, empty keys) of a bricks.xml."""
+    n = C.c_uint32()
+    ini = (C.c_uint32 * 3 * MAX_LEVELS)()
+    real = (C.c_uint32 * 3 * MAX_LEVELS)()
+    keys = (C.c_uint64 * max_empty)()
+    ne = C.c_size_t()
+    check(lib.gc_bricks_xml_read(str(path).encode(), C.byref(n), ini, real, keys, max_empty, C.byref(ne)))
+    return ([tuple(ini[l]) for l in range(n.value)], [tuple(real[l]) for l in range(n.value)],
+            list(keys[: min(ne.value, max_empty)]))
+
+
 # ---------------------------------------------------------------------------
 class CacheManager:
     """GPU brick cache + ray caster entry (CacheManager<T> + RayCastDVR)."""
@@ -455,6 +508,13 @@ class CacheManager:
         keys = (C.c_uint64 * max(1, len(empty_keys)))(*[int(k) for k in empty_keys])
         self._keep.append((offs, keys, store))
         check(lib.gc_cache_set_volume_source_host(self._h, volume, vp(ptr), size, offs, keys, len(empty_keys)))
+
+    def set_source_files(self, volume_dir, empty_keys=(), volume=0, threads=0):
+        """The reference's brick files under volume_dir, read by the loader."""
+        keys = (C.c_uint64 * max(1, len(empty_keys)))(*[int(k) for k in empty_keys])
+        self._keep.append(keys)
+        check(lib.gc_cache_set_volume_source_files(self._h, volume, str(volume_dir).encode(), keys, len(empty_keys),
+                                                   threads))
 
     def set_source_callback(self, fn, empty_keys=(), volume=0):
         cb = LOADER_FN(fn)

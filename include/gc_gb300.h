@@ -246,6 +246,14 @@ int gc_cache_set_source_callback(gc_cache_t cache, gc_brick_loader_fn fn, void *
                                  const uint64_t *empty_keys, size_t n_empty);
 /* The same for one volume of a shared cache (the calls above set volume 0).
  * Level numbers, brick keys and empty keys are the volume's own. */
+/* Brick files of the reference's on-disk store under volume_dir (below): the
+ * loader reads and decompresses each missing big brick with up to `threads`
+ * worker threads into the pinned staging buffer, uploaded with
+ * cudaMemcpyAsync (BricksManager::get_brick / load_brick,
+ * BricksManager.cpp:29-78, 191-227).  A missing file is GC_BRICK_UNKNOWN; a
+ * corrupt one stops the loader with GC_ERR_IO.  Needs liblz4. */
+int gc_cache_set_volume_source_files(gc_cache_t cache, uint32_t volume, const char *volume_dir,
+                                     const uint64_t *empty_keys, size_t n_empty, uint32_t threads);
 int gc_cache_set_volume_source_host(gc_cache_t cache, uint32_t volume, const void *bricks, uint64_t bytes,
                                     const uint64_t *level_offsets, const uint64_t *empty_keys, size_t n_empty);
 int gc_cache_set_volume_source_callback(gc_cache_t cache, uint32_t volume, gc_brick_loader_fn fn, void *user,
@@ -388,6 +396,31 @@ int gc_render_batch(gc_cache_t cache, const gc_view *views, uint32_t n, void *st
  * the autotuner of the Python host (gcgb300.autotune_render). */
 int gc_render_tuning_set(uint32_t scheduler, uint32_t tile_w, uint32_t threads, uint32_t blocks_per_sm);
 int gc_render_tuning_get(uint32_t out[4]);
+
+/* ------------------------------------------------------------------------ */
+/* The reference's on-disk brick store (BricksManager.cpp:81-227,
+ * BrickKey.cpp:38-44, MetaData.cpp:36-216):
+ *   <volume_dir>bricks_B_B_B/L<l>/L<l>_<x>_<y>_<z>.raw   one LZ4 block (LZ4_compress_HC
+ *       level 9) of the (BB*B)^3 x encoded_bytes voxels of big brick (x, y, z)
+ *   <volume_dir>bricks_B_B_B/bricks.xml                  level sizes, empty bricks
+ * volume_dir is the reference's VolumeDirectory (a trailing '/' is added).
+ * The codec is the system's liblz4, loaded at run time: without it these
+ * calls return GC_ERR_UNSUPPORTED (gc_lz4_available() tells beforehand).
+ * Stores are the in-memory layout of gc_cache_set_source_host (level l at
+ * level_offsets[l], big bricks in (z, y, x) order); threads 0 = all cores. */
+int gc_lz4_available(void);
+int gc_brick_files_write(const char *volume_dir, const gc_volume_desc *vol, const gc_layout *layout,
+                         const void *store, uint64_t bytes, const uint64_t *level_offsets, uint32_t threads);
+int gc_brick_files_read(const char *volume_dir, const gc_volume_desc *vol, const gc_layout *layout, void *store,
+                        uint64_t bytes, const uint64_t *level_offsets, uint32_t threads);
+/* MetaData::write_bricks_xml: byte for byte the reference's file (histogram
+ * bins all 0, as the reference never fills them). */
+int gc_bricks_xml_write(const char *volume_dir, const gc_volume_desc *vol, const gc_layout *layout,
+                        const uint64_t *empty_keys, size_t n_empty);
+/* MetaData::load for the level sizes and the empty big bricks (up to
+ * max_empty keys stored; *n_empty is the count in the file). */
+int gc_bricks_xml_read(const char *path, uint32_t *n_levels, uint32_t initial[][3], uint32_t real[][3],
+                       uint64_t *empty_keys, size_t max_empty, size_t *n_empty);
 
 /* ------------------------------------------------------------------------ */
 /* Continuous batching of views over one cache (the batched and served forms;

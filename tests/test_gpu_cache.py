@@ -56,8 +56,9 @@ def device_reads_pageable(torch):
 # device reads pageable memory, else staged), "pinned" = page-locked store
 # (always gathered), "staged" = GC_CACHE_STAGED_UPLOAD (host copies + one
 # cudaMemcpyAsync)
-@pytest.mark.parametrize("maxreq,route", [(50, "pageable"), (700, "pageable"), (700, "pinned"), (50, "staged")])
-def test_update_replay_with_installs(gc, orc, torch_cuda, maxreq, route):
+@pytest.mark.parametrize("maxreq,route", [(50, "pageable"), (700, "pageable"), (700, "pinned"), (50, "staged"),
+                                          (300, "files")])
+def test_update_replay_with_installs(gc, orc, torch_cuda, maxreq, route, tmp_path):
     size = (256, 256, 256)
     vol = gc.volume_desc(size, 16, 1, 1, 1)
     layout = gc.compute_layout(vol)
@@ -65,9 +66,16 @@ def test_update_replay_with_installs(gc, orc, torch_cuda, maxreq, route):
     store, offs = scenario.orc_store(orc, gc, o.reshape(-1).view(np.uint8), vol, layout)
     cm = gc.CacheManager(vol, layout, (10, 10, 10), max_requests=maxreq, sync_loader=True,
                          staged_upload=route == "staged")
-    src = torch_cuda.from_numpy(store).pin_memory() if route == "pinned" else store
-    cm.set_source_host(src, offs)
-    expect_direct = route == "pinned" or (route == "pageable" and device_reads_pageable(torch_cuda))
+    if route == "files":  # the reference's LZ4 brick files, read by the loader's threads
+        if not gc.lz4_available():
+            pytest.skip("liblz4 is not installed")
+        gc.write_brick_files(tmp_path, vol, layout, store, offs)
+        cm.set_source_files(tmp_path, threads=4)
+        expect_direct = False
+    else:
+        src = torch_cuda.from_numpy(store).pin_memory() if route == "pinned" else store
+        cm.set_source_host(src, offs)
+        expect_direct = route == "pinned" or (route == "pageable" and device_reads_pageable(torch_cuda))
     assert cm.stats().upload_direct == int(expect_direct)
     oc = orc.Cache(cm.desc)
     oc.set_source(store, offs)
