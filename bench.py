@@ -434,6 +434,23 @@ def run_ours(args):
     torch.cuda.nvtx.range_pop()
     touched = S.cm.stats().last_used
     render_ms = statistics.median([a.elapsed_time(b) for a, b in ev])
+    # the same launch with empty-space skipping off (identical image), for the record
+    gc.render_empty_skip(False)
+    ev_off = []
+    for _ in range(3):
+        views, bufs = S.views(last)
+        with torch.cuda.stream(S.stream):
+            bufs[0][1].zero_()
+            bufs[0][2].zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(S.stream)
+            S.cm.render(views[0], S.sp)
+            e1.record(S.stream)
+            ev_off.append((e0, e1))
+            S.cm.update(S.sp)
+    torch.cuda.synchronize()
+    gc.render_empty_skip(True)
+    render_ms_noskip = statistics.median([a.elapsed_time(b) for a, b in ev_off])
     algo = touched * cfg["B"] ** 3 * vol.encoded_bytes + W * H * PIXEL_BYTES
     peak, peak_kind = measured_peak()
     achieved = algo / (render_ms / 1e3) / 1e9
@@ -463,7 +480,8 @@ def run_ours(args):
                      "frac": round(achieved / peak, 5), "traffic": None,
                      "kernel": "render_pixels_kernel" if gc.render_tuning()[0] == 1 else "render_kernel",
                      "peak_kind": peak_kind, "algorithmic_bytes_per_launch": int(algo),
-                     "launch_ms": round(render_ms, 4), "touched_bricks": int(touched),
+                     "launch_ms": round(render_ms, 4), "launch_ms_without_empty_skip": round(render_ms_noskip, 4),
+                     "touched_bricks": int(touched),
                      "note": f"converged {W}x{H} view of {args.config}; compulsory bytes = touched bricks x B^3 x "
                              f"{vol.encoded_bytes} B + {PIXEL_BYTES} B/pixel"},
         "render_tuning": {"scheduler_tile_threads_bps": list(tuned[0][0]) if tuned else None,

@@ -48,8 +48,17 @@ struct CacheView {
     uint32_t eb;          // bytes per voxel of every volume, 0 when the volumes differ
     uint32_t nc;          // channels per voxel (1, or 2 for two 8-bit channels)
     uint64_t slot_bytes;  // pool slot stride: B^3 x the widest voxel
+    const unsigned long long *slot_bins;  // per slot: value bins its voxels cover (empty-space skipping)
     uint32_t ts;
 };
+
+// Empty-space skipping: voxel values are quantized into kValueBins bins of
+// [0, 1]; a slot records the bins its brick's voxels cover (one bit each,
+// widened by one bin on either side) and a view the bins its transfer function
+// can make visible.  A brick whose bins are all invisible contributes no
+// sample above the compositing threshold, so the march steps through it
+// without sampling (same t sequence, same image).
+constexpr uint32_t kValueBins = 64;
 
 // Per-launch ray-caster parameters of one view.
 struct ViewParams {
@@ -75,6 +84,8 @@ struct ViewParams {
     uint32_t level_base;                // first cache level of the view's volume
     uint32_t nlevels;                   // levels of the view's volume
     uint32_t eb;                        // bytes per voxel of the view's volume
+    uint32_t skip_empty;                // step through invisible bricks without sampling (DVR, one channel)
+    unsigned long long visible;         // bins the view's transfer function can make visible
     uint32_t mark_done;                 // batched passes: a finished ray leaves -1 - t in tbuf and
                                         // later passes skip its pixel (rgba already final)
 };
@@ -109,6 +120,8 @@ struct InstallArgs {
     uint32_t *slot_level;
     float4 *slot_vpos;
     uint8_t *pool;
+    unsigned long long *slot_bins;  // per slot value-bin mask, written with the brick
+    uint32_t nc;               // channels per voxel (bins only for one channel)
     uint64_t slot_bytes;       // pool slot stride
     uint64_t big_stride;       // staging stride of one big brick
     uint32_t sx, sy;
@@ -134,9 +147,12 @@ struct RenderTuning {
     uint32_t scheduler = 1;
     uint32_t threads = 128;
     uint32_t blocks_per_sm = 0;
+    uint32_t skip_empty = 1;  // empty-space skipping on (results are the same either way)
     uint32_t tile_w = 8;  // ray tile of one warp: tile_w x (32 / tile_w) pixels
 };
 RenderTuning &render_tuning();
+// Fills ViewParams::visible of n device views from their transfer functions.
+void launch_view_bins(ViewParams *views_dev, uint32_t n, cudaStream_t s);
 void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams *views_dev,
                    const ViewParams *views_host, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
                    uint32_t *err, cudaStream_t s);
@@ -145,7 +161,7 @@ void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams 
 struct RenderGraph {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaGraphNode_t copy = nullptr, kern = nullptr;
+    cudaGraphNode_t copy = nullptr, bins = nullptr, kern = nullptr;
     void *func = nullptr;
     uint32_t threads = 0;
     uint64_t replays = 0;

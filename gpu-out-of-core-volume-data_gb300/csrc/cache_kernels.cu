@@ -301,6 +301,53 @@ __global__ void __launch_bounds__(256) install_place_kernel(InstallArgs a, const
             dst[v] = src[soff];
         }
     }
+    if (!a.slot_bins) return;
+    // Value range of the brick, as value bins (empty-space skipping): min and
+    // max over its B^3 voxels (covering included), normalized like the
+    // samplers, widened by one bin on either side.
+    __syncthreads();
+    if (a.nc != 1) {
+        if (threadIdx.x == 0) a.slot_bins[slot] = ~0ull;  // several channels: never skipped
+        return;
+    }
+    float lo = 3.4e38f, hi = -3.4e38f;
+    const uint32_t nvox = B * B * B;
+    for (uint32_t v = threadIdx.x; v < nvox; v += blockDim.x) {
+        float x;
+        if (eb == 1)
+            x = static_cast<float>(dst[v]) * (1.0f / 255.0f);
+        else if (eb == 2)
+            x = static_cast<float>(reinterpret_cast<const uint16_t *>(dst)[v]) * (1.0f / 65535.0f);
+        else
+            x = reinterpret_cast<const float *>(dst)[v];
+        lo = fminf(lo, x);
+        hi = fmaxf(hi, x);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    __shared__ float s_lo[8], s_hi[8];
+    const uint32_t warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31u) == 0) {
+        s_lo[warp] = lo;
+        s_hi[warp] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (uint32_t w = 1; w < (blockDim.x + 31) / 32; ++w) {
+            lo = fminf(lo, s_lo[w]);
+            hi = fmaxf(hi, s_hi[w]);
+        }
+        auto bin = [](float x) {
+            const float f = floorf(x * static_cast<float>(kValueBins));
+            return f < 0.f ? 0 : (f > kValueBins - 1.f ? static_cast<int>(kValueBins) - 1 : static_cast<int>(f));
+        };
+        const int b0 = max(bin(lo) - 1, 0), b1 = min(bin(hi) + 1, static_cast<int>(kValueBins) - 1);
+        const unsigned long long upto = b1 >= 63 ? ~0ull : ((1ull << (b1 + 1)) - 1ull);
+        a.slot_bins[slot] = upto & ~((1ull << b0) - 1ull);
+    }
 }
 
 // reference_new_bricks (CacheManagerKernels.hpp:308-357) for the MRPD-only

@@ -111,6 +111,7 @@ struct gc_cache {
     uint4 *mrpd = nullptr;
     uint32_t *req = nullptr, *usage = nullptr, *order[2] = {nullptr, nullptr}, *slot_level = nullptr;
     float4 *slot_vpos = nullptr;
+    unsigned long long *slot_bins = nullptr;  // value bins of each slot's brick (empty-space skipping)
     uint8_t *pool = nullptr;
     uint64_t *status_lru = nullptr, *status_miss = nullptr;
     gc::ScanCtl *ctl_lru = nullptr, *ctl_miss = nullptr;
@@ -416,6 +417,7 @@ static CacheView cache_view(const gc_cache *C) {
     cv.eb = C->eb;
     cv.nc = C->nc;
     cv.slot_bytes = C->slot_bytes;
+    cv.slot_bins = C->slot_bins;
     cv.ts = C->ts;
     return cv;
 }
@@ -446,6 +448,8 @@ static void install(gc_cache *C, cudaStream_t s) {
     a.Beff = C->Beff;
     a.slot_bytes = C->slot_bytes;
     a.big_stride = C->big_stride;
+    a.slot_bins = C->slot_bins;
+    a.nc = C->nc;
     a.asked = C->d_asked;
     a.big_index = C->d_big_index;
     a.big_coord = C->d_big_coord;
@@ -524,7 +528,7 @@ static void destroy(gc_cache *C) {
     }
     cudaSetDevice(C->device);
     cudaDeviceSynchronize();
-    void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool,
+    void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool, C->slot_bins,
                    C->status_lru, C->status_miss, C->ctl_lru, C->ctl_miss, C->d_count, C->d_misc, C->d_queue,
                    C->d_list, C->d_asked, C->d_big_coord, C->d_big_index, C->d_src, C->d_staging, C->d_views};
     for (void *p : dev)
@@ -571,6 +575,9 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
     out.sampler = in.sampler;
     out.tfw = in.tf_width;
     out.tfh = in.tf_height > 0 ? in.tf_height : 1;
+    // empty-space skipping: DVR of one channel through a 1D transfer function
+    out.skip_empty = render_tuning().skip_empty && in.mode == GC_MODE_DVR && V.desc.channels == 1 ? 1u : 0u;
+    out.visible = ~0ull;  // filled from the transfer function on the device (view_bins_kernel)
     out.tf = in.tf;
     out.rgba = in.rgba;
     out.tbuf = in.tbuf;
@@ -617,6 +624,7 @@ static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s
     }
     // pageable source: the call returns once the data is staged
     GC_CUDA(cudaMemcpyAsync(C->d_views, vp.data(), n * sizeof(ViewParams), cudaMemcpyHostToDevice, s));
+    launch_view_bins(C->d_views, n, s);
     launch_render(cache_view(C), C->lt, C->d_views, vp.data(), n, tiles, C->d_queue, nullptr, s);
 }
 
@@ -728,6 +736,8 @@ int gc_cache_create_shared(const gc_cache_desc *desc, const gc_volume_desc *volu
         C->slot_level = dalloc<uint32_t>(C->nslots, "slot levels");
         C->slot_vpos = dalloc<float4>(C->nslots, "slot positions");
         C->pool = dalloc<uint8_t>(C->nslots * C->slot_bytes, "brick pool");
+        C->slot_bins = dalloc<unsigned long long>(C->nslots, "slot value bins");
+        GC_CUDA(cudaMemset(C->slot_bins, 0xff, C->nslots * sizeof(unsigned long long)));
         C->status_lru = dalloc<uint64_t>(lookback_tiles(C->nslots), "scan status");
         C->status_miss = dalloc<uint64_t>(lookback_tiles(C->nentries), "scan status");
         C->ctl_lru = dalloc<ScanCtl>(1, "scan control");

@@ -214,12 +214,13 @@ __device__ __forceinline__ float sample_trilinear(const T *__restrict__ b, uint3
     return (c0 + (c1 - c0) * wz) / VoxelTraits<T>::kMax;
 }
 
-enum Status { kMapped = 0, kUnmapped = 1, kEmpty = 2 };
+enum Status { kMapped = 0, kUnmapped = 1, kEmpty = 2, kInvisible = 3 };
 
 // Per-thread page-walk state (K_CacheManager::_previousCoords / _previousEntries).
 struct Walk {
     uint32_t pcx, pcy, pcz;
     uint4 entry;
+    bool invisible;  // the mapped brick holds no value the view's transfer function shows
 };
 
 // Voxel sampling of one brick (slot base address), typed by T; MixedVoxel
@@ -325,7 +326,8 @@ __device__ __forceinline__ typename SampleOf<T>::type sample_any(const uint8_t *
 // (K_CacheManager.hpp:265-361).
 template <typename T>
 __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt, uint32_t sampler, uint32_t eb,
-                                     uint32_t lvl, V3 np, Walk &w, typename SampleOf<T>::type &sample) {
+                                     unsigned long long visible, uint32_t lvl, V3 np, Walk &w,
+                                     typename SampleOf<T>::type &sample) {
     const float px = np.x * lt.ior[lvl][0];
     const float py = np.y * lt.ior[lvl][1];
     const float pz = np.z * lt.ior[lvl][2];
@@ -348,7 +350,9 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
         if (fresh) {
             uint32_t *u = cv.usage + slot;
             if (*u != cv.ts) *u = cv.ts;
+            w.invisible = (__ldg(cv.slot_bins + slot) & visible) == 0ull;
         }
+        if (w.invisible) return kInvisible;  // no sample of this brick reaches the compositing threshold
         const float fx = px * static_cast<float>(lt.vvox[lvl][0]);
         const float fy = py * static_cast<float>(lt.vvox[lvl][1]);
         const float fz = pz * static_cast<float>(lt.vvox[lvl][2]);
@@ -458,6 +462,7 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
     }
     r.w.pcx = r.w.pcy = r.w.pcz = UINT_MAX;
     r.w.entry = make_uint4(0, 0, 0, 0);
+    r.w.invisible = false;
     r.maxOp = r.dvr ? 0.f : vp.state[4 * i];
     return true;
 }
@@ -487,7 +492,12 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
     }
     const uint32_t lod = r.lod;
     typename SampleOf<T>::type sample{};
-    const int st = fetch<T>(cv, lt, vp.sampler, vp.eb, vp.level_base + lod, np, r.w, sample);
+    const int st = fetch<T>(cv, lt, vp.sampler, vp.eb, vp.visible, vp.level_base + lod, np, r.w, sample);
+    if (st == kInvisible) {  // the step of a sample whose opacity stays below 0.001
+        r.t += vp.step[lod];
+        r.pos = r.pos + r.dir * vp.step[lod];
+        return true;
+    }
     if (st != kMapped) {
         if (st == kUnmapped) {
             vp.tbuf[r.i] = r.t;
@@ -656,6 +666,10 @@ RenderTuning &render_tuning() {
 }  // namespace gc
 
 extern "C" {
+int gc_render_empty_skip(int enable) {
+    return gc::guard([&] { gc::render_tuning().skip_empty = enable ? 1u : 0u; });
+}
+
 int gc_render_tuning_set(uint32_t scheduler, uint32_t tile_w, uint32_t threads, uint32_t blocks_per_sm) {
     return gc::guard([&] {
         GC_REQUIRE(scheduler <= 1, "scheduler must be 0 (tile) or 1 (pixel)");
@@ -689,6 +703,46 @@ struct RenderLaunch {
     void *func;
     uint32_t grid, threads;
 };
+// Visible value bins of each view (empty-space skipping).  A sample whose
+// value lies in bin b reads transfer-function entries within
+// [floor(b/64 w - 1/2) - 1, floor((b+1)/64 w - 1/2) + 2]; its opacity after the
+// correction 1 - (1 - a)^k is below k a / (1 - a) <= 1.05 k a for a <= 0.04,
+// so with a the largest alpha of those entries and k the largest exponent of
+// the view's levels, a bin with 1.05 k a < 0.0009 never reaches the
+// compositing threshold 0.001.  One warp per view, two bins per lane.
+__global__ void view_bins_kernel(ViewParams *views, uint32_t n) {
+    const uint32_t v = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31u;
+    if (v >= n) return;
+    ViewParams &vp = views[v];
+    if (!vp.skip_empty) {
+        if (lane == 0) vp.visible = ~0ull;
+        return;
+    }
+    float kmax = 0.f;
+    for (uint32_t l = 0; l < vp.nlevels; ++l) kmax = fmaxf(kmax, vp.kexp[l]);
+    const int w = static_cast<int>(vp.tfw);
+    unsigned long long mine = 0;
+    for (uint32_t b = lane; b < kValueBins; b += 32) {
+        const float lo = static_cast<float>(b) / kValueBins, hi = static_cast<float>(b + 1) / kValueBins;
+        int i0 = static_cast<int>(floorf(lo * w - 0.5f)) - 1, i1 = static_cast<int>(floorf(hi * w - 0.5f)) + 2;
+        i0 = max(i0, 0);
+        i1 = min(i1, w - 1);
+        float amax = 0.f;
+        for (int i = i0; i <= i1; ++i) amax = fmaxf(amax, __ldg(vp.tf + 4 * i + 3));
+        const bool visible = !(amax <= 0.04f && 1.05f * kmax * amax < 0.0009f);
+        if (visible) mine |= 1ull << b;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mine |= __shfl_xor_sync(0xffffffffu, mine, o);
+    if (lane == 0) vp.visible = mine;
+}
+
+void launch_view_bins(ViewParams *views_dev, uint32_t n, cudaStream_t s) {
+    view_bins_kernel<<<div_up(n, 4u), 128, 0, s>>>(views_dev, n);
+    GC_CUDA(cudaGetLastError());
+    count_launch();
+}
+
 // Voxel kind of a cache: its voxel width (1, 2, 4), 0 when its volumes'
 // widths differ, kTwoChannelU8 for two 8-bit channels.
 constexpr uint32_t kTwoChannelU8 = 0x202;
@@ -748,8 +802,9 @@ void RenderGraph::reset() {
     func = nullptr;
 }
 
-// The batched form's launch: an instantiated graph of two nodes -- the copy of
-// the view table from pinned host memory and the persistent ray caster -- is
+// The batched form's launch: an instantiated graph of three nodes -- the copy
+// of the view table from pinned host memory, the views' visible value bins
+// and the persistent ray caster -- is
 // replayed every tick; only the kernel's arguments (timestamp, view and tile
 // counts, grid) and the copy's size change, through the executable graph's
 // node-update calls.  The graph is rebuilt when the tuning changes the kernel.
@@ -770,18 +825,27 @@ void launch_render_graph(RenderGraph &g, const CacheView &cv, const LevelTables 
     kp.kernelParams = args;
     kp.extra = nullptr;
     const size_t bytes = static_cast<size_t>(nviews) * sizeof(ViewParams);
+    ViewParams *vbins = views_dev;
+    void *bargs[] = {&vbins, &nviews};
+    cudaKernelNodeParams bp = {};
+    bp.func = reinterpret_cast<void *>(view_bins_kernel);
+    bp.gridDim = dim3(div_up(nviews, 4u));
+    bp.blockDim = dim3(128);
+    bp.kernelParams = bargs;
     if (g.exec && (g.func != L.func || g.threads != L.threads)) g.reset();
     if (!g.exec) {
         GC_CUDA(cudaGraphCreate(&g.graph, 0));
         GC_CUDA(cudaGraphAddMemcpyNode1D(&g.copy, g.graph, nullptr, 0, views_dev, views_pinned, bytes,
                                          cudaMemcpyHostToDevice));
-        GC_CUDA(cudaGraphAddKernelNode(&g.kern, g.graph, &g.copy, 1, &kp));
+        GC_CUDA(cudaGraphAddKernelNode(&g.bins, g.graph, &g.copy, 1, &bp));
+        GC_CUDA(cudaGraphAddKernelNode(&g.kern, g.graph, &g.bins, 1, &kp));
         GC_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
         g.func = L.func;
         g.threads = L.threads;
     } else {
         GC_CUDA(cudaGraphExecMemcpyNodeSetParams1D(g.exec, g.copy, views_dev, views_pinned, bytes,
                                                    cudaMemcpyHostToDevice));
+        GC_CUDA(cudaGraphExecKernelNodeSetParams(g.exec, g.bins, &bp));
         GC_CUDA(cudaGraphExecKernelNodeSetParams(g.exec, g.kern, &kp));
     }
     GC_CUDA(cudaGraphLaunch(g.exec, s));

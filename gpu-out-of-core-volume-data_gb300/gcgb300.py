@@ -129,6 +129,7 @@ _SIGS = {
     "gc_cache_set_volume_source_host": [vp, C.c_uint32, vp, C.c_uint64, P(C.c_uint64), P(C.c_uint64), C.c_size_t],
     "gc_cache_set_volume_source_callback": [vp, C.c_uint32, LOADER_FN, vp, P(C.c_uint64), C.c_size_t],
     "gc_cache_create_shared": [P(CacheDesc), P(VolumeDesc), P(Layout), C.c_uint32, P(vp)],
+    "gc_render_empty_skip": [C.c_int],
     "gc_cache_set_volume_source_files": [vp, C.c_uint32, C.c_char_p, P(C.c_uint64), C.c_size_t, C.c_uint32],
     "gc_lz4_available": [],
     "gc_brick_files_write": [C.c_char_p, P(VolumeDesc), P(Layout), vp, C.c_uint64, P(C.c_uint64), C.c_uint32],
@@ -414,6 +415,11 @@ def make_view(inv_view, width, height, tf_ptr, tf_width, rgba_ptr, tbuf_ptr, sta
     return View((C.c_float * 12)(*inv_view), width, height, (C.c_float * 3)(*bbox_min), (C.c_float * 3)(*bbox_max),
                 tstep, focal, early_alpha, mode, sampler, tf_width, vp(tf_ptr), vp(rgba_ptr), vp(tbuf_ptr),
                 vp(state_ptr), vp(status_ptr or None), volume, tf_height)
+
+
+def render_empty_skip(enable):
+    """Empty-space skipping of the ray caster (on by default; same images)."""
+    check(lib.gc_render_empty_skip(1 if enable else 0))
 
 
 def lz4_available():

@@ -396,6 +396,13 @@ int gc_render_batch(gc_cache_t cache, const gc_view *views, uint32_t n, void *st
  * the autotuner of the Python host (gcgb300.autotune_render). */
 int gc_render_tuning_set(uint32_t scheduler, uint32_t tile_w, uint32_t threads, uint32_t blocks_per_sm);
 int gc_render_tuning_get(uint32_t out[4]);
+/* Empty-space skipping (process-wide, on by default; images are identical
+ * either way): each pool slot records the value range of its brick and each
+ * DVR view of a one-channel volume the value range its transfer function can
+ * make visible; a ray steps through a brick with no visible value without
+ * sampling it (the same t steps; samples there stay below the 0.001
+ * compositing threshold).  No counterpart in the reference. */
+int gc_render_empty_skip(int enable);
 
 /* ------------------------------------------------------------------------ */
 /* The reference's on-disk brick store (BricksManager.cpp:81-227,

@@ -74,3 +74,38 @@ def test_autotuner_candidates_render_identically(gc, orc, torch_cuda, restore_tu
             assert np.array_equal(a, r), cand
     best, timings = gc.autotune_render(s.cm, views, clear, candidates=gc.AUTOTUNE_CANDIDATES[:6], repeats=2)
     assert gc.render_tuning() == best and len(timings) == 6
+
+
+@pytest.mark.parametrize("tf_kind,sampler", [("ramp", 0), ("bumps", 1), ("ramp", 1)])
+def test_empty_space_skipping_changes_nothing(gc, orc, torch_cuda, tf_kind, sampler):
+    """With empty-space skipping off and on, every frame's image, t buffer,
+    colour state and cache state are identical (the loop is also checked
+    against the oracle with skipping on, its default, by the tests above)."""
+    runs = []
+    try:
+        for skip in (False, True):
+            gc.render_empty_skip(skip)
+            s = Scene(gc, orc, torch_cuda, (64, 64, 64), 2, 16, 1, (1, 1, 1), (6, 6, 6), 216)
+            tf = scenario.ramp_tf() if tf_kind == "ramp" else scenario.bumps_tf(4)
+            tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
+            g, _ = s.buffers(72, 56)
+            frames = []
+            for f in range(10):
+                if f % 5 == 0:
+                    for x in g:
+                        x.zero_()
+                v = s.view(scenario.orbit_camera(gc, f // 5 + 1, 12, 2.4), 72, 56, tf_dev, 256, g, sampler=sampler,
+                           early_alpha=0.99)
+                s.cm.render(v)
+                s.cm.update()
+                torch_cuda.cuda.synchronize()
+                lru = np.zeros(s.oc.nslots, dtype=s.oc.lru().dtype)
+                s.cm.dump(gc.DUMP_LRU, lru)
+                frames.append([x.cpu().numpy().copy() for x in g] + [lru])
+            runs.append(frames)
+            s.cm.close()
+    finally:
+        gc.render_empty_skip(True)
+    for f, (a, b) in enumerate(zip(*runs)):
+        for k in range(4):
+            assert np.array_equal(a[k], b[k]), (f, k)
