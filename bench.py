@@ -394,8 +394,10 @@ def run_ours(args):
         if not tuned:
             tuned.append(autotune(gc, torch, S, spec(args.warmup - 1), args))
         s0, l0 = S.cm.stats(), gc.kernel_launches()
+        torch.cuda.nvtx.range_push("timed_e2e" if e2e else "timed")
         wall, lat, info = timed(torch, S.stream, lambda i: S.converge(spec(args.warmup + i), e2e=e2e,
                                                                       cap=cfg.get("cap", 64)), args.steps)
+        torch.cuda.nvtx.range_pop()
         launches = gc.kernel_launches() - l0
         s1 = S.cm.stats()
         return S, wall, lat, info, launches, s0, s1
@@ -415,8 +417,12 @@ def run_ours(args):
     iters = [i for i, _ in info]
     conv = sum(1 for _, c in info if c)
 
-    # Roofline of the dominant kernel on a converged view: full work per launch.
-    last = spec(args.warmup + args.steps - 1)
+    # Roofline of the dominant kernel: a fixed view of the path (the last timed
+    # view of the default run), converged, re-rendered from scratch (full work
+    # per launch) after an L2 flush, 5 launches timed with CUDA events.
+    last = spec(cfg.get("roofline_frame", 42))
+    S.converge(last, cap=cfg.get("cap", 64))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > L2 (126 MB)
     ev = []
     torch.cuda.nvtx.range_push("roofline")
     for _ in range(5):
@@ -424,6 +430,7 @@ def run_ours(args):
         with torch.cuda.stream(S.stream):
             bufs[0][1].zero_()
             bufs[0][2].zero_()
+            flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(S.stream)
             S.cm.render(views[0], S.sp)
@@ -442,6 +449,7 @@ def run_ours(args):
         with torch.cuda.stream(S.stream):
             bufs[0][1].zero_()
             bufs[0][2].zero_()
+            flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(S.stream)
             S.cm.render(views[0], S.sp)
@@ -482,7 +490,8 @@ def run_ours(args):
                      "peak_kind": peak_kind, "algorithmic_bytes_per_launch": int(algo),
                      "launch_ms": round(render_ms, 4), "launch_ms_without_empty_skip": round(render_ms_noskip, 4),
                      "touched_bricks": int(touched),
-                     "note": f"converged {W}x{H} view of {args.config}; compulsory bytes = touched bricks x B^3 x "
+                     "note": f"view {cfg.get('roofline_frame', 42)} of the {args.config} path, converged, "
+                             f"re-rendered after an L2 flush; compulsory bytes = touched bricks x B^3 x "
                              f"{vol.encoded_bytes} B + {PIXEL_BYTES} B/pixel"},
         "render_tuning": {"scheduler_tile_threads_bps": list(tuned[0][0]) if tuned else None,
                           "candidates_timed": len(tuned[0][1]) if tuned else 0},
