@@ -45,6 +45,7 @@ struct CacheView {
     uint32_t mx, my, mz;
     uint32_t sx, sy, sz;
     uint32_t B, c, Beff;
+    uint32_t beff_magic;  // ceil(2^31 / Beff) for the exact multiply-shift modulo (0: use %)
     uint32_t eb;          // bytes per voxel of every volume, 0 when the volumes differ
     uint32_t nc;          // channels per voxel (1, or 2 for two 8-bit channels)
     uint64_t slot_bytes;  // pool slot stride: B^3 x the widest voxel
@@ -78,6 +79,7 @@ struct ViewParams {
     float inv_size[GC_MAX_LEVELS][3];   // bboxSizeMin / initial level size
     float step[GC_MAX_LEVELS];          // LODStepSize
     float kexp[GC_MAX_LEVELS];          // LODStepSize / tstep (opacity correction exponent)
+    float alpha_floor[GC_MAX_LEVELS];   // alphas at or below this cannot reach the 0.001 threshold
     uint32_t tiles_x;                   // warp tiles per row
     uint32_t tile_shift;                // log2 of the tile width
     uint32_t tile_begin;                // first global tile index of this view

@@ -101,6 +101,7 @@ struct gc_cache {
     std::vector<uint32_t> level_volume;  // volume of each cache level
     gc::LevelTables lt;
     uint32_t mx = 0, my = 0, mz = 0, nslots = 0, B = 0, c = 0, Beff = 0;
+    uint32_t beff_magic = 0;          // ceil(2^31 / Beff) when every level has < 2^24 voxels per axis
     uint32_t eb = 0;                  // voxel bytes of every volume, 0 when they differ
     uint32_t nc = 1;                  // channels per voxel (the same for every volume)
     uint64_t nentries = 0;
@@ -178,6 +179,11 @@ static void build_tables(gc_cache *C) {
     }
     lt.nlevels = l;
     C->mx = off;
+    // exact multiply-shift modulo by Beff for voxel coordinates below 2^24
+    bool small = C->Beff >= 1 && C->Beff <= 128;
+    for (uint32_t k = 0; k < l; ++k)
+        for (int a = 0; a < 3; ++a) small = small && lt.vvox[k][a] < (1u << 24);
+    C->beff_magic = small ? static_cast<uint32_t>(((1ull << 31) + C->Beff - 1) / C->Beff) : 0u;
 }
 
 // Resolve the asked bricks: RequestHandler::handle_request (RequestHandler.hpp:277-372).
@@ -414,6 +420,7 @@ static CacheView cache_view(const gc_cache *C) {
     cv.B = C->B;
     cv.c = C->c;
     cv.Beff = C->Beff;
+    cv.beff_magic = C->beff_magic;
     cv.eb = C->eb;
     cv.nc = C->nc;
     cv.slot_bytes = C->slot_bytes;
@@ -596,6 +603,9 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
         const uint32_t mn = std::min(L.initial[l][0], std::min(L.initial[l][1], L.initial[l][2]));
         out.step[l] = (bmin / static_cast<float>(mn)) / 2.f;
         out.kexp[l] = out.step[l] / in.tstep;
+        // 1 - (1 - a)^k <= k a / (1 - a) <= 1.05 k a for a <= 0.04: below the
+        // floor the corrected opacity stays under 0.0009 (threshold 0.001)
+        out.alpha_floor[l] = out.kexp[l] > 0.f ? std::min(0.04f, 0.0009f / (1.05f * out.kexp[l])) : 0.f;
     }
     const uint32_t tw = render_tuning().tile_w;
     out.tiles_x = div_up(in.width, tw);

@@ -179,12 +179,22 @@ __device__ __forceinline__ float sample_corner(const T *__restrict__ b, uint32_t
     }
 }
 
+// x mod (B - 2c) by a multiply-shift: with m = ceil(2^31 / d), floor(x m / 2^31)
+// is floor(x / d) for every x < 2^24 and d <= 128 (the host sets m only when
+// every level's voxel count is below 2^24; m = 0 falls back to %).
+__device__ __forceinline__ uint32_t mod_beff(uint32_t x, uint32_t d, uint32_t m) {
+    if (m == 0) return x % d;
+    const uint32_t q = static_cast<uint32_t>((static_cast<uint64_t>(x) * m) >> 31);
+    return x - q * d;
+}
+
 // Trilinear sampler at the fractional position f (voxels of the level); the
 // pair (i0, i0 + 1) is clamped to the brick (only reachable with covering 0).
-__device__ __forceinline__ void tri_axis(float f, uint32_t c, uint32_t beff, uint32_t B, uint32_t &i0, float &w) {
+__device__ __forceinline__ void tri_axis(float f, uint32_t c, uint32_t beff, uint32_t magic, uint32_t B,
+                                         uint32_t &i0, float &w) {
     const uint32_t m = static_cast<uint32_t>(f);
     const float fr = f - static_cast<float>(m);
-    const uint32_t l = c + m % beff;
+    const uint32_t l = c + mod_beff(m, beff, magic);
     if (fr >= 0.5f) {
         i0 = l;
         w = fr - 0.5f;
@@ -250,16 +260,16 @@ __device__ __forceinline__ float sample_slot(const uint8_t *base, uint32_t /*eb*
     const T *b = reinterpret_cast<const T *>(base);
     const uint32_t B = cv.B;
     if (sampler == GC_SAMPLER_REFERENCE) {
-        const uint32_t lx = cv.c + static_cast<uint32_t>(fx) % cv.Beff;
-        const uint32_t ly = cv.c + static_cast<uint32_t>(fy) % cv.Beff;
-        const uint32_t lz = cv.c + static_cast<uint32_t>(fz) % cv.Beff;
+        const uint32_t lx = cv.c + mod_beff(static_cast<uint32_t>(fx), cv.Beff, cv.beff_magic);
+        const uint32_t ly = cv.c + mod_beff(static_cast<uint32_t>(fy), cv.Beff, cv.beff_magic);
+        const uint32_t lz = cv.c + mod_beff(static_cast<uint32_t>(fz), cv.Beff, cv.beff_magic);
         return sample_corner<T>(b, B, lx, ly, lz);
     }
     uint32_t x0, y0, z0;
     float wx, wy, wz;
-    tri_axis(fx, cv.c, cv.Beff, B, x0, wx);
-    tri_axis(fy, cv.c, cv.Beff, B, y0, wy);
-    tri_axis(fz, cv.c, cv.Beff, B, z0, wz);
+    tri_axis(fx, cv.c, cv.Beff, cv.beff_magic, B, x0, wx);
+    tri_axis(fy, cv.c, cv.Beff, cv.beff_magic, B, y0, wy);
+    tri_axis(fz, cv.c, cv.Beff, cv.beff_magic, B, z0, wz);
     return sample_trilinear<T>(b, B, x0, y0, z0, wx, wy, wz);
 }
 template <>
@@ -275,9 +285,9 @@ __device__ __forceinline__ float2 sample_slot_two(const uint8_t *__restrict__ b,
                                                   uint32_t sampler, float fx, float fy, float fz) {
     const uint32_t B = cv.B, BB = B * B;
     if (sampler == GC_SAMPLER_REFERENCE) {
-        uint32_t lx = cv.c + static_cast<uint32_t>(fx) % cv.Beff;
-        uint32_t ly = cv.c + static_cast<uint32_t>(fy) % cv.Beff;
-        uint32_t lz = cv.c + static_cast<uint32_t>(fz) % cv.Beff;
+        uint32_t lx = cv.c + mod_beff(static_cast<uint32_t>(fx), cv.Beff, cv.beff_magic);
+        uint32_t ly = cv.c + mod_beff(static_cast<uint32_t>(fy), cv.Beff, cv.beff_magic);
+        uint32_t lz = cv.c + mod_beff(static_cast<uint32_t>(fz), cv.Beff, cv.beff_magic);
         lx = lx > 0 ? lx : 1u;
         ly = ly > 0 ? ly : 1u;
         lz = lz > 0 ? lz : 1u;
@@ -294,9 +304,9 @@ __device__ __forceinline__ float2 sample_slot_two(const uint8_t *__restrict__ b,
     }
     uint32_t x0, y0, z0;
     float wx, wy, wz;
-    tri_axis(fx, cv.c, cv.Beff, B, x0, wx);
-    tri_axis(fy, cv.c, cv.Beff, B, y0, wy);
-    tri_axis(fz, cv.c, cv.Beff, B, z0, wz);
+    tri_axis(fx, cv.c, cv.Beff, cv.beff_magic, B, x0, wx);
+    tri_axis(fy, cv.c, cv.Beff, cv.beff_magic, B, y0, wy);
+    tri_axis(fz, cv.c, cv.Beff, cv.beff_magic, B, z0, wz);
     const uint32_t i = (z0 * B + y0) * B + x0;
     float out[2];
 #pragma unroll
@@ -515,7 +525,10 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
     }
     if (r.dvr) {
         float4 col = classify(vp, sample);
-        col.w = 1.0f - gc_pow(1.0f - col.w, vp.kexp[lod]);
+        // Opacity correction 1 - (1 - a)^k.  For a <= alpha_floor[lod] the
+        // corrected opacity is below 1.05 k a <= 0.0009, under the compositing
+        // threshold: the correction is skipped, the result is the same.
+        col.w = col.w > vp.alpha_floor[lod] ? 1.0f - gc_pow(1.0f - col.w, vp.kexp[lod]) : 0.0f;
         if (col.w > 0.001f) {
             col.x *= col.w;
             col.y *= col.w;
