@@ -85,6 +85,12 @@ CONFIGS = {
 }
 DIAG = 2.0 * math.sqrt(3.0)
 PIXEL_BYTES = 44  # RGBA 4 + t 4+4 + colour state 16+16 per pixel and launch
+# DRAM bytes (read + write) of the c2 roofline launch (view 42, converged, after
+# an L2 flush), from one ncu capture of this command:
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none --nvtx
+#       --nvtx-include roofline/ -k regex:render -c 2 python bench.py --steps 4 --warmup 3 --no-cpu-baseline --no-batched
+# (profiles/render_kernel_c2_1024x1024.md).  None for the other configs.
+ROOFLINE_TRAFFIC = {"c2": 107_050_000}
 
 
 def workload(name, cfg):
@@ -485,7 +491,7 @@ def run_ours(args):
                 "h2d_bytes_per_step": int((s1_e.bytes_h2d - s0_e.bytes_h2d) / args.steps) + 700,
                 "d2h_bytes_per_step": W * H * 4, "latency_ms": {"p50": pct(lat_e, 50), "p99": pct(lat_e, 99)}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 5), "traffic": None,
+                     "frac": round(achieved / peak, 5), "traffic": ROOFLINE_TRAFFIC.get(args.config),
                      "kernel": "render_pixels_kernel" if gc.render_tuning()[0] == 1 else "render_kernel",
                      "peak_kind": peak_kind, "algorithmic_bytes_per_launch": int(algo),
                      "launch_ms": round(render_ms, 4), "launch_ms_without_empty_skip": round(render_ms_noskip, 4),
