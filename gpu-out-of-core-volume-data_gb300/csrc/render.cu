@@ -53,6 +53,11 @@ __device__ __forceinline__ V3 cross(V3 a, V3 b) {
     return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 __device__ __forceinline__ float clampf(float f, float a, float b) { return fmaxf(a, fminf(f, b)); }
+// Fused multiply-add at the places the oracle uses fmaf (the unit is built
+// with -fmad=false, so no other operation is contracted and every rounding is
+// the oracle's).
+__device__ __forceinline__ float fmad(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ V3 fma3(V3 a, float b, V3 c) { return v3(fmad(a.x, b, c.x), fmad(a.y, b, c.y), fmad(a.z, b, c.z)); }
 __device__ __forceinline__ float saturate(float x) { return (x != x) ? 0.0f : fminf(fmaxf(x, 0.0f), 1.0f); }
 
 // log2 for normal x > 0: x = m 2^e, m in [sqrt(1/2), sqrt(2)), then
@@ -67,25 +72,25 @@ __device__ __forceinline__ float gc_log2(float x) {
     }
     const float s = (m - 1.0f) / (m + 1.0f);
     const float s2 = s * s;
-    float p = s2 * 0.11111111f + 0.14285715f;
-    p = p * s2 + 0.2f;
-    p = p * s2 + 0.33333334f;
-    p = p * s2 + 1.0f;
+    float p = fmad(s2, 0.11111111f, 0.14285715f);
+    p = fmad(p, s2, 0.2f);
+    p = fmad(p, s2, 0.33333334f);
+    p = fmad(p, s2, 1.0f);
     const float ln = (2.0f * s) * p;
-    return static_cast<float>(e) + ln * 1.44269504f;
+    return fmad(ln, 1.44269504f, static_cast<float>(e));
 }
 // exp2 for y <= 0: y = n + f, f in [-1/2, 1/2], e^(f ln 2) by Taylor to degree 7.
 __device__ __forceinline__ float gc_exp2(float y) {
     if (y < -125.0f) return 0.0f;
     const float n = floorf(y + 0.5f);
     const float t = (y - n) * 0.69314718f;
-    float p = t * 0.00019841270f + 0.0013888889f;
-    p = p * t + 0.0083333333f;
-    p = p * t + 0.041666668f;
-    p = p * t + 0.16666667f;
-    p = p * t + 0.5f;
-    p = p * t + 1.0f;
-    p = p * t + 1.0f;
+    float p = fmad(t, 0.00019841270f, 0.0013888889f);
+    p = fmad(p, t, 0.0083333333f);
+    p = fmad(p, t, 0.041666668f);
+    p = fmad(p, t, 0.16666667f);
+    p = fmad(p, t, 0.5f);
+    p = fmad(p, t, 1.0f);
+    p = fmad(p, t, 1.0f);
     const float scale = __uint_as_float(static_cast<uint32_t>(static_cast<int>(n) + 127) << 23);
     return p * scale;
 }
@@ -96,7 +101,7 @@ __device__ __forceinline__ float gc_pow(float x, float k) {
 }
 
 __device__ __forceinline__ float4 tf_lookup(const float *__restrict__ tf, uint32_t w, float s) {
-    const float xb = s * static_cast<float>(w) - 0.5f;
+    const float xb = fmad(s, static_cast<float>(w), -0.5f);
     const float fl = floorf(xb);
     const float a = xb - fl;
     int i0 = static_cast<int>(fl);
@@ -106,8 +111,8 @@ __device__ __forceinline__ float4 tf_lookup(const float *__restrict__ tf, uint32
     i1 = i1 < 0 ? 0 : (i1 > hi ? hi : i1);
     const float4 t0 = __ldg(reinterpret_cast<const float4 *>(tf) + i0);
     const float4 t1 = __ldg(reinterpret_cast<const float4 *>(tf) + i1);
-    return make_float4(t0.x + (t1.x - t0.x) * a, t0.y + (t1.y - t0.y) * a, t0.z + (t1.z - t0.z) * a,
-                       t0.w + (t1.w - t0.w) * a);
+    return make_float4(fmad(t1.x - t0.x, a, t0.x), fmad(t1.y - t0.y, a, t0.y), fmad(t1.z - t0.z, a, t0.z),
+                       fmad(t1.w - t0.w, a, t0.w));
 }
 
 // 2D transfer function (two-channel volumes): a w x h table of RGBA, channel
@@ -115,7 +120,7 @@ __device__ __forceinline__ float4 tf_lookup(const float *__restrict__ tf, uint32
 // axis (bilinear, edge-clamped).
 __device__ __forceinline__ float4 tf2d_lookup(const float *__restrict__ tf, uint32_t w, uint32_t h, float s0,
                                               float s1) {
-    const float xb = s0 * static_cast<float>(w) - 0.5f, yb = s1 * static_cast<float>(h) - 0.5f;
+    const float xb = fmad(s0, static_cast<float>(w), -0.5f), yb = fmad(s1, static_cast<float>(h), -0.5f);
     const float flx = floorf(xb), fly = floorf(yb);
     const float ax = xb - flx, ay = yb - fly;
     const int hx = static_cast<int>(w) - 1, hy = static_cast<int>(h) - 1;
@@ -127,12 +132,12 @@ __device__ __forceinline__ float4 tf2d_lookup(const float *__restrict__ tf, uint
     const float4 *t = reinterpret_cast<const float4 *>(tf);
     const float4 t00 = __ldg(t + j0 * static_cast<int>(w) + i0), t10 = __ldg(t + j0 * static_cast<int>(w) + i1);
     const float4 t01 = __ldg(t + j1 * static_cast<int>(w) + i0), t11 = __ldg(t + j1 * static_cast<int>(w) + i1);
-    const float4 r0 = make_float4(t00.x + (t10.x - t00.x) * ax, t00.y + (t10.y - t00.y) * ax,
-                                  t00.z + (t10.z - t00.z) * ax, t00.w + (t10.w - t00.w) * ax);
-    const float4 r1 = make_float4(t01.x + (t11.x - t01.x) * ax, t01.y + (t11.y - t01.y) * ax,
-                                  t01.z + (t11.z - t01.z) * ax, t01.w + (t11.w - t01.w) * ax);
-    return make_float4(r0.x + (r1.x - r0.x) * ay, r0.y + (r1.y - r0.y) * ay, r0.z + (r1.z - r0.z) * ay,
-                       r0.w + (r1.w - r0.w) * ay);
+    const float4 r0 = make_float4(fmad(t10.x - t00.x, ax, t00.x), fmad(t10.y - t00.y, ax, t00.y),
+                                  fmad(t10.z - t00.z, ax, t00.z), fmad(t10.w - t00.w, ax, t00.w));
+    const float4 r1 = make_float4(fmad(t11.x - t01.x, ax, t01.x), fmad(t11.y - t01.y, ax, t01.y),
+                                  fmad(t11.z - t01.z, ax, t01.z), fmad(t11.w - t01.w, ax, t01.w));
+    return make_float4(fmad(r1.x - r0.x, ay, r0.x), fmad(r1.y - r0.y, ay, r0.y), fmad(r1.z - r0.z, ay, r0.z),
+                       fmad(r1.w - r0.w, ay, r0.w));
 }
 
 template <typename T>
@@ -215,13 +220,13 @@ template <typename T>
 __device__ __forceinline__ float sample_trilinear(const T *__restrict__ b, uint32_t B, uint32_t x0, uint32_t y0,
                                                   uint32_t z0, float wx, float wy, float wz) {
     const uint32_t i = (z0 * B + y0) * B + x0, BB = B * B;
-    const float c00 = ldv(b, i) + (ldv(b, i + 1) - ldv(b, i)) * wx;
-    const float c10 = ldv(b, i + B) + (ldv(b, i + B + 1) - ldv(b, i + B)) * wx;
-    const float c01 = ldv(b, i + BB) + (ldv(b, i + BB + 1) - ldv(b, i + BB)) * wx;
-    const float c11 = ldv(b, i + BB + B) + (ldv(b, i + BB + B + 1) - ldv(b, i + BB + B)) * wx;
-    const float c0 = c00 + (c10 - c00) * wy;
-    const float c1 = c01 + (c11 - c01) * wy;
-    return (c0 + (c1 - c0) * wz) / VoxelTraits<T>::kMax;
+    const float c00 = fmad(ldv(b, i + 1) - ldv(b, i), wx, ldv(b, i));
+    const float c10 = fmad(ldv(b, i + B + 1) - ldv(b, i + B), wx, ldv(b, i + B));
+    const float c01 = fmad(ldv(b, i + BB + 1) - ldv(b, i + BB), wx, ldv(b, i + BB));
+    const float c11 = fmad(ldv(b, i + BB + B + 1) - ldv(b, i + BB + B), wx, ldv(b, i + BB + B));
+    const float c0 = fmad(c10 - c00, wy, c00);
+    const float c1 = fmad(c11 - c01, wy, c01);
+    return fmad(c1 - c0, wz, c0) / VoxelTraits<T>::kMax;
 }
 
 enum Status { kMapped = 0, kUnmapped = 1, kEmpty = 2, kInvisible = 3 };
@@ -312,13 +317,13 @@ __device__ __forceinline__ float2 sample_slot_two(const uint8_t *__restrict__ b,
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         auto lv = [&](uint32_t j) { return static_cast<float>(__ldg(b + 2 * j + k)); };
-        const float c00 = lv(i) + (lv(i + 1) - lv(i)) * wx;
-        const float c10 = lv(i + B) + (lv(i + B + 1) - lv(i + B)) * wx;
-        const float c01 = lv(i + BB) + (lv(i + BB + 1) - lv(i + BB)) * wx;
-        const float c11 = lv(i + BB + B) + (lv(i + BB + B + 1) - lv(i + BB + B)) * wx;
-        const float c0 = c00 + (c10 - c00) * wy;
-        const float c1 = c01 + (c11 - c01) * wy;
-        out[k] = (c0 + (c1 - c0) * wz) / 255.0f;
+        const float c00 = fmad(lv(i + 1) - lv(i), wx, lv(i));
+        const float c10 = fmad(lv(i + B + 1) - lv(i + B), wx, lv(i + B));
+        const float c01 = fmad(lv(i + BB + 1) - lv(i + BB), wx, lv(i + BB));
+        const float c11 = fmad(lv(i + BB + B + 1) - lv(i + BB + B), wx, lv(i + BB + B));
+        const float c0 = fmad(c10 - c00, wy, c00);
+        const float c1 = fmad(c11 - c01, wy, c01);
+        out[k] = fmad(c1 - c0, wz, c0) / 255.0f;
     }
     return make_float2(out[0], out[1]);
 }
@@ -486,7 +491,7 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
     const float alpha = r.t / r.tfar;
     const float pX = r.endX * alpha;
     const float pY = r.endY * alpha;
-    V3 tp = r.pos * 0.495f + v3(0.495f, 0.495f, 0.495f);
+    V3 tp = fma3(r.pos, 0.495f, v3(0.495f, 0.495f, 0.495f));
     tp.z = 1.0f - tp.z;
     const V3 np = v3(clampf(tp.x, 0.f, 0.99f), clampf(tp.y, 0.f, 0.99f), clampf(tp.z, 0.f, 0.99f));
     // compute_LOD: the level only grows along a ray because the pixel
@@ -505,7 +510,7 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
     const int st = fetch<T>(cv, lt, vp.sampler, vp.eb, vp.visible, vp.level_base + lod, np, r.w, sample);
     if (st == kInvisible) {  // the step of a sample whose opacity stays below 0.001
         r.t += vp.step[lod];
-        r.pos = r.pos + r.dir * vp.step[lod];
+        r.pos = fma3(r.dir, vp.step[lod], r.pos);
         return true;
     }
     if (st != kMapped) {
@@ -520,7 +525,7 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
         }
         r.t += vp.tstep;
         if (r.t > r.tfar) return false;
-        r.pos = r.pos + r.dir * vp.tstep;
+        r.pos = fma3(r.dir, vp.tstep, r.pos);
         return true;
     }
     if (r.dvr) {
@@ -534,16 +539,16 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
             col.y *= col.w;
             col.z *= col.w;
             const float rr = 1.0f - r.fc.w;
-            r.fc.x = r.fc.x + col.x * rr;
-            r.fc.y = r.fc.y + col.y * rr;
-            r.fc.z = r.fc.z + col.z * rr;
-            r.fc.w = r.fc.w + col.w * rr;
+            r.fc.x = fmad(col.x, rr, r.fc.x);
+            r.fc.y = fmad(col.y, rr, r.fc.y);
+            r.fc.z = fmad(col.z, rr, r.fc.z);
+            r.fc.w = fmad(col.w, rr, r.fc.w);
         }
     } else {
         r.maxOp = fmaxf(r.maxOp, first_channel(sample));
     }
     r.t += vp.step[lod];
-    r.pos = r.pos + r.dir * vp.step[lod];
+    r.pos = fma3(r.dir, vp.step[lod], r.pos);
     return true;
 }
 

@@ -712,6 +712,9 @@ static f3 norm3(f3 a) {
 }
 static f3 cross3(f3 a, f3 b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
 static float clampf_(float f, float a, float b) { return fmaxf(a, fminf(f, b)); }
+/* a * b + c fused per component: the fused multiply-adds of the CUDA ray
+   caster (render.cu fmad/fma3) at the same places, so every rounding agrees. */
+static f3 fma3o(f3 a, float b, f3 c) { return mk(fmaf(a.x, b, c.x), fmaf(a.y, b, c.y), fmaf(a.z, b, c.z)); }
 static float sat(float x) { return (x != x) ? 0.0f : fminf(fmaxf(x, 0.0f), 1.0f); }
 
 static uint32_t f2u(float f) {
@@ -734,24 +737,24 @@ static float o_log2(float x) {
     }
     float s = (m - 1.0f) / (m + 1.0f);
     float s2 = s * s;
-    float p = s2 * 0.11111111f + 0.14285715f;
-    p = p * s2 + 0.2f;
-    p = p * s2 + 0.33333334f;
-    p = p * s2 + 1.0f;
+    float p = fmaf(s2, 0.11111111f, 0.14285715f);
+    p = fmaf(p, s2, 0.2f);
+    p = fmaf(p, s2, 0.33333334f);
+    p = fmaf(p, s2, 1.0f);
     float ln = (2.0f * s) * p;
-    return (float)e + ln * 1.44269504f;
+    return fmaf(ln, 1.44269504f, (float)e);
 }
 static float o_exp2(float y) {
     if (y < -125.0f) return 0.0f;
     float n = floorf(y + 0.5f);
     float t = (y - n) * 0.69314718f;
-    float p = t * 0.00019841270f + 0.0013888889f;
-    p = p * t + 0.0083333333f;
-    p = p * t + 0.041666668f;
-    p = p * t + 0.16666667f;
-    p = p * t + 0.5f;
-    p = p * t + 1.0f;
-    p = p * t + 1.0f;
+    float p = fmaf(t, 0.00019841270f, 0.0013888889f);
+    p = fmaf(p, t, 0.0083333333f);
+    p = fmaf(p, t, 0.041666668f);
+    p = fmaf(p, t, 0.16666667f);
+    p = fmaf(p, t, 0.5f);
+    p = fmaf(p, t, 1.0f);
+    p = fmaf(p, t, 1.0f);
     float scale = u2f((uint32_t)((int)n + 127) << 23);
     return p * scale;
 }
@@ -765,15 +768,15 @@ typedef struct {
     float x, y, z, w;
 } f4;
 static f4 tf_lookup(const float *tf, uint32_t w, float s) {
-    float xb = s * (float)w - 0.5f;
+    float xb = fmaf(s, (float)w, -0.5f);
     float fl = floorf(xb);
     float a = xb - fl;
     int i0 = (int)fl, i1 = i0 + 1, hi = (int)w - 1;
     i0 = i0 < 0 ? 0 : (i0 > hi ? hi : i0);
     i1 = i1 < 0 ? 0 : (i1 > hi ? hi : i1);
     const float *t0 = tf + 4 * i0, *t1 = tf + 4 * i1;
-    f4 r = {t0[0] + (t1[0] - t0[0]) * a, t0[1] + (t1[1] - t0[1]) * a, t0[2] + (t1[2] - t0[2]) * a,
-            t0[3] + (t1[3] - t0[3]) * a};
+    f4 r = {fmaf(t1[0] - t0[0], a, t0[0]), fmaf(t1[1] - t0[1], a, t0[1]), fmaf(t1[2] - t0[2], a, t0[2]),
+            fmaf(t1[3] - t0[3], a, t0[3])};
     return r;
 }
 
@@ -782,7 +785,7 @@ static f4 tf_lookup(const float *tf, uint32_t w, float s) {
    reference, whose ray caster reads one channel; same rule as tf_lookup on
    each axis). */
 static f4 tf2d_lookup(const float *tf, uint32_t w, uint32_t h, float s0, float s1) {
-    float xb = s0 * (float)w - 0.5f, yb = s1 * (float)h - 0.5f;
+    float xb = fmaf(s0, (float)w, -0.5f), yb = fmaf(s1, (float)h, -0.5f);
     float flx = floorf(xb), fly = floorf(yb);
     float ax = xb - flx, ay = yb - fly;
     int hx = (int)w - 1, hy = (int)h - 1;
@@ -795,11 +798,11 @@ static f4 tf2d_lookup(const float *tf, uint32_t w, uint32_t h, float s0, float s
     const float *t01 = tf + 4 * (j1 * (int)w + i0), *t11 = tf + 4 * (j1 * (int)w + i1);
     float r0[4], r1[4];
     for (int k = 0; k < 4; ++k) {
-        r0[k] = t00[k] + (t10[k] - t00[k]) * ax;
-        r1[k] = t01[k] + (t11[k] - t01[k]) * ax;
+        r0[k] = fmaf(t10[k] - t00[k], ax, t00[k]);
+        r1[k] = fmaf(t11[k] - t01[k], ax, t01[k]);
     }
-    f4 r = {r0[0] + (r1[0] - r0[0]) * ay, r0[1] + (r1[1] - r0[1]) * ay, r0[2] + (r1[2] - r0[2]) * ay,
-            r0[3] + (r1[3] - r0[3]) * ay};
+    f4 r = {fmaf(r1[0] - r0[0], ay, r0[0]), fmaf(r1[1] - r0[1], ay, r0[1]), fmaf(r1[2] - r0[2], ay, r0[2]),
+            fmaf(r1[3] - r0[3], ay, r0[3])};
     return r;
 }
 
@@ -899,13 +902,13 @@ static int fetch32(orc_cache *c, uint32_t sampler, uint32_t lod, f3 np, walk *w,
                 uint32_t i = (z0 * B + y0) * B + x0;
                 for (int k = 0; k < 2; ++k) {
 #define LV2(j) ((float)sb[2 * (j) + k])
-                    float c00 = LV2(i) + (LV2(i + 1) - LV2(i)) * wx;
-                    float c10 = LV2(i + B) + (LV2(i + B + 1) - LV2(i + B)) * wx;
-                    float c01 = LV2(i + BB2) + (LV2(i + BB2 + 1) - LV2(i + BB2)) * wx;
-                    float c11 = LV2(i + BB2 + B) + (LV2(i + BB2 + B + 1) - LV2(i + BB2 + B)) * wx;
+                    float c00 = fmaf(LV2(i + 1) - LV2(i), wx, LV2(i));
+                    float c10 = fmaf(LV2(i + B + 1) - LV2(i + B), wx, LV2(i + B));
+                    float c01 = fmaf(LV2(i + BB2 + 1) - LV2(i + BB2), wx, LV2(i + BB2));
+                    float c11 = fmaf(LV2(i + BB2 + B + 1) - LV2(i + BB2 + B), wx, LV2(i + BB2 + B));
 #undef LV2
-                    float c0 = c00 + (c10 - c00) * wy, c1 = c01 + (c11 - c01) * wy;
-                    sample[k] = (c0 + (c1 - c0) * wz) / 255.0f;
+                    float c0 = fmaf(c10 - c00, wy, c00), c1 = fmaf(c11 - c01, wy, c01);
+                    sample[k] = fmaf(c1 - c0, wz, c0) / 255.0f;
                 }
             }
             return 0;
@@ -937,14 +940,14 @@ static int fetch32(orc_cache *c, uint32_t sampler, uint32_t lod, f3 np, walk *w,
             tri_axis(fz, c->c, c->Beff, B, &z0, &wz);
             uint32_t i = (z0 * B + y0) * B + x0, BB2 = B * B;
 #define LV(k) voxel_value(c, sb, (k))
-            float c00 = LV(i) + (LV(i + 1) - LV(i)) * wx;
-            float c10 = LV(i + B) + (LV(i + B + 1) - LV(i + B)) * wx;
-            float c01 = LV(i + BB2) + (LV(i + BB2 + 1) - LV(i + BB2)) * wx;
-            float c11 = LV(i + BB2 + B) + (LV(i + BB2 + B + 1) - LV(i + BB2 + B)) * wx;
+            float c00 = fmaf(LV(i + 1) - LV(i), wx, LV(i));
+            float c10 = fmaf(LV(i + B + 1) - LV(i + B), wx, LV(i + B));
+            float c01 = fmaf(LV(i + BB2 + 1) - LV(i + BB2), wx, LV(i + BB2));
+            float c11 = fmaf(LV(i + BB2 + B + 1) - LV(i + BB2 + B), wx, LV(i + BB2 + B));
 #undef LV
-            float c0 = c00 + (c10 - c00) * wy, c1 = c01 + (c11 - c01) * wy;
+            float c0 = fmaf(c10 - c00, wy, c00), c1 = fmaf(c11 - c01, wy, c01);
             float mx = c->eb == 1 ? 255.0f : (c->eb == 2 ? 65535.0f : 1.0f);
-            *sample = (c0 + (c1 - c0) * wz) / mx;
+            *sample = fmaf(c1 - c0, wz, c0) / mx;
         }
         return 0;
     }
@@ -1013,7 +1016,7 @@ static void march32(orc_cache *c, const gc_view *v, const float *tf, const lod_t
         while ((!dvr || fc.w < v->early_alpha) && t < tfar) {
             float alpha = t / tfar;
             float pX = endX * alpha, pY = endY * alpha;
-            f3 tp = add3(muls(pos, 0.495f), mk(0.495f, 0.495f, 0.495f));
+            f3 tp = mk(fmaf(pos.x, 0.495f, 0.495f), fmaf(pos.y, 0.495f, 0.495f), fmaf(pos.z, 0.495f, 0.495f));
             tp.z = 1.0f - tp.z;
             f3 np = mk(clampf_(tp.x, 0.f, 0.99f), clampf_(tp.y, 0.f, 0.99f), clampf_(tp.z, 0.f, 0.99f));
             /* compute_LOD, full scan */
@@ -1043,7 +1046,7 @@ static void march32(orc_cache *c, const gc_view *v, const float *tf, const lod_t
                 }
                 t += v->tstep;
                 if (t > tfar) break;
-                pos = add3(pos, muls(dir, v->tstep));
+                pos = fma3o(dir, v->tstep, pos);
                 continue;
             }
             if (dvr) {
@@ -1055,16 +1058,16 @@ static void march32(orc_cache *c, const gc_view *v, const float *tf, const lod_t
                     col.y *= col.w;
                     col.z *= col.w;
                     float r = 1.0f - fc.w;
-                    fc.x = fc.x + col.x * r;
-                    fc.y = fc.y + col.y * r;
-                    fc.z = fc.z + col.z * r;
-                    fc.w = fc.w + col.w * r;
+                    fc.x = fmaf(col.x, r, fc.x);
+                    fc.y = fmaf(col.y, r, fc.y);
+                    fc.z = fmaf(col.z, r, fc.z);
+                    fc.w = fmaf(col.w, r, fc.w);
                 }
             } else {
                 maxOp = fmaxf(maxOp, sample);
             }
             t += T->step[lod];
-            pos = add3(pos, muls(dir, T->step[lod]));
+            pos = fma3o(dir, T->step[lod], pos);
         }
         if (!unm) {
             tbuf[i] = t;
