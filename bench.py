@@ -355,9 +355,32 @@ def autotune(gc, torch, S, specs, args):
     return best, timings
 
 
+def rank_barrier():
+    """Barrier across the replicas (torchrun ranks); a no-op for one process."""
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.barrier()
+
+
+def max_over_ranks(values, device="cpu"):
+    """Element-wise maximum of `values` over the replicas (the slowest rank's
+    time); the values themselves for one process."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
 def timed(torch, stream, fn, steps):
-    """Per-step latencies (CUDA events on the launch stream) and wall time."""
+    """Per-step latencies (CUDA events on the launch stream) and wall time,
+    bracketed by a barrier across replicas and a device synchronize."""
     lat, info = [], []
+    rank_barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for i in range(steps):
@@ -368,6 +391,7 @@ def timed(torch, stream, fn, steps):
         lat.append((a, b))
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
+    rank_barrier()
     return wall, [x.elapsed_time(y) for x, y in lat], info
 
 
@@ -415,10 +439,7 @@ def run_ours(args):
     S_e.close()
     S, wall, lat, info, launches, s0, s1 = plain_pass(False)
     clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([wall, wall_e], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        wall, wall_e = t.tolist()
+    wall, wall_e = max_over_ranks([wall, wall_e], device="cuda")  # replicas: the slowest rank's time
     rays = W * H * args.steps * world
     iters = [i for i, _ in info]
     conv = sum(1 for _, c in info if c)
