@@ -86,6 +86,7 @@ struct ViewParams {
     uint32_t level_base;                // first cache level of the view's volume
     uint32_t nlevels;                   // levels of the view's volume
     uint32_t eb;                        // bytes per voxel of the view's volume
+    uint32_t fallback;                  // sample a coarser mapped level where a brick is missing (preview)
     uint32_t skip_empty;                // step through invisible bricks without sampling (DVR, one channel)
     unsigned long long visible;         // bins the view's transfer function can make visible
     uint32_t mark_done;                 // batched passes: a finished ray leaves -1 - t in tbuf and

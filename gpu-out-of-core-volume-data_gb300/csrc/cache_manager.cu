@@ -590,6 +590,7 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
     out.tbuf = in.tbuf;
     out.state = in.state;
     out.status = in.status;
+    out.fallback = in.fallback ? 1u : 0u;
     const float bsx = in.bbox_max[0] - in.bbox_min[0];
     const float bsy = in.bbox_max[1] - in.bbox_min[1];
     const float bsz = in.bbox_max[2] - in.bbox_min[2];

@@ -229,7 +229,7 @@ __device__ __forceinline__ float sample_trilinear(const T *__restrict__ b, uint3
     return fmad(c1 - c0, wz, c0) / VoxelTraits<T>::kMax;
 }
 
-enum Status { kMapped = 0, kUnmapped = 1, kEmpty = 2, kInvisible = 3 };
+enum Status { kMapped = 0, kUnmapped = 1, kEmpty = 2, kInvisible = 3, kCoarser = 4 };
 
 // Per-thread page-walk state (K_CacheManager::_previousCoords / _previousEntries).
 struct Walk {
@@ -341,8 +341,8 @@ __device__ __forceinline__ typename SampleOf<T>::type sample_any(const uint8_t *
 // (K_CacheManager.hpp:265-361).
 template <typename T>
 __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt, uint32_t sampler, uint32_t eb,
-                                     unsigned long long visible, uint32_t lvl, V3 np, Walk &w,
-                                     typename SampleOf<T>::type &sample) {
+                                     unsigned long long visible, uint32_t lvl, uint32_t lvl_end, bool fallback,
+                                     V3 np, Walk &w, typename SampleOf<T>::type &sample) {
     const float px = np.x * lt.ior[lvl][0];
     const float py = np.y * lt.ior[lvl][1];
     const float pz = np.z * lt.ior[lvl][2];
@@ -378,6 +378,27 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
         // raise_brick_request (K_CacheManager.hpp:364-396): same coordinates
         uint32_t *r = cv.req + idx;
         if (*r != cv.ts) *r = cv.ts;
+        // Coarser-level fallback (K_CacheManager::get, K_CacheManager.hpp:163-260):
+        // the request stays on the asked level; the first mapped coarser level
+        // of the volume is sampled instead, an empty one ends the lookup.
+        for (uint32_t l2 = lvl + 1; fallback && l2 < lvl_end; ++l2) {
+            const float qx = np.x * lt.ior[l2][0], qy = np.y * lt.ior[l2][1], qz = np.z * lt.ior[l2][2];
+            const uint32_t c2x = lt.off[l2] + static_cast<uint32_t>(qx * static_cast<float>(lt.nb[l2][0]));
+            const uint32_t c2y = static_cast<uint32_t>(qy * static_cast<float>(lt.nb[l2][1]));
+            const uint32_t c2z = static_cast<uint32_t>(qz * static_cast<float>(lt.nb[l2][2]));
+            const uint4 e2 = __ldg(cv.mrpd + c2x + static_cast<uint64_t>(c2y) * cv.mx +
+                                   static_cast<uint64_t>(c2z) * cv.mx * cv.my);
+            if (e2.w == 2u) return kEmpty;
+            if (e2.w != 1u) continue;
+            const uint32_t B = cv.B;
+            const uint32_t slot = e2.x / B + (e2.y / B) * cv.sx + (e2.z / B) * cv.sx * cv.sy;
+            uint32_t *u = cv.usage + slot;
+            if (*u != cv.ts) *u = cv.ts;
+            sample = sample_any<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, eb, cv, sampler,
+                                   qx * static_cast<float>(lt.vvox[l2][0]), qy * static_cast<float>(lt.vvox[l2][1]),
+                                   qz * static_cast<float>(lt.vvox[l2][2]));
+            return kCoarser;
+        }
         return kUnmapped;
     }
     return kEmpty;
@@ -394,6 +415,7 @@ struct Ray {
     uint32_t lod;
     Walk w;
     bool unm, dvr;
+    bool coarse;  // a coarser level stood in for a missing brick (fallback mode)
 };
 
 // Eye ray, box intersection and progressive resume.  Returns false when the
@@ -444,6 +466,7 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
     r.i = i;
     r.dvr = vp.mode == GC_MODE_DVR;
     r.unm = false;
+    r.coarse = false;
     r.fc = r.dvr ? state[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     if (!hit) {
         r.fc.x = 0.f;
@@ -507,13 +530,15 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
     }
     const uint32_t lod = r.lod;
     typename SampleOf<T>::type sample{};
-    const int st = fetch<T>(cv, lt, vp.sampler, vp.eb, vp.visible, vp.level_base + lod, np, r.w, sample);
+    const int st = fetch<T>(cv, lt, vp.sampler, vp.eb, vp.visible, vp.level_base + lod, vp.level_base + vp.nlevels,
+                            vp.fallback != 0u, np, r.w, sample);
+    if (st == kCoarser) r.coarse = true;  // sampled below; the image is a preview
     if (st == kInvisible) {  // the step of a sample whose opacity stays below 0.001
         r.t += vp.step[lod];
         r.pos = fma3(r.dir, vp.step[lod], r.pos);
         return true;
     }
-    if (st != kMapped) {
+    if (st != kMapped && st != kCoarser) {
         if (st == kUnmapped) {
             vp.tbuf[r.i] = r.t;
             if (r.dvr)
@@ -619,17 +644,22 @@ __global__ void __launch_bounds__(256) render_kernel(const CacheView cv, const L
         const uint32_t ty = local / vp->tiles_x, tx = local - ty * vp->tiles_x;
         const uint32_t sh = vp->tile_shift, tw = 1u << sh;
         const uint32_t x = (tx << sh) + (lane & (tw - 1u)), y = ty * (32u >> sh) + (lane >> sh);
-        bool unm = false;
+        bool unm = false, coarse_any = false;
         if (x < vp->W && y < vp->H) {
             Ray r;
             if (ray_setup<T>(lt, vp, x, y, r)) {
                 while (ray_step<T>(cv, lt, r)) {
                 }
                 unm = ray_finish(r);
+                coarse_any = r.coarse;
             }
         }
         const uint32_t any = __ballot_sync(0xffffffffu, unm);
         if (any && lane == 0 && vp->status) atomicOr(vp->status, 1u);
+        if (vp->fallback && vp->status) {  // bit 1: a coarser level stood in (preview image)
+            const uint32_t coarse = __ballot_sync(0xffffffffu, coarse_any);
+            if (coarse && lane == 0) atomicOr(vp->status, 2u);
+        }
     }
     retire_warp(queue, nwarps);
 }
@@ -670,6 +700,7 @@ __global__ void __launch_bounds__(256) render_pixels_kernel(const CacheView cv, 
         if (active && !ray_step<T>(cv, lt, r)) {
             active = false;
             if (ray_finish(r) && r.vp->status && *r.vp->status == 0u) atomicOr(r.vp->status, 1u);
+            if (r.coarse && r.vp->status) atomicOr(r.vp->status, 2u);
         }
         if (exhausted && !__any_sync(0xffffffffu, active)) break;
     }

@@ -78,7 +78,8 @@ class View(C.Structure):
                 ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3), ("tstep", C.c_float),
                 ("focal", C.c_float), ("early_alpha", C.c_float), ("mode", C.c_uint32), ("sampler", C.c_uint32),
                 ("tf_width", C.c_uint32), ("tf", C.c_void_p), ("rgba", C.c_void_p), ("tbuf", C.c_void_p),
-                ("state", C.c_void_p), ("status", C.c_void_p), ("volume", C.c_uint32), ("tf_height", C.c_uint32)]
+                ("state", C.c_void_p), ("status", C.c_void_p), ("volume", C.c_uint32), ("tf_height", C.c_uint32),
+                ("fallback", C.c_uint32)]
 
 
 class BatchDesc(C.Structure):
@@ -411,10 +412,11 @@ class TransferFunction:
 
 def make_view(inv_view, width, height, tf_ptr, tf_width, rgba_ptr, tbuf_ptr, state_ptr, tstep=2.0 / 256.0,
               focal=2.0, early_alpha=0.95, mode=MODE_DVR, sampler=SAMPLER_REFERENCE,
-              bbox_min=(-1.0, -1.0, -1.0), bbox_max=(1.0, 1.0, 1.0), status_ptr=0, volume=0, tf_height=0):
+              bbox_min=(-1.0, -1.0, -1.0), bbox_max=(1.0, 1.0, 1.0), status_ptr=0, volume=0, tf_height=0,
+              fallback=0):
     return View((C.c_float * 12)(*inv_view), width, height, (C.c_float * 3)(*bbox_min), (C.c_float * 3)(*bbox_max),
                 tstep, focal, early_alpha, mode, sampler, tf_width, vp(tf_ptr), vp(rgba_ptr), vp(tbuf_ptr),
-                vp(state_ptr), vp(status_ptr or None), volume, tf_height)
+                vp(state_ptr), vp(status_ptr or None), volume, tf_height, fallback)
 
 
 def render_empty_skip(enable):

@@ -365,6 +365,14 @@ typedef struct gc_view {
                                  channel 1 across rows, read bilinearly; MIP
                                  classifies the maximum of channel 0 with row 0.
                                  0 or 1 for one-channel volumes                 */
+    uint32_t fallback;        /* 0: the reference's ray caster (a ray stops at a
+                                 missing brick).  1: preview mode of
+                                 K_CacheManager::get (K_CacheManager.hpp:163-260):
+                                 the missing brick is requested and the first
+                                 mapped coarser level is sampled instead; status
+                                 bit 1 is then set.  Such an image is a preview,
+                                 not the converged image: restart the view's
+                                 progressive buffers every frame.               */
 } gc_view;
 
 /* Camera of updateViewMatrix (Display_helper.cpp:93-118): the rows of

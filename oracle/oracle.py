@@ -48,7 +48,8 @@ class View(C.Structure):
                 ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3), ("tstep", C.c_float),
                 ("focal", C.c_float), ("early_alpha", C.c_float), ("mode", C.c_uint32), ("sampler", C.c_uint32),
                 ("tf_width", C.c_uint32), ("tf", C.c_void_p), ("rgba", C.c_void_p), ("tbuf", C.c_void_p),
-                ("state", C.c_void_p), ("status", C.c_void_p), ("volume", C.c_uint32), ("tf_height", C.c_uint32)]
+                ("state", C.c_void_p), ("status", C.c_void_p), ("volume", C.c_uint32), ("tf_height", C.c_uint32),
+                ("fallback", C.c_uint32)]
 
 
 LRU_DTYPE = np.dtype([("cx", "<u4"), ("cy", "<u4"), ("cz", "<u4"), ("level", "<u4"), ("vx", "<f4"),

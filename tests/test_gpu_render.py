@@ -288,3 +288,46 @@ def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, park, sync, r
         assert st.parked > 0
     b.close()
     assert s2.cm.stats().device_error == 0
+
+
+def test_coarser_level_fallback_preview(gc, orc, torch_cuda):
+    """Preview mode of K_CacheManager::get: where a brick is missing a ray
+    samples the first mapped coarser level instead of stopping.  With every
+    brick resident it gives the normal image bit for bit; with only the
+    coarse levels resident it covers more of the image than the first frame
+    of the normal method and says so in status bit 1."""
+    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 216)
+    tf_dev = torch_cuda.from_numpy(scenario.ramp_tf().reshape(-1)).cuda()
+    st = torch_cuda.zeros(1, dtype=torch_cuda.int32, device="cuda")
+    W, H = 80, 64
+
+    def frame(m, fallback):
+        g, _ = s.buffers(W, H)
+        v = s.view(m, W, H, tf_dev, 256, g, fallback=fallback)
+        v.status = st.data_ptr()
+        st.zero_()
+        s.cm.render(v)
+        torch_cuda.cuda.synchronize()
+        return g[0].cpu().numpy(), int(st.item())
+
+    # a far view pages in the coarse levels only
+    far = scenario.orbit_camera(gc, 2, 12, 9.0)
+    for _ in range(12):
+        _, stf = frame(far, 0)
+        if s.cm.update() and stf == 0:
+            break
+    near = scenario.orbit_camera(gc, 2, 12, 2.2)
+    img0, st0 = frame(near, 0)
+    img1, st1 = frame(near, 1)
+    assert st0 & 1 and st1 & 2  # normal rays stopped at missing bricks; the preview used coarse levels
+    cover0, cover1 = ((img0 >> 24) > 0).mean(), ((img1 >> 24) > 0).mean()
+    assert cover1 > cover0, (cover0, cover1)
+    # converge the near view, then the preview equals the normal image
+    for _ in range(30):
+        _, stn = frame(near, 0)
+        if s.cm.update() and stn == 0:
+            break
+    ref, stn = frame(near, 0)
+    img2, st2 = frame(near, 1)
+    assert stn == 0 and st2 == 0
+    assert np.array_equal(ref, img2)
