@@ -238,6 +238,7 @@ def measured_peak():
 
 
 PIN_STORES = False  # --pin-stores: brick stores in page-locked host memory
+LAST_PREPROCESS = {}  # stage timings of the last make_store (device mip, bricking, store copy)
 
 
 def make_store(gc, torch, cfg):
@@ -258,7 +259,10 @@ def make_store(gc, torch, cfg):
                                              channel=ch, field=1), dev.data_ptr())
     torch.cuda.synchronize()
     t1 = time.time()
-    store, offs, _ = gc.pre_process(vol, layout, dev, pin=PIN_STORES)
+    tm = {}
+    store, offs, _ = gc.pre_process(vol, layout, dev, pin=PIN_STORES, timings=tm)
+    LAST_PREPROCESS.clear()
+    LAST_PREPROCESS.update(tm)
     del dev
     torch.cuda.empty_cache()
     t2 = time.time()
@@ -450,6 +454,7 @@ def run_ours(args):
     last = spec(cfg.get("roofline_frame", 42))
     S.converge(last, cap=cfg.get("cap", 64))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > L2 (126 MB)
+    samples0 = S.cm.stats().samples
     ev = []
     torch.cuda.nvtx.range_push("roofline")
     for _ in range(5):
@@ -467,6 +472,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     touched = S.cm.stats().last_used
+    samples = (S.cm.stats().samples - samples0) / len(ev)
     render_ms = statistics.median([a.elapsed_time(b) for a, b in ev])
     # the same launch with empty-space skipping off (identical image), for the record
     gc.render_empty_skip(False)
@@ -505,6 +511,14 @@ def run_ours(args):
                                                 if args.config == "c5" else
                                                 "in-core volume; L2 not flushed (the c1 case is for profiling)"),
                    "preprocess_s": round(prep_s, 2)},
+        "preprocess": {"mip_build_s": round(LAST_PREPROCESS.get("mip_s", 0.0), 4),
+                       "mip_build_gbs": round((2 * LAST_PREPROCESS.get("pyramid_bytes", 0) - LAST_PREPROCESS.get(
+                           "level0_bytes", 0)) / max(LAST_PREPROCESS.get("mip_s", 1e-9), 1e-9) / 1e9, 1),
+                       "bricking_s": round(LAST_PREPROCESS.get("brick_s", 0.0), 4),
+                       "store_copy_s": round(LAST_PREPROCESS.get("copy_s", 0.0), 4),
+                       "note": "device mip pyramid (every level read once, every coarser level written: "
+                               "2 x pyramid - level 0 bytes, over the mip time), device bricking, copy of the "
+                               "brick store to host memory"},
         "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
         "iterations_per_view": {"mean": round(statistics.mean(iters), 2), "max": max(iters)},
         "converged_views": f"{conv}/{args.steps}",
@@ -516,7 +530,9 @@ def run_ours(args):
                      "kernel": "render_pixels_kernel" if gc.render_tuning()[0] == 1 else "render_kernel",
                      "peak_kind": peak_kind, "algorithmic_bytes_per_launch": int(algo),
                      "launch_ms": round(render_ms, 4), "launch_ms_without_empty_skip": round(render_ms_noskip, 4),
-                     "touched_bricks": int(touched),
+                     "touched_bricks": int(touched), "samples_per_launch": int(samples),
+                     "gather_bytes_per_launch": int(samples * (8 * vol.encoded_bytes + 16)),
+                     "gather_gbs": round(samples * (8 * vol.encoded_bytes + 16) / (render_ms / 1e3) / 1e9, 1),
                      "note": f"view {cfg.get('roofline_frame', 42)} of the {args.config} path, converged, "
                              f"re-rendered after an L2 flush; compulsory bytes = touched bricks x B^3 x "
                              f"{vol.encoded_bytes} B + {PIXEL_BYTES} B/pixel"},
@@ -800,6 +816,10 @@ def run_batched(gc, torch, args):
             "ratio": round(batched["value"] / plain["value"], 3)}
 
 
+def vol_bytes_per_voxel(cfg):
+    return cfg["bpc"] * cfg.get("channels", 1)
+
+
 def cpu_baseline(gc, S, cfg, spec, args):
     """The oracle's FP32 ray-march (all host threads) on a bounded sample of
     converged c2 views, reading a snapshot of the GPU's cache state."""
@@ -826,7 +846,19 @@ def cpu_baseline(gc, S, cfg, spec, args):
         if el > args.cpu_seconds:
             break
     oc.close()
+    # the CPU restatement of the mip reduction (down_sampling_inner) on a bounded
+    # 512 x 512 x 64 sample of the same voxel type, single thread
+    nc = cfg.get("channels", 1)
+    sample = np.random.default_rng(1).integers(0, 255, size=512 * 512 * 64 * vol_bytes_per_voxel(cfg),
+                                               dtype=np.uint8)
+    t1 = time.perf_counter()
+    reps = 0
+    while time.perf_counter() - t1 < 2.0:
+        orc.mip_level(sample, (512, 512, 64), vol_bytes_per_voxel(cfg), nc)
+        reps += 1
+    mip_cpu = reps * sample.nbytes * 1.125 / (time.perf_counter() - t1) / 1e9
     return {"value": round(W * H * frames / el / 1e6, 4), "unit": "Mrays/s", "cores": os.cpu_count(),
+            "mip_cpu_gbs_1thread": round(mip_cpu, 2),
             "kind": "port", "sample": f"{frames} renders of one converged {W}x{H} {args.config} view from the GPU's cache "
                                       f"snapshot (oracle FP32 ray-march, {os.cpu_count()} threads)"}
 

@@ -50,6 +50,7 @@ struct CacheView {
     uint32_t nc;          // channels per voxel (1, or 2 for two 8-bit channels)
     uint64_t slot_bytes;  // pool slot stride: B^3 x the widest voxel
     const unsigned long long *slot_bins;  // per slot: value bins its voxels cover (empty-space skipping)
+    unsigned long long *samples;          // running count of samples taken (resident-brick reads)
     uint32_t ts;
 };
 

@@ -113,6 +113,7 @@ struct gc_cache {
     uint32_t *req = nullptr, *usage = nullptr, *order[2] = {nullptr, nullptr}, *slot_level = nullptr;
     float4 *slot_vpos = nullptr;
     unsigned long long *slot_bins = nullptr;  // value bins of each slot's brick (empty-space skipping)
+    unsigned long long *d_samples = nullptr;  // samples taken by the ray caster since creation
     uint8_t *pool = nullptr;
     uint64_t *status_lru = nullptr, *status_miss = nullptr;
     gc::ScanCtl *ctl_lru = nullptr, *ctl_miss = nullptr;
@@ -425,6 +426,7 @@ static CacheView cache_view(const gc_cache *C) {
     cv.nc = C->nc;
     cv.slot_bytes = C->slot_bytes;
     cv.slot_bins = C->slot_bins;
+    cv.samples = C->d_samples;
     cv.ts = C->ts;
     return cv;
 }
@@ -535,7 +537,7 @@ static void destroy(gc_cache *C) {
     }
     cudaSetDevice(C->device);
     cudaDeviceSynchronize();
-    void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool, C->slot_bins,
+    void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool, C->slot_bins, C->d_samples,
                    C->status_lru, C->status_miss, C->ctl_lru, C->ctl_miss, C->d_count, C->d_misc, C->d_queue,
                    C->d_list, C->d_asked, C->d_big_coord, C->d_big_index, C->d_src, C->d_staging, C->d_views};
     for (void *p : dev)
@@ -748,6 +750,8 @@ int gc_cache_create_shared(const gc_cache_desc *desc, const gc_volume_desc *volu
         C->slot_vpos = dalloc<float4>(C->nslots, "slot positions");
         C->pool = dalloc<uint8_t>(C->nslots * C->slot_bytes, "brick pool");
         C->slot_bins = dalloc<unsigned long long>(C->nslots, "slot value bins");
+        C->d_samples = dalloc<unsigned long long>(1, "sample counter");
+        GC_CUDA(cudaMemset(C->d_samples, 0, sizeof(unsigned long long)));
         GC_CUDA(cudaMemset(C->slot_bins, 0xff, C->nslots * sizeof(unsigned long long)));
         C->status_lru = dalloc<uint64_t>(lookback_tiles(C->nslots), "scan status");
         C->status_miss = dalloc<uint64_t>(lookback_tiles(C->nentries), "scan status");
@@ -968,9 +972,12 @@ int gc_cache_stats_get(gc_cache_t C, gc_cache_stats *out) {
         std::lock_guard<std::mutex> g(C->mu);
         uint32_t used = 0;
         GC_CUDA(cudaMemcpy(&used, C->d_count, sizeof(used), cudaMemcpyDeviceToHost));
+        unsigned long long samples = 0;
+        GC_CUDA(cudaMemcpy(&samples, C->d_samples, sizeof(samples), cudaMemcpyDeviceToHost));
         *out = C->stats;
         out->device_error = a.err | b.err;
         out->upload_direct = C->gather ? 1u : 0u;
+        out->samples = samples;
         out->last_used = used;
     });
 }

@@ -416,6 +416,7 @@ struct Ray {
     Walk w;
     bool unm, dvr;
     bool coarse;  // a coarser level stood in for a missing brick (fallback mode)
+    uint32_t nsamp;  // samples taken (voxel reads of a resident brick)
 };
 
 // Eye ray, box intersection and progressive resume.  Returns false when the
@@ -467,6 +468,7 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
     r.dvr = vp.mode == GC_MODE_DVR;
     r.unm = false;
     r.coarse = false;
+    r.nsamp = 0;
     r.fc = r.dvr ? state[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     if (!hit) {
         r.fc.x = 0.f;
@@ -533,6 +535,7 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
     const int st = fetch<T>(cv, lt, vp.sampler, vp.eb, vp.visible, vp.level_base + lod, vp.level_base + vp.nlevels,
                             vp.fallback != 0u, np, r.w, sample);
     if (st == kCoarser) r.coarse = true;  // sampled below; the image is a preview
+    if (st == kMapped || st == kCoarser) ++r.nsamp;
     if (st == kInvisible) {  // the step of a sample whose opacity stays below 0.001
         r.t += vp.step[lod];
         r.pos = fma3(r.dir, vp.step[lod], r.pos);
@@ -645,6 +648,7 @@ __global__ void __launch_bounds__(256) render_kernel(const CacheView cv, const L
         const uint32_t sh = vp->tile_shift, tw = 1u << sh;
         const uint32_t x = (tx << sh) + (lane & (tw - 1u)), y = ty * (32u >> sh) + (lane >> sh);
         bool unm = false, coarse_any = false;
+        uint32_t nsamp = 0;
         if (x < vp->W && y < vp->H) {
             Ray r;
             if (ray_setup<T>(lt, vp, x, y, r)) {
@@ -652,8 +656,11 @@ __global__ void __launch_bounds__(256) render_kernel(const CacheView cv, const L
                 }
                 unm = ray_finish(r);
                 coarse_any = r.coarse;
+                nsamp = r.nsamp;
             }
         }
+        const uint32_t tile_samples = __reduce_add_sync(0xffffffffu, nsamp);
+        if (lane == 0 && tile_samples) atomicAdd(cv.samples, static_cast<unsigned long long>(tile_samples));
         const uint32_t any = __ballot_sync(0xffffffffu, unm);
         if (any && lane == 0 && vp->status) atomicOr(vp->status, 1u);
         if (vp->fallback && vp->status) {  // bit 1: a coarser level stood in (preview image)
@@ -701,6 +708,7 @@ __global__ void __launch_bounds__(256) render_pixels_kernel(const CacheView cv, 
             active = false;
             if (ray_finish(r) && r.vp->status && *r.vp->status == 0u) atomicOr(r.vp->status, 1u);
             if (r.coarse && r.vp->status) atomicOr(r.vp->status, 2u);
+            if (r.nsamp) atomicAdd(cv.samples, static_cast<unsigned long long>(r.nsamp));
         }
         if (exhausted && !__any_sync(0xffffffffu, active)) break;
     }

@@ -70,7 +70,7 @@ class CacheStats(C.Structure):
                 ("bricks_installed", C.c_uint64), ("bricks_empty", C.c_uint64), ("bytes_h2d", C.c_uint64),
                 ("load_errors", C.c_uint64), ("last_requests", C.c_uint32), ("last_used", C.c_uint32),
                 ("device_error", C.c_uint32), ("load_cycles", C.c_uint64), ("loader_host_ns", C.c_uint64),
-                ("upload_ns", C.c_uint64), ("upload_direct", C.c_uint32)]
+                ("upload_ns", C.c_uint64), ("upload_direct", C.c_uint32), ("samples", C.c_uint64)]
 
 
 class View(C.Structure):
@@ -328,7 +328,7 @@ def brick_store_offsets(layout, vol):
     return offs, off, big
 
 
-def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host", pin=False):
+def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host", pin=False, timings=None):
     """Application::pre_process (Applications/DVR-ray-caster/src/Application.cu:148-197)
     run on the device: mip pyramid, bricking of every level and empty flags.
 
@@ -337,8 +337,11 @@ def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host
     one uint8 tensor (host memory unless store == "device"; pinned when pin),
     their per-level byte offsets, and the gc_brick_key of every big brick whose
     values are all below empty_threshold (none when it is None, like the
-    reference's default threshold 0).
+    reference's default threshold 0).  timings (a dict) receives the seconds
+    of the device mip build, the device bricking and the store copy.
     """
+    import time
+
     import torch
 
     eb, nc = vol.encoded_bytes, vol.channels
@@ -350,7 +353,11 @@ def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host
     pyr = torch.empty(total, dtype=torch.uint8, device=dev)
     n0 = level0.numel() * level0.element_size()
     pyr[:n0].copy_(level0.reshape(-1).view(torch.uint8))
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
     Mipmapper.process(pyr.data_ptr(), layout, offs, eb, nc, stream)
+    torch.cuda.synchronize(dev)
+    t1 = time.perf_counter()
     soffs, stotal, big = brick_store_offsets(layout, vol)
     bricks = torch.empty(stotal, dtype=torch.uint8, device=dev)
     for l in range(layout.nb_levels):
@@ -368,11 +375,16 @@ def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host
                 x, y, z = i % nb[0], (i // nb[0]) % nb[1], i // (nb[0] * nb[1])
                 empty_keys.append(brick_key(l, x, y, z))
     torch.cuda.synchronize(dev)
+    t2 = time.perf_counter()
+    if timings is not None:
+        timings.update(mip_s=t1 - t0, brick_s=t2 - t1, level0_bytes=n0, pyramid_bytes=total, store_bytes=stotal)
     del pyr
     if store == "device":
         return bricks, soffs, empty_keys
     host = torch.empty(stotal, dtype=torch.uint8, pin_memory=pin)
     host.copy_(bricks)
+    if timings is not None:
+        timings["copy_s"] = time.perf_counter() - t2
     del bricks
     return host, soffs, empty_keys
 

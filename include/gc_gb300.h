@@ -290,6 +290,8 @@ typedef struct gc_cache_stats {
     uint64_t upload_ns;           /* device time of the side-stream H2D copies */
     uint32_t upload_direct;       /* 1: host-store bricks are gathered by a kernel
                                      reading the store; 0: staged copies         */
+    uint64_t samples;             /* ray-caster samples taken (each reads 8 voxels
+                                     and a page-directory entry)                 */
 } gc_cache_stats;
 int gc_cache_stats_get(gc_cache_t cache, gc_cache_stats *out);
 
