@@ -342,8 +342,9 @@ class Session:
         self.cm.close()
 
 
-def autotune(gc, torch, S, specs, args):
-    """Autotunes the ray caster's launch configuration on converged views."""
+def autotune(gc, torch, S, specs, args, per_view=False):
+    """Autotunes the ray caster's launch configuration on converged views
+    (per_view: one launch per view, as the plain path renders)."""
     S.converge(specs, cap=S.cfg.get("cap", 64))
     views, bufs = S.views(specs)
 
@@ -353,7 +354,7 @@ def autotune(gc, torch, S, specs, args):
             b[2].zero_()
 
     with torch.cuda.stream(S.stream):
-        best, timings = gc.autotune_render(S.cm, views, clear, stream=S.sp, repeats=3)
+        best, timings = gc.autotune_render(S.cm, views, clear, stream=S.sp, repeats=3, per_view=per_view)
     log(f"autotune: best {best} of {len(timings)} ({min(timings.values()):.3f} ms vs default "
         f"{timings.get(str((1, 8, 128, 0)), float('nan')):.3f} ms)")
     return best, timings
@@ -425,8 +426,6 @@ def run_ours(args):
         S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
         for f in range(args.warmup):
             S.converge(spec(f), cap=cfg.get("cap", 64))
-        if not tuned:
-            tuned.append(autotune(gc, torch, S, spec(args.warmup - 1), args))
         s0, l0 = S.cm.stats(), gc.kernel_launches()
         torch.cuda.nvtx.range_push("timed_e2e" if e2e else "timed")
         wall, lat, info = timed(torch, S.stream, lambda i: S.converge(spec(args.warmup + i), e2e=e2e,
@@ -436,7 +435,12 @@ def run_ours(args):
         s1 = S.cm.stats()
         return S, wall, lat, info, launches, s0, s1
 
-    tuned = []
+    # launch configuration: autotuned once, on three views spread along the
+    # path (near, middle, far), in a cache of its own
+    T = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
+    n = cfg.get("frames", 120)
+    tuned = [autotune(gc, torch, T, [spec(f)[0] for f in (2, n // 6, n // 3)], args, per_view=True)]
+    T.close()
     clocks = ClockSampler()
     clocks.start()
     S_e, wall_e, lat_e, _, _, s0_e, s1_e = plain_pass(True)

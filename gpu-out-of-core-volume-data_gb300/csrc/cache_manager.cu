@@ -585,7 +585,7 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
     out.tfw = in.tf_width;
     out.tfh = in.tf_height > 0 ? in.tf_height : 1;
     // empty-space skipping: DVR of one channel through a 1D transfer function
-    out.skip_empty = render_tuning().skip_empty && in.mode == GC_MODE_DVR && V.desc.channels == 1 ? 1u : 0u;
+    out.skip_empty = in.mode == GC_MODE_DVR && V.desc.channels == 1 ? render_tuning().skip_empty : 0u;
     out.visible = ~0ull;  // filled from the transfer function on the device (view_bins_kernel)
     out.tf = in.tf;
     out.rgba = in.rgba;

@@ -638,13 +638,16 @@ AUTOTUNE_CANDIDATES = [(sched, tw, th, bps) for sched in (1, 0) for tw in (8, 4,
                        for bps in (0, 4)]
 
 
-def autotune_render(cache, views, clear, stream=0, candidates=None, repeats=3, cache_file=None, key=None):
+def autotune_render(cache, views, clear, stream=0, candidates=None, repeats=3, cache_file=None, key=None,
+                    per_view=False):
     """Chooses the ray caster's launch configuration (scheduler, ray-tile
     shape, threads per block, blocks per SM) by timing `views` (a list of View
     whose bricks are resident) under each candidate, applies the fastest and
-    returns (best, timings).  `clear()` restarts the views' progressive buffers
-    before each timed render.  With cache_file and key, a previous choice for
-    the same key is reused without timing.  Images do not depend on the choice."""
+    returns (best, timings).  The views render in one launch (the batched
+    form), or with per_view one launch each, timed in sum (the plain per-view
+    path).  `clear()` restarts the views' progressive buffers before each timed
+    render.  With cache_file and key, a previous choice for the same key is
+    reused without timing.  Images do not depend on the choice."""
     import json
     import torch
 
@@ -668,7 +671,11 @@ def autotune_render(cache, views, clear, stream=0, candidates=None, repeats=3, c
             clear()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(s)
-            check(lib.gc_render_batch(cache.handle, arr, len(views), vp(stream)))
+            if per_view:
+                for i in range(len(views)):
+                    check(lib.gc_render(cache.handle, C.byref(arr[i]), vp(stream)))
+            else:
+                check(lib.gc_render_batch(cache.handle, arr, len(views), vp(stream)))
             b.record(s)
             b.synchronize()
             if r:

@@ -106,6 +106,6 @@ def test_empty_space_skipping_changes_nothing(gc, orc, torch_cuda, tf_kind, samp
             s.cm.close()
     finally:
         gc.render_empty_skip(True)
-    for f, (a, b) in enumerate(zip(*runs)):
+    for f, frames in enumerate(zip(*runs)):
         for k in range(4):
-            assert np.array_equal(a[k], b[k]), (f, k)
+            assert all(np.array_equal(frames[0][k], other[k]) for other in frames[1:]), (f, k)
