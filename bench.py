@@ -85,6 +85,7 @@ CONFIGS = {
 }
 DIAG = 2.0 * math.sqrt(3.0)
 PIXEL_BYTES = 44  # RGBA 4 + t 4+4 + colour state 16+16 per pixel and launch
+OUR_DEFAULT_STEPS = 40  # views the GPU arm times by default (the reference arm samples that range)
 # DRAM bytes (read + write) of the c2 roofline launch (view 42, converged, after
 # an L2 flush), from one ncu capture of this command:
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none --nvtx
@@ -887,32 +888,38 @@ def run_reference(args):
     st_np = store.numpy()
     oc.set_source(st_np, offs)
     W, H = cfg["W"], cfg["H"]
-    tf = tf_table(cfg["tf"])
+    tf = tf2d_table() if cfg["tf"] == "2d" else tf_table(cfg["tf"])
+    tfh, tfw = (tf.shape[0], tf.shape[1]) if tf.ndim == 3 else (0, tf.shape[0])
+    tf = tf.reshape(-1)
     focal = 1.0 / math.tan(math.radians(cfg["fov"]) / 2)
     rgba = np.zeros(W * H, np.uint32)
     tb = np.zeros(W * H, np.float32)
     st = np.zeros(W * H * 4, np.float32)
 
     def view_to_convergence(f):
-        v = gc.make_view(path_camera(gc, cfg, f), W, H, 0, 256, 0, 0, 0, tstep=2.0 / 256.0, focal=focal,
-                         early_alpha=cfg["early"])
+        v = gc.make_view(path_camera(gc, cfg, f), W, H, 0, tfw, 0, 0, 0, tstep=2.0 / 256.0, focal=focal,
+                         early_alpha=cfg["early"], tf_height=tfh)
         tb[:] = 0
         st[:] = 0
-        for it in range(64):
+        for it in range(cfg.get("cap", 64)):
             oc.render(v, tf, rgba, tb, st)
             if oc.update():
                 return it + 1
 
+    # A bounded sample of the views our arm times (views warmup .. warmup + 39
+    # of the path by default): `steps` views spread evenly over that range.
+    span = OUR_DEFAULT_STEPS
+    picks = sorted({args.warmup + round(i * (span - 1) / max(1, args.steps - 1)) for i in range(args.steps)})
     for f in range(args.warmup):
         view_to_convergence(f)
     lat = []
     t0 = time.perf_counter()
-    for i in range(args.steps):
+    for f in picks:
         a = time.perf_counter()
-        view_to_convergence(args.warmup + i)
+        view_to_convergence(f)
         lat.append(1e3 * (time.perf_counter() - a))
     el = time.perf_counter() - t0
-    value = W * H * args.steps / el / 1e6
+    value = W * H * len(picks) / el / 1e6
     out = {"impl": "reference", "metric": "Mrays/s", "value": round(value, 4), "unit": "Mrays/s", "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * el / args.steps, 3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": workload(args.config, cfg)[1],
@@ -921,7 +928,8 @@ def run_reference(args):
                       "view": [W, H], "max_requests": args.max_requests, "pool_slots": list(pool)},
            "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
-                            "sample": f"{args.steps} views after {args.warmup} warm-up views: oracle FP32 "
+                            "sample": f"views {picks} of the path (spread over the views the GPU arm times) "
+                                      f"after {args.warmup} warm-up views, each to convergence: oracle FP32 "
                                       f"ray-march + cache update, {os.cpu_count()} threads"},
            "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
