@@ -16,8 +16,25 @@
  *   orc_render        RayCasters.cu:35-349, 484-567; K_CacheManager.hpp:265-396;
  *                     K_CacheDevice.hpp:188-336; K_MultiResolutionPageDirectory.hpp:141-180;
  *                     VolumeRayCaster.cu:136-161
+ *   orc_render (two channels, 2D transfer function)   no reference counterpart
+ *
+ * Pinning (how the restatement is tied to the reference):
+ *   orc_layout, orc_brick_level   PINNED: checked against outputs of the
+ *       reference's own init_meta_data / process_bricking compiled from its
+ *       sources (tests/golden/layout.json, bricker.json; oracle/build.py).
+ *   bricks.xml format             PINNED: goldens written by the reference's
+ *       MetaData::write_bricks_xml (tests/golden/bricks_xml/).
+ *   orc_mip_level, orc_empty, orc_cache_*, orc_render   PARITY UNPINNED by
+ *       reference execution: the reference implements them only as CUDA kernels
+ *       (and its sources do not exist where the GPU runs), so they are literal
+ *       restatements of the cited code, checked by closed-form properties and
+ *       against the FP64 restatement (orc_render_f64), not against the
+ *       reference's own outputs.  Two-channel rendering has no reference at all.
+ *
  * Build with -ffp-contract=off: every float operation is rounded separately,
- * in source order, like the CUDA kernels built with -fmad=false.
+ * in source order, like the CUDA kernels built with -fmad=false; the fused
+ * multiply-adds of the CUDA ray caster are written here as fmaf at the same
+ * places.
  */
 #include "gc_oracle.h"
 
