@@ -331,3 +331,38 @@ def test_coarser_level_fallback_preview(gc, orc, torch_cuda):
     img2, st2 = frame(near, 1)
     assert stn == 0 and st2 == 0
     assert np.array_equal(ref, img2)
+
+
+@pytest.mark.parametrize("case", ["inside", "one_pixel", "one_row", "miss", "bbox"])
+def test_edge_views_match_oracle(gc, orc, torch_cuda, case):
+    """Views at the edges of the method, frame by frame against the FP32
+    oracle with the cache state: a camera inside the volume (rays start at
+    t = 0), a 1x1 and a 97x1 image, a view that misses the volume (every pixel
+    written as background), and a non-unit bounding box."""
+    s = Scene(gc, orc, torch_cuda, (64, 48, 56), 1, 16, 1, (1, 1, 1), (6, 6, 6), 120)
+    tf = scenario.ramp_tf()
+    tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
+    W, H = {"one_pixel": (1, 1), "one_row": (97, 1)}.get(case, (45, 37))
+    kw = {}
+    if case == "inside":
+        m = gc.look_at((0.2, 0.1, 0.3), (-0.5, 0.0, -0.6))
+    elif case == "miss":
+        m = gc.look_at((0.0, 0.0, 6.0), (0.0, 0.0, 12.0))  # looking away from the volume
+    else:
+        m = scenario.orbit_camera(gc, 1, 12, 2.8)
+    if case == "bbox":
+        kw = dict(bbox_min=(-1.2, -0.8, -1.0), bbox_max=(0.9, 1.1, 0.7))
+    g, o = s.buffers(W, H)
+    for f in range(8):
+        v = s.view(m, W, H, tf_dev, 256, g, **kw)
+        s.cm.render(v)
+        s.oc.render(v, tf, *o)
+        torch_cuda.cuda.synchronize()
+        assert rgba_diff(g[0].cpu().numpy(), o[0]).max() <= RGBA_TOL_FP32, (case, f)
+        assert np.array_equal(g[1].cpu().numpy(), o[1]) and np.array_equal(g[2].cpu().numpy(), o[2]), (case, f)
+        assert s.cm.update() == s.oc.update(), (case, f)
+        s.compare_cache(f"{case} frame {f}")
+    if case == "miss":
+        assert not (g[0].cpu().numpy() >> 24).any()
+    if case == "inside":  # rays start inside the volume and advance through it
+        assert (g[1].cpu().numpy() > 0).mean() > 0.5
