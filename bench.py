@@ -660,9 +660,9 @@ def run_c3(args):
     data = (vol, layout, store, offs)
     views, warm = c3_views(gc, cfg, args.batches)
     rays = sum(W * H for _, W, H in views)
-    S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
-    best, _ = autotune(gc, torch, S, warm[:4], args)
-    S.close()
+    tune_b, tune_p = c3_tunings(gc, torch, cfg, data, warm, args)
+    best = tune_b
+    gc.render_tuning(*tune_b)
     batched, wall = batched_pass(gc, torch, cfg, data, views, warm, args)
     out = {"metric": "Mrays/s", "value": batched["value"], "unit": "Mrays/s", "n_gpus": 1, "steps": len(views),
            "warmup": len(warm), "ms_per_step": round(1e3 * wall / len(views), 4), "higher_is_better": True,
@@ -674,6 +674,7 @@ def run_c3(args):
                       "preprocess_s": round(prep_s, 2)},
            "batched": batched}
     if not args.no_plain:
+        gc.render_tuning(*tune_p)
         plain, _ = plain_views_pass(gc, torch, cfg, data, views, warm, args)
         out["plain_same_views"] = plain
         out["ratio"] = round(batched["value"] / plain["value"], 3)
@@ -799,6 +800,18 @@ def c4_serve(gc, torch, cfg, vols, stores, args):
     return out
 
 
+def c3_tunings(gc, torch, cfg, data, warm, args):
+    """Launch tunings of the two c3 arms, each for its own launch shape, on
+    the warm-up views in a cache of their own: the batched arm on one launch
+    of 8 views, the plain arm on one launch per view (4 views)."""
+    vol, layout, store, offs = data
+    T = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
+    tune_b, _ = autotune(gc, torch, T, warm[:8], args)
+    tune_p, _ = autotune(gc, torch, T, warm[:4], args, per_view=True)
+    T.close()
+    return tune_b, tune_p
+
+
 def run_batched(gc, torch, args):
     """c3: the same views rendered batched (continuous batching, all views
     that can progress in one persistent launch per tick) and plain (one view
@@ -808,8 +821,12 @@ def run_batched(gc, torch, args):
     data = (vol, layout, store, offs)
     views, warm = c3_views(gc, cfg, args.batches)
     rays = sum(W * H for _, W, H in views)
+    tune_b, tune_p = c3_tunings(gc, torch, cfg, data, warm, args)
+    gc.render_tuning(*tune_b)
     batched, _ = batched_pass(gc, torch, cfg, data, views, warm, args)
+    gc.render_tuning(*tune_p)
     plain, _ = plain_views_pass(gc, torch, cfg, data, views, warm, args)
+    batched["render_tuning"], plain["render_tuning"] = list(tune_b), list(tune_p)
     return {"config": {"workload": f"c3: {len(views)} views ({args.batches} x {cfg['batch']}), sizes "
                                    f"{list(cfg['sizes'])}, cameras at 0.5-3.0x diagonal; BrickSize 32, 4 GiB pool; "
                                    f"all submitted at t0, continuous batching with a {args.batch_pixels} pixel "
@@ -952,7 +969,7 @@ def main():
     ap.add_argument("--batches", type=int, default=3)
     ap.add_argument("--batch-cap", type=int, default=256)
     ap.add_argument("--batch-pixels", type=int, default=16 << 20)
-    ap.add_argument("--occupancy", type=float, default=0.6)
+    ap.add_argument("--occupancy", type=float, default=0.45)
     ap.add_argument("--admit", type=int, default=4)
     ap.add_argument("--upload", choices=["auto", "staged"], default="auto",
                     help="brick upload route: auto = gather kernel reading the host store where the device can, "
