@@ -579,7 +579,7 @@ def batched_pass(gc, torch, cfg, data, views, warm, args):
     S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests, sync=False)
     B = gc.Batch(S.cm, max_views=cfg["batch"], max_pixels=args.batch_pixels, max_passes=args.batch_cap,
                  max_occupancy=args.occupancy, max_admit=args.admit, park_above=args.park,
-                 reorder_window=args.reorder)
+                 reorder_window=args.reorder, overlap_loads=args.overlap)
 
     def run_all(vs, base):
         for i, (m, W, H) in enumerate(vs):
@@ -670,7 +670,8 @@ def run_c3(args):
            "data": "synthetic (seeded blobs + value noise, 2048^3 u16; no public dataset)",
            "config": {"workload": f"c3: {len(views)} views, batched (continuous batching), each to convergence",
                       "rays": int(rays), "reorder": args.reorder, "occupancy": args.occupancy,
-                      "admit": args.admit, "park_above": args.park, "render_tuning": list(best),
+                      "admit": args.admit, "park_above": args.park, "overlap_loads": bool(args.overlap),
+                      "render_tuning": list(best),
                       "preprocess_s": round(prep_s, 2)},
            "batched": batched}
     if not args.no_plain:
@@ -742,7 +743,7 @@ def c4_serve(gc, torch, cfg, vols, stores, args):
     sp = stream.cuda_stream
     B = gc.Batch(cm, max_views=cfg["batch"], max_pixels=args.batch_pixels, max_passes=args.batch_cap,
                  max_occupancy=args.occupancy, max_admit=args.admit, reorder_window=args.reorder,
-                 park_above=args.park)
+                 park_above=args.park, overlap_loads=args.overlap)
     bufs, lat, passes, conv, rays_done = {}, [], [], 0, 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -785,6 +786,7 @@ def c4_serve(gc, torch, cfg, vols, stores, args):
                                   f"({cm.info.pool_bytes / 2**30:.1f} GiB), sizes {list(cfg['sizes'])}, 4 TFs",
                       "offered_mrays_per_s": round(rays / args.duration / 1e6, 2), "reorder": args.reorder,
                       "occupancy": args.occupancy, "admit": args.admit, "park_above": args.park,
+                      "overlap_loads": bool(args.overlap),
                       "upload": "staged" if args.upload == "staged" else "gather",
                       "stores": "pinned" if PIN_STORES else "pageable",
                       "max_passes": args.batch_cap},
@@ -981,6 +983,9 @@ def main():
                          "through the device's own mappings)")
     ap.add_argument("--park", type=float, default=0.0,
                     help="batched/serving: park the newest view while demand exceeds this fraction of the pool")
+    ap.add_argument("--no-overlap", dest="overlap", action="store_false",
+                    help="batched/serving: one brick load at a time (default: loads overlap rendering through "
+                         "two miss lists with in-flight marks)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")

@@ -142,6 +142,13 @@ void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s)
 // of 16.
 void launch_gather_bricks(const ulonglong2 *src, uint32_t n, uint64_t stride, uint8_t *dst, bool vec16,
                           cudaStream_t s);
+// In-flight marks (page-directory flag 3) of the batched form's overlapped
+// loads: mark the first min(ctl->total, maxreq) entries of a miss list; unmark
+// (3 -> 0) the first n entries of a list after its install.
+void launch_mark_in_flight(const uint4 *list, const ScanCtl *ctl, uint32_t maxreq, const LevelTables &lt,
+                           uint32_t mx, uint32_t my, uint64_t nentries, uint4 *mrpd, cudaStream_t s);
+void launch_unmark_in_flight(const uint4 *list, uint32_t n, const LevelTables &lt, uint32_t mx, uint32_t my,
+                             uint64_t nentries, uint4 *mrpd, cudaStream_t s);
 void launch_completude(const float4 *slot_vpos, uint32_t nslots, uint32_t *count, cudaStream_t s);
 
 // Ray caster (render.cu).  Launch configuration of the ray caster, process

@@ -375,7 +375,7 @@ __global__ void __launch_bounds__(1024) install_reference_kernel(InstallArgs a, 
             }
         if (dup || c >= a.nentries) continue;
         const uint4 e = a.mrpd[c];
-        if (e.w >= 1) continue;
+        if (e.w == 1u || e.w == 2u) continue;  // mapped or empty already (3 = in flight: install it)
         if (i < a.n_nonempty) {
             const uint32_t slot = a.order[a.nslots - a.n_nonempty + i];
             const uint32_t sx = slot % a.sx, sy = (slot / a.sx) % a.sy, sz = slot / (a.sx * a.sy);
@@ -489,6 +489,53 @@ void launch_gather_bricks(const ulonglong2 *src, uint32_t n, uint64_t stride, ui
         gather_bricks_kernel<uint4><<<grid, 256, 0, s>>>(src, n, stride, dst);
     else
         gather_bricks_kernel<uint8_t><<<grid, 256, 0, s>>>(src, n, stride, dst);
+    GC_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+// In-flight marks of the batched form's overlapped loads: the entries of a
+// miss list (x, y, z, level) handed to the loader are flagged 3 so that rays
+// stop there without requesting them again; after the install, the entries
+// still flagged (bricks that did not load) go back to 0.
+__device__ __forceinline__ uint64_t list_entry_index(const LevelTables &lt, uint4 b, uint32_t mx, uint32_t my) {
+    return static_cast<uint64_t>(lt.off[b.w] + b.x) + static_cast<uint64_t>(b.y) * mx +
+           static_cast<uint64_t>(b.z) * mx * my;
+}
+
+__global__ void mark_in_flight_kernel(const uint4 *__restrict__ list, const ScanCtl *ctl, uint32_t maxreq,
+                                      const LevelTables lt, uint32_t mx, uint32_t my, uint64_t nentries, uint4 *mrpd) {
+    const uint32_t n = min(ctl->total, maxreq);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint4 b = list[i];
+        if (b.w >= lt.nlevels) continue;
+        const uint64_t e = list_entry_index(lt, b, mx, my);
+        if (e < nentries && mrpd[e].w == 0u) mrpd[e].w = 3u;
+    }
+}
+
+__global__ void unmark_in_flight_kernel(const uint4 *__restrict__ list, uint32_t n, const LevelTables lt,
+                                        uint32_t mx, uint32_t my, uint64_t nentries, uint4 *mrpd) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint4 b = list[i];
+        if (b.w >= lt.nlevels) continue;
+        const uint64_t e = list_entry_index(lt, b, mx, my);
+        if (e < nentries && mrpd[e].w == 3u) mrpd[e] = make_uint4(0, 0, 0, 0);
+    }
+}
+
+void launch_mark_in_flight(const uint4 *list, const ScanCtl *ctl, uint32_t maxreq, const LevelTables &lt,
+                           uint32_t mx, uint32_t my, uint64_t nentries, uint4 *mrpd, cudaStream_t s) {
+    const uint32_t grid = std::max(1u, std::min<uint32_t>(div_up(maxreq, 256), static_cast<uint32_t>(sm_count()) * 2));
+    mark_in_flight_kernel<<<grid, 256, 0, s>>>(list, ctl, maxreq, lt, mx, my, nentries, mrpd);
+    GC_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+void launch_unmark_in_flight(const uint4 *list, uint32_t n, const LevelTables &lt, uint32_t mx, uint32_t my,
+                             uint64_t nentries, uint4 *mrpd, cudaStream_t s) {
+    if (n == 0) return;
+    const uint32_t grid = std::max(1u, std::min<uint32_t>(div_up(n, 256), static_cast<uint32_t>(sm_count()) * 2));
+    unmark_in_flight_kernel<<<grid, 256, 0, s>>>(list, n, lt, mx, my, nentries, mrpd);
     GC_CUDA(cudaGetLastError());
     count_launch();
 }

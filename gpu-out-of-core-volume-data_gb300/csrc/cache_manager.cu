@@ -118,20 +118,28 @@ struct gc_cache {
     uint64_t *status_lru = nullptr, *status_miss = nullptr;
     gc::ScanCtl *ctl_lru = nullptr, *ctl_miss = nullptr;
     uint32_t *d_count = nullptr, *d_misc = nullptr, *d_queue = nullptr;
-    uint4 *d_list = nullptr, *d_asked = nullptr, *d_big_coord = nullptr;
+    uint4 *d_asked = nullptr, *d_big_coord = nullptr;
     uint32_t *d_big_index = nullptr;
     ulonglong2 *d_src = nullptr;      // gather list: {host address, bytes} per big brick
     uint8_t *d_staging = nullptr;
     gc::ViewParams *d_views = nullptr;
     uint32_t max_views = 256;
     // pinned host buffers
-    uint4 *h_list = nullptr, *h_asked = nullptr, *h_big_coord = nullptr;
-    uint32_t *h_total = nullptr, *h_big_index = nullptr, *h_misc = nullptr;
+    uint4 *h_asked = nullptr, *h_big_coord = nullptr;
+    uint32_t *h_big_index = nullptr, *h_misc = nullptr;
+    // Miss lists: the scan writes one, the loader serves one.  The plain frame
+    // loop only uses list 0; the batched form's overlapped loads use both.
+    struct MissList {
+        uint4 *d = nullptr, *h = nullptr;  // up to max_requests (x, y, z, level)
+        uint32_t *total = nullptr;         // pinned: misses found (uncapped)
+        cudaEvent_t ev = nullptr;          // the list and total are on the host
+    } lists[2];
+    int cur_load = 0;  // list the loader serves
     ulonglong2 *h_src = nullptr;
     uint8_t *h_staging = nullptr;
     cudaStream_t side = nullptr;
     cudaStream_t frame_stream = nullptr;  // stream of the update in progress (synchronous loader)
-    cudaEvent_t ev_list = nullptr, ev_upload = nullptr, ev_upload_begin = nullptr;
+    cudaEvent_t ev_upload = nullptr, ev_upload_begin = nullptr;
     bool upload_timed = false;  // ev_upload_begin/ev_upload bracket an upload not yet counted
     int cur = 0;
     uint32_t ts = 1, epoch_lru = 0, epoch_miss = 0;
@@ -211,7 +219,7 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     uint32_t read_threads = 1;
     uint64_t bytes_up = 0;
     for (uint32_t i = 0; i < n; ++i) {
-        const uint4 b = C->h_list[i];  // (x, y, z, cache level)
+        const uint4 b = C->lists[C->cur_load].h[i];  // (x, y, z, cache level)
         const Volume &V = C->vols[C->level_volume[b.w < C->lt.nlevels ? b.w : 0]];
         const uint32_t lvl = b.w - V.level_base;  // level within the volume
         const uint32_t *BB = V.desc.big_brick_size;
@@ -321,9 +329,9 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     // stable partition: non-empty first, then empty (RequestHandler.hpp:354-369)
     uint32_t k = 0;
     for (uint32_t i = 0; i < n; ++i)
-        if (kind[i] == 0) C->h_asked[k++] = C->h_list[i];
+        if (kind[i] == 0) C->h_asked[k++] = C->lists[C->cur_load].h[i];
     for (uint32_t i = 0; i < n; ++i)
-        if (kind[i] == 1) C->h_asked[k++] = C->h_list[i];
+        if (kind[i] == 1) C->h_asked[k++] = C->lists[C->cur_load].h[i];
     std::memcpy(C->h_big_index, big_index.data(), big_index.size() * sizeof(uint32_t));
     C->pend_n = k;
     C->pend_nonempty = n_nonempty;
@@ -362,7 +370,7 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
 // bricks are pending for install.
 static bool serve_request(gc_cache *C) {
     GC_CUDA(cudaSetDevice(C->device));
-    GC_CUDA(cudaEventSynchronize(C->ev_list));
+    GC_CUDA(cudaEventSynchronize(C->lists[C->cur_load].ev));
     // The previous upload has normally completed (its install ran before this
     // scan); waiting on it also keeps the staging buffers from being refilled
     // under a copy when the caller switches streams between frames.
@@ -373,7 +381,7 @@ static bool serve_request(gc_cache *C) {
         C->stats.upload_ns += static_cast<uint64_t>(static_cast<double>(ms) * 1e6);
         C->upload_timed = false;
     }
-    const uint32_t total = *C->h_total;
+    const uint32_t total = *C->lists[C->cur_load].total;
     const uint32_t n = std::min(total, C->d.max_requests);
     C->stats.last_requests = total;
     C->stats.requests_raised += total;
@@ -472,12 +480,15 @@ static void install(gc_cache *C, cudaStream_t s) {
     C->pend_nonempty = 0;
 }
 
-static void scan_requests(gc_cache *C, cudaStream_t s) {
-    launch_miss_compact(C->req, C->nentries - 1, C->ts, C->d.max_requests, C->d_list, C->lt, C->mx, C->my,
+// Miss scan into list `slot`; mark: flag the listed entries in flight (3).
+static void scan_requests(gc_cache *C, cudaStream_t s, int slot = 0, bool mark = false) {
+    gc_cache::MissList &L = C->lists[slot];
+    launch_miss_compact(C->req, C->nentries - 1, C->ts, C->d.max_requests, L.d, C->lt, C->mx, C->my,
                         C->status_miss, C->ctl_miss, ++C->epoch_miss, s);
-    GC_CUDA(cudaMemcpyAsync(C->h_list, C->d_list, C->d.max_requests * sizeof(uint4), cudaMemcpyDeviceToHost, s));
-    GC_CUDA(cudaMemcpyAsync(C->h_total, &C->ctl_miss->total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    GC_CUDA(cudaEventRecord(C->ev_list, s));
+    if (mark) launch_mark_in_flight(L.d, C->ctl_miss, C->d.max_requests, C->lt, C->mx, C->my, C->nentries, C->mrpd, s);
+    GC_CUDA(cudaMemcpyAsync(L.h, L.d, C->d.max_requests * sizeof(uint4), cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaMemcpyAsync(L.total, &C->ctl_miss->total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    GC_CUDA(cudaEventRecord(L.ev, s));
 }
 
 static bool update(gc_cache *C, cudaStream_t s) {
@@ -539,14 +550,16 @@ static void destroy(gc_cache *C) {
     cudaDeviceSynchronize();
     void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool, C->slot_bins, C->d_samples,
                    C->status_lru, C->status_miss, C->ctl_lru, C->ctl_miss, C->d_count, C->d_misc, C->d_queue,
-                   C->d_list, C->d_asked, C->d_big_coord, C->d_big_index, C->d_src, C->d_staging, C->d_views};
+                   C->lists[0].d, C->lists[1].d, C->d_asked, C->d_big_coord, C->d_big_index, C->d_src,
+                   C->d_staging, C->d_views};
     for (void *p : dev)
         if (p) cudaFree(p);
-    void *host[] = {C->h_list,  C->h_asked, C->h_big_coord, C->h_total,
+    void *host[] = {C->lists[0].h, C->lists[1].h, C->lists[0].total, C->lists[1].total, C->h_asked, C->h_big_coord,
                     C->h_big_index, C->h_misc, C->h_src, C->h_staging};
     for (void *p : host)
         if (p) cudaFreeHost(p);
-    if (C->ev_list) cudaEventDestroy(C->ev_list);
+    for (auto &L : C->lists)
+        if (L.ev) cudaEventDestroy(L.ev);
     if (C->ev_upload) cudaEventDestroy(C->ev_upload);
     if (C->ev_upload_begin) cudaEventDestroy(C->ev_upload_begin);
     if (C->side) cudaStreamDestroy(C->side);
@@ -760,22 +773,24 @@ int gc_cache_create_shared(const gc_cache_desc *desc, const gc_volume_desc *volu
         C->d_count = dalloc<uint32_t>(1, "counter");
         C->d_misc = dalloc<uint32_t>(1, "counter");
         C->d_queue = dalloc<uint32_t>(4, "work queue");
-        C->d_list = dalloc<uint4>(maxr, "miss list");
+        for (auto &L : C->lists) L.d = dalloc<uint4>(maxr, "miss list");
         C->d_asked = dalloc<uint4>(maxr, "asked list");
         C->d_big_coord = dalloc<uint4>(maxr, "big brick coords");
         C->d_big_index = dalloc<uint32_t>(maxr, "big brick indexes");
         C->d_src = dalloc<ulonglong2>(maxr, "brick gather list");
         C->d_staging = dalloc<uint8_t>(maxr * C->big_stride, "staging");
         C->d_views = dalloc<ViewParams>(C->max_views, "views");
-        C->h_list = halloc<uint4>(maxr);
+        for (auto &L : C->lists) {
+            L.h = halloc<uint4>(maxr);
+            L.total = halloc<uint32_t>(1);
+            *L.total = 0;
+        }
         C->h_asked = halloc<uint4>(maxr);
         C->h_big_coord = halloc<uint4>(maxr);
         C->h_big_index = halloc<uint32_t>(maxr);
         C->h_src = halloc<ulonglong2>(maxr);
-        C->h_total = halloc<uint32_t>(1);
         C->h_misc = halloc<uint32_t>(1);
         C->h_staging = halloc<uint8_t>(maxr * C->big_stride);
-        *C->h_total = 0;
         *C->h_misc = 0;
         GC_CUDA(cudaMemset(C->mrpd, 0, C->nentries * sizeof(uint4)));
         GC_CUDA(cudaMemset(C->req, 0, C->nentries * sizeof(uint32_t)));
@@ -793,7 +808,7 @@ int gc_cache_create_shared(const gc_cache_desc *desc, const gc_volume_desc *volu
         int least = 0, greatest = 0;
         GC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
         GC_CUDA(cudaStreamCreateWithPriority(&C->side, cudaStreamNonBlocking, greatest));
-        GC_CUDA(cudaEventCreateWithFlags(&C->ev_list, cudaEventDisableTiming));
+        for (auto &L : C->lists) GC_CUDA(cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming));
         GC_CUDA(cudaEventCreate(&C->ev_upload));
         GC_CUDA(cudaEventCreate(&C->ev_upload_begin));
         GC_CUDA(cudaDeviceSynchronize());
@@ -1038,11 +1053,12 @@ int gc_cache_last_misses(gc_cache_t C, uint32_t *out4, uint32_t max, uint32_t *c
             std::unique_lock<std::mutex> lk(C->mu);
             C->cv.wait(lk, [&] { return !C->busy; });
         }
-        GC_CUDA(cudaEventSynchronize(C->ev_list));
-        const uint32_t n = std::min(std::min(*C->h_total, C->d.max_requests), max);
-        std::memcpy(out4, C->h_list, static_cast<size_t>(n) * sizeof(uint4));
+        const auto &L = C->lists[C->cur_load];
+        GC_CUDA(cudaEventSynchronize(L.ev));
+        const uint32_t n = std::min(std::min(*L.total, C->d.max_requests), max);
+        std::memcpy(out4, L.h, static_cast<size_t>(n) * sizeof(uint4));
         *count = n;
-        *total = *C->h_total;
+        *total = *L.total;
     });
 }
 
@@ -1173,6 +1189,7 @@ struct gc_batch {
         std::chrono::steady_clock::time_point submitted;
         bool started;      // progressive buffers cleared (first admission)
         uint64_t seq;      // admission sequence number (the newest is parked first)
+        uint64_t wait;     // overlapped loads: serial of the load the view waits for (0: none)
     };
     uint64_t admissions = 0;
     float last_cam[3] = {0.f, 0.f, 0.f};  // camera of the last admitted view
@@ -1191,11 +1208,52 @@ struct gc_batch {
     gc_batch_stats st;
     gc::RenderGraph graph;                // the replayed launch
     gc::ViewParams *h_views = nullptr;    // pinned view table the graph copies
+    // Overlapped loads: each miss list is a load with a serial number; a view
+    // waits for the load its requests went into.  List slot state: 0 free,
+    // 1 scanned and waiting for the loader, 2 with the loader.
+    int slot_state[2] = {0, 0};
+    uint64_t slot_serial[2] = {0, 0};
+    uint64_t next_serial = 1;
+    std::unordered_set<uint64_t> completed;  // loads installed (or empty)
+    uint32_t used_prev = 0;                   // slots used by the previous render (the other cohort)
+    cudaStream_t stream = nullptr;            // stream of the last overlapped tick
 };
 
 namespace gc {
+// Overlapped loads leave in-flight marks in the page directory until their
+// install; a batch that ends first waits for the loader, installs what it
+// finished and clears the marks of every list it still holds, so that the
+// cache serves later frames as if the batch had run to the end.
+static void batch_drain_loads(gc_batch *b) {
+    gc_cache *C = b->cache;
+    if (!b->d.overlap_loads || (b->slot_state[0] == 0 && b->slot_state[1] == 0)) return;
+    cudaSetDevice(C->device);
+    cudaStream_t s = b->stream;
+    bool installable = false;
+    {
+        std::unique_lock<std::mutex> lk(C->mu);
+        C->cv.wait(lk, [&] { return !C->busy; });  // the loader's load is finite
+        installable = C->done && b->slot_state[C->cur_load] == 2;
+        C->done = false;
+        C->loader_error.clear();
+    }
+    if (installable) install(C, s);
+    for (int k = 0; k < 2; ++k) {
+        if (b->slot_state[k] == 0) continue;
+        const gc_cache::MissList &L = C->lists[k];
+        launch_unmark_in_flight(L.d, std::min(*L.total, C->d.max_requests), C->lt, C->mx, C->my, C->nentries,
+                                C->mrpd, s);
+        b->slot_state[k] = 0;
+    }
+    cudaStreamSynchronize(s);
+}
+
 static void batch_destroy(gc_batch *b) {
     if (!b) return;
+    try {
+        batch_drain_loads(b);
+    } catch (const std::exception &) {
+    }
     if (b->d_status) cudaFree(b->d_status);
     if (b->h_status) cudaFreeHost(b->h_status);
     if (b->h_views) cudaFreeHost(b->h_views);
@@ -1206,6 +1264,202 @@ static void batch_destroy(gc_batch *b) {
 }
 }  // namespace gc
 
+namespace gc {
+// Admission: queued views in arrival order (or, with a reorder window, the one
+// whose camera is nearest the last admitted view's) while the budgets allow;
+// at least one view is active.  By cache memory: the active views' demand --
+// slots used plus missing bricks found -- must stay within max_occupancy of
+// the pool slots.  `all`: admission is open this tick.
+static void batch_admit(gc_batch *b, gc_cache *C, cudaStream_t s, bool all, double demand) {
+    uint64_t pixels = 0;
+    for (auto &it : b->active) pixels += static_cast<uint64_t>(it.view.width) * it.view.height;
+    const bool occ_ok =
+        b->d.max_occupancy <= 0.f || demand <= b->d.max_occupancy * static_cast<double>(C->nslots);
+    uint32_t admitted = 0;
+    auto cam_dist = [&](const gc_view &v) {  // camera = translation column of the view matrix
+        const float dx = v.inv_view[3] - b->last_cam[0], dy = v.inv_view[7] - b->last_cam[1],
+                    dz = v.inv_view[11] - b->last_cam[2];
+        // views of another volume share no bricks: farther than any camera
+        return dx * dx + dy * dy + dz * dz + (v.volume != b->last_volume ? 1e30f : 0.f);
+    };
+    while (!b->queue.empty() && b->active.size() < b->d.max_views) {
+        size_t pick = 0;
+        if (b->d.reorder_window > 1 && b->have_cam && b->queue.front().skipped < b->d.reorder_window) {
+            const size_t w = std::min<size_t>(b->queue.size(), b->d.reorder_window);
+            float best = cam_dist(b->queue[0].view);
+            for (size_t k = 1; k < w; ++k) {
+                const float d = cam_dist(b->queue[k].view);
+                if (d < best) {
+                    best = d;
+                    pick = k;
+                }
+            }
+        }
+        const gc_view &v = b->queue[pick].view;
+        const uint64_t px = static_cast<uint64_t>(v.width) * v.height;
+        if (!b->active.empty() && (!all || pixels + px > b->d.max_pixels || !occ_ok ||
+                                   (b->d.max_admit && admitted >= b->d.max_admit)))
+            break;
+        ++admitted;
+        if (!b->queue[pick].started) {  // a parked view resumes with its progress
+            GC_CUDA(cudaMemsetAsync(v.tbuf, 0, px * sizeof(float), s));
+            GC_CUDA(cudaMemsetAsync(v.state, 0, px * 4 * sizeof(float), s));
+            b->queue[pick].started = true;
+        }
+        b->queue[pick].seq = b->admissions++;
+        pixels += px;
+        b->last_cam[0] = v.inv_view[3];
+        b->last_cam[1] = v.inv_view[7];
+        b->last_cam[2] = v.inv_view[11];
+        b->last_volume = v.volume;
+        b->have_cam = true;
+        if (pick) b->queue.front().skipped++;
+        b->active.push_back(b->queue[pick]);
+        b->queue.erase(b->queue.begin() + static_cast<std::ptrdiff_t>(pick));
+    }
+}
+
+// The overlapped tick (gc_batch_desc.overlap_loads; asynchronous loader).
+// Loads complete in order.  A tick: finish the load the loader completed
+// (install, clear its leftover in-flight marks, free its list), hand a waiting
+// list to an idle loader, admit, render the views whose awaited load has
+// completed, and -- when a list is free -- scan their requests into it with
+// in-flight marks.  The loader then uploads one cohort's bricks while the
+// other cohort renders.
+static void batch_tick_overlapped(gc_batch *b, gc_cache *C, cudaStream_t s, uint32_t *n_active,
+                                  uint32_t *n_queued) {
+    b->stream = s;
+    auto hand_to_loader = [&] {  // the oldest waiting list, if the loader is idle
+        std::unique_lock<std::mutex> lk(C->mu);
+        if (C->busy || C->done) return;
+        int pick = -1;
+        for (int k = 0; k < 2; ++k)
+            if (b->slot_state[k] == 1 && (pick < 0 || b->slot_serial[k] < b->slot_serial[pick])) pick = k;
+        if (pick < 0) return;
+        // the loader waits on this event: it covers the scan of the list and
+        // the install just enqueued, which reads the staging buffers that
+        // the load refills
+        GC_CUDA(cudaEventRecord(C->lists[pick].ev, s));
+        C->cur_load = pick;
+        b->slot_state[pick] = 2;
+        C->busy = true;
+        C->has_request = true;
+        C->cv.notify_all();
+    };
+    {  // 1. the load the loader finished
+        std::unique_lock<std::mutex> lk(C->mu);
+        if (!C->loader_error.empty()) {
+            std::string e = C->loader_error;
+            C->loader_error.clear();
+            fail(GC_ERR_IO, "brick loader: " + e);
+        }
+        const int k = C->cur_load;
+        if (!C->busy && b->slot_state[k] == 2) {
+            const bool installable = C->done;
+            lk.unlock();
+            if (installable) {
+                install(C, s);
+                b->installs++;
+                b->st.install_ticks++;
+            }
+            const gc_cache::MissList &L = C->lists[k];
+            launch_unmark_in_flight(L.d, std::min(*L.total, C->d.max_requests), C->lt, C->mx, C->my, C->nentries,
+                                    C->mrpd, s);
+            lk.lock();
+            C->done = false;
+            b->slot_state[k] = 0;
+            b->completed.insert(b->slot_serial[k]);
+        }
+    }
+    hand_to_loader();
+    int free_slot = b->slot_state[0] == 0 ? 0 : (b->slot_state[1] == 0 ? 1 : -1);
+    // 2. admission while a list is free (a new view's first pass feeds a scan)
+    batch_admit(b, C, s, free_slot >= 0,
+                static_cast<double>(b->last_used) + b->used_prev + static_cast<double>(b->last_misses));
+    const uint32_t na = static_cast<uint32_t>(b->active.size());
+    if (n_active) *n_active = na;
+    if (n_queued) *n_queued = static_cast<uint32_t>(b->queue.size());
+    // 3. views whose awaited load completed (or never rendered)
+    std::vector<uint32_t> sel;
+    if (free_slot >= 0)
+        for (uint32_t i = 0; i < na; ++i)
+            if (b->active[i].wait == 0 || b->completed.count(b->active[i].wait)) sel.push_back(i);
+    if (sel.empty()) {
+        if (na) {
+            const auto t0 = std::chrono::steady_clock::now();
+            wait_loader(C, 5);
+            b->st.wait_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        }
+        return;
+    }
+    const uint32_t n = static_cast<uint32_t>(sel.size());
+    std::vector<gc_view> views(n);
+    for (uint32_t k = 0; k < n; ++k) {
+        views[k] = b->active[sel[k]].view;
+        views[k].status = b->d_status + k;
+    }
+    GC_CUDA(cudaMemsetAsync(b->d_status, 0, n * sizeof(uint32_t), s));
+    GC_CUDA(cudaEventRecord(b->ev_r0, s));
+    render(C, views.data(), n, s, true, &b->graph, b->h_views);
+    GC_CUDA(cudaEventRecord(b->ev_r1, s));
+    GC_CUDA(cudaMemcpyAsync(b->h_status, b->d_status, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    lru_update(C, s);
+    GC_CUDA(cudaMemcpyAsync(b->h_status + b->d.max_views, C->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    // 4. their requests into the free list, marked in flight
+    C->frame_stream = s;
+    scan_requests(C, s, free_slot, true);
+    const uint64_t serial = b->next_serial++;
+    b->slot_state[free_slot] = 1;
+    b->slot_serial[free_slot] = serial;
+    C->ts++;
+    C->stats.frames++;
+    GC_CUDA(cudaEventRecord(b->ev, s));
+    GC_CUDA(cudaEventSynchronize(b->ev));
+    b->used_prev = b->last_used;
+    b->last_used = b->h_status[b->d.max_views];
+    const uint32_t misses = *C->lists[free_slot].total;  // copied on this stream before the event
+    b->last_misses = misses;
+    uint64_t wait = serial;
+    if (misses == 0) {  // nothing to load: the list is done; wait for the newest load still out
+        b->slot_state[free_slot] = 0;
+        b->completed.insert(serial);
+        wait = 0;
+        for (int k = 0; k < 2; ++k)
+            if (b->slot_state[k] != 0) wait = std::max(wait, b->slot_serial[k]);
+    }
+    hand_to_loader();
+    float rms = 0.f;
+    GC_CUDA(cudaEventElapsedTime(&rms, b->ev_r0, b->ev_r1));
+    b->st.render_ms += rms;
+    b->st.render_ticks++;
+    b->st.view_passes += n;
+    // 5. retire converged views; the others wait for this tick's load
+    const auto now = std::chrono::steady_clock::now();
+    std::vector<char> gone(na, 0);
+    for (uint32_t k = 0; k < n; ++k) {
+        auto &it = b->active[sel[k]];
+        it.passes++;
+        it.wait = wait;
+        const bool conv = (b->h_status[k] & 1u) == 0;
+        if (conv || (b->d.max_passes && it.passes >= b->d.max_passes)) {
+            gc_batch_result r;
+            r.tag = it.tag;
+            r.passes = it.passes;
+            r.converged = conv ? 1u : 0u;
+            r.latency_ms = std::chrono::duration<double, std::milli>(now - it.submitted).count();
+            b->done.push_back(r);
+            gone[sel[k]] = 1;
+        }
+    }
+    std::vector<gc_batch::Item> keep;
+    keep.reserve(na);
+    for (uint32_t i = 0; i < na; ++i)
+        if (!gone[i]) keep.push_back(b->active[i]);
+    b->active.swap(keep);
+}
+
+}  // namespace gc
+
 extern "C" {
 
 int gc_batch_create(gc_cache_t C, const gc_batch_desc *desc, gc_batch_t *out) {
@@ -1214,6 +1468,7 @@ int gc_batch_create(gc_cache_t C, const gc_batch_desc *desc, gc_batch_t *out) {
         GC_REQUIRE(C && desc && out, "null argument");
         GC_REQUIRE(desc->max_views >= 1 && desc->max_views <= C->max_views, "max_views must be in [1, 256]");
         GC_REQUIRE(desc->max_pixels >= 1, "max_pixels must be >= 1");
+        GC_REQUIRE(!desc->overlap_loads || !C->sync_mode(), "overlapped loads need the asynchronous loader");
         GC_CUDA(cudaSetDevice(C->device));
         b = new gc_batch();
         b->cache = C;
@@ -1241,7 +1496,7 @@ int gc_batch_submit(gc_batch_t b, const gc_view *view, uint64_t tag) {
         GC_REQUIRE(b && view, "null argument");
         ViewParams check;
         fill_view(b->cache, *view, check);  // validates the view now, not at admission
-        b->queue.push_back({*view, tag, 0, gc_batch::kNever, 0, std::chrono::steady_clock::now(), false, 0});
+        b->queue.push_back({*view, tag, 0, gc_batch::kNever, 0, std::chrono::steady_clock::now(), false, 0, 0});
     });
 }
 
@@ -1261,6 +1516,10 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
                 b->st.tick_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
             }
         } tick_clock{b, t_tick};
+        if (b->d.overlap_loads) {
+            batch_tick_overlapped(b, C, s, n_active, n_queued);
+            return;
+        }
         if (batch_install(C, s)) {
             b->installs++;
             b->st.install_ticks++;
@@ -1269,57 +1528,7 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         // loader is idle; only then are views admitted, so that a new view's
         // first pass feeds the scan that ends the tick.
         const bool all = loader_idle(C);
-        // admission: views in arrival order while the budgets allow (at least
-        // one active view).  By cache memory: the demand of the active views
-        // -- slots their last full pass used plus the missing bricks the last
-        // scan found -- must stay within max_occupancy of the pool slots.
-        uint64_t pixels = 0;
-        for (auto &it : b->active) pixels += static_cast<uint64_t>(it.view.width) * it.view.height;
-        const double demand = static_cast<double>(b->last_used) + static_cast<double>(b->last_misses);
-        const bool occ_ok =
-            b->d.max_occupancy <= 0.f || demand <= b->d.max_occupancy * static_cast<double>(C->nslots);
-        uint32_t admitted = 0;
-        auto cam_dist = [&](const gc_view &v) {  // camera = translation column of the view matrix
-            const float dx = v.inv_view[3] - b->last_cam[0], dy = v.inv_view[7] - b->last_cam[1],
-                        dz = v.inv_view[11] - b->last_cam[2];
-            // views of another volume share no bricks: farther than any camera
-            return dx * dx + dy * dy + dz * dz + (v.volume != b->last_volume ? 1e30f : 0.f);
-        };
-        while (!b->queue.empty() && b->active.size() < b->d.max_views) {
-            size_t pick = 0;
-            if (b->d.reorder_window > 1 && b->have_cam && b->queue.front().skipped < b->d.reorder_window) {
-                const size_t w = std::min<size_t>(b->queue.size(), b->d.reorder_window);
-                float best = cam_dist(b->queue[0].view);
-                for (size_t k = 1; k < w; ++k) {
-                    const float d = cam_dist(b->queue[k].view);
-                    if (d < best) {
-                        best = d;
-                        pick = k;
-                    }
-                }
-            }
-            const gc_view &v = b->queue[pick].view;
-            const uint64_t px = static_cast<uint64_t>(v.width) * v.height;
-            if (!b->active.empty() && (!all || pixels + px > b->d.max_pixels || !occ_ok ||
-                                       (b->d.max_admit && admitted >= b->d.max_admit)))
-                break;
-            ++admitted;
-            if (!b->queue[pick].started) {  // a parked view resumes with its progress
-                GC_CUDA(cudaMemsetAsync(v.tbuf, 0, px * sizeof(float), s));
-                GC_CUDA(cudaMemsetAsync(v.state, 0, px * 4 * sizeof(float), s));
-                b->queue[pick].started = true;
-            }
-            b->queue[pick].seq = b->admissions++;
-            pixels += px;
-            b->last_cam[0] = v.inv_view[3];
-            b->last_cam[1] = v.inv_view[7];
-            b->last_cam[2] = v.inv_view[11];
-            b->last_volume = v.volume;
-            b->have_cam = true;
-            if (pick) b->queue.front().skipped++;
-            b->active.push_back(b->queue[pick]);
-            b->queue.erase(b->queue.begin() + static_cast<std::ptrdiff_t>(pick));
-        }
+        batch_admit(b, C, s, all, static_cast<double>(b->last_used) + static_cast<double>(b->last_misses));
         const uint32_t na = static_cast<uint32_t>(b->active.size());
         if (n_active) *n_active = na;
         if (n_queued) *n_queued = static_cast<uint32_t>(b->queue.size());
@@ -1359,7 +1568,7 @@ int gc_batch_tick(gc_batch_t b, void *stream, uint32_t *n_active, uint32_t *n_qu
         b->st.render_ms += rms;
         b->st.render_ticks++;
         b->st.view_passes += n;
-        if (scanned) b->last_misses = *C->h_total;  // copied on this stream before the event
+        if (scanned) b->last_misses = *C->lists[0].total;  // copied on this stream before the event
         const auto now = std::chrono::steady_clock::now();
         std::vector<char> gone(na, 0);
         for (uint32_t k = 0; k < n; ++k) {

@@ -374,6 +374,7 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
         sample = sample_any<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, eb, cv, sampler, fx, fy, fz);
         return kMapped;
     }
+    if (e.w == 3u) return kUnmapped;  // on its way (batched form): already requested
     if (e.w == 0u) {
         // raise_brick_request (K_CacheManager.hpp:364-396): same coordinates
         uint32_t *r = cv.req + idx;

@@ -85,7 +85,7 @@ class View(C.Structure):
 class BatchDesc(C.Structure):
     _fields_ = [("max_views", C.c_uint32), ("max_pixels", C.c_uint64), ("max_passes", C.c_uint32),
                 ("max_occupancy", C.c_float), ("max_admit", C.c_uint32), ("park_above", C.c_float),
-                ("reorder_window", C.c_uint32)]
+                ("reorder_window", C.c_uint32), ("overlap_loads", C.c_uint32)]
 
 
 class BatchStats(C.Structure):
@@ -600,10 +600,11 @@ class Batch:
     """Continuous batching of views over one cache (gc_batch_*)."""
 
     def __init__(self, cache, max_views=64, max_pixels=1 << 24, max_passes=0, max_occupancy=0.0, max_admit=0,
-                 park_above=0.0, reorder_window=0):
+                 park_above=0.0, reorder_window=0, overlap_loads=False):
         self.cache = cache
         self._h = vp()
-        d = BatchDesc(max_views, max_pixels, max_passes, max_occupancy, max_admit, park_above, reorder_window)
+        d = BatchDesc(max_views, max_pixels, max_passes, max_occupancy, max_admit, park_above, reorder_window,
+                      1 if overlap_loads else 0)
         check(lib.gc_batch_create(cache.handle, C.byref(d), C.byref(self._h)))
 
     def submit(self, view, tag):

@@ -480,6 +480,14 @@ typedef struct gc_batch_desc {
                                 them in the cache); the oldest queued view is
                                 admitted once passed over reorder_window
                                 times.  0 or 1: arrival order.                 */
+    uint32_t overlap_loads;  /* 1: overlap brick loads with rendering (needs the
+                                cache's asynchronous loader).  The bricks of a
+                                miss list are marked in flight in the page
+                                directory (rays stop there without requesting
+                                them again); while the loader uploads one list,
+                                the views waiting on the previous one render
+                                and scan into a second list.  Images are the
+                                same.  0: one load at a time.                  */
 } gc_batch_desc;
 typedef struct gc_batch_result {
     uint64_t tag;

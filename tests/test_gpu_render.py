@@ -232,22 +232,10 @@ def test_async_loader_converges_to_same_image(gc, orc, torch_cuda):
     assert np.array_equal(imgs[0], imgs[1])
 
 
-@pytest.mark.parametrize("park,sync,reorder", [(0.0, True, 0), (0.0, False, 0), (0.05, True, 0), (0.05, False, 4),
-                                               (0.0, True, 3)])
-def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, park, sync, reorder):
-    """Continuous batching (admission by pixel budget, one persistent launch
-    per tick, skipped passes for views that cannot progress, retirement on
-    convergence) gives every view the image it gets when rendered alone to
-    convergence, with the synchronous or the asynchronous loader, with
-    arrival-order or locality-ordered admission and with views parked under
-    memory pressure (a low park threshold parks views often; they resume from
-    their progressive state); the per-view status word reports convergence
-    exactly."""
-    specs = [((64, 48), 1), ((33, 17), 4), ((96, 80), 7), ((40, 40), 10), ((80, 24), 5)]
-    tf = scenario.ramp_tf()
+def single_view_images(gc, orc, torch_cuda, specs, tf_dev):
+    """Each view rendered alone to convergence through the plain frame loop."""
     single = []
     s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 64)
-    tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
     status = torch_cuda.zeros(1, dtype=torch_cuda.int32, device="cuda")
     for (W, H), cam in specs:
         g, _ = s.buffers(W, H)
@@ -262,9 +250,36 @@ def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, park, sync, r
         assert int(status.item()) == 0
         single.append(g[0].cpu().numpy())
     s.cm.close()
+    return single
+
+
+def in_flight_marks(gc, cm, nentries):
+    mrpd = np.zeros((nentries, 4), np.uint32)
+    cm.dump(gc.DUMP_MRPD, mrpd)
+    return int((mrpd[:, 3] == 3).sum())
+
+
+@pytest.mark.parametrize("park,sync,reorder,overlap", [(0.0, True, 0, False), (0.0, False, 0, False),
+                                                       (0.05, True, 0, False), (0.05, False, 4, False),
+                                                       (0.0, True, 3, False), (0.0, False, 0, True),
+                                                       (0.0, False, 4, True)])
+def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, park, sync, reorder, overlap):
+    """Continuous batching (admission by pixel budget, one persistent launch
+    per tick, skipped passes for views that cannot progress, retirement on
+    convergence) gives every view the image it gets when rendered alone to
+    convergence, with the synchronous or the asynchronous loader, with
+    arrival-order or locality-ordered admission, with views parked under
+    memory pressure (a low park threshold parks views often; they resume from
+    their progressive state) and with overlapped loads (bricks in flight are
+    marked in the page directory; the marks are gone once the batch ends);
+    the per-view status word reports convergence exactly."""
+    specs = [((64, 48), 1), ((33, 17), 4), ((96, 80), 7), ((40, 40), 10), ((80, 24), 5)]
+    tf_dev = torch_cuda.from_numpy(scenario.ramp_tf().reshape(-1)).cuda()
+    single = single_view_images(gc, orc, torch_cuda, specs, tf_dev)
 
     s2 = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 64, sync=sync)
-    b = gc.Batch(s2.cm, max_views=3, max_pixels=96 * 80 + 64 * 48, park_above=park, reorder_window=reorder)
+    b = gc.Batch(s2.cm, max_views=3, max_pixels=96 * 80 + 64 * 48, park_above=park, reorder_window=reorder,
+                 overlap_loads=overlap)
     bufs = []
     for i, ((W, H), cam) in enumerate(specs):
         g, _ = s2.buffers(W, H)
@@ -288,6 +303,40 @@ def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, park, sync, r
         assert st.parked > 0
     b.close()
     assert s2.cm.stats().device_error == 0
+    assert in_flight_marks(gc, s2.cm, s2.oc.nentries) == 0
+
+
+def test_overlapped_batch_closed_mid_load(gc, orc, torch_cuda):
+    """A batch with overlapped loads that ends while bricks are in flight
+    installs or releases them: no page-directory entry stays marked, and the
+    plain frame loop then renders a view to the image it gets alone."""
+    specs = [((64, 48), 1), ((33, 17), 4), ((96, 80), 7)]
+    tf_dev = torch_cuda.from_numpy(scenario.ramp_tf().reshape(-1)).cuda()
+    single = single_view_images(gc, orc, torch_cuda, specs, tf_dev)
+    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 64, sync=False)
+    b = gc.Batch(s.cm, max_views=3, max_pixels=1 << 16, overlap_loads=True)
+    for i, ((W, H), cam) in enumerate(specs):
+        g, _ = s.buffers(W, H)
+        b.submit(s.view(scenario.orbit_camera(gc, cam, 12, 3.0), W, H, tf_dev, 256, g), tag=i)
+    for _ in range(3):
+        b.tick()
+    b.close()
+    torch_cuda.cuda.synchronize()
+    assert in_flight_marks(gc, s.cm, s.oc.nentries) == 0
+    status = torch_cuda.zeros(1, dtype=torch_cuda.int32, device="cuda")
+    (W, H), cam = specs[2]
+    g, _ = s.buffers(W, H)
+    v = s.view(scenario.orbit_camera(gc, cam, 12, 3.0), W, H, tf_dev, 256, g)
+    v.status = status.data_ptr()
+    for it in range(64):
+        status.zero_()
+        s.cm.render(v)
+        s.cm.update()
+        if int(status.item()) == 0:
+            break
+    assert int(status.item()) == 0
+    assert np.array_equal(g[0].cpu().numpy(), single[2])
+    assert s.cm.stats().device_error == 0
 
 
 def test_coarser_level_fallback_preview(gc, orc, torch_cuda):
