@@ -92,6 +92,7 @@ OUR_DEFAULT_STEPS = 40  # views the GPU arm times by default (the reference arm 
 #       --nvtx-include roofline/ -k regex:render -c 2 python bench.py --steps 4 --warmup 3 --no-cpu-baseline --no-batched
 # (profiles/render_kernel_c2_1024x1024.md).  None for the other configs.
 ROOFLINE_TRAFFIC = {"c2": 107_050_000}
+BRICK_BINS = {}  # value bins of every brick, by brick-store address
 
 
 def workload(name, cfg):
@@ -261,7 +262,9 @@ def make_store(gc, torch, cfg):
     torch.cuda.synchronize()
     t1 = time.time()
     tm = {}
-    store, offs, _ = gc.pre_process(vol, layout, dev, pin=PIN_STORES, timings=tm)
+    bins = []
+    store, offs, _ = gc.pre_process(vol, layout, dev, pin=PIN_STORES, timings=tm, value_bins=bins)
+    BRICK_BINS[store.data_ptr()] = bins[0]
     LAST_PREPROCESS.clear()
     LAST_PREPROCESS.update(tm)
     del dev
@@ -276,6 +279,7 @@ class Session:
     """One cache + the buffers of its views, driven through the C ABI."""
 
     staged = False  # GC_CACHE_STAGED_UPLOAD for every session (--upload staged)
+    brick_bins = False  # give the cache the value bins of every brick (--brick-bins)
 
     def __init__(self, gc, torch, cfg, vol, layout, store, offs, max_requests, sync=True):
         self.gc, self.torch, self.cfg = gc, torch, cfg
@@ -283,6 +287,8 @@ class Session:
         self.cm = gc.CacheManager(vol, layout, self.pool, max_requests=max_requests, sync_loader=sync,
                                   staged_upload=Session.staged)
         self.cm.set_source_host(store, offs)
+        if Session.brick_bins:
+            self.cm.set_brick_bins(BRICK_BINS[store.data_ptr()])
         self.vol = vol
         tf = tf2d_table() if cfg["tf"] == "2d" else tf_table(cfg["tf"])
         self.tfh, self.tfw = (tf.shape[0], tf.shape[1]) if tf.ndim == 3 else (0, tf.shape[0])
@@ -447,9 +453,26 @@ def run_ours(args):
     S_e, wall_e, lat_e, _, _, s0_e, s1_e = plain_pass(True)
     S_e.close()
     S, wall, lat, info, launches, s0, s1 = plain_pass(False)
+    with_bins = None
+    if not args.brick_bins:
+        # the same views with the value bins of every brick given to the cache:
+        # invisible missing bricks are stepped through, not loaded (images
+        # within the reference's own resume rounding; not its request sequence)
+        Session.brick_bins = True
+        S_b, wall_b, _, info_b, _, s0_b, s1_b = plain_pass(False)
+        Session.brick_bins = False
+        S_b.close()
+        with_bins = (wall_b, info_b, cache_delta(s0_b, s1_b))
     clk = clocks.stop()
     wall, wall_e = max_over_ranks([wall, wall_e], device="cuda")  # replicas: the slowest rank's time
     rays = W * H * args.steps * world
+    if with_bins:
+        wall_b, info_b, cd_b = with_bins
+        wall_b, = max_over_ranks([wall_b], device="cuda")
+        with_bins = {"value": round(rays / wall_b / 1e6, 3), "unit": "Mrays/s",
+                     "ms_per_step": round(1e3 * wall_b / args.steps, 4),
+                     "iterations_per_view": round(statistics.mean(i for i, _ in info_b), 2),
+                     "brick_h2d_bytes_per_step": int(cd_b["brick_h2d_bytes"] / args.steps), "cache": cd_b}
     iters = [i for i, _ in info]
     conv = sum(1 for _, c in info if c)
 
@@ -509,7 +532,7 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dt, "data": data_txt,
         "config": {"workload": wl, "brick_size": cfg["B"], "covering": cfg["c"], "pool_slots": list(S.pool),
                    "pool_gib": round(pool_bytes / 2**30, 3), "view": [W, H], "max_requests": args.max_requests,
-                   "loader": "sync", "upload": "gather kernel reading the host store"
+                   "brick_bins": bool(args.brick_bins), "loader": "sync", "upload": "gather kernel reading the host store"
                    if S.cm.stats().upload_direct else "staged host copies + cudaMemcpyAsync",
                    "l2": "inputs > L2 (2 GiB pool, 103 MB page directory, 28 GiB host brick store)"
                    if args.config == "c2" else ("inputs > L2 (8 GiB pool, 43 GiB host brick store)"
@@ -547,6 +570,8 @@ def run_ours(args):
         "cache": cache_delta(s0, s1),
         "clocks": clk,
     }
+    if with_bins:
+        out["with_brick_bins"] = with_bins
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(gc, S, cfg, last, args)
     S.close()
@@ -568,6 +593,7 @@ def cache_delta(s0, s1):
             "loader_host_ms": round((s1.loader_host_ns - s0.loader_host_ns) / 1e6, 2),
             "upload_ms": round(up_ms, 2), "upload_gbs": round(nbytes / (up_ms / 1e3) / 1e9, 1) if up_ms > 0 else None,
             "upload_route": "gather" if s1.upload_direct else "staged",
+            "samples": int(s1.samples - s0.samples),
             "device_error": int(s1.device_error)}
 
 
@@ -670,7 +696,7 @@ def run_c3(args):
            "data": "synthetic (seeded blobs + value noise, 2048^3 u16; no public dataset)",
            "config": {"workload": f"c3: {len(views)} views, batched (continuous batching), each to convergence",
                       "rays": int(rays), "reorder": args.reorder, "occupancy": args.occupancy,
-                      "admit": args.admit, "park_above": args.park, "overlap_loads": bool(args.overlap),
+                      "admit": args.admit, "park_above": args.park, "overlap_loads": bool(args.overlap), "brick_bins": bool(args.brick_bins),
                       "render_tuning": list(best),
                       "preprocess_s": round(prep_s, 2)},
            "batched": batched}
@@ -679,6 +705,17 @@ def run_c3(args):
         plain, _ = plain_views_pass(gc, torch, cfg, data, views, warm, args)
         out["plain_same_views"] = plain
         out["ratio"] = round(batched["value"] / plain["value"], 3)
+    if not args.brick_bins:  # both arms again with brick value bins given to the caches
+        Session.brick_bins = True
+        gc.render_tuning(*tune_b)
+        bb_, _ = batched_pass(gc, torch, cfg, data, views, warm, args)
+        bins = {"batched": bb_}
+        if not args.no_plain:
+            gc.render_tuning(*tune_p)
+            bins["plain_same_views"], _ = plain_views_pass(gc, torch, cfg, data, views, warm, args)
+            bins["ratio"] = round(bb_["value"] / bins["plain_same_views"]["value"], 3)
+        Session.brick_bins = False
+        out["with_brick_bins"] = bins
     print(json.dumps(out), flush=True)
 
 
@@ -723,6 +760,8 @@ def c4_serve(gc, torch, cfg, vols, stores, args):
                          shared=vols, staged_upload=args.upload == "staged")
     for k, (store, offs) in enumerate(stores):
         cm.set_source_host(store, offs, volume=k)
+        if Session.brick_bins:
+            cm.set_brick_bins(BRICK_BINS[store.data_ptr()], volume=k)
     tfs = [torch.from_numpy(tf_table(kind, seed).reshape(-1)).cuda()
            for kind, seed in (("ramp", 0), ("bumps", 3), ("bumps", 4), ("bumps", 5))]
     focal = 1.0 / math.tan(math.radians(cfg["fov"]) / 2)
@@ -786,7 +825,7 @@ def c4_serve(gc, torch, cfg, vols, stores, args):
                                   f"({cm.info.pool_bytes / 2**30:.1f} GiB), sizes {list(cfg['sizes'])}, 4 TFs",
                       "offered_mrays_per_s": round(rays / args.duration / 1e6, 2), "reorder": args.reorder,
                       "occupancy": args.occupancy, "admit": args.admit, "park_above": args.park,
-                      "overlap_loads": bool(args.overlap),
+                      "overlap_loads": bool(args.overlap), "brick_bins": bool(args.brick_bins),
                       "upload": "staged" if args.upload == "staged" else "gather",
                       "stores": "pinned" if PIN_STORES else "pageable",
                       "max_passes": args.batch_cap},
@@ -829,15 +868,27 @@ def run_batched(gc, torch, args):
     gc.render_tuning(*tune_p)
     plain, _ = plain_views_pass(gc, torch, cfg, data, views, warm, args)
     batched["render_tuning"], plain["render_tuning"] = list(tune_b), list(tune_p)
-    return {"config": {"workload": f"c3: {len(views)} views ({args.batches} x {cfg['batch']}), sizes "
+    bins = None
+    if not args.brick_bins:  # both arms again with brick value bins given to the caches
+        Session.brick_bins = True
+        gc.render_tuning(*tune_b)
+        bb_, _ = batched_pass(gc, torch, cfg, data, views, warm, args)
+        gc.render_tuning(*tune_p)
+        bp_, _ = plain_views_pass(gc, torch, cfg, data, views, warm, args)
+        Session.brick_bins = False
+        bins = {"batched": bb_, "plain_same_views": bp_, "ratio": round(bb_["value"] / bp_["value"], 3)}
+    out = {"config": {"workload": f"c3: {len(views)} views ({args.batches} x {cfg['batch']}), sizes "
                                    f"{list(cfg['sizes'])}, cameras at 0.5-3.0x diagonal; BrickSize 32, 4 GiB pool; "
                                    f"all submitted at t0, continuous batching with a {args.batch_pixels} pixel "
                                    f"budget, admission while demand (used + missing) <= {args.occupancy} of the "
                                    f"pool, <= {args.admit} admissions per tick, "
-                                   f"asynchronous loader",
+                                   f"asynchronous loader" + (", overlapped loads" if args.overlap else ""),
                        "preprocess_s": round(prep_s, 2), "rays": int(rays)},
             "unit": "Mrays/s", "batched": batched, "plain_same_views": plain,
             "ratio": round(batched["value"] / plain["value"], 3)}
+    if bins:
+        out["with_brick_bins"] = bins
+    return out
 
 
 def vol_bytes_per_voxel(cfg):
@@ -983,6 +1034,10 @@ def main():
                          "through the device's own mappings)")
     ap.add_argument("--park", type=float, default=0.0,
                     help="batched/serving: park the newest view while demand exceeds this fraction of the pool")
+    ap.add_argument("--brick-bins", action="store_true",
+                    help="give each cache the value bins of every brick: missing bricks the transfer function "
+                         "cannot make visible are stepped through, not loaded (same images; not the reference's "
+                         "request sequence)")
     ap.add_argument("--no-overlap", dest="overlap", action="store_false",
                     help="batched/serving: one brick load at a time (default: loads overlap rendering through "
                          "two miss lists with in-flight marks)")
@@ -995,6 +1050,7 @@ def main():
         args.steps = 40 if args.impl == "ours" else 2
     args.warmup = max(3, args.warmup)
     Session.staged = args.upload == "staged"
+    Session.brick_bins = args.brick_bins
     global PIN_STORES
     PIN_STORES = args.pin_stores
     if args.config != "c2":

@@ -50,6 +50,7 @@ struct CacheView {
     uint32_t nc;          // channels per voxel (1, or 2 for two 8-bit channels)
     uint64_t slot_bytes;  // pool slot stride: B^3 x the widest voxel
     const unsigned long long *slot_bins;  // per slot: value bins its voxels cover (empty-space skipping)
+    const unsigned long long *entry_bins; // per page-directory entry: its brick's value bins (nullptr: none given)
     unsigned long long *samples;          // running count of samples taken (resident-brick reads)
     uint32_t ts;
 };
@@ -140,6 +141,8 @@ void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s)
 // Copies brick i (src[i] = {device-readable host address, bytes}) to
 // dst + i * stride; vec16: every address, size and the stride are multiples
 // of 16.
+void launch_brick_bins(const uint8_t *level, const uint32_t nb[3], const uint32_t nbig[3], const uint32_t bb[3],
+                       uint32_t B, uint32_t eb, unsigned long long *bins, cudaStream_t s);
 void launch_gather_bricks(const ulonglong2 *src, uint32_t n, uint64_t stride, uint8_t *dst, bool vec16,
                           cudaStream_t s);
 // In-flight marks (page-directory flag 3) of the batched form's overlapped

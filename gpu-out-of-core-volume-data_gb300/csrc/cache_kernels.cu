@@ -259,6 +259,88 @@ __global__ void install_evict_kernel(InstallArgs a, const LevelTables lt) {
     if (e < a.nentries) a.mrpd[e] = make_uint4(0, 0, 0, 0);
 }
 
+// Value range of a brick as value bins (empty-space skipping): min and max
+// over its voxels (covering included), normalized like the samplers, widened
+// by one bin on either side.  `at(v)` gives the address of voxel v; one
+// block per brick (up to 256 threads); the result is valid in thread 0.
+template <class At>
+__device__ unsigned long long block_value_bins(uint32_t nvox, uint32_t eb, At at) {
+    float lo = 3.4e38f, hi = -3.4e38f;
+    for (uint32_t v = threadIdx.x; v < nvox; v += blockDim.x) {
+        const uint8_t *p = at(v);
+        float x;
+        if (eb == 1)
+            x = static_cast<float>(*p) * (1.0f / 255.0f);
+        else if (eb == 2)
+            x = static_cast<float>(*reinterpret_cast<const uint16_t *>(p)) * (1.0f / 65535.0f);
+        else
+            x = *reinterpret_cast<const float *>(p);
+        lo = fminf(lo, x);
+        hi = fmaxf(hi, x);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    __shared__ float s_lo[8], s_hi[8];
+    const uint32_t warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31u) == 0) {
+        s_lo[warp] = lo;
+        s_hi[warp] = hi;
+    }
+    __syncthreads();
+    unsigned long long bins = 0;
+    if (threadIdx.x == 0) {
+        for (uint32_t w = 1; w < (blockDim.x + 31) / 32; ++w) {
+            lo = fminf(lo, s_lo[w]);
+            hi = fmaxf(hi, s_hi[w]);
+        }
+        auto bin = [](float x) {
+            const float f = floorf(x * static_cast<float>(kValueBins));
+            return f < 0.f ? 0 : (f > kValueBins - 1.f ? static_cast<int>(kValueBins) - 1 : static_cast<int>(f));
+        };
+        const int b0 = max(bin(lo) - 1, 0), b1 = min(bin(hi) + 1, static_cast<int>(kValueBins) - 1);
+        const unsigned long long upto = b1 >= 63 ? ~0ull : ((1ull << (b1 + 1)) - 1ull);
+        bins = upto & ~((1ull << b0) - 1ull);
+    }
+    return bins;
+}
+
+// Value bins of every brick of one level, read from the level's big bricks
+// on the device: the mask the install computes for the same brick in a pool
+// slot.  One block per brick of the level's brick grid (x fastest).
+__global__ void __launch_bounds__(256) brick_bins_kernel(const uint8_t *__restrict__ level, uint32_t nbx, uint32_t nby,
+                                                         uint32_t nbz, uint32_t gbx, uint32_t gby, uint32_t bb0,
+                                                         uint32_t bb1, uint32_t bb2, uint32_t B, uint32_t eb,
+                                                         unsigned long long *bins) {
+    const uint64_t i = blockIdx.x;
+    const uint32_t x = static_cast<uint32_t>(i % nbx), y = static_cast<uint32_t>((i / nbx) % nby),
+                   z = static_cast<uint32_t>(i / (static_cast<uint64_t>(nbx) * nby));
+    if (z >= nbz) return;
+    const uint32_t gx = x / bb0, gy = y / bb1, gz = z / bb2;
+    const uint32_t bvx = bb0 * B, bvy = bb1 * B, bvz = bb2 * B;
+    const uint8_t *big =
+        level + ((static_cast<uint64_t>(gz) * gby + gy) * gbx + gx) * (static_cast<uint64_t>(bvx) * bvy * bvz * eb);
+    const uint32_t ox = (x - gx * bb0) * B, oy = (y - gy * bb1) * B, oz = (z - gz * bb2) * B;
+    const unsigned long long m = block_value_bins(B * B * B, eb, [&](uint32_t v) {
+        const uint32_t lx = v % B, ly = (v / B) % B, lz = v / (B * B);
+        return big + ((static_cast<uint64_t>(oz + lz) * bvy + (oy + ly)) * bvx + (ox + lx)) * eb;
+    });
+    if (threadIdx.x == 0) bins[i] = m;
+}
+
+void launch_brick_bins(const uint8_t *level, const uint32_t nb[3], const uint32_t nbig[3], const uint32_t bb[3],
+                       uint32_t B, uint32_t eb, unsigned long long *bins, cudaStream_t s) {
+    const uint64_t n = static_cast<uint64_t>(nb[0]) * nb[1] * nb[2];
+    if (n == 0) return;
+    GC_REQUIRE(n < (1ull << 31), "too many bricks in one level");
+    brick_bins_kernel<<<static_cast<uint32_t>(n), 256, 0, s>>>(level, nb[0], nb[1], nb[2], nbig[0], nbig[1], bb[0],
+                                                              bb[1], bb[2], B, eb, bins);
+    GC_CUDA(cudaGetLastError());
+    count_launch();
+}
+
 // compute_lru_volume_position + copy_lru_position + write_brick
 // (CacheManagerKernels.cu:90-114, CacheManagerKernels.hpp:59-107): one block
 // per non-empty brick copies B^3 voxels from the staged big brick into the
@@ -302,52 +384,13 @@ __global__ void __launch_bounds__(256) install_place_kernel(InstallArgs a, const
         }
     }
     if (!a.slot_bins) return;
-    // Value range of the brick, as value bins (empty-space skipping): min and
-    // max over its B^3 voxels (covering included), normalized like the
-    // samplers, widened by one bin on either side.
     __syncthreads();
     if (a.nc != 1) {
         if (threadIdx.x == 0) a.slot_bins[slot] = ~0ull;  // several channels: never skipped
         return;
     }
-    float lo = 3.4e38f, hi = -3.4e38f;
-    const uint32_t nvox = B * B * B;
-    for (uint32_t v = threadIdx.x; v < nvox; v += blockDim.x) {
-        float x;
-        if (eb == 1)
-            x = static_cast<float>(dst[v]) * (1.0f / 255.0f);
-        else if (eb == 2)
-            x = static_cast<float>(reinterpret_cast<const uint16_t *>(dst)[v]) * (1.0f / 65535.0f);
-        else
-            x = reinterpret_cast<const float *>(dst)[v];
-        lo = fminf(lo, x);
-        hi = fmaxf(hi, x);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-    }
-    __shared__ float s_lo[8], s_hi[8];
-    const uint32_t warp = threadIdx.x >> 5;
-    if ((threadIdx.x & 31u) == 0) {
-        s_lo[warp] = lo;
-        s_hi[warp] = hi;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (uint32_t w = 1; w < (blockDim.x + 31) / 32; ++w) {
-            lo = fminf(lo, s_lo[w]);
-            hi = fmaxf(hi, s_hi[w]);
-        }
-        auto bin = [](float x) {
-            const float f = floorf(x * static_cast<float>(kValueBins));
-            return f < 0.f ? 0 : (f > kValueBins - 1.f ? static_cast<int>(kValueBins) - 1 : static_cast<int>(f));
-        };
-        const int b0 = max(bin(lo) - 1, 0), b1 = min(bin(hi) + 1, static_cast<int>(kValueBins) - 1);
-        const unsigned long long upto = b1 >= 63 ? ~0ull : ((1ull << (b1 + 1)) - 1ull);
-        a.slot_bins[slot] = upto & ~((1ull << b0) - 1ull);
-    }
+    const unsigned long long bins = block_value_bins(B * B * B, eb, [&](uint32_t v) { return dst + v * eb; });
+    if (threadIdx.x == 0) a.slot_bins[slot] = bins;
 }
 
 // reference_new_bricks (CacheManagerKernels.hpp:308-357) for the MRPD-only

@@ -91,6 +91,7 @@ struct Volume {
     uint32_t level_base = 0;
     uint64_t brick_bytes = 0, big_bytes = 0;
     Source src;
+    std::vector<uint64_t> bins;  // value bins of every brick (all levels), empty: none given
 };
 
 }  // namespace gc
@@ -113,6 +114,8 @@ struct gc_cache {
     uint32_t *req = nullptr, *usage = nullptr, *order[2] = {nullptr, nullptr}, *slot_level = nullptr;
     float4 *slot_vpos = nullptr;
     unsigned long long *slot_bins = nullptr;  // value bins of each slot's brick (empty-space skipping)
+    unsigned long long *entry_bins = nullptr; // value bins of each entry's brick (given per volume), or null
+    bool entry_bins_dirty = false;
     unsigned long long *d_samples = nullptr;  // samples taken by the ray caster since creation
     uint8_t *pool = nullptr;
     uint64_t *status_lru = nullptr, *status_miss = nullptr;
@@ -434,6 +437,7 @@ static CacheView cache_view(const gc_cache *C) {
     cv.nc = C->nc;
     cv.slot_bytes = C->slot_bytes;
     cv.slot_bins = C->slot_bins;
+    cv.entry_bins = C->entry_bins;
     cv.samples = C->d_samples;
     cv.ts = C->ts;
     return cv;
@@ -548,7 +552,7 @@ static void destroy(gc_cache *C) {
     }
     cudaSetDevice(C->device);
     cudaDeviceSynchronize();
-    void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool, C->slot_bins, C->d_samples,
+    void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool, C->slot_bins, C->entry_bins, C->d_samples,
                    C->status_lru, C->status_miss, C->ctl_lru, C->ctl_miss, C->d_count, C->d_misc, C->d_queue,
                    C->lists[0].d, C->lists[1].d, C->d_asked, C->d_big_coord, C->d_big_index, C->d_src,
                    C->d_staging, C->d_views};
@@ -630,11 +634,51 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
 
 // graph + pinned view table: the batched form replays a CUDA graph instead
 // of launching (launch_render_graph)
+// Page-directory table of brick value bins from the volumes' bins: ~0 (never
+// skipped) for levels without bins and for the bricks of empty big bricks,
+// which step like empty bricks once installed and so must be requested.
+static void refresh_entry_bins(gc_cache *C, cudaStream_t s) {
+    if (!C->entry_bins_dirty) return;
+    C->entry_bins_dirty = false;
+    bool any = false;
+    for (const Volume &V : C->vols) any = any || !V.bins.empty();
+    if (!any) {
+        if (C->entry_bins) {
+            GC_CUDA(cudaStreamSynchronize(s));
+            GC_CUDA(cudaFree(C->entry_bins));
+            C->entry_bins = nullptr;
+        }
+        return;
+    }
+    std::vector<uint64_t> h(C->nentries, ~0ull);
+    for (const Volume &V : C->vols) {
+        if (V.bins.empty()) continue;
+        const gc_layout &L = V.layout;
+        const uint32_t *BB = V.desc.big_brick_size;
+        uint64_t k = 0;
+        for (uint32_t l = 0; l < L.nb_levels; ++l) {
+            const uint32_t lvl = V.level_base + l;
+            for (uint32_t z = 0; z < L.nb_bricks[l][2]; ++z)
+                for (uint32_t y = 0; y < L.nb_bricks[l][1]; ++y)
+                    for (uint32_t x = 0; x < L.nb_bricks[l][0]; ++x, ++k) {
+                        const uint64_t e = C->lt.off[lvl] + x + static_cast<uint64_t>(y) * C->mx +
+                                           static_cast<uint64_t>(z) * C->mx * C->my;
+                        const bool empty = V.src.empty.count(gc_brick_key(l, x / BB[0], y / BB[1], z / BB[2])) != 0;
+                        h[e] = empty ? ~0ull : V.bins[k];
+                    }
+        }
+    }
+    if (!C->entry_bins) C->entry_bins = dalloc<unsigned long long>(C->nentries, "page-directory value bins");
+    GC_CUDA(cudaMemcpyAsync(C->entry_bins, h.data(), C->nentries * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    GC_CUDA(cudaStreamSynchronize(s));
+}
+
 static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s, bool mark_done = false,
                    RenderGraph *graph = nullptr, ViewParams *pinned = nullptr) {
     GC_REQUIRE(views && n >= 1, "no views");
     GC_REQUIRE(n <= C->max_views, "too many views in one batch");
     GC_CUDA(cudaSetDevice(C->device));
+    refresh_entry_bins(C, s);
     std::vector<ViewParams> vp(n);
     uint32_t tiles = 0;
     for (uint32_t i = 0; i < n; ++i) {
@@ -874,6 +918,7 @@ int gc_cache_set_volume_source_host(gc_cache_t C, uint32_t volume, const void *b
         src.level_off.assign(level_offsets, level_offsets + L.nb_levels);
         for (size_t i = 0; i < n_empty; ++i) src.empty.insert(empty_keys[i]);
         update_upload_route(C);
+        C->entry_bins_dirty = true;
     });
 }
 
@@ -894,6 +939,7 @@ int gc_cache_set_volume_source_files(gc_cache_t C, uint32_t volume, const char *
         src.threads = threads;
         for (size_t i = 0; i < n_empty; ++i) src.empty.insert(empty_keys[i]);
         update_upload_route(C);
+        C->entry_bins_dirty = true;
     });
 }
 
@@ -911,6 +957,43 @@ int gc_cache_set_volume_source_callback(gc_cache_t C, uint32_t volume, gc_brick_
         src.user = user;
         for (size_t i = 0; i < n_empty; ++i) src.empty.insert(empty_keys[i]);
         update_upload_route(C);
+        C->entry_bins_dirty = true;
+    });
+}
+
+int gc_cache_set_volume_brick_bins(gc_cache_t C, uint32_t volume, const uint64_t *bins, uint64_t n) {
+    return guard([&] {
+        GC_REQUIRE(C && (bins || n == 0), "null argument");
+        GC_REQUIRE(volume < C->vols.size(), "no such volume in this cache");
+        Volume &V = C->vols[volume];
+        const gc_layout &L = V.layout;
+        uint64_t want = 0;
+        for (uint32_t l = 0; l < L.nb_levels; ++l)
+            want += static_cast<uint64_t>(L.nb_bricks[l][0]) * L.nb_bricks[l][1] * L.nb_bricks[l][2];
+        GC_REQUIRE(n == 0 || n == want, "brick bins: " + std::to_string(n) + " given, the volume has " +
+                                            std::to_string(want) + " bricks");
+        V.bins.assign(bins, bins + n);
+        C->entry_bins_dirty = true;
+    });
+}
+
+int gc_brick_value_bins(const gc_volume_desc *vol, const gc_layout *layout, uint32_t level, const void *level_bricks,
+                        uint64_t *bins, void *stream) {
+    return guard([&] {
+        GC_REQUIRE(vol && layout && level_bricks && bins, "null argument");
+        GC_REQUIRE(level < layout->nb_levels, "no such level");
+        const uint32_t *nb = layout->nb_bricks[level];
+        const uint64_t n = static_cast<uint64_t>(nb[0]) * nb[1] * nb[2];
+        cudaStream_t s = as_stream(stream);
+        if (vol->channels != 1) {  // the install never skips a multi-channel brick
+            GC_CUDA(cudaMemsetAsync(bins, 0xff, n * sizeof(uint64_t), s));
+            return;
+        }
+        GC_REQUIRE(vol->encoded_bytes == 1 || vol->encoded_bytes == 2 || vol->encoded_bytes == 4,
+                   "voxel width must be 1, 2 or 4 bytes");
+        launch_brick_bins(static_cast<const uint8_t *>(level_bricks), nb, layout->nb_big_bricks[level],
+                          vol->big_brick_size, vol->brick_size, vol->encoded_bytes,
+                          reinterpret_cast<unsigned long long *>(bins), s);
     });
 }
 

@@ -376,6 +376,13 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
     }
     if (e.w == 3u) return kUnmapped;  // on its way (batched form): already requested
     if (e.w == 0u) {
+        // A missing brick whose value bins (given for every brick) are all
+        // invisible: stepped through like a resident invisible brick, never
+        // requested.
+        if (cv.entry_bins) {
+            if (fresh) w.invisible = (__ldg(cv.entry_bins + idx) & visible) == 0ull;
+            if (w.invisible) return kInvisible;
+        }
         // raise_brick_request (K_CacheManager.hpp:364-396): same coordinates
         uint32_t *r = cv.req + idx;
         if (*r != cv.ts) *r = cv.ts;

@@ -123,6 +123,8 @@ _SIGS = {
     "gc_mip_build": [vp, P(Layout), P(C.c_uint64), C.c_uint32, C.c_uint32, vp],
     "gc_bricks_build": [vp, P(C.c_uint32), P(VolumeDesc), P(C.c_uint32), vp, vp],
     "gc_bricks_empty": [vp, C.c_uint64, P(VolumeDesc), C.c_float, vp, vp],
+    "gc_brick_value_bins": [P(VolumeDesc), P(Layout), C.c_uint32, vp, vp, vp],
+    "gc_cache_set_volume_brick_bins": [vp, C.c_uint32, P(C.c_uint64), C.c_uint64],
     "gc_brick_key": [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32],
     "gc_cache_create": [P(CacheDesc), P(vp)], "gc_cache_destroy": [vp],
     "gc_cache_set_source_host": [vp, vp, C.c_uint64, P(C.c_uint64), P(C.c_uint64), C.c_size_t],
@@ -306,6 +308,12 @@ def process_empty(bricks_ptr, nb_big, vol, threshold, flags_ptr, stream=0):
                               vp(stream)))
 
 
+def brick_value_bins(vol, layout, level, level_ptr, bins_ptr, stream=0):
+    """Value bins of every brick of one level (nb_bricks.x*y*z uint64 words,
+    x fastest) from the level's big bricks in device memory."""
+    check(lib.gc_brick_value_bins(C.byref(vol), C.byref(layout), level, vp(level_ptr), vp(bins_ptr), vp(stream)))
+
+
 def pyramid_offsets(layout, encoded_bytes, align=256):
     """Byte offsets of each level in one device buffer (level 0 first)."""
     offs, off = [], 0
@@ -328,7 +336,8 @@ def brick_store_offsets(layout, vol):
     return offs, off, big
 
 
-def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host", pin=False, timings=None):
+def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host", pin=False, timings=None,
+                value_bins=None):
     """Application::pre_process (Applications/DVR-ray-caster/src/Application.cu:148-197)
     run on the device: mip pyramid, bricking of every level and empty flags.
 
@@ -339,9 +348,12 @@ def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host
     values are all below empty_threshold (none when it is None, like the
     reference's default threshold 0).  timings (a dict) receives the seconds
     of the device mip build, the device bricking and the store copy.
+    value_bins (a list) receives one numpy uint64 array: the value bins of
+    every brick of every level, in the order CacheManager.set_brick_bins takes.
     """
     import time
 
+    import numpy as np
     import torch
 
     eb, nc = vol.encoded_bytes, vol.channels
@@ -374,6 +386,16 @@ def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host
             for i in torch.nonzero(flags).flatten().tolist():
                 x, y, z = i % nb[0], (i // nb[0]) % nb[1], i // (nb[0] * nb[1])
                 empty_keys.append(brick_key(l, x, y, z))
+    if value_bins is not None:
+        counts = [layout.nb_bricks[l][0] * layout.nb_bricks[l][1] * layout.nb_bricks[l][2]
+                  for l in range(layout.nb_levels)]
+        bins = torch.empty(sum(counts), dtype=torch.int64, device=dev)
+        at = 0
+        for l in range(layout.nb_levels):
+            brick_value_bins(vol, layout, l, bricks.data_ptr() + soffs[l], bins.data_ptr() + 8 * at, stream)
+            at += counts[l]
+        torch.cuda.synchronize(dev)
+        value_bins.append(bins.cpu().numpy().view(np.uint64))
     torch.cuda.synchronize(dev)
     t2 = time.perf_counter()
     if timings is not None:
@@ -528,6 +550,16 @@ class CacheManager:
         keys = (C.c_uint64 * max(1, len(empty_keys)))(*[int(k) for k in empty_keys])
         self._keep.append((offs, keys, store))
         check(lib.gc_cache_set_volume_source_host(self._h, volume, vp(ptr), size, offs, keys, len(empty_keys)))
+
+    def set_brick_bins(self, bins, volume=0):
+        """Value bins of every brick of the volume (pre_process(value_bins=...)):
+        missing bricks the transfer function cannot make visible are stepped
+        through, not loaded.  None or empty removes them."""
+        import numpy as np
+
+        a = np.ascontiguousarray(np.asarray([] if bins is None else bins, dtype=np.uint64))
+        self._keep.append(a)
+        check(lib.gc_cache_set_volume_brick_bins(self._h, volume, a.ctypes.data_as(P(C.c_uint64)), a.size))
 
     def set_source_files(self, volume_dir, empty_keys=(), volume=0, threads=0):
         """The reference's brick files under volume_dir, read by the loader."""

@@ -258,6 +258,27 @@ int gc_cache_set_volume_source_host(gc_cache_t cache, uint32_t volume, const voi
                                     const uint64_t *level_offsets, const uint64_t *empty_keys, size_t n_empty);
 int gc_cache_set_volume_source_callback(gc_cache_t cache, uint32_t volume, gc_brick_loader_fn fn, void *user,
                                         const uint64_t *empty_keys, size_t n_empty);
+/* Brick value bins (an extension; the reference has none).  Bit b of a
+ * brick's word is set when its voxel values (covering included) reach value
+ * bin b of 64 over [0, 1], widened by one bin on either side -- the mask the
+ * ray caster's empty-space skipping keeps per pool slot.  Given for every
+ * brick of a volume (n = sum over levels of nb_bricks.x*y*z; level order, x
+ * fastest within a level), a ray steps through a MISSING brick whose bins its
+ * transfer function cannot make visible, as it does through a resident one,
+ * instead of stopping to request it: such bricks are never loaded.  Images
+ * are the same; the requests, the loads and the cache state are not the
+ * reference's.  The bricks of the volume's empty big bricks are always
+ * requested (an empty brick steps by the base step), so a callback source
+ * that reports more bricks empty than its empty keys name must give those
+ * bricks all bits set.  n = 0 removes the volume's bins.  Takes effect at the
+ * next render. */
+int gc_cache_set_volume_brick_bins(gc_cache_t cache, uint32_t volume, const uint64_t *bins, uint64_t n);
+/* The value bins of every brick of one level (nb_bricks.x*y*z words, x
+ * fastest) from the level's big bricks in device memory (the layout
+ * gc_bricks_build writes), into device memory bins; all bits set for a
+ * volume of several channels. */
+int gc_brick_value_bins(const gc_volume_desc *vol, const gc_layout *layout, uint32_t level, const void *level_bricks,
+                        uint64_t *bins, void *stream);
 /* CacheManager::update (CacheManager.hpp:318-354).  *converged = 1 when the
  * request list was empty this frame. */
 int gc_cache_update(gc_cache_t cache, void *stream, int *converged);
