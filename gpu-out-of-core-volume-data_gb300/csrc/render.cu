@@ -170,16 +170,17 @@ __device__ __forceinline__ float sample_corner(const T *__restrict__ b, uint32_t
     ly = ly > 0 ? ly : 1u;
     lz = lz > 0 ? lz : 1u;
     const uint32_t i0 = ((lz - 1) * B + (ly - 1)) * B + (lx - 1);
-    const uint32_t BB = B * B;
+    // the four x pairs of the 2x2x2 block: rows y, y+1 of slices z, z+1
+    const T *p0 = b + i0;
+    const T *p1 = p0 + B, *p2 = p0 + B * B;
+    const T *p3 = p2 + B;
     if constexpr (sizeof(T) < 4) {
-        const uint32_t s = static_cast<uint32_t>(__ldg(b + i0)) + __ldg(b + i0 + 1) + __ldg(b + i0 + B) +
-                           __ldg(b + i0 + B + 1) + __ldg(b + i0 + BB) + __ldg(b + i0 + BB + 1) +
-                           __ldg(b + i0 + BB + B) + __ldg(b + i0 + BB + B + 1);
+        const uint32_t s = static_cast<uint32_t>(__ldg(p0)) + __ldg(p0 + 1) + __ldg(p1) + __ldg(p1 + 1) + __ldg(p2) +
+                           __ldg(p2 + 1) + __ldg(p3) + __ldg(p3 + 1);
         return static_cast<float>(s) / VoxelTraits<T>::kSum8;
     } else {
-        const float s = ((__ldg(b + i0) + __ldg(b + i0 + 1)) + (__ldg(b + i0 + B) + __ldg(b + i0 + B + 1))) +
-                        ((__ldg(b + i0 + BB) + __ldg(b + i0 + BB + 1)) +
-                         (__ldg(b + i0 + BB + B) + __ldg(b + i0 + BB + B + 1)));
+        const float s = ((__ldg(p0) + __ldg(p0 + 1)) + (__ldg(p1) + __ldg(p1 + 1))) +
+                        ((__ldg(p2) + __ldg(p2 + 1)) + (__ldg(p3) + __ldg(p3 + 1)));
         return s * 0.125f;
     }
 }
@@ -234,7 +235,8 @@ enum Status { kMapped = 0, kUnmapped = 1, kEmpty = 2, kInvisible = 3, kCoarser =
 // Per-thread page-walk state (K_CacheManager::_previousCoords / _previousEntries).
 struct Walk {
     uint32_t pcx, pcy, pcz;
-    uint4 entry;
+    uint32_t flag;   // flag of the entry last read (0 unmapped, 1 mapped, 2 empty, 3 in flight)
+    uint32_t slot;   // pool slot of a mapped entry (decoded when the entry is read)
     bool invisible;  // the mapped brick holds no value the view's transfer function shows
 };
 
@@ -254,9 +256,11 @@ struct SampleOf<TwoU8> {
 };
 __device__ __forceinline__ float first_channel(float s) { return s; }
 __device__ __forceinline__ float first_channel(float2 s) { return s.x; }
-__device__ __forceinline__ float4 classify(const ViewParams &vp, float s) { return tf_lookup(vp.tf, vp.tfw, s); }
-__device__ __forceinline__ float4 classify(const ViewParams &vp, float2 s) {
-    return tf2d_lookup(vp.tf, vp.tfw, vp.tfh, s.x, s.y);
+__device__ __forceinline__ float4 classify(const float *tf, uint32_t tfw, const ViewParams &, float s) {
+    return tf_lookup(tf, tfw, s);
+}
+__device__ __forceinline__ float4 classify(const float *tf, uint32_t tfw, const ViewParams &vp, float2 s) {
+    return tf2d_lookup(tf, tfw, vp.tfh, s.x, s.y);
 }
 
 template <typename T>
@@ -340,9 +344,11 @@ __device__ __forceinline__ typename SampleOf<T>::type sample_any(const uint8_t *
 // view's level base + its LOD): K_CacheManager::get_normalized
 // (K_CacheManager.hpp:265-361).
 template <typename T>
-__device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt, uint32_t sampler, uint32_t eb,
-                                     unsigned long long visible, uint32_t lvl, uint32_t lvl_end, bool fallback,
-                                     V3 np, Walk &w, typename SampleOf<T>::type &sample) {
+__device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt, uint32_t sampler,
+                                     const ViewParams &vp, uint32_t lvl, uint32_t lvl_end, V3 np, Walk &w,
+                                     typename SampleOf<T>::type &sample) {
+    // read where used (rare paths): the view's voxel width (mixed pools), its
+    // visible bins (a newly entered brick) and its fallback flag (a missing one)
     const float px = np.x * lt.ior[lvl][0];
     const float py = np.y * lt.ior[lvl][1];
     const float pz = np.z * lt.ior[lvl][2];
@@ -352,35 +358,39 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
     const uint64_t idx = cx + static_cast<uint64_t>(cy) * cv.mx + static_cast<uint64_t>(cz) * cv.mx * cv.my;
     bool fresh = false;
     if (cx != w.pcx || cy != w.pcy || cz != w.pcz) {
-        w.entry = __ldg(cv.mrpd + idx);
+        const uint4 e = __ldg(cv.mrpd + idx);
         w.pcx = cx;
         w.pcy = cy;
         w.pcz = cz;
+        w.flag = e.w;
         fresh = true;
+        if (e.w == 1u) {
+            const uint32_t B = cv.B;
+            w.slot = e.x / B + (e.y / B) * cv.sx + (e.z / B) * cv.sx * cv.sy;
+        }
     }
-    const uint4 e = w.entry;
-    if (e.w == 1u) {
-        const uint32_t B = cv.B;
-        const uint32_t slot = e.x / B + (e.y / B) * cv.sx + (e.z / B) * cv.sx * cv.sy;
+    const uint32_t flag = w.flag;
+    if (flag == 1u) {
+        const uint32_t slot = w.slot;
         if (fresh) {
             uint32_t *u = cv.usage + slot;
             if (*u != cv.ts) *u = cv.ts;
-            w.invisible = (__ldg(cv.slot_bins + slot) & visible) == 0ull;
+            w.invisible = (__ldg(cv.slot_bins + slot) & vp.visible) == 0ull;
         }
         if (w.invisible) return kInvisible;  // no sample of this brick reaches the compositing threshold
         const float fx = px * static_cast<float>(lt.vvox[lvl][0]);
         const float fy = py * static_cast<float>(lt.vvox[lvl][1]);
         const float fz = pz * static_cast<float>(lt.vvox[lvl][2]);
-        sample = sample_any<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, eb, cv, sampler, fx, fy, fz);
+        sample = sample_any<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, vp.eb, cv, sampler, fx, fy, fz);
         return kMapped;
     }
-    if (e.w == 3u) return kUnmapped;  // on its way (batched form): already requested
-    if (e.w == 0u) {
+    if (flag == 3u) return kUnmapped;  // on its way (batched form): already requested
+    if (flag == 0u) {
         // A missing brick whose value bins (given for every brick) are all
         // invisible: stepped through like a resident invisible brick, never
         // requested.
         if (cv.entry_bins) {
-            if (fresh) w.invisible = (__ldg(cv.entry_bins + idx) & visible) == 0ull;
+            if (fresh) w.invisible = (__ldg(cv.entry_bins + idx) & vp.visible) == 0ull;
             if (w.invisible) return kInvisible;
         }
         // raise_brick_request (K_CacheManager.hpp:364-396): same coordinates
@@ -389,7 +399,7 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
         // Coarser-level fallback (K_CacheManager::get, K_CacheManager.hpp:163-260):
         // the request stays on the asked level; the first mapped coarser level
         // of the volume is sampled instead, an empty one ends the lookup.
-        for (uint32_t l2 = lvl + 1; fallback && l2 < lvl_end; ++l2) {
+        for (uint32_t l2 = lvl + 1; vp.fallback != 0u && l2 < lvl_end; ++l2) {
             const float qx = np.x * lt.ior[l2][0], qy = np.y * lt.ior[l2][1], qz = np.z * lt.ior[l2][2];
             const uint32_t c2x = lt.off[l2] + static_cast<uint32_t>(qx * static_cast<float>(lt.nb[l2][0]));
             const uint32_t c2y = static_cast<uint32_t>(qy * static_cast<float>(lt.nb[l2][1]));
@@ -402,7 +412,7 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
             const uint32_t slot = e2.x / B + (e2.y / B) * cv.sx + (e2.z / B) * cv.sx * cv.sy;
             uint32_t *u = cv.usage + slot;
             if (*u != cv.ts) *u = cv.ts;
-            sample = sample_any<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, eb, cv, sampler,
+            sample = sample_any<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, vp.eb, cv, sampler,
                                    qx * static_cast<float>(lt.vvox[l2][0]), qy * static_cast<float>(lt.vvox[l2][1]),
                                    qz * static_cast<float>(lt.vvox[l2][2]));
             return kCoarser;
@@ -421,6 +431,15 @@ struct Ray {
     float t, tfar, endX, endY, sL, sU, maxOp;
     float4 fc;
     uint32_t lod;
+    // The view's per-sample parameters, read once per ray: the march stores
+    // to global memory (usage and request stamps), so reads through the view
+    // pointer would be repeated at every step.  step, afloor and kexp belong
+    // to the current level of detail.
+    float early, step, afloor, kexp;
+    const float *tf;
+    uint32_t tfw;
+    uint32_t lvl, lvl_end;  // cache level of the current LOD; end of the view's levels
+    uint32_t sampler;
     Walk w;
     bool unm, dvr;
     bool coarse;  // a coarser level stood in for a missing brick (fallback mode)
@@ -508,8 +527,18 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
         r.sL = length(dirLeft * n1);
         r.sU = length(dirUp * n1);
     }
+    r.early = vp.early;
+    r.step = vp.step[0];
+    r.afloor = vp.alpha_floor[0];
+    r.kexp = vp.kexp[0];
+    r.tf = vp.tf;
+    r.tfw = vp.tfw;
+    r.lvl = vp.level_base;
+    r.lvl_end = vp.level_base + vp.nlevels;
+    r.sampler = vp.sampler;
     r.w.pcx = r.w.pcy = r.w.pcz = UINT_MAX;
-    r.w.entry = make_uint4(0, 0, 0, 0);
+    r.w.flag = 0;
+    r.w.slot = 0;
     r.w.invisible = false;
     r.maxOp = r.dvr ? 0.f : vp.state[4 * i];
     return true;
@@ -520,33 +549,40 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
 template <typename T>
 __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables &lt, Ray &r) {
     const ViewParams &vp = *r.vp;
-    if (!((!r.dvr || r.fc.w < vp.early) && r.t < r.tfar)) return false;
-    const float alpha = r.t / r.tfar;
-    const float pX = r.endX * alpha;
-    const float pY = r.endY * alpha;
+    if (!((!r.dvr || r.fc.w < r.early) && r.t < r.tfar)) return false;
     V3 tp = fma3(r.pos, 0.495f, v3(0.495f, 0.495f, 0.495f));
     tp.z = 1.0f - tp.z;
     const V3 np = v3(clampf(tp.x, 0.f, 0.99f), clampf(tp.y, 0.f, 0.99f), clampf(tp.z, 0.f, 0.99f));
     // compute_LOD: the level only grows along a ray because the pixel
-    // footprint grows with t, so the scan resumes at the current level.
-    const uint32_t nl = vp.nlevels;
-    while (r.lod + 1 < nl && !(r.sL >= pX || r.sU >= pY)) {
-        ++r.lod;
-        if (r.lod + 1 < nl) {
-            const V3 nn = v3(vp.inv_size[r.lod + 1][0], vp.inv_size[r.lod + 1][1], vp.inv_size[r.lod + 1][2]);
-            r.sL = length(r.dirLeft * nn);
-            r.sU = length(r.dirUp * nn);
+    // footprint grows with t, so the scan resumes at the current level (and
+    // the footprint is not needed once the ray is at the coarsest level).
+    if (r.lvl + 1 < r.lvl_end) {
+        const float alpha = r.t / r.tfar;
+        const float pX = r.endX * alpha;
+        const float pY = r.endY * alpha;
+        if (!(r.sL >= pX || r.sU >= pY)) {
+            do {
+                ++r.lod;
+                ++r.lvl;
+                if (r.lvl + 1 < r.lvl_end) {
+                    const V3 nn =
+                        v3(vp.inv_size[r.lod + 1][0], vp.inv_size[r.lod + 1][1], vp.inv_size[r.lod + 1][2]);
+                    r.sL = length(r.dirLeft * nn);
+                    r.sU = length(r.dirUp * nn);
+                }
+            } while (r.lvl + 1 < r.lvl_end && !(r.sL >= pX || r.sU >= pY));
+            r.step = vp.step[r.lod];
+            r.afloor = vp.alpha_floor[r.lod];
+            r.kexp = vp.kexp[r.lod];
         }
     }
-    const uint32_t lod = r.lod;
     typename SampleOf<T>::type sample{};
-    const int st = fetch<T>(cv, lt, vp.sampler, vp.eb, vp.visible, vp.level_base + lod, vp.level_base + vp.nlevels,
-                            vp.fallback != 0u, np, r.w, sample);
+    const int st = fetch<T>(cv, lt, r.sampler, vp, r.lvl, r.lvl_end, np, r.w, sample);
     if (st == kCoarser) r.coarse = true;  // sampled below; the image is a preview
     if (st == kMapped || st == kCoarser) ++r.nsamp;
     if (st == kInvisible) {  // the step of a sample whose opacity stays below 0.001
-        r.t += vp.step[lod];
-        r.pos = fma3(r.dir, vp.step[lod], r.pos);
+        r.t += r.step;
+        r.pos = fma3(r.dir, r.step, r.pos);
         return true;
     }
     if (st != kMapped && st != kCoarser) {
@@ -565,11 +601,11 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
         return true;
     }
     if (r.dvr) {
-        float4 col = classify(vp, sample);
+        float4 col = classify(r.tf, r.tfw, vp, sample);
         // Opacity correction 1 - (1 - a)^k.  For a <= alpha_floor[lod] the
         // corrected opacity is below 1.05 k a <= 0.0009, under the compositing
         // threshold: the correction is skipped, the result is the same.
-        col.w = col.w > vp.alpha_floor[lod] ? 1.0f - gc_pow(1.0f - col.w, vp.kexp[lod]) : 0.0f;
+        col.w = col.w > r.afloor ? 1.0f - gc_pow(1.0f - col.w, r.kexp) : 0.0f;
         if (col.w > 0.001f) {
             col.x *= col.w;
             col.y *= col.w;
@@ -583,8 +619,8 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
     } else {
         r.maxOp = fmaxf(r.maxOp, first_channel(sample));
     }
-    r.t += vp.step[lod];
-    r.pos = fma3(r.dir, vp.step[lod], r.pos);
+    r.t += r.step;
+    r.pos = fma3(r.dir, r.step, r.pos);
     return true;
 }
 
