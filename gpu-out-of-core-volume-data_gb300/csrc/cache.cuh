@@ -49,8 +49,12 @@ struct CacheView {
     uint32_t eb;          // bytes per voxel of every volume, 0 when the volumes differ
     uint32_t nc;          // channels per voxel (1, or 2 for two 8-bit channels)
     uint64_t slot_bytes;  // pool slot stride: B^3 x the widest voxel
-    const unsigned long long *slot_bins;  // per slot: value bins its voxels cover (empty-space skipping)
-    const unsigned long long *entry_bins; // per page-directory entry: its brick's value bins (nullptr: none given)
+    // per page-directory entry, read beside the entry: the value bins of a
+    // mapped entry's brick (written by the install), the user's bins of the
+    // brick where given (gc_cache_set_volume_brick_bins), else all bits
+    const unsigned long long *entry_bins;
+    uint32_t bins_user;   // an unmapped entry with invisible bins is stepped through (user bins given)
+    uint32_t b_shift;     // log2(B) when B is a power of two, else 32 (divide)
     unsigned long long *samples;          // running count of samples taken (resident-brick reads)
     uint32_t ts;
 };
@@ -126,6 +130,8 @@ struct InstallArgs {
     float4 *slot_vpos;
     uint8_t *pool;
     unsigned long long *slot_bins;  // per slot value-bin mask, written with the brick
+    unsigned long long *entry_bins; // per page-directory entry (see CacheView::entry_bins)
+    const unsigned long long *user_bins;  // the user's per-entry bins, or null
     uint32_t nc;               // channels per voxel (bins only for one channel)
     uint64_t slot_bytes;       // pool slot stride
     uint64_t big_stride;       // staging stride of one big brick
@@ -138,6 +144,11 @@ struct InstallArgs {
     uint32_t n, n_nonempty;
 };
 void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s);
+// Rebuilds the per-entry bins after the user's bins changed: user (or all
+// bits) everywhere, then the bins of every resident brick at its entry.
+void launch_live_bins(const LevelTables &lt, const float4 *slot_vpos, const uint32_t *slot_level,
+                      const unsigned long long *slot_bins, uint32_t nslots, uint32_t mx, uint32_t my,
+                      uint64_t nentries, unsigned long long *entry_bins, cudaStream_t s);
 // Copies brick i (src[i] = {device-readable host address, bytes}) to
 // dst + i * stride; vec16: every address, size and the stride are multiples
 // of 16.

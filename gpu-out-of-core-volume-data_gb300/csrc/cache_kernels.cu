@@ -256,7 +256,10 @@ __global__ void install_evict_kernel(InstallArgs a, const LevelTables lt) {
     const float4 vp = a.slot_vpos[slot];
     if (vp.x < 0.f) return;  // slot never held a brick
     const uint64_t e = mrpd_index(lt, a.slot_level[slot], vp.x, vp.y, vp.z, a.mx, a.my);
-    if (e < a.nentries) a.mrpd[e] = make_uint4(0, 0, 0, 0);
+    if (e < a.nentries) {
+        a.mrpd[e] = make_uint4(0, 0, 0, 0);
+        a.entry_bins[e] = a.user_bins ? a.user_bins[e] : ~0ull;
+    }
 }
 
 // Value range of a brick as value bins (empty-space skipping): min and max
@@ -423,6 +426,7 @@ __global__ void __launch_bounds__(1024) install_reference_kernel(InstallArgs a, 
             const uint32_t slot = a.order[a.nslots - a.n_nonempty + i];
             const uint32_t sx = slot % a.sx, sy = (slot / a.sx) % a.sy, sz = slot / (a.sx * a.sy);
             a.mrpd[c] = make_uint4(sx * a.B, sy * a.B, sz * a.B, 1u);
+            a.entry_bins[c] = a.slot_bins[slot];
         } else {
             a.mrpd[c] = make_uint4(0, 0, 0, 2u);
         }
@@ -464,6 +468,27 @@ void launch_miss_compact(const uint32_t *req, uint64_t nscan, uint32_t ts, uint3
                          uint32_t epoch, cudaStream_t s) {
     miss_compact_kernel<<<lookback_tiles(nscan), kThreads, 0, s>>>(req, nscan, ts, maxreq, list, lt, mx, my,
                                                                    status, ctl, epoch);
+    GC_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+__global__ void live_bins_kernel(const LevelTables lt, const float4 *__restrict__ slot_vpos,
+                                 const uint32_t *__restrict__ slot_level,
+                                 const unsigned long long *__restrict__ slot_bins, uint32_t nslots, uint32_t mx,
+                                 uint32_t my, uint64_t nentries, unsigned long long *entry_bins) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += gridDim.x * blockDim.x) {
+        const float4 vp = slot_vpos[i];
+        if (vp.x < 0.f) continue;  // slot never held a brick
+        const uint64_t e = mrpd_index(lt, slot_level[i], vp.x, vp.y, vp.z, mx, my);
+        if (e < nentries) entry_bins[e] = slot_bins[i];
+    }
+}
+
+void launch_live_bins(const LevelTables &lt, const float4 *slot_vpos, const uint32_t *slot_level,
+                      const unsigned long long *slot_bins, uint32_t nslots, uint32_t mx, uint32_t my,
+                      uint64_t nentries, unsigned long long *entry_bins, cudaStream_t s) {
+    const uint32_t grid = std::max(1u, std::min<uint32_t>(div_up(nslots, 256), static_cast<uint32_t>(sm_count()) * 4));
+    live_bins_kernel<<<grid, 256, 0, s>>>(lt, slot_vpos, slot_level, slot_bins, nslots, mx, my, nentries, entry_bins);
     GC_CUDA(cudaGetLastError());
     count_launch();
 }

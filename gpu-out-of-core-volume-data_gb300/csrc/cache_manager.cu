@@ -114,7 +114,9 @@ struct gc_cache {
     uint32_t *req = nullptr, *usage = nullptr, *order[2] = {nullptr, nullptr}, *slot_level = nullptr;
     float4 *slot_vpos = nullptr;
     unsigned long long *slot_bins = nullptr;  // value bins of each slot's brick (empty-space skipping)
-    unsigned long long *entry_bins = nullptr; // value bins of each entry's brick (given per volume), or null
+    unsigned long long *entry_bins = nullptr; // per entry: resident brick's bins, else the user's, else ~0
+    unsigned long long *user_bins = nullptr;  // per entry: the user's brick bins (given per volume), or null
+    uint32_t b_shift = 32;                     // log2(B) for a power-of-two brick size
     bool entry_bins_dirty = false;
     unsigned long long *d_samples = nullptr;  // samples taken by the ray caster since creation
     uint8_t *pool = nullptr;
@@ -436,8 +438,9 @@ static CacheView cache_view(const gc_cache *C) {
     cv.eb = C->eb;
     cv.nc = C->nc;
     cv.slot_bytes = C->slot_bytes;
-    cv.slot_bins = C->slot_bins;
     cv.entry_bins = C->entry_bins;
+    cv.bins_user = C->user_bins ? 1u : 0u;
+    cv.b_shift = C->b_shift;
     cv.samples = C->d_samples;
     cv.ts = C->ts;
     return cv;
@@ -470,6 +473,8 @@ static void install(gc_cache *C, cudaStream_t s) {
     a.slot_bytes = C->slot_bytes;
     a.big_stride = C->big_stride;
     a.slot_bins = C->slot_bins;
+    a.entry_bins = C->entry_bins;
+    a.user_bins = C->user_bins;
     a.nc = C->nc;
     a.asked = C->d_asked;
     a.big_index = C->d_big_index;
@@ -552,7 +557,7 @@ static void destroy(gc_cache *C) {
     }
     cudaSetDevice(C->device);
     cudaDeviceSynchronize();
-    void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool, C->slot_bins, C->entry_bins, C->d_samples,
+    void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool, C->slot_bins, C->entry_bins, C->user_bins, C->d_samples,
                    C->status_lru, C->status_miss, C->ctl_lru, C->ctl_miss, C->d_count, C->d_misc, C->d_queue,
                    C->lists[0].d, C->lists[1].d, C->d_asked, C->d_big_coord, C->d_big_index, C->d_src,
                    C->d_staging, C->d_views};
@@ -634,20 +639,26 @@ static void fill_view(const gc_cache *C, const gc_view &in, ViewParams &out) {
 
 // graph + pinned view table: the batched form replays a CUDA graph instead
 // of launching (launch_render_graph)
-// Page-directory table of brick value bins from the volumes' bins: ~0 (never
-// skipped) for levels without bins and for the bricks of empty big bricks,
-// which step like empty bricks once installed and so must be requested.
+// Page-directory table of the user's brick value bins from the volumes' bins:
+// ~0 (never skipped) for levels without bins and for the bricks of empty big
+// bricks, which step like empty bricks once installed and so must be
+// requested.  The per-entry table the ray caster reads is then rebuilt: the
+// user's bins, with every resident brick's own bins at its entry.
 static void refresh_entry_bins(gc_cache *C, cudaStream_t s) {
     if (!C->entry_bins_dirty) return;
     C->entry_bins_dirty = false;
     bool any = false;
     for (const Volume &V : C->vols) any = any || !V.bins.empty();
+    GC_CUDA(cudaStreamSynchronize(s));
     if (!any) {
-        if (C->entry_bins) {
-            GC_CUDA(cudaStreamSynchronize(s));
-            GC_CUDA(cudaFree(C->entry_bins));
-            C->entry_bins = nullptr;
+        if (C->user_bins) {
+            GC_CUDA(cudaFree(C->user_bins));
+            C->user_bins = nullptr;
         }
+        GC_CUDA(cudaMemsetAsync(C->entry_bins, 0xff, C->nentries * sizeof(uint64_t), s));
+        launch_live_bins(C->lt, C->slot_vpos, C->slot_level, C->slot_bins, C->nslots, C->mx, C->my, C->nentries,
+                         C->entry_bins, s);
+        GC_CUDA(cudaStreamSynchronize(s));
         return;
     }
     std::vector<uint64_t> h(C->nentries, ~0ull);
@@ -668,8 +679,11 @@ static void refresh_entry_bins(gc_cache *C, cudaStream_t s) {
                     }
         }
     }
-    if (!C->entry_bins) C->entry_bins = dalloc<unsigned long long>(C->nentries, "page-directory value bins");
-    GC_CUDA(cudaMemcpyAsync(C->entry_bins, h.data(), C->nentries * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    if (!C->user_bins) C->user_bins = dalloc<unsigned long long>(C->nentries, "page-directory user bins");
+    GC_CUDA(cudaMemcpyAsync(C->user_bins, h.data(), C->nentries * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    GC_CUDA(cudaMemcpyAsync(C->entry_bins, C->user_bins, C->nentries * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+    launch_live_bins(C->lt, C->slot_vpos, C->slot_level, C->slot_bins, C->nslots, C->mx, C->my, C->nentries,
+                     C->entry_bins, s);
     GC_CUDA(cudaStreamSynchronize(s));
 }
 
@@ -807,6 +821,11 @@ int gc_cache_create_shared(const gc_cache_desc *desc, const gc_volume_desc *volu
         C->slot_vpos = dalloc<float4>(C->nslots, "slot positions");
         C->pool = dalloc<uint8_t>(C->nslots * C->slot_bytes, "brick pool");
         C->slot_bins = dalloc<unsigned long long>(C->nslots, "slot value bins");
+        C->entry_bins = dalloc<unsigned long long>(C->nentries, "page-directory value bins");
+        GC_CUDA(cudaMemset(C->entry_bins, 0xff, C->nentries * sizeof(unsigned long long)));
+        C->b_shift = 32;
+        for (uint32_t k = 0; k < 31; ++k)
+            if ((1u << k) == C->B) C->b_shift = k;
         C->d_samples = dalloc<unsigned long long>(1, "sample counter");
         GC_CUDA(cudaMemset(C->d_samples, 0, sizeof(unsigned long long)));
         GC_CUDA(cudaMemset(C->slot_bins, 0xff, C->nslots * sizeof(unsigned long long)));

@@ -356,27 +356,28 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
     const uint32_t cy = static_cast<uint32_t>(py * static_cast<float>(lt.nb[lvl][1]));
     const uint32_t cz = static_cast<uint32_t>(pz * static_cast<float>(lt.nb[lvl][2]));
     const uint64_t idx = cx + static_cast<uint64_t>(cy) * cv.mx + static_cast<uint64_t>(cz) * cv.mx * cv.my;
-    bool fresh = false;
     if (cx != w.pcx || cy != w.pcy || cz != w.pcz) {
+        // A new entry: the entry and its value bins are read together (one
+        // memory round trip); the usage stamp of a mapped brick is a plain
+        // store (idempotent, like the reference's per-sample stamp).
         const uint4 e = __ldg(cv.mrpd + idx);
+        const unsigned long long bins = __ldg(cv.entry_bins + idx);
         w.pcx = cx;
         w.pcy = cy;
         w.pcz = cz;
         w.flag = e.w;
-        fresh = true;
+        w.invisible = (bins & vp.visible) == 0ull && (e.w == 1u || (e.w == 0u && cv.bins_user));
         if (e.w == 1u) {
             const uint32_t B = cv.B;
-            w.slot = e.x / B + (e.y / B) * cv.sx + (e.z / B) * cv.sx * cv.sy;
+            w.slot = cv.b_shift < 32u ? (e.x >> cv.b_shift) + (e.y >> cv.b_shift) * cv.sx +
+                                            (e.z >> cv.b_shift) * cv.sx * cv.sy
+                                      : e.x / B + (e.y / B) * cv.sx + (e.z / B) * cv.sx * cv.sy;
+            cv.usage[w.slot] = cv.ts;
         }
     }
     const uint32_t flag = w.flag;
     if (flag == 1u) {
         const uint32_t slot = w.slot;
-        if (fresh) {
-            uint32_t *u = cv.usage + slot;
-            if (*u != cv.ts) *u = cv.ts;
-            w.invisible = (__ldg(cv.slot_bins + slot) & vp.visible) == 0ull;
-        }
         if (w.invisible) return kInvisible;  // no sample of this brick reaches the compositing threshold
         const float fx = px * static_cast<float>(lt.vvox[lvl][0]);
         const float fy = py * static_cast<float>(lt.vvox[lvl][1]);
@@ -389,13 +390,9 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
         // A missing brick whose value bins (given for every brick) are all
         // invisible: stepped through like a resident invisible brick, never
         // requested.
-        if (cv.entry_bins) {
-            if (fresh) w.invisible = (__ldg(cv.entry_bins + idx) & vp.visible) == 0ull;
-            if (w.invisible) return kInvisible;
-        }
+        if (w.invisible) return kInvisible;
         // raise_brick_request (K_CacheManager.hpp:364-396): same coordinates
-        uint32_t *r = cv.req + idx;
-        if (*r != cv.ts) *r = cv.ts;
+        cv.req[idx] = cv.ts;
         // Coarser-level fallback (K_CacheManager::get, K_CacheManager.hpp:163-260):
         // the request stays on the asked level; the first mapped coarser level
         // of the volume is sampled instead, an empty one ends the lookup.
@@ -410,8 +407,7 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
             if (e2.w != 1u) continue;
             const uint32_t B = cv.B;
             const uint32_t slot = e2.x / B + (e2.y / B) * cv.sx + (e2.z / B) * cv.sx * cv.sy;
-            uint32_t *u = cv.usage + slot;
-            if (*u != cv.ts) *u = cv.ts;
+            cv.usage[slot] = cv.ts;
             sample = sample_any<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, vp.eb, cv, sampler,
                                    qx * static_cast<float>(lt.vvox[l2][0]), qy * static_cast<float>(lt.vvox[l2][1]),
                                    qz * static_cast<float>(lt.vvox[l2][2]));
