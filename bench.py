@@ -91,7 +91,7 @@ OUR_DEFAULT_STEPS = 40  # views the GPU arm times by default (the reference arm 
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none --nvtx
 #       --nvtx-include roofline/ -k regex:render -c 2 python bench.py --steps 4 --warmup 3 --no-cpu-baseline --no-batched
 # (profiles/render_kernel_c2_1024x1024.md).  None for the other configs.
-ROOFLINE_TRAFFIC = {"c2": 107_050_000}
+ROOFLINE_TRAFFIC = {"c2": 107_531_000}
 BRICK_BINS = {}  # value bins of every brick, by brick-store address
 
 
