@@ -932,8 +932,15 @@ def cpu_baseline(gc, S, cfg, spec, args):
         orc.mip_level(sample, (512, 512, 64), vol_bytes_per_voxel(cfg), nc)
         reps += 1
     mip_cpu = reps * sample.nbytes * 1.125 / (time.perf_counter() - t1) / 1e9
+    # the same over all host cores (z pairs split between threads)
+    t1 = time.perf_counter()
+    reps = 0
+    while time.perf_counter() - t1 < 2.0:
+        orc.mip_level(sample, (512, 512, 64), vol_bytes_per_voxel(cfg), nc, threads=0)
+        reps += 1
+    mip_cpu_all = reps * sample.nbytes * 1.125 / (time.perf_counter() - t1) / 1e9
     return {"value": round(W * H * frames / el / 1e6, 4), "unit": "Mrays/s", "cores": os.cpu_count(),
-            "mip_cpu_gbs_1thread": round(mip_cpu, 2),
+            "mip_cpu_gbs_1thread": round(mip_cpu, 2), "mip_cpu_gbs_all_cores": round(mip_cpu_all, 2),
             "kind": "port", "sample": f"{frames} renders of one converged {W}x{H} {args.config} view from the GPU's cache "
                                       f"snapshot (oracle FP32 ray-march, {os.cpu_count()} threads)"}
 

@@ -188,6 +188,16 @@ int orc_layout(const gc_volume_desc *v, gc_layout *L) {
 /* down_sampling_inner for one z pair, as the kernel indexes it: the input
  * holds the 2 slices of the chunk, rows of inputWidth voxels. */
 void orc_mip_level(const void *src, void *dst, const uint32_t dims[3], uint32_t eb, uint32_t nc) {
+    orc_mip_level_mt(src, dst, dims, eb, nc, 1);
+}
+
+/* The same, z pairs spread over `threads` host threads (<= 0: all). */
+void orc_mip_level_mt(const void *src, void *dst, const uint32_t dims[3], uint32_t eb, uint32_t nc, int threads) {
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#else
+    (void)threads;
+#endif
     const uint8_t *in = (const uint8_t *)src;
     uint8_t *out = (uint8_t *)dst;
     const uint32_t inputWidth = dims[0], inputHeight = dims[1];
@@ -197,7 +207,11 @@ void orc_mip_level(const void *src, void *dst, const uint32_t dims[3], uint32_t 
     const uint32_t outputHeight = inputHeight / 2;
     const uint64_t in_slice2 = (uint64_t)inputWidthStep * inputHeight * 2;
     const uint64_t out_slice = (uint64_t)outputWidthStep * outputHeight;
-    for (uint32_t oz = 0; oz < dims[2] / 2; ++oz) {
+    const int64_t nz = dims[2] / 2;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(threads)
+#endif
+    for (int64_t oz = 0; oz < nz; ++oz) {
         const uint8_t *input = in + oz * in_slice2;
         uint8_t *output = out + oz * out_slice;
         for (uint32_t outputYIndex = 0; outputYIndex < outputHeight; ++outputYIndex)

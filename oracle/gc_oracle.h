@@ -28,6 +28,7 @@ int orc_layout(const gc_volume_desc *v, gc_layout *out);
 
 /* one mip pass (down_sampling_inner) */
 void orc_mip_level(const void *src, void *dst, const uint32_t dims[3], uint32_t eb, uint32_t nc);
+void orc_mip_level_mt(const void *src, void *dst, const uint32_t dims[3], uint32_t eb, uint32_t nc, int threads);
 
 /* bricking of one level (process_bricking); out receives all big bricks */
 void orc_brick_level(const void *level, const uint32_t dims[3], const gc_volume_desc *v,

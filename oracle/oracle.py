@@ -63,6 +63,7 @@ _SIGS = {
     "orc_generate": ([P(Generator), vp], None),
     "orc_layout": ([P(VolumeDesc), P(Layout)], C.c_int),
     "orc_mip_level": ([vp, vp, P(C.c_uint32), C.c_uint32, C.c_uint32], None),
+    "orc_mip_level_mt": ([vp, vp, P(C.c_uint32), C.c_uint32, C.c_uint32, C.c_int], None),
     "orc_brick_level": ([vp, P(C.c_uint32), P(VolumeDesc), P(C.c_uint32), vp], None),
     "orc_empty": ([vp, C.c_uint64, C.c_uint64, C.c_uint32, C.c_float, vp], None),
     "orc_cache_create": ([P(CacheDesc)], vp),
@@ -126,10 +127,14 @@ def layout(vol):
     return L
 
 
-def mip_level(src, dims, eb, nc):
+def mip_level(src, dims, eb, nc, threads=1):
+    """threads: host threads over the z pairs (<= 0: all)."""
     dt = src.dtype
     out = np.zeros(((dims[2] // 2) * (dims[1] // 2) * (dims[0] // 2) * eb) // dt.itemsize, dtype=dt)
-    lib.orc_mip_level(ptr(np.ascontiguousarray(src)), ptr(out), U3(*dims), eb, nc)
+    if threads == 1:
+        lib.orc_mip_level(ptr(np.ascontiguousarray(src)), ptr(out), U3(*dims), eb, nc)
+    else:
+        lib.orc_mip_level_mt(ptr(np.ascontiguousarray(src)), ptr(out), U3(*dims), eb, nc, threads)
     return out
 
 

@@ -93,3 +93,14 @@ def test_bricker_general_formula_matches_reference(orc, name):
     got = general_bricks(vol.reshape(-1).view(np.uint8).reshape(-1, eb), case["size"], case["B"], case["c"],
                          case["bb"], case["nb_big"], eb)
     assert hashlib.sha256(got.tobytes()).hexdigest() == case["sha256"]
+
+
+@pytest.mark.parametrize("dims,eb,nc,dtype", [((64, 48, 32), 1, 1, np.uint8), ((40, 32, 16), 2, 1, np.uint16),
+                                              ((32, 16, 8), 2, 2, np.uint8)])
+def test_oracle_mip_threads_equal_one_thread(orc, dims, eb, nc, dtype):
+    """The all-cores mip restatement (the CPU baseline's second figure) gives
+    the single-thread result byte for byte."""
+    rng = np.random.default_rng(3)
+    n = dims[0] * dims[1] * dims[2] * eb // np.dtype(dtype).itemsize
+    src = rng.integers(0, np.iinfo(dtype).max, size=n, dtype=dtype)
+    assert np.array_equal(orc.mip_level(src, dims, eb, nc), orc.mip_level(src, dims, eb, nc, threads=0))
