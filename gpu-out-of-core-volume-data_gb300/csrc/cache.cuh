@@ -35,6 +35,8 @@ struct LevelTables {
     float ior[kMaxCacheLevels][3];        // initial / real size (CacheManager.hpp:271-285)
     uint32_t eb[kMaxCacheLevels];         // bytes per voxel of the level's volume
     uint32_t bb[kMaxCacheLevels][3];      // big-brick size (in bricks) of the level's volume
+    float nbf[kMaxCacheLevels][3];        // nb and vvox as floats (exact: both < 2^24), for the
+    float vvoxf[kMaxCacheLevels][3];      // ray caster's per-sample page walk
 };
 
 struct CacheView {

@@ -181,6 +181,8 @@ static void build_tables(gc_cache *C) {
             for (int a = 0; a < 3; ++a) {
                 lt.nb[l][a] = L.nb_bricks[k][a];
                 lt.vvox[l][a] = L.nb_bricks[k][a] * C->Beff;
+                lt.nbf[l][a] = static_cast<float>(lt.nb[l][a]);
+                lt.vvoxf[l][a] = static_cast<float>(lt.vvox[l][a]);
                 lt.ior[l][a] = static_cast<float>(L.initial[k][a]) / static_cast<float>(L.real[k][a]);
                 lt.bb[l][a] = V.desc.big_brick_size[a];
             }

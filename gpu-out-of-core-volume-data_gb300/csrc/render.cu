@@ -352,9 +352,9 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
     const float px = np.x * lt.ior[lvl][0];
     const float py = np.y * lt.ior[lvl][1];
     const float pz = np.z * lt.ior[lvl][2];
-    const uint32_t cx = lt.off[lvl] + static_cast<uint32_t>(px * static_cast<float>(lt.nb[lvl][0]));
-    const uint32_t cy = static_cast<uint32_t>(py * static_cast<float>(lt.nb[lvl][1]));
-    const uint32_t cz = static_cast<uint32_t>(pz * static_cast<float>(lt.nb[lvl][2]));
+    const uint32_t cx = lt.off[lvl] + static_cast<uint32_t>(px * lt.nbf[lvl][0]);
+    const uint32_t cy = static_cast<uint32_t>(py * lt.nbf[lvl][1]);
+    const uint32_t cz = static_cast<uint32_t>(pz * lt.nbf[lvl][2]);
     const uint64_t idx = cx + static_cast<uint64_t>(cy) * cv.mx + static_cast<uint64_t>(cz) * cv.mx * cv.my;
     if (cx != w.pcx || cy != w.pcy || cz != w.pcz) {
         // A new entry: the entry and its value bins are read together (one
@@ -379,9 +379,9 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
     if (flag == 1u) {
         const uint32_t slot = w.slot;
         if (w.invisible) return kInvisible;  // no sample of this brick reaches the compositing threshold
-        const float fx = px * static_cast<float>(lt.vvox[lvl][0]);
-        const float fy = py * static_cast<float>(lt.vvox[lvl][1]);
-        const float fz = pz * static_cast<float>(lt.vvox[lvl][2]);
+        const float fx = px * lt.vvoxf[lvl][0];
+        const float fy = py * lt.vvoxf[lvl][1];
+        const float fz = pz * lt.vvoxf[lvl][2];
         sample = sample_any<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, vp.eb, cv, sampler, fx, fy, fz);
         return kMapped;
     }
@@ -436,11 +436,26 @@ struct Ray {
     uint32_t tfw;
     uint32_t lvl, lvl_end;  // cache level of the current LOD; end of the view's levels
     uint32_t sampler;
+    float t_lo;  // below this t the LOD test surely keeps the level (+inf at the coarsest)
     Walk w;
     bool unm, dvr;
     bool coarse;  // a coarser level stood in for a missing brick (fallback mode)
     uint32_t nsamp;  // samples taken (voxel reads of a resident brick)
 };
+
+// compute_LOD keeps the level while sL >= RN(endX * RN(t / tfar)) or
+// sU >= RN(endY * RN(t / tfar)).  Each rounding grows a value by at most a
+// factor (1 + 2^-24), so t <= sL * tfar / (endX * (1 + 2^-24)^2) already keeps
+// it (likewise for Y; an axis with end 0 always does).  The bound below is
+// that, computed in float (three more roundings) and shrunk by 2^-19, which
+// covers all five; at or above it the exact test runs, so the level sequence
+// is the reference's.
+__device__ __forceinline__ float lod_keep_bound(float sL, float sU, float endX, float endY, float tfar, bool last) {
+    if (last) return __int_as_float(0x7f800000);
+    float bx = endX > 0.f ? sL / endX * tfar : __int_as_float(0x7f800000);
+    float by = endY > 0.f ? sU / endY * tfar : __int_as_float(0x7f800000);
+    return fmaxf(bx, by) * (1.0f - 1.0f / 524288.0f);
+}
 
 // Eye ray, box intersection and progressive resume.  Returns false when the
 // ray has nothing to march (the pixel is then already written).
@@ -532,6 +547,7 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
     r.lvl = vp.level_base;
     r.lvl_end = vp.level_base + vp.nlevels;
     r.sampler = vp.sampler;
+    r.t_lo = lod_keep_bound(r.sL, r.sU, r.endX, r.endY, r.tfar, r.lvl + 1 >= r.lvl_end);
     r.w.pcx = r.w.pcy = r.w.pcz = UINT_MAX;
     r.w.flag = 0;
     r.w.slot = 0;
@@ -552,7 +568,7 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
     // compute_LOD: the level only grows along a ray because the pixel
     // footprint grows with t, so the scan resumes at the current level (and
     // the footprint is not needed once the ray is at the coarsest level).
-    if (r.lvl + 1 < r.lvl_end) {
+    if (r.t >= r.t_lo) {  // near or past the level change: the exact test
         const float alpha = r.t / r.tfar;
         const float pX = r.endX * alpha;
         const float pY = r.endY * alpha;
@@ -570,6 +586,7 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
             r.step = vp.step[r.lod];
             r.afloor = vp.alpha_floor[r.lod];
             r.kexp = vp.kexp[r.lod];
+            r.t_lo = lod_keep_bound(r.sL, r.sU, r.endX, r.endY, r.tfar, r.lvl + 1 >= r.lvl_end);
         }
     }
     typename SampleOf<T>::type sample{};
