@@ -66,36 +66,47 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &t
     return pre + x - v;
 }
 
-// Decoupled look-back (single thread).  Status word: [63:62] flag
+// Decoupled look-back (one warp).  Status word: [63:62] flag
 // (1 aggregate, 2 inclusive prefix), [61:32] launch epoch, [31:0] value.
 __device__ uint32_t lookback(uint64_t *status, uint32_t tile, uint32_t agg, uint32_t epoch, uint32_t *err) {
+    // Called by the 32 lanes of warp 0: each round reads the statuses of the
+    // 32 nearest unvisited predecessors at once (lane 0 the nearest) and sums
+    // the window up to the first inclusive prefix, waiting while a tile in
+    // that range has not published yet.  Returns the exclusive prefix (all
+    // lanes).
+    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t ep = epoch & 0x3FFFFFFFu;
     const uint64_t E = static_cast<uint64_t>(ep) << 32;
     if (tile == 0) {
-        st_release(&status[0], (2ull << 62) | E | agg);
+        if (lane == 0) st_release(&status[0], (2ull << 62) | E | agg);
         return 0;
     }
-    st_release(&status[tile], (1ull << 62) | E | agg);
+    if (lane == 0) st_release(&status[tile], (1ull << 62) | E | agg);
     uint32_t excl = 0;
-    int64_t j = static_cast<int64_t>(tile) - 1;
+    int64_t top = static_cast<int64_t>(tile) - 1;
     uint32_t spins = 0;
-    while (j >= 0) {
-        const uint64_t s = ld_acquire(&status[j]);
+    for (;;) {
+        const int64_t j = top - static_cast<int64_t>(lane);
+        uint64_t s = (2ull << 62) | E;  // before tile 0: an inclusive prefix of 0
+        if (j >= 0) s = ld_acquire(&status[j]);
         const uint32_t flag = static_cast<uint32_t>(s >> 62);
-        const uint32_t sep = static_cast<uint32_t>(s >> 32) & 0x3FFFFFFFu;
-        if (sep != ep || flag == 0) {
+        const bool ready = (static_cast<uint32_t>(s >> 32) & 0x3FFFFFFFu) == ep && flag != 0;
+        const uint32_t incl = __ballot_sync(0xffffffffu, ready && flag == 2);
+        const uint32_t last = incl ? static_cast<uint32_t>(__ffs(incl)) - 1u : 31u;  // last lane needed
+        const uint32_t need = last == 31u ? 0xffffffffu : ((2u << last) - 1u);
+        if (__ballot_sync(0xffffffffu, !ready) & need) {
             if (++spins > kMaxSpins) {
-                atomicOr(err, kErrLookback);
+                if (lane == 0) atomicOr(err, kErrLookback);
                 break;
             }
             __nanosleep(64);
             continue;
         }
-        excl += static_cast<uint32_t>(s);
-        if (flag == 2) break;
-        --j;
+        excl += __reduce_add_sync(0xffffffffu, lane <= last ? static_cast<uint32_t>(s) : 0u);
+        if (incl) break;
+        top -= 32;
     }
-    st_release(&status[tile], (2ull << 62) | E | (excl + agg));
+    if (lane == 0) st_release(&status[tile], (2ull << 62) | E | (excl + agg));
     return excl;
 }
 
@@ -146,7 +157,10 @@ __global__ void __launch_bounds__(kThreads) lru_partition_kernel(const uint32_t 
     }
     uint32_t tile_total;
     const uint32_t excl_thread = block_exclusive_scan(__popc(flags), tile_total);
-    if (threadIdx.x == 0) s_excl = lookback(status, tile, tile_total, epoch, &ctl->err);
+    if (threadIdx.x < 32) {
+        const uint32_t e = lookback(status, tile, tile_total, epoch, &ctl->err);
+        if (threadIdx.x == 0) s_excl = e;
+    }
     __syncthreads();
     const uint32_t total_used = *count;
     uint32_t used_before = s_excl + excl_thread;
@@ -211,7 +225,10 @@ __global__ void __launch_bounds__(kThreads) miss_compact_kernel(const uint32_t *
     }
     uint32_t tile_total;
     const uint32_t excl_thread = block_exclusive_scan(__popc(flags), tile_total);
-    if (threadIdx.x == 0) s_excl = lookback(status, tile, tile_total, epoch, &ctl->err);
+    if (threadIdx.x < 32) {
+        const uint32_t e = lookback(status, tile, tile_total, epoch, &ctl->err);
+        if (threadIdx.x == 0) s_excl = e;
+    }
     __syncthreads();
     uint32_t rank = s_excl + excl_thread;
     if (flags && rank < maxreq) {
