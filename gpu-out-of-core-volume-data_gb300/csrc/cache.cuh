@@ -62,11 +62,12 @@ struct CacheView {
 };
 
 // Empty-space skipping: voxel values are quantized into kValueBins bins of
-// [0, 1]; a slot records the bins its brick's voxels cover (one bit each,
-// widened by one bin on either side) and a view the bins its transfer function
-// can make visible.  A brick whose bins are all invisible contributes no
-// sample above the compositing threshold, so the march steps through it
-// without sampling (same t sequence, same image).
+// [0, 1]; the install records the bins a brick's voxels cover (one bit each,
+// widened by one bin on either side) for its slot and its page-directory
+// entry, and a view the bins its transfer function can make visible.  A brick
+// whose bins are all invisible contributes no sample above the compositing
+// threshold, so the march steps through it without sampling (same t
+// sequence, same image).
 constexpr uint32_t kValueBins = 64;
 
 // Per-launch ray-caster parameters of one view.
