@@ -30,7 +30,8 @@ no public dataset is used):
       latency from arrival to retirement.
 The pool and page directory exceed L2 (129 MB) for c2/c3/c4.  Bricks are paged
 in by a gather kernel reading the host store over the host link where the
-device can (--upload staged: host copies + cudaMemcpyAsync).
+device can (--upload staged: host copies + cudaMemcpyAsync).  The host brick
+stores are page-locked (--pageable-stores: pageable; c4's always pageable).
 
 value  : views rendered into device buffers.
 e2e    : the same through the C ABI with the converged RGBA frame read back
@@ -239,7 +240,7 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-PIN_STORES = False  # --pin-stores: brick stores in page-locked host memory
+PIN_STORES = True  # brick stores in page-locked host memory (--pageable-stores: not)
 LAST_PREPROCESS = {}  # stage timings of the last make_store (device mip, bricking, store copy)
 
 
@@ -534,6 +535,7 @@ def run_ours(args):
                    "pool_gib": round(pool_bytes / 2**30, 3), "view": [W, H], "max_requests": args.max_requests,
                    "brick_bins": bool(args.brick_bins), "loader": "sync", "upload": "gather kernel reading the host store"
                    if S.cm.stats().upload_direct else "staged host copies + cudaMemcpyAsync",
+                   "stores": "pinned" if PIN_STORES else "pageable",
                    "l2": "inputs > L2 (2 GiB pool, 103 MB page directory, 28 GiB host brick store)"
                    if args.config == "c2" else ("inputs > L2 (8 GiB pool, 43 GiB host brick store)"
                                                 if args.config == "c5" else
@@ -727,11 +729,14 @@ def run_c4(args):
     resolution and one of 4 transfer functions; each is submitted to the
     continuous batch at its arrival time and retired when converged.  Latency =
     arrival -> retirement; Mrays/s = rays of all requests / time to the last
-    retirement."""
+    retirement.  The three stores (85 GiB) stay in pageable host memory: page-
+    locking them would hold half of the host's memory."""
     import torch
 
     import gcgb300 as gc
 
+    global PIN_STORES
+    PIN_STORES = False
     cfg = CONFIGS["c4"]
     vols, stores, prep = c4_stores(gc, torch, cfg)
     out = c4_serve(gc, torch, cfg, vols, stores, args)
@@ -1036,9 +1041,9 @@ def main():
                          "staged = host copies into pinned staging + cudaMemcpyAsync")
     ap.add_argument("--reorder", type=int, default=192,
                     help="batched admission: locality window over queued views (0: arrival order)")
-    ap.add_argument("--pin-stores", action="store_true",
-                    help="keep the host brick stores in page-locked memory (read by the gather kernel "
-                         "through the device's own mappings)")
+    ap.add_argument("--pageable-stores", dest="pin_stores", action="store_false",
+                    help="keep the host brick stores in pageable memory (read by the gather kernel where the "
+                         "device accesses pageable memory) instead of page-locked memory")
     ap.add_argument("--park", type=float, default=0.0,
                     help="batched/serving: park the newest view while demand exceeds this fraction of the pool")
     ap.add_argument("--brick-bins", action="store_true",
