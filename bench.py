@@ -483,7 +483,7 @@ def run_ours(args):
     last = spec(cfg.get("roofline_frame", 42))
     S.converge(last, cap=cfg.get("cap", 64))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > L2 (126 MB)
-    samples0 = S.cm.stats().samples
+    samples0, marched0 = S.cm.stats().samples, S.cm.stats().rays_marched
     ev = []
     torch.cuda.nvtx.range_push("roofline")
     for _ in range(5):
@@ -502,6 +502,7 @@ def run_ours(args):
     torch.cuda.nvtx.range_pop()
     touched = S.cm.stats().last_used
     samples = (S.cm.stats().samples - samples0) / len(ev)
+    rays_hit = (S.cm.stats().rays_marched - marched0) / len(ev)
     render_ms = statistics.median([a.elapsed_time(b) for a, b in ev])
     # the same launch with empty-space skipping off (identical image), for the record
     gc.render_empty_skip(False)
@@ -561,6 +562,7 @@ def run_ours(args):
                      "peak_kind": peak_kind, "algorithmic_bytes_per_launch": int(algo),
                      "launch_ms": round(render_ms, 4), "launch_ms_without_empty_skip": round(render_ms_noskip, 4),
                      "touched_bricks": int(touched), "samples_per_launch": int(samples),
+                     "rays_hit_box_per_launch": int(rays_hit),
                      "gather_bytes_per_launch": int(samples * (8 * vol.encoded_bytes + 16)),
                      "gather_gbs": round(samples * (8 * vol.encoded_bytes + 16) / (render_ms / 1e3) / 1e9, 1),
                      "note": f"view {cfg.get('roofline_frame', 42)} of the {args.config} path, converged, "
@@ -944,8 +946,22 @@ def cpu_baseline(gc, S, cfg, spec, args):
         orc.mip_level(sample, (512, 512, 64), vol_bytes_per_voxel(cfg), nc, threads=0)
         reps += 1
     mip_cpu_all = reps * sample.nbytes * 1.125 / (time.perf_counter() - t1) / 1e9
+    # the CPU restatement of process_bricking (checked against the reference's
+    # own bricker), one thread, on a bounded 256 x 256 x 128 level of the voxel type
+    bdims = (256, 256, 128)
+    bvol = gc.volume_desc(bdims, cfg["B"], cfg["c"], vol_bytes_per_voxel(cfg), nc, cfg.get("bb", (1, 1, 1)))
+    blay = gc.compute_layout(bvol)
+    level = np.random.default_rng(2).integers(0, 255, size=bdims[0] * bdims[1] * bdims[2] * vol_bytes_per_voxel(cfg),
+                                              dtype=np.uint8)
+    t1 = time.perf_counter()
+    reps = 0
+    while time.perf_counter() - t1 < 2.0:
+        orc.brick_level(level, bdims, bvol, tuple(blay.nb_big_bricks[0]))
+        reps += 1
+    brick_cpu = reps * level.nbytes / (time.perf_counter() - t1) / 1e9
     return {"value": round(W * H * frames / el / 1e6, 4), "unit": "Mrays/s", "cores": os.cpu_count(),
             "mip_cpu_gbs_1thread": round(mip_cpu, 2), "mip_cpu_gbs_all_cores": round(mip_cpu_all, 2),
+            "bricking_cpu_gbs_1thread": round(brick_cpu, 3),
             "kind": "port", "sample": f"{frames} renders of one converged {W}x{H} {args.config} view from the GPU's cache "
                                       f"snapshot (oracle FP32 ray-march, {os.cpu_count()} threads)"}
 

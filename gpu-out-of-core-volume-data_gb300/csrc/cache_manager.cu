@@ -828,8 +828,8 @@ int gc_cache_create_shared(const gc_cache_desc *desc, const gc_volume_desc *volu
         C->b_shift = 32;
         for (uint32_t k = 0; k < 31; ++k)
             if ((1u << k) == C->B) C->b_shift = k;
-        C->d_samples = dalloc<unsigned long long>(1, "sample counter");
-        GC_CUDA(cudaMemset(C->d_samples, 0, sizeof(unsigned long long)));
+        C->d_samples = dalloc<unsigned long long>(2, "sample and ray counters");
+        GC_CUDA(cudaMemset(C->d_samples, 0, 2 * sizeof(unsigned long long)));
         GC_CUDA(cudaMemset(C->slot_bins, 0xff, C->nslots * sizeof(unsigned long long)));
         C->status_lru = dalloc<uint64_t>(lookback_tiles(C->nslots), "scan status");
         C->status_miss = dalloc<uint64_t>(lookback_tiles(C->nentries), "scan status");
@@ -1091,12 +1091,13 @@ int gc_cache_stats_get(gc_cache_t C, gc_cache_stats *out) {
         std::lock_guard<std::mutex> g(C->mu);
         uint32_t used = 0;
         GC_CUDA(cudaMemcpy(&used, C->d_count, sizeof(used), cudaMemcpyDeviceToHost));
-        unsigned long long samples = 0;
-        GC_CUDA(cudaMemcpy(&samples, C->d_samples, sizeof(samples), cudaMemcpyDeviceToHost));
+        unsigned long long counts[2] = {0, 0};
+        GC_CUDA(cudaMemcpy(counts, C->d_samples, sizeof(counts), cudaMemcpyDeviceToHost));
         *out = C->stats;
         out->device_error = a.err | b.err;
         out->upload_direct = C->gather ? 1u : 0u;
-        out->samples = samples;
+        out->samples = counts[0];
+        out->rays_marched = counts[1];
         out->last_used = used;
     });
 }

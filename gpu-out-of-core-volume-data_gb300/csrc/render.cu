@@ -704,11 +704,12 @@ __global__ void __launch_bounds__(256) render_kernel(const CacheView cv, const L
         const uint32_t ty = local / vp->tiles_x, tx = local - ty * vp->tiles_x;
         const uint32_t sh = vp->tile_shift, tw = 1u << sh;
         const uint32_t x = (tx << sh) + (lane & (tw - 1u)), y = ty * (32u >> sh) + (lane >> sh);
-        bool unm = false, coarse_any = false;
+        bool unm = false, coarse_any = false, marched = false;
         uint32_t nsamp = 0;
         if (x < vp->W && y < vp->H) {
             Ray r;
             if (ray_setup<T>(lt, vp, x, y, r)) {
+                marched = true;
                 while (ray_step<T>(cv, lt, r)) {
                 }
                 unm = ray_finish(r);
@@ -717,7 +718,9 @@ __global__ void __launch_bounds__(256) render_kernel(const CacheView cv, const L
             }
         }
         const uint32_t tile_samples = __reduce_add_sync(0xffffffffu, nsamp);
+        const uint32_t tile_rays = __popc(__ballot_sync(0xffffffffu, marched));
         if (lane == 0 && tile_samples) atomicAdd(cv.samples, static_cast<unsigned long long>(tile_samples));
+        if (lane == 0 && tile_rays) atomicAdd(cv.samples + 1, static_cast<unsigned long long>(tile_rays));
         const uint32_t any = __ballot_sync(0xffffffffu, unm);
         if (any && lane == 0 && vp->status) atomicOr(vp->status, 1u);
         if (vp->fallback && vp->status) {  // bit 1: a coarser level stood in (preview image)
@@ -760,6 +763,9 @@ __global__ void __launch_bounds__(256) render_pixels_kernel(const CacheView cv, 
                     if (x < vp->W && y < vp->H) active = ray_setup<T>(lt, vp, x, y, r);
                 }
             }
+            const uint32_t started = __ballot_sync(0xffffffffu, ((idle >> lane) & 1u) && active);
+            if (started && static_cast<int>(lane) == leader)
+                atomicAdd(cv.samples + 1, static_cast<unsigned long long>(__popc(started)));
         }
         if (active && !ray_step<T>(cv, lt, r)) {
             active = false;

@@ -70,7 +70,8 @@ class CacheStats(C.Structure):
                 ("bricks_installed", C.c_uint64), ("bricks_empty", C.c_uint64), ("bytes_h2d", C.c_uint64),
                 ("load_errors", C.c_uint64), ("last_requests", C.c_uint32), ("last_used", C.c_uint32),
                 ("device_error", C.c_uint32), ("load_cycles", C.c_uint64), ("loader_host_ns", C.c_uint64),
-                ("upload_ns", C.c_uint64), ("upload_direct", C.c_uint32), ("samples", C.c_uint64)]
+                ("upload_ns", C.c_uint64), ("upload_direct", C.c_uint32), ("samples", C.c_uint64),
+                ("rays_marched", C.c_uint64)]
 
 
 class View(C.Structure):

@@ -404,14 +404,18 @@ def test_edge_views_match_oracle(gc, orc, torch_cuda, case):
     g, o = s.buffers(W, H)
     for f in range(8):
         v = s.view(m, W, H, tf_dev, 256, g, **kw)
+        marched0 = s.cm.stats().rays_marched
         s.cm.render(v)
         s.oc.render(v, tf, *o)
         torch_cuda.cuda.synchronize()
+        if f == 0 and case != "inside":  # a fresh frame marches exactly the rays that hit the box
+            assert s.cm.stats().rays_marched - marched0 == int((o[1] > 0).sum()), case
         assert rgba_diff(g[0].cpu().numpy(), o[0]).max() <= RGBA_TOL_FP32, (case, f)
         assert np.array_equal(g[1].cpu().numpy(), o[1]) and np.array_equal(g[2].cpu().numpy(), o[2]), (case, f)
         assert s.cm.update() == s.oc.update(), (case, f)
         s.compare_cache(f"{case} frame {f}")
     if case == "miss":
         assert not (g[0].cpu().numpy() >> 24).any()
+        assert s.cm.stats().rays_marched == 0
     if case == "inside":  # rays start inside the volume and advance through it
         assert (g[1].cpu().numpy() > 0).mean() > 0.5
