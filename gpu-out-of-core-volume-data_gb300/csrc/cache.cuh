@@ -58,7 +58,7 @@ struct CacheView {
     uint32_t bins_user;   // an unmapped entry with invisible bins is stepped through (user bins given)
     uint32_t b_shift;     // log2(B) when B is a power of two, else 32 (divide)
     unsigned long long *samples;          // running counts: [0] samples taken (resident-brick reads),
-                                          // [1] rays whose march started
+                                          // [1] rays that took a first step
     uint32_t ts;
 };
 

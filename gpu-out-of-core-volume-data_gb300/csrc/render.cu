@@ -556,6 +556,12 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
     return true;
 }
 
+// The ray passes the march loop's first test: it takes at least one sample
+// (a ray whose box lies behind the camera, or a finished ray, does not).
+__device__ __forceinline__ bool ray_enters(const Ray &r) {
+    return (!r.dvr || r.fc.w < r.early) && r.t < r.tfar;
+}
+
 // One iteration of the march loop (RayCasters.cu:122-188).  Returns false
 // when the loop ends.
 template <typename T>
@@ -709,7 +715,7 @@ __global__ void __launch_bounds__(256) render_kernel(const CacheView cv, const L
         if (x < vp->W && y < vp->H) {
             Ray r;
             if (ray_setup<T>(lt, vp, x, y, r)) {
-                marched = true;
+                marched = ray_enters(r);
                 while (ray_step<T>(cv, lt, r)) {
                 }
                 unm = ray_finish(r);
@@ -763,7 +769,7 @@ __global__ void __launch_bounds__(256) render_pixels_kernel(const CacheView cv, 
                     if (x < vp->W && y < vp->H) active = ray_setup<T>(lt, vp, x, y, r);
                 }
             }
-            const uint32_t started = __ballot_sync(0xffffffffu, ((idle >> lane) & 1u) && active);
+            const uint32_t started = __ballot_sync(0xffffffffu, ((idle >> lane) & 1u) && active && ray_enters(r));
             if (started && static_cast<int>(lane) == leader)
                 atomicAdd(cv.samples + 1, static_cast<unsigned long long>(__popc(started)));
         }

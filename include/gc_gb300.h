@@ -313,8 +313,9 @@ typedef struct gc_cache_stats {
                                      reading the store; 0: staged copies         */
     uint64_t samples;             /* ray-caster samples taken (each reads 8 voxels
                                      and a page-directory entry)                 */
-    uint64_t rays_marched;        /* rays whose march started in a launch (they
-                                     hit the volume's box and were not finished) */
+    uint64_t rays_marched;        /* rays that took a first step in a launch (they
+                                     meet the volume's box ahead of the camera
+                                     and were not finished)                      */
 } gc_cache_stats;
 int gc_cache_stats_get(gc_cache_t cache, gc_cache_stats *out);
 
