@@ -92,7 +92,14 @@ struct ViewParams {
     float alpha_floor[GC_MAX_LEVELS];   // alphas at or below this cannot reach the 0.001 threshold
     uint32_t tiles_x;                   // warp tiles per row
     uint32_t tile_shift;                // log2 of the tile width
-    uint32_t tile_begin;                // first global tile index of this view
+    // Work order: the tiles of the screen rectangle that can hold rays meeting
+    // the box (rx0, ry0, rw, rh in tiles) come first in the queue, for every
+    // view; the other tiles (rays that miss) follow.
+    uint32_t rx0, ry0, rw, rh;
+    uint32_t rect_begin;                // first queue index of this view's rectangle tiles
+    uint32_t out_begin;                 // first queue index of its other tiles
+    uint32_t rect_total;                // rectangle tiles of all views (the same in every view)
+    uint32_t tile_begin;                // unused by the kernels (kept for the layout)
     uint32_t level_base;                // first cache level of the view's volume
     uint32_t nlevels;                   // levels of the view's volume
     uint32_t eb;                        // bytes per voxel of the view's volume

@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <mutex>
@@ -689,6 +690,64 @@ static void refresh_entry_bins(gc_cache *C, cudaStream_t s) {
     GC_CUDA(cudaStreamSynchronize(s));
 }
 
+// The tiles whose rays can meet the view's box: the box's 8 corners projected
+// with the ray caster's camera (a ray through pixel (x, y) has the camera
+// direction (u, v, -focal), u = 2 (x + 0.5) / W - 1, v likewise, turned by the
+// view matrix), their bounding rectangle widened by a pixel.  When a corner
+// lies on or behind the camera plane the whole image is the rectangle.  Only
+// the order of the work depends on it: every tile is rendered either way.
+static void screen_rect(ViewParams &v) {
+    const uint32_t tw = 1u << v.tile_shift, th = 32u >> v.tile_shift;
+    const uint32_t ntx = v.tiles_x, nty = div_up(v.H, th);
+    v.rx0 = 0;
+    v.ry0 = 0;
+    v.rw = ntx;
+    v.rh = nty;
+    double R[3][3], o[3];
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) R[r][c] = v.m[4 * r + c];
+        o[r] = v.m[4 * r + 3];
+    }
+    // inverse of the 3x3 part (world direction = R * camera direction)
+    const double det = R[0][0] * (R[1][1] * R[2][2] - R[1][2] * R[2][1]) -
+                       R[0][1] * (R[1][0] * R[2][2] - R[1][2] * R[2][0]) +
+                       R[0][2] * (R[1][0] * R[2][1] - R[1][1] * R[2][0]);
+    if (!(std::fabs(det) > 1e-12) || !(v.focal > 0.f)) return;
+    double I[3][3];
+    I[0][0] = (R[1][1] * R[2][2] - R[1][2] * R[2][1]) / det;
+    I[0][1] = (R[0][2] * R[2][1] - R[0][1] * R[2][2]) / det;
+    I[0][2] = (R[0][1] * R[1][2] - R[0][2] * R[1][1]) / det;
+    I[1][0] = (R[1][2] * R[2][0] - R[1][0] * R[2][2]) / det;
+    I[1][1] = (R[0][0] * R[2][2] - R[0][2] * R[2][0]) / det;
+    I[1][2] = (R[0][2] * R[1][0] - R[0][0] * R[1][2]) / det;
+    I[2][0] = (R[1][0] * R[2][1] - R[1][1] * R[2][0]) / det;
+    I[2][1] = (R[0][1] * R[2][0] - R[0][0] * R[2][1]) / det;
+    I[2][2] = (R[0][0] * R[1][1] - R[0][1] * R[1][0]) / det;
+    double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
+    for (int k = 0; k < 8; ++k) {
+        const double P[3] = {(k & 1) ? v.bmax[0] : v.bmin[0], (k & 2) ? v.bmax[1] : v.bmin[1],
+                             (k & 4) ? v.bmax[2] : v.bmin[2]};
+        double q[3];
+        for (int r = 0; r < 3; ++r)
+            q[r] = I[r][0] * (P[0] - o[0]) + I[r][1] * (P[1] - o[1]) + I[r][2] * (P[2] - o[2]);
+        if (!(q[2] < -1e-6)) return;  // a corner on or behind the camera plane
+        const double u = -v.focal * q[0] / q[2], w = -v.focal * q[1] / q[2];
+        const double x = (u + 1.0) * 0.5 * v.W - 0.5, y = (w + 1.0) * 0.5 * v.H - 0.5;
+        xmin = std::min(xmin, x);
+        xmax = std::max(xmax, x);
+        ymin = std::min(ymin, y);
+        ymax = std::max(ymax, y);
+    }
+    auto clampi = [](double a, double lo, double hi) { return a < lo ? lo : (a > hi ? hi : a); };
+    const double tx0 = clampi(std::floor((xmin - 1.0) / tw), 0, ntx), tx1 = clampi(std::floor((xmax + 1.0) / tw) + 1, 0, ntx);
+    const double ty0 = clampi(std::floor((ymin - 1.0) / th), 0, nty), ty1 = clampi(std::floor((ymax + 1.0) / th) + 1, 0, nty);
+    v.rx0 = static_cast<uint32_t>(tx0);
+    v.ry0 = static_cast<uint32_t>(ty0);
+    v.rw = tx1 > tx0 ? static_cast<uint32_t>(tx1 - tx0) : 0u;
+    v.rh = ty1 > ty0 ? static_cast<uint32_t>(ty1 - ty0) : 0u;
+    if (v.rw == 0 || v.rh == 0) v.rw = v.rh = 0;
+}
+
 static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s, bool mark_done = false,
                    RenderGraph *graph = nullptr, ViewParams *pinned = nullptr) {
     GC_REQUIRE(views && n >= 1, "no views");
@@ -696,12 +755,20 @@ static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s
     GC_CUDA(cudaSetDevice(C->device));
     refresh_entry_bins(C, s);
     std::vector<ViewParams> vp(n);
-    uint32_t tiles = 0;
+    uint32_t tiles = 0, rect_total = 0;
     for (uint32_t i = 0; i < n; ++i) {
         fill_view(C, views[i], vp[i]);
         vp[i].mark_done = mark_done ? 1u : 0u;
         vp[i].tile_begin = tiles;
         tiles += vp[i].tiles_x * div_up(views[i].height, 32u >> vp[i].tile_shift);
+        screen_rect(vp[i]);
+        vp[i].rect_begin = rect_total;
+        rect_total += vp[i].rw * vp[i].rh;
+    }
+    for (uint32_t i = 0, out = rect_total; i < n; ++i) {
+        vp[i].rect_total = rect_total;
+        vp[i].out_begin = out;
+        out += vp[i].tiles_x * div_up(vp[i].H, 32u >> vp[i].tile_shift) - vp[i].rw * vp[i].rh;
     }
     if (graph) {
         std::memcpy(pinned, vp.data(), n * sizeof(ViewParams));

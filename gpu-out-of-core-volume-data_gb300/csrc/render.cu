@@ -669,16 +669,47 @@ __device__ __forceinline__ bool ray_finish(Ray &r) {
     return r.unm;
 }
 
-__device__ __forceinline__ uint32_t find_view(const ViewParams *__restrict__ views, uint32_t nviews, uint32_t t) {
+// The view and tile of queue index t: first the screen-rectangle tiles of
+// every view (rows of the rectangle), then the other tiles of every view in
+// raster order.
+__device__ __forceinline__ const ViewParams *tile_of(const ViewParams *__restrict__ views, uint32_t nviews,
+                                                     uint32_t t, uint32_t &tx, uint32_t &ty) {
+    const bool in_rect = t < views[0].rect_total;
     uint32_t lo = 0, hi = nviews - 1;
-    while (lo < hi) {
+    while (lo < hi) {  // the last view whose range starts at or before t
         const uint32_t mid = (lo + hi + 1) >> 1;
-        if (views[mid].tile_begin <= t)
+        if ((in_rect ? views[mid].rect_begin : views[mid].out_begin) <= t)
             lo = mid;
         else
             hi = mid - 1;
     }
-    return lo;
+    const ViewParams *vp = views + lo;
+    if (in_rect) {
+        const uint32_t local = t - vp->rect_begin, row = local / vp->rw;
+        ty = vp->ry0 + row;
+        tx = vp->rx0 + (local - row * vp->rw);
+        return vp;
+    }
+    uint32_t u = t - vp->out_begin;
+    const uint32_t ntx = vp->tiles_x, above = vp->ry0 * ntx;
+    if (u < above) {
+        ty = u / ntx;
+        tx = u - ty * ntx;
+        return vp;
+    }
+    u -= above;
+    const uint32_t side = ntx - vp->rw, beside = vp->rh * side;
+    if (u < beside) {
+        const uint32_t row = u / side, col = u - row * side;
+        ty = vp->ry0 + row;
+        tx = col < vp->rx0 ? col : col + vp->rw;
+        return vp;
+    }
+    u -= beside;
+    const uint32_t row = u / ntx;
+    ty = vp->ry0 + vp->rh + row;
+    tx = u - row * ntx;
+    return vp;
 }
 
 // The last warp of a launch resets the work queue for the next launch.
@@ -705,9 +736,8 @@ __global__ void __launch_bounds__(256) render_kernel(const CacheView cv, const L
         if (lane == 0) t = atomicAdd(queue, 1u);
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= total_tiles) break;
-        const ViewParams *vp = views + find_view(views, nviews, t);
-        const uint32_t local = t - vp->tile_begin;
-        const uint32_t ty = local / vp->tiles_x, tx = local - ty * vp->tiles_x;
+        uint32_t tx, ty;
+        const ViewParams *vp = tile_of(views, nviews, t, tx, ty);
         const uint32_t sh = vp->tile_shift, tw = 1u << sh;
         const uint32_t x = (tx << sh) + (lane & (tw - 1u)), y = ty * (32u >> sh) + (lane >> sh);
         bool unm = false, coarse_any = false, marched = false;
@@ -761,9 +791,8 @@ __global__ void __launch_bounds__(256) render_pixels_kernel(const CacheView cv, 
                 const uint32_t p = base + __popc(idle & ((1u << lane) - 1u));
                 if (p < total) {
                     const uint32_t t = p >> 5, k = p & 31u;
-                    const ViewParams *vp = views + find_view(views, nviews, t);
-                    const uint32_t local = t - vp->tile_begin;
-                    const uint32_t ty = local / vp->tiles_x, tx = local - ty * vp->tiles_x;
+                    uint32_t tx, ty;
+                    const ViewParams *vp = tile_of(views, nviews, t, tx, ty);
                     const uint32_t sh = vp->tile_shift, tw = 1u << sh;
                     const uint32_t x = (tx << sh) + (k & (tw - 1u)), y = ty * (32u >> sh) + (k >> sh);
                     if (x < vp->W && y < vp->H) active = ray_setup<T>(lt, vp, x, y, r);
