@@ -99,7 +99,6 @@ struct ViewParams {
     uint32_t rect_begin;                // first queue index of this view's rectangle tiles
     uint32_t out_begin;                 // first queue index of its other tiles
     uint32_t rect_total;                // rectangle tiles of all views (the same in every view)
-    uint32_t tile_begin;                // unused by the kernels (kept for the layout)
     uint32_t level_base;                // first cache level of the view's volume
     uint32_t nlevels;                   // levels of the view's volume
     uint32_t eb;                        // bytes per voxel of the view's volume

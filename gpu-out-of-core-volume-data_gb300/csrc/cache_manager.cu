@@ -759,7 +759,6 @@ static void render(gc_cache *C, const gc_view *views, uint32_t n, cudaStream_t s
     for (uint32_t i = 0; i < n; ++i) {
         fill_view(C, views[i], vp[i]);
         vp[i].mark_done = mark_done ? 1u : 0u;
-        vp[i].tile_begin = tiles;
         tiles += vp[i].tiles_x * div_up(views[i].height, 32u >> vp[i].tile_shift);
         screen_rect(vp[i]);
         vp[i].rect_begin = rect_total;
