@@ -684,10 +684,14 @@ __device__ __forceinline__ const ViewParams *tile_of(const ViewParams *__restric
             hi = mid - 1;
     }
     const ViewParams *vp = views + lo;
-    if (in_rect) {
-        const uint32_t local = t - vp->rect_begin, row = local / vp->rw;
+    if (in_rect) {  // rows from the middle of the rectangle outwards (the longest rays first)
+        const uint32_t local = t - vp->rect_begin, k = local / vp->rw;
+        const uint32_t mid = (vp->rh - 1) / 2, half = (k + 1) / 2;
+        uint32_t row = (k & 1u) ? mid + half : mid - half;
+        if (half > mid) row = k;             // above ran out: the rest, in order, lie below
+        else if (row >= vp->rh) row = mid - half;  // below ran out (even heights): keep above
         ty = vp->ry0 + row;
-        tx = vp->rx0 + (local - row * vp->rw);
+        tx = vp->rx0 + (local - k * vp->rw);
         return vp;
     }
     uint32_t u = t - vp->out_begin;
