@@ -227,3 +227,41 @@ def test_bins_count_is_checked(gc, torch_cuda):
     cm.set_brick_bins(bins)
     cm.set_brick_bins(None)  # removed
     cm.close()
+
+
+def test_bins_set_and_removed_mid_run(gc, torch_cuda):
+    """Bins given after bricks are resident, then taken away: the per-entry
+    table is rebuilt each time (resident bricks keep their own bins) and the
+    warm image stays the same bit for bit."""
+    built = build(gc, torch_cuda, (96, 96, 96), 1, 16, 1, (1, 1, 1))
+    vol, layout, store, offs, empty, bins = built
+    tf = scenario.ramp_tf()
+    tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
+    cm = gc.CacheManager(vol, layout, IN_CORE, max_requests=96)
+    cm.set_source_host(store, offs, empty)
+    st = torch_cuda.zeros(1, dtype=torch_cuda.int32, device="cuda")
+    (W, H), cam, dist = SPECS[2]
+    g = (torch_cuda.zeros(W * H, dtype=torch_cuda.int32, device="cuda"),
+         torch_cuda.zeros(W * H, dtype=torch_cuda.float32, device="cuda"),
+         torch_cuda.zeros(W * H * 4, dtype=torch_cuda.float32, device="cuda"))
+    v = gc.make_view(scenario.orbit_camera(gc, cam, 12, dist), W, H, tf_dev.data_ptr(), 256, g[0].data_ptr(),
+                     g[1].data_ptr(), g[2].data_ptr())
+    v.status = st.data_ptr()
+
+    def warm_image():
+        assert converge(cm, v, st)
+        for x in g:
+            x.zero_()
+        st.zero_()
+        cm.render(v)
+        cm.update()
+        assert int(st.item()) == 0
+        return g[0].cpu().numpy()
+
+    ref = warm_image()
+    cm.set_brick_bins(bins)
+    assert np.array_equal(warm_image(), ref)
+    cm.set_brick_bins(None)
+    assert np.array_equal(warm_image(), ref)
+    assert cm.stats().device_error == 0
+    cm.close()
