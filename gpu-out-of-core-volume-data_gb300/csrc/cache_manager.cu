@@ -1640,6 +1640,7 @@ int gc_batch_create(gc_cache_t C, const gc_batch_desc *desc, gc_batch_t *out) {
         GC_REQUIRE(desc->max_views >= 1 && desc->max_views <= C->max_views, "max_views must be in [1, 256]");
         GC_REQUIRE(desc->max_pixels >= 1, "max_pixels must be >= 1");
         GC_REQUIRE(!desc->overlap_loads || !C->sync_mode(), "overlapped loads need the asynchronous loader");
+        GC_REQUIRE(!desc->overlap_loads || !(desc->park_above > 0.f), "parking is not available with overlapped loads");
         GC_CUDA(cudaSetDevice(C->device));
         b = new gc_batch();
         b->cache = C;

@@ -497,7 +497,7 @@ typedef struct gc_batch_desc {
                                 admitted view leaves the batch for the front of
                                 the queue with its progressive state kept, and
                                 resumes when admission allows (<= 0: never; not
-                                applied with overlap_loads)                    */
+                                available with overlap_loads)                  */
     uint32_t reorder_window; /* locality-aware admission: pick, among the first
                                 reorder_window queued views, the one whose
                                 camera is nearest the last admitted view's

@@ -306,6 +306,18 @@ def test_batch_scheduler_matches_single_views(gc, orc, torch_cuda, park, sync, r
     assert in_flight_marks(gc, s2.cm, s2.oc.nentries) == 0
 
 
+def test_overlapped_batch_argument_checks(gc, orc, torch_cuda):
+    """Overlapped loads need the asynchronous loader and exclude parking."""
+    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 64, sync=True)
+    with pytest.raises(gc.GcError, match="asynchronous loader"):
+        gc.Batch(s.cm, overlap_loads=True)
+    s.cm.close()
+    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 64, sync=False)
+    with pytest.raises(gc.GcError, match="parking"):
+        gc.Batch(s.cm, overlap_loads=True, park_above=0.5)
+    s.cm.close()
+
+
 def test_overlapped_batch_closed_mid_load(gc, orc, torch_cuda):
     """A batch with overlapped loads that ends while bricks are in flight
     installs or releases them: no page-directory entry stays marked, and the
