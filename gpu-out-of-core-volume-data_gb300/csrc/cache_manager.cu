@@ -514,6 +514,7 @@ static bool update(gc_cache *C, cudaStream_t s) {
             C->done = false;
         } else {
             scan_requests(C, s);
+            C->cur_load = 0;  // the loader serves list 0 (an overlapped batch may have left 1)
             C->done = serve_request(C);
             converged = (C->stats.last_requests == 0);
         }
@@ -537,6 +538,7 @@ static bool update(gc_cache *C, cudaStream_t s) {
         } else {
             lk.unlock();
             scan_requests(C, s);
+            C->cur_load = 0;  // the loader serves list 0 (an overlapped batch may have left 1)
             lk.lock();
             C->busy = true;
             C->has_request = true;
@@ -1319,6 +1321,7 @@ static bool batch_update(gc_cache *C, cudaStream_t s) {
     if (C->sync_mode()) {
         if (!C->done) {
             scan_requests(C, s);
+            C->cur_load = 0;  // the loader serves list 0 (an overlapped batch may have left 1)
             C->done = serve_request(C);
             scanned = true;
         }
@@ -1327,6 +1330,7 @@ static bool batch_update(gc_cache *C, cudaStream_t s) {
         if (!C->busy && !C->done) {
             lk.unlock();
             scan_requests(C, s);
+            C->cur_load = 0;  // the loader serves list 0 (an overlapped batch may have left 1)
             lk.lock();
             C->busy = true;
             C->has_request = true;
@@ -1416,6 +1420,7 @@ static void batch_drain_loads(gc_batch *b) {
                                 C->mrpd, s);
         b->slot_state[k] = 0;
     }
+    C->cur_load = 0;
     cudaStreamSynchronize(s);
 }
 
