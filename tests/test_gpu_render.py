@@ -318,10 +318,12 @@ def test_overlapped_batch_argument_checks(gc, orc, torch_cuda):
     s.cm.close()
 
 
-def test_overlapped_batch_closed_mid_load(gc, orc, torch_cuda):
+@pytest.mark.parametrize("ticks", [1, 2, 3, 4, 5])
+def test_overlapped_batch_closed_mid_load(gc, orc, torch_cuda, ticks):
     """A batch with overlapped loads that ends while bricks are in flight
     installs or releases them: no page-directory entry stays marked, and the
-    plain frame loop then renders a view to the image it gets alone."""
+    plain frame loop then renders a view to the image it gets alone, whichever
+    of the two miss lists the batch used last."""
     specs = [((64, 48), 1), ((33, 17), 4), ((96, 80), 7)]
     tf_dev = torch_cuda.from_numpy(scenario.ramp_tf().reshape(-1)).cuda()
     single = single_view_images(gc, orc, torch_cuda, specs, tf_dev)
@@ -330,7 +332,7 @@ def test_overlapped_batch_closed_mid_load(gc, orc, torch_cuda):
     for i, ((W, H), cam) in enumerate(specs):
         g, _ = s.buffers(W, H)
         b.submit(s.view(scenario.orbit_camera(gc, cam, 12, 3.0), W, H, tf_dev, 256, g), tag=i)
-    for _ in range(3):
+    for _ in range(ticks):
         b.tick()
     b.close()
     torch_cuda.cuda.synchronize()
