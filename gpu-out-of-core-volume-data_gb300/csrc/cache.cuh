@@ -147,6 +147,8 @@ struct InstallArgs {
     uint64_t big_stride;       // staging stride of one big brick
     uint32_t sx, sy;
     uint32_t B, Beff;
+    uint32_t *owner;           // per page-directory entry: lowest list index naming it (~0 between installs)
+    uint64_t *coords;          // per list element: its page-directory entry
     const uint4 *asked;        // partitioned asked list: non-empty first
     const uint32_t *big_index; // per non-empty brick
     const uint4 *big_coord;    // per loaded big brick
@@ -165,7 +167,7 @@ void launch_live_bins(const LevelTables &lt, const float4 *slot_vpos, const uint
 void launch_brick_bins(const uint8_t *level, const uint32_t nb[3], const uint32_t nbig[3], const uint32_t bb[3],
                        uint32_t B, uint32_t eb, unsigned long long *bins, cudaStream_t s);
 void launch_gather_bricks(const ulonglong2 *src, uint32_t n, uint64_t stride, uint8_t *dst, bool vec16,
-                          cudaStream_t s);
+                          bool beside, cudaStream_t s);
 // In-flight marks (page-directory flag 3) of the batched form's overlapped
 // loads: mark the first min(ctl->total, maxreq) entries of a miss list; unmark
 // (3 -> 0) the first n entries of a list after its install.

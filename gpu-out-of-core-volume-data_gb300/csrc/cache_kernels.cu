@@ -417,36 +417,35 @@ __global__ void __launch_bounds__(256) install_place_kernel(InstallArgs a, const
 // hierarchy: in list order (non-empty first), an unmapped entry becomes
 // {slot position, 1} or {0, 0, 0, 2} for an empty brick; an entry that is
 // already mapped or empty is left alone.  The reference walks the list in one
-// thread; here each brick is one thread and a brick whose MRPD entry also
-// belongs to an earlier list element yields to it, which is the serial order.
-__global__ void __launch_bounds__(1024) install_reference_kernel(InstallArgs a, const LevelTables lt,
-                                                                 float one_over_beff) {
-    extern __shared__ uint64_t s_coord[];
-    for (uint32_t i = threadIdx.x; i < a.n; i += blockDim.x) {
-        const uint4 b = a.asked[i];
-        const float4 v = brick_origin(lt, b, one_over_beff);
-        s_coord[i] = mrpd_index(lt, b.w, v.x, v.y, v.z, a.mx, a.my);
-    }
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < a.n; i += blockDim.x) {
-        const uint64_t c = s_coord[i];
-        bool dup = false;
-        for (uint32_t j = 0; j < i; ++j)
-            if (s_coord[j] == c) {
-                dup = true;
-                break;
-            }
-        if (dup || c >= a.nentries) continue;
-        const uint4 e = a.mrpd[c];
-        if (e.w == 1u || e.w == 2u) continue;  // mapped or empty already (3 = in flight: install it)
-        if (i < a.n_nonempty) {
-            const uint32_t slot = a.order[a.nslots - a.n_nonempty + i];
-            const uint32_t sx = slot % a.sx, sy = (slot / a.sx) % a.sy, sz = slot / (a.sx * a.sy);
-            a.mrpd[c] = make_uint4(sx * a.B, sy * a.B, sz * a.B, 1u);
-            a.entry_bins[c] = a.slot_bins[slot];
-        } else {
-            a.mrpd[c] = make_uint4(0, 0, 0, 2u);
-        }
+// thread; here each brick is one thread, and a brick whose MRPD entry also
+// belongs to an earlier list element yields to it, which is the serial order:
+// the first pass leaves the lowest list index naming each entry in `owner`,
+// the second lets only that element act (and puts the owner word back).
+__global__ void install_owner_kernel(InstallArgs a, const LevelTables lt, float one_over_beff) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const uint4 b = a.asked[i];
+    const float4 v = brick_origin(lt, b, one_over_beff);
+    const uint64_t c = mrpd_index(lt, b.w, v.x, v.y, v.z, a.mx, a.my);
+    a.coords[i] = c;
+    if (c < a.nentries) atomicMin(a.owner + c, i);
+}
+
+__global__ void install_reference_kernel(InstallArgs a) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const uint64_t c = a.coords[i];
+    if (c >= a.nentries || a.owner[c] != i) return;  // an earlier element names the same entry
+    a.owner[c] = 0xffffffffu;  // later readers see a value that is not their index either way
+    const uint4 e = a.mrpd[c];
+    if (e.w == 1u || e.w == 2u) return;  // mapped or empty already (3 = in flight: install it)
+    if (i < a.n_nonempty) {
+        const uint32_t slot = a.order[a.nslots - a.n_nonempty + i];
+        const uint32_t sx = slot % a.sx, sy = (slot / a.sx) % a.sy, sz = slot / (a.sx * a.sy);
+        a.mrpd[c] = make_uint4(sx * a.B, sy * a.B, sz * a.B, 1u);
+        a.entry_bins[c] = a.slot_bins[slot];
+    } else {
+        a.mrpd[c] = make_uint4(0, 0, 0, 2u);
     }
 }
 
@@ -521,12 +520,10 @@ void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s)
         GC_CUDA(cudaGetLastError());
         count_launch();
     }
-    const size_t smem = static_cast<size_t>(a.n) * sizeof(uint64_t);
-    GC_REQUIRE(smem <= 200 * 1024, "too many bricks in one install");
-    if (smem > 48 * 1024)
-        GC_CUDA(cudaFuncSetAttribute(install_reference_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem)));
-    install_reference_kernel<<<1, 1024, smem, s>>>(a, lt, one_over_beff);
+    install_owner_kernel<<<div_up(a.n, 256u), 256, 0, s>>>(a, lt, one_over_beff);
+    GC_CUDA(cudaGetLastError());
+    count_launch();
+    install_reference_kernel<<<div_up(a.n, 256u), 256, 0, s>>>(a);
     GC_CUDA(cudaGetLastError());
     count_launch();
 }
@@ -535,19 +532,18 @@ void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s)
 // block-strided over bricks, each brick copied by the whole block with
 // 16-byte loads when aligned.  The reads travel over the host link; the
 // writes land in the device staging buffer the install kernels read.
-// Four independent loads per thread are in flight before their stores: the
+// kIlp independent loads per thread are in flight before their stores: the
 // host link's latency (microseconds) needs many bytes in flight per SM.
-template <typename W>
-__global__ void gather_bricks_kernel(const ulonglong2 *__restrict__ src, uint32_t n, uint64_t stride,
-                                     uint8_t *__restrict__ dst) {
-    constexpr uint32_t kIlp = 4;
+template <typename W, uint32_t kIlp>
+__device__ __forceinline__ void gather_bricks(const ulonglong2 *__restrict__ src, uint32_t n, uint64_t stride,
+                                              uint8_t *__restrict__ dst) {
     for (uint32_t b = blockIdx.x; b < n; b += gridDim.x) {
         const ulonglong2 e = src[b];  // {address, bytes}
         const W *sp = reinterpret_cast<const W *>(e.x);
         W *dp = reinterpret_cast<W *>(dst + static_cast<uint64_t>(b) * stride);
         const uint64_t words = e.y / sizeof(W);
-        const uint64_t stride = static_cast<uint64_t>(blockDim.x) * kIlp;
-        for (uint64_t i0 = threadIdx.x; i0 < words; i0 += stride) {
+        const uint64_t step = static_cast<uint64_t>(blockDim.x) * kIlp;
+        for (uint64_t i0 = threadIdx.x; i0 < words; i0 += step) {
             W v[kIlp];
 #pragma unroll
             for (uint32_t k = 0; k < kIlp; ++k) {
@@ -562,18 +558,42 @@ __global__ void gather_bricks_kernel(const ulonglong2 *__restrict__ src, uint32_
         }
     }
 }
+template <typename W>
+__global__ void gather_bricks_kernel(const ulonglong2 *__restrict__ src, uint32_t n, uint64_t stride,
+                                     uint8_t *__restrict__ dst) {
+    gather_bricks<W, 4>(src, n, stride, dst);
+}
+// At most 32 registers per thread (128 threads, 16 blocks): fits beside the ray caster.
+template <typename W>
+__global__ void __launch_bounds__(128, 16) gather_bricks_beside_kernel(const ulonglong2 *__restrict__ src, uint32_t n,
+                                                                      uint64_t stride, uint8_t *__restrict__ dst) {
+    gather_bricks<W, 2>(src, n, stride, dst);
+}
 
 void launch_gather_bricks(const ulonglong2 *src, uint32_t n, uint64_t stride, uint8_t *dst, bool vec16,
-                          cudaStream_t s) {
+                          bool beside, cudaStream_t s) {
     if (n == 0) return;
-    // one block of 256 per SM (four 16-byte loads in flight per thread)
-    // saturates the host link; more would only take SM slots from the ray
-    // caster running beside it
-    const uint32_t grid = std::min<uint32_t>(n, static_cast<uint32_t>(sm_count()));
-    if (vec16)
-        gather_bricks_kernel<uint4><<<grid, 256, 0, s>>>(src, n, stride, dst);
-    else
-        gather_bricks_kernel<uint8_t><<<grid, 256, 0, s>>>(src, n, stride, dst);
+    const uint32_t sms = static_cast<uint32_t>(sm_count());
+    if (beside) {
+        // Next to a persistent ray-caster launch: at its occupancy each SM
+        // sub-partition keeps 1024 registers free, room for one warp of 32
+        // registers per thread -- a 128-thread block of 4 warps per SM runs
+        // during the render instead of after it (two 16-byte loads in flight
+        // per thread).
+        const uint32_t grid = std::min<uint32_t>(n, 2 * sms);
+        if (vec16)
+            gather_bricks_beside_kernel<uint4><<<grid, 128, 0, s>>>(src, n, stride, dst);
+        else
+            gather_bricks_beside_kernel<uint8_t><<<grid, 128, 0, s>>>(src, n, stride, dst);
+    } else {
+        // alone on the device: one block of 256 per SM (four 16-byte loads in
+        // flight per thread) saturates the host link
+        const uint32_t grid = std::min<uint32_t>(n, sms);
+        if (vec16)
+            gather_bricks_kernel<uint4><<<grid, 256, 0, s>>>(src, n, stride, dst);
+        else
+            gather_bricks_kernel<uint8_t><<<grid, 256, 0, s>>>(src, n, stride, dst);
+    }
     GC_CUDA(cudaGetLastError());
     count_launch();
 }

@@ -125,6 +125,8 @@ struct gc_cache {
     gc::ScanCtl *ctl_lru = nullptr, *ctl_miss = nullptr;
     uint32_t *d_count = nullptr, *d_misc = nullptr, *d_queue = nullptr;
     uint4 *d_asked = nullptr, *d_big_coord = nullptr;
+    uint32_t *d_owner = nullptr;   // install: lowest list index per page-directory entry (~0 between installs)
+    uint64_t *d_coords = nullptr;  // install: page-directory entry per list element
     uint32_t *d_big_index = nullptr;
     ulonglong2 *d_src = nullptr;      // gather list: {host address, bytes} per big brick
     uint8_t *d_staging = nullptr;
@@ -356,7 +358,7 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     GC_CUDA(cudaEventRecord(C->ev_upload_begin, s));
     if (nbig && gather) {
         GC_CUDA(cudaMemcpyAsync(C->d_src, C->h_src, nbig * sizeof(ulonglong2), cudaMemcpyHostToDevice, s));
-        launch_gather_bricks(C->d_src, nbig, C->big_stride, C->d_staging, C->vec16, s);
+        launch_gather_bricks(C->d_src, nbig, C->big_stride, C->d_staging, C->vec16, !C->sync_mode(), s);
     } else if (nbig) {
         GC_CUDA(cudaMemcpyAsync(C->d_staging, C->h_staging, static_cast<size_t>(nbig) * C->big_stride,
                                 cudaMemcpyHostToDevice, s));
@@ -480,6 +482,8 @@ static void install(gc_cache *C, cudaStream_t s) {
     a.user_bins = C->user_bins;
     a.nc = C->nc;
     a.asked = C->d_asked;
+    a.owner = C->d_owner;
+    a.coords = C->d_coords;
     a.big_index = C->d_big_index;
     a.big_coord = C->d_big_coord;
     a.staging = C->d_staging;
@@ -564,7 +568,7 @@ static void destroy(gc_cache *C) {
     cudaDeviceSynchronize();
     void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool, C->slot_bins, C->entry_bins, C->user_bins, C->d_samples,
                    C->status_lru, C->status_miss, C->ctl_lru, C->ctl_miss, C->d_count, C->d_misc, C->d_queue,
-                   C->lists[0].d, C->lists[1].d, C->d_asked, C->d_big_coord, C->d_big_index, C->d_src,
+                   C->lists[0].d, C->lists[1].d, C->d_asked, C->d_owner, C->d_coords, C->d_big_coord, C->d_big_index, C->d_src,
                    C->d_staging, C->d_views};
     for (void *p : dev)
         if (p) cudaFree(p);
@@ -908,6 +912,9 @@ int gc_cache_create_shared(const gc_cache_desc *desc, const gc_volume_desc *volu
         C->d_queue = dalloc<uint32_t>(4, "work queue");
         for (auto &L : C->lists) L.d = dalloc<uint4>(maxr, "miss list");
         C->d_asked = dalloc<uint4>(maxr, "asked list");
+        C->d_coords = dalloc<uint64_t>(maxr, "install entries");
+        C->d_owner = dalloc<uint32_t>(C->nentries, "install owners");
+        GC_CUDA(cudaMemset(C->d_owner, 0xff, C->nentries * sizeof(uint32_t)));
         C->d_big_coord = dalloc<uint4>(maxr, "big brick coords");
         C->d_big_index = dalloc<uint32_t>(maxr, "big brick indexes");
         C->d_src = dalloc<ulonglong2>(maxr, "brick gather list");
@@ -1560,6 +1567,20 @@ static void batch_tick_overlapped(gc_batch *b, gc_cache *C, cudaStream_t s, uint
     if (free_slot >= 0)
         for (uint32_t i = 0; i < na; ++i)
             if (b->active[i].wait == 0 || b->completed.count(b->active[i].wait)) sel.push_back(i);
+    // With no load in flight or waiting, the ready views are split into two
+    // cohorts of about equal pixels: the first renders now and its bricks
+    // load while the second renders in the next tick, and from then on each
+    // cohort renders while the other's bricks load.
+    if (sel.size() >= 2 && b->slot_state[0] == 0 && b->slot_state[1] == 0) {
+        uint64_t total = 0, half = 0;
+        for (uint32_t i : sel) total += static_cast<uint64_t>(b->active[i].view.width) * b->active[i].view.height;
+        size_t k = 0;
+        while (k < sel.size() - 1 && 2 * half < total) {
+            half += static_cast<uint64_t>(b->active[sel[k]].view.width) * b->active[sel[k]].view.height;
+            ++k;
+        }
+        sel.resize(std::max<size_t>(k, 1));
+    }
     if (sel.empty()) {
         if (na) {
             const auto t0 = std::chrono::steady_clock::now();
