@@ -1,0 +1,196 @@
+"""Parity against the reference's OWN GPU code run on the same GPU.
+
+oracle/_ref/librefgpu.so (oracle/build.py + oracle/ref_gpu_driver.cu) compiles
+the reference's Mipmapper.cu, CacheManagerKernels.cu + CacheManager.hpp +
+RequestHandler.hpp and RayCasters.cu, unchanged, from a staged copy of its
+sources.  These tests feed the reference and the CUDA path the same voxels
+and compare:
+
+  * mip pyramid, brick files, empty bricks, level sizes      -- bit-exact;
+  * the cache state machine in lockstep: each frame both caches get the
+    reference ray caster's usage/request buffers, both update, and the LRU
+    order, page directory, miss list, converged flag, completude and pool
+    bytes must be equal                                          -- bit-exact;
+  * the ray caster: each frame both renderers start from the same cache state
+    and the same progressive buffers; RGBA within RGBA_TOL (1/255) per channel.
+
+The reference hard-codes its transfer function at 128 samples and early ray
+termination at alpha 0.95 (RayCasters.cu:137); both sides use those here.
+Its kernels run with nvcc's default FMA contraction and the texture unit's
+filtering; the CUDA path computes the same method in exactly rounded FP32
+(see RGBA_TOL)."""
+import os
+
+import numpy as np
+import pytest
+
+import scenario
+from oracle import refgpu
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(not refgpu.available(),
+                                 reason="no staged copy of the reference sources (oracle/_ref/src)")]
+
+RGBA_TOL = 1  # per channel, in 1/255 units
+
+# name: size, bytes per voxel, B, covering, empty threshold (voxel units), pool slots, W, H, mode, views, frames/view
+GEOMS = {
+    "c1_u8": ((256, 256, 256), 1, 16, 1, 0.0),
+    "u16_empty": ((256, 256, 256), 2, 16, 1, 30.0 * 257),
+    "u8_b32_c2": ((128, 128, 128), 1, 32, 2, 28.0),
+}
+
+
+@pytest.fixture(scope="module")
+def prepared(gc, torch_cuda, tmp_path_factory):
+    """Each geometry preprocessed once by the reference and by the CUDA path."""
+    cache = {}
+
+    def get(name):
+        if name in cache:
+            return cache[name]
+        size, bpc, B, c, thr = GEOMS[name]
+        vol = gc.volume_desc(size, B, c, bpc, 1)
+        layout = gc.compute_layout(vol)
+        d = scenario.gpu_volume(gc, torch_cuda, size, bpc, 7 + len(cache), 10)
+        ref = refgpu.RefGpu(tmp_path_factory.mktemp(name), size, B, c, bpc)
+        ref.preprocess(d.cpu().numpy(), empty_threshold=thr)
+        store, offs, empty = gc.pre_process(vol, layout, d, empty_threshold=thr if thr > 0 else None)
+        cache[name] = (vol, layout, d, ref, store, offs, empty)
+        return cache[name]
+
+    return get
+
+
+@pytest.mark.parametrize("name", sorted(GEOMS))
+def test_preprocess_matches_reference(gc, torch_cuda, prepared, name):
+    """Mipmapper::process, process_bricking, BrickProcessor::process_empty and
+    write_bricks_xml of the reference vs gc_mip_build, gc_bricks_build and
+    gc_bricks_empty on the device."""
+    vol, layout, d, ref, store, offs, empty = prepared(name)
+    eb = vol.encoded_bytes
+    # mip levels, bit for bit
+    poffs, total = gc.pyramid_offsets(layout, eb)
+    pyr = torch_cuda.empty(total, dtype=torch_cuda.uint8, device="cuda")
+    pyr[: d.numel()].copy_(d.view(torch_cuda.uint8))
+    gc.Mipmapper.process(pyr.data_ptr(), layout, poffs, eb, 1)
+    torch_cuda.cuda.synchronize()
+    host = pyr.cpu().numpy()
+    dt = np.uint8 if eb == 1 else np.uint16
+    for l in range(1, layout.nb_levels):
+        dims = tuple(layout.initial[l])
+        n = dims[0] * dims[1] * dims[2] * eb
+        ours = host[poffs[l]: poffs[l] + n].view(dt)
+        theirs = ref.mip_level(l, dims)
+        assert np.array_equal(ours, theirs), f"level {l}: {int(np.count_nonzero(ours != theirs))} voxels differ"
+    # level sizes and empty bricks of bricks.xml
+    ini, real, ref_empty = gc.read_bricks_xml(ref.bricks_xml)
+    assert ini == [tuple(layout.initial[l]) for l in range(layout.nb_levels)]
+    assert real == [tuple(layout.real[l]) for l in range(layout.nb_levels)]
+    assert sorted(ref_empty) == sorted(empty)
+    if GEOMS[name][4] > 0:
+        total_big = sum(int(np.prod(layout.nb_big_bricks[l])) for l in range(layout.nb_levels))
+        assert 0 < len(empty) < total_big, "threshold should leave empty and non-empty bricks"
+    # the reference's brick files hold the bytes of the device bricker
+    theirs = np.zeros(store.numel(), np.uint8)
+    gc.read_brick_files(ref.voldir, vol, layout, theirs, offs, threads=8)
+    assert np.array_equal(theirs, store.numpy())
+
+
+def stable_nonempty_first(lst, empty_keys, gc, vol):
+    """RequestHandler::handle_request's reorder (RequestHandler.hpp:353-368):
+    bricks of non-empty big bricks first, each group in list order."""
+    bb = vol.big_brick_size
+    es = set(empty_keys)
+    flag = [gc.brick_key(int(w), int(x) // bb[0], int(y) // bb[1], int(z) // bb[2]) in es for x, y, z, w in lst]
+    return np.array([e for e, f in zip(lst, flag) if not f] + [e for e, f in zip(lst, flag) if f],
+                    dtype=np.uint32).reshape(-1, 4)
+
+
+def rgba_diff(a, b):
+    return np.abs(a.view(np.uint8).astype(np.int32) - b.view(np.uint8).astype(np.int32))
+
+
+# name: geometry, pool slots, W, H, mode, camera distances (one view each), frame cap per view
+LOCKSTEP = {
+    "c1_dvr_orbit": ("c1_u8", (21, 21, 21), 512, 512, 0, [2.0] * 12, 200),
+    "c1_mop": ("c1_u8", (21, 21, 21), 256, 256, 1, [2.0, 1.4, 2.6], 200),
+    "u16_evicting_dvr": ("u16_empty", (9, 9, 9), 256, 256, 0, [3.0, 2.2, 1.2, 0.8, 2.4], 40),
+    "b32_c2_dvr": ("u8_b32_c2", (6, 6, 6), 192, 160, 0, [2.4, 1.0], 60),
+}
+
+
+@pytest.mark.parametrize("case", sorted(LOCKSTEP))
+def test_cache_and_ray_caster_match_reference(gc, torch_cuda, prepared, case):
+    geom, pool, W, H, mode, dists, cap = LOCKSTEP[case]
+    vol, layout, d, ref, store, offs, empty = prepared(geom)
+    t = torch_cuda
+    ref.open(pool)
+    try:
+        cm = gc.CacheManager(vol, layout, pool, max_requests=50, sync_loader=True)
+        cm.set_source_host(store, offs, empty_keys=empty)
+        assert tuple(cm.info.mrpd_dims) == ref.mrpd_dims
+        # LOD tables of display_volume_raycaster
+        inv, steps = ref.lod_tables()
+        assert inv.shape[0] == layout.nb_levels
+        tf = scenario.ramp_tf(width=128) if mode == 0 else scenario.bumps_tf(5, width=128)
+        tf_dev = t.from_numpy(tf.reshape(-1).copy()).cuda()
+        pad = W + 16  # the reference tests x > width: one more row of slack
+        mk = lambda dt, k=1: t.zeros((W * H + pad) * k, dtype=dt, device="cuda")
+        r_rgba, r_t, r_st = mk(t.int32), mk(t.float32), mk(t.float32, 4)
+        o_rgba, o_t, o_st = mk(t.int32), mk(t.float32), mk(t.float32, 4)
+        nslots = pool[0] * pool[1] * pool[2]
+        B3 = vol.brick_size ** 3
+        worst, frames, differing_px, usage_mismatch, t_mismatch = 0, 0, 0, 0, 0
+        for vi, dist in enumerate(dists):
+            m = scenario.orbit_camera(gc, vi, len(dists), dist)
+            for x in (r_rgba, r_t, r_st):
+                x.zero_()
+            view = gc.make_view(m, W, H, tf_dev.data_ptr(), 128, o_rgba.data_ptr(), o_t.data_ptr(), o_st.data_ptr(),
+                                mode=mode)
+            for f in range(cap):
+                # both renderers start from the reference's progressive state
+                o_t.copy_(r_t)
+                o_st.copy_(r_st)
+                ref.render(m, W, H, view.tstep, tf, mode, r_rgba.data_ptr(), r_t.data_ptr(), r_st.data_ptr())
+                cm.render(view)
+                t.cuda.synchronize()
+                dif = rgba_diff(o_rgba[: W * H].cpu().numpy(), r_rgba[: W * H].cpu().numpy())
+                worst = max(worst, int(dif.max()))
+                differing_px += int(np.count_nonzero(dif.max(axis=-1) if dif.ndim > 1 else dif))
+                assert dif.max() <= RGBA_TOL, f"view {vi} frame {f}: RGBA off by {dif.max()}/255"
+                t_mismatch += int((o_t[: W * H] != r_t[: W * H]).sum())
+                # the cache state machine: both caches take the reference's buffers
+                ru, rq = ref.dump(refgpu.DUMP_USAGE), ref.dump(refgpu.DUMP_REQUESTS)
+                ou, oq = cm.dump(gc.DUMP_USAGE, np.zeros_like(ru)), cm.dump(gc.DUMP_REQUESTS, np.zeros_like(rq))
+                usage_mismatch += int(np.count_nonzero(ou != ru)) + int(np.count_nonzero(oq != rq))
+                cm.load_buffer(gc.DUMP_USAGE, ru)
+                cm.load_buffer(gc.DUMP_REQUESTS, rq)
+                ts = ref.timestamp()
+                assert cm.timestamp() == ts
+                c_ref, c_ours = ref.update(), cm.update()
+                frames += 1
+                tag = f"view {vi} frame {f} (ts {ts})"
+                assert c_ref == c_ours, tag
+                lru = cm.dump(gc.DUMP_LRU, np.zeros(nslots, refgpu.LRU_DTYPE))
+                assert np.array_equal(lru, ref.dump(refgpu.DUMP_LRU)), tag + ": LRU order"
+                mrpd = cm.dump(gc.DUMP_MRPD, np.zeros(int(np.prod(ref.mrpd_dims)) * 4, np.uint32))
+                assert np.array_equal(mrpd, ref.dump(refgpu.DUMP_MRPD)), tag + ": page directory"
+                # a scan that found bricks hands them to the reference's
+                # request handler, which puts non-empty big bricks first
+                total, ours = cm.last_misses()
+                asked, _ = ref.asked()
+                if len(ours):
+                    assert np.array_equal(stable_nonempty_first(ours, empty, gc, vol), asked), tag + ": miss list"
+                if f % 4 == 3 or c_ref:
+                    pool_b = cm.dump(gc.DUMP_POOL, np.zeros(nslots * B3 * vol.encoded_bytes, np.uint8))
+                    assert np.array_equal(pool_b, ref.dump(refgpu.DUMP_POOL).view(np.uint8)), tag + ": pool"
+                    assert cm.completude() == ref.completude(), tag
+                if c_ref:
+                    break
+        assert cm.stats().device_error == 0
+        print(f"\n{case}: {frames} frames, RGBA max diff {worst}/255, pixels differing {differing_px}, "
+              f"t mismatches {t_mismatch}, usage/request words differing before replay {usage_mismatch}")
+        cm.close()
+    finally:
+        ref.close()
