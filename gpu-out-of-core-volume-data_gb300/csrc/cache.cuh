@@ -125,9 +125,11 @@ void launch_lru_count(const uint32_t *usage, uint32_t nslots, uint32_t ts, uint3
 void launch_lru_partition(const uint32_t *order_in, uint32_t *order_out, const uint32_t *usage, uint32_t ts,
                           uint32_t nslots, const uint32_t *count, uint64_t *status, ScanCtl *ctl,
                           uint32_t epoch, cudaStream_t s);
+// silent_tile: a scan tile that publishes nothing (tests of the bounded
+// look-back's error path; 0xffffffff = none).
 void launch_miss_compact(const uint32_t *req, uint64_t nscan, uint32_t ts, uint32_t maxreq, uint4 *list,
                          const LevelTables &lt, uint32_t mx, uint32_t my, uint64_t *status, ScanCtl *ctl,
-                         uint32_t epoch, cudaStream_t s);
+                         uint32_t epoch, cudaStream_t s, uint32_t silent_tile = 0xffffffffu);
 uint32_t lookback_tiles(uint64_t n);
 
 struct InstallArgs {

@@ -20,6 +20,7 @@
 // Every look-back wait is bounded; on expiry the kernel sets ScanCtl::err.
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -68,13 +69,16 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &t
 
 // Decoupled look-back (one warp).  Status word: [63:62] flag
 // (1 aggregate, 2 inclusive prefix), [61:32] launch epoch, [31:0] value.
-__device__ uint32_t lookback(uint64_t *status, uint32_t tile, uint32_t agg, uint32_t epoch, uint32_t *err) {
+__device__ uint32_t lookback(uint64_t *status, uint32_t tile, uint32_t agg, uint32_t epoch, uint32_t *err,
+                             uint32_t silent_tile = 0xffffffffu) {
     // Called by the 32 lanes of warp 0: each round reads the statuses of the
     // 32 nearest unvisited predecessors at once (lane 0 the nearest) and sums
     // the window up to the first inclusive prefix, waiting while a tile in
     // that range has not published yet.  Returns the exclusive prefix (all
-    // lanes).
+    // lanes).  silent_tile (tests of the error path only) names a tile that
+    // publishes nothing, so that its successor's bounded wait runs out.
     const uint32_t lane = threadIdx.x & 31u;
+    if (tile == silent_tile) return 0;
     const uint32_t ep = epoch & 0x3FFFFFFFu;
     const uint64_t E = static_cast<uint64_t>(ep) << 32;
     if (tile == 0) {
@@ -201,7 +205,7 @@ __global__ void __launch_bounds__(kThreads) miss_compact_kernel(const uint32_t *
                                                                 uint32_t ts, uint32_t maxreq,
                                                                 uint4 *__restrict__ list, const LevelTables lt,
                                                                 uint32_t mx, uint32_t my, uint64_t *status,
-                                                                ScanCtl *ctl, uint32_t epoch) {
+                                                                ScanCtl *ctl, uint32_t epoch, uint32_t silent_tile) {
     __shared__ uint32_t s_tile, s_excl;
     if (threadIdx.x == 0) s_tile = atomicAdd(&ctl->ticket, 1u);
     __syncthreads();
@@ -226,7 +230,7 @@ __global__ void __launch_bounds__(kThreads) miss_compact_kernel(const uint32_t *
     uint32_t tile_total;
     const uint32_t excl_thread = block_exclusive_scan(__popc(flags), tile_total);
     if (threadIdx.x < 32) {
-        const uint32_t e = lookback(status, tile, tile_total, epoch, &ctl->err);
+        const uint32_t e = lookback(status, tile, tile_total, epoch, &ctl->err, silent_tile);
         if (threadIdx.x == 0) s_excl = e;
     }
     __syncthreads();
@@ -481,9 +485,9 @@ void launch_lru_partition(const uint32_t *order_in, uint32_t *order_out, const u
 
 void launch_miss_compact(const uint32_t *req, uint64_t nscan, uint32_t ts, uint32_t maxreq, uint4 *list,
                          const LevelTables &lt, uint32_t mx, uint32_t my, uint64_t *status, ScanCtl *ctl,
-                         uint32_t epoch, cudaStream_t s) {
+                         uint32_t epoch, cudaStream_t s, uint32_t silent_tile) {
     miss_compact_kernel<<<lookback_tiles(nscan), kThreads, 0, s>>>(req, nscan, ts, maxreq, list, lt, mx, my,
-                                                                   status, ctl, epoch);
+                                                                   status, ctl, epoch, silent_tile);
     GC_CUDA(cudaGetLastError());
     count_launch();
 }
@@ -685,6 +689,20 @@ constexpr int kNoAllocMaxDevices = 64;
 static uint64_t *g_noalloc_ptr[kNoAllocMaxDevices] = {};
 static std::mutex g_noalloc_mu;
 
+// The scan's result word for the caller: the count of flagged entries, or
+// GC_MISS_LIST_FAILED when one of its bounded look-back waits ran out (the list
+// is then not valid).  Read on the device, so the call stays asynchronous.
+__global__ void noalloc_total_kernel(const ScanCtl *ctl, uint32_t *out_total) {
+    *out_total = ctl->err ? GC_MISS_LIST_FAILED : ctl->total;
+}
+
+// Test hook of the error path: GC_TEST_NOALLOC_SILENT_TILE=<k> makes scan tile
+// k publish nothing, so that tile k + 1's bounded look-back wait runs out.
+static uint32_t noalloc_silent_tile() {
+    const char *v = std::getenv("GC_TEST_NOALLOC_SILENT_TILE");
+    return (v && *v) ? static_cast<uint32_t>(std::strtoul(v, nullptr, 10)) : 0xffffffffu;
+}
+
 static uint64_t *noalloc_scratch() {
     int dev = 0;
     GC_CUDA(cudaGetDevice(&dev));
@@ -706,6 +724,10 @@ extern "C" int gc_miss_list_noalloc(const uint32_t *requests, uint64_t n_entries
     using namespace gc;
     return guard([&] {
         GC_REQUIRE(requests && layout && out_list && out_total, "null argument");
+        // the scan reads the request words and writes the list 16 bytes at a time
+        GC_REQUIRE(reinterpret_cast<uintptr_t>(requests) % 16 == 0 && reinterpret_cast<uintptr_t>(out_list) % 16 == 0,
+                   "requests and out_list must be 16-byte aligned");
+        GC_REQUIRE(reinterpret_cast<uintptr_t>(out_total) % 4 == 0, "out_total must be 4-byte aligned");
         GC_REQUIRE(n_entries >= 2, "the request buffer needs at least 2 entries");
         GC_REQUIRE(n_entries - 1 <= kNoAllocMaxEntries,
                    "request buffer too large for the allocation-free scan: at most 8388609 entries "
@@ -735,7 +757,9 @@ extern "C" int gc_miss_list_noalloc(const uint32_t *requests, uint64_t n_entries
         GC_CUDA(cudaMemsetAsync(status, 0, lookback_tiles(n_entries - 1) * sizeof(uint64_t), s));
         static std::atomic<uint32_t> epoch{0};
         launch_miss_compact(requests, n_entries - 1, timestamp, max_requests, reinterpret_cast<uint4 *>(out_list),
-                            lt, mx, my, status, ctl, epoch.fetch_add(1) + 1, s);
-        GC_CUDA(cudaMemcpyAsync(out_total, &ctl->total, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+                            lt, mx, my, status, ctl, epoch.fetch_add(1) + 1, s, noalloc_silent_tile());
+        noalloc_total_kernel<<<1, 1, 0, s>>>(ctl, out_total);
+        GC_CUDA(cudaGetLastError());
+        count_launch();
     });
 }

@@ -29,6 +29,7 @@ SAMPLER_REFERENCE, SAMPLER_TRILINEAR = 0, 1
 CACHE_SYNC_LOADER = 1
 CACHE_STAGED_UPLOAD = 2
 DUMP_MRPD, DUMP_LRU, DUMP_USAGE, DUMP_REQUESTS, DUMP_POOL = 0, 1, 2, 3, 4
+MISS_LIST_FAILED = 0xFFFFFFFF  # gc_miss_list_noalloc: a bounded wait of the scan ran out
 
 U3 = C.c_uint32 * 3
 L3 = (C.c_uint32 * 3) * MAX_LEVELS

@@ -348,11 +348,17 @@ int gc_cache_last_misses(gc_cache_t cache, uint32_t *out4, uint32_t max, uint32_
  * library keeps until exit, so it suits callers that cannot allocate (stream
  * capture, hard frame deadlines, hosts that own all device memory).  Limits:
  * n_entries - 1 <= 8,388,608 (2048 scan tiles of 4096); larger buffers are
- * rejected with GC_ERR_INVALID.  The first call on a device looks the array's
+ * rejected with GC_ERR_INVALID.  requests and out_list must be 16-byte
+ * aligned and out_total 4-byte aligned (GC_ERR_INVALID otherwise, before any
+ * device work).  The first call on a device looks the array's
  * address up (cudaGetSymbolAddress): make that first call before any stream
  * capture.  All calls share the array: calls whose work overlaps on the GPU
  * (other streams, other host threads) race and corrupt each other's results;
- * order them on one stream. */
+ * order them on one stream.  The call is asynchronous, so a failure on the
+ * device is reported on the device: when one of the scan's bounded waits ran
+ * out, *out_total receives GC_MISS_LIST_FAILED instead of a count and
+ * out_list is not valid. */
+#define GC_MISS_LIST_FAILED 0xffffffffu
 int gc_miss_list_noalloc(const uint32_t *requests, uint64_t n_entries, uint32_t timestamp,
                          const gc_layout *layout, uint32_t max_requests, uint32_t *out_list,
                          uint32_t *out_total, void *stream);

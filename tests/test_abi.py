@@ -178,3 +178,16 @@ def test_struct_layouts_match_header(tmp_path):
     for cname, pyname in (("gc_view", "View"), ("gc_cache_desc", "CacheDesc"), ("gc_volume_desc", "VolumeDesc"),
                           ("gc_layout", "Layout")):
         assert ctypes.sizeof(getattr(orc, pyname)) == c_layout[(cname, "sizeof")], ("oracle", cname)
+
+
+def test_no_alloc_miss_list_rejects_misaligned_pointers(gc):
+    """gc_miss_list_noalloc reads the request words and writes the list 16
+    bytes at a time: pointers without that alignment are rejected before any
+    device work (the addresses below are never dereferenced)."""
+    vol = gc.volume_desc((64, 64, 64), 16, 1, 1, 1)
+    layout = gc.compute_layout(vol)
+    n = sum(layout.nb_bricks[l][0] for l in range(layout.nb_levels)) * layout.nb_bricks[0][1] * layout.nb_bricks[0][2]
+    for req, lst, tot in ((0x10004, 0x20000, 0x30000), (0x10000, 0x20008, 0x30000), (0x10000, 0x20000, 0x30002)):
+        with pytest.raises(gc.GcError, match="aligned") as e:
+            gc.miss_list_noalloc(req, n, 1, layout, 50, lst, tot)
+        assert e.value.code == 1  # GC_ERR_INVALID

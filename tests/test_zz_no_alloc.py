@@ -61,3 +61,39 @@ def test_no_alloc_miss_list_equals_cache_update(gc, torch_cuda):
         gc.miss_list_noalloc(out_list.data_ptr(), 2048 * 4096 + 2, 1, layout, MAX_REQ, out_list.data_ptr(),
                              out_total.data_ptr())
     cm.close()
+
+
+def test_no_alloc_scan_reports_an_expired_wait(gc, torch_cuda, monkeypatch):
+    """Every look-back wait of the scan is bounded.  The test hook
+    GC_TEST_NOALLOC_SILENT_TILE makes one scan tile publish nothing -- a flag
+    that nothing sets -- so that the next tile's wait runs out: the call must
+    then report GC_MISS_LIST_FAILED in out_total (not hang, not fault), and the
+    next call without the hook must give the right list again (the scratch
+    keeps no stale error)."""
+    torch = torch_cuda
+    vol = gc.volume_desc((256, 256, 256), 16, 1, 1, 1)  # 14,079 entries: 4 scan tiles
+    layout = gc.compute_layout(vol)
+    cm = gc.CacheManager(vol, layout, (8, 8, 8), max_requests=50, sync_loader=True)
+    cm.set_source_callback(lambda *a: gc.BRICK_UNKNOWN)
+    mx, my, mz = cm.info.mrpd_dims
+    n = mx * my * mz
+    rng = np.random.default_rng(7)
+    ts = cm.timestamp()
+    req = request_buffer(rng, layout, mx, my, mz, ts, 300, 100)
+    cm.load_buffer(gc.DUMP_REQUESTS, req)
+    cm.update()
+    total_ref, list_ref = cm.last_misses()
+    d_req = torch.from_numpy(req.view(np.int32)).cuda()
+    out_list = torch.zeros(50 * 4, dtype=torch.int32, device="cuda")
+    out_total = torch.zeros(1, dtype=torch.int32, device="cuda")
+    monkeypatch.setenv("GC_TEST_NOALLOC_SILENT_TILE", "1")
+    gc.miss_list_noalloc(d_req.data_ptr(), n, ts, layout, 50, out_list.data_ptr(), out_total.data_ptr())
+    torch.cuda.synchronize()
+    assert int(out_total.item()) & 0xFFFFFFFF == gc.MISS_LIST_FAILED
+    monkeypatch.delenv("GC_TEST_NOALLOC_SILENT_TILE")
+    gc.miss_list_noalloc(d_req.data_ptr(), n, ts, layout, 50, out_list.data_ptr(), out_total.data_ptr())
+    torch.cuda.synchronize()
+    total = int(out_total.item())
+    assert total == total_ref > 50
+    assert np.array_equal(out_list.cpu().numpy().view(np.uint32).reshape(-1, 4), list_ref)
+    cm.close()
