@@ -10,7 +10,11 @@ counts time until "Frame done" (ref:bench.sh:39-55): restart the progressive
 buffers (the camera moved), then repeat {render, cache update} until the
 update reports an empty miss list.  Each iteration pages the missing bricks in
 from host memory (miss scan -> loader -> upload on a side stream -> install).
-Rays are counted once per converged view.
+Rays are counted once per converged view.  The first `warmup` views of the
+path warm the cache; the `steps` timed views are spread evenly over the rest
+of the path (config.timed_views), so a fly-through's close-up end counts as
+much as its far start.  Both arms time the same views and print the same
+`config`.
 
 Workloads (seeded synthetic volumes with the shapes of the benchmark configs;
 no public dataset is used):
@@ -38,7 +42,9 @@ e2e    : the same through the C ABI with the converged RGBA frame read back
          into pinned host memory inside the timed region; brick bytes paged in
          (H2D) and the frame (D2H) are counted per step.
 --impl reference runs the CPU port of the same method (the oracle's FP32
-ray-march + cache state machine, all host threads) on a bounded sample.
+ray-march + cache state machine, all host threads) over the same views, with
+its brick store built on the host by the oracle: that process loads no GPU
+library.
 """
 import argparse
 import json
@@ -86,7 +92,6 @@ CONFIGS = {
 }
 DIAG = 2.0 * math.sqrt(3.0)
 PIXEL_BYTES = 44  # RGBA 4 + t 4+4 + colour state 16+16 per pixel and launch
-OUR_DEFAULT_STEPS = 40  # views the GPU arm times by default (the reference arm samples that range)
 # DRAM bytes (read + write) of the c2 roofline launch (view 42, converged, after
 # an L2 flush), from one ncu capture of this command:
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none --nvtx
@@ -121,6 +126,50 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+def pool_slots(cfg):
+    """Pool slots of a config: given, or the cube of slots holding pool_bytes
+    of bricks grown round-robin per axis (Application.cu:85-93, the same
+    formula as gc_pool_dims)."""
+    if cfg.get("pool_slots"):
+        return tuple(cfg["pool_slots"])
+    eb = cfg["bpc"] * cfg.get("channels", 1)
+    entries = cfg["pool_bytes"] // (cfg["B"] ** 3 * eb)
+    edge = int(round(entries ** (1.0 / 3.0)))
+    while edge ** 3 > entries:
+        edge -= 1
+    while (edge + 1) ** 3 <= entries:
+        edge += 1
+    d, axis = [edge, edge, edge], 0
+    while d[0] * d[1] * d[2] < entries:
+        d[axis] += 1
+        axis = (axis + 1) % 3
+    return tuple(d)
+
+
+def timed_views(cfg, steps, warmup):
+    """The path views a run times: after views 0 .. warmup-1 (the warm-up),
+    `steps` views spread evenly over the rest of the path, so that the far
+    views at its start and the close-up views at its end both count."""
+    n = cfg["frames"]
+    return [warmup + (i * (n - warmup)) // steps for i in range(steps)]
+
+
+def bench_config(name, cfg, args):
+    """The `config` object of the bench line: static parameters only, the same
+    for the GPU arm and the reference arm."""
+    wl = workload(name, cfg)[0]
+    pool = pool_slots(cfg)
+    eb = cfg["bpc"] * cfg.get("channels", 1)
+    l2 = {"c2": "inputs > L2 (2 GiB pool, 103 MB page directory, 28 GiB host brick store)",
+          "c5": "inputs > L2 (8 GiB pool, 43 GiB host brick store)"}.get(
+        name, "in-core volume; L2 not flushed (the c1 case is for profiling)")
+    return {"workload": wl, "brick_size": cfg["B"], "covering": cfg["c"], "pool_slots": list(pool),
+            "pool_gib": round(pool[0] * pool[1] * pool[2] * cfg["B"] ** 3 * eb / 2 ** 30, 3),
+            "view": [cfg["W"], cfg["H"]], "max_requests": args.max_requests, "early_alpha": cfg["early"],
+            "warmup_views": list(range(args.warmup)), "timed_views": timed_views(cfg, args.steps, args.warmup),
+            "l2": l2}
+
+
 def tf2d_table(seed=5, width=64, height=64):
     """2D RGBA table (height rows of width entries) for two-channel volumes:
     alpha from seeded bumps over channel 0, modulated along channel 1."""
@@ -152,25 +201,49 @@ def tf_table(kind, seed=3):
     return np.concatenate([rgb, np.clip(a, 0, 1)[:, None]], 1).astype(np.float32)
 
 
-def path_camera(gc, cfg, f, rank=0):
+def look_at_host(eye, target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0)):
+    """gc_look_at restated on the host (double arithmetic on the float inputs,
+    rounded to float like the C ABI), so that the CPU arm needs no GPU library:
+    columns (right, up, -forward, eye) of the 3x4 inverse view matrix."""
+    f32 = lambda v: float(np.float32(v))  # noqa: E731
+    e, t, u = [f32(x) for x in eye], [f32(x) for x in target], [f32(x) for x in up]
+
+    def norm(v):
+        n = math.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+        return [v[0] / n, v[1] / n, v[2] / n]
+
+    def cross(a, b):
+        return [a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]]
+
+    fw = norm([t[a] - e[a] for a in range(3)])
+    r = norm(cross(fw, u))
+    uu = cross(r, fw)
+    out = []
+    for a in range(3):
+        out += [f32(r[a]), f32(uu[a]), f32(-fw[a]), e[a]]
+    return out
+
+
+def path_camera(look_at, cfg, f, rank=0):
+    """Camera of view f of the config's path; look_at is gc.look_at or look_at_host."""
     n = cfg["frames"]
     t = (f % n) / max(1, n - 1)
     if cfg["path"] == "cross":  # through the interior, looking ahead along the path
         a, b = (-0.85, -0.25, -0.8), (0.85, 0.3, 0.8)
         eye = tuple(p + (q - p) * t for p, q in zip(a, b))
         ahead = tuple(e + (q - p) * 0.5 for e, p, q in zip(eye, a, b))
-        return gc.look_at(eye, ahead)
+        return look_at(eye, ahead)
     if cfg["path"] == "orbit":
         ang = 2 * math.pi * ((f + rank * 7) % n) / n
         d = cfg["dist"][0] * DIAG
-        return gc.look_at((d * math.sin(ang) * math.cos(0.3), d * math.sin(0.3), d * math.cos(ang) * math.cos(0.3)))
+        return look_at((d * math.sin(ang) * math.cos(0.3), d * math.sin(0.3), d * math.cos(ang) * math.cos(0.3)))
     d = (cfg["dist"][0] + (cfg["dist"][1] - cfg["dist"][0]) * t) * DIAG
     ang = 0.6 * t + 0.4 * rank
     dirv = (math.sin(ang) * 0.8, 0.35, math.cos(ang))
     nrm = math.sqrt(sum(c * c for c in dirv))
     eye = tuple(d * c / nrm for c in dirv)
     target = tuple(0.15 * math.sin(3 * t + rank) * c for c in (1.0, 0.5, 0.2))
-    return gc.look_at(eye, target)
+    return look_at(eye, target)
 
 
 def batch_views(gc, cfg, seed, n):
@@ -427,7 +500,12 @@ def run_ours(args):
     cfg = CONFIGS[args.config]
     vol, layout, store, offs, prep_s = make_store(gc, torch, cfg)
     W, H = cfg["W"], cfg["H"]
-    spec = lambda f: [(path_camera(gc, cfg, f, rank), W, H)]  # noqa: E731
+    spec = lambda f: [(path_camera(gc.look_at, cfg, f, rank), W, H)]  # noqa: E731
+    views = timed_views(cfg, args.steps, args.warmup)
+    assert tuple(pool_slots(cfg)) == tuple(gc.pool_dims(vol, cfg["pool_bytes"]) if cfg["pool_bytes"] else cfg["pool_slots"])
+    # the reference arm computes the same cameras without the GPU library
+    assert all(path_camera(gc.look_at, cfg, f, rank) == path_camera(look_at_host, cfg, f, rank)
+               for f in list(range(args.warmup)) + views)
 
     def plain_pass(e2e):
         """Fresh cache; warm-up views, then the timed views (same views for value and e2e)."""
@@ -436,7 +514,7 @@ def run_ours(args):
             S.converge(spec(f), cap=cfg.get("cap", 64))
         s0, l0 = S.cm.stats(), gc.kernel_launches()
         torch.cuda.nvtx.range_push("timed_e2e" if e2e else "timed")
-        wall, lat, info = timed(torch, S.stream, lambda i: S.converge(spec(args.warmup + i), e2e=e2e,
+        wall, lat, info = timed(torch, S.stream, lambda i: S.converge(spec(views[i]), e2e=e2e,
                                                                       cap=cfg.get("cap", 64)), args.steps)
         torch.cuda.nvtx.range_pop()
         launches = gc.kernel_launches() - l0
@@ -532,16 +610,11 @@ def run_ours(args):
         "metric": "Mrays/s", "value": round(rays / wall / 1e6, 3), "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * wall / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dt, "data": data_txt,
-        "config": {"workload": wl, "brick_size": cfg["B"], "covering": cfg["c"], "pool_slots": list(S.pool),
-                   "pool_gib": round(pool_bytes / 2**30, 3), "view": [W, H], "max_requests": args.max_requests,
-                   "brick_bins": bool(args.brick_bins), "loader": "sync", "upload": "gather kernel reading the host store"
-                   if S.cm.stats().upload_direct else "staged host copies + cudaMemcpyAsync",
-                   "stores": "pinned" if PIN_STORES else "pageable",
-                   "l2": "inputs > L2 (2 GiB pool, 103 MB page directory, 28 GiB host brick store)"
-                   if args.config == "c2" else ("inputs > L2 (8 GiB pool, 43 GiB host brick store)"
-                                                if args.config == "c5" else
-                                                "in-core volume; L2 not flushed (the c1 case is for profiling)"),
-                   "preprocess_s": round(prep_s, 2)},
+        "config": bench_config(args.config, cfg, args),
+        "setup": {"pool_gib": round(pool_bytes / 2**30, 3), "brick_bins": bool(args.brick_bins), "loader": "sync",
+                  "upload": "gather kernel reading the host store" if S.cm.stats().upload_direct
+                  else "staged host copies + cudaMemcpyAsync",
+                  "stores": "pinned" if PIN_STORES else "pageable", "preprocess_s": round(prep_s, 2)},
         "preprocess": {"mip_build_s": round(LAST_PREPROCESS.get("mip_s", 0.0), 4),
                        "mip_build_gbs": round((2 * LAST_PREPROCESS.get("pyramid_bytes", 0) - LAST_PREPROCESS.get(
                            "level0_bytes", 0)) / max(LAST_PREPROCESS.get("mip_s", 1e-9), 1e-9) / 1e9, 1),
@@ -578,6 +651,7 @@ def run_ours(args):
         out["with_brick_bins"] = with_bins
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(gc, S, cfg, last, args)
+        out["parity_max_abs"] = out["cpu_baseline"]["parity"]["max_abs_rgba"]
     S.close()
     del store
     if rank == 0 and not args.no_batched:
@@ -928,6 +1002,12 @@ def cpu_baseline(gc, S, cfg, spec, args):
         if el > args.cpu_seconds:
             break
     oc.close()
+    # parity: the GPU's last render of this view (from scratch, same cache
+    # state) against the oracle's render of it
+    gpu_img = S.buffers(0, W, H)[0].cpu().numpy().view(np.uint8).astype(np.int32)
+    dif = np.abs(gpu_img - rgba.view(np.uint8).astype(np.int32)).reshape(-1, 4).max(axis=1)
+    parity = {"max_abs_rgba": int(dif.max()), "pixels": int(W * H), "pixels_differing": int(np.count_nonzero(dif)),
+              "vs": "the FP32 oracle's render of the same view from the GPU's cache state (units of 1/255)"}
     # the CPU restatement of the mip reduction (down_sampling_inner) on a bounded
     # 512 x 512 x 64 sample of the same voxel type, single thread
     nc = cfg.get("channels", 1)
@@ -963,72 +1043,107 @@ def cpu_baseline(gc, S, cfg, spec, args):
             "mip_cpu_gbs_1thread": round(mip_cpu, 2), "mip_cpu_gbs_all_cores": round(mip_cpu_all, 2),
             "bricking_cpu_gbs_1thread": round(brick_cpu, 3),
             "kind": "port", "sample": f"{frames} renders of one converged {W}x{H} {args.config} view from the GPU's cache "
-                                      f"snapshot (oracle FP32 ray-march, {os.cpu_count()} threads)"}
+                                      f"snapshot (oracle FP32 ray-march, {os.cpu_count()} threads)",
+            "parity": parity}
+
+
+def make_store_cpu(cfg):
+    """The brick store of a config built on the host cores by the oracle alone
+    (generator, mip restatement, bricker restatement checked against the
+    reference's own bricker): no GPU library is loaded."""
+    from oracle import oracle as orc
+
+    size, bpc, nc = cfg["size"], cfg["bpc"], cfg.get("channels", 1)
+    eb = bpc * nc
+    u3 = orc.U3
+    vol = orc.VolumeDesc(u3(*size), cfg["B"], u3(*cfg.get("bb", (1, 1, 1))), cfg["c"], eb, nc, u3(2, 2, 2))
+    layout = orc.layout(vol)
+    t0 = time.time()
+    blobs = orc.blobs(cfg["seed"], cfg["nblobs"], size, cfg["sigma"][0], cfg["sigma"][1], cfg["amp"][0],
+                      cfg["amp"][1])
+    level = orc.generate(size, bpc, cfg["seed"], blobs, cfg["nblobs"], cfg["noise"], channels=nc)
+    for ch in range(1, nc):
+        orc.generate(size, bpc, cfg["seed"] + ch, blobs, cfg["nblobs"], cfg["noise"] * 4, channels=nc, channel=ch,
+                     field=1, out=level)
+    level = level.reshape(-1)
+    t1 = time.time()
+    big = cfg["B"] ** 3 * int(np.prod(cfg.get("bb", (1, 1, 1)))) * eb
+    offs, total = [], 0
+    for l in range(layout.nb_levels):
+        offs.append(total)
+        total += int(np.prod(layout.nb_big_bricks[l])) * big
+    store = np.empty(total, np.uint8)
+    for l in range(layout.nb_levels):
+        if l > 0:
+            level = orc.mip_level(level, tuple(layout.initial[l - 1]), eb, nc, threads=0)
+        n = int(np.prod(layout.nb_big_bricks[l])) * big
+        orc.brick_level(level.view(np.uint8), tuple(layout.initial[l]), vol, tuple(layout.nb_big_bricks[l]),
+                        out=store[offs[l]:offs[l] + n])
+    log(f"volume {size} B{cfg['B']} on the host: generated {t1 - t0:.1f}s, mip + bricks {time.time() - t1:.1f}s "
+        f"({total / 2**30:.2f} GiB)")
+    return vol, layout, store, offs
 
 
 def run_reference(args):
-    """CPU port of the plain path: each view rendered to convergence by the
-    oracle's ray-march + cache state machine on the host cores."""
+    """The reference arm: the CPU port of the plain path (the oracle's FP32
+    ray-march + cache state machine on all host cores), each of the GPU arm's
+    timed views rendered to convergence.  Loads only the oracle library."""
     if int(os.environ.get("RANK", "0")) != 0:
         return
-    import torch
-
-    import gcgb300 as gc
     from oracle import oracle as orc
 
     cfg = CONFIGS[args.config]
-    # inputs: the brick store (built on the device; bytes identical to the
-    # oracle's own mip + bricker, tests/test_gpu_preprocess.py)
-    vol, layout, store, offs, prep_s = make_store(gc, torch, cfg)
-    pool = cfg["pool_slots"] or gc.pool_dims(vol, cfg["pool_bytes"])
-    desc = gc.CacheDesc(vol, layout, gc.u3(pool), args.max_requests, gc.CACHE_SYNC_LOADER, 0)
+    vol, layout, store, offs = make_store_cpu(cfg)
+    pool = pool_slots(cfg)
+    desc = orc.CacheDesc(vol, layout, orc.U3(*pool), args.max_requests, 1, 0)  # GC_CACHE_SYNC_LOADER
     oc = orc.Cache(desc)
-    st_np = store.numpy()
-    oc.set_source(st_np, offs)
+    oc.set_source(store, offs)
     W, H = cfg["W"], cfg["H"]
     tf = tf2d_table() if cfg["tf"] == "2d" else tf_table(cfg["tf"])
     tfh, tfw = (tf.shape[0], tf.shape[1]) if tf.ndim == 3 else (0, tf.shape[0])
-    tf = tf.reshape(-1)
+    tf = np.ascontiguousarray(tf.reshape(-1))
     focal = 1.0 / math.tan(math.radians(cfg["fov"]) / 2)
     rgba = np.zeros(W * H, np.uint32)
     tb = np.zeros(W * H, np.float32)
     st = np.zeros(W * H * 4, np.float32)
+    F3 = orc.C.c_float * 3
 
     def view_to_convergence(f):
-        v = gc.make_view(path_camera(gc, cfg, f), W, H, 0, tfw, 0, 0, 0, tstep=2.0 / 256.0, focal=focal,
-                         early_alpha=cfg["early"], tf_height=tfh)
+        m = path_camera(look_at_host, cfg, f)
+        v = orc.View((orc.C.c_float * 12)(*m), W, H, F3(-1, -1, -1), F3(1, 1, 1), 2.0 / 256.0, focal, cfg["early"],
+                     0, 0, tfw, None, None, None, None, None, 0, tfh, 0)
         tb[:] = 0
         st[:] = 0
         for it in range(cfg.get("cap", 64)):
             oc.render(v, tf, rgba, tb, st)
             if oc.update():
-                return it + 1
+                return it + 1, True
+        return cfg.get("cap", 64), False
 
-    # A bounded sample of the views our arm times (views warmup .. warmup + 39
-    # of the path by default): `steps` views spread evenly over that range.
-    span = OUR_DEFAULT_STEPS
-    picks = sorted({args.warmup + round(i * (span - 1) / max(1, args.steps - 1)) for i in range(args.steps)})
+    views = timed_views(cfg, args.steps, args.warmup)
     for f in range(args.warmup):
         view_to_convergence(f)
-    lat = []
+    lat, info = [], []
     t0 = time.perf_counter()
-    for f in picks:
+    for f in views:
         a = time.perf_counter()
-        view_to_convergence(f)
+        info.append(view_to_convergence(f))
         lat.append(1e3 * (time.perf_counter() - a))
     el = time.perf_counter() - t0
-    value = W * H * len(picks) / el / 1e6
+    value = W * H * len(views) / el / 1e6
+    wl, dt, data_txt = workload(args.config, cfg)
+    sample = (f"the {len(views)} views the GPU arm times, each to convergence after {args.warmup} warm-up views: "
+              f"oracle FP32 ray-march + cache state machine, {os.cpu_count()} threads")
     out = {"impl": "reference", "metric": "Mrays/s", "value": round(value, 4), "unit": "Mrays/s", "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * el / args.steps, 3),
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": workload(args.config, cfg)[1],
-           "data": workload(args.config, cfg)[2],
-           "config": {"workload": workload(args.config, cfg)[0] + " (CPU port on host cores)",
-                      "view": [W, H], "max_requests": args.max_requests, "pool_slots": list(pool)},
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dt, "data": data_txt,
+           "config": bench_config(args.config, cfg, args),
            "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+           "iterations_per_view": {"mean": round(statistics.mean(i for i, _ in info), 2),
+                                   "max": max(i for i, _ in info)},
+           "converged_views": f"{sum(1 for _, c in info if c)}/{len(views)}",
            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
-                            "sample": f"views {picks} of the path (spread over the views the GPU arm times) "
-                                      f"after {args.warmup} warm-up views, each to convergence: oracle FP32 "
-                                      f"ray-march + cache update, {os.cpu_count()} threads"},
+                            "sample": sample},
            "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
     oc.close()
@@ -1075,7 +1190,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="c3: skip the plain loop over the same views")
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = 40 if args.impl == "ours" else 2
+        args.steps = 20
     args.warmup = max(3, args.warmup)
     Session.staged = args.upload == "staged"
     Session.brick_bins = args.brick_bins

@@ -115,6 +115,10 @@ static int64_t value_noise(uint32_t x, uint32_t y, uint32_t z, uint32_t lp, uint
 
 void orc_generate(const gc_generator *g, void *dst) {
     const int64_t maxval = g->bytes_per_channel == 1 ? 255 : 65535;
+    /* every voxel is independent: rows spread over the host threads */
+#ifdef _OPENMP
+#pragma omp parallel for collapse(2) schedule(dynamic, 16)
+#endif
     for (uint32_t z = 0; z < g->size[2]; ++z)
         for (uint32_t y = 0; y < g->size[1]; ++y)
             for (uint32_t x = 0; x < g->size[0]; ++x) {
@@ -987,6 +991,15 @@ static int fetch32(orc_cache *c, uint32_t sampler, uint32_t lod, f3 np, walk *w,
         return 1;
     }
     return 2;
+}
+
+/* One sample of K_CacheManager::get_normalized with a fresh page walk (the
+ * device-side handle's gc_sample_normalized): 0 mapped (*out written), 1
+ * unmapped (requested), 2 empty. */
+int orc_sample_normalized(orc_cache *c, uint32_t level, float x, float y, float z, float *out) {
+    walk w;
+    w.pcx = w.pcy = w.pcz = UINT32_MAX;
+    return fetch32(c, GC_SAMPLER_REFERENCE, level, mk(x, y, z), &w, out);
 }
 
 static void march32(orc_cache *c, const gc_view *v, const float *tf, const lod_tables *T, uint32_t x, uint32_t y,

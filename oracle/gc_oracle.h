@@ -74,6 +74,10 @@ void orc_render(orc_cache *c, const gc_view *view, const float *tf, uint32_t *rg
 void orc_render_f64(orc_cache *c, const gc_view *view, const float *tf, uint32_t *rgba, double *tbuf,
                     double *state, uint32_t *usage, uint32_t *req, int threads);
 
+/* one sample of K_CacheManager::get_normalized with a fresh page walk:
+ * 0 mapped (*out written, usage stamped), 1 unmapped (requested), 2 empty */
+int orc_sample_normalized(orc_cache *c, uint32_t level, float x, float y, float z, float *out);
+
 /* exposed for unit tests of the series pow */
 float orc_pow(float x, float k);
 

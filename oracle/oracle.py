@@ -81,6 +81,7 @@ _SIGS = {
     "orc_render": ([vp, P(View), vp, vp, vp, vp, C.c_int], None),
     "orc_render_f64": ([vp, P(View), vp, vp, vp, vp, vp, vp, C.c_int], None),
     "orc_pow": ([C.c_float, C.c_float], C.c_float),
+    "orc_sample_normalized": ([vp, C.c_uint32, C.c_float, C.c_float, C.c_float, P(C.c_float)], C.c_int),
 }
 
 
@@ -138,11 +139,15 @@ def mip_level(src, dims, eb, nc, threads=1):
     return out
 
 
-def brick_level(level, dims, vol, nb_big):
+def brick_level(level, dims, vol, nb_big, out=None):
+    """out: optional uint8 array (e.g. a slice of a whole store) receiving the bricks."""
     v = conv(VolumeDesc, vol)
     B = v.brick_size
     big = B ** 3 * v.big_brick_size[0] * v.big_brick_size[1] * v.big_brick_size[2] * v.encoded_bytes
-    out = np.zeros(nb_big[0] * nb_big[1] * nb_big[2] * big, dtype=np.uint8)
+    n = nb_big[0] * nb_big[1] * nb_big[2] * big
+    if out is None:
+        out = np.zeros(n, dtype=np.uint8)
+    assert out.dtype == np.uint8 and out.size == n and out.flags.c_contiguous
     lib.orc_brick_level(ptr(np.ascontiguousarray(level)), U3(*dims), C.byref(v), U3(*nb_big), ptr(out))
     return out
 
@@ -223,6 +228,12 @@ class Cache:
         v = conv(View, view)
         lib.orc_render_f64(self.h, C.byref(v), ptr(tf), ptr(rgba), ptr(tbuf), ptr(state), ptr(usage), ptr(req),
                            threads)
+
+    def sample_normalized(self, level, x, y, z):
+        """(status, value) of one K_CacheManager::get_normalized sample."""
+        out = C.c_float(-1.0)
+        st = lib.orc_sample_normalized(self.h, level, x, y, z, C.byref(out))
+        return st, out.value
 
     def close(self):
         if self.h:

@@ -433,3 +433,68 @@ def test_edge_views_match_oracle(gc, orc, torch_cuda, case):
         assert s.cm.stats().rays_marched == 0
     if case == "inside":  # rays start inside the volume and advance through it
         assert (g[1].cpu().numpy() > 0).mean() > 0.5
+
+
+def test_c1_orbit_matches_oracle(gc, orc, torch_cuda):
+    """The c1 benchmark case at full size, as bench.py --config c1 runs it:
+    256^3 u8 (seed 1, 8 blobs, sigma 10-40, amplitude 60-200, noise 20), B16,
+    covering 1, 21^3 pool slots, 512^2 views on the 36-view orbit at 2.0x the
+    diagonal (fov 45 deg), ramp transfer function, early termination at 0.99,
+    8192 requests per cycle, every view rendered to convergence.  Every
+    frame's RGBA, t buffer and colour state equal the FP32 oracle's, and the
+    cache state (LRU, usage, requests, page directory, pool) equals the
+    oracle's after every update."""
+    import math
+
+    import bench
+
+    cfg = bench.CONFIGS["c1"]
+    size, W, H = cfg["size"], cfg["W"], cfg["H"]
+    vol = gc.volume_desc(size, cfg["B"], cfg["c"], 1, 1)
+    layout = gc.compute_layout(vol)
+    blobs = gc.generator_blobs(cfg["seed"], cfg["nblobs"], size, cfg["sigma"][0], cfg["sigma"][1], cfg["amp"][0],
+                               cfg["amp"][1])
+    d = torch_cuda.empty(size[0] * size[1] * size[2], dtype=torch_cuda.uint8, device="cuda")
+    gc.generate_volume(gc.make_generator(size, 1, cfg["seed"], blobs, cfg["noise"]), d.data_ptr())
+    store, offs, _ = gc.pre_process(vol, layout, d)
+    ob = orc.blobs(cfg["seed"], cfg["nblobs"], size, cfg["sigma"][0], cfg["sigma"][1], cfg["amp"][0], cfg["amp"][1])
+    ovol = orc.generate(size, 1, cfg["seed"], ob, cfg["nblobs"], cfg["noise"])
+    ref, roffs = scenario.orc_store(orc, gc, ovol.reshape(-1).view(np.uint8), vol, layout)
+    assert np.array_equal(store.numpy(), ref)
+    s = Scene.__new__(Scene)
+    s.gc, s.orc, s.torch, s.vol, s.layout = gc, orc, torch_cuda, vol, layout
+    s.cm = gc.CacheManager(vol, layout, cfg["pool_slots"], max_requests=8192, sync_loader=True)
+    s.cm.set_source_host(store, offs)
+    s.oc = orc.Cache(s.cm.desc)
+    s.oc.set_source(ref, roffs)
+    tf = bench.tf_table(cfg["tf"])
+    tf_dev = torch_cuda.from_numpy(tf.reshape(-1).copy()).cuda()
+    g, o = s.buffers(W, H)
+    focal = 1.0 / math.tan(math.radians(cfg["fov"]) / 2)
+    frames = 0
+    for view in range(cfg["frames"]):
+        m = bench.path_camera(gc.look_at, cfg, view)
+        for x in g:
+            x.zero_()
+        for x in o:
+            x[:] = 0
+        v = s.view(m, W, H, tf_dev, tf.shape[0], g, focal=focal, early_alpha=cfg["early"])
+        for it in range(64):
+            s.cm.render(v)
+            s.oc.render(v, tf, *o)
+            torch_cuda.cuda.synchronize()
+            tag = f"view {view} iteration {it}"
+            d = rgba_diff(g[0].cpu().numpy(), o[0])
+            assert d.max() <= RGBA_TOL_FP32, f"{tag}: RGBA off by {d.max()}"
+            assert np.array_equal(g[1].cpu().numpy(), o[1]), f"{tag}: t buffer"
+            assert np.array_equal(g[2].cpu().numpy(), o[2]), f"{tag}: colour state"
+            c1, c2 = s.cm.update(), s.oc.update()
+            assert c1 == c2, tag
+            s.compare_cache(tag)
+            frames += 1
+            if c1:
+                break
+        assert c1, f"view {view} did not converge"
+        assert (g[0].cpu().numpy() >> 24).astype(bool).mean() > 0.01  # the orbit sees the volume
+    assert frames >= cfg["frames"] and s.cm.stats().device_error == 0
+    s.cm.close()

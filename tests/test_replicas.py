@@ -32,7 +32,7 @@ def worker(rank, world, port, out):
         bench.rank_barrier()
         walls = bench.max_over_ranks([1.0 + rank, 10.0 - rank])
         cfg = bench.CONFIGS["c2"]
-        views = [tuple(round(v, 5) for v in bench.path_camera(gc, cfg, f, rank)) for f in range(3)]
+        views = [tuple(round(v, 5) for v in bench.path_camera(gc.look_at, cfg, f, rank)) for f in range(3)]
         out.put((rank, walls, views))
     finally:
         dist.destroy_process_group()
