@@ -201,16 +201,66 @@ struct BrickParams {
     uint32_t nbig[3];     // big bricks per axis
     uint32_t eb;
     uint64_t nsmall;      // small bricks in the level
+    uint32_t fast;        // 16-byte rows: B*eb and D[0]*eb multiples of 16, level and out 16-byte aligned
 };
 
+// One voxel of a small brick the slow way (bricks on the level's edge, odd
+// voxel widths): zero outside the level or in an unvisited brick.
+__device__ __forceinline__ void brick_voxel(const uint8_t *__restrict__ level, uint8_t *__restrict__ dptr,
+                                            const BrickParams &p, bool visited, int64_t gx, int64_t gy, int64_t gz) {
+    const bool inside = visited && gx >= 0 && gy >= 0 && gz >= 0 && gx < p.D[0] && gy < p.D[1] && gz < p.D[2];
+    const uint8_t *sptr = level + ((static_cast<uint64_t>(gz) * p.D[1] + gy) * p.D[0] + gx) * p.eb;
+    switch (p.eb) {
+        case 1:
+            *dptr = inside ? __ldg(sptr) : uint8_t(0);
+            break;
+        case 2:
+            *reinterpret_cast<uint16_t *>(dptr) = inside ? __ldg(reinterpret_cast<const uint16_t *>(sptr)) : uint16_t(0);
+            break;
+        case 4:
+            *reinterpret_cast<uint32_t *>(dptr) = inside ? __ldg(reinterpret_cast<const uint32_t *>(sptr)) : 0u;
+            break;
+        default:
+            for (uint32_t b = 0; b < p.eb; ++b) dptr[b] = inside ? sptr[b] : 0;
+    }
+}
+
+// 16 bytes of a source row starting at byte `s` (0..15) of the aligned pair (a, b).
+__device__ __forceinline__ uint4 row_bytes16(uint4 a, uint4 b, uint32_t s) {
+    const uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    const uint32_t r = (s & 3u) * 8u;
+    uint32_t o[4];
+    // s / 4 is the same for every thread of a brick: a uniform branch with
+    // constant register indices in each arm
+    switch (s >> 2) {
+#define GC_ROW_CASE(Q)                                                                  \
+    case Q:                                                                             \
+        _Pragma("unroll") for (int k = 0; k < 4; ++k) o[k] = __funnelshift_r(w[Q + k], w[Q + k + 1], r); \
+        break;
+        GC_ROW_CASE(0)
+        GC_ROW_CASE(1)
+        GC_ROW_CASE(2)
+        GC_ROW_CASE(3)
+#undef GC_ROW_CASE
+    }
+    return make_uint4(o[0], o[1], o[2], o[3]);
+}
+
+// One CTA per small brick (grid-stride).  A brick whose B^3 source voxels all
+// lie inside the level (the great majority) is copied row by row in 16-byte
+// chunks: every row of the brick starts at the same byte offset s modulo 16
+// of the level (rows are D[0]*eb bytes apart, a multiple of 16), so each
+// chunk is two aligned 16-byte loads and a funnel shift by s, stored with one
+// 16-byte store.  Bricks on the level's edge, unvisited ones and odd voxel
+// widths take the per-voxel path.
 __global__ void __launch_bounds__(256) brick_kernel(const uint8_t *__restrict__ level,
                                                     uint8_t *__restrict__ out, BrickParams p) {
     const uint32_t B = p.B;
     const uint32_t bvx = p.BB[0] * B, bvy = p.BB[1] * B;
     const uint64_t big_bytes = static_cast<uint64_t>(bvx) * bvy * (p.BB[2] * B) * p.eb;
+    const uint32_t nsx = p.nbig[0] * p.BB[0], nsy = p.nbig[1] * p.BB[1];
     for (uint64_t sb = blockIdx.x; sb < p.nsmall; sb += gridDim.x) {
         // small brick grid = nbig * BB per axis, x fastest
-        const uint32_t nsx = p.nbig[0] * p.BB[0], nsy = p.nbig[1] * p.BB[1];
         const uint32_t sx = static_cast<uint32_t>(sb % nsx);
         const uint32_t sy = static_cast<uint32_t>((sb / nsx) % nsy);
         const uint32_t sz = static_cast<uint32_t>(sb / (static_cast<uint64_t>(nsx) * nsy));
@@ -226,36 +276,33 @@ __global__ void __launch_bounds__(256) brick_kernel(const uint8_t *__restrict__ 
         // where their covering border reaches into the volume.
         const bool visited = static_cast<uint64_t>(sx) * p.Beff < p.D[0] &&
                              static_cast<uint64_t>(sy) * p.Beff < p.D[1] && static_cast<uint64_t>(sz) * p.Beff < p.D[2];
+        const bool interior = visited && ox >= 0 && oy >= 0 && oz >= 0 && ox + B <= p.D[0] && oy + B <= p.D[1] &&
+                              oz + B <= p.D[2];
+        if (p.fast && interior) {
+            const uint32_t cpr = B * p.eb / 16u;  // 16-byte chunks per row
+            const uint32_t nchunks = B * B * cpr;
+            const uint64_t row_stride = static_cast<uint64_t>(p.D[0]) * p.eb;
+            const uint64_t src0 = ((static_cast<uint64_t>(oz) * p.D[1] + oy) * p.D[0] + ox) * p.eb;
+            const uint32_t s = static_cast<uint32_t>(src0 & 15u);
+            const uint64_t slice = row_stride * p.D[1];
+            uint8_t *obase = bbase + (static_cast<uint64_t>(ix) * B) * p.eb;
+            for (uint32_t c = threadIdx.x; c < nchunks; c += blockDim.x) {
+                const uint32_t cx = c % cpr, row = c / cpr;
+                const uint32_t ly = row % B, lz = row / B;
+                const uint64_t src = src0 - s + lz * slice + ly * row_stride + cx * 16u;
+                const uint4 a = __ldg(reinterpret_cast<const uint4 *>(level + src));
+                const uint4 v = s ? row_bytes16(a, __ldg(reinterpret_cast<const uint4 *>(level + src + 16)), s) : a;
+                uint8_t *dst = obase + ((static_cast<uint64_t>(iz * B + lz) * bvy + (iy * B + ly)) * bvx) * p.eb +
+                               cx * 16u;
+                *reinterpret_cast<uint4 *>(dst) = v;
+            }
+            continue;
+        }
         const uint32_t nvox = B * B * B;
         for (uint32_t v = threadIdx.x; v < nvox; v += blockDim.x) {
             const uint32_t lx = v % B, ly = (v / B) % B, lz = v / (B * B);
-            const int64_t gx_ = ox + lx, gy_ = oy + ly, gz_ = oz + lz;
             uint8_t *dptr = bbase + ((static_cast<uint64_t>(iz * B + lz) * bvy + (iy * B + ly)) * bvx + (ix * B + lx)) * p.eb;
-            const bool inside = visited && gx_ >= 0 && gy_ >= 0 && gz_ >= 0 && gx_ < p.D[0] && gy_ < p.D[1] &&
-                                gz_ < p.D[2];
-            const uint8_t *sptr = level + ((static_cast<uint64_t>(gz_) * p.D[1] + gy_) * p.D[0] + gx_) * p.eb;
-            switch (p.eb) {
-                case 1: {
-                    uint8_t v = 0;
-                    if (inside) v = __ldg(sptr);
-                    *dptr = v;
-                    break;
-                }
-                case 2: {
-                    uint16_t v = 0;
-                    if (inside) v = __ldg(reinterpret_cast<const uint16_t *>(sptr));
-                    *reinterpret_cast<uint16_t *>(dptr) = v;
-                    break;
-                }
-                case 4: {
-                    uint32_t v = 0;
-                    if (inside) v = __ldg(reinterpret_cast<const uint32_t *>(sptr));
-                    *reinterpret_cast<uint32_t *>(dptr) = v;
-                    break;
-                }
-                default:
-                    for (uint32_t b = 0; b < p.eb; ++b) dptr[b] = inside ? sptr[b] : 0;
-            }
+            brick_voxel(level, dptr, p, visited, ox + lx, oy + ly, oz + lz);
         }
     }
 }
@@ -338,6 +385,12 @@ int gc_bricks_build(const void *level, const uint32_t level_dims[3], const gc_vo
         p.Beff = p.B - 2 * p.c;
         p.eb = vol->encoded_bytes;
         p.nsmall = static_cast<uint64_t>(p.nbig[0] * p.BB[0]) * (p.nbig[1] * p.BB[1]) * (p.nbig[2] * p.BB[2]);
+        // 16-byte row chunks: whole chunks per brick row, rows 16 bytes apart
+        // in the level (so every row of a brick has the same alignment), and
+        // both buffers 16-byte aligned
+        p.fast = (p.eb == 1 || p.eb == 2 || p.eb == 4) && (p.B * p.eb) % 16 == 0 &&
+                 (static_cast<uint64_t>(p.D[0]) * p.eb) % 16 == 0 &&
+                 reinterpret_cast<uintptr_t>(level) % 16 == 0 && reinterpret_cast<uintptr_t>(out) % 16 == 0;
         const uint64_t grid = std::min<uint64_t>(p.nsmall, static_cast<uint64_t>(sm_count()) * 16);
         brick_kernel<<<static_cast<unsigned>(grid), 256, 0, as_stream(stream)>>>(
             static_cast<const uint8_t *>(level), static_cast<uint8_t *>(out), p);

@@ -66,6 +66,11 @@ BRICK_CASES = [
     ((70, 50, 40), 2, 1, 32, 1, (1, 1, 1)),
     ((48, 40, 36), 1, 2, 16, 2, (2, 2, 2)),
     ((50, 30, 45), 1, 1, 8, 1, (2, 1, 3)),
+    # 16-byte row path of the bricker at every start offset: covering 2 with
+    # B32 u16, covering 0, and 4-byte voxels (two u16 channels) in big bricks
+    ((96, 80, 64), 2, 1, 32, 2, (1, 1, 1)),
+    ((64, 64, 32), 1, 1, 16, 0, (1, 1, 1)),
+    ((64, 48, 40), 2, 2, 16, 1, (1, 2, 1)),
 ]
 
 
