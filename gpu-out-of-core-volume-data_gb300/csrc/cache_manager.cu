@@ -1133,6 +1133,41 @@ int gc_cache_volume_levels(gc_cache_t C, uint32_t volume, uint32_t *level_base, 
     });
 }
 
+int gc_cache_device_view_get(gc_cache_t C, uint32_t volume, gc_cache_device_view *out) {
+    return guard([&] {
+        GC_REQUIRE(C && out, "null argument");
+        GC_REQUIRE(volume < C->vols.size(), "no such volume in this cache");
+        const gc::Volume &v = C->vols[volume];
+        GC_REQUIRE(v.desc.channels == 1, "the device view samples one-channel volumes");
+        std::memset(out, 0, sizeof(*out));
+        out->mrpd = reinterpret_cast<const uint32_t *>(C->mrpd);
+        out->requests = C->req;
+        out->usage = C->usage;
+        out->pool = C->pool;
+        out->slot_bytes = C->slot_bytes;
+        out->mrpd_dims[0] = C->mx;
+        out->mrpd_dims[1] = C->my;
+        out->mrpd_dims[2] = C->mz;
+        out->pool_slots[0] = C->d.cache_size[0];
+        out->pool_slots[1] = C->d.cache_size[1];
+        out->pool_slots[2] = C->d.cache_size[2];
+        out->brick_size = C->B;
+        out->covering = C->c;
+        out->voxel_bytes = v.desc.encoded_bytes;
+        out->timestamp = C->ts;
+        out->n_levels = v.layout.nb_levels;
+        for (uint32_t l = 0; l < v.layout.nb_levels; ++l) {
+            const uint32_t cl = v.level_base + l;
+            out->level_offset[l] = C->lt.off[cl];
+            for (int a = 0; a < 3; ++a) {
+                out->level_bricks[l][a] = C->lt.nb[cl][a];
+                out->level_voxels[l][a] = C->lt.vvox[cl][a];
+                out->level_initial_over_real[l][a] = C->lt.ior[cl][a];
+            }
+        }
+    });
+}
+
 int gc_cache_timestamp(gc_cache_t C, uint32_t *ts) {
     return guard([&] {
         GC_REQUIRE(C && ts, "null argument");
@@ -1398,6 +1433,7 @@ struct gc_batch {
     uint64_t next_serial = 1;
     std::unordered_set<uint64_t> completed;  // loads installed (or empty)
     uint32_t used_prev = 0;                   // slots used by the previous render (the other cohort)
+    bool split_back = false;                  // the next cohort split renders the back half first
     cudaStream_t stream = nullptr;            // stream of the last overlapped tick
 };
 
@@ -1568,9 +1604,11 @@ static void batch_tick_overlapped(gc_batch *b, gc_cache *C, cudaStream_t s, uint
         for (uint32_t i = 0; i < na; ++i)
             if (b->active[i].wait == 0 || b->completed.count(b->active[i].wait)) sel.push_back(i);
     // With no load in flight or waiting, the ready views are split into two
-    // cohorts of about equal pixels: the first renders now and its bricks
-    // load while the second renders in the next tick, and from then on each
-    // cohort renders while the other's bricks load.
+    // cohorts of about equal pixels: one renders now and its bricks load
+    // while the other renders in the next tick, and from then on each cohort
+    // renders while the other's bricks load.  The half that goes first
+    // alternates between splits, so that a front half whose pass started no
+    // load cannot hold the back half back split after split.
     if (sel.size() >= 2 && b->slot_state[0] == 0 && b->slot_state[1] == 0) {
         uint64_t total = 0, half = 0;
         for (uint32_t i : sel) total += static_cast<uint64_t>(b->active[i].view.width) * b->active[i].view.height;
@@ -1579,7 +1617,12 @@ static void batch_tick_overlapped(gc_batch *b, gc_cache *C, cudaStream_t s, uint
             half += static_cast<uint64_t>(b->active[sel[k]].view.width) * b->active[sel[k]].view.height;
             ++k;
         }
-        sel.resize(std::max<size_t>(k, 1));
+        k = std::max<size_t>(k, 1);
+        if (b->split_back)
+            sel.erase(sel.begin(), sel.begin() + static_cast<std::ptrdiff_t>(k));
+        else
+            sel.resize(k);
+        b->split_back = !b->split_back;
     }
     if (sel.empty()) {
         if (na) {

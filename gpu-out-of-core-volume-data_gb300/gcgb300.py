@@ -84,6 +84,15 @@ class View(C.Structure):
                 ("fallback", C.c_uint32)]
 
 
+class CacheDeviceView(C.Structure):
+    _fields_ = [("mrpd", C.c_void_p), ("requests", C.c_void_p), ("usage", C.c_void_p), ("pool", C.c_void_p),
+                ("slot_bytes", C.c_uint64), ("mrpd_dims", C.c_uint32 * 3), ("pool_slots", C.c_uint32 * 3),
+                ("brick_size", C.c_uint32), ("covering", C.c_uint32), ("voxel_bytes", C.c_uint32),
+                ("timestamp", C.c_uint32), ("n_levels", C.c_uint32), ("level_offset", C.c_uint32 * MAX_LEVELS),
+                ("level_bricks", (C.c_uint32 * 3) * MAX_LEVELS), ("level_voxels", (C.c_uint32 * 3) * MAX_LEVELS),
+                ("level_initial_over_real", (C.c_float * 3) * MAX_LEVELS)]
+
+
 class BatchDesc(C.Structure):
     _fields_ = [("max_views", C.c_uint32), ("max_pixels", C.c_uint64), ("max_passes", C.c_uint32),
                 ("max_occupancy", C.c_float), ("max_admit", C.c_uint32), ("park_above", C.c_float),
@@ -143,6 +152,7 @@ _SIGS = {
     "gc_bricks_xml_read": [C.c_char_p, P(C.c_uint32), P(C.c_uint32 * 3), P(C.c_uint32 * 3), P(C.c_uint64),
                            C.c_size_t, P(C.c_size_t)],
     "gc_cache_volume_levels": [vp, C.c_uint32, P(C.c_uint32), P(C.c_uint32)],
+    "gc_cache_device_view_get": [vp, C.c_uint32, P(CacheDeviceView)],
     "gc_cache_update": [vp, vp, P(C.c_int)], "gc_cache_completude": [vp, vp, P(C.c_float)],
     "gc_cache_timestamp": [vp, P(C.c_uint32)], "gc_cache_info_get": [vp, P(CacheInfo)],
     "gc_cache_stats_get": [vp, P(CacheStats)], "gc_cache_dump": [vp, C.c_int, vp, C.c_size_t],
@@ -377,6 +387,8 @@ def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host
     for l in range(layout.nb_levels):
         process_bricking(pyr.data_ptr() + offs[l], layout.initial[l], vol, layout.nb_big_bricks[l],
                          bricks.data_ptr() + soffs[l], stream)
+    torch.cuda.synchronize(dev)
+    t_bricks = time.perf_counter()
     empty_keys = []
     if empty_threshold is not None:
         for l in range(layout.nb_levels):
@@ -401,7 +413,9 @@ def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host
     torch.cuda.synchronize(dev)
     t2 = time.perf_counter()
     if timings is not None:
-        timings.update(mip_s=t1 - t0, brick_s=t2 - t1, level0_bytes=n0, pyramid_bytes=total, store_bytes=stotal)
+        timings.update(mip_s=t1 - t0, brick_s=t_bricks - t1, flags_bins_s=t2 - t_bricks, level0_bytes=n0,
+                       pyramid_bytes=sum(layout.mip[l][0] * layout.mip[l][1] * layout.mip[l][2] * eb
+                                         for l in range(layout.nb_levels)), store_bytes=stotal)
     del pyr
     if store == "device":
         return bricks, soffs, empty_keys
@@ -610,6 +624,14 @@ class CacheManager:
         n, tot = C.c_uint32(), C.c_uint32()
         check(lib.gc_cache_last_misses(self._h, out.ctypes.data_as(P(C.c_uint32)), m, C.byref(n), C.byref(tot)))
         return tot.value, out[: n.value]
+
+    def device_view(self, volume=0):
+        """The device-side handle (gc_cache_device_view) of one volume, for a
+        user kernel sampling with gc_sample_normalized; valid until the next
+        update."""
+        v = CacheDeviceView()
+        check(lib.gc_cache_device_view_get(self._h, volume, C.byref(v)))
+        return v
 
     def load_buffer(self, what, buf):
         check(lib.gc_cache_load_buffer(self._h, what, vp(buf.ctypes.data), buf.nbytes))

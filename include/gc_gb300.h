@@ -367,6 +367,37 @@ int gc_miss_list_noalloc(const uint32_t *requests, uint64_t n_entries, uint32_t 
 int gc_cache_load_buffer(gc_cache_t cache, int what, const void *src, size_t bytes);
 
 /* ------------------------------------------------------------------------ */
+/* Device-side handle of the cache for a host application's own kernels:
+ * K_CacheManager<T> and its get_normalized (K_CacheManager.hpp:61-71,
+ * 265-361), the object CacheManager::to_kernel_object() returns
+ * (CacheManager.hpp:292-309).  gc_cache_device_view_get fills this plain
+ * struct -- device pointers and the level tables of one volume of the cache --
+ * to be passed BY VALUE to a kernel, which samples with
+ * gc_sample_normalized() of include/gc_cache_device.cuh.  Like the
+ * reference's kernel object it is valid until the next gc_cache_update of the
+ * cache (the timestamp changes every update; installs change the page
+ * directory and pool).  One-channel volumes (the reference's sampler). */
+typedef struct gc_cache_device_view {
+    const uint32_t *mrpd;        /* page directory: 4 words per entry (cacheX, cacheY, cacheZ, flag) */
+    uint32_t *requests;          /* request word per page-directory entry                           */
+    uint32_t *usage;             /* last-use word per pool slot                                     */
+    const uint8_t *pool;         /* pool slots of B^3 voxels, x fastest, slot_bytes apart            */
+    uint64_t slot_bytes;
+    uint32_t mrpd_dims[3];       /* entries per axis, levels packed along x                          */
+    uint32_t pool_slots[3];      /* slots per axis (slot = x + y*sx + z*sx*sy)                       */
+    uint32_t brick_size;         /* B                                                                */
+    uint32_t covering;           /* c                                                                */
+    uint32_t voxel_bytes;        /* 1 (u8), 2 (u16) or 4 (f32)                                       */
+    uint32_t timestamp;          /* the frame's timestamp: written into usage and requests           */
+    uint32_t n_levels;           /* levels of the volume                                             */
+    uint32_t level_offset[GC_MAX_LEVELS];          /* page-directory x offset of each level            */
+    uint32_t level_bricks[GC_MAX_LEVELS][3];       /* bricks per axis                                   */
+    uint32_t level_voxels[GC_MAX_LEVELS][3];       /* virtualized voxels per axis (bricks x (B - 2c))  */
+    float level_initial_over_real[GC_MAX_LEVELS][3]; /* initial / real level size                     */
+} gc_cache_device_view;
+int gc_cache_device_view_get(gc_cache_t cache, uint32_t volume, gc_cache_device_view *out);
+
+/* ------------------------------------------------------------------------ */
 /* Ray caster: RayCastDVR / RayCastMOP (RayCasters.cu:35-468) with the LOD
  * tables of display_volume_raycaster (VolumeRayCaster.cu:141-175) and the
  * camera of update_CUDA_inv_view_model_matrix (RayCasters.cu:587-590). */
