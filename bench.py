@@ -498,6 +498,7 @@ def run_ours(args):
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
     cfg = CONFIGS[args.config]
+    gc.render_precision(gc.RENDER_FAST if args.precision == "fast" else gc.RENDER_EXACT)
     vol, layout, store, offs, prep_s = make_store(gc, torch, cfg)
     W, H = cfg["W"], cfg["H"]
     spec = lambda f: [(path_camera(gc.look_at, cfg, f, rank), W, H)]  # noqa: E731
@@ -600,6 +601,19 @@ def run_ours(args):
     torch.cuda.synchronize()
     gc.render_empty_skip(True)
     render_ms_noskip = statistics.median([a.elapsed_time(b) for a, b in ev_off])
+    # the roofline view's image from each ray-caster build (from scratch, same
+    # cache state) for the parity check against the oracle
+    images = {}
+    for name, prec in (("exact", gc.RENDER_EXACT), ("fast", gc.RENDER_FAST)):
+        gc.render_precision(prec)
+        views, bufs = S.views(last)
+        with torch.cuda.stream(S.stream):
+            bufs[0][1].zero_()
+            bufs[0][2].zero_()
+            S.cm.render(views[0], S.sp)
+        torch.cuda.synchronize()
+        images[name] = bufs[0][0].cpu().numpy().view(np.uint32).copy()
+    gc.render_precision(gc.RENDER_FAST if args.precision == "fast" else gc.RENDER_EXACT)
     algo = touched * cfg["B"] ** 3 * vol.encoded_bytes + W * H * PIXEL_BYTES
     peak, peak_kind = measured_peak()
     achieved = algo / (render_ms / 1e3) / 1e9
@@ -612,6 +626,7 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dt, "data": data_txt,
         "config": bench_config(args.config, cfg, args),
         "setup": {"pool_gib": round(pool_bytes / 2**30, 3), "brick_bins": bool(args.brick_bins), "loader": "sync",
+                  "ray_caster_build": args.precision,
                   "upload": "gather kernel reading the host store" if S.cm.stats().upload_direct
                   else "staged host copies + cudaMemcpyAsync",
                   "stores": "pinned" if PIN_STORES else "pageable", "preprocess_s": round(prep_s, 2)},
@@ -619,10 +634,18 @@ def run_ours(args):
                        "mip_build_gbs": round((2 * LAST_PREPROCESS.get("pyramid_bytes", 0) - LAST_PREPROCESS.get(
                            "level0_bytes", 0)) / max(LAST_PREPROCESS.get("mip_s", 1e-9), 1e-9) / 1e9, 1),
                        "bricking_s": round(LAST_PREPROCESS.get("brick_s", 0.0), 4),
+                       "bricking_gbs": round((LAST_PREPROCESS.get("pyramid_bytes", 0) + LAST_PREPROCESS.get(
+                           "store_bytes", 0)) / max(LAST_PREPROCESS.get("brick_s", 1e-9), 1e-9) / 1e9, 1),
+                       "bricking_frac": round((LAST_PREPROCESS.get("pyramid_bytes", 0) + LAST_PREPROCESS.get(
+                           "store_bytes", 0)) / max(LAST_PREPROCESS.get("brick_s", 1e-9), 1e-9) / 1e9
+                           / measured_peak()[0], 3),
+                       "value_bins_s": round(LAST_PREPROCESS.get("flags_bins_s", 0.0), 4),
                        "store_copy_s": round(LAST_PREPROCESS.get("copy_s", 0.0), 4),
                        "note": "device mip pyramid (every level read once, every coarser level written: "
-                               "2 x pyramid - level 0 bytes, over the mip time), device bricking, copy of the "
-                               "brick store to host memory"},
+                               "2 x pyramid - level 0 bytes, over the mip time); device bricking (every level "
+                               "read once + the brick store written, over the bricking time; fraction of the "
+                               "measured HBM peak); value bins of every brick; copy of the brick store to host "
+                               "memory"},
         "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
         "iterations_per_view": {"mean": round(statistics.mean(iters), 2), "max": max(iters)},
         "converged_views": f"{conv}/{args.steps}",
@@ -650,12 +673,19 @@ def run_ours(args):
     if with_bins:
         out["with_brick_bins"] = with_bins
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(gc, S, cfg, last, args)
+        out["cpu_baseline"] = cpu_baseline(gc, S, cfg, last, args, images)
         out["parity_max_abs"] = out["cpu_baseline"]["parity"]["max_abs_rgba"]
     S.close()
     del store
+    if rank == 0 and not args.no_reference_gpu:
+        try:
+            out["reference_gpu_build"] = reference_gpu_baseline(gc, torch, args)
+        except Exception as e:  # a reported baseline: its failure does not void the line
+            out["reference_gpu_build"] = {"unavailable": f"{type(e).__name__}: {e}"[:300]}
     if rank == 0 and not args.no_batched:
         out["batched"] = run_batched(gc, torch, args)
+    if rank == 0 and not args.no_serving:
+        out["serving"] = run_serving_sweep(gc, torch, args)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -922,6 +952,49 @@ def c4_serve(gc, torch, cfg, vols, stores, args):
     return out
 
 
+SERVING_RATES = (25.0, 50.0, 100.0, 200.0)  # requests per second tried by the default run
+SERVING_SECONDS = 2.0
+SERVING_P99_MS = 1000.0  # a rate is sustained while the p99 latency stays below this
+
+
+def run_serving_sweep(gc, torch, args):
+    """The serving form (c4) in the default run: the three volumes in one
+    shared pool, Poisson arrivals at each rate of SERVING_RATES for
+    SERVING_SECONDS, each on a fresh cache; per rate the served Mrays/s
+    (rays of all requests over the time to the last retirement), p50/p99
+    latency (arrival -> retirement) and upload GB/s, and the highest rate the
+    server sustains: every request converged with a p99 latency under
+    SERVING_P99_MS (no queue building up)."""
+    global PIN_STORES
+    pinned = PIN_STORES
+    PIN_STORES = False
+    cfg = CONFIGS["c4"]
+    vols, stores, prep = c4_stores(gc, torch, cfg)
+    PIN_STORES = pinned
+    rates, sustained = [], None
+    for rate in SERVING_RATES:
+        a = argparse.Namespace(**vars(args))
+        a.rate, a.duration = rate, SERVING_SECONDS
+        r = c4_serve(gc, torch, cfg, vols, stores, a)
+        offered = r["config"]["offered_mrays_per_s"]
+        done, total = (int(x) for x in r["converged"].split("/"))
+        ok = done == total and r["latency_ms"]["p99"] is not None and r["latency_ms"]["p99"] <= SERVING_P99_MS
+        rates.append({"rate_per_s": rate, "requests": r["steps"], "offered_mrays_per_s": offered,
+                      "served_mrays_per_s": r["value"], "latency_ms": r["latency_ms"], "converged": r["converged"],
+                      "passes_per_request": r["passes_per_request"], "upload_gbs": r["cache"]["upload_gbs"],
+                      "sustained": ok})
+        if ok:
+            sustained = rate
+    del stores
+    return {"workload": f"c4: 1024^3 u8 + 2048^3 u16 + 4096x4096x2048 u8 (seeds 11-13) in one shared 24 GiB pool; "
+                        f"Poisson requests over {SERVING_SECONDS} s per rate, random volume, camera (0.5-3.0x the "
+                        f"diagonal), size {list(cfg['sizes'])} and one of 4 transfer functions; continuous batching",
+            "rates": rates, "sustained_rate_per_s": sustained, "sustained_means": f"all requests converged, p99 <= "
+                                                                                     f"{SERVING_P99_MS:.0f} ms",
+            "sustained_p99_ms": next((x["latency_ms"]["p99"] for x in rates if x["rate_per_s"] == sustained), None),
+            "preprocess_s": round(prep, 1), "stores": "pageable host memory (85 GiB)"}
+
+
 def c3_tunings(gc, torch, cfg, data, warm, args):
     """Launch tunings of the two c3 arms, each for its own launch shape, on
     the warm-up views in a cache of their own: the batched arm on one launch
@@ -972,13 +1045,106 @@ def run_batched(gc, torch, args):
     return out
 
 
+def reference_gpu_baseline(gc, torch, args, views=12):
+    """The reference's own CUDA build (oracle/_ref/librefgpu.so: its
+    Mipmapper, CacheManager<uchar1> and RayCastDVR compiled for sm_103a) timed
+    on this GPU beside our plain path on the same c1 views, each rendered to
+    convergence.  Both run the reference's fixed parameters -- 128-entry
+    transfer function, early termination at alpha 0.95, focal length 2, 50
+    brick requests per cycle -- so both caches go through the same frame
+    sequence (their states are equal frame by frame, tests/test_gpu_reference.py)
+    and the times compare the two implementations of the same work."""
+    from oracle import refgpu
+
+    if not refgpu.available():
+        return {"unavailable": "no staged copy of the reference sources (oracle/_ref/src)"}
+    cfg = dict(CONFIGS["c1"])
+    size, W, H = cfg["size"], cfg["W"], cfg["H"]
+    vol = gc.volume_desc(size, cfg["B"], cfg["c"], 1, 1)
+    layout = gc.compute_layout(vol)
+    blobs = gc.generator_blobs(cfg["seed"], cfg["nblobs"], size, cfg["sigma"][0], cfg["sigma"][1], cfg["amp"][0],
+                               cfg["amp"][1])
+    dev = torch.empty(size[0] * size[1] * size[2], dtype=torch.uint8, device="cuda")
+    gc.generate_volume(gc.make_generator(size, 1, cfg["seed"], blobs, cfg["noise"]), dev.data_ptr())
+    torch.cuda.synchronize()
+    tmp = tempfile.mkdtemp(prefix="refgpu_")
+    ref = refgpu.RefGpu(tmp, size, cfg["B"], cfg["c"], 1)
+    t0 = time.perf_counter()
+    ref.preprocess(dev.cpu().numpy())
+    ref_pre = time.perf_counter() - t0
+    store, offs, _ = gc.pre_process(vol, layout, dev)
+    pool = pool_slots(cfg)
+    ref.open(pool)
+    tf = tf_table(cfg["tf"])
+    tf128 = np.ascontiguousarray(tf[np.round(np.linspace(0, tf.shape[0] - 1, 128)).astype(int)])
+    tf_dev = torch.from_numpy(tf128.reshape(-1).copy()).cuda()
+    bufs = [torch.zeros((W * H + W + 16) * k, dtype=dt, device="cuda")
+            for dt, k in ((torch.int32, 1), (torch.float32, 1), (torch.float32, 4))]
+    cams = [path_camera(gc.look_at, cfg, f) for f in range(views)]
+
+    def run_ref():
+        frames = 0
+        for m in cams:
+            for b in bufs[1:]:
+                b.zero_()
+            for _ in range(2000):
+                ref.render(m, W, H, 2.0 / 256.0, tf128, 0, *[b.data_ptr() for b in bufs])
+                frames += 1
+                if ref.update():
+                    break
+        return frames
+
+    def run_ours(max_requests):
+        cm = gc.CacheManager(vol, layout, pool, max_requests=max_requests, sync_loader=True)
+        cm.set_source_host(store, offs)
+        frames = 0
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        for m in cams:
+            for b in bufs[1:]:
+                b.zero_()
+            v = gc.make_view(m, W, H, tf_dev.data_ptr(), 128, *[b.data_ptr() for b in bufs])  # early 0.95, focal 2
+            for _ in range(2000):
+                cm.render(v)
+                frames += 1
+                if cm.update():
+                    break
+        torch.cuda.synchronize()
+        el = time.perf_counter() - a
+        cm.close()
+        return frames, el
+
+    a = time.perf_counter()
+    ref_frames = run_ref()
+    ref_s = time.perf_counter() - a
+    ref.close()
+    ours_frames, ours_s = run_ours(50)
+    ours8k_frames, ours8k_s = run_ours(args.max_requests)
+    rays = W * H * views
+    return {"workload": f"c1 volume and orbit (first {views} views, {W}x{H}), each view to convergence, with the "
+                        f"reference's fixed parameters: 128-entry transfer function, early termination 0.95, focal "
+                        f"length 2, 50 requests per cycle; fresh caches of {list(pool)} slots",
+            "reference_gpu": {"value": round(rays / ref_s / 1e6, 3), "unit": "Mrays/s", "frames": ref_frames,
+                              "ms_per_frame": round(1e3 * ref_s / ref_frames, 3),
+                              "preprocess_s": round(ref_pre, 2),
+                              "what": "the reference's CacheManager<uchar1> + RayCastDVR built for sm_103a, its "
+                                      "request handler loading its own LZ4 brick files"},
+            "ours_same_requests": {"value": round(rays / ours_s / 1e6, 3), "unit": "Mrays/s", "frames": ours_frames,
+                                   "ms_per_frame": round(1e3 * ours_s / ours_frames, 3)},
+            "ours_max_requests": {"value": round(rays / ours8k_s / 1e6, 3), "unit": "Mrays/s",
+                                  "frames": ours8k_frames, "max_requests": args.max_requests},
+            "ratio_same_requests": round(ref_s / ours_s, 2)}
+
+
 def vol_bytes_per_voxel(cfg):
     return cfg["bpc"] * cfg.get("channels", 1)
 
 
-def cpu_baseline(gc, S, cfg, spec, args):
+def cpu_baseline(gc, S, cfg, spec, args, images):
     """The oracle's FP32 ray-march (all host threads) on a bounded sample of
-    converged c2 views, reading a snapshot of the GPU's cache state."""
+    converged c2 views, reading a snapshot of the GPU's cache state; its image
+    is compared with the GPU's images of the same view (images: build name ->
+    RGBA8 array)."""
     from oracle import oracle as orc
 
     (m, W, H), = spec
@@ -1002,12 +1168,15 @@ def cpu_baseline(gc, S, cfg, spec, args):
         if el > args.cpu_seconds:
             break
     oc.close()
-    # parity: the GPU's last render of this view (from scratch, same cache
-    # state) against the oracle's render of it
-    gpu_img = S.buffers(0, W, H)[0].cpu().numpy().view(np.uint8).astype(np.int32)
-    dif = np.abs(gpu_img - rgba.view(np.uint8).astype(np.int32)).reshape(-1, 4).max(axis=1)
-    parity = {"max_abs_rgba": int(dif.max()), "pixels": int(W * H), "pixels_differing": int(np.count_nonzero(dif)),
-              "vs": "the FP32 oracle's render of the same view from the GPU's cache state (units of 1/255)"}
+    # parity: the GPU's renders of this view (from scratch, same cache state)
+    # against the oracle's render of it
+    parity = {"vs": "the FP32 oracle's render of the same view from the GPU's cache state (units of 1/255)",
+              "pixels": int(W * H)}
+    for name, img in images.items():
+        dif = np.abs(img.view(np.uint8).astype(np.int32) - rgba.view(np.uint8).astype(np.int32)).reshape(-1, 4).max(1)
+        parity[name] = {"max_abs_rgba": int(dif.max()), "pixels_differing": int(np.count_nonzero(dif)),
+                        "pixels_beyond_1": int(np.count_nonzero(dif > 1))}
+    parity["max_abs_rgba"] = parity["exact"]["max_abs_rgba"]
     # the CPU restatement of the mip reduction (down_sampling_inner) on a bounded
     # 512 x 512 x 64 sample of the same voxel type, single thread
     nc = cfg.get("channels", 1)
@@ -1187,6 +1356,14 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--precision", choices=["exact", "fast"], default="fast",
+                    help="ray-caster build: exact (the FP32 oracle's operations, bit for bit) or fast (FMA "
+                         "contraction, rsqrtf, hardware log2/exp2; validated against the FP64 oracle and the "
+                         "reference's ray caster)")
+    ap.add_argument("--no-serving", action="store_true",
+                    help="skip the serving (c4) rate sweep of the default run")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip the reference's own CUDA build timed beside our plain path (c1 views)")
     ap.add_argument("--no-plain", action="store_true", help="c3: skip the plain loop over the same views")
     args = ap.parse_args()
     if args.steps is None:
@@ -1198,6 +1375,7 @@ def main():
     PIN_STORES = args.pin_stores
     if args.config != "c2":
         args.no_batched = True
+        args.no_serving = True
     if args.impl == "reference" and args.config in ("c3", "c4"):
         print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm covers the plain configs "
                                                               "(c1, c2); c3 is the batched form"}), flush=True)

@@ -188,8 +188,18 @@ struct RenderTuning {
     uint32_t blocks_per_sm = 0;
     uint32_t skip_empty = 1;  // empty-space skipping on (results are the same either way)
     uint32_t tile_w = 8;  // ray tile of one warp: tile_w x (32 / tile_w) pixels
+    uint32_t precision = 0;  // 0: exact build (the oracle's operations); 1: fast build
 };
 RenderTuning &render_tuning();
+// Ray-caster kernels of a voxel kind (1, 2, 4 bytes; 0 mixed widths; 0x202
+// two 8-bit channels) and scheduler, from the exact build (render.cu) or the
+// fast build (render_fast.cu); nullptr for an unsupported kind.
+namespace exact {
+void *march_kernel(uint32_t kind, bool pixels);
+}
+namespace fast {
+void *march_kernel(uint32_t kind, bool pixels);
+}
 // Fills ViewParams::visible of n device views from their transfer functions.
 void launch_view_bins(ViewParams *views_dev, uint32_t n, cudaStream_t s);
 void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams *views_dev,

@@ -32,7 +32,23 @@
 #include "cache.cuh"
 #include "gc_internal.h"
 
+// The march below is compiled twice: here (namespace gc::exact, built with
+// -fmad=false: the oracle's operation sequence) and by render_fast.cu with
+// GC_RENDER_FAST defined (namespace gc::fast, built with FMA contraction, see
+// the math helpers).  The host code at the end of this file is compiled once
+// and launches either set (gc_render_precision_set).
+#ifdef GC_RENDER_FAST
+#define GC_MARCH_NS fast
+#else
+#define GC_MARCH_NS exact
+#endif
+// resident 256-thread blocks per SM the register allocation must allow
+#ifndef GC_RENDER_MIN_BLOCKS
+#define GC_RENDER_MIN_BLOCKS 1
+#endif
+
 namespace gc {
+namespace GC_MARCH_NS {
 
 
 struct V3 {
@@ -46,8 +62,12 @@ __device__ __forceinline__ V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y *
 __device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ float length(V3 a) { return sqrtf(dot(a, a)); }
 __device__ __forceinline__ V3 normalize(V3 a) {
+#ifdef GC_RENDER_FAST
+    return a * rsqrtf(dot(a, a));  // as the reference's helper_math normalize
+#else
     const float inv = 1.0f / sqrtf(dot(a, a));
     return a * inv;
+#endif
 }
 __device__ __forceinline__ V3 cross(V3 a, V3 b) {
     return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
@@ -97,7 +117,21 @@ __device__ __forceinline__ float gc_exp2(float y) {
 __device__ __forceinline__ float gc_pow(float x, float k) {
     if (!(x > 0.0f)) return 0.0f;
     if (x == 1.0f) return 1.0f;
+#ifdef GC_RENDER_FAST
+    return __powf(x, k);  // the hardware log2 / exp2 pair
+#else
     return gc_exp2(k * gc_log2(x));
+#endif
+}
+
+// Division by a constant: exactly rounded in the exact build, a multiply by
+// the reciprocal in the fast one.
+__device__ __forceinline__ float div_const(float x, float d) {
+#ifdef GC_RENDER_FAST
+    return x * (1.0f / d);
+#else
+    return x / d;
+#endif
 }
 
 __device__ __forceinline__ float4 tf_lookup(const float *__restrict__ tf, uint32_t w, float s) {
@@ -177,7 +211,7 @@ __device__ __forceinline__ float sample_corner(const T *__restrict__ b, uint32_t
     if constexpr (sizeof(T) < 4) {
         const uint32_t s = static_cast<uint32_t>(__ldg(p0)) + __ldg(p0 + 1) + __ldg(p1) + __ldg(p1 + 1) + __ldg(p2) +
                            __ldg(p2 + 1) + __ldg(p3) + __ldg(p3 + 1);
-        return static_cast<float>(s) / VoxelTraits<T>::kSum8;
+        return div_const(static_cast<float>(s), VoxelTraits<T>::kSum8);
     } else {
         const float s = ((__ldg(p0) + __ldg(p0 + 1)) + (__ldg(p1) + __ldg(p1 + 1))) +
                         ((__ldg(p2) + __ldg(p2 + 1)) + (__ldg(p3) + __ldg(p3 + 1)));
@@ -227,7 +261,7 @@ __device__ __forceinline__ float sample_trilinear(const T *__restrict__ b, uint3
     const float c11 = fmad(ldv(b, i + BB + B + 1) - ldv(b, i + BB + B), wx, ldv(b, i + BB + B));
     const float c0 = fmad(c10 - c00, wy, c00);
     const float c1 = fmad(c11 - c01, wy, c01);
-    return fmad(c1 - c0, wz, c0) / VoxelTraits<T>::kMax;
+    return div_const(fmad(c1 - c0, wz, c0), VoxelTraits<T>::kMax);
 }
 
 enum Status { kMapped = 0, kUnmapped = 1, kEmpty = 2, kInvisible = 3, kCoarser = 4 };
@@ -309,7 +343,7 @@ __device__ __forceinline__ float2 sample_slot_two(const uint8_t *__restrict__ b,
             s0 += v.x;
             s1 += v.y;
         }
-        return make_float2(static_cast<float>(s0) / 2040.0f, static_cast<float>(s1) / 2040.0f);
+        return make_float2(div_const(static_cast<float>(s0), 2040.0f), div_const(static_cast<float>(s1), 2040.0f));
     }
     uint32_t x0, y0, z0;
     float wx, wy, wz;
@@ -327,7 +361,7 @@ __device__ __forceinline__ float2 sample_slot_two(const uint8_t *__restrict__ b,
         const float c11 = fmad(lv(i + BB + B + 1) - lv(i + BB + B), wx, lv(i + BB + B));
         const float c0 = fmad(c10 - c00, wy, c00);
         const float c1 = fmad(c11 - c01, wy, c01);
-        out[k] = fmad(c1 - c0, wz, c0) / 255.0f;
+        out[k] = div_const(fmad(c1 - c0, wz, c0), 255.0f);
     }
     return make_float2(out[0], out[1]);
 }
@@ -731,7 +765,7 @@ __device__ __forceinline__ void retire_warp(uint32_t *queue, uint32_t nwarps) {
 // Tile scheduler: a warp takes one tile (tile_w x 32/tile_w pixels) at a time
 // from the queue and marches its 32 rays to completion.
 template <typename T>
-__global__ void __launch_bounds__(256) render_kernel(const CacheView cv, const LevelTables lt,
+__global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_kernel(const CacheView cv, const LevelTables lt,
                                                      const ViewParams *__restrict__ views, uint32_t nviews,
                                                      uint32_t total_tiles, uint32_t *queue, uint32_t nwarps) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -776,7 +810,7 @@ __global__ void __launch_bounds__(256) render_kernel(const CacheView cv, const L
 // waits for its slowest ray.  Pixels are enumerated tile by tile, which keeps
 // consecutive grabs spatially close.
 template <typename T>
-__global__ void __launch_bounds__(256) render_pixels_kernel(const CacheView cv, const LevelTables lt,
+__global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_pixels_kernel(const CacheView cv, const LevelTables lt,
                                                             const ViewParams *__restrict__ views, uint32_t nviews,
                                                             uint32_t total_tiles, uint32_t *queue, uint32_t nwarps) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -817,6 +851,29 @@ __global__ void __launch_bounds__(256) render_pixels_kernel(const CacheView cv, 
     retire_warp(queue, nwarps);
 }
 
+// Kernel of a voxel kind (1, 2, 4 bytes, 0 mixed, kTwoChannelU8) and scheduler.
+void *march_kernel(uint32_t kind, bool pixels) {
+    switch (kind) {
+        case 1: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<uint8_t>)
+                              : reinterpret_cast<void *>(render_kernel<uint8_t>);
+        case 2: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<uint16_t>)
+                              : reinterpret_cast<void *>(render_kernel<uint16_t>);
+        case 4: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<float>)
+                              : reinterpret_cast<void *>(render_kernel<float>);
+        case 0: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<MixedVoxel>)
+                              : reinterpret_cast<void *>(render_kernel<MixedVoxel>);
+        case 0x202: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<TwoU8>)
+                                  : reinterpret_cast<void *>(render_kernel<TwoU8>);
+        default: return nullptr;
+    }
+}
+
+}  // namespace GC_MARCH_NS
+}  // namespace gc
+
+#ifndef GC_RENDER_FAST
+namespace gc {
+
 RenderTuning &render_tuning() {
     static RenderTuning t;
     return t;
@@ -825,6 +882,19 @@ RenderTuning &render_tuning() {
 }  // namespace gc
 
 extern "C" {
+int gc_render_precision_set(int precision) {
+    return gc::guard([&] {
+        GC_REQUIRE(precision == GC_RENDER_EXACT || precision == GC_RENDER_FAST_BUILD,
+                   "precision must be GC_RENDER_EXACT or GC_RENDER_FAST_BUILD");
+        gc::render_tuning().precision = static_cast<uint32_t>(precision);
+    });
+}
+int gc_render_precision_get(int *precision) {
+    return gc::guard([&] {
+        GC_REQUIRE(precision, "null argument");
+        *precision = static_cast<int>(gc::render_tuning().precision);
+    });
+}
 int gc_render_empty_skip(int enable) {
     return gc::guard([&] { gc::render_tuning().skip_empty = enable ? 1u : 0u; });
 }
@@ -911,32 +981,26 @@ static RenderLaunch render_launch_config(uint32_t eb, uint32_t total_tiles) {
     const RenderTuning tune = render_tuning();
     const uint32_t threads = tune.threads;
     GC_REQUIRE(threads == 64 || threads == 128 || threads == 256, "render threads must be 64, 128 or 256");
-    static int occupancy[2][5][3] = {};
+    // kernel of the voxel kind (1, 2, 4 bytes; 0: volumes of different voxel
+    // widths share the cache; two 8-bit channels with a 2D transfer function)
+    // from the exact or the fast build
+    const bool pix = tune.scheduler == 1, fast_build = tune.precision == 1;
+    void *kernel = fast_build ? fast::march_kernel(eb, pix) : exact::march_kernel(eb, pix);
+    if (!kernel) fail(GC_ERR_UNSUPPORTED, "the ray caster supports one channel of 1, 2 or 4 bytes");
+    const int slot = eb == 1 ? 0 : eb == 2 ? 1 : eb == 4 ? 2 : eb == 0 ? 3 : 4;
+    static int occupancy[2][2][5][3] = {};
     const int tslot = threads == 64 ? 0 : (threads == 128 ? 1 : 2);
-    auto config = [&](auto kernel, int sched, int slot) {
-        int &occ = occupancy[sched][slot][tslot];
-        if (!occ) {
-            int b = 0;
-            GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, static_cast<int>(threads), 0));
-            occ = std::max(1, b);
-        }
-        int per_sm = occ;
-        if (tune.blocks_per_sm > 0) per_sm = std::min(per_sm, static_cast<int>(tune.blocks_per_sm));
-        const uint32_t max_blocks = static_cast<uint32_t>(sm_count() * per_sm);
-        const uint32_t want = div_up(total_tiles, threads / 32);
-        return RenderLaunch{reinterpret_cast<void *>(kernel), std::max(1u, std::min(max_blocks, want)), threads};
-    };
-    const bool pix = tune.scheduler == 1;
-    switch (eb) {
-        case 1: return pix ? config(render_pixels_kernel<uint8_t>, 1, 0) : config(render_kernel<uint8_t>, 0, 0);
-        case 2: return pix ? config(render_pixels_kernel<uint16_t>, 1, 1) : config(render_kernel<uint16_t>, 0, 1);
-        case 4: return pix ? config(render_pixels_kernel<float>, 1, 2) : config(render_kernel<float>, 0, 2);
-        case 0:  // volumes of different voxel widths share the cache
-            return pix ? config(render_pixels_kernel<MixedVoxel>, 1, 3) : config(render_kernel<MixedVoxel>, 0, 3);
-        case kTwoChannelU8:  // two 8-bit channels per voxel (2D transfer function)
-            return pix ? config(render_pixels_kernel<TwoU8>, 1, 4) : config(render_kernel<TwoU8>, 0, 4);
-        default: fail(GC_ERR_UNSUPPORTED, "the ray caster supports one channel of 1, 2 or 4 bytes");
+    int &occ = occupancy[fast_build ? 1 : 0][pix ? 1 : 0][slot][tslot];
+    if (!occ) {
+        int b = 0;
+        GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, static_cast<int>(threads), 0));
+        occ = std::max(1, b);
     }
+    int per_sm = occ;
+    if (tune.blocks_per_sm > 0) per_sm = std::min(per_sm, static_cast<int>(tune.blocks_per_sm));
+    const uint32_t max_blocks = static_cast<uint32_t>(sm_count() * per_sm);
+    const uint32_t want = div_up(total_tiles, threads / 32);
+    return RenderLaunch{kernel, std::max(1u, std::min(max_blocks, want)), threads};
 }
 
 void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams *views_dev,
@@ -1013,3 +1077,4 @@ void launch_render_graph(RenderGraph &g, const CacheView &cv, const LevelTables 
 }
 
 }  // namespace gc
+#endif  // GC_RENDER_FAST

@@ -28,9 +28,10 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 # order (the host oracle evaluates the same sequence).
 EXTRA = {
     "render.cu": ["-fmad=false"],
+    "render_fast.cu": ["-fmad=true"],  # the fast build of the same march (render_fast.cu includes render.cu)
 }
 SOURCES = ["config.cpp", "generate.cu", "preprocess.cu", "cache_kernels.cu", "cache_manager.cu", "render.cu",
-           "brickfiles.cpp"]
+           "render_fast.cu", "brickfiles.cpp"]
 
 
 def nvcc():
@@ -46,10 +47,16 @@ def _headers_mtime():
     return max(os.path.getmtime(p) for p in paths)
 
 
+# units that include another unit's source
+INCLUDES = {"render_fast.cu": ["render.cu"]}
+
+
 def _compile(src, hdr_mtime, verbose):
     path = os.path.join(CSRC, src)
     obj = os.path.join(BUILD, src + ".o")
-    if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(path), hdr_mtime):
+    newest = max([os.path.getmtime(path), hdr_mtime] + [os.path.getmtime(os.path.join(CSRC, d))
+                                                         for d in INCLUDES.get(src, [])])
+    if os.path.exists(obj) and os.path.getmtime(obj) >= newest:
         return obj, False
     cmd = [nvcc()] + ARCH + COMMON + EXTRA.get(src, [])
     if src.endswith(".cpp"):

@@ -168,6 +168,7 @@ _SIGS = {
     "gc_miss_list_noalloc": [vp, C.c_uint64, C.c_uint32, P(Layout), C.c_uint32, vp, vp, vp],
     "gc_render_tuning_set": [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32],
     "gc_render_tuning_get": [P(C.c_uint32)],
+    "gc_render_precision_set": [C.c_int], "gc_render_precision_get": [P(C.c_int)],
 }
 _RESTYPES = {"gc_last_error": C.c_char_p, "gc_version": C.c_char_p, "gc_brick_key": C.c_uint64,
              "gc_kernel_launches": C.c_uint64}
@@ -467,6 +468,18 @@ def make_view(inv_view, width, height, tf_ptr, tf_width, rgba_ptr, tbuf_ptr, sta
     return View((C.c_float * 12)(*inv_view), width, height, (C.c_float * 3)(*bbox_min), (C.c_float * 3)(*bbox_max),
                 tstep, focal, early_alpha, mode, sampler, tf_width, vp(tf_ptr), vp(rgba_ptr), vp(tbuf_ptr),
                 vp(state_ptr), vp(status_ptr or None), volume, tf_height, fallback)
+
+
+RENDER_EXACT, RENDER_FAST = 0, 1
+
+
+def render_precision(precision=None):
+    """Set (RENDER_EXACT / RENDER_FAST) and/or return the ray caster's arithmetic."""
+    if precision is not None:
+        check(lib.gc_render_precision_set(int(precision)))
+    out = C.c_int()
+    check(lib.gc_render_precision_get(C.byref(out)))
+    return out.value
 
 
 def render_empty_skip(enable):

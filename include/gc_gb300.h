@@ -467,6 +467,19 @@ int gc_render_batch(gc_cache_t cache, const gc_view *views, uint32_t n, void *st
  * the autotuner of the Python host (gcgb300.autotune_render). */
 int gc_render_tuning_set(uint32_t scheduler, uint32_t tile_w, uint32_t threads, uint32_t blocks_per_sm);
 int gc_render_tuning_get(uint32_t out[4]);
+/* Arithmetic of the ray caster (process-wide).  GC_RENDER_EXACT (default):
+ * every float operation separately rounded in a fixed order, exactly rounded
+ * division, square root and power -- the same values as the FP32 oracle, bit
+ * for bit.  GC_RENDER_FAST_BUILD: the same method compiled with fused
+ * multiply-add contraction, rsqrtf, the hardware log2/exp2 pair for the
+ * opacity correction and reciprocal multiplies (the operations of the
+ * reference's own build); images within 1/255 of the double-precision
+ * method except where a float decision of the march (early termination,
+ * brick and level boundaries) lands within rounding distance. */
+#define GC_RENDER_EXACT 0
+#define GC_RENDER_FAST_BUILD 1
+int gc_render_precision_set(int precision);
+int gc_render_precision_get(int *precision);
 /* Empty-space skipping (process-wide, on by default; images are identical
  * either way): each pool slot records the value range of its brick and each
  * DVR view of a one-channel volume the value range its transfer function can

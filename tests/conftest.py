@@ -40,3 +40,13 @@ def torch_cuda():
         pytest.fail("CUDA device required for gpu-marked tests")
     torch.cuda.init()
     return torch
+
+
+@pytest.fixture(autouse=True)
+def exact_ray_caster():
+    """Every test starts and ends with the exact ray-caster build (the FP32
+    oracle's operations); tests of the fast build switch it on themselves."""
+    yield
+    mod = sys.modules.get("gcgb300")
+    if mod is not None:
+        mod.render_precision(mod.RENDER_EXACT)

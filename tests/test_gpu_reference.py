@@ -130,9 +130,12 @@ LOCKSTEP = {
 }
 
 
+@pytest.mark.parametrize("precision", ["exact", "fast"])
 @pytest.mark.parametrize("case", sorted(LOCKSTEP))
-def test_cache_and_ray_caster_match_reference(gc, torch_cuda, prepared, case):
+def test_cache_and_ray_caster_match_reference(gc, torch_cuda, prepared, case, precision):
+    """Both builds of the ray caster (exact and fast) against the reference's."""
     geom, pool, W, H, mode, dists, cap = LOCKSTEP[case]
+    gc.render_precision(gc.RENDER_FAST if precision == "fast" else gc.RENDER_EXACT)
     vol, layout, d, ref, store, offs, empty = prepared(geom)
     t = torch_cuda
     ref.open(pool)
@@ -203,7 +206,7 @@ def test_cache_and_ray_caster_match_reference(gc, torch_cuda, prepared, case):
                     conv_worst = max(conv_worst, int(dif.max()))
                     break
         assert cm.stats().device_error == 0
-        print(f"\n{case}: {frames} frames; RGBA beyond {RGBA_TOL}/255: {beyond} of {compared} pixels (max {worst}); "
+        print(f"\n{case} ({precision}): {frames} frames; RGBA beyond {RGBA_TOL}/255: {beyond} of {compared} pixels (max {worst}); "
               f"converged images: {conv_beyond} of {conv_compared} (max {conv_worst}); t differing {t_mismatch}; "
               f"usage/request words differing before replay {usage_mismatch}")
         assert beyond <= OUTLIER_SHARE * compared, (beyond, compared, worst)

@@ -16,6 +16,7 @@ pytestmark = pytest.mark.gpu
 
 RGBA_TOL_FP32 = 0
 RGBA_TOL_FP64 = 1
+FAST_OUTLIER_SHARE = 1e-3  # fast build vs FP64: pixels allowed beyond 1/255 (termination crossings)
 
 
 class Scene:
@@ -162,9 +163,14 @@ def test_batch_matches_sequential_oracle(gc, orc, torch_cuda):
         s.compare_cache(f"frame {f}")
 
 
-def test_converged_image_vs_fp64_oracle(gc, orc, torch_cuda):
+@pytest.mark.parametrize("precision", ["exact", "fast"])
+def test_converged_image_vs_fp64_oracle(gc, orc, torch_cuda, precision):
     """After convergence the FP32 CUDA image is within 1/255 of the
-    double-precision restatement of the same method."""
+    double-precision restatement of the same method: every pixel for the exact
+    build; for the fast build (FMA contraction, rsqrtf, hardware log2/exp2)
+    all but FAST_OUTLIER_SHARE of the pixels, those where the accumulated
+    alpha crosses the early-termination threshold one sample apart."""
+    gc.render_precision(gc.RENDER_FAST if precision == "fast" else gc.RENDER_EXACT)
     s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 216)
     tf = scenario.ramp_tf()
     tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
@@ -193,8 +199,11 @@ def test_converged_image_vs_fp64_oracle(gc, orc, torch_cuda):
         s.cm.dump(gc.DUMP_MRPD, s.oc.mrpd())
         s.cm.dump(gc.DUMP_POOL, s.oc.pool())
         s.oc.render_f64(v, tf, r64, np.zeros(W * H), np.zeros(W * H * 4), scratch_u, scratch_r)
-        d = rgba_diff(g[0].cpu().numpy(), r64)
-        assert d.max() <= RGBA_TOL_FP64, (mode, sampler, d.max())
+        d = rgba_diff(g[0].cpu().numpy(), r64).reshape(-1, 4).max(axis=1)
+        if precision == "exact":
+            assert d.max() <= RGBA_TOL_FP64, (mode, sampler, d.max())
+        else:
+            assert np.count_nonzero(d > RGBA_TOL_FP64) <= FAST_OUTLIER_SHARE * d.size, (mode, sampler, d.max())
         assert (g[0].cpu().numpy() >> 24).astype(bool).mean() > 0.05  # the image is not empty
 
 
@@ -394,6 +403,44 @@ def test_coarser_level_fallback_preview(gc, orc, torch_cuda):
     img2, st2 = frame(near, 1)
     assert stn == 0 and st2 == 0
     assert np.array_equal(ref, img2)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_coarser_level_fallback_matches_oracle(gc, orc, torch_cuda, mode):
+    """The preview mode against the oracle's restatement of the level walk of
+    K_CacheManager::get (K_CacheManager.hpp:163-260): a missing brick is
+    requested on the asked level only, the first mapped coarser level is
+    sampled instead, an empty one ends the lookup.  Coarse levels are paged in
+    by a far view, then a near view is previewed frame by frame (progressive
+    buffers restarted each frame, as the mode requires): RGBA, t buffer,
+    colour state and the cache state after every update equal the oracle's."""
+    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 60)
+    tf = scenario.ramp_tf() if mode == 0 else scenario.bumps_tf(4)
+    tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
+    W, H = 72, 56
+    g, o = s.buffers(W, H)
+    far, near = scenario.orbit_camera(gc, 2, 12, 9.0), scenario.orbit_camera(gc, 2, 12, 2.2)
+    coarse_frames = 0
+    for f in range(14):
+        m, fb = (far, 0) if f < 6 else (near, 1)
+        for x in g:
+            x.zero_()
+        for x in o:
+            x[:] = 0
+        v = s.view(m, W, H, tf_dev, 256, g, mode=mode, fallback=fb)
+        st = torch_cuda.zeros(1, dtype=torch_cuda.int32, device="cuda")
+        v.status = st.data_ptr()
+        s.cm.render(v)
+        s.oc.render(v, tf, *o)
+        torch_cuda.cuda.synchronize()
+        coarse_frames += bool(int(st.item()) & 2)
+        d = rgba_diff(g[0].cpu().numpy(), o[0])
+        assert d.max() <= RGBA_TOL_FP32, f"frame {f}: RGBA off by {d.max()}"
+        assert np.array_equal(g[1].cpu().numpy(), o[1]), f"frame {f}: t buffer"
+        assert np.array_equal(g[2].cpu().numpy(), o[2]), f"frame {f}: colour state"
+        assert s.cm.update() == s.oc.update(), f"frame {f}"
+        s.compare_cache(f"frame {f}")
+    assert coarse_frames > 0, "the near view never sampled a coarser level"
 
 
 @pytest.mark.parametrize("case", ["inside", "one_pixel", "one_row", "miss", "bbox"])
