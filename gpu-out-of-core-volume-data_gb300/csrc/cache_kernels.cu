@@ -581,9 +581,9 @@ void launch_gather_bricks(const ulonglong2 *src, uint32_t n, uint64_t stride, ui
     if (beside) {
         // Next to a persistent ray-caster launch: at its occupancy each SM
         // sub-partition keeps 1024 registers free, room for one warp of 32
-        // registers per thread -- a 128-thread block of 4 warps per SM runs
-        // during the render instead of after it (two 16-byte loads in flight
-        // per thread).
+        // registers per thread -- 128-thread blocks (one warp per
+        // sub-partition), two per SM over the grid, run during the render
+        // instead of after it (two 16-byte loads in flight per thread).
         const uint32_t grid = std::min<uint32_t>(n, 2 * sms);
         if (vec16)
             gather_bricks_beside_kernel<uint4><<<grid, 128, 0, s>>>(src, n, stride, dst);

@@ -202,6 +202,8 @@ struct BrickParams {
     uint32_t eb;
     uint64_t nsmall;      // small bricks in the level
     uint32_t fast;        // 16-byte rows: B*eb and D[0]*eb multiples of 16, level and out 16-byte aligned
+    uint32_t b_shift;     // log2(B) (fast path: B a power of two)
+    uint32_t cpr_shift;   // log2(16-byte chunks per brick row)
 };
 
 // One voxel of a small brick the slow way (bricks on the level's edge, odd
@@ -246,26 +248,32 @@ __device__ __forceinline__ uint4 row_bytes16(uint4 a, uint4 b, uint32_t s) {
     return make_uint4(o[0], o[1], o[2], o[3]);
 }
 
-// One CTA per small brick (grid-stride).  A brick whose B^3 source voxels all
-// lie inside the level (the great majority) is copied row by row in 16-byte
-// chunks: every row of the brick starts at the same byte offset s modulo 16
-// of the level (rows are D[0]*eb bytes apart, a multiple of 16), so each
-// chunk is two aligned 16-byte loads and a funnel shift by s, stored with one
-// 16-byte store.  Bricks on the level's edge, unvisited ones and odd voxel
-// widths take the per-voxel path.
+// One warp per small brick (grid-stride over bricks), the brick copied in
+// 16-byte output chunks (p.fast: B a power of two, whole chunks per row, rows
+// 16 bytes apart in the level).  A chunk whose source row lies inside the
+// level and whose voxels all lie inside the row -- all chunks of an interior
+// brick -- starts at the same byte offset s modulo 16 as every other such
+// chunk of the brick, so it is two aligned 16-byte loads and a funnel shift by
+// s, stored with one 16-byte store.  A row outside the level, or an unvisited
+// brick, stores zeros; a chunk straddling the level's x edge is assembled
+// voxel by voxel.  Odd voxel widths and unaligned buffers take the per-voxel
+// path throughout.  The per-brick index arithmetic is done once per warp and
+// brick (16 chunks per lane for B16 u16), the per-chunk one with shifts.
 __global__ void __launch_bounds__(256) brick_kernel(const uint8_t *__restrict__ level,
                                                     uint8_t *__restrict__ out, BrickParams p) {
     const uint32_t B = p.B;
     const uint32_t bvx = p.BB[0] * B, bvy = p.BB[1] * B;
     const uint64_t big_bytes = static_cast<uint64_t>(bvx) * bvy * (p.BB[2] * B) * p.eb;
     const uint32_t nsx = p.nbig[0] * p.BB[0], nsy = p.nbig[1] * p.BB[1];
-    for (uint64_t sb = blockIdx.x; sb < p.nsmall; sb += gridDim.x) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t nsmall = static_cast<uint32_t>(p.nsmall);  // < 2^32 (checked on the host)
+    for (uint32_t sb = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sb < nsmall; sb += nwarps) {
         // small brick grid = nbig * BB per axis, x fastest
-        const uint32_t sx = static_cast<uint32_t>(sb % nsx);
-        const uint32_t sy = static_cast<uint32_t>((sb / nsx) % nsy);
-        const uint32_t sz = static_cast<uint32_t>(sb / (static_cast<uint64_t>(nsx) * nsy));
+        const uint32_t sx = sb % nsx, rest = sb / nsx;
+        const uint32_t sy = rest % nsy, sz = rest / nsy;
         const uint32_t gx = sx / p.BB[0], gy = sy / p.BB[1], gz = sz / p.BB[2];
-        const uint32_t ix = sx % p.BB[0], iy = sy % p.BB[1], iz = sz % p.BB[2];
+        const uint32_t ix = sx - gx * p.BB[0], iy = sy - gy * p.BB[1], iz = sz - gz * p.BB[2];
         const uint64_t big = (static_cast<uint64_t>(gz) * p.nbig[1] + gy) * p.nbig[0] + gx;
         uint8_t *bbase = out + big * big_bytes;
         const int64_t ox = static_cast<int64_t>(sx) * p.Beff - p.c;
@@ -276,30 +284,39 @@ __global__ void __launch_bounds__(256) brick_kernel(const uint8_t *__restrict__ 
         // where their covering border reaches into the volume.
         const bool visited = static_cast<uint64_t>(sx) * p.Beff < p.D[0] &&
                              static_cast<uint64_t>(sy) * p.Beff < p.D[1] && static_cast<uint64_t>(sz) * p.Beff < p.D[2];
-        const bool interior = visited && ox >= 0 && oy >= 0 && oz >= 0 && ox + B <= p.D[0] && oy + B <= p.D[1] &&
-                              oz + B <= p.D[2];
-        if (p.fast && interior) {
-            const uint32_t cpr = B * p.eb / 16u;  // 16-byte chunks per row
-            const uint32_t nchunks = B * B * cpr;
+        if (p.fast) {
+            const uint32_t k = 16u / p.eb;                  // voxels per chunk
+            const uint32_t nchunks = 1u << (2u * p.b_shift + p.cpr_shift);
             const uint64_t row_stride = static_cast<uint64_t>(p.D[0]) * p.eb;
-            const uint64_t src0 = ((static_cast<uint64_t>(oz) * p.D[1] + oy) * p.D[0] + ox) * p.eb;
-            const uint32_t s = static_cast<uint32_t>(src0 & 15u);
-            const uint64_t slice = row_stride * p.D[1];
-            uint8_t *obase = bbase + (static_cast<uint64_t>(ix) * B) * p.eb;
-            for (uint32_t c = threadIdx.x; c < nchunks; c += blockDim.x) {
-                const uint32_t cx = c % cpr, row = c / cpr;
-                const uint32_t ly = row % B, lz = row / B;
-                const uint64_t src = src0 - s + lz * slice + ly * row_stride + cx * 16u;
-                const uint4 a = __ldg(reinterpret_cast<const uint4 *>(level + src));
-                const uint4 v = s ? row_bytes16(a, __ldg(reinterpret_cast<const uint4 *>(level + src + 16)), s) : a;
-                uint8_t *dst = obase + ((static_cast<uint64_t>(iz * B + lz) * bvy + (iy * B + ly)) * bvx) * p.eb +
-                               cx * 16u;
-                *reinterpret_cast<uint4 *>(dst) = v;
+            // byte offset modulo 16 of the brick's first voxel in any row (rows
+            // are multiples of 16 bytes apart; ox may be negative)
+            const uint32_t s = static_cast<uint32_t>(ox * static_cast<int64_t>(p.eb)) & 15u;
+            uint8_t *obase = bbase + ((static_cast<uint64_t>(iz) * B * bvy + iy * B) * bvx + ix * B) * p.eb;
+            const uint64_t drow = static_cast<uint64_t>(bvx) * p.eb;  // output row stride
+#pragma unroll 4
+            for (uint32_t c = lane; c < nchunks; c += 32u) {
+                const uint32_t cx = c & ((1u << p.cpr_shift) - 1u), row = c >> p.cpr_shift;
+                const uint32_t ly = row & (B - 1u), lz = row >> p.b_shift;
+                uint8_t *dst = obase + (static_cast<uint64_t>(lz) * bvy + ly) * drow + cx * 16u;
+                const int64_t ry = oy + ly, rz = oz + lz, x0 = ox + static_cast<int64_t>(cx) * k;
+                const bool row_in = visited && ry >= 0 && rz >= 0 && ry < p.D[1] && rz < p.D[2];
+                if (!row_in) {
+                    *reinterpret_cast<uint4 *>(dst) = make_uint4(0u, 0u, 0u, 0u);
+                } else if (x0 >= 0 && x0 + k <= p.D[0]) {
+                    const uint64_t src = (static_cast<uint64_t>(rz) * p.D[1] + ry) * row_stride +
+                                         static_cast<uint64_t>(x0) * p.eb - s;
+                    const uint4 a = __ldg(reinterpret_cast<const uint4 *>(level + src));
+                    *reinterpret_cast<uint4 *>(dst) =
+                        s ? row_bytes16(a, __ldg(reinterpret_cast<const uint4 *>(level + src + 16)), s) : a;
+                } else {
+                    for (uint32_t v = 0; v < k; ++v)
+                        brick_voxel(level, dst + v * p.eb, p, true, x0 + v, ry, rz);
+                }
             }
             continue;
         }
         const uint32_t nvox = B * B * B;
-        for (uint32_t v = threadIdx.x; v < nvox; v += blockDim.x) {
+        for (uint32_t v = lane; v < nvox; v += 32u) {
             const uint32_t lx = v % B, ly = (v / B) % B, lz = v / (B * B);
             uint8_t *dptr = bbase + ((static_cast<uint64_t>(iz * B + lz) * bvy + (iy * B + ly)) * bvx + (ix * B + lx)) * p.eb;
             brick_voxel(level, dptr, p, visited, ox + lx, oy + ly, oz + lz);
@@ -388,10 +405,16 @@ int gc_bricks_build(const void *level, const uint32_t level_dims[3], const gc_vo
         // 16-byte row chunks: whole chunks per brick row, rows 16 bytes apart
         // in the level (so every row of a brick has the same alignment), and
         // both buffers 16-byte aligned
-        p.fast = (p.eb == 1 || p.eb == 2 || p.eb == 4) && (p.B * p.eb) % 16 == 0 &&
+        GC_REQUIRE(p.nsmall < (1ull << 32), "too many bricks in one level");
+        p.fast = (p.eb == 1 || p.eb == 2 || p.eb == 4) && (p.B & (p.B - 1)) == 0 && (p.B * p.eb) % 16 == 0 &&
                  (static_cast<uint64_t>(p.D[0]) * p.eb) % 16 == 0 &&
                  reinterpret_cast<uintptr_t>(level) % 16 == 0 && reinterpret_cast<uintptr_t>(out) % 16 == 0;
-        const uint64_t grid = std::min<uint64_t>(p.nsmall, static_cast<uint64_t>(sm_count()) * 16);
+        p.b_shift = p.cpr_shift = 0;
+        while ((1u << p.b_shift) < p.B) ++p.b_shift;
+        while (p.fast && (16u << p.cpr_shift) < p.B * p.eb) ++p.cpr_shift;
+        // one warp per brick: 8 warps per block, enough blocks to fill every SM
+        const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>((p.nsmall + 7) / 8,
+                                                                       static_cast<uint64_t>(sm_count()) * 8));
         brick_kernel<<<static_cast<unsigned>(grid), 256, 0, as_stream(stream)>>>(
             static_cast<const uint8_t *>(level), static_cast<uint8_t *>(out), p);
         GC_CUDA(cudaGetLastError());

@@ -892,8 +892,9 @@ typedef struct {
     uint32_t e[4];
 } walk;
 
-/* sample[0] (and sample[1] for two 8-bit channels, voxel i channel k at byte 2i+k) */
-static int fetch32(orc_cache *c, uint32_t sampler, uint32_t lod, f3 np, walk *w, float *sample) {
+/* sample[0] (and sample[1] for two 8-bit channels, voxel i channel k at byte 2i+k);
+ * request: stamp the request word of a missing brick */
+static int fetch32_at(orc_cache *c, uint32_t sampler, uint32_t lod, f3 np, walk *w, float *sample, int request) {
     float px = np.x * c->ior[lod][0], py = np.y * c->ior[lod][1], pz = np.z * c->ior[lod][2];
     uint32_t cx = c->off[lod] + (uint32_t)(px * (float)c->nb[lod][0]);
     uint32_t cy = (uint32_t)(py * (float)c->nb[lod][1]);
@@ -987,10 +988,28 @@ static int fetch32(orc_cache *c, uint32_t sampler, uint32_t lod, f3 np, walk *w,
         return 0;
     }
     if (w->e[3] == 0) {
-        __atomic_store_n(&c->req[idx], c->ts, __ATOMIC_RELAXED);
+        if (request) __atomic_store_n(&c->req[idx], c->ts, __ATOMIC_RELAXED);
         return 1;
     }
     return 2;
+}
+
+/* 0 mapped, 1 unmapped (requested), 2 empty, 4 a coarser level sampled.
+ * fallback: the preview mode of K_CacheManager::get (K_CacheManager.hpp:163-260):
+ * the missing brick is requested on the asked level only, then the levels
+ * above it are read in order: the first mapped one is sampled (its usage
+ * stamped), an empty one ends the lookup, an unmapped one is passed over. */
+static int fetch32(orc_cache *c, uint32_t sampler, uint32_t lod, f3 np, walk *w, float *sample, int fallback) {
+    int st = fetch32_at(c, sampler, lod, np, w, sample, 1);
+    if (st != 1 || !fallback) return st;
+    for (uint32_t l2 = lod + 1; l2 < c->nl; ++l2) {
+        walk w2;
+        w2.pcx = w2.pcy = w2.pcz = 0xffffffffu;
+        int s2 = fetch32_at(c, sampler, l2, np, &w2, sample, 0);
+        if (s2 == 2) return 2;
+        if (s2 == 0) return 4;
+    }
+    return 1;
 }
 
 /* One sample of K_CacheManager::get_normalized with a fresh page walk (the
@@ -999,7 +1018,7 @@ static int fetch32(orc_cache *c, uint32_t sampler, uint32_t lod, f3 np, walk *w,
 int orc_sample_normalized(orc_cache *c, uint32_t level, float x, float y, float z, float *out) {
     walk w;
     w.pcx = w.pcy = w.pcz = UINT32_MAX;
-    return fetch32(c, GC_SAMPLER_REFERENCE, level, mk(x, y, z), &w, out);
+    return fetch32(c, GC_SAMPLER_REFERENCE, level, mk(x, y, z), &w, out, 0);
 }
 
 static void march32(orc_cache *c, const gc_view *v, const float *tf, const lod_tables *T, uint32_t x, uint32_t y,
@@ -1071,9 +1090,9 @@ static void march32(orc_cache *c, const gc_view *v, const float *tf, const lod_t
                 if (sl >= pX * 1.0f || su >= pY * 1.0f) break;
             }
             float smp[2] = {0.f, 0.f};
-            int st = fetch32(c, v->sampler, lod, np, &w, smp);
+            int st = fetch32(c, v->sampler, lod, np, &w, smp, v->fallback != 0);
             float sample = smp[0];
-            if (st != 0) {
+            if (st != 0 && st != 4) {
                 if (st == 1) {
                     if (!unm) {
                         tbuf[i] = t;

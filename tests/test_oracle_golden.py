@@ -104,3 +104,24 @@ def test_oracle_mip_threads_equal_one_thread(orc, dims, eb, nc, dtype):
     n = dims[0] * dims[1] * dims[2] * eb // np.dtype(dtype).itemsize
     src = rng.integers(0, np.iinfo(dtype).max, size=n, dtype=dtype)
     assert np.array_equal(orc.mip_level(src, dims, eb, nc), orc.mip_level(src, dims, eb, nc, threads=0))
+
+
+def test_brick_origins_never_alias():
+    """The install finds a brick's page-directory entry from its float origin
+    x / (V * (1 / (B - 2c))) + FLT_EPSILON (CacheManagerKernels.cu:75-86):
+    for every brick count up to 4000 per axis and the brick sizes / coverings
+    in use, distinct bricks land on distinct entries, so an install list
+    (distinct requests) never names one entry twice.  The install's
+    lowest-index-wins owner word (the serial order of reference_new_bricks)
+    therefore only guards against lists that name an entry twice by hand."""
+    import numpy as np
+
+    f32 = np.float32
+    eps = f32(1.1920928955078125e-7)
+    for B, c in ((8, 1), (16, 0), (16, 1), (16, 2), (32, 1), (32, 2), (64, 1)):
+        one_over = f32(1.0) / f32(B - 2 * c)
+        for nb in range(1, 4001):
+            x = np.arange(nb, dtype=np.float32)
+            origin = (x / (f32(nb * (B - 2 * c)) * one_over)).astype(np.float32) + eps
+            entry = (origin * f32(nb)).astype(np.float32).astype(np.int64)
+            assert np.array_equal(entry, np.arange(nb)), (B, c, nb)
