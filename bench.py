@@ -51,6 +51,7 @@ import json
 import math
 import os
 import statistics
+import shutil
 import subprocess
 import sys
 import tempfile
@@ -75,12 +76,17 @@ CONFIGS = {
     "c3": dict(VOL2048, B=32, c=1, pool_bytes=4 << 30, pool_slots=None, batch=64,
                sizes=((256, 256), (512, 512), (1024, 1024), (1920, 1080)), dist=(0.5, 3.0), tf="bumps",
                early=0.99, fov=45.0),
-    # large stress, scaled to the box (4096^3 x 2 channels with covering 2 needs ~300 GB of host brick
-    # store; the box has 197 GB of RAM): two u8 channels (blob field + independent noise field),
-    # covering 2, big bricks 2^3, 8 GiB pool, 2048^2 views on a path through the interior, 2D TF
-    "c5": dict(size=(2048, 2048, 2048), bpc=1, channels=2, nblobs=32, sigma=(40.0, 300.0), amp=(60, 200), noise=20,
+    # large stress: 4096^3 x 2 u8 channels (blob field + independent noise field), covering 2, big
+    # bricks 2^3, 8 GiB pool, 2048^2 views on a path through the interior, 2D TF.  Its bricked store
+    # (~375 GB with covering 2) fits no host memory here; the volume's mip pyramid (146 GiB) stays on
+    # the device and missing bricks are cut from it (run_stress; --config c5 runs the plain loop on a
+    # 2048^3 x 2 host store instead)
+    "c5": dict(size=(4096, 4096, 4096), bpc=1, channels=2, nblobs=32, sigma=(80.0, 600.0), amp=(60, 200), noise=20,
                seed=5, B=16, c=2, bb=(2, 2, 2), pool_bytes=8 << 30, pool_slots=None, W=2048, H=2048, frames=240,
                path="cross", dist=(0.0, 0.0), tf="2d", early=0.99, fov=45.0, cap=256),
+    "c5_host": dict(size=(2048, 2048, 2048), bpc=1, channels=2, nblobs=32, sigma=(40.0, 300.0), amp=(60, 200),
+                    noise=20, seed=5, B=16, c=2, bb=(2, 2, 2), pool_bytes=8 << 30, pool_slots=None, W=2048, H=2048,
+                    frames=240, path="cross", dist=(0.0, 0.0), tf="2d", early=0.99, fov=45.0, cap=256),
     # serving: three resident volumes sharing one 24 GiB pool, Poisson requests
     "c4": dict(B=16, c=1, pool_bytes=24 << 30, rate=200.0, duration=6.0, batch=64,
                sizes=((256, 256), (512, 512), (1024, 1024), (1920, 1080)), dist=(0.5, 3.0), early=0.99, fov=45.0,
@@ -161,7 +167,7 @@ def bench_config(name, cfg, args):
     pool = pool_slots(cfg)
     eb = cfg["bpc"] * cfg.get("channels", 1)
     l2 = {"c2": "inputs > L2 (2 GiB pool, 103 MB page directory, 28 GiB host brick store)",
-          "c5": "inputs > L2 (8 GiB pool, 43 GiB host brick store)"}.get(
+          "c5_host": "inputs > L2 (8 GiB pool, 43 GiB host brick store)"}.get(
         name, "in-core volume; L2 not flushed (the c1 case is for profiling)")
     return {"workload": wl, "brick_size": cfg["B"], "covering": cfg["c"], "pool_slots": list(pool),
             "pool_gib": round(pool[0] * pool[1] * pool[2] * cfg["B"] ** 3 * eb / 2 ** 30, 3),
@@ -514,13 +520,20 @@ def run_ours(args):
         for f in range(args.warmup):
             S.converge(spec(f), cap=cfg.get("cap", 64))
         s0, l0 = S.cm.stats(), gc.kernel_launches()
+        ev = None if e2e else render_events
         torch.cuda.nvtx.range_push("timed_e2e" if e2e else "timed")
         wall, lat, info = timed(torch, S.stream, lambda i: S.converge(spec(views[i]), e2e=e2e,
-                                                                      cap=cfg.get("cap", 64)), args.steps)
+                                                                      cap=cfg.get("cap", 64), render_events=ev),
+                                args.steps)
         torch.cuda.nvtx.range_pop()
         launches = gc.kernel_launches() - l0
         s1 = S.cm.stats()
         return S, wall, lat, info, launches, s0, s1
+
+    # ray-caster launches of the timed value pass, bracketed by CUDA events on
+    # the launch stream: the live split of a step's time (the launch list under
+    # ncu serialises launches and slows the upload's host reads)
+    render_events = []
 
     # launch configuration: autotuned once, on three views spread along the
     # path (near, middle, far), in a cache of its own
@@ -676,7 +689,8 @@ def run_ours(args):
         out["cpu_baseline"] = cpu_baseline(gc, S, cfg, last, args, images)
         out["parity_max_abs"] = out["cpu_baseline"]["parity"]["max_abs_rgba"]
     S.close()
-    del store
+    del store, S
+    release_memory(torch)
     if rank == 0 and not args.no_reference_gpu:
         try:
             out["reference_gpu_build"] = reference_gpu_baseline(gc, torch, args)
@@ -684,12 +698,29 @@ def run_ours(args):
             out["reference_gpu_build"] = {"unavailable": f"{type(e).__name__}: {e}"[:300]}
     if rank == 0 and not args.no_batched:
         out["batched"] = run_batched(gc, torch, args)
+        release_memory(torch)
     if rank == 0 and not args.no_serving:
         out["serving"] = run_serving_sweep(gc, torch, args)
+        release_memory(torch)
+    if rank == 0 and not args.no_stress:
+        try:
+            out["stress"] = run_stress(gc, torch, args)
+        except Exception as e:  # a reported stress leg: its failure does not void the line
+            out["stress"] = {"unavailable": f"{type(e).__name__}: {e}"[:300]}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def release_memory(torch):
+    """Returns cached device blocks and cached page-locked host blocks (the
+    brick stores of a finished leg) to the system before the next leg."""
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    host_empty = getattr(torch._C, "_host_emptyCache", None)
+    if host_empty is not None:
+        host_empty()
 
 
 def cache_delta(s0, s1):
@@ -825,6 +856,107 @@ def run_c3(args):
         Session.brick_bins = False
         out["with_brick_bins"] = bins
     print(json.dumps(out), flush=True)
+
+
+STRESS_VIEWS = 3  # views of the c5 path the default run renders
+
+
+def run_stress(gc, torch, args, nviews=STRESS_VIEWS):
+    """c5 at its configured size.  The 4096^3 x 2-channel volume (128 GiB) is
+    generated on the device and its mip pyramid built there (146 GiB, kept
+    resident); an 8 GiB cache takes its bricks from that pyramid: each missing
+    big brick is cut from its level on the device with the bricker's rule
+    (gc_cache_set_volume_source_device) -- no brick store exists.  Views of
+    the path through the interior, 2048^2, 2D transfer function, each to
+    convergence (at most `cap` iterations)."""
+    cfg = CONFIGS["c5"]
+    size, nc = cfg["size"], cfg["channels"]
+    eb = cfg["bpc"] * nc
+    vol = gc.volume_desc(size, cfg["B"], cfg["c"], eb, nc, cfg["bb"])
+    layout = gc.compute_layout(vol)
+    poffs, total = gc.pyramid_offsets(layout, eb)
+    torch.cuda.empty_cache()
+    pyr = torch.empty(total, dtype=torch.uint8, device="cuda")
+    blobs = gc.generator_blobs(cfg["seed"], cfg["nblobs"], size, cfg["sigma"][0], cfg["sigma"][1], cfg["amp"][0],
+                               cfg["amp"][1])
+    t0 = time.perf_counter()
+    gc.generate_volume(gc.make_generator(size, cfg["bpc"], cfg["seed"], blobs, cfg["noise"], channels=nc, channel=0,
+                                         field=0), pyr.data_ptr())
+    for ch in range(1, nc):
+        gc.generate_volume(gc.make_generator(size, cfg["bpc"], cfg["seed"] + ch, blobs, cfg["noise"] * 4,
+                                             channels=nc, channel=ch, field=1), pyr.data_ptr())
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    gc.Mipmapper.process(pyr.data_ptr(), layout, poffs, eb, nc)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    level0 = size[0] * size[1] * size[2] * eb
+    pyramid_bytes = sum(layout.mip[l][0] * layout.mip[l][1] * layout.mip[l][2] * eb for l in range(layout.nb_levels))
+    pool = pool_slots(cfg)
+    cm = gc.CacheManager(vol, layout, pool, max_requests=args.max_requests, sync_loader=True)
+    cm.set_source_device(pyr.data_ptr(), poffs, keep=pyr)
+    tf = tf2d_table()
+    tfh, tfw = tf.shape[0], tf.shape[1]
+    tf_dev = torch.from_numpy(tf.reshape(-1).copy()).cuda()
+    W, H = cfg["W"], cfg["H"]
+    bufs = [torch.zeros(W * H * k, dtype=dt, device="cuda") for dt, k in ((torch.int32, 1), (torch.float32, 1),
+                                                                        (torch.float32, 4))]
+    focal = 1.0 / math.tan(math.radians(cfg["fov"]) / 2)
+    frames = [timed_views(cfg, nviews, 1)[i] for i in range(nviews)]
+    stream = torch.cuda.Stream()
+    lat, iters, conv = [], [], 0
+    s0 = cm.stats()
+    torch.cuda.synchronize()
+    a = time.perf_counter()
+    for f in frames:
+        v = gc.make_view(path_camera(gc.look_at, cfg, f), W, H, tf_dev.data_ptr(), tfw, *[b.data_ptr() for b in bufs],
+                         tstep=2.0 / 256.0, focal=focal, early_alpha=cfg["early"], tf_height=tfh)
+        b0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for b in bufs[1:]:
+                b.zero_()
+            it, ok = 0, False
+            while not ok and it < cfg["cap"]:
+                cm.render(v, stream.cuda_stream)
+                ok = cm.update(stream.cuda_stream)
+                it += 1
+        stream.synchronize()
+        lat.append(1e3 * (time.perf_counter() - b0))
+        iters.append(it)
+        conv += int(ok)
+    wall = time.perf_counter() - a
+    s1 = cm.stats()
+    cm.close()
+    del pyr
+    torch.cuda.empty_cache()
+    return {"workload": f"c5: 4096^3 x 2 u8 channels (128 GiB), B16, covering 2, big bricks 2^3, {list(pool)} pool "
+                        f"slots (8 GiB), {W}x{H} views {frames} of the {cfg['frames']}-view path through the interior, "
+                        f"2D transfer function, each to convergence (<= {cfg['cap']} iterations); bricks cut on "
+                        f"demand from the device-resident mip pyramid",
+            "value": round(W * H * len(frames) / wall / 1e6, 3), "unit": "Mrays/s",
+            "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+            "iterations_per_view": iters, "converged_views": f"{conv}/{len(frames)}",
+            "bricks_installed": int(s1.bricks_installed - s0.bricks_installed),
+            "brick_bytes_cut": int((s1.bricks_installed - s0.bricks_installed) * cfg["B"] ** 3 * eb),
+            "host_upload_bytes": int(s1.bytes_h2d - s0.bytes_h2d),
+            "generate_s": round(t1 - t0, 2),
+            "mip_build": {"s": round(t2 - t1, 4), "pyramid_gib": round(pyramid_bytes / 2**30, 1),
+                          "gbs": round((2 * pyramid_bytes - level0) / (t2 - t1) / 1e9, 1),
+                          "note": "every level read once and every coarser level written, over the build time"}}
+
+
+def run_c5(args):
+    """`--config c5`: the stress leg alone, printed as its own line."""
+    import torch
+
+    import gcgb300 as gc
+
+    gc.render_precision(gc.RENDER_FAST if args.precision == "fast" else gc.RENDER_EXACT)
+    r = run_stress(gc, torch, args, nviews=args.steps)
+    print(json.dumps({"metric": "Mrays/s", "value": r.get("value"), "unit": "Mrays/s", "n_gpus": 1,
+                      "steps": args.steps, "warmup": 0, "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "u8x2", "data": "synthetic (seeded blob field + noise field)",
+                      "config": {"workload": r.get("workload")}, "stress": r}), flush=True)
 
 
 def run_c4(args):
@@ -1118,6 +1250,45 @@ def reference_gpu_baseline(gc, torch, args, views=12):
     ref_frames = run_ref()
     ref_s = time.perf_counter() - a
     ref.close()
+    # mip-pyramid build: the reference's Mipmapper (file in, 512 MB chunks through
+    # the device, files out) vs the device pyramid build, on a 512^3 x 2-channel
+    # u8 volume (the c5 voxel type)
+    msize = (512, 512, 512)
+    mvol = gc.volume_desc(msize, 16, 2, 2, 2, (2, 2, 2))
+    mlayout = gc.compute_layout(mvol)
+    mblobs = gc.generator_blobs(5, 8, msize, 10.0, 75.0, 60, 200)
+    mpoffs, mtotal = gc.pyramid_offsets(mlayout, 2)
+    mpyr = torch.empty(mtotal, dtype=torch.uint8, device="cuda")
+    gc.generate_volume(gc.make_generator(msize, 1, 5, mblobs, 20, channels=2, channel=0, field=0), mpyr.data_ptr())
+    gc.generate_volume(gc.make_generator(msize, 1, 6, mblobs, 80, channels=2, channel=1, field=1), mpyr.data_ptr())
+    torch.cuda.synchronize()
+    raw = mpyr[: msize[0] * msize[1] * msize[2] * 2].cpu().numpy()
+    mdir = tempfile.mkdtemp(prefix="refmip_")
+    mref = refgpu.RefGpu(mdir, msize, 16, 2, 2, big_brick=(2, 2, 2), channels=2)
+    mref.write_volume(raw)
+    a = time.perf_counter()
+    mref.mipmap()
+    ref_mip_s = time.perf_counter() - a
+    gc.Mipmapper.process(mpyr.data_ptr(), mlayout, mpoffs, 2, 2)  # warm
+    torch.cuda.synchronize()
+    a = time.perf_counter()
+    gc.Mipmapper.process(mpyr.data_ptr(), mlayout, mpoffs, 2, 2)
+    torch.cuda.synchronize()
+    our_mip_s = time.perf_counter() - a
+    mdims = [tuple(mlayout.mip[l]) for l in range(mlayout.nb_levels)]
+    mbytes = sum(d[0] * d[1] * d[2] * 2 for d in mdims)
+    same = all(np.array_equal(mref.mip_level(l, d).view(np.uint8),
+                              mpyr[mpoffs[l]: mpoffs[l] + d[0] * d[1] * d[2] * 2].cpu().numpy())
+               for l, d in enumerate(mdims) if l > 0)
+    shutil.rmtree(mdir, ignore_errors=True)
+    mip = {"volume": "512^3 x 2 u8 channels", "pyramid_bytes": int(mbytes), "levels_identical": bool(same),
+           "reference_s": round(ref_mip_s, 4), "ours_s": round(our_mip_s, 5),
+           "reference_gbs": round((2 * mbytes - raw.nbytes) / ref_mip_s / 1e9, 2),
+           "ours_gbs": round((2 * mbytes - raw.nbytes) / our_mip_s / 1e9, 1),
+           "what": "the reference's Mipmapper::process (reads the level file, 512 MB chunks through the device, "
+                   "writes the level files) vs gc_mip_build on the device-resident volume; bytes = every level read "
+                   "once + every coarser level written"}
+    del mpyr
     ours_frames, ours_s = run_ours(50)
     ours8k_frames, ours8k_s = run_ours(args.max_requests)
     rays = W * H * views
@@ -1133,7 +1304,7 @@ def reference_gpu_baseline(gc, torch, args, views=12):
                                    "ms_per_frame": round(1e3 * ours_s / ours_frames, 3)},
             "ours_max_requests": {"value": round(rays / ours8k_s / 1e6, 3), "unit": "Mrays/s",
                                   "frames": ours8k_frames, "max_requests": args.max_requests},
-            "ratio_same_requests": round(ref_s / ours_s, 2)}
+            "ratio_same_requests": round(ref_s / ours_s, 2), "mip_build": mip}
 
 
 def vol_bytes_per_voxel(cfg):
@@ -1324,10 +1495,11 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default="c2",
+    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5", "c5_host"], default="c2",
                     help="c2: the plain out-of-core line (+ the c3 batched object); c1: small in-core plain case; "
                          "c3: the batched form alone; c4: serving (three volumes, shared pool, Poisson requests); "
-                         "c5: two-channel 2D-TF stress (plain loop)")
+                         "c5: two-channel 2D-TF stress at 4096^3 from the device-resident pyramid; "
+                         "c5_host: the same at 2048^3 from a host brick store (plain loop)")
     ap.add_argument("--rate", type=float, default=200.0, help="c4: request arrivals per second")
     ap.add_argument("--duration", type=float, default=6.0, help="c4: seconds of arrivals")
     ap.add_argument("--max-requests", type=int, default=8192)
@@ -1360,6 +1532,8 @@ def main():
                     help="ray-caster build: exact (the FP32 oracle's operations, bit for bit) or fast (FMA "
                          "contraction, rsqrtf, hardware log2/exp2; validated against the FP64 oracle and the "
                          "reference's ray caster)")
+    ap.add_argument("--no-stress", action="store_true",
+                    help="skip the c5 stress leg (4096^3 x 2 channels) of the default run")
     ap.add_argument("--no-serving", action="store_true",
                     help="skip the serving (c4) rate sweep of the default run")
     ap.add_argument("--no-reference-gpu", action="store_true",
@@ -1376,6 +1550,7 @@ def main():
     if args.config != "c2":
         args.no_batched = True
         args.no_serving = True
+        args.no_stress = True
     if args.impl == "reference" and args.config in ("c3", "c4"):
         print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm covers the plain configs "
                                                               "(c1, c2); c3 is the batched form"}), flush=True)
@@ -1385,6 +1560,8 @@ def main():
         run_c3(args)
     elif args.config == "c4":
         run_c4(args)
+    elif args.config == "c5":
+        run_c5(args)
     else:
         run_ours(args)
 

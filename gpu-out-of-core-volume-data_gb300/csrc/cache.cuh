@@ -109,6 +109,37 @@ struct ViewParams {
                                         // later passes skip its pixel (rgba already final)
 };
 
+// The bricking rule of one level (Bricker_v2.cpp:79-252): the level bricker
+// (gc_bricks_build) and the on-demand cut of the device-levels brick source.
+struct BrickParams {
+    uint32_t D[3];        // level size (voxels)
+    uint32_t B, c, Beff;
+    uint32_t BB[3];
+    uint32_t nbig[3];     // big bricks per axis
+    uint32_t eb;
+    uint64_t nsmall;      // small bricks in the level
+    uint32_t fast;        // 16-byte rows: B a power of two, B*eb and D[0]*eb multiples of 16, buffers 16-byte aligned
+    uint32_t b_shift;     // log2(B) (fast path: B a power of two)
+    uint32_t cpr_shift;   // log2(16-byte chunks per brick row)
+};
+
+// A device-resident mip pyramid as a volume's brick source: a missing big
+// brick is cut from its level with the bricker's rule into the staging slot
+// the install reads (gc_cache_set_volume_source_device).
+struct CutSource {
+    const uint8_t *pyramid = nullptr;
+    uint64_t offset[GC_MAX_LEVELS] = {};    // byte offset of each level
+    uint32_t dims[GC_MAX_LEVELS][3] = {};   // level sizes
+    uint32_t fast[GC_MAX_LEVELS] = {};      // the 16-byte path applies to the level
+    BrickParams p = {};                     // B, c, Beff, BB, eb, shifts
+};
+struct CutSources {
+    CutSource vol[4];
+};
+// Cut jobs: {x, y, z, slot << 8 | volume << 6 | level} big bricks.
+void launch_cut_bricks(const CutSources &srcs, const uint4 *jobs, uint32_t n, uint8_t *staging, uint64_t stride,
+                       cudaStream_t s);
+
 // Scan control block shared by the decoupled look-back kernels.
 struct ScanCtl {
     uint32_t ticket;

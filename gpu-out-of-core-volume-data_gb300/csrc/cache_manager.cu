@@ -70,7 +70,7 @@ __global__ void init_slots_kernel(uint32_t *order, uint32_t *level, float4 *vpos
 }
 
 struct Source {
-    int kind = 0;  // 0 none, 1 host store, 2 callback, 3 brick files
+    int kind = 0;  // 0 none, 1 host store, 2 callback, 3 brick files, 5 device-resident pyramid
     std::string dir;       // brick files: the volume directory (with '/')
     uint32_t threads = 0;  // brick files: reader threads
     const uint8_t *host = nullptr;
@@ -130,6 +130,8 @@ struct gc_cache {
     uint32_t *d_big_index = nullptr;
     ulonglong2 *d_src = nullptr;      // gather list: {host address, bytes} per big brick
     uint8_t *d_staging = nullptr;
+    gc::CutSources cut;               // device-resident pyramids of the volumes that have one
+    uint4 *d_cut = nullptr, *h_cut = nullptr;  // cut jobs of a load cycle (device-levels sources)
     gc::ViewParams *d_views = nullptr;
     uint32_t max_views = 256;
     // pinned host buffers
@@ -228,6 +230,7 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     std::vector<FileRead> reads;
     uint32_t read_threads = 1;
     uint64_t bytes_up = 0;
+    uint32_t ncut = 0, nhost = 0;  // big bricks cut on the device / taken from host sources
     for (uint32_t i = 0; i < n; ++i) {
         const uint4 b = C->lists[C->cur_load].h[i];  // (x, y, z, cache level)
         const Volume &V = C->vols[C->level_volume[b.w < C->lt.nlevels ? b.w : 0]];
@@ -249,6 +252,7 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
             continue;
         }
         int status = GC_BRICK_UNKNOWN;
+        bool on_device = false;
         const Source &src = V.src;
         uint8_t *stage = C->h_staging + static_cast<uint64_t>(nbig) * C->big_stride;
         if (src.empty.count(gc_brick_key(lvl, gx, gy, gz))) {  // the volume's own brick keys
@@ -268,6 +272,16 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
             }
         } else if (src.kind == 2) {
             status = src.fn(src.user, lvl, gx, gy, gz, stage, V.big_bytes);
+        } else if (src.kind == 5) {
+            const gc_layout &L = V.layout;
+            if (lvl < L.nb_levels && gx < L.nb_big_bricks[lvl][0] && gy < L.nb_big_bricks[lvl][1] &&
+                gz < L.nb_big_bricks[lvl][2]) {
+                const uint32_t vol = C->level_volume[b.w];
+                C->h_cut[ncut++] = make_uint4(gx, gy, gz, (nbig << 8) | (vol << 6) | lvl);
+                if (C->gather) C->h_src[nbig] = make_ulonglong2(0, 0);  // nothing to gather for this slot
+                on_device = true;
+                status = GC_BRICK_SUCCESS;
+            }
         } else if (src.kind == 3) {
             std::string p = brick_file_path(src.dir, V.desc.brick_size, lvl, gx, gy, gz);
             struct stat st;
@@ -278,7 +292,10 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
             }
         }
         if (status == GC_BRICK_SUCCESS) {
-            bytes_up += V.big_bytes;
+            if (!on_device) {
+                bytes_up += V.big_bytes;
+                ++nhost;
+            }
             asked[key] = static_cast<int32_t>(nbig);
             C->h_big_coord[nbig] = make_uint4(gx, gy, gz, b.w);
             big_index.push_back(nbig);
@@ -356,12 +373,16 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     const bool gather = C->gather;
     cudaStream_t s = C->sync_mode() && gather ? C->frame_stream : C->side;
     GC_CUDA(cudaEventRecord(C->ev_upload_begin, s));
-    if (nbig && gather) {
+    if (nhost && gather) {
         GC_CUDA(cudaMemcpyAsync(C->d_src, C->h_src, nbig * sizeof(ulonglong2), cudaMemcpyHostToDevice, s));
         launch_gather_bricks(C->d_src, nbig, C->big_stride, C->d_staging, C->vec16, !C->sync_mode(), s);
-    } else if (nbig) {
+    } else if (nhost) {
         GC_CUDA(cudaMemcpyAsync(C->d_staging, C->h_staging, static_cast<size_t>(nbig) * C->big_stride,
                                 cudaMemcpyHostToDevice, s));
+    }
+    if (ncut) {  // after the host bricks: a staged copy covers every slot
+        GC_CUDA(cudaMemcpyAsync(C->d_cut, C->h_cut, ncut * sizeof(uint4), cudaMemcpyHostToDevice, s));
+        launch_cut_bricks(C->cut, C->d_cut, ncut, C->d_staging, C->big_stride, s);
     }
     GC_CUDA(cudaMemcpyAsync(C->d_asked, C->h_asked, k * sizeof(uint4), cudaMemcpyHostToDevice, s));
     if (n_nonempty) {
@@ -569,11 +590,11 @@ static void destroy(gc_cache *C) {
     void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool, C->slot_bins, C->entry_bins, C->user_bins, C->d_samples,
                    C->status_lru, C->status_miss, C->ctl_lru, C->ctl_miss, C->d_count, C->d_misc, C->d_queue,
                    C->lists[0].d, C->lists[1].d, C->d_asked, C->d_owner, C->d_coords, C->d_big_coord, C->d_big_index, C->d_src,
-                   C->d_staging, C->d_views};
+                   C->d_staging, C->d_views, C->d_cut};
     for (void *p : dev)
         if (p) cudaFree(p);
     void *host[] = {C->lists[0].h, C->lists[1].h, C->lists[0].total, C->lists[1].total, C->h_asked, C->h_big_coord,
-                    C->h_big_index, C->h_misc, C->h_src, C->h_staging};
+                    C->h_big_index, C->h_misc, C->h_src, C->h_staging, C->h_cut};
     for (void *p : host)
         if (p) cudaFreeHost(p);
     for (auto &L : C->lists)
@@ -1011,6 +1032,57 @@ int gc_cache_set_volume_source_host(gc_cache_t C, uint32_t volume, const void *b
         src.direct = direct;
         src.dev = dev;
         src.vec16 = aligned && reinterpret_cast<uintptr_t>(dev) % 16 == 0;
+        src.level_off.assign(level_offsets, level_offsets + L.nb_levels);
+        for (size_t i = 0; i < n_empty; ++i) src.empty.insert(empty_keys[i]);
+        update_upload_route(C);
+        C->entry_bins_dirty = true;
+    });
+}
+
+int gc_cache_set_volume_source_device(gc_cache_t C, uint32_t volume, const void *pyramid,
+                                      const uint64_t *level_offsets, const uint64_t *empty_keys, size_t n_empty) {
+    return guard([&] {
+        GC_REQUIRE(C && pyramid && level_offsets && (empty_keys || n_empty == 0), "null argument");
+        GC_REQUIRE(volume < C->vols.size(), "no such volume in this cache");
+        GC_CUDA(cudaSetDevice(C->device));
+        cudaPointerAttributes at;
+        GC_CUDA(cudaPointerGetAttributes(&at, pyramid));
+        GC_REQUIRE(at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged,
+                   "the pyramid must be device memory");
+        const Volume &V = C->vols[volume];
+        const gc_layout &L = V.layout;
+        CutSource cs;
+        cs.pyramid = static_cast<const uint8_t *>(pyramid);
+        BrickParams &p = cs.p;
+        p.B = V.desc.brick_size;
+        p.c = V.desc.covering;
+        p.Beff = p.B - 2 * p.c;
+        for (int a = 0; a < 3; ++a) p.BB[a] = V.desc.big_brick_size[a];
+        p.eb = V.desc.encoded_bytes;
+        while ((1u << p.b_shift) < p.B) ++p.b_shift;
+        const bool pow2 = (p.B & (p.B - 1)) == 0;
+        while (pow2 && (16u << p.cpr_shift) < p.B * p.eb) ++p.cpr_shift;
+        for (uint32_t l = 0; l < L.nb_levels; ++l) {
+            GC_REQUIRE(L.mip[l][0] == L.initial[l][0] && L.mip[l][1] == L.initial[l][1] &&
+                           L.mip[l][2] == L.initial[l][2],
+                       "the pyramid's level sizes differ from the metadata sizes");
+            cs.offset[l] = level_offsets[l];
+            for (int a = 0; a < 3; ++a) cs.dims[l][a] = L.mip[l][a];
+            cs.fast[l] = (p.eb == 1 || p.eb == 2 || p.eb == 4) && pow2 && (p.B * p.eb) % 16 == 0 &&
+                         (static_cast<uint64_t>(L.mip[l][0]) * p.eb) % 16 == 0 &&
+                         (reinterpret_cast<uintptr_t>(pyramid) + level_offsets[l]) % 16 == 0 &&
+                         C->big_stride % 16 == 0;
+        }
+        std::lock_guard<std::mutex> g(C->mu);
+        GC_REQUIRE(!C->busy, "the loader is busy");
+        if (!C->d_cut) {
+            C->d_cut = dalloc<uint4>(C->d.max_requests, "cut jobs");
+            GC_CUDA(cudaMallocHost(reinterpret_cast<void **>(&C->h_cut), C->d.max_requests * sizeof(uint4)));
+        }
+        C->cut.vol[volume] = cs;
+        Source &src = C->vols[volume].src;
+        src = Source();
+        src.kind = 5;
         src.level_off.assign(level_offsets, level_offsets + L.nb_levels);
         for (size_t i = 0; i < n_empty; ++i) src.empty.insert(empty_keys[i]);
         update_upload_route(C);

@@ -6,6 +6,7 @@
 // (GcCore/src/libPreprocessor/Bricker_v2.cpp:79-252).
 #include <cstring>
 
+#include "cache.cuh"
 #include "gc_internal.h"
 
 namespace gc {
@@ -194,17 +195,6 @@ static void launch_mip(const void *src, void *dst, const uint32_t d[3], uint32_t
 // b * (B - 2c) is outside the level on some axis.  Output layout: big bricks in (z, y, x)
 // raster order, each (BB*B)^3 voxels x-fastest; small brick (i, j, k) of a big
 // brick at voxel offset (i*B, j*B, k*B) (Bricker_v2.cpp:149-152, 295-299).
-struct BrickParams {
-    uint32_t D[3];
-    uint32_t B, c, Beff;
-    uint32_t BB[3];
-    uint32_t nbig[3];     // big bricks per axis
-    uint32_t eb;
-    uint64_t nsmall;      // small bricks in the level
-    uint32_t fast;        // 16-byte rows: B*eb and D[0]*eb multiples of 16, level and out 16-byte aligned
-    uint32_t b_shift;     // log2(B) (fast path: B a power of two)
-    uint32_t cpr_shift;   // log2(16-byte chunks per brick row)
-};
 
 // One voxel of a small brick the slow way (bricks on the level's edge, odd
 // voxel widths): zero outside the level or in an unvisited brick.
@@ -248,22 +238,110 @@ __device__ __forceinline__ uint4 row_bytes16(uint4 a, uint4 b, uint32_t s) {
     return make_uint4(o[0], o[1], o[2], o[3]);
 }
 
-// One warp per small brick (grid-stride over bricks), the brick copied in
-// 16-byte output chunks (p.fast: B a power of two, whole chunks per row, rows
-// 16 bytes apart in the level).  A chunk whose source row lies inside the
-// level and whose voxels all lie inside the row -- all chunks of an interior
-// brick -- starts at the same byte offset s modulo 16 as every other such
-// chunk of the brick, so it is two aligned 16-byte loads and a funnel shift by
-// s, stored with one 16-byte store.  A row outside the level, or an unvisited
-// brick, stores zeros; a chunk straddling the level's x edge is assembled
-// voxel by voxel.  Odd voxel widths and unaligned buffers take the per-voxel
-// path throughout.  The per-brick index arithmetic is done once per warp and
-// brick (16 chunks per lane for B16 u16), the per-chunk one with shifts.
-__global__ void __launch_bounds__(256) brick_kernel(const uint8_t *__restrict__ level,
-                                                    uint8_t *__restrict__ out, BrickParams p) {
+// Copies small brick (sx, sy, sz) of a level into its place in a big brick
+// (big_base; (ix, iy, iz) = its position among the big brick's BB bricks),
+// with the 32 lanes of a warp.  p.fast (B a power of two, whole 16-byte
+// chunks per row, rows 16 bytes apart in the level, 16-byte aligned buffers):
+// the brick goes in 16-byte output chunks.  A chunk whose source row lies
+// inside the level and whose voxels all lie inside the row -- all chunks of an
+// interior brick -- starts at the same byte offset s modulo 16 as every other
+// such chunk of the brick, so it is two aligned 16-byte loads and a funnel
+// shift by s, stored with one 16-byte store.  A row outside the level, or an
+// unvisited brick, stores zeros; a chunk straddling the level's x edge is
+// assembled voxel by voxel.  Otherwise the brick is copied voxel by voxel.
+__device__ __forceinline__ void copy_small_brick(const uint8_t *__restrict__ level, const BrickParams &p,
+                                                 uint32_t sx, uint32_t sy, uint32_t sz, uint8_t *big_base,
+                                                 uint32_t ix, uint32_t iy, uint32_t iz, uint32_t lane) {
     const uint32_t B = p.B;
     const uint32_t bvx = p.BB[0] * B, bvy = p.BB[1] * B;
-    const uint64_t big_bytes = static_cast<uint64_t>(bvx) * bvy * (p.BB[2] * B) * p.eb;
+    const int64_t ox = static_cast<int64_t>(sx) * p.Beff - p.c;
+    const int64_t oy = static_cast<int64_t>(sy) * p.Beff - p.c;
+    const int64_t oz = static_cast<int64_t>(sz) * p.Beff - p.c;
+    // The reference visits a small brick only if its start lies inside the
+    // level on every axis (Bricker_v2.cpp:203-221); the others stay zero even
+    // where their covering border reaches into the volume.
+    const bool visited = static_cast<uint64_t>(sx) * p.Beff < p.D[0] &&
+                         static_cast<uint64_t>(sy) * p.Beff < p.D[1] && static_cast<uint64_t>(sz) * p.Beff < p.D[2];
+    if (p.fast) {
+        const uint32_t k = 16u / p.eb;                  // voxels per chunk
+        const uint32_t nchunks = 1u << (2u * p.b_shift + p.cpr_shift);
+        const uint64_t row_stride = static_cast<uint64_t>(p.D[0]) * p.eb;
+        // byte offset modulo 16 of the brick's first voxel in any row (rows
+        // are multiples of 16 bytes apart; ox may be negative)
+        const uint32_t s = static_cast<uint32_t>(ox * static_cast<int64_t>(p.eb)) & 15u;
+        uint8_t *obase = big_base + ((static_cast<uint64_t>(iz) * B * bvy + iy * B) * bvx + ix * B) * p.eb;
+        const uint64_t drow = static_cast<uint64_t>(bvx) * p.eb;  // output row stride
+        if (visited && ox >= 0 && oy >= 0 && oz >= 0 && ox + B <= p.D[0] && oy + B <= p.D[1] && oz + B <= p.D[2]) {
+            // Interior brick (the common case, the same branch for the whole
+            // warp): no per-chunk tests; each lane issues the loads of 4 chunks
+            // before it stores them.  The second load of a pair ends at or
+            // before the end of its row: the chunk's first voxel byte plus 16
+            // lies inside the row, and rows end on 16-byte boundaries.
+            const uint8_t *sbase = level + (static_cast<uint64_t>(oz) * p.D[1] + static_cast<uint64_t>(oy)) * row_stride +
+                                   static_cast<uint64_t>(ox) * p.eb - s;
+            const uint32_t cmask = (1u << p.cpr_shift) - 1u;
+            for (uint32_t c0 = lane; c0 < nchunks; c0 += 128u) {
+                uint4 a[4], b[4] = {};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const uint32_t c = c0 + 32u * u;
+                    if (c < nchunks) {
+                        const uint32_t row = c >> p.cpr_shift;
+                        const uint8_t *src = sbase + (static_cast<uint64_t>(row >> p.b_shift) * p.D[1] + (row & (B - 1u))) *
+                                                         row_stride + (c & cmask) * 16u;
+                        a[u] = __ldg(reinterpret_cast<const uint4 *>(src));
+                        if (s) b[u] = __ldg(reinterpret_cast<const uint4 *>(src + 16));
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const uint32_t c = c0 + 32u * u;
+                    if (c < nchunks) {
+                        const uint32_t row = c >> p.cpr_shift;
+                        uint8_t *dst = obase + (static_cast<uint64_t>(row >> p.b_shift) * bvy + (row & (B - 1u))) * drow +
+                                       (c & cmask) * 16u;
+                        *reinterpret_cast<uint4 *>(dst) = s ? row_bytes16(a[u], b[u], s) : a[u];
+                    }
+                }
+            }
+            return;
+        }
+#pragma unroll 4
+        for (uint32_t c = lane; c < nchunks; c += 32u) {
+            const uint32_t cx = c & ((1u << p.cpr_shift) - 1u), row = c >> p.cpr_shift;
+            const uint32_t ly = row & (B - 1u), lz = row >> p.b_shift;
+            uint8_t *dst = obase + (static_cast<uint64_t>(lz) * bvy + ly) * drow + cx * 16u;
+            const int64_t ry = oy + ly, rz = oz + lz, x0 = ox + static_cast<int64_t>(cx) * k;
+            const bool row_in = visited && ry >= 0 && rz >= 0 && ry < p.D[1] && rz < p.D[2];
+            if (!row_in) {
+                *reinterpret_cast<uint4 *>(dst) = make_uint4(0u, 0u, 0u, 0u);
+            } else if (x0 >= 0 && x0 + k <= p.D[0]) {
+                const uint64_t src = (static_cast<uint64_t>(rz) * p.D[1] + ry) * row_stride +
+                                     static_cast<uint64_t>(x0) * p.eb - s;
+                const uint4 a = __ldg(reinterpret_cast<const uint4 *>(level + src));
+                *reinterpret_cast<uint4 *>(dst) =
+                    s ? row_bytes16(a, __ldg(reinterpret_cast<const uint4 *>(level + src + 16)), s) : a;
+            } else {
+                for (uint32_t v = 0; v < k; ++v)
+                    brick_voxel(level, dst + v * p.eb, p, true, x0 + v, ry, rz);
+            }
+        }
+        return;
+    }
+    const uint32_t nvox = B * B * B;
+    for (uint32_t v = lane; v < nvox; v += 32u) {
+        const uint32_t lx = v % B, ly = (v / B) % B, lz = v / (B * B);
+        uint8_t *dptr = big_base + ((static_cast<uint64_t>(iz * B + lz) * bvy + (iy * B + ly)) * bvx + (ix * B + lx)) * p.eb;
+        brick_voxel(level, dptr, p, visited, ox + lx, oy + ly, oz + lz);
+    }
+}
+
+// The bricker of one level: one warp per small brick (grid-stride over
+// bricks); the per-brick index arithmetic is done once per warp and brick
+// (16 chunks per lane for B16 u16), the per-chunk one with shifts.
+__global__ void __launch_bounds__(256) brick_kernel(const uint8_t *__restrict__ level,
+                                                    uint8_t *__restrict__ out, BrickParams p) {
+    const uint64_t big_bytes = static_cast<uint64_t>(p.BB[0] * p.B) * (p.BB[1] * p.B) * (p.BB[2] * p.B) * p.eb;
     const uint32_t nsx = p.nbig[0] * p.BB[0], nsy = p.nbig[1] * p.BB[1];
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -273,55 +351,44 @@ __global__ void __launch_bounds__(256) brick_kernel(const uint8_t *__restrict__ 
         const uint32_t sx = sb % nsx, rest = sb / nsx;
         const uint32_t sy = rest % nsy, sz = rest / nsy;
         const uint32_t gx = sx / p.BB[0], gy = sy / p.BB[1], gz = sz / p.BB[2];
-        const uint32_t ix = sx - gx * p.BB[0], iy = sy - gy * p.BB[1], iz = sz - gz * p.BB[2];
         const uint64_t big = (static_cast<uint64_t>(gz) * p.nbig[1] + gy) * p.nbig[0] + gx;
-        uint8_t *bbase = out + big * big_bytes;
-        const int64_t ox = static_cast<int64_t>(sx) * p.Beff - p.c;
-        const int64_t oy = static_cast<int64_t>(sy) * p.Beff - p.c;
-        const int64_t oz = static_cast<int64_t>(sz) * p.Beff - p.c;
-        // The reference visits a small brick only if its start lies inside the
-        // level on every axis (Bricker_v2.cpp:203-221); the others stay zero even
-        // where their covering border reaches into the volume.
-        const bool visited = static_cast<uint64_t>(sx) * p.Beff < p.D[0] &&
-                             static_cast<uint64_t>(sy) * p.Beff < p.D[1] && static_cast<uint64_t>(sz) * p.Beff < p.D[2];
-        if (p.fast) {
-            const uint32_t k = 16u / p.eb;                  // voxels per chunk
-            const uint32_t nchunks = 1u << (2u * p.b_shift + p.cpr_shift);
-            const uint64_t row_stride = static_cast<uint64_t>(p.D[0]) * p.eb;
-            // byte offset modulo 16 of the brick's first voxel in any row (rows
-            // are multiples of 16 bytes apart; ox may be negative)
-            const uint32_t s = static_cast<uint32_t>(ox * static_cast<int64_t>(p.eb)) & 15u;
-            uint8_t *obase = bbase + ((static_cast<uint64_t>(iz) * B * bvy + iy * B) * bvx + ix * B) * p.eb;
-            const uint64_t drow = static_cast<uint64_t>(bvx) * p.eb;  // output row stride
-#pragma unroll 4
-            for (uint32_t c = lane; c < nchunks; c += 32u) {
-                const uint32_t cx = c & ((1u << p.cpr_shift) - 1u), row = c >> p.cpr_shift;
-                const uint32_t ly = row & (B - 1u), lz = row >> p.b_shift;
-                uint8_t *dst = obase + (static_cast<uint64_t>(lz) * bvy + ly) * drow + cx * 16u;
-                const int64_t ry = oy + ly, rz = oz + lz, x0 = ox + static_cast<int64_t>(cx) * k;
-                const bool row_in = visited && ry >= 0 && rz >= 0 && ry < p.D[1] && rz < p.D[2];
-                if (!row_in) {
-                    *reinterpret_cast<uint4 *>(dst) = make_uint4(0u, 0u, 0u, 0u);
-                } else if (x0 >= 0 && x0 + k <= p.D[0]) {
-                    const uint64_t src = (static_cast<uint64_t>(rz) * p.D[1] + ry) * row_stride +
-                                         static_cast<uint64_t>(x0) * p.eb - s;
-                    const uint4 a = __ldg(reinterpret_cast<const uint4 *>(level + src));
-                    *reinterpret_cast<uint4 *>(dst) =
-                        s ? row_bytes16(a, __ldg(reinterpret_cast<const uint4 *>(level + src + 16)), s) : a;
-                } else {
-                    for (uint32_t v = 0; v < k; ++v)
-                        brick_voxel(level, dst + v * p.eb, p, true, x0 + v, ry, rz);
-                }
-            }
-            continue;
-        }
-        const uint32_t nvox = B * B * B;
-        for (uint32_t v = lane; v < nvox; v += 32u) {
-            const uint32_t lx = v % B, ly = (v / B) % B, lz = v / (B * B);
-            uint8_t *dptr = bbase + ((static_cast<uint64_t>(iz * B + lz) * bvy + (iy * B + ly)) * bvx + (ix * B + lx)) * p.eb;
-            brick_voxel(level, dptr, p, visited, ox + lx, oy + ly, oz + lz);
+        copy_small_brick(level, p, sx, sy, sz, out + big * big_bytes, sx - gx * p.BB[0], sy - gy * p.BB[1],
+                         sz - gz * p.BB[2], lane);
+    }
+}
+
+// Bricks cut on demand from a device-resident pyramid (the device-levels
+// brick source): job j = big brick (x, y, z) of level `lvl` of volume `vol`
+// into staging slot `slot`; one block per job, its warps over the job's small
+// bricks, each by the level bricker's rule.
+__global__ void __launch_bounds__(256) cut_bricks_kernel(const CutSources srcs, const uint4 *__restrict__ jobs,
+                                                         uint32_t n, uint8_t *__restrict__ staging,
+                                                         uint64_t stride) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (uint32_t j = blockIdx.x; j < n; j += gridDim.x) {
+        const uint4 job = jobs[j];
+        const uint32_t lvl = job.w & 63u, vol = (job.w >> 6) & 3u, slot = job.w >> 8;
+        const CutSource &cs = srcs.vol[vol];
+        BrickParams p = cs.p;
+        for (int a = 0; a < 3; ++a) p.D[a] = cs.dims[lvl][a];
+        p.fast = cs.fast[lvl];
+        const uint32_t nsub = p.BB[0] * p.BB[1] * p.BB[2];
+        for (uint32_t sub = warp; sub < nsub; sub += nw) {
+            const uint32_t ix = sub % p.BB[0], iy = (sub / p.BB[0]) % p.BB[1], iz = sub / (p.BB[0] * p.BB[1]);
+            copy_small_brick(cs.pyramid + cs.offset[lvl], p, job.x * p.BB[0] + ix, job.y * p.BB[1] + iy,
+                             job.z * p.BB[2] + iz, staging + static_cast<uint64_t>(slot) * stride, ix, iy, iz,
+                             lane);
         }
     }
+}
+
+void launch_cut_bricks(const CutSources &srcs, const uint4 *jobs, uint32_t n, uint8_t *staging, uint64_t stride,
+                       cudaStream_t s) {
+    if (n == 0) return;
+    cut_bricks_kernel<<<std::min<uint32_t>(n, static_cast<uint32_t>(sm_count()) * 8), 256, 0, s>>>(srcs, jobs, n,
+                                                                                                 staging, stride);
+    GC_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 // Empty flags: 1 if every channel value of the big brick is < threshold

@@ -141,6 +141,7 @@ _SIGS = {
     "gc_cache_set_source_host": [vp, vp, C.c_uint64, P(C.c_uint64), P(C.c_uint64), C.c_size_t],
     "gc_cache_set_source_callback": [vp, LOADER_FN, vp, P(C.c_uint64), C.c_size_t],
     "gc_cache_set_volume_source_host": [vp, C.c_uint32, vp, C.c_uint64, P(C.c_uint64), P(C.c_uint64), C.c_size_t],
+    "gc_cache_set_volume_source_device": [vp, C.c_uint32, vp, P(C.c_uint64), P(C.c_uint64), C.c_size_t],
     "gc_cache_set_volume_source_callback": [vp, C.c_uint32, LOADER_FN, vp, P(C.c_uint64), C.c_size_t],
     "gc_cache_create_shared": [P(CacheDesc), P(VolumeDesc), P(Layout), C.c_uint32, P(vp)],
     "gc_render_empty_skip": [C.c_int],
@@ -579,6 +580,15 @@ class CacheManager:
         keys = (C.c_uint64 * max(1, len(empty_keys)))(*[int(k) for k in empty_keys])
         self._keep.append((offs, keys, store))
         check(lib.gc_cache_set_volume_source_host(self._h, volume, vp(ptr), size, offs, keys, len(empty_keys)))
+
+    def set_source_device(self, pyramid_ptr, level_offsets, empty_keys=(), volume=0, keep=None):
+        """A device-resident mip pyramid (level l at byte offset level_offsets[l],
+        e.g. from Mipmapper.process) as the brick source: missing bricks are cut
+        from it on the device.  `keep`: an object holding the pyramid alive."""
+        offs = (C.c_uint64 * MAX_LEVELS)(*[int(o) for o in level_offsets])
+        keys = (C.c_uint64 * max(1, len(empty_keys)))(*[int(k) for k in empty_keys])
+        self._keep.append((offs, keys, keep))
+        check(lib.gc_cache_set_volume_source_device(self._h, volume, vp(pyramid_ptr), offs, keys, len(empty_keys)))
 
     def set_brick_bins(self, bins, volume=0):
         """Value bins of every brick of the volume (pre_process(value_bins=...)):

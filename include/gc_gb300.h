@@ -256,6 +256,19 @@ int gc_cache_set_volume_source_files(gc_cache_t cache, uint32_t volume, const ch
                                      const uint64_t *empty_keys, size_t n_empty, uint32_t threads);
 int gc_cache_set_volume_source_host(gc_cache_t cache, uint32_t volume, const void *bricks, uint64_t bytes,
                                     const uint64_t *level_offsets, const uint64_t *empty_keys, size_t n_empty);
+/* A device-resident mip pyramid as the brick source (an extension: the
+ * reference always loads bricks from storage).  `pyramid` is device memory
+ * holding every level of the volume, level l at byte offset level_offsets[l]
+ * (the layout gc_mip_build leaves: level 0 from the caller, the coarser
+ * levels computed on the device).  A missing big brick is cut from its level
+ * on the device, with the bricker's rule (process_bricking: covering border,
+ * zeros outside the level and in unvisited bricks), straight into the
+ * staging memory the install reads: no brick store and no host transfer.
+ * It suits volumes whose pyramid fits in device memory but whose bricked
+ * store does not fit the host (4096^3 x 2 channels: a 146 GiB pyramid, a
+ * 375 GB store).  The pyramid must outlive the cache. */
+int gc_cache_set_volume_source_device(gc_cache_t cache, uint32_t volume, const void *pyramid,
+                                      const uint64_t *level_offsets, const uint64_t *empty_keys, size_t n_empty);
 int gc_cache_set_volume_source_callback(gc_cache_t cache, uint32_t volume, gc_brick_loader_fn fn, void *user,
                                         const uint64_t *empty_keys, size_t n_empty);
 /* Brick value bins (an extension; the reference has none).  Bit b of a

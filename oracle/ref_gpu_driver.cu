@@ -416,6 +416,17 @@ int refgpu_preprocess(float empty_threshold) {
     });
 }
 
+// Mipmapper::process alone (Mipmapper.cu:401-525): the mip files of the
+// configured volume, for timing the reference's preprocessor.
+int refgpu_mipmap(void) {
+    return guarded([&] {
+        tdns::data::MetaData md;
+        tdns::preprocessor::Mipmapper mipmapper;
+        mipmapper.process(md);
+        if (md.get_initial_levels().empty()) throw std::runtime_error("Mipmapper::process produced no level");
+    });
+}
+
 // load_volume_configuration + MetaData::load + CacheManager<T> (Application::run,
 // Application.cu:43-133) with a pool of cache_size slots.
 int refgpu_open(const char *cfg_path, const uint32_t cache_size[3], int gpu) {

@@ -41,6 +41,7 @@ def load():
         u32p = C.POINTER(C.c_uint32)
         lib.refgpu_config_load.argtypes = [C.c_char_p]
         lib.refgpu_preprocess.argtypes = [C.c_float]
+        lib.refgpu_mipmap.argtypes = []
         lib.refgpu_open.argtypes = [C.c_char_p, u32p, C.c_int]
         lib.refgpu_render.argtypes = [C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.c_float,
                                       C.POINTER(C.c_float), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -74,7 +75,7 @@ class RefGpu:
     CacheManager.  workdir receives <workdir>/vol/vol.raw (the level-0
     voxels), the reference's mipmap/ files, brick files and bricks.xml."""
 
-    def __init__(self, workdir, size, brick_size, covering, encoded_bytes, big_brick=(1, 1, 1)):
+    def __init__(self, workdir, size, brick_size, covering, encoded_bytes, big_brick=(1, 1, 1), channels=1):
         self.lib = load()
         self.workdir = os.path.join(os.path.abspath(workdir), "")
         self.voldir = os.path.join(self.workdir, "vol", "")
@@ -85,7 +86,7 @@ class RefGpu:
         write_config(self.cfg, {
             "BrickSize": brick_size, "BigBrickSizeX": big_brick[0], "BigBrickSizeY": big_brick[1],
             "BigBrickSizeZ": big_brick[2], "VoxelCovering": covering, "NumberEncodedBytes": encoded_bytes,
-            "NumberChannels": 1, "size_X": size[0], "size_Y": size[1], "size_Z": size[2],
+            "NumberChannels": channels, "size_X": size[0], "size_Y": size[1], "size_Z": size[2],
             "downScale_X": 2, "downScale_Y": 2, "downScale_Z": 2,
             "WorkingDirectory": self.workdir, "VolumeFile": "vol.raw"})
         self.opened = False
@@ -97,6 +98,16 @@ class RefGpu:
             f.write(np.ascontiguousarray(level0_bytes).tobytes())
         _check(self.lib.refgpu_config_load(self.cfg.encode()))
         _check(self.lib.refgpu_preprocess(C.c_float(empty_threshold)))
+
+    def write_volume(self, level0_bytes):
+        """The level-0 voxels as the reference's volume file."""
+        with open(os.path.join(self.voldir, "vol.raw"), "wb") as f:
+            f.write(np.ascontiguousarray(level0_bytes).tobytes())
+
+    def mipmap(self):
+        """Mipmapper::process alone on the volume file (the mip files)."""
+        _check(self.lib.refgpu_config_load(self.cfg.encode()))
+        _check(self.lib.refgpu_mipmap())
 
     def mip_level(self, level, dims):
         dt = np.uint8 if self.eb == 1 else np.uint16

@@ -190,3 +190,64 @@ def test_unknown_bricks_stay_unmapped(gc, orc, torch_cuda):
     assert st.load_errors == sum(1 for c in calls if sum(c[1:]) % 3 == 0) > 0
     assert st.bricks_installed == len(calls) - st.load_errors
     assert int((mrpd[:, 3] == 1).sum()) == st.bricks_installed and st.device_error == 0
+
+
+@pytest.mark.parametrize("size,bpc,ch,B,c,bb", [
+    ((64, 64, 64), 1, 1, 16, 1, (1, 1, 1)),
+    ((96, 64, 80), 2, 1, 32, 2, (2, 1, 1)),
+    ((64, 48, 56), 1, 2, 16, 2, (2, 2, 2)),   # the c5 brick layout: two u8 channels, covering 2, big bricks 2^3
+    ((64, 64, 32), 1, 1, 16, 0, (1, 1, 1)),
+])
+def test_device_source_equals_host_store(gc, torch_cuda, size, bpc, ch, B, c, bb):
+    """gc_cache_set_volume_source_device: missing bricks cut on the device from
+    the resident pyramid give the same frames as the brick store the
+    bricker writes (gc_cache_set_source_host): every frame's image, and after
+    every update the LRU order, page directory and pool bytes, bit for bit."""
+    torch = torch_cuda
+    vol = gc.volume_desc(size, B, c, bpc * ch, ch, bb)
+    layout = gc.compute_layout(vol)
+    d = scenario.gpu_volume(gc, torch, size, bpc, 31, 5, channels=ch)
+    store, offs, empty = gc.pre_process(vol, layout, d, empty_threshold=30.0 * (257 if bpc == 2 else 1))
+    poffs, total = gc.pyramid_offsets(layout, vol.encoded_bytes)
+    pyr = torch.empty(total, dtype=torch.uint8, device="cuda")
+    pyr[: d.numel() * d.element_size()].copy_(d.view(torch.uint8))
+    gc.Mipmapper.process(pyr.data_ptr(), layout, poffs, vol.encoded_bytes, ch)
+    torch.cuda.synchronize()
+    caches = []
+    for kind in ("host", "device"):
+        cm = gc.CacheManager(vol, layout, (5, 5, 5), max_requests=60, sync_loader=True)
+        if kind == "host":
+            cm.set_source_host(store, offs, empty_keys=empty)
+        else:
+            cm.set_source_device(pyr.data_ptr(), poffs, empty_keys=empty, keep=pyr)
+        caches.append(cm)
+    W, H = 40, 32
+    tf = scenario.tf2d(3) if ch == 2 else scenario.ramp_tf()
+    tfh, tfw = (tf.shape[0], tf.shape[1]) if ch == 2 else (0, tf.shape[0])
+    tf_dev = torch.from_numpy(tf.reshape(-1).copy()).cuda()
+    bufs = [[torch.zeros(W * H * k, dtype=dt, device="cuda") for dt, k in ((torch.int32, 1), (torch.float32, 1),
+                                                                          (torch.float32, 4))] for _ in caches]
+    nslots = 125
+    for f in range(16):
+        m = scenario.orbit_camera(gc, f // 4, 8, 2.2 + 0.2 * (f // 4))
+        imgs = []
+        for cm, b in zip(caches, bufs):
+            if f % 4 == 0:
+                for x in b:
+                    x.zero_()
+            cm.render(gc.make_view(m, W, H, tf_dev.data_ptr(), tfw, *[x.data_ptr() for x in b], tf_height=tfh))
+            torch.cuda.synchronize()
+            imgs.append(b[0].cpu().numpy())
+        assert np.array_equal(imgs[0], imgs[1]), f"frame {f}: image"
+        assert caches[0].update() == caches[1].update(), f"frame {f}"
+        for what, dtype, n in ((gc.DUMP_LRU, np.uint8, nslots * 28), (gc.DUMP_MRPD, np.uint32, caches[0].info.mrpd_dims[0]
+                                                                      * caches[0].info.mrpd_dims[1]
+                                                                      * caches[0].info.mrpd_dims[2] * 4),
+                               (gc.DUMP_POOL, np.uint8, caches[0].info.pool_bytes)):
+            a, b2 = (cm.dump(what, np.zeros(n, dtype)) for cm in caches)
+            assert np.array_equal(a, b2), (f, what)
+    st = [cm.stats() for cm in caches]
+    assert st[1].bricks_installed == st[0].bricks_installed > 0
+    assert st[1].bytes_h2d == 0 and st[1].device_error == 0
+    for cm in caches:
+        cm.close()
