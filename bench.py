@@ -1087,6 +1087,7 @@ def c4_serve(gc, torch, cfg, vols, stores, args):
 SERVING_RATES = (25.0, 50.0, 100.0, 200.0)  # requests per second tried by the default run
 SERVING_SECONDS = 2.0
 SERVING_P99_MS = 1000.0  # a rate is sustained while the p99 latency stays below this
+SERVING_KEEP_UP = 0.95  # ... and the server keeps up with at least this share of the offered rays
 
 
 def run_serving_sweep(gc, torch, args):
@@ -1095,8 +1096,11 @@ def run_serving_sweep(gc, torch, args):
     SERVING_SECONDS, each on a fresh cache; per rate the served Mrays/s
     (rays of all requests over the time to the last retirement), p50/p99
     latency (arrival -> retirement) and upload GB/s, and the highest rate the
-    server sustains: every request converged with a p99 latency under
-    SERVING_P99_MS (no queue building up)."""
+    server sustains: it serves at least SERVING_KEEP_UP of the offered rays
+    per second with a p99 latency under SERVING_P99_MS (no queue building
+    up).  Requests that reach the pass cap without converging (a close view
+    whose working set the pool cannot hold) retire with their preview image
+    and are counted in `converged`."""
     global PIN_STORES
     pinned = PIN_STORES
     PIN_STORES = False
@@ -1109,8 +1113,8 @@ def run_serving_sweep(gc, torch, args):
         a.rate, a.duration = rate, SERVING_SECONDS
         r = c4_serve(gc, torch, cfg, vols, stores, a)
         offered = r["config"]["offered_mrays_per_s"]
-        done, total = (int(x) for x in r["converged"].split("/"))
-        ok = done == total and r["latency_ms"]["p99"] is not None and r["latency_ms"]["p99"] <= SERVING_P99_MS
+        ok = (r["value"] >= SERVING_KEEP_UP * offered and r["latency_ms"]["p99"] is not None
+              and r["latency_ms"]["p99"] <= SERVING_P99_MS)
         rates.append({"rate_per_s": rate, "requests": r["steps"], "offered_mrays_per_s": offered,
                       "served_mrays_per_s": r["value"], "latency_ms": r["latency_ms"], "converged": r["converged"],
                       "passes_per_request": r["passes_per_request"], "upload_gbs": r["cache"]["upload_gbs"],
@@ -1121,8 +1125,8 @@ def run_serving_sweep(gc, torch, args):
     return {"workload": f"c4: 1024^3 u8 + 2048^3 u16 + 4096x4096x2048 u8 (seeds 11-13) in one shared 24 GiB pool; "
                         f"Poisson requests over {SERVING_SECONDS} s per rate, random volume, camera (0.5-3.0x the "
                         f"diagonal), size {list(cfg['sizes'])} and one of 4 transfer functions; continuous batching",
-            "rates": rates, "sustained_rate_per_s": sustained, "sustained_means": f"all requests converged, p99 <= "
-                                                                                     f"{SERVING_P99_MS:.0f} ms",
+            "rates": rates, "sustained_rate_per_s": sustained,
+            "sustained_means": f"served >= {SERVING_KEEP_UP:.0%} of the offered Mrays/s, p99 <= {SERVING_P99_MS:.0f} ms",
             "sustained_p99_ms": next((x["latency_ms"]["p99"] for x in rates if x["rate_per_s"] == sustained), None),
             "preprocess_s": round(prep, 1), "stores": "pageable host memory (85 GiB)"}
 

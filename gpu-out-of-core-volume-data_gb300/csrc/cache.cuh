@@ -45,9 +45,10 @@ struct CacheView {
     uint32_t *usage;
     const uint8_t *pool;
     uint32_t mx, my, mz;
+    uint32_t mxy;         // mx * my (the page directory has fewer than 2^32 - 1 entries)
     uint32_t sx, sy, sz;
     uint32_t B, c, Beff;
-    uint32_t beff_magic;  // ceil(2^31 / Beff) for the exact multiply-shift modulo (0: use %)
+    uint32_t beff_magic;  // ceil(2^32 / Beff) for the exact multiply-high modulo (0: use %)
     uint32_t eb;          // bytes per voxel of every volume, 0 when the volumes differ
     uint32_t nc;          // channels per voxel (1, or 2 for two 8-bit channels)
     uint64_t slot_bytes;  // pool slot stride: B^3 x the widest voxel

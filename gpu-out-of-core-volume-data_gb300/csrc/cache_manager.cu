@@ -103,7 +103,7 @@ struct gc_cache {
     std::vector<uint32_t> level_volume;  // volume of each cache level
     gc::LevelTables lt;
     uint32_t mx = 0, my = 0, mz = 0, nslots = 0, B = 0, c = 0, Beff = 0;
-    uint32_t beff_magic = 0;          // ceil(2^31 / Beff) when every level has < 2^24 voxels per axis
+    uint32_t beff_magic = 0;          // ceil(2^32 / Beff) for 2 <= Beff <= 128
     uint32_t eb = 0;                  // voxel bytes of every volume, 0 when they differ
     uint32_t nc = 1;                  // channels per voxel (the same for every volume)
     uint64_t nentries = 0;
@@ -200,11 +200,17 @@ static void build_tables(gc_cache *C) {
     }
     lt.nlevels = l;
     C->mx = off;
-    // exact multiply-shift modulo by Beff for voxel coordinates below 2^24
-    bool small = C->Beff >= 1 && C->Beff <= 128;
+    // the ray caster's page walk: one 32-bit index per entry, float-to-integer
+    // floors exact below 2^23 voxels per axis
+    GC_REQUIRE(static_cast<uint64_t>(C->mx) * C->my * C->mz < 0xffffffffull,
+               "page directory too large (2^32 - 1 entries at most)");
     for (uint32_t k = 0; k < l; ++k)
-        for (int a = 0; a < 3; ++a) small = small && lt.vvox[k][a] < (1u << 24);
-    C->beff_magic = small ? static_cast<uint32_t>(((1ull << 31) + C->Beff - 1) / C->Beff) : 0u;
+        for (int a = 0; a < 3; ++a)
+            GC_REQUIRE(lt.vvox[k][a] < (1u << 23), "level sizes up to 2^23 voxels per axis are supported");
+    // exact multiply-high modulo by Beff (voxel coordinates below 2^25)
+    C->beff_magic = C->Beff >= 2 && C->Beff <= 128
+                        ? static_cast<uint32_t>(((1ull << 32) + C->Beff - 1) / C->Beff)
+                        : 0u;
 }
 
 // Resolve the asked bricks: RequestHandler::handle_request (RequestHandler.hpp:277-372).
@@ -453,6 +459,7 @@ static CacheView cache_view(const gc_cache *C) {
     cv.pool = C->pool;
     cv.mx = C->mx;
     cv.my = C->my;
+    cv.mxy = C->mx * C->my;
     cv.mz = C->mz;
     cv.sx = C->d.cache_size[0];
     cv.sy = C->d.cache_size[1];

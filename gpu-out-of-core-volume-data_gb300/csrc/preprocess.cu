@@ -357,6 +357,95 @@ __global__ void __launch_bounds__(256) brick_kernel(const uint8_t *__restrict__ 
     }
 }
 
+// Bytes [s, s + 16) of the 32-byte pair (a, b) for a per-lane s in 0..15: a
+// two-level select by whole words, then a funnel shift by the byte remainder.
+__device__ __forceinline__ uint4 window16(uint4 a, uint4 b, uint32_t s) {
+    const bool w2 = (s & 8u) != 0u, w1 = (s & 4u) != 0u;
+    const uint32_t u0 = w2 ? a.z : a.x, u1 = w2 ? a.w : a.y, u2 = w2 ? b.x : a.z, u3 = w2 ? b.y : a.w,
+                   u4 = w2 ? b.z : b.x, u5 = w2 ? b.w : b.y;
+    const uint32_t v0 = w1 ? u1 : u0, v1 = w1 ? u2 : u1, v2 = w1 ? u3 : u2, v3 = w1 ? u4 : u3, v4 = w1 ? u5 : u4;
+    const uint32_t r = (s & 3u) * 8u;
+    return make_uint4(__funnelshift_r(v0, v1, r), __funnelshift_r(v1, v2, r), __funnelshift_r(v2, v3, r),
+                      __funnelshift_r(v3, v4, r));
+}
+
+// Row-mapped bricker (p.fast and at most 32 16-byte chunks per brick row): a
+// warp takes a run of nb = 32 / cpr bricks adjacent along x (one (sy, sz)
+// brick row), lane q holding chunk q % cpr of brick q / cpr, and walks the
+// B x B rows of the run.  Each row step reads one contiguous span of the
+// level row (nb bricks' windows, about 32 chunks, each fetched by at most two
+// lanes and merged in L1) and writes each brick's row chunk with one 16-byte
+// store.  Rows are whole 16-byte chunks of the level (row bytes a multiple of
+// 16, aligned level), so a chunk lies entirely inside or outside the row:
+// chunks outside read as zero, which is the bricker's value there (outside
+// the level); rows outside the level and unvisited bricks store zeros.  Row
+// steps go four at a time, their loads issued before their stores.
+__global__ void __launch_bounds__(256) brick_rows_kernel(const uint8_t *__restrict__ level,
+                                                         uint8_t *__restrict__ out, BrickParams p, uint32_t ngx) {
+    const uint32_t B = p.B, eb = p.eb;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t nb = 32u >> p.cpr_shift;
+    const uint32_t j = lane >> p.cpr_shift, k = lane & ((1u << p.cpr_shift) - 1u);
+    const uint32_t nsx = p.nbig[0] * p.BB[0], nsy = p.nbig[1] * p.BB[1], nsz = p.nbig[2] * p.BB[2];
+    const uint32_t bvx = p.BB[0] * B, bvy = p.BB[1] * B;
+    const uint64_t big_bytes = static_cast<uint64_t>(bvx) * bvy * (p.BB[2] * B) * eb;
+    const uint64_t row_bytes = static_cast<uint64_t>(p.D[0]) * eb;
+    const int64_t row_chunks = static_cast<int64_t>(row_bytes >> 4);
+    const uint64_t drow = static_cast<uint64_t>(bvx) * eb;  // output row stride
+    const uint32_t nseg_xy = ngx * nsy;
+    const uint64_t nseg = static_cast<uint64_t>(nseg_xy) * nsz;
+    const uint32_t nrows = B * B;
+    const uint64_t gwarp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (uint64_t seg = gwarp; seg < nseg; seg += nwarps) {
+        const uint32_t sz = static_cast<uint32_t>(seg / nseg_xy);
+        const uint32_t rem = static_cast<uint32_t>(seg - static_cast<uint64_t>(sz) * nseg_xy);
+        const uint32_t sy = rem / ngx, g = rem - sy * ngx;
+        const uint32_t sx = g * nb + j;
+        const bool valid = sx < nsx;
+        const bool yz_vis = static_cast<uint64_t>(sy) * p.Beff < p.D[1] && static_cast<uint64_t>(sz) * p.Beff < p.D[2];
+        const bool x_vis = static_cast<uint64_t>(sx) * p.Beff < p.D[0];
+        // this lane's source window in any row: bytes [o, o + 16), o = its
+        // chunk's first voxel byte (negative in the covering left of x = 0)
+        const int64_t o = (static_cast<int64_t>(sx) * p.Beff - p.c) * eb + 16 * static_cast<int64_t>(k);
+        const int64_t ca = o >> 4;  // floor
+        const uint32_t s = static_cast<uint32_t>(o - ca * 16);
+        const bool a_in = x_vis && ca >= 0 && ca < row_chunks;
+        const bool b_in = x_vis && s != 0u && ca + 1 >= 0 && ca + 1 < row_chunks;
+        const uint32_t gx = valid ? sx / p.BB[0] : 0u, gy = sy / p.BB[1], gz = sz / p.BB[2];
+        const uint32_t ix = sx - gx * p.BB[0], iy = sy - gy * p.BB[1], iz = sz - gz * p.BB[2];
+        const uint64_t big = (static_cast<uint64_t>(gz) * p.nbig[1] + gy) * p.nbig[0] + gx;
+        uint8_t *dst = out + big * big_bytes + ((static_cast<uint64_t>(iz) * B * bvy + iy * B) * bvx + ix * B) * eb +
+                       16u * k;
+        const int64_t y0 = static_cast<int64_t>(sy) * p.Beff - p.c, z0 = static_cast<int64_t>(sz) * p.Beff - p.c;
+        for (uint32_t r0 = 0; r0 < nrows; r0 += 4u) {
+            uint4 a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t r = r0 + u, ly = r & (B - 1u), lz = r >> p.b_shift;
+                const int64_t y = y0 + ly, z = z0 + lz;
+                const bool row_in = yz_vis && y >= 0 && z >= 0 && y < p.D[1] && z < p.D[2];
+                a[u] = make_uint4(0u, 0u, 0u, 0u);
+                b[u] = a[u];
+                if (row_in) {
+                    const uint4 *row = reinterpret_cast<const uint4 *>(
+                        level + (static_cast<uint64_t>(z) * p.D[1] + static_cast<uint64_t>(y)) * row_bytes);
+                    if (a_in) a[u] = __ldg(row + ca);
+                    if (b_in) b[u] = __ldg(row + ca + 1);
+                }
+            }
+            if (valid) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const uint32_t r = r0 + u, ly = r & (B - 1u), lz = r >> p.b_shift;
+                    *reinterpret_cast<uint4 *>(dst + (static_cast<uint64_t>(lz) * bvy + ly) * drow) =
+                        window16(a[u], b[u], s);
+                }
+            }
+        }
+    }
+}
+
 // Bricks cut on demand from a device-resident pyramid (the device-levels
 // brick source): job j = big brick (x, y, z) of level `lvl` of volume `vol`
 // into staging slot `slot`; one block per job, its warps over the job's small
@@ -479,6 +568,19 @@ int gc_bricks_build(const void *level, const uint32_t level_dims[3], const gc_vo
         p.b_shift = p.cpr_shift = 0;
         while ((1u << p.b_shift) < p.B) ++p.b_shift;
         while (p.fast && (16u << p.cpr_shift) < p.B * p.eb) ++p.cpr_shift;
+        if (p.fast && p.cpr_shift <= 5) {
+            // runs of 32 / cpr bricks along x, one warp per run and brick row
+            const uint32_t nb = 32u >> p.cpr_shift;
+            const uint32_t ngx = (p.nbig[0] * p.BB[0] + nb - 1) / nb;
+            const uint64_t nseg = static_cast<uint64_t>(ngx) * (p.nbig[1] * p.BB[1]) * (p.nbig[2] * p.BB[2]);
+            const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>((nseg + 7) / 8,
+                                                                           static_cast<uint64_t>(sm_count()) * 8));
+            brick_rows_kernel<<<static_cast<unsigned>(grid), 256, 0, as_stream(stream)>>>(
+                static_cast<const uint8_t *>(level), static_cast<uint8_t *>(out), p, ngx);
+            GC_CUDA(cudaGetLastError());
+            count_launch();
+            return;
+        }
         // one warp per brick: 8 warps per block, enough blocks to fill every SM
         const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>((p.nsmall + 7) / 8,
                                                                        static_cast<uint64_t>(sm_count()) * 8));

@@ -134,11 +134,30 @@ __device__ __forceinline__ float div_const(float x, float d) {
 #endif
 }
 
+// Integer conversions without the conversion unit (its quarter-rate pipe and
+// scoreboard latency sit on every step of the march); both are exact.
+// floor(v) for 0 <= v < 2^23: v + 2^23 rounded toward -inf is 2^23 + floor(v),
+// whose low mantissa bits are floor(v).
+__device__ __forceinline__ uint32_t floor_u(float v) {
+    return __float_as_uint(__fadd_rd(v, 8388608.0f)) - 0x4B000000u;
+}
+// floor(v) for -2^22 <= v < 2^22, as an integer and as a float.
+__device__ __forceinline__ int floor_i(float v, float &fl) {
+    const float t = __fadd_rd(v, 12582912.0f);  // 1.5 * 2^23 + floor(v)
+    fl = t - 12582912.0f;
+    return __float_as_int(t) - 0x4B400000;
+}
+// (float)u for u < 2^23.
+__device__ __forceinline__ float u2f(uint32_t u) { return __uint_as_float(0x4B000000u | u) - 8388608.0f; }
+
 __device__ __forceinline__ float4 tf_lookup(const float *__restrict__ tf, uint32_t w, float s) {
-    const float xb = fmad(s, static_cast<float>(w), -0.5f);
-    const float fl = floorf(xb);
+    // xb is clamped into floor_i's range first: outside [-1, w] both indices
+    // clamp to the same table entry, so the value is unchanged (a NaN sample,
+    // possible only from a float volume holding NaN, reads entry 0)
+    const float xb = fminf(fmaxf(fmad(s, static_cast<float>(w), -0.5f), -2.0f), static_cast<float>(w) + 1.0f);
+    float fl;
+    int i0 = floor_i(xb, fl);
     const float a = xb - fl;
-    int i0 = static_cast<int>(fl);
     int i1 = i0 + 1;
     const int hi = static_cast<int>(w) - 1;
     i0 = i0 < 0 ? 0 : (i0 > hi ? hi : i0);
@@ -154,11 +173,13 @@ __device__ __forceinline__ float4 tf_lookup(const float *__restrict__ tf, uint32
 // axis (bilinear, edge-clamped).
 __device__ __forceinline__ float4 tf2d_lookup(const float *__restrict__ tf, uint32_t w, uint32_t h, float s0,
                                               float s1) {
-    const float xb = fmad(s0, static_cast<float>(w), -0.5f), yb = fmad(s1, static_cast<float>(h), -0.5f);
-    const float flx = floorf(xb), fly = floorf(yb);
+    const float xb = fminf(fmaxf(fmad(s0, static_cast<float>(w), -0.5f), -2.0f), static_cast<float>(w) + 1.0f);
+    const float yb = fminf(fmaxf(fmad(s1, static_cast<float>(h), -0.5f), -2.0f), static_cast<float>(h) + 1.0f);
+    float flx, fly;
+    int i0 = floor_i(xb, flx), j0 = floor_i(yb, fly);
     const float ax = xb - flx, ay = yb - fly;
     const int hx = static_cast<int>(w) - 1, hy = static_cast<int>(h) - 1;
-    int i0 = static_cast<int>(flx), i1 = i0 + 1, j0 = static_cast<int>(fly), j1 = j0 + 1;
+    int i1 = i0 + 1, j1 = j0 + 1;
     i0 = i0 < 0 ? 0 : (i0 > hx ? hx : i0);
     i1 = i1 < 0 ? 0 : (i1 > hx ? hx : i1);
     j0 = j0 < 0 ? 0 : (j0 > hy ? hy : j0);
@@ -211,7 +232,7 @@ __device__ __forceinline__ float sample_corner(const T *__restrict__ b, uint32_t
     if constexpr (sizeof(T) < 4) {
         const uint32_t s = static_cast<uint32_t>(__ldg(p0)) + __ldg(p0 + 1) + __ldg(p1) + __ldg(p1 + 1) + __ldg(p2) +
                            __ldg(p2 + 1) + __ldg(p3) + __ldg(p3 + 1);
-        return div_const(static_cast<float>(s), VoxelTraits<T>::kSum8);
+        return div_const(u2f(s), VoxelTraits<T>::kSum8);
     } else {
         const float s = ((__ldg(p0) + __ldg(p0 + 1)) + (__ldg(p1) + __ldg(p1 + 1))) +
                         ((__ldg(p2) + __ldg(p2 + 1)) + (__ldg(p3) + __ldg(p3 + 1)));
@@ -219,21 +240,20 @@ __device__ __forceinline__ float sample_corner(const T *__restrict__ b, uint32_t
     }
 }
 
-// x mod (B - 2c) by a multiply-shift: with m = ceil(2^31 / d), floor(x m / 2^31)
-// is floor(x / d) for every x < 2^24 and d <= 128 (the host sets m only when
-// every level's voxel count is below 2^24; m = 0 falls back to %).
+// x mod (B - 2c) by a multiply-high: with m = ceil(2^32 / d), the high word of
+// x m is floor(x / d) for every x < 2^25 and 2 <= d <= 128 (voxel coordinates
+// are below 2^23, checked at cache creation; m = 0 falls back to %).
 __device__ __forceinline__ uint32_t mod_beff(uint32_t x, uint32_t d, uint32_t m) {
     if (m == 0) return x % d;
-    const uint32_t q = static_cast<uint32_t>((static_cast<uint64_t>(x) * m) >> 31);
-    return x - q * d;
+    return x - __umulhi(x, m) * d;
 }
 
 // Trilinear sampler at the fractional position f (voxels of the level); the
 // pair (i0, i0 + 1) is clamped to the brick (only reachable with covering 0).
 __device__ __forceinline__ void tri_axis(float f, uint32_t c, uint32_t beff, uint32_t magic, uint32_t B,
                                          uint32_t &i0, float &w) {
-    const uint32_t m = static_cast<uint32_t>(f);
-    const float fr = f - static_cast<float>(m);
+    const uint32_t m = floor_u(f);
+    const float fr = f - u2f(m);
     const uint32_t l = c + mod_beff(m, beff, magic);
     if (fr >= 0.5f) {
         i0 = l;
@@ -268,7 +288,7 @@ enum Status { kMapped = 0, kUnmapped = 1, kEmpty = 2, kInvisible = 3, kCoarser =
 
 // Per-thread page-walk state (K_CacheManager::_previousCoords / _previousEntries).
 struct Walk {
-    uint32_t pcx, pcy, pcz;
+    uint32_t pidx;   // page-directory index of the entry last read (one word per (x, y, z))
     uint32_t flag;   // flag of the entry last read (0 unmapped, 1 mapped, 2 empty, 3 in flight)
     uint32_t slot;   // pool slot of a mapped entry (decoded when the entry is read)
     bool invisible;  // the mapped brick holds no value the view's transfer function shows
@@ -303,9 +323,9 @@ __device__ __forceinline__ float sample_slot(const uint8_t *base, uint32_t /*eb*
     const T *b = reinterpret_cast<const T *>(base);
     const uint32_t B = cv.B;
     if (sampler == GC_SAMPLER_REFERENCE) {
-        const uint32_t lx = cv.c + mod_beff(static_cast<uint32_t>(fx), cv.Beff, cv.beff_magic);
-        const uint32_t ly = cv.c + mod_beff(static_cast<uint32_t>(fy), cv.Beff, cv.beff_magic);
-        const uint32_t lz = cv.c + mod_beff(static_cast<uint32_t>(fz), cv.Beff, cv.beff_magic);
+        const uint32_t lx = cv.c + mod_beff(floor_u(fx), cv.Beff, cv.beff_magic);
+        const uint32_t ly = cv.c + mod_beff(floor_u(fy), cv.Beff, cv.beff_magic);
+        const uint32_t lz = cv.c + mod_beff(floor_u(fz), cv.Beff, cv.beff_magic);
         return sample_corner<T>(b, B, lx, ly, lz);
     }
     uint32_t x0, y0, z0;
@@ -328,9 +348,9 @@ __device__ __forceinline__ float2 sample_slot_two(const uint8_t *__restrict__ b,
                                                   uint32_t sampler, float fx, float fy, float fz) {
     const uint32_t B = cv.B, BB = B * B;
     if (sampler == GC_SAMPLER_REFERENCE) {
-        uint32_t lx = cv.c + mod_beff(static_cast<uint32_t>(fx), cv.Beff, cv.beff_magic);
-        uint32_t ly = cv.c + mod_beff(static_cast<uint32_t>(fy), cv.Beff, cv.beff_magic);
-        uint32_t lz = cv.c + mod_beff(static_cast<uint32_t>(fz), cv.Beff, cv.beff_magic);
+        uint32_t lx = cv.c + mod_beff(floor_u(fx), cv.Beff, cv.beff_magic);
+        uint32_t ly = cv.c + mod_beff(floor_u(fy), cv.Beff, cv.beff_magic);
+        uint32_t lz = cv.c + mod_beff(floor_u(fz), cv.Beff, cv.beff_magic);
         lx = lx > 0 ? lx : 1u;
         ly = ly > 0 ? ly : 1u;
         lz = lz > 0 ? lz : 1u;
@@ -343,7 +363,7 @@ __device__ __forceinline__ float2 sample_slot_two(const uint8_t *__restrict__ b,
             s0 += v.x;
             s1 += v.y;
         }
-        return make_float2(div_const(static_cast<float>(s0), 2040.0f), div_const(static_cast<float>(s1), 2040.0f));
+        return make_float2(div_const(u2f(s0), 2040.0f), div_const(u2f(s1), 2040.0f));
     }
     uint32_t x0, y0, z0;
     float wx, wy, wz;
@@ -386,19 +406,18 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
     const float px = np.x * lt.ior[lvl][0];
     const float py = np.y * lt.ior[lvl][1];
     const float pz = np.z * lt.ior[lvl][2];
-    const uint32_t cx = lt.off[lvl] + static_cast<uint32_t>(px * lt.nbf[lvl][0]);
-    const uint32_t cy = static_cast<uint32_t>(py * lt.nbf[lvl][1]);
-    const uint32_t cz = static_cast<uint32_t>(pz * lt.nbf[lvl][2]);
-    const uint64_t idx = cx + static_cast<uint64_t>(cy) * cv.mx + static_cast<uint64_t>(cz) * cv.mx * cv.my;
-    if (cx != w.pcx || cy != w.pcy || cz != w.pcz) {
+    const uint32_t cx = lt.off[lvl] + floor_u(px * lt.nbf[lvl][0]);
+    const uint32_t cy = floor_u(py * lt.nbf[lvl][1]);
+    const uint32_t cz = floor_u(pz * lt.nbf[lvl][2]);
+    // the page directory has fewer than 2^32 - 1 entries (checked at creation)
+    const uint32_t idx = cx + cy * cv.mx + cz * cv.mxy;
+    if (idx != w.pidx) {
         // A new entry: the entry and its value bins are read together (one
         // memory round trip); the usage stamp of a mapped brick is a plain
         // store (idempotent, like the reference's per-sample stamp).
         const uint4 e = __ldg(cv.mrpd + idx);
         const unsigned long long bins = __ldg(cv.entry_bins + idx);
-        w.pcx = cx;
-        w.pcy = cy;
-        w.pcz = cz;
+        w.pidx = idx;
         w.flag = e.w;
         w.invisible = (bins & vp.visible) == 0ull && (e.w == 1u || (e.w == 0u && cv.bins_user));
         if (e.w == 1u) {
@@ -582,7 +601,7 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
     r.lvl_end = vp.level_base + vp.nlevels;
     r.sampler = vp.sampler;
     r.t_lo = lod_keep_bound(r.sL, r.sU, r.endX, r.endY, r.tfar, r.lvl + 1 >= r.lvl_end);
-    r.w.pcx = r.w.pcy = r.w.pcz = UINT_MAX;
+    r.w.pidx = UINT_MAX;
     r.w.flag = 0;
     r.w.slot = 0;
     r.w.invisible = false;

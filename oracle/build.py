@@ -17,7 +17,9 @@ ROOT = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "libgcoracle.so")
 REF_OUT = os.path.join(HERE, "_ref")
 REF_BIN = os.path.join(REF_OUT, "refdriver")
-REFERENCE = os.environ.get("GC_REFERENCE_DIR", "/root/reference")
+# the reference checkout: GC_REFERENCE_DIR, else a directory named "reference"
+# beside this repository
+REFERENCE = os.environ.get("GC_REFERENCE_DIR", os.path.join(os.path.dirname(ROOT), "reference"))
 
 
 def build_oracle(force=False):
