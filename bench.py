@@ -323,13 +323,77 @@ PIN_STORES = True  # brick stores in page-locked host memory (--pageable-stores:
 LAST_PREPROCESS = {}  # stage timings of the last make_store (device mip, bricking, store copy)
 
 
+SHM_DIR = "/dev/shm"
+
+
+def host_register(torch, t):
+    """Page-locks a host tensor's pages for this process (cudaHostRegister);
+    False where that is not possible (no device, or the call fails)."""
+    if not torch.cuda.is_available():
+        return False
+    return int(torch.cuda.cudart().cudaHostRegister(t.data_ptr(), t.numel() * t.element_size(), 0)) == 0
+
+
+def node_shared_store(torch, key, nbytes, fill):
+    """One host brick store for all replicas of a node.  With one process,
+    fill(out) gets a host tensor of nbytes (page-locked when PIN_STORES) and
+    returns the bins of every brick.  With several (torchrun), the rank with
+    LOCAL_RANK 0 runs fill on a tensor mapping a file in /dev/shm, the other
+    ranks map the same file after a barrier (the pages exist once on the
+    node, each process page-locks its own mapping), and the file's name is
+    removed once every rank holds its mapping.  The bins travel beside it.
+    Returns (store tensor, bins)."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world == 1:
+        out = torch.empty(nbytes, dtype=torch.uint8, pin_memory=PIN_STORES)
+        return out, fill(out)
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    path = os.path.join(SHM_DIR, f"gc_store_{os.environ.get('MASTER_PORT', '0')}_{key}")
+    if local == 0:
+        mm = np.memmap(path, dtype=np.uint8, mode="w+", shape=(nbytes,))
+        out = torch.from_numpy(mm)
+        if PIN_STORES:
+            host_register(torch, out)
+        bins = fill(out)
+        mm.flush()
+        np.save(path + ".bins.npy", np.asarray(bins, dtype=np.uint64))
+    rank_barrier()
+    if local != 0:
+        mm = np.memmap(path, dtype=np.uint8, mode="r+", shape=(nbytes,))
+        out = torch.from_numpy(mm)
+        if PIN_STORES:
+            host_register(torch, out)
+        bins = np.load(path + ".bins.npy")
+    rank_barrier()
+    if local == 0:
+        os.remove(path)
+        os.remove(path + ".bins.npy")
+    return out, bins
+
+
 def make_store(gc, torch, cfg):
     """Synthetic volume generated on the device, pre-processed (mip + bricks) on
-    the device, brick store moved to host memory (the out-of-core source)."""
+    the device, brick store moved to host memory (the out-of-core source);
+    replicas on one node share one store (node_shared_store)."""
     size, bpc = cfg["size"], cfg["bpc"]
     nc = cfg.get("channels", 1)
     vol = gc.volume_desc(size, cfg["B"], cfg["c"], bpc * nc, nc, cfg.get("bb", (1, 1, 1)))
     layout = gc.compute_layout(vol)
+    offs, nbytes, _ = gc.brick_store_offsets(layout, vol)
+    t0 = time.time()
+    key = f"{size[0]}x{size[1]}x{size[2]}_{bpc}x{nc}_B{cfg['B']}c{cfg['c']}_s{cfg['seed']}"
+    store, bins = node_shared_store(torch, key, nbytes, lambda out: build_store(gc, torch, cfg, vol, layout, out))
+    BRICK_BINS[store.data_ptr()] = bins
+    t2 = time.time()
+    log(f"volume {size} B{cfg['B']}: store of {store.numel() / 2**30:.2f} GiB of bricks in {t2 - t0:.2f}s")
+    return vol, layout, store, offs, t2 - t0
+
+
+def build_store(gc, torch, cfg, vol, layout, out):
+    """The volume generated and pre-processed on the device, its bricks copied
+    into the host tensor `out`; returns the bins of every brick."""
+    size, bpc = cfg["size"], cfg["bpc"]
+    nc = cfg.get("channels", 1)
     t0 = time.time()
     blobs = gc.generator_blobs(cfg["seed"], cfg["nblobs"], size, cfg["sigma"][0], cfg["sigma"][1], cfg["amp"][0],
                                cfg["amp"][1])
@@ -343,16 +407,13 @@ def make_store(gc, torch, cfg):
     t1 = time.time()
     tm = {}
     bins = []
-    store, offs, _ = gc.pre_process(vol, layout, dev, pin=PIN_STORES, timings=tm, value_bins=bins)
-    BRICK_BINS[store.data_ptr()] = bins[0]
+    gc.pre_process(vol, layout, dev, timings=tm, value_bins=bins, host_out=out)
     LAST_PREPROCESS.clear()
     LAST_PREPROCESS.update(tm)
     del dev
     torch.cuda.empty_cache()
-    t2 = time.time()
-    log(f"volume {size} B{cfg['B']}: generated {t1 - t0:.2f}s, pre-processed "
-        f"({store.numel() / 2**30:.2f} GiB of bricks) {t2 - t1:.2f}s")
-    return vol, layout, store, offs, t2 - t0
+    log(f"volume {size} B{cfg['B']}: generated {t1 - t0:.2f}s, pre-processed {time.time() - t1:.2f}s")
+    return bins[0]
 
 
 class Session:
@@ -520,7 +581,8 @@ def run_ours(args):
         for f in range(args.warmup):
             S.converge(spec(f), cap=cfg.get("cap", 64))
         s0, l0 = S.cm.stats(), gc.kernel_launches()
-        ev = None if e2e else render_events
+        ev = None if e2e else []
+        render_events[:] = [] if ev is None else [ev]
         torch.cuda.nvtx.range_push("timed_e2e" if e2e else "timed")
         wall, lat, info = timed(torch, S.stream, lambda i: S.converge(spec(views[i]), e2e=e2e,
                                                                       cap=cfg.get("cap", 64), render_events=ev),
@@ -530,9 +592,9 @@ def run_ours(args):
         s1 = S.cm.stats()
         return S, wall, lat, info, launches, s0, s1
 
-    # ray-caster launches of the timed value pass, bracketed by CUDA events on
-    # the launch stream: the live split of a step's time (the launch list under
-    # ncu serialises launches and slows the upload's host reads)
+    # ray-caster launches of the last timed value pass, bracketed by CUDA
+    # events on the launch stream: the live split of a step's time (the launch
+    # list under ncu serialises launches and slows the upload's host reads)
     render_events = []
 
     # launch configuration: autotuned once, on three views spread along the
@@ -546,6 +608,9 @@ def run_ours(args):
     S_e, wall_e, lat_e, _, _, s0_e, s1_e = plain_pass(True)
     S_e.close()
     S, wall, lat, info, launches, s0, s1 = plain_pass(False)
+    torch.cuda.synchronize()
+    render_ms_total = sum(a.elapsed_time(b) for a, b in render_events[0])
+    render_launches = len(render_events[0])
     with_bins = None
     if not args.brick_bins:
         # the same views with the value bins of every brick given to the cache:
@@ -681,6 +746,11 @@ def run_ours(args):
                           "candidates_timed": len(tuned[0][1]) if tuned else 0},
         "gpu_launches": int(launches),
         "cache": cache_delta(s0, s1),
+        "step_split": {"render_ms_per_step": round(render_ms_total / args.steps, 3),
+                       "other_ms_per_step": round(1e3 * wall / args.steps - render_ms_total / args.steps, 3),
+                       "render_launches_per_step": round(render_launches / args.steps, 2),
+                       "note": "ray-caster launches timed with CUDA events on the launch stream; other = the "
+                               "cache updates (LRU, miss scan, host resolve, brick upload, install)"},
         "clocks": clk,
     }
     if with_bins:

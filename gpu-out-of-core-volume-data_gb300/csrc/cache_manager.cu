@@ -97,6 +97,25 @@ struct Volume {
 
 }  // namespace gc
 
+// The loader's per-cycle scratch, kept between cycles: the list element kinds,
+// the big-brick index of each non-empty element, and an open-addressing
+// table from big-brick key to its staging slot (-1 empty, -2 unknown) that
+// folds the elements of one big brick into one load.
+struct ResolveScratch {
+    std::vector<int> kind;
+    std::vector<uint32_t> big_index;
+    std::vector<uint64_t> keys;  // kNoKey marks a free table cell
+    std::vector<int32_t> vals;
+    static constexpr uint64_t kNoKey = ~0ull;
+    // the cell of `key` (found or free) in a power-of-two table
+    size_t cell(uint64_t key) const {
+        const size_t mask = keys.size() - 1;
+        size_t h = static_cast<size_t>((key * 0x9E3779B97F4A7C15ull) >> 32) & mask;
+        while (keys[h] != kNoKey && keys[h] != key) h = (h + 1) & mask;
+        return h;
+    }
+};
+
 struct gc_cache {
     gc_cache_desc d;                  // d.volume / d.layout: volume 0
     std::vector<gc::Volume> vols;
@@ -132,6 +151,7 @@ struct gc_cache {
     uint8_t *d_staging = nullptr;
     gc::CutSources cut;               // device-resident pyramids of the volumes that have one
     uint4 *d_cut = nullptr, *h_cut = nullptr;  // cut jobs of a load cycle (device-levels sources)
+    ResolveScratch resolve;           // the loader's per-cycle scratch
     gc::ViewParams *d_views = nullptr;
     uint32_t max_views = 256;
     // pinned host buffers
@@ -217,11 +237,25 @@ static void build_tables(gc_cache *C) {
 // Returns the number of bricks to install (non-empty first), or 0.
 static void resolve_and_upload(gc_cache *C, uint32_t n) {
     const auto t_begin = std::chrono::steady_clock::now();
-    std::unordered_map<uint64_t, int32_t> asked;
-    std::vector<int> kind(n, 0);  // 0 non-empty, 1 empty, 2 unknown (dropped)
+    ResolveScratch &R = C->resolve;
+    R.kind.assign(n, 0);  // 0 non-empty, 1 empty, 2 unknown (dropped)
+    std::vector<int> &kind = R.kind;
     uint32_t n_nonempty = 0, nbig = 0;
-    std::vector<uint32_t> big_index;
+    std::vector<uint32_t> &big_index = R.big_index;
+    big_index.clear();
     big_index.reserve(n);
+    // Elements of one big brick share one load.  With one-brick big bricks
+    // every element of the miss list (distinct page-directory entries) is
+    // its own big brick and the table is skipped.
+    bool dedupe = false;
+    for (const Volume &V : C->vols)
+        dedupe = dedupe || V.desc.big_brick_size[0] * V.desc.big_brick_size[1] * V.desc.big_brick_size[2] > 1;
+    if (dedupe) {
+        size_t cap = 16;
+        while (cap < 2 * static_cast<size_t>(n)) cap <<= 1;
+        R.keys.assign(cap, ResolveScratch::kNoKey);
+        R.vals.assign(cap, 0);
+    }
     struct Copy {
         const uint8_t *src;
         uint8_t *dst;
@@ -244,24 +278,28 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
         const uint32_t *BB = V.desc.big_brick_size;
         const uint32_t gx = b.x / BB[0], gy = b.y / BB[1], gz = b.z / BB[2];
         const uint64_t key = gc_brick_key(b.w, gx, gy, gz);
-        auto it = asked.find(key);
-        if (it != asked.end()) {
-            if (it->second == -1)
-                kind[i] = 1;
-            else if (it->second == -2)
-                kind[i] = 2;
-            else {
-                kind[i] = 0;
-                big_index.push_back(static_cast<uint32_t>(it->second));
-                ++n_nonempty;
+        size_t cell = 0;
+        if (dedupe) {
+            cell = R.cell(key);
+            if (R.keys[cell] == key) {
+                const int32_t v = R.vals[cell];
+                if (v == -1)
+                    kind[i] = 1;
+                else if (v == -2)
+                    kind[i] = 2;
+                else {
+                    kind[i] = 0;
+                    big_index.push_back(static_cast<uint32_t>(v));
+                    ++n_nonempty;
+                }
+                continue;
             }
-            continue;
         }
         int status = GC_BRICK_UNKNOWN;
         bool on_device = false;
         const Source &src = V.src;
         uint8_t *stage = C->h_staging + static_cast<uint64_t>(nbig) * C->big_stride;
-        if (src.empty.count(gc_brick_key(lvl, gx, gy, gz))) {  // the volume's own brick keys
+        if (!src.empty.empty() && src.empty.count(gc_brick_key(lvl, gx, gy, gz))) {  // the volume's own keys
             status = GC_BRICK_EMPTY;
         } else if (src.kind == 1) {
             const gc_layout &L = V.layout;
@@ -297,26 +335,31 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
                 status = GC_BRICK_SUCCESS;
             }
         }
+        int32_t val;
         if (status == GC_BRICK_SUCCESS) {
             if (!on_device) {
                 bytes_up += V.big_bytes;
                 ++nhost;
             }
-            asked[key] = static_cast<int32_t>(nbig);
+            val = static_cast<int32_t>(nbig);
             C->h_big_coord[nbig] = make_uint4(gx, gy, gz, b.w);
             big_index.push_back(nbig);
             ++nbig;
             ++n_nonempty;
             kind[i] = 0;
         } else if (status == GC_BRICK_EMPTY) {
-            asked[key] = -1;
+            val = -1;
             kind[i] = 1;
         } else {
             // The reference asserts here (RequestHandler.hpp:348-350).  The
             // brick stays unmapped and is requested again by a later frame.
-            asked[key] = -2;
+            val = -2;
             kind[i] = 2;
             C->stats.load_errors++;
+        }
+        if (dedupe) {
+            R.keys[cell] = key;
+            R.vals[cell] = val;
         }
     }
     // Host-store bricks are copied into the pinned staging buffer by up to 8

@@ -351,7 +351,7 @@ def brick_store_offsets(layout, vol):
 
 
 def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host", pin=False, timings=None,
-                value_bins=None):
+                value_bins=None, host_out=None):
     """Application::pre_process (Applications/DVR-ray-caster/src/Application.cu:148-197)
     run on the device: mip pyramid, bricking of every level and empty flags.
 
@@ -364,6 +364,9 @@ def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host
     of the device mip build, the device bricking and the store copy.
     value_bins (a list) receives one numpy uint64 array: the value bins of
     every brick of every level, in the order CacheManager.set_brick_bins takes.
+    host_out: a host uint8 tensor of the store's size receiving the bricks
+    (e.g. a mapping shared by several processes); returned in place of a new
+    host tensor.
     """
     import time
 
@@ -423,7 +426,12 @@ def pre_process(vol, layout, level0, stream=0, empty_threshold=None, store="host
     del pyr
     if store == "device":
         return bricks, soffs, empty_keys
-    host = torch.empty(stotal, dtype=torch.uint8, pin_memory=pin)
+    if host_out is not None:
+        if host_out.numel() * host_out.element_size() != stotal or host_out.device.type != "cpu":
+            raise GcError(1, f"host_out must be a host tensor of {stotal} bytes")
+        host = host_out.view(torch.uint8).reshape(-1)
+    else:
+        host = torch.empty(stotal, dtype=torch.uint8, pin_memory=pin)
     host.copy_(bricks)
     if timings is not None:
         timings["copy_s"] = time.perf_counter() - t2
