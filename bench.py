@@ -1015,6 +1015,85 @@ def run_stress(gc, torch, args, nviews=STRESS_VIEWS):
                           "note": "every level read once and every coarser level written, over the build time"}}
 
 
+def run_roofline_only(args):
+    """`--roofline-only`: the c2 roofline launch alone, for ncu captures.  The
+    volume's mip pyramid is built on the device and serves as the brick source
+    (nothing is read from host memory under the profiler); views roofline-2
+    .. roofline are rendered to convergence, the pyramid is released (the
+    pool then holds every brick the view needs; no update follows), and the
+    roofline view is re-rendered from scratch after an L2 flush `--steps`
+    times inside the NVTX range "roofline" (about 3 GB held on the device).
+    Prints one JSON line with the launch times (CUDA events)."""
+    import torch
+
+    import gcgb300 as gc
+
+    gc.render_precision(gc.RENDER_FAST if args.precision == "fast" else gc.RENDER_EXACT)
+    cfg = CONFIGS["c2"]
+    size, eb = cfg["size"], cfg["bpc"]
+    vol = gc.volume_desc(size, cfg["B"], cfg["c"], eb, 1, (1, 1, 1))
+    layout = gc.compute_layout(vol)
+    poffs, total = gc.pyramid_offsets(layout, eb)
+    pyr = torch.empty(total, dtype=torch.uint8, device="cuda")
+    blobs = gc.generator_blobs(cfg["seed"], cfg["nblobs"], size, cfg["sigma"][0], cfg["sigma"][1], cfg["amp"][0],
+                               cfg["amp"][1])
+    gc.generate_volume(gc.make_generator(size, eb, cfg["seed"], blobs, cfg["noise"]), pyr.data_ptr())
+    gc.Mipmapper.process(pyr.data_ptr(), layout, poffs, eb, 1)
+    torch.cuda.synchronize()
+    if args.tuning:
+        gc.render_tuning(*[int(x) for x in args.tuning.split(",")])
+    cm = gc.CacheManager(vol, layout, pool_slots(cfg), max_requests=args.max_requests, sync_loader=True)
+    cm.set_source_device(pyr.data_ptr(), poffs, keep=pyr)
+    tf = torch.from_numpy(tf_table(cfg["tf"]).reshape(-1).copy()).cuda()
+    W, H = cfg["W"], cfg["H"]
+    bufs = [torch.zeros(W * H * k, dtype=dt, device="cuda") for dt, k in ((torch.int32, 1), (torch.float32, 1),
+                                                                        (torch.float32, 4))]
+    focal = 1.0 / math.tan(math.radians(cfg["fov"]) / 2)
+    stream = torch.cuda.Stream()
+    frame = cfg.get("roofline_frame", 42)
+    iters = []
+    for f in (frame - 2, frame - 1, frame):
+        v = gc.make_view(path_camera(gc.look_at, cfg, f), W, H, tf.data_ptr(), 256, *[b.data_ptr() for b in bufs],
+                         tstep=2.0 / 256.0, focal=focal, early_alpha=cfg["early"])
+        with torch.cuda.stream(stream):
+            bufs[1].zero_()
+            bufs[2].zero_()
+            it, ok = 0, False
+            while not ok and it < 128:
+                cm.render(v, stream.cuda_stream)
+                ok = cm.update(stream.cuda_stream)
+                it += 1
+        stream.synchronize()
+        iters.append(it)
+    cm.drop_sources()
+    del pyr
+    torch.cuda.empty_cache()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    times = []
+    s0 = cm.stats().samples
+    torch.cuda.nvtx.range_push("roofline")
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            bufs[1].zero_()
+            bufs[2].zero_()
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            cm.render(v, stream.cuda_stream)
+            e1.record(stream)
+        stream.synchronize()
+        times.append(e0.elapsed_time(e1))
+    torch.cuda.nvtx.range_pop()
+    st = cm.stats()
+    print(json.dumps({"roofline_only": {"view": frame, "iterations_to_converge": iters,
+                                        "launch_ms": [round(t, 4) for t in times],
+                                        "samples_per_launch": (st.samples - s0) / max(1, args.steps),
+                                        "tuning": list(gc.render_tuning()),
+                                        "device_gb_reserved": round(torch.cuda.memory_reserved() / 1e9, 2)}}),
+          flush=True)
+    cm.close()
+
+
 def run_c5(args):
     """`--config c5`: the stress leg alone, printed as its own line."""
     import torch
@@ -1613,6 +1692,10 @@ def main():
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip the reference's own CUDA build timed beside our plain path (c1 views)")
     ap.add_argument("--no-plain", action="store_true", help="c3: skip the plain loop over the same views")
+    ap.add_argument("--roofline-only", action="store_true",
+                    help="only the c2 roofline launch, --steps times, bricks from the device pyramid (for ncu)")
+    ap.add_argument("--tuning", default=None,
+                    help="ray-caster launch tuning 'scheduler,tile_w,threads,blocks_per_sm' for --roofline-only")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 20
@@ -1636,6 +1719,8 @@ def main():
         run_c4(args)
     elif args.config == "c5":
         run_c5(args)
+    elif args.roofline_only:
+        run_roofline_only(args)
     else:
         run_ours(args)
 

@@ -394,6 +394,38 @@ __device__ __forceinline__ typename SampleOf<T>::type sample_any(const uint8_t *
         return sample_slot<T>(base, eb, cv, sampler, fx, fy, fz);
 }
 
+// The sample position of a ray position in normalized volume coordinates
+// (RayCasters.cu:128-133): scaled into [0, 1], z flipped, clamped to [0, 0.99].
+__device__ __forceinline__ V3 norm_pos(V3 pos) {
+    V3 tp = fma3(pos, 0.495f, v3(0.495f, 0.495f, 0.495f));
+    tp.z = 1.0f - tp.z;
+    return v3(clampf(tp.x, 0.f, 0.99f), clampf(tp.y, 0.f, 0.99f), clampf(tp.z, 0.f, 0.99f));
+}
+
+// Page-directory index of the normalized position np at cache level lvl
+// (K_CacheManager::get_normalized's walk, K_CacheManager.hpp:265-300); p
+// receives the level position np * initial / real.
+__device__ __forceinline__ uint32_t entry_index(const CacheView &cv, const LevelTables &lt, uint32_t lvl, V3 np,
+                                                V3 &p) {
+    p = v3(np.x * lt.ior[lvl][0], np.y * lt.ior[lvl][1], np.z * lt.ior[lvl][2]);
+    const uint32_t cx = lt.off[lvl] + floor_u(p.x * lt.nbf[lvl][0]);
+    const uint32_t cy = floor_u(p.y * lt.nbf[lvl][1]);
+    const uint32_t cz = floor_u(p.z * lt.nbf[lvl][2]);
+    // the page directory has fewer than 2^32 - 1 entries (checked at creation)
+    return cx + cy * cv.mx + cz * cv.mxy;
+}
+
+// Voxel sample of the resident brick in `slot` at level position p.
+template <typename T>
+__device__ __forceinline__ typename SampleOf<T>::type sample_entry(const CacheView &cv, const LevelTables &lt,
+                                                                   uint32_t sampler, const ViewParams &vp,
+                                                                   uint32_t lvl, uint32_t slot, V3 p) {
+    const float fx = p.x * lt.vvoxf[lvl][0];
+    const float fy = p.y * lt.vvoxf[lvl][1];
+    const float fz = p.z * lt.vvoxf[lvl][2];
+    return sample_any<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, vp.eb, cv, sampler, fx, fy, fz);
+}
+
 // Page walk + sample at the normalized position np of cache level lvl (the
 // view's level base + its LOD): K_CacheManager::get_normalized
 // (K_CacheManager.hpp:265-361).
@@ -403,14 +435,8 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
                                      typename SampleOf<T>::type &sample) {
     // read where used (rare paths): the view's voxel width (mixed pools), its
     // visible bins (a newly entered brick) and its fallback flag (a missing one)
-    const float px = np.x * lt.ior[lvl][0];
-    const float py = np.y * lt.ior[lvl][1];
-    const float pz = np.z * lt.ior[lvl][2];
-    const uint32_t cx = lt.off[lvl] + floor_u(px * lt.nbf[lvl][0]);
-    const uint32_t cy = floor_u(py * lt.nbf[lvl][1]);
-    const uint32_t cz = floor_u(pz * lt.nbf[lvl][2]);
-    // the page directory has fewer than 2^32 - 1 entries (checked at creation)
-    const uint32_t idx = cx + cy * cv.mx + cz * cv.mxy;
+    V3 p;
+    const uint32_t idx = entry_index(cv, lt, lvl, np, p);
     if (idx != w.pidx) {
         // A new entry: the entry and its value bins are read together (one
         // memory round trip); the usage stamp of a mapped brick is a plain
@@ -430,12 +456,8 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
     }
     const uint32_t flag = w.flag;
     if (flag == 1u) {
-        const uint32_t slot = w.slot;
         if (w.invisible) return kInvisible;  // no sample of this brick reaches the compositing threshold
-        const float fx = px * lt.vvoxf[lvl][0];
-        const float fy = py * lt.vvoxf[lvl][1];
-        const float fz = pz * lt.vvoxf[lvl][2];
-        sample = sample_any<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, vp.eb, cv, sampler, fx, fy, fz);
+        sample = sample_entry<T>(cv, lt, sampler, vp, lvl, w.slot, p);
         return kMapped;
     }
     if (flag == 3u) return kUnmapped;  // on its way (batched form): already requested
@@ -615,15 +637,31 @@ __device__ __forceinline__ bool ray_enters(const Ray &r) {
     return (!r.dvr || r.fc.w < r.early) && r.t < r.tfar;
 }
 
+// Front-to-back compositing of one classified, opacity-corrected sample
+// (RayCasters.cu:163-176).  Opacity correction 1 - (1 - a)^k is applied by
+// the caller; for a <= alpha_floor[lod] the corrected opacity is below
+// 1.05 k a <= 0.0009, under the compositing threshold, so the callers skip
+// it with the same result.
+__device__ __forceinline__ void composite(Ray &r, float4 col) {
+    if (col.w > 0.001f) {
+        col.x *= col.w;
+        col.y *= col.w;
+        col.z *= col.w;
+        const float rr = 1.0f - r.fc.w;
+        r.fc.x = fmad(col.x, rr, r.fc.x);
+        r.fc.y = fmad(col.y, rr, r.fc.y);
+        r.fc.z = fmad(col.z, rr, r.fc.z);
+        r.fc.w = fmad(col.w, rr, r.fc.w);
+    }
+}
+
 // One iteration of the march loop (RayCasters.cu:122-188).  Returns false
 // when the loop ends.
 template <typename T>
 __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables &lt, Ray &r) {
     const ViewParams &vp = *r.vp;
     if (!((!r.dvr || r.fc.w < r.early) && r.t < r.tfar)) return false;
-    V3 tp = fma3(r.pos, 0.495f, v3(0.495f, 0.495f, 0.495f));
-    tp.z = 1.0f - tp.z;
-    const V3 np = v3(clampf(tp.x, 0.f, 0.99f), clampf(tp.y, 0.f, 0.99f), clampf(tp.z, 0.f, 0.99f));
+    const V3 np = norm_pos(r.pos);
     // compute_LOD: the level only grows along a ray because the pixel
     // footprint grows with t, so the scan resumes at the current level (and
     // the footprint is not needed once the ray is at the coarsest level).
@@ -674,20 +712,8 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
     }
     if (r.dvr) {
         float4 col = classify(r.tf, r.tfw, vp, sample);
-        // Opacity correction 1 - (1 - a)^k.  For a <= alpha_floor[lod] the
-        // corrected opacity is below 1.05 k a <= 0.0009, under the compositing
-        // threshold: the correction is skipped, the result is the same.
         col.w = col.w > r.afloor ? 1.0f - gc_pow(1.0f - col.w, r.kexp) : 0.0f;
-        if (col.w > 0.001f) {
-            col.x *= col.w;
-            col.y *= col.w;
-            col.z *= col.w;
-            const float rr = 1.0f - r.fc.w;
-            r.fc.x = fmad(col.x, rr, r.fc.x);
-            r.fc.y = fmad(col.y, rr, r.fc.y);
-            r.fc.z = fmad(col.z, rr, r.fc.z);
-            r.fc.w = fmad(col.w, rr, r.fc.w);
-        }
+        composite(r, col);
     } else {
         r.maxOp = fmaxf(r.maxOp, first_channel(sample));
     }

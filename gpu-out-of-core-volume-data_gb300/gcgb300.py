@@ -600,6 +600,12 @@ class CacheManager:
         self._keep.append((offs, keys, keep))
         check(lib.gc_cache_set_volume_source_device(self._h, volume, vp(pyramid_ptr), offs, keys, len(empty_keys)))
 
+    def drop_sources(self):
+        """Releases this object's references to the brick sources given so
+        far (host stores, pyramids, key arrays).  The cache keeps the pointers:
+        call update() only after giving a source again."""
+        self._keep.clear()
+
     def set_brick_bins(self, bins, volume=0):
         """Value bins of every brick of the volume (pre_process(value_bins=...)):
         missing bricks the transfer function cannot make visible are stepped
