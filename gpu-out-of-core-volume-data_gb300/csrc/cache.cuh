@@ -224,13 +224,14 @@ struct RenderTuning {
 };
 RenderTuning &render_tuning();
 // Ray-caster kernels of a voxel kind (1, 2, 4 bytes; 0 mixed widths; 0x202
-// two 8-bit channels) and scheduler, from the exact build (render.cu) or the
-// fast build (render_fast.cu); nullptr for an unsupported kind.
+// two 8-bit channels), scheduler and brick size (16 and 32 have kernels
+// compiled for them), from the exact build (render.cu) or the fast build
+// (render_fast.cu); nullptr for an unsupported kind.
 namespace exact {
-void *march_kernel(uint32_t kind, bool pixels);
+void *march_kernel(uint32_t kind, bool pixels, uint32_t brick_size);
 }
 namespace fast {
-void *march_kernel(uint32_t kind, bool pixels);
+void *march_kernel(uint32_t kind, bool pixels, uint32_t brick_size);
 }
 // Fills ViewParams::visible of n device views from their transfer functions.
 void launch_view_bins(ViewParams *views_dev, uint32_t n, cudaStream_t s);

@@ -218,9 +218,12 @@ struct VoxelTraits<float> {
 // With covering >= 1 both voxels lie in the brick; with covering 0 the lower
 // one is clamped to the brick edge (the reference then reads the neighbouring
 // slot of its texture).
-template <typename T>
-__device__ __forceinline__ float sample_corner(const T *__restrict__ b, uint32_t B, uint32_t lx, uint32_t ly,
+// BS: the brick size when known at compile time (its row and slice strides
+// become immediate load offsets), 0 for the run-time B.
+template <typename T, uint32_t BS>
+__device__ __forceinline__ float sample_corner(const T *__restrict__ b, uint32_t Brt, uint32_t lx, uint32_t ly,
                                                uint32_t lz) {
+    const uint32_t B = BS ? BS : Brt;
     lx = lx > 0 ? lx : 1u;
     ly = ly > 0 ? ly : 1u;
     lz = lz > 0 ? lz : 1u;
@@ -271,9 +274,10 @@ template <typename T>
 __device__ __forceinline__ float ldv(const T *__restrict__ b, uint32_t i) {
     return static_cast<float>(__ldg(b + i));
 }
-template <typename T>
-__device__ __forceinline__ float sample_trilinear(const T *__restrict__ b, uint32_t B, uint32_t x0, uint32_t y0,
+template <typename T, uint32_t BS>
+__device__ __forceinline__ float sample_trilinear(const T *__restrict__ b, uint32_t Brt, uint32_t x0, uint32_t y0,
                                                   uint32_t z0, float wx, float wy, float wz) {
+    const uint32_t B = BS ? BS : Brt;
     const uint32_t i = (z0 * B + y0) * B + x0, BB = B * B;
     const float c00 = fmad(ldv(b, i + 1) - ldv(b, i), wx, ldv(b, i));
     const float c10 = fmad(ldv(b, i + B + 1) - ldv(b, i + B), wx, ldv(b, i + B));
@@ -290,7 +294,7 @@ enum Status { kMapped = 0, kUnmapped = 1, kEmpty = 2, kInvisible = 3, kCoarser =
 struct Walk {
     uint32_t pidx;   // page-directory index of the entry last read (one word per (x, y, z))
     uint32_t flag;   // flag of the entry last read (0 unmapped, 1 mapped, 2 empty, 3 in flight)
-    uint32_t slot;   // pool slot of a mapped entry (decoded when the entry is read)
+    const uint8_t *base;  // pool slot of a mapped entry (decoded when the entry is read)
     bool invisible;  // the mapped brick holds no value the view's transfer function shows
 };
 
@@ -317,36 +321,36 @@ __device__ __forceinline__ float4 classify(const float *tf, uint32_t tfw, const 
     return tf2d_lookup(tf, tfw, vp.tfh, s.x, s.y);
 }
 
-template <typename T>
-__device__ __forceinline__ float sample_slot(const uint8_t *base, uint32_t /*eb*/, const CacheView &cv,
+template <typename T, uint32_t BS>
+__device__ __forceinline__ float sample_slot(const uint8_t *base, uint32_t eb, const CacheView &cv,
                                              uint32_t sampler, float fx, float fy, float fz) {
-    const T *b = reinterpret_cast<const T *>(base);
-    const uint32_t B = cv.B;
-    if (sampler == GC_SAMPLER_REFERENCE) {
-        const uint32_t lx = cv.c + mod_beff(floor_u(fx), cv.Beff, cv.beff_magic);
-        const uint32_t ly = cv.c + mod_beff(floor_u(fy), cv.Beff, cv.beff_magic);
-        const uint32_t lz = cv.c + mod_beff(floor_u(fz), cv.Beff, cv.beff_magic);
-        return sample_corner<T>(b, B, lx, ly, lz);
+    if constexpr (std::is_same<T, MixedVoxel>::value) {
+        if (eb == 1) return sample_slot<uint8_t, BS>(base, eb, cv, sampler, fx, fy, fz);
+        if (eb == 2) return sample_slot<uint16_t, BS>(base, eb, cv, sampler, fx, fy, fz);
+        return sample_slot<float, BS>(base, eb, cv, sampler, fx, fy, fz);
+    } else {
+        const T *b = reinterpret_cast<const T *>(base);
+        const uint32_t B = BS ? BS : cv.B;
+        if (sampler == GC_SAMPLER_REFERENCE) {
+            const uint32_t lx = cv.c + mod_beff(floor_u(fx), cv.Beff, cv.beff_magic);
+            const uint32_t ly = cv.c + mod_beff(floor_u(fy), cv.Beff, cv.beff_magic);
+            const uint32_t lz = cv.c + mod_beff(floor_u(fz), cv.Beff, cv.beff_magic);
+            return sample_corner<T, BS>(b, B, lx, ly, lz);
+        }
+        uint32_t x0, y0, z0;
+        float wx, wy, wz;
+        tri_axis(fx, cv.c, cv.Beff, cv.beff_magic, B, x0, wx);
+        tri_axis(fy, cv.c, cv.Beff, cv.beff_magic, B, y0, wy);
+        tri_axis(fz, cv.c, cv.Beff, cv.beff_magic, B, z0, wz);
+        return sample_trilinear<T, BS>(b, B, x0, y0, z0, wx, wy, wz);
     }
-    uint32_t x0, y0, z0;
-    float wx, wy, wz;
-    tri_axis(fx, cv.c, cv.Beff, cv.beff_magic, B, x0, wx);
-    tri_axis(fy, cv.c, cv.Beff, cv.beff_magic, B, y0, wy);
-    tri_axis(fz, cv.c, cv.Beff, cv.beff_magic, B, z0, wz);
-    return sample_trilinear<T>(b, B, x0, y0, z0, wx, wy, wz);
-}
-template <>
-__device__ __forceinline__ float sample_slot<MixedVoxel>(const uint8_t *base, uint32_t eb, const CacheView &cv,
-                                                         uint32_t sampler, float fx, float fy, float fz) {
-    if (eb == 1) return sample_slot<uint8_t>(base, eb, cv, sampler, fx, fy, fz);
-    if (eb == 2) return sample_slot<uint16_t>(base, eb, cv, sampler, fx, fy, fz);
-    return sample_slot<float>(base, eb, cv, sampler, fx, fy, fz);
 }
 // Two interleaved u8 channels: each channel sampled with the one-channel
 // rule (corner mean of 8 voxels, or trilinear), voxel i channel k at byte 2i+k.
+template <uint32_t BS>
 __device__ __forceinline__ float2 sample_slot_two(const uint8_t *__restrict__ b, const CacheView &cv,
                                                   uint32_t sampler, float fx, float fy, float fz) {
-    const uint32_t B = cv.B, BB = B * B;
+    const uint32_t B = BS ? BS : cv.B, BB = B * B;
     if (sampler == GC_SAMPLER_REFERENCE) {
         uint32_t lx = cv.c + mod_beff(floor_u(fx), cv.Beff, cv.beff_magic);
         uint32_t ly = cv.c + mod_beff(floor_u(fy), cv.Beff, cv.beff_magic);
@@ -385,13 +389,13 @@ __device__ __forceinline__ float2 sample_slot_two(const uint8_t *__restrict__ b,
     }
     return make_float2(out[0], out[1]);
 }
-template <typename T>
+template <typename T, uint32_t BS>
 __device__ __forceinline__ typename SampleOf<T>::type sample_any(const uint8_t *base, uint32_t eb, const CacheView &cv,
                                                                  uint32_t sampler, float fx, float fy, float fz) {
     if constexpr (std::is_same<T, TwoU8>::value)
-        return sample_slot_two(base, cv, sampler, fx, fy, fz);
+        return sample_slot_two<BS>(base, cv, sampler, fx, fy, fz);
     else
-        return sample_slot<T>(base, eb, cv, sampler, fx, fy, fz);
+        return sample_slot<T, BS>(base, eb, cv, sampler, fx, fy, fz);
 }
 
 // The sample position of a ray position in normalized volume coordinates
@@ -415,21 +419,21 @@ __device__ __forceinline__ uint32_t entry_index(const CacheView &cv, const Level
     return cx + cy * cv.mx + cz * cv.mxy;
 }
 
-// Voxel sample of the resident brick in `slot` at level position p.
-template <typename T>
+// Voxel sample of the resident brick at `base` (its pool slot) at level position p.
+template <typename T, uint32_t BS>
 __device__ __forceinline__ typename SampleOf<T>::type sample_entry(const CacheView &cv, const LevelTables &lt,
                                                                    uint32_t sampler, const ViewParams &vp,
-                                                                   uint32_t lvl, uint32_t slot, V3 p) {
+                                                                   uint32_t lvl, const uint8_t *base, V3 p) {
     const float fx = p.x * lt.vvoxf[lvl][0];
     const float fy = p.y * lt.vvoxf[lvl][1];
     const float fz = p.z * lt.vvoxf[lvl][2];
-    return sample_any<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, vp.eb, cv, sampler, fx, fy, fz);
+    return sample_any<T, BS>(base, vp.eb, cv, sampler, fx, fy, fz);
 }
 
 // Page walk + sample at the normalized position np of cache level lvl (the
 // view's level base + its LOD): K_CacheManager::get_normalized
 // (K_CacheManager.hpp:265-361).
-template <typename T>
+template <typename T, uint32_t BS>
 __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt, uint32_t sampler,
                                      const ViewParams &vp, uint32_t lvl, uint32_t lvl_end, V3 np, Walk &w,
                                      typename SampleOf<T>::type &sample) {
@@ -448,16 +452,17 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
         w.invisible = (bins & vp.visible) == 0ull && (e.w == 1u || (e.w == 0u && cv.bins_user));
         if (e.w == 1u) {
             const uint32_t B = cv.B;
-            w.slot = cv.b_shift < 32u ? (e.x >> cv.b_shift) + (e.y >> cv.b_shift) * cv.sx +
-                                            (e.z >> cv.b_shift) * cv.sx * cv.sy
-                                      : e.x / B + (e.y / B) * cv.sx + (e.z / B) * cv.sx * cv.sy;
-            cv.usage[w.slot] = cv.ts;
+            const uint32_t slot = cv.b_shift < 32u ? (e.x >> cv.b_shift) + (e.y >> cv.b_shift) * cv.sx +
+                                                         (e.z >> cv.b_shift) * cv.sx * cv.sy
+                                                   : e.x / B + (e.y / B) * cv.sx + (e.z / B) * cv.sx * cv.sy;
+            cv.usage[slot] = cv.ts;
+            w.base = cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes;
         }
     }
     const uint32_t flag = w.flag;
     if (flag == 1u) {
         if (w.invisible) return kInvisible;  // no sample of this brick reaches the compositing threshold
-        sample = sample_entry<T>(cv, lt, sampler, vp, lvl, w.slot, p);
+        sample = sample_entry<T, BS>(cv, lt, sampler, vp, lvl, w.base, p);
         return kMapped;
     }
     if (flag == 3u) return kUnmapped;  // on its way (batched form): already requested
@@ -483,7 +488,7 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
             const uint32_t B = cv.B;
             const uint32_t slot = e2.x / B + (e2.y / B) * cv.sx + (e2.z / B) * cv.sx * cv.sy;
             cv.usage[slot] = cv.ts;
-            sample = sample_any<T>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, vp.eb, cv, sampler,
+            sample = sample_any<T, BS>(cv.pool + static_cast<uint64_t>(slot) * cv.slot_bytes, vp.eb, cv, sampler,
                                    qx * static_cast<float>(lt.vvox[l2][0]), qy * static_cast<float>(lt.vvox[l2][1]),
                                    qz * static_cast<float>(lt.vvox[l2][2]));
             return kCoarser;
@@ -625,7 +630,7 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
     r.t_lo = lod_keep_bound(r.sL, r.sU, r.endX, r.endY, r.tfar, r.lvl + 1 >= r.lvl_end);
     r.w.pidx = UINT_MAX;
     r.w.flag = 0;
-    r.w.slot = 0;
+    r.w.base = nullptr;
     r.w.invisible = false;
     r.maxOp = r.dvr ? 0.f : vp.state[4 * i];
     return true;
@@ -657,7 +662,7 @@ __device__ __forceinline__ void composite(Ray &r, float4 col) {
 
 // One iteration of the march loop (RayCasters.cu:122-188).  Returns false
 // when the loop ends.
-template <typename T>
+template <typename T, uint32_t BS>
 __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables &lt, Ray &r) {
     const ViewParams &vp = *r.vp;
     if (!((!r.dvr || r.fc.w < r.early) && r.t < r.tfar)) return false;
@@ -687,7 +692,7 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
         }
     }
     typename SampleOf<T>::type sample{};
-    const int st = fetch<T>(cv, lt, r.sampler, vp, r.lvl, r.lvl_end, np, r.w, sample);
+    const int st = fetch<T, BS>(cv, lt, r.sampler, vp, r.lvl, r.lvl_end, np, r.w, sample);
     if (st == kCoarser) r.coarse = true;  // sampled below; the image is a preview
     if (st == kMapped || st == kCoarser) ++r.nsamp;
     if (st == kInvisible) {  // the step of a sample whose opacity stays below 0.001
@@ -809,7 +814,7 @@ __device__ __forceinline__ void retire_warp(uint32_t *queue, uint32_t nwarps) {
 
 // Tile scheduler: a warp takes one tile (tile_w x 32/tile_w pixels) at a time
 // from the queue and marches its 32 rays to completion.
-template <typename T>
+template <typename T, uint32_t BS>
 __global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_kernel(const CacheView cv, const LevelTables lt,
                                                      const ViewParams *__restrict__ views, uint32_t nviews,
                                                      uint32_t total_tiles, uint32_t *queue, uint32_t nwarps) {
@@ -829,7 +834,7 @@ __global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_kernel(const
             Ray r;
             if (ray_setup<T>(lt, vp, x, y, r)) {
                 marched = ray_enters(r);
-                while (ray_step<T>(cv, lt, r)) {
+                while (ray_step<T, BS>(cv, lt, r)) {
                 }
                 unm = ray_finish(r);
                 coarse_any = r.coarse;
@@ -854,7 +859,7 @@ __global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_kernel(const
 // the next pixels of the queue (one warp-aggregated atomic), so a warp never
 // waits for its slowest ray.  Pixels are enumerated tile by tile, which keeps
 // consecutive grabs spatially close.
-template <typename T>
+template <typename T, uint32_t BS>
 __global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_pixels_kernel(const CacheView cv, const LevelTables lt,
                                                             const ViewParams *__restrict__ views, uint32_t nviews,
                                                             uint32_t total_tiles, uint32_t *queue, uint32_t nwarps) {
@@ -885,7 +890,7 @@ __global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_pixels_kerne
             if (started && static_cast<int>(lane) == leader)
                 atomicAdd(cv.samples + 1, static_cast<unsigned long long>(__popc(started)));
         }
-        if (active && !ray_step<T>(cv, lt, r)) {
+        if (active && !ray_step<T, BS>(cv, lt, r)) {
             active = false;
             if (ray_finish(r) && r.vp->status && *r.vp->status == 0u) atomicOr(r.vp->status, 1u);
             if (r.coarse && r.vp->status) atomicOr(r.vp->status, 2u);
@@ -896,21 +901,28 @@ __global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_pixels_kerne
     retire_warp(queue, nwarps);
 }
 
-// Kernel of a voxel kind (1, 2, 4 bytes, 0 mixed, kTwoChannelU8) and scheduler.
-void *march_kernel(uint32_t kind, bool pixels) {
+// Kernel of a voxel kind (1, 2, 4 bytes, 0 mixed, kTwoChannelU8), scheduler
+// and brick size (16 and 32 compiled for their size, others at run time).
+template <uint32_t BS>
+void *march_kernel_bs(uint32_t kind, bool pixels) {
     switch (kind) {
-        case 1: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<uint8_t>)
-                              : reinterpret_cast<void *>(render_kernel<uint8_t>);
-        case 2: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<uint16_t>)
-                              : reinterpret_cast<void *>(render_kernel<uint16_t>);
-        case 4: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<float>)
-                              : reinterpret_cast<void *>(render_kernel<float>);
-        case 0: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<MixedVoxel>)
-                              : reinterpret_cast<void *>(render_kernel<MixedVoxel>);
-        case 0x202: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<TwoU8>)
-                                  : reinterpret_cast<void *>(render_kernel<TwoU8>);
+        case 1: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<uint8_t, BS>)
+                              : reinterpret_cast<void *>(render_kernel<uint8_t, BS>);
+        case 2: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<uint16_t, BS>)
+                              : reinterpret_cast<void *>(render_kernel<uint16_t, BS>);
+        case 4: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<float, BS>)
+                              : reinterpret_cast<void *>(render_kernel<float, BS>);
+        case 0: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<MixedVoxel, BS>)
+                              : reinterpret_cast<void *>(render_kernel<MixedVoxel, BS>);
+        case 0x202: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<TwoU8, BS>)
+                                  : reinterpret_cast<void *>(render_kernel<TwoU8, BS>);
         default: return nullptr;
     }
+}
+void *march_kernel(uint32_t kind, bool pixels, uint32_t brick_size) {
+    if (brick_size == 16) return march_kernel_bs<16>(kind, pixels);
+    if (brick_size == 32) return march_kernel_bs<32>(kind, pixels);
+    return march_kernel_bs<0>(kind, pixels);
 }
 
 }  // namespace GC_MARCH_NS
@@ -1022,7 +1034,7 @@ void launch_view_bins(ViewParams *views_dev, uint32_t n, cudaStream_t s) {
 constexpr uint32_t kTwoChannelU8 = 0x202;
 static uint32_t voxel_kind(const CacheView &cv) { return cv.nc == 2 ? kTwoChannelU8 : cv.eb; }
 
-static RenderLaunch render_launch_config(uint32_t eb, uint32_t total_tiles) {
+static RenderLaunch render_launch_config(uint32_t eb, uint32_t brick_size, uint32_t total_tiles) {
     const RenderTuning tune = render_tuning();
     const uint32_t threads = tune.threads;
     GC_REQUIRE(threads == 64 || threads == 128 || threads == 256, "render threads must be 64, 128 or 256");
@@ -1030,12 +1042,13 @@ static RenderLaunch render_launch_config(uint32_t eb, uint32_t total_tiles) {
     // widths share the cache; two 8-bit channels with a 2D transfer function)
     // from the exact or the fast build
     const bool pix = tune.scheduler == 1, fast_build = tune.precision == 1;
-    void *kernel = fast_build ? fast::march_kernel(eb, pix) : exact::march_kernel(eb, pix);
+    void *kernel = fast_build ? fast::march_kernel(eb, pix, brick_size) : exact::march_kernel(eb, pix, brick_size);
     if (!kernel) fail(GC_ERR_UNSUPPORTED, "the ray caster supports one channel of 1, 2 or 4 bytes");
     const int slot = eb == 1 ? 0 : eb == 2 ? 1 : eb == 4 ? 2 : eb == 0 ? 3 : 4;
-    static int occupancy[2][2][5][3] = {};
+    static int occupancy[2][2][5][3][3] = {};
     const int tslot = threads == 64 ? 0 : (threads == 128 ? 1 : 2);
-    int &occ = occupancy[fast_build ? 1 : 0][pix ? 1 : 0][slot][tslot];
+    const int bslot = brick_size == 16 ? 0 : (brick_size == 32 ? 1 : 2);
+    int &occ = occupancy[fast_build ? 1 : 0][pix ? 1 : 0][slot][tslot][bslot];
     if (!occ) {
         int b = 0;
         GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, static_cast<int>(threads), 0));
@@ -1052,7 +1065,7 @@ void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams 
                    const ViewParams * /*views_host*/, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
                    uint32_t * /*err*/, cudaStream_t s) {
     if (total_tiles == 0) return;
-    const RenderLaunch L = render_launch_config(voxel_kind(cv), total_tiles);
+    const RenderLaunch L = render_launch_config(voxel_kind(cv), cv.B, total_tiles);
     uint32_t nwarps = L.grid * (L.threads / 32);
     void *args[] = {const_cast<CacheView *>(&cv), const_cast<LevelTables *>(&lt), &views_dev, &nviews, &total_tiles,
                     &queue, &nwarps};
@@ -1080,7 +1093,7 @@ void launch_render_graph(RenderGraph &g, const CacheView &cv, const LevelTables 
                          const ViewParams *views_pinned, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
                          cudaStream_t s) {
     if (total_tiles == 0) return;
-    const RenderLaunch L = render_launch_config(voxel_kind(cv), total_tiles);
+    const RenderLaunch L = render_launch_config(voxel_kind(cv), cv.B, total_tiles);
     uint32_t nwarps = L.grid * (L.threads / 32);
     const ViewParams *vd = views_dev;
     void *args[] = {const_cast<CacheView *>(&cv), const_cast<LevelTables *>(&lt), &vd, &nviews, &total_tiles,
