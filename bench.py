@@ -100,10 +100,10 @@ DIAG = 2.0 * math.sqrt(3.0)
 PIXEL_BYTES = 44  # RGBA 4 + t 4+4 + colour state 16+16 per pixel and launch
 # DRAM bytes (read + write) of the c2 roofline launch (view 42, converged, after
 # an L2 flush), from one ncu capture of this command:
-#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none --nvtx
-#       --nvtx-include roofline/ -k regex:render -c 2 python bench.py --steps 4 --warmup 3 --no-cpu-baseline --no-batched
+#   ncu --set full --clock-control none --nvtx --nvtx-include roofline/ -k regex:render_kernel -c 1
+#       python bench.py --roofline-only --steps 3 --tuning 0,16,128,0
 # (profiles/render_kernel_c2_1024x1024.md).  None for the other configs.
-ROOFLINE_TRAFFIC = {"c2": 107_531_000}
+ROOFLINE_TRAFFIC = {"c2": 106_319_872}
 BRICK_BINS = {}  # value bins of every brick, by brick-store address
 
 
@@ -601,7 +601,7 @@ def run_ours(args):
     # path (near, middle, far), in a cache of its own
     T = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
     n = cfg.get("frames", 120)
-    tuned = [autotune(gc, torch, T, [spec(f)[0] for f in (2, n // 6, n // 3)], args, per_view=True)]
+    tuned = [autotune(gc, torch, T, [spec(f)[0] for f in (n // 6, n // 2, 5 * n // 6)], args, per_view=True)]
     T.close()
     clocks = ClockSampler()
     clocks.start()
@@ -1013,6 +1013,40 @@ def run_stress(gc, torch, args, nviews=STRESS_VIEWS):
             "mip_build": {"s": round(t2 - t1, 4), "pyramid_gib": round(pyramid_bytes / 2**30, 1),
                           "gbs": round((2 * pyramid_bytes - level0) / (t2 - t1) / 1e9, 1),
                           "note": "every level read once and every coarser level written, over the build time"}}
+
+
+def run_preprocess_only(args):
+    """`--preprocess-only`: the device pre-processing of the c2 volume type
+    (u16, B16, covering 1) at --size^3 with the brick store kept on the device
+    (twice; the second timed): mip pyramid, bricking of every level, value
+    bins.  For profiler captures of the mip and bricking kernels (1024^3: about
+    8 GB on the device).  Prints one JSON line with the stage timings."""
+    import torch
+
+    import gcgb300 as gc
+
+    cfg = CONFIGS["c2"]
+    n = args.size
+    size = (n, n, n)
+    vol = gc.volume_desc(size, cfg["B"], cfg["c"], cfg["bpc"], 1, (1, 1, 1))
+    layout = gc.compute_layout(vol)
+    blobs = gc.generator_blobs(cfg["seed"], cfg["nblobs"], size, cfg["sigma"][0] * n / 2048,
+                               cfg["sigma"][1] * n / 2048, cfg["amp"][0], cfg["amp"][1])
+    d = torch.empty(n ** 3 * cfg["bpc"], dtype=torch.uint8, device="cuda")
+    gc.generate_volume(gc.make_generator(size, cfg["bpc"], cfg["seed"], blobs, cfg["noise"]), d.data_ptr())
+    tm = {}
+    for _ in range(2):
+        bricks, _, _ = gc.pre_process(vol, layout, d, timings=tm, store="device", value_bins=[])
+        del bricks
+    torch.cuda.synchronize()
+    peak = measured_peak()[0]
+    mip_gbs = (2 * tm["pyramid_bytes"] - tm["level0_bytes"]) / tm["mip_s"] / 1e9
+    brick_gbs = (tm["pyramid_bytes"] + tm["store_bytes"]) / tm["brick_s"] / 1e9
+    print(json.dumps({"preprocess_only": {"volume": f"{n}^3 u16, B16, covering 1", "mip_s": round(tm["mip_s"], 5),
+                                          "mip_gbs": round(mip_gbs, 1), "mip_frac": round(mip_gbs / peak, 3),
+                                          "bricking_s": round(tm["brick_s"], 5), "bricking_gbs": round(brick_gbs, 1),
+                                          "bricking_frac": round(brick_gbs / peak, 3),
+                                          "value_bins_s": round(tm["flags_bins_s"], 5)}}), flush=True)
 
 
 def run_roofline_only(args):
@@ -1694,6 +1728,9 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="c3: skip the plain loop over the same views")
     ap.add_argument("--roofline-only", action="store_true",
                     help="only the c2 roofline launch, --steps times, bricks from the device pyramid (for ncu)")
+    ap.add_argument("--preprocess-only", action="store_true",
+                    help="only the device pre-processing (mip, bricks, bins) of a --size^3 u16 volume (for ncu)")
+    ap.add_argument("--size", type=int, default=2048, help="--preprocess-only: volume edge")
     ap.add_argument("--tuning", default=None,
                     help="ray-caster launch tuning 'scheduler,tile_w,threads,blocks_per_sm' for --roofline-only")
     args = ap.parse_args()
@@ -1721,6 +1758,8 @@ def main():
         run_c5(args)
     elif args.roofline_only:
         run_roofline_only(args)
+    elif args.preprocess_only:
+        run_preprocess_only(args)
     else:
         run_ours(args)
 
