@@ -427,6 +427,26 @@ int refgpu_mipmap(void) {
     });
 }
 
+// Mipmapper::process then process_bricking of every level (one thread per
+// level, LZ4 brick files, as Application::pre_process runs them), each timed
+// on the host clock: the reference's preprocessor stages for the bench.
+int refgpu_preprocess_timed(double *mip_s, double *brick_s) {
+    return guarded([&] {
+        if (!mip_s || !brick_s) throw std::runtime_error("null argument");
+        tdns::data::MetaData md;
+        tdns::preprocessor::Mipmapper mipmapper;
+        const auto t0 = std::chrono::steady_clock::now();
+        mipmapper.process(md);
+        const auto t1 = std::chrono::steady_clock::now();
+        if (md.get_initial_levels().empty()) throw std::runtime_error("Mipmapper::process produced no level");
+        std::vector<Vector3ui> levels = md.get_initial_levels();
+        brick_levels(md, levels);
+        const auto t2 = std::chrono::steady_clock::now();
+        *mip_s = std::chrono::duration<double>(t1 - t0).count();
+        *brick_s = std::chrono::duration<double>(t2 - t1).count();
+    });
+}
+
 // load_volume_configuration + MetaData::load + CacheManager<T> (Application::run,
 // Application.cu:43-133) with a pool of cache_size slots.
 int refgpu_open(const char *cfg_path, const uint32_t cache_size[3], int gpu) {

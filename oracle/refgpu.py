@@ -42,6 +42,7 @@ def load():
         lib.refgpu_config_load.argtypes = [C.c_char_p]
         lib.refgpu_preprocess.argtypes = [C.c_float]
         lib.refgpu_mipmap.argtypes = []
+        lib.refgpu_preprocess_timed.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
         lib.refgpu_open.argtypes = [C.c_char_p, u32p, C.c_int]
         lib.refgpu_render.argtypes = [C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.c_float,
                                       C.POINTER(C.c_float), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -108,6 +109,14 @@ class RefGpu:
         """Mipmapper::process alone on the volume file (the mip files)."""
         _check(self.lib.refgpu_config_load(self.cfg.encode()))
         _check(self.lib.refgpu_mipmap())
+
+    def preprocess_timed(self):
+        """Mipmapper::process then process_bricking of every level (LZ4 brick
+        files, one thread per level) on the volume file; (mip s, bricking s)."""
+        _check(self.lib.refgpu_config_load(self.cfg.encode()))
+        m, b = C.c_double(0.0), C.c_double(0.0)
+        _check(self.lib.refgpu_preprocess_timed(C.byref(m), C.byref(b)))
+        return m.value, b.value
 
     def mip_level(self, level, dims):
         dt = np.uint8 if self.eb == 1 else np.uint16
