@@ -287,21 +287,9 @@ __global__ void install_evict_kernel(InstallArgs a, const LevelTables lt) {
 // over its voxels (covering included), normalized like the samplers, widened
 // by one bin on either side.  `at(v)` gives the address of voxel v; one
 // block per brick (up to 256 threads); the result is valid in thread 0.
-template <class At>
-__device__ unsigned long long block_value_bins(uint32_t nvox, uint32_t eb, At at) {
-    float lo = 3.4e38f, hi = -3.4e38f;
-    for (uint32_t v = threadIdx.x; v < nvox; v += blockDim.x) {
-        const uint8_t *p = at(v);
-        float x;
-        if (eb == 1)
-            x = static_cast<float>(*p) * (1.0f / 255.0f);
-        else if (eb == 2)
-            x = static_cast<float>(*reinterpret_cast<const uint16_t *>(p)) * (1.0f / 65535.0f);
-        else
-            x = *reinterpret_cast<const float *>(p);
-        lo = fminf(lo, x);
-        hi = fmaxf(hi, x);
-    }
+// The block's value bins from each thread's min and max (normalized like the
+// samplers); the result is valid in thread 0.
+__device__ unsigned long long block_bins_from(float lo, float hi) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
@@ -329,6 +317,47 @@ __device__ unsigned long long block_value_bins(uint32_t nvox, uint32_t eb, At at
         bins = upto & ~((1ull << b0) - 1ull);
     }
     return bins;
+}
+template <class At>
+__device__ unsigned long long block_value_bins(uint32_t nvox, uint32_t eb, At at) {
+    float lo = 3.4e38f, hi = -3.4e38f;
+    for (uint32_t v = threadIdx.x; v < nvox; v += blockDim.x) {
+        const uint8_t *p = at(v);
+        float x;
+        if (eb == 1)
+            x = static_cast<float>(*p) * (1.0f / 255.0f);
+        else if (eb == 2)
+            x = static_cast<float>(*reinterpret_cast<const uint16_t *>(p)) * (1.0f / 65535.0f);
+        else
+            x = *reinterpret_cast<const float *>(p);
+        lo = fminf(lo, x);
+        hi = fmaxf(hi, x);
+    }
+    return block_bins_from(lo, hi);
+}
+
+// Min and max over the voxels of a 16-byte chunk, into (lo, hi) as the
+// samplers normalize them (integer min / max first: the normalization is
+// monotone, so the result is block_value_bins').
+__device__ __forceinline__ void chunk_range(uint4 c, uint32_t eb, float &lo, float &hi) {
+    if (eb == 1) {
+        const uint32_t mn = __vminu4(__vminu4(c.x, c.y), __vminu4(c.z, c.w));
+        const uint32_t mx = __vmaxu4(__vmaxu4(c.x, c.y), __vmaxu4(c.z, c.w));
+        const uint32_t mn1 = min(min(mn & 0xffu, (mn >> 8) & 0xffu), min((mn >> 16) & 0xffu, mn >> 24));
+        const uint32_t mx1 = max(max(mx & 0xffu, (mx >> 8) & 0xffu), max((mx >> 16) & 0xffu, mx >> 24));
+        lo = fminf(lo, static_cast<float>(mn1) * (1.0f / 255.0f));
+        hi = fmaxf(hi, static_cast<float>(mx1) * (1.0f / 255.0f));
+    } else if (eb == 2) {
+        const uint32_t mn = __vminu2(__vminu2(c.x, c.y), __vminu2(c.z, c.w));
+        const uint32_t mx = __vmaxu2(__vmaxu2(c.x, c.y), __vmaxu2(c.z, c.w));
+        lo = fminf(lo, static_cast<float>(min(mn & 0xffffu, mn >> 16)) * (1.0f / 65535.0f));
+        hi = fmaxf(hi, static_cast<float>(max(mx & 0xffffu, mx >> 16)) * (1.0f / 65535.0f));
+    } else {
+        lo = fminf(fminf(lo, fminf(__uint_as_float(c.x), __uint_as_float(c.y))),
+                   fminf(__uint_as_float(c.z), __uint_as_float(c.w)));
+        hi = fmaxf(fmaxf(hi, fmaxf(__uint_as_float(c.x), __uint_as_float(c.y))),
+                   fmaxf(__uint_as_float(c.z), __uint_as_float(c.w)));
+    }
 }
 
 // Value bins of every brick of one level, read from the level's big bricks
@@ -389,15 +418,46 @@ __global__ void __launch_bounds__(256) install_place_kernel(InstallArgs a, const
     uint8_t *dst = a.pool + static_cast<uint64_t>(slot) * a.slot_bytes;
     const uint32_t row_bytes = B * eb;
     const uint32_t rows = B * B;
-    if (row_bytes % 16 == 0 && (reinterpret_cast<uintptr_t>(src) % 16 == 0) && ((bvx * eb) % 16 == 0)) {
-        const uint32_t vec_per_row = row_bytes / 16;
-        for (uint32_t v = threadIdx.x; v < rows * vec_per_row; v += blockDim.x) {
-            const uint32_t r = v / vec_per_row, q = v % vec_per_row;
-            const uint32_t ly = r % B, lz = r / B;
-            const uint64_t soff = ((static_cast<uint64_t>(oz + lz) * bvy + (oy + ly)) * bvx + ox) * eb + q * 16;
-            const uint4 val = __ldcs(reinterpret_cast<const uint4 *>(src + soff));
-            reinterpret_cast<uint4 *>(dst + static_cast<uint64_t>(r) * row_bytes)[q] = val;
+    const uint32_t vec_per_row = row_bytes / 16;
+    const bool pow2 = (B & (B - 1u)) == 0u && (vec_per_row & (vec_per_row - 1u)) == 0u;
+    if (row_bytes % 16 == 0 && pow2 && (reinterpret_cast<uintptr_t>(src) % 16 == 0) && ((bvx * eb) % 16 == 0)) {
+        // 16-byte chunks, four loads in flight per thread before their
+        // stores; the brick's value range is taken from the loaded chunks
+        // (one read of the brick for both)
+        const uint32_t qs = __ffs(vec_per_row) - 1u, bs = __ffs(B) - 1u;
+        const uint32_t nvec = rows * vec_per_row;
+        const bool bins = a.slot_bins && a.nc == 1;
+        float lo = 3.4e38f, hi = -3.4e38f;
+        for (uint32_t v0 = threadIdx.x; v0 < nvec; v0 += 4u * blockDim.x) {
+            uint4 val[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t v = v0 + u * blockDim.x;
+                if (v < nvec) {
+                    const uint32_t r = v >> qs, q = v & (vec_per_row - 1u);
+                    const uint32_t ly = r & (B - 1u), lz = r >> bs;
+                    const uint64_t soff =
+                        ((static_cast<uint64_t>(oz + lz) * bvy + (oy + ly)) * bvx + ox) * eb + q * 16u;
+                    val[u] = __ldcs(reinterpret_cast<const uint4 *>(src + soff));
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t v = v0 + u * blockDim.x;
+                if (v < nvec) {
+                    reinterpret_cast<uint4 *>(dst)[v] = val[u];
+                    if (bins) chunk_range(val[u], eb, lo, hi);
+                }
+            }
         }
+        if (!a.slot_bins) return;
+        if (a.nc != 1) {
+            if (threadIdx.x == 0) a.slot_bins[slot] = ~0ull;  // several channels: never skipped
+            return;
+        }
+        const unsigned long long b2 = block_bins_from(lo, hi);
+        if (threadIdx.x == 0) a.slot_bins[slot] = b2;
+        return;
     } else {
         const uint32_t nbytes = rows * row_bytes;
         for (uint32_t v = threadIdx.x; v < nbytes; v += blockDim.x) {
