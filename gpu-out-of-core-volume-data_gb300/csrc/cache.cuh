@@ -13,6 +13,12 @@
 //   pool   bytes             slot-major bricks: slot s = x + y*sx + z*sx*sy holds
 //                            B^3 voxels x-fastest (the reference uses a cudaArray
 //                            of (sx*B, sy*B, sz*B) voxels)
+// Two-level directory (pt_block P > 0) instead of mrpd:
+//   top    uint32[tx*ty*tz]  one word per P^3 bricks of a level, levels packed
+//                            along x: table slot << 1 | 1, or 0
+//   table  uint4[slots*P^3]  brick entries of each table slot's block, x fastest
+//   pt_usage / pt_order[2] / pt_keys   the table pool's usage words, LRU order
+//                            and the block each slot holds
 #pragma once
 
 #include <cstdint>
@@ -37,10 +43,35 @@ struct LevelTables {
     uint32_t bb[kMaxCacheLevels][3];      // big-brick size (in bricks) of the level's volume
     float nbf[kMaxCacheLevels][3];        // nb and vvox as floats (exact: both < 2^24), for the
     float vvoxf[kMaxCacheLevels][3];      // ray caster's per-sample page walk
+    uint32_t pt_off[kMaxCacheLevels];     // two-level directory: x offset of each level's words
 };
 
+// Two-level page directory (the page-table hierarchy of CacheManager with one
+// table cache, CacheManager.hpp:151-236): brick (x, y, z) of level l -- x
+// counted inside the level -- has its entry in the block of directory word
+// pt_word(), at pt_local() inside it.  shift = 0: one-level directory.
+struct PageTable {
+    uint32_t *top;        // per directory word: table slot << 1 | 1, or 0
+    uint4 *table;         // brick entries, 1 << (3 * shift) per table slot
+    uint32_t *usage;      // last-use word per table slot
+    uint32_t shift;       // log2(P)
+    uint32_t tx, txy;     // directory words per row, per slice
+};
+__host__ __device__ __forceinline__ uint32_t pt_word(const PageTable &pt, const LevelTables &lt, uint32_t l,
+                                                     uint32_t x, uint32_t y, uint32_t z) {
+    return lt.pt_off[l] + (x >> pt.shift) + (y >> pt.shift) * pt.tx + (z >> pt.shift) * pt.txy;
+}
+__host__ __device__ __forceinline__ uint32_t pt_local(const PageTable &pt, uint32_t x, uint32_t y, uint32_t z) {
+    const uint32_t m = (1u << pt.shift) - 1u;
+    return (x & m) | ((y & m) << pt.shift) | ((z & m) << (2u * pt.shift));
+}
+__host__ __device__ __forceinline__ uint64_t pt_entry(const PageTable &pt, uint32_t slot, uint32_t local) {
+    return (static_cast<uint64_t>(slot) << (3u * pt.shift)) + local;
+}
+
 struct CacheView {
-    uint4 *mrpd;
+    uint4 *mrpd;          // one-level directory (null with a two-level one)
+    PageTable pt;
     uint32_t *req;
     uint32_t *usage;
     const uint8_t *pool;
@@ -166,6 +197,14 @@ uint32_t lookback_tiles(uint64_t n);
 
 struct InstallArgs {
     uint4 *mrpd;
+    PageTable pt;              // two-level directory (pt.shift > 0; mrpd is then null)
+    uint32_t pt_slots;
+    const uint32_t *pt_order;  // the table pool's current LRU order
+    uint4 *pt_keys;            // per table slot: first brick (x, y, z) of its block and the level, or all ones
+    uint32_t *pt_claim;        // per directory word: lowest list index claiming it (~0 between installs)
+    uint32_t *pt_word_of;      // per list element: the directory word it claims, or ~0
+    uint2 *pt_jobs;            // claimed words in list order: {word, element}
+    uint32_t *pt_njobs;
     uint32_t mx, my;
     uint64_t nentries;
     const uint32_t *order;     // current LRU order
@@ -194,7 +233,14 @@ void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s)
 // bits) everywhere, then the bins of every resident brick at its entry.
 void launch_live_bins(const LevelTables &lt, const float4 *slot_vpos, const uint32_t *slot_level,
                       const unsigned long long *slot_bins, uint32_t nslots, uint32_t mx, uint32_t my,
-                      uint64_t nentries, unsigned long long *entry_bins, cudaStream_t s);
+                      uint64_t nentries, unsigned long long *entry_bins, const PageTable &pt, uint32_t sx,
+                      uint32_t sy, uint32_t B, cudaStream_t s);
+// The brick entries of a two-level directory as the flat directory would
+// hold them (0 where the block is not resident), for state dumps.
+void launch_pt_flatten(const PageTable &pt, const LevelTables &lt, uint32_t mx, uint32_t my, uint64_t nentries,
+                       uint4 *out, cudaStream_t s);
+// Table pool: slots in raster order, no block held.
+void launch_pt_init(uint32_t *order, uint4 *keys, uint32_t nslots, cudaStream_t s);
 // Copies brick i (src[i] = {device-readable host address, bytes}) to
 // dst + i * stride; vec16: every address, size and the stride are multiples
 // of 16.
@@ -225,13 +271,14 @@ struct RenderTuning {
 RenderTuning &render_tuning();
 // Ray-caster kernels of a voxel kind (1, 2, 4 bytes; 0 mixed widths; 0x202
 // two 8-bit channels), scheduler and brick size (16 and 32 have kernels
-// compiled for them), from the exact build (render.cu) or the fast build
-// (render_fast.cu); nullptr for an unsupported kind.
+// compiled for them; a two-level page directory has kernels of its own),
+// from the exact build (render.cu) or the fast build (render_fast.cu);
+// nullptr for an unsupported kind.
 namespace exact {
-void *march_kernel(uint32_t kind, bool pixels, uint32_t brick_size);
+void *march_kernel(uint32_t kind, bool pixels, uint32_t brick_size, bool two_level);
 }
 namespace fast {
-void *march_kernel(uint32_t kind, bool pixels, uint32_t brick_size);
+void *march_kernel(uint32_t kind, bool pixels, uint32_t brick_size, bool two_level);
 }
 // Fills ViewParams::visible of n device views from their transfer functions.
 void launch_view_bins(ViewParams *views_dev, uint32_t n, cudaStream_t s);

@@ -256,6 +256,26 @@ __device__ __forceinline__ uint64_t mrpd_index(const LevelTables &lt, uint32_t l
     const uint32_t z = static_cast<uint32_t>(__fmul_rn(vz, static_cast<float>(lt.nb[level][2])));
     return x + static_cast<uint64_t>(y) * mx + static_cast<uint64_t>(z) * mx * my;
 }
+// The same brick as (x inside the level, y, z): its place in a two-level directory.
+__device__ __forceinline__ uint3 brick_at(const LevelTables &lt, uint32_t level, float vx, float vy, float vz) {
+    return make_uint3(static_cast<uint32_t>(__fmul_rn(vx, static_cast<float>(lt.nb[level][0]))),
+                      static_cast<uint32_t>(__fmul_rn(vy, static_cast<float>(lt.nb[level][1]))),
+                      static_cast<uint32_t>(__fmul_rn(vz, static_cast<float>(lt.nb[level][2]))));
+}
+__device__ __forceinline__ bool brick_inside(const LevelTables &lt, uint32_t level, uint3 q) {
+    return q.x < lt.nb[level][0] && q.y < lt.nb[level][1] && q.z < lt.nb[level][2];
+}
+// The brick entry of q in a two-level directory, or null when its block is
+// not resident.
+__device__ __forceinline__ uint4 *pt_entry_of(const PageTable &pt, const LevelTables &lt, uint32_t level, uint3 q) {
+    const uint32_t t = pt.top[pt_word(pt, lt, level, q.x, q.y, q.z)];
+    if (!(t & 1u)) return nullptr;
+    return pt.table + pt_entry(pt, t >> 1, pt_local(pt, q.x, q.y, q.z));
+}
+// Page-directory entry (x, y, z, 1) of pool slot `slot`.
+__device__ __forceinline__ uint4 slot_entry(uint32_t slot, uint32_t sx, uint32_t sy, uint32_t B) {
+    return make_uint4((slot % sx) * B, ((slot / sx) % sy) * B, (slot / (sx * sy)) * B, 1u);
+}
 
 // compute_volume_position (CacheManagerKernels.cu:75-86):
 // x / (V.x * (1 / (B - 2c))) + FLT_EPSILON.
@@ -276,11 +296,24 @@ __global__ void install_evict_kernel(InstallArgs a, const LevelTables lt) {
     const uint32_t slot = a.order[a.nslots - a.n_nonempty + i];
     const float4 vp = a.slot_vpos[slot];
     if (vp.x < 0.f) return;  // slot never held a brick
-    const uint64_t e = mrpd_index(lt, a.slot_level[slot], vp.x, vp.y, vp.z, a.mx, a.my);
-    if (e < a.nentries) {
+    const uint32_t level = a.slot_level[slot];
+    const uint64_t e = mrpd_index(lt, level, vp.x, vp.y, vp.z, a.mx, a.my);
+    if (e >= a.nentries) return;
+    if (a.pt.shift) {
+        // Two levels: the entry is cleared only where it still names this
+        // slot -- after its block was evicted the brick may be unreachable,
+        // or resident again in another slot.
+        const uint3 q = brick_at(lt, level, vp.x, vp.y, vp.z);
+        if (!brick_inside(lt, level, q)) return;
+        uint4 *pe = pt_entry_of(a.pt, lt, level, q);
+        if (!pe) return;
+        const uint4 cur = *pe, mine = slot_entry(slot, a.sx, a.sy, a.B);
+        if (cur.w != 1u || cur.x != mine.x || cur.y != mine.y || cur.z != mine.z) return;
+        *pe = make_uint4(0, 0, 0, 0);
+    } else {
         a.mrpd[e] = make_uint4(0, 0, 0, 0);
-        a.entry_bins[e] = a.user_bins ? a.user_bins[e] : ~0ull;
     }
+    a.entry_bins[e] = a.user_bins ? a.user_bins[e] : ~0ull;
 }
 
 // Value range of a brick as value bins (empty-space skipping): min and max
@@ -495,21 +528,120 @@ __global__ void install_owner_kernel(InstallArgs a, const LevelTables lt, float 
     if (c < a.nentries) atomicMin(a.owner + c, i);
 }
 
-__global__ void install_reference_kernel(InstallArgs a) {
+__global__ void install_reference_kernel(InstallArgs a, const LevelTables lt, float one_over_beff) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const uint64_t c = a.coords[i];
     if (c >= a.nentries || a.owner[c] != i) return;  // an earlier element names the same entry
     a.owner[c] = 0xffffffffu;  // later readers see a value that is not their index either way
-    const uint4 e = a.mrpd[c];
+    uint4 *pe = a.mrpd + c;
+    if (a.pt.shift) {
+        // two levels: the entry lives in the block of its directory word (none
+        // when the table pool had no slot left for it: the brick stays unmapped)
+        const uint4 b = a.asked[i];
+        const float4 v = brick_origin(lt, b, one_over_beff);
+        const uint3 q = brick_at(lt, b.w, v.x, v.y, v.z);
+        if (!brick_inside(lt, b.w, q)) return;
+        pe = pt_entry_of(a.pt, lt, b.w, q);
+        if (!pe) return;
+    }
+    const uint4 e = *pe;
     if (e.w == 1u || e.w == 2u) return;  // mapped or empty already (3 = in flight: install it)
     if (i < a.n_nonempty) {
         const uint32_t slot = a.order[a.nslots - a.n_nonempty + i];
-        const uint32_t sx = slot % a.sx, sy = (slot / a.sx) % a.sy, sz = slot / (a.sx * a.sy);
-        a.mrpd[c] = make_uint4(sx * a.B, sy * a.B, sz * a.B, 1u);
+        *pe = slot_entry(slot, a.sx, a.sy, a.B);
         a.entry_bins[c] = a.slot_bins[slot];
     } else {
-        a.mrpd[c] = make_uint4(0, 0, 0, 2u);
+        *pe = make_uint4(0, 0, 0, 2u);
+    }
+}
+
+// Two-level directory: table blocks for the new bricks.  Each element that
+// acts for its entry (the owner) and whose directory word has no block claims
+// the word; the lowest element index wins.
+__global__ void install_pt_claim_kernel(InstallArgs a, const LevelTables lt, float one_over_beff) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    uint32_t word = 0xffffffffu;
+    const uint64_t c = a.coords[i];
+    if (c < a.nentries && a.owner[c] == i) {
+        const uint4 b = a.asked[i];
+        const float4 v = brick_origin(lt, b, one_over_beff);
+        const uint3 q = brick_at(lt, b.w, v.x, v.y, v.z);
+        const uint32_t w = pt_word(a.pt, lt, b.w, q.x, q.y, q.z);
+        if (brick_inside(lt, b.w, q) && !(a.pt.top[w] & 1u)) {
+            word = w;
+            atomicMin(a.pt_claim + w, i);
+        }
+    }
+    a.pt_word_of[i] = word;
+}
+
+// The claimed words in list order (one block): the k-th winner gets the k-th
+// of the table slots taken from the LRU tail.
+__global__ void __launch_bounds__(1024) install_pt_rank_kernel(InstallArgs a) {
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_base;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    if (threadIdx.x == 0) s_base = 0;
+    __syncthreads();
+    for (uint32_t i0 = 0; i0 < a.n; i0 += blockDim.x) {
+        const uint32_t i = i0 + threadIdx.x;
+        const uint32_t w = i < a.n ? a.pt_word_of[i] : 0xffffffffu;
+        const bool win = w != 0xffffffffu && a.pt_claim[w] == i;
+        const uint32_t bal = __ballot_sync(0xffffffffu, win);
+        if (lane == 0) s_warp[warp] = __popc(bal);
+        __syncthreads();
+        uint32_t before = s_base;
+        for (uint32_t k = 0; k < warp; ++k) before += s_warp[k];
+        if (win) a.pt_jobs[before + __popc(bal & ((1u << lane) - 1u))] = make_uint2(w, i);
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (uint32_t k = 0; k < nwarps; ++k) s_base += s_warp[k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *a.pt_njobs = s_base;
+}
+
+// One block per claimed word: the table slot at LRU-tail position k leaves
+// the block it held (its directory word cleared, the value bins of its mapped
+// entries reverted), is cleared and takes the claimed word.  Claims beyond
+// the table pool's size get no slot.
+__global__ void __launch_bounds__(256) install_pt_apply_kernel(InstallArgs a, const LevelTables lt,
+                                                               float one_over_beff) {
+    const uint32_t m = *a.pt_njobs, k = blockIdx.x;
+    if (k >= m) return;
+    const uint2 job = a.pt_jobs[k];
+    const uint32_t npt = min(m, a.pt_slots);
+    if (k >= npt) {
+        if (threadIdx.x == 0) a.pt_claim[job.x] = 0xffffffffu;
+        return;
+    }
+    const uint32_t slot = a.pt_order[a.pt_slots - npt + k];
+    const uint32_t P = 1u << a.pt.shift, P3 = P * P * P;
+    uint4 *blk = a.pt.table + pt_entry(a.pt, slot, 0);
+    const uint4 old = a.pt_keys[slot];
+    if (old.w != 0xffffffffu) {
+        for (uint32_t j = threadIdx.x; j < P3; j += blockDim.x) {
+            if (blk[j].w != 1u) continue;
+            const uint32_t dx = j & (P - 1u), dy = (j >> a.pt.shift) & (P - 1u), dz = j >> (2u * a.pt.shift);
+            const uint64_t e = static_cast<uint64_t>(lt.off[old.w] + old.x + dx) +
+                               static_cast<uint64_t>(old.y + dy) * a.mx +
+                               static_cast<uint64_t>(old.z + dz) * a.mx * a.my;
+            a.entry_bins[e] = a.user_bins ? a.user_bins[e] : ~0ull;
+        }
+    }
+    __syncthreads();  // the old entries are read before they are cleared
+    for (uint32_t j = threadIdx.x; j < P3; j += blockDim.x) blk[j] = make_uint4(0, 0, 0, 0);
+    if (threadIdx.x == 0) {
+        if (old.w != 0xffffffffu) a.pt.top[pt_word(a.pt, lt, old.w, old.x, old.y, old.z)] = 0u;
+        const uint4 b = a.asked[job.y];
+        const float4 v = brick_origin(lt, b, one_over_beff);
+        const uint3 q = brick_at(lt, b.w, v.x, v.y, v.z);
+        const uint32_t msk = ~(P - 1u);
+        a.pt_keys[slot] = make_uint4(q.x & msk, q.y & msk, q.z & msk, b.w);
+        a.pt.top[job.x] = slot << 1 | 1u;
+        a.pt_claim[job.x] = 0xffffffffu;
     }
 }
 
@@ -555,20 +687,32 @@ void launch_miss_compact(const uint32_t *req, uint64_t nscan, uint32_t ts, uint3
 __global__ void live_bins_kernel(const LevelTables lt, const float4 *__restrict__ slot_vpos,
                                  const uint32_t *__restrict__ slot_level,
                                  const unsigned long long *__restrict__ slot_bins, uint32_t nslots, uint32_t mx,
-                                 uint32_t my, uint64_t nentries, unsigned long long *entry_bins) {
+                                 uint32_t my, uint64_t nentries, unsigned long long *entry_bins, const PageTable pt,
+                                 uint32_t sx, uint32_t sy, uint32_t B) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += gridDim.x * blockDim.x) {
         const float4 vp = slot_vpos[i];
         if (vp.x < 0.f) continue;  // slot never held a brick
-        const uint64_t e = mrpd_index(lt, slot_level[i], vp.x, vp.y, vp.z, mx, my);
-        if (e < nentries) entry_bins[e] = slot_bins[i];
+        const uint32_t level = slot_level[i];
+        const uint64_t e = mrpd_index(lt, level, vp.x, vp.y, vp.z, mx, my);
+        if (e >= nentries) continue;
+        if (pt.shift) {  // two levels: only a slot its entry names is live
+            const uint3 q = brick_at(lt, level, vp.x, vp.y, vp.z);
+            if (!brick_inside(lt, level, q)) continue;
+            const uint4 *pe = pt_entry_of(pt, lt, level, q);
+            const uint4 mine = slot_entry(i, sx, sy, B);
+            if (!pe || pe->w != 1u || pe->x != mine.x || pe->y != mine.y || pe->z != mine.z) continue;
+        }
+        entry_bins[e] = slot_bins[i];
     }
 }
 
 void launch_live_bins(const LevelTables &lt, const float4 *slot_vpos, const uint32_t *slot_level,
                       const unsigned long long *slot_bins, uint32_t nslots, uint32_t mx, uint32_t my,
-                      uint64_t nentries, unsigned long long *entry_bins, cudaStream_t s) {
+                      uint64_t nentries, unsigned long long *entry_bins, const PageTable &pt, uint32_t sx,
+                      uint32_t sy, uint32_t B, cudaStream_t s) {
     const uint32_t grid = std::max(1u, std::min<uint32_t>(div_up(nslots, 256), static_cast<uint32_t>(sm_count()) * 4));
-    live_bins_kernel<<<grid, 256, 0, s>>>(lt, slot_vpos, slot_level, slot_bins, nslots, mx, my, nentries, entry_bins);
+    live_bins_kernel<<<grid, 256, 0, s>>>(lt, slot_vpos, slot_level, slot_bins, nslots, mx, my, nentries, entry_bins,
+                                          pt, sx, sy, B);
     GC_CUDA(cudaGetLastError());
     count_launch();
 }
@@ -587,7 +731,58 @@ void launch_install(const InstallArgs &a, const LevelTables &lt, cudaStream_t s)
     install_owner_kernel<<<div_up(a.n, 256u), 256, 0, s>>>(a, lt, one_over_beff);
     GC_CUDA(cudaGetLastError());
     count_launch();
-    install_reference_kernel<<<div_up(a.n, 256u), 256, 0, s>>>(a);
+    if (a.pt.shift) {
+        install_pt_claim_kernel<<<div_up(a.n, 256u), 256, 0, s>>>(a, lt, one_over_beff);
+        GC_CUDA(cudaGetLastError());
+        install_pt_rank_kernel<<<1, 1024, 0, s>>>(a);
+        GC_CUDA(cudaGetLastError());
+        install_pt_apply_kernel<<<a.n, 256, 0, s>>>(a, lt, one_over_beff);
+        GC_CUDA(cudaGetLastError());
+        count_launch(3);
+    }
+    install_reference_kernel<<<div_up(a.n, 256u), 256, 0, s>>>(a, lt, one_over_beff);
+    GC_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+__global__ void pt_flatten_kernel(const PageTable pt, const LevelTables lt, uint32_t mx, uint32_t my,
+                                  uint64_t nentries, uint4 *out) {
+    for (uint64_t e = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; e < nentries;
+         e += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint32_t X = static_cast<uint32_t>(e % mx), y = static_cast<uint32_t>((e / mx) % my);
+        const uint32_t z = static_cast<uint32_t>(e / (static_cast<uint64_t>(mx) * my));
+        uint4 v = make_uint4(0, 0, 0, 0);
+        for (uint32_t l = 0; l < lt.nlevels; ++l) {
+            if (X < lt.off[l] || X >= lt.off[l] + lt.nb[l][0]) continue;
+            const uint3 q = make_uint3(X - lt.off[l], y, z);
+            if (brick_inside(lt, l, q)) {
+                const uint32_t t = pt.top[pt_word(pt, lt, l, q.x, q.y, q.z)];
+                if (t & 1u) v = pt.table[pt_entry(pt, t >> 1, pt_local(pt, q.x, q.y, q.z))];
+            }
+            break;
+        }
+        out[e] = v;
+    }
+}
+
+void launch_pt_flatten(const PageTable &pt, const LevelTables &lt, uint32_t mx, uint32_t my, uint64_t nentries,
+                       uint4 *out, cudaStream_t s) {
+    const uint32_t grid =
+        static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>((nentries + 255) / 256, sm_count() * 8ull)));
+    pt_flatten_kernel<<<grid, 256, 0, s>>>(pt, lt, mx, my, nentries, out);
+    GC_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+__global__ void pt_init_kernel(uint32_t *order, uint4 *keys, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        order[i] = i;
+        keys[i] = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+    }
+}
+
+void launch_pt_init(uint32_t *order, uint4 *keys, uint32_t nslots, cudaStream_t s) {
+    pt_init_kernel<<<std::max(1u, std::min<uint32_t>(div_up(nslots, 256), 4096)), 256, 0, s>>>(order, keys, nslots);
     GC_CUDA(cudaGetLastError());
     count_launch();
 }

@@ -140,6 +140,17 @@ struct gc_cache {
     bool entry_bins_dirty = false;
     unsigned long long *d_samples = nullptr;  // samples taken by the ray caster since creation
     uint8_t *pool = nullptr;
+    // two-level directory (d.pt_block > 0): directory words, table pool, its
+    // LRU (ping-pong like the brick pool's) and the install's claim scratch
+    gc::PageTable pt{};
+    uint32_t pt_slots = 0, pt_dims[3] = {0, 0, 0}, pt_cur = 0, epoch_pt = 0;
+    uint64_t pt_words = 0;
+    uint32_t *pt_order[2] = {nullptr, nullptr};
+    uint4 *pt_keys = nullptr;
+    uint32_t *pt_claim = nullptr, *pt_word_of = nullptr, *pt_njobs = nullptr;
+    uint2 *pt_jobs = nullptr;
+    uint64_t *status_pt = nullptr;
+    gc::ScanCtl *ctl_pt = nullptr;
     uint64_t *status_lru = nullptr, *status_miss = nullptr;
     gc::ScanCtl *ctl_lru = nullptr, *ctl_miss = nullptr;
     uint32_t *d_count = nullptr, *d_misc = nullptr, *d_queue = nullptr;
@@ -220,6 +231,21 @@ static void build_tables(gc_cache *C) {
     }
     lt.nlevels = l;
     C->mx = off;
+    if (C->d.pt_block) {
+        // directory words of the two-level directory: ceil(bricks / P) per
+        // axis and level (CacheManager.hpp:160-176), levels packed along x
+        const uint32_t P = C->d.pt_block;
+        uint32_t toff = 0;
+        C->pt_dims[1] = C->pt_dims[2] = 0;
+        for (uint32_t k = 0; k < l; ++k) {
+            lt.pt_off[k] = toff;
+            toff += (lt.nb[k][0] + P - 1) / P;
+            C->pt_dims[1] = std::max(C->pt_dims[1], (lt.nb[k][1] + P - 1) / P);
+            C->pt_dims[2] = std::max(C->pt_dims[2], (lt.nb[k][2] + P - 1) / P);
+        }
+        C->pt_dims[0] = toff;
+        C->pt_words = static_cast<uint64_t>(C->pt_dims[0]) * C->pt_dims[1] * C->pt_dims[2];
+    }
     // the ray caster's page walk: one 32-bit index per entry, float-to-integer
     // floors exact below 2^23 voxels per axis
     GC_REQUIRE(static_cast<uint64_t>(C->mx) * C->my * C->mz < 0xffffffffull,
@@ -497,6 +523,7 @@ static void loader_main(gc_cache *C) {
 static CacheView cache_view(const gc_cache *C) {
     CacheView cv;
     cv.mrpd = C->mrpd;
+    cv.pt = C->pt;
     cv.req = C->req;
     cv.usage = C->usage;
     cv.pool = C->pool;
@@ -527,6 +554,15 @@ static void lru_update(gc_cache *C, cudaStream_t s) {
     launch_lru_partition(C->order[C->cur], C->order[C->cur ^ 1], C->usage, C->ts, C->nslots, C->d_count,
                          C->status_lru, C->ctl_lru, ++C->epoch_lru, s);
     C->cur ^= 1;
+    if (C->pt.shift) {
+        // the table pool's LRU (CacheManager::lru_update's loop over the
+        // table caches, CacheManager.hpp:386-406); its counter word is
+        // pt_njobs, free between installs
+        launch_lru_count(C->pt.usage, C->pt_slots, C->ts, C->pt_njobs, s);
+        launch_lru_partition(C->pt_order[C->pt_cur], C->pt_order[C->pt_cur ^ 1], C->pt.usage, C->ts, C->pt_slots,
+                             C->pt_njobs, C->status_pt, C->ctl_pt, ++C->epoch_pt, s);
+        C->pt_cur ^= 1;
+    }
 }
 
 static void install(gc_cache *C, cudaStream_t s) {
@@ -534,6 +570,14 @@ static void install(gc_cache *C, cudaStream_t s) {
     GC_CUDA(cudaStreamWaitEvent(s, C->ev_upload, 0));
     InstallArgs a;
     a.mrpd = C->mrpd;
+    a.pt = C->pt;
+    a.pt_slots = C->pt_slots;
+    a.pt_order = C->pt_order[C->pt_cur];
+    a.pt_keys = C->pt_keys;
+    a.pt_claim = C->pt_claim;
+    a.pt_word_of = C->pt_word_of;
+    a.pt_jobs = C->pt_jobs;
+    a.pt_njobs = C->pt_njobs;
     a.mx = C->mx;
     a.my = C->my;
     a.nentries = C->nentries;
@@ -637,7 +681,8 @@ static void destroy(gc_cache *C) {
     }
     cudaSetDevice(C->device);
     cudaDeviceSynchronize();
-    void *dev[] = {C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool, C->slot_bins, C->entry_bins, C->user_bins, C->d_samples,
+    void *dev[] = {C->pt.top, C->pt.table, C->pt.usage, C->pt_order[0], C->pt_order[1], C->pt_keys, C->pt_claim,
+                   C->pt_word_of, C->pt_jobs, C->pt_njobs, C->status_pt, C->ctl_pt, C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool, C->slot_bins, C->entry_bins, C->user_bins, C->d_samples,
                    C->status_lru, C->status_miss, C->ctl_lru, C->ctl_miss, C->d_count, C->d_misc, C->d_queue,
                    C->lists[0].d, C->lists[1].d, C->d_asked, C->d_owner, C->d_coords, C->d_big_coord, C->d_big_index, C->d_src,
                    C->d_staging, C->d_views, C->d_cut};
@@ -737,7 +782,7 @@ static void refresh_entry_bins(gc_cache *C, cudaStream_t s) {
         }
         GC_CUDA(cudaMemsetAsync(C->entry_bins, 0xff, C->nentries * sizeof(uint64_t), s));
         launch_live_bins(C->lt, C->slot_vpos, C->slot_level, C->slot_bins, C->nslots, C->mx, C->my, C->nentries,
-                         C->entry_bins, s);
+                         C->entry_bins, C->pt, C->d.cache_size[0], C->d.cache_size[1], C->B, s);
         GC_CUDA(cudaStreamSynchronize(s));
         return;
     }
@@ -763,7 +808,7 @@ static void refresh_entry_bins(gc_cache *C, cudaStream_t s) {
     GC_CUDA(cudaMemcpyAsync(C->user_bins, h.data(), C->nentries * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
     GC_CUDA(cudaMemcpyAsync(C->entry_bins, C->user_bins, C->nentries * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
     launch_live_bins(C->lt, C->slot_vpos, C->slot_level, C->slot_bins, C->nslots, C->mx, C->my, C->nentries,
-                     C->entry_bins, s);
+                     C->entry_bins, C->pt, C->d.cache_size[0], C->d.cache_size[1], C->B, s);
     GC_CUDA(cudaStreamSynchronize(s));
 }
 
@@ -957,7 +1002,40 @@ int gc_cache_create_shared(const gc_cache_desc *desc, const gc_volume_desc *volu
         GC_REQUIRE(C->nentries >= 2, "page directory too small");
         GC_REQUIRE(C->nentries < (1ull << 32), "page directory too large");
         const uint32_t maxr = desc->max_requests;
-        C->mrpd = dalloc<uint4>(C->nentries, "page directory");
+        if (desc->pt_block) {
+            uint32_t shift = 0;
+            while ((1u << shift) < desc->pt_block) ++shift;
+            GC_REQUIRE(desc->pt_block >= 2 && desc->pt_block <= 16 && (1u << shift) == desc->pt_block,
+                       "pt_block must be 0 or a power of two from 2 to 16");
+            GC_REQUIRE(desc->pt_slots >= 1 && desc->pt_slots < (1u << 30), "pt_slots must be in [1, 2^30)");
+            C->pt_slots = desc->pt_slots;
+            C->pt.shift = shift;
+            C->pt.tx = C->pt_dims[0];
+            C->pt.txy = C->pt_dims[0] * C->pt_dims[1];
+            const uint64_t per = 1ull << (3 * shift);
+            C->pt.top = dalloc<uint32_t>(C->pt_words, "page-table directory");
+            C->pt.table = dalloc<uint4>(C->pt_slots * per, "page-table pool");
+            C->pt.usage = dalloc<uint32_t>(C->pt_slots, "page-table usage");
+            C->pt_order[0] = dalloc<uint32_t>(C->pt_slots, "page-table LRU");
+            C->pt_order[1] = dalloc<uint32_t>(C->pt_slots, "page-table LRU");
+            C->pt_keys = dalloc<uint4>(C->pt_slots, "page-table keys");
+            C->pt_claim = dalloc<uint32_t>(C->pt_words, "page-table claims");
+            C->pt_word_of = dalloc<uint32_t>(maxr, "page-table claim words");
+            C->pt_jobs = dalloc<uint2>(maxr, "page-table jobs");
+            C->pt_njobs = dalloc<uint32_t>(1, "page-table job count");
+            C->status_pt = dalloc<uint64_t>(lookback_tiles(C->pt_slots), "scan status");
+            C->ctl_pt = dalloc<ScanCtl>(1, "scan control");
+            GC_CUDA(cudaMemset(C->pt.top, 0, C->pt_words * sizeof(uint32_t)));
+            GC_CUDA(cudaMemset(C->pt.table, 0, C->pt_slots * per * sizeof(uint4)));
+            GC_CUDA(cudaMemset(C->pt.usage, 0, C->pt_slots * sizeof(uint32_t)));
+            GC_CUDA(cudaMemset(C->pt_claim, 0xff, C->pt_words * sizeof(uint32_t)));
+            GC_CUDA(cudaMemset(C->status_pt, 0, lookback_tiles(C->pt_slots) * sizeof(uint64_t)));
+            GC_CUDA(cudaMemset(C->ctl_pt, 0, sizeof(ScanCtl)));
+            launch_pt_init(C->pt_order[0], C->pt_keys, C->pt_slots, nullptr);
+        } else {
+            C->mrpd = dalloc<uint4>(C->nentries, "page directory");
+            GC_CUDA(cudaMemset(C->mrpd, 0, C->nentries * sizeof(uint4)));
+        }
         C->req = dalloc<uint32_t>(C->nentries, "request buffer");
         C->usage = dalloc<uint32_t>(C->nslots, "usage buffer");
         C->order[0] = dalloc<uint32_t>(C->nslots, "LRU");
@@ -1003,7 +1081,6 @@ int gc_cache_create_shared(const gc_cache_desc *desc, const gc_volume_desc *volu
         C->h_misc = halloc<uint32_t>(1);
         C->h_staging = halloc<uint8_t>(maxr * C->big_stride);
         *C->h_misc = 0;
-        GC_CUDA(cudaMemset(C->mrpd, 0, C->nentries * sizeof(uint4)));
         GC_CUDA(cudaMemset(C->req, 0, C->nentries * sizeof(uint32_t)));
         GC_CUDA(cudaMemset(C->usage, 0, C->nslots * sizeof(uint32_t)));
         GC_CUDA(cudaMemset(C->pool, 0, C->nslots * C->slot_bytes));
@@ -1286,7 +1363,13 @@ int gc_cache_device_view_get(gc_cache_t C, uint32_t volume, gc_cache_device_view
                 out->level_voxels[l][a] = C->lt.vvox[cl][a];
                 out->level_initial_over_real[l][a] = C->lt.ior[cl][a];
             }
+            out->pt_level_offset[l] = C->lt.pt_off[cl];
         }
+        out->pt_top = C->pt.top;
+        out->pt_pool = reinterpret_cast<const uint32_t *>(C->pt.table);
+        out->pt_usage = C->pt.usage;
+        out->pt_shift = C->pt.shift;
+        for (int a = 0; a < 3; ++a) out->pt_dims[a] = C->pt_dims[a];
     });
 }
 
@@ -1310,6 +1393,11 @@ int gc_cache_info_get(gc_cache_t C, gc_cache_info *out) {
         for (uint32_t l = 0; l < std::min<uint32_t>(C->lt.nlevels, GC_MAX_LEVELS); ++l)
             out->level_offset[l] = C->lt.off[l];
         out->pool_bytes = static_cast<uint64_t>(C->nslots) * C->slot_bytes;
+        out->pt_block = C->d.pt_block;
+        out->pt_slots = C->pt_slots;
+        for (int a = 0; a < 3; ++a) out->pt_dims[a] = C->pt_dims[a];
+        for (uint32_t l = 0; l < std::min<uint32_t>(C->lt.nlevels, GC_MAX_LEVELS); ++l)
+            out->pt_level_offset[l] = C->lt.pt_off[l];
     });
 }
 
@@ -1342,8 +1430,41 @@ int gc_cache_dump(gc_cache_t C, int what, void *dst, size_t bytes) {
         switch (what) {
             case GC_DUMP_MRPD:
                 GC_REQUIRE(bytes == C->nentries * sizeof(uint4), "wrong size for the page directory");
-                GC_CUDA(cudaMemcpy(dst, C->mrpd, bytes, cudaMemcpyDeviceToHost));
+                if (C->pt.shift) {
+                    uint4 *flat = dalloc<uint4>(C->nentries, "flattened page directory");
+                    launch_pt_flatten(C->pt, C->lt, C->mx, C->my, C->nentries, flat, nullptr);
+                    const cudaError_t e = cudaMemcpy(dst, flat, bytes, cudaMemcpyDeviceToHost);
+                    cudaFree(flat);
+                    GC_CUDA(e);
+                } else {
+                    GC_CUDA(cudaMemcpy(dst, C->mrpd, bytes, cudaMemcpyDeviceToHost));
+                }
                 break;
+            case GC_DUMP_PT_TOP:
+            case GC_DUMP_PT_POOL:
+            case GC_DUMP_PT_LRU:
+            case GC_DUMP_PT_USAGE:
+            case GC_DUMP_PT_KEYS: {
+                GC_REQUIRE(C->pt.shift, "the cache has a one-level page directory");
+                const void *src = C->pt.top;
+                size_t want = C->pt_words * sizeof(uint32_t);
+                if (what == GC_DUMP_PT_POOL) {
+                    src = C->pt.table;
+                    want = (static_cast<size_t>(C->pt_slots) << (3 * C->pt.shift)) * sizeof(uint4);
+                } else if (what == GC_DUMP_PT_LRU) {
+                    src = C->pt_order[C->pt_cur];
+                    want = C->pt_slots * sizeof(uint32_t);
+                } else if (what == GC_DUMP_PT_USAGE) {
+                    src = C->pt.usage;
+                    want = C->pt_slots * sizeof(uint32_t);
+                } else if (what == GC_DUMP_PT_KEYS) {
+                    src = C->pt_keys;
+                    want = C->pt_slots * sizeof(uint4);
+                }
+                GC_REQUIRE(bytes == want, "wrong size for the page-table dump");
+                GC_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+                break;
+            }
             case GC_DUMP_REQUESTS:
                 GC_REQUIRE(bytes == C->nentries * sizeof(uint32_t), "wrong size for the request buffer");
                 GC_CUDA(cudaMemcpy(dst, C->req, bytes, cudaMemcpyDeviceToHost));
@@ -1831,6 +1952,7 @@ int gc_batch_create(gc_cache_t C, const gc_batch_desc *desc, gc_batch_t *out) {
         GC_REQUIRE(desc->max_views >= 1 && desc->max_views <= C->max_views, "max_views must be in [1, 256]");
         GC_REQUIRE(desc->max_pixels >= 1, "max_pixels must be >= 1");
         GC_REQUIRE(!desc->overlap_loads || !C->sync_mode(), "overlapped loads need the asynchronous loader");
+        GC_REQUIRE(!desc->overlap_loads || !C->pt.shift, "overlapped loads need the one-level page directory");
         GC_REQUIRE(!desc->overlap_loads || !(desc->park_above > 0.f), "parking is not available with overlapped loads");
         GC_CUDA(cudaSetDevice(C->device));
         b = new gc_batch();

@@ -410,13 +410,27 @@ __device__ __forceinline__ V3 norm_pos(V3 pos) {
 // (K_CacheManager::get_normalized's walk, K_CacheManager.hpp:265-300); p
 // receives the level position np * initial / real.
 __device__ __forceinline__ uint32_t entry_index(const CacheView &cv, const LevelTables &lt, uint32_t lvl, V3 np,
-                                                V3 &p) {
+                                                V3 &p, uint3 &q) {
     p = v3(np.x * lt.ior[lvl][0], np.y * lt.ior[lvl][1], np.z * lt.ior[lvl][2]);
-    const uint32_t cx = lt.off[lvl] + floor_u(p.x * lt.nbf[lvl][0]);
-    const uint32_t cy = floor_u(p.y * lt.nbf[lvl][1]);
-    const uint32_t cz = floor_u(p.z * lt.nbf[lvl][2]);
+    q = make_uint3(floor_u(p.x * lt.nbf[lvl][0]), floor_u(p.y * lt.nbf[lvl][1]), floor_u(p.z * lt.nbf[lvl][2]));
     // the page directory has fewer than 2^32 - 1 entries (checked at creation)
-    return cx + cy * cv.mx + cz * cv.mxy;
+    return lt.off[lvl] + q.x + q.y * cv.mx + q.z * cv.mxy;
+}
+
+// The page-directory entry of brick q (x inside the level) of cache level
+// lvl, flat index idx.  Two-level directory: the directory word, then the
+// entry in its table block (the table slot's usage word stamped, as the
+// reference's table-cache read does, K_CacheDevice.hpp:314-336); a word
+// without a block reads as an unmapped entry.  TL: the kernels compiled for a
+// two-level directory (the one-level kernels carry none of this).
+template <bool TL>
+__device__ __forceinline__ uint4 load_entry(const CacheView &cv, const LevelTables &lt, uint32_t lvl, uint32_t idx,
+                                            uint3 q) {
+    if constexpr (!TL) return __ldg(cv.mrpd + idx);
+    const uint32_t t = __ldg(cv.pt.top + pt_word(cv.pt, lt, lvl, q.x, q.y, q.z));
+    if (!(t & 1u)) return make_uint4(0u, 0u, 0u, 0u);
+    cv.pt.usage[t >> 1] = cv.ts;
+    return __ldg(cv.pt.table + pt_entry(cv.pt, t >> 1, pt_local(cv.pt, q.x, q.y, q.z)));
 }
 
 // Voxel sample of the resident brick at `base` (its pool slot) at level position p.
@@ -433,19 +447,20 @@ __device__ __forceinline__ typename SampleOf<T>::type sample_entry(const CacheVi
 // Page walk + sample at the normalized position np of cache level lvl (the
 // view's level base + its LOD): K_CacheManager::get_normalized
 // (K_CacheManager.hpp:265-361).
-template <typename T, uint32_t BS>
+template <typename T, uint32_t BS, bool TL>
 __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt, uint32_t sampler,
                                      const ViewParams &vp, uint32_t lvl, uint32_t lvl_end, V3 np, Walk &w,
                                      typename SampleOf<T>::type &sample) {
     // read where used (rare paths): the view's voxel width (mixed pools), its
     // visible bins (a newly entered brick) and its fallback flag (a missing one)
     V3 p;
-    const uint32_t idx = entry_index(cv, lt, lvl, np, p);
+    uint3 q;
+    const uint32_t idx = entry_index(cv, lt, lvl, np, p, q);
     if (idx != w.pidx) {
         // A new entry: the entry and its value bins are read together (one
         // memory round trip); the usage stamp of a mapped brick is a plain
         // store (idempotent, like the reference's per-sample stamp).
-        const uint4 e = __ldg(cv.mrpd + idx);
+        const uint4 e = load_entry<TL>(cv, lt, lvl, idx, q);
         const unsigned long long bins = __ldg(cv.entry_bins + idx);
         w.pidx = idx;
         w.flag = e.w;
@@ -478,11 +493,10 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
         // of the volume is sampled instead, an empty one ends the lookup.
         for (uint32_t l2 = lvl + 1; vp.fallback != 0u && l2 < lvl_end; ++l2) {
             const float qx = np.x * lt.ior[l2][0], qy = np.y * lt.ior[l2][1], qz = np.z * lt.ior[l2][2];
-            const uint32_t c2x = lt.off[l2] + static_cast<uint32_t>(qx * static_cast<float>(lt.nb[l2][0]));
-            const uint32_t c2y = static_cast<uint32_t>(qy * static_cast<float>(lt.nb[l2][1]));
-            const uint32_t c2z = static_cast<uint32_t>(qz * static_cast<float>(lt.nb[l2][2]));
-            const uint4 e2 = __ldg(cv.mrpd + c2x + static_cast<uint64_t>(c2y) * cv.mx +
-                                   static_cast<uint64_t>(c2z) * cv.mx * cv.my);
+            const uint3 q2 = make_uint3(static_cast<uint32_t>(qx * static_cast<float>(lt.nb[l2][0])),
+                                        static_cast<uint32_t>(qy * static_cast<float>(lt.nb[l2][1])),
+                                        static_cast<uint32_t>(qz * static_cast<float>(lt.nb[l2][2])));
+            const uint4 e2 = load_entry<TL>(cv, lt, l2, lt.off[l2] + q2.x + q2.y * cv.mx + q2.z * cv.mxy, q2);
             if (e2.w == 2u) return kEmpty;
             if (e2.w != 1u) continue;
             const uint32_t B = cv.B;
@@ -662,7 +676,7 @@ __device__ __forceinline__ void composite(Ray &r, float4 col) {
 
 // One iteration of the march loop (RayCasters.cu:122-188).  Returns false
 // when the loop ends.
-template <typename T, uint32_t BS>
+template <typename T, uint32_t BS, bool TL>
 __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables &lt, Ray &r) {
     const ViewParams &vp = *r.vp;
     if (!((!r.dvr || r.fc.w < r.early) && r.t < r.tfar)) return false;
@@ -692,7 +706,7 @@ __device__ __forceinline__ bool ray_step(const CacheView &cv, const LevelTables 
         }
     }
     typename SampleOf<T>::type sample{};
-    const int st = fetch<T, BS>(cv, lt, r.sampler, vp, r.lvl, r.lvl_end, np, r.w, sample);
+    const int st = fetch<T, BS, TL>(cv, lt, r.sampler, vp, r.lvl, r.lvl_end, np, r.w, sample);
     if (st == kCoarser) r.coarse = true;  // sampled below; the image is a preview
     if (st == kMapped || st == kCoarser) ++r.nsamp;
     if (st == kInvisible) {  // the step of a sample whose opacity stays below 0.001
@@ -814,7 +828,7 @@ __device__ __forceinline__ void retire_warp(uint32_t *queue, uint32_t nwarps) {
 
 // Tile scheduler: a warp takes one tile (tile_w x 32/tile_w pixels) at a time
 // from the queue and marches its 32 rays to completion.
-template <typename T, uint32_t BS>
+template <typename T, uint32_t BS, bool TL>
 __global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_kernel(const CacheView cv, const LevelTables lt,
                                                      const ViewParams *__restrict__ views, uint32_t nviews,
                                                      uint32_t total_tiles, uint32_t *queue, uint32_t nwarps) {
@@ -834,7 +848,7 @@ __global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_kernel(const
             Ray r;
             if (ray_setup<T>(lt, vp, x, y, r)) {
                 marched = ray_enters(r);
-                while (ray_step<T, BS>(cv, lt, r)) {
+                while (ray_step<T, BS, TL>(cv, lt, r)) {
                 }
                 unm = ray_finish(r);
                 coarse_any = r.coarse;
@@ -859,7 +873,7 @@ __global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_kernel(const
 // the next pixels of the queue (one warp-aggregated atomic), so a warp never
 // waits for its slowest ray.  Pixels are enumerated tile by tile, which keeps
 // consecutive grabs spatially close.
-template <typename T, uint32_t BS>
+template <typename T, uint32_t BS, bool TL>
 __global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_pixels_kernel(const CacheView cv, const LevelTables lt,
                                                             const ViewParams *__restrict__ views, uint32_t nviews,
                                                             uint32_t total_tiles, uint32_t *queue, uint32_t nwarps) {
@@ -890,7 +904,7 @@ __global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_pixels_kerne
             if (started && static_cast<int>(lane) == leader)
                 atomicAdd(cv.samples + 1, static_cast<unsigned long long>(__popc(started)));
         }
-        if (active && !ray_step<T, BS>(cv, lt, r)) {
+        if (active && !ray_step<T, BS, TL>(cv, lt, r)) {
             active = false;
             if (ray_finish(r) && r.vp->status && *r.vp->status == 0u) atomicOr(r.vp->status, 1u);
             if (r.coarse && r.vp->status) atomicOr(r.vp->status, 2u);
@@ -902,27 +916,29 @@ __global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_pixels_kerne
 }
 
 // Kernel of a voxel kind (1, 2, 4 bytes, 0 mixed, kTwoChannelU8), scheduler
-// and brick size (16 and 32 compiled for their size, others at run time).
-template <uint32_t BS>
+// and brick size (16 and 32 compiled for their size, others at run time);
+// TL: for a two-level page directory.
+template <uint32_t BS, bool TL>
 void *march_kernel_bs(uint32_t kind, bool pixels) {
     switch (kind) {
-        case 1: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<uint8_t, BS>)
-                              : reinterpret_cast<void *>(render_kernel<uint8_t, BS>);
-        case 2: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<uint16_t, BS>)
-                              : reinterpret_cast<void *>(render_kernel<uint16_t, BS>);
-        case 4: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<float, BS>)
-                              : reinterpret_cast<void *>(render_kernel<float, BS>);
-        case 0: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<MixedVoxel, BS>)
-                              : reinterpret_cast<void *>(render_kernel<MixedVoxel, BS>);
-        case 0x202: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<TwoU8, BS>)
-                                  : reinterpret_cast<void *>(render_kernel<TwoU8, BS>);
+        case 1: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<uint8_t, BS, TL>)
+                              : reinterpret_cast<void *>(render_kernel<uint8_t, BS, TL>);
+        case 2: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<uint16_t, BS, TL>)
+                              : reinterpret_cast<void *>(render_kernel<uint16_t, BS, TL>);
+        case 4: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<float, BS, TL>)
+                              : reinterpret_cast<void *>(render_kernel<float, BS, TL>);
+        case 0: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<MixedVoxel, BS, TL>)
+                              : reinterpret_cast<void *>(render_kernel<MixedVoxel, BS, TL>);
+        case 0x202: return pixels ? reinterpret_cast<void *>(render_pixels_kernel<TwoU8, BS, TL>)
+                                  : reinterpret_cast<void *>(render_kernel<TwoU8, BS, TL>);
         default: return nullptr;
     }
 }
-void *march_kernel(uint32_t kind, bool pixels, uint32_t brick_size) {
-    if (brick_size == 16) return march_kernel_bs<16>(kind, pixels);
-    if (brick_size == 32) return march_kernel_bs<32>(kind, pixels);
-    return march_kernel_bs<0>(kind, pixels);
+void *march_kernel(uint32_t kind, bool pixels, uint32_t brick_size, bool two_level) {
+    if (two_level) return march_kernel_bs<0, true>(kind, pixels);
+    if (brick_size == 16) return march_kernel_bs<16, false>(kind, pixels);
+    if (brick_size == 32) return march_kernel_bs<32, false>(kind, pixels);
+    return march_kernel_bs<0, false>(kind, pixels);
 }
 
 }  // namespace GC_MARCH_NS
@@ -1034,7 +1050,7 @@ void launch_view_bins(ViewParams *views_dev, uint32_t n, cudaStream_t s) {
 constexpr uint32_t kTwoChannelU8 = 0x202;
 static uint32_t voxel_kind(const CacheView &cv) { return cv.nc == 2 ? kTwoChannelU8 : cv.eb; }
 
-static RenderLaunch render_launch_config(uint32_t eb, uint32_t brick_size, uint32_t total_tiles) {
+static RenderLaunch render_launch_config(uint32_t eb, uint32_t brick_size, bool two_level, uint32_t total_tiles) {
     const RenderTuning tune = render_tuning();
     const uint32_t threads = tune.threads;
     GC_REQUIRE(threads == 64 || threads == 128 || threads == 256, "render threads must be 64, 128 or 256");
@@ -1042,12 +1058,13 @@ static RenderLaunch render_launch_config(uint32_t eb, uint32_t brick_size, uint3
     // widths share the cache; two 8-bit channels with a 2D transfer function)
     // from the exact or the fast build
     const bool pix = tune.scheduler == 1, fast_build = tune.precision == 1;
-    void *kernel = fast_build ? fast::march_kernel(eb, pix, brick_size) : exact::march_kernel(eb, pix, brick_size);
+    void *kernel = fast_build ? fast::march_kernel(eb, pix, brick_size, two_level)
+                              : exact::march_kernel(eb, pix, brick_size, two_level);
     if (!kernel) fail(GC_ERR_UNSUPPORTED, "the ray caster supports one channel of 1, 2 or 4 bytes");
     const int slot = eb == 1 ? 0 : eb == 2 ? 1 : eb == 4 ? 2 : eb == 0 ? 3 : 4;
-    static int occupancy[2][2][5][3][3] = {};
+    static int occupancy[2][2][5][3][4] = {};
     const int tslot = threads == 64 ? 0 : (threads == 128 ? 1 : 2);
-    const int bslot = brick_size == 16 ? 0 : (brick_size == 32 ? 1 : 2);
+    const int bslot = two_level ? 3 : (brick_size == 16 ? 0 : (brick_size == 32 ? 1 : 2));
     int &occ = occupancy[fast_build ? 1 : 0][pix ? 1 : 0][slot][tslot][bslot];
     if (!occ) {
         int b = 0;
@@ -1065,7 +1082,7 @@ void launch_render(const CacheView &cv, const LevelTables &lt, const ViewParams 
                    const ViewParams * /*views_host*/, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
                    uint32_t * /*err*/, cudaStream_t s) {
     if (total_tiles == 0) return;
-    const RenderLaunch L = render_launch_config(voxel_kind(cv), cv.B, total_tiles);
+    const RenderLaunch L = render_launch_config(voxel_kind(cv), cv.B, cv.pt.shift != 0u, total_tiles);
     uint32_t nwarps = L.grid * (L.threads / 32);
     void *args[] = {const_cast<CacheView *>(&cv), const_cast<LevelTables *>(&lt), &views_dev, &nviews, &total_tiles,
                     &queue, &nwarps};
@@ -1093,7 +1110,7 @@ void launch_render_graph(RenderGraph &g, const CacheView &cv, const LevelTables 
                          const ViewParams *views_pinned, uint32_t nviews, uint32_t total_tiles, uint32_t *queue,
                          cudaStream_t s) {
     if (total_tiles == 0) return;
-    const RenderLaunch L = render_launch_config(voxel_kind(cv), cv.B, total_tiles);
+    const RenderLaunch L = render_launch_config(voxel_kind(cv), cv.B, cv.pt.shift != 0u, total_tiles);
     uint32_t nwarps = L.grid * (L.threads / 32);
     const ViewParams *vd = views_dev;
     void *args[] = {const_cast<CacheView *>(&cv), const_cast<LevelTables *>(&lt), &vd, &nviews, &total_tiles,

@@ -29,6 +29,7 @@ SAMPLER_REFERENCE, SAMPLER_TRILINEAR = 0, 1
 CACHE_SYNC_LOADER = 1
 CACHE_STAGED_UPLOAD = 2
 DUMP_MRPD, DUMP_LRU, DUMP_USAGE, DUMP_REQUESTS, DUMP_POOL = 0, 1, 2, 3, 4
+DUMP_PT_TOP, DUMP_PT_POOL, DUMP_PT_LRU, DUMP_PT_USAGE, DUMP_PT_KEYS = 5, 6, 7, 8, 9
 MISS_LIST_FAILED = 0xFFFFFFFF  # gc_miss_list_noalloc: a bounded wait of the scan ran out
 
 U3 = C.c_uint32 * 3
@@ -58,12 +59,13 @@ class Generator(C.Structure):
 
 class CacheDesc(C.Structure):
     _fields_ = [("volume", VolumeDesc), ("layout", Layout), ("cache_size", U3), ("max_requests", C.c_uint32),
-                ("flags", C.c_uint32), ("gpu", C.c_int32)]
+                ("flags", C.c_uint32), ("gpu", C.c_int32), ("pt_block", C.c_uint32), ("pt_slots", C.c_uint32)]
 
 
 class CacheInfo(C.Structure):
     _fields_ = [("mrpd_dims", U3), ("nb_slots", C.c_uint32), ("slot_voxels", C.c_uint32),
-                ("level_offset", C.c_uint32 * MAX_LEVELS), ("pool_bytes", C.c_uint64)]
+                ("level_offset", C.c_uint32 * MAX_LEVELS), ("pool_bytes", C.c_uint64), ("pt_block", C.c_uint32),
+                ("pt_slots", C.c_uint32), ("pt_dims", U3), ("pt_level_offset", C.c_uint32 * MAX_LEVELS)]
 
 
 class CacheStats(C.Structure):
@@ -90,7 +92,9 @@ class CacheDeviceView(C.Structure):
                 ("brick_size", C.c_uint32), ("covering", C.c_uint32), ("voxel_bytes", C.c_uint32),
                 ("timestamp", C.c_uint32), ("n_levels", C.c_uint32), ("level_offset", C.c_uint32 * MAX_LEVELS),
                 ("level_bricks", (C.c_uint32 * 3) * MAX_LEVELS), ("level_voxels", (C.c_uint32 * 3) * MAX_LEVELS),
-                ("level_initial_over_real", (C.c_float * 3) * MAX_LEVELS)]
+                ("level_initial_over_real", (C.c_float * 3) * MAX_LEVELS), ("pt_top", C.c_void_p),
+                ("pt_pool", C.c_void_p), ("pt_usage", C.c_void_p), ("pt_shift", C.c_uint32),
+                ("pt_dims", C.c_uint32 * 3), ("pt_level_offset", C.c_uint32 * MAX_LEVELS)]
 
 
 class BatchDesc(C.Structure):
@@ -549,11 +553,13 @@ class CacheManager:
     """GPU brick cache + ray caster entry (CacheManager<T> + RayCastDVR)."""
 
     def __init__(self, vol, layout, cache_size, max_requests=50, sync_loader=True, gpu=0, staged_upload=False,
-                 shared=None):
+                 shared=None, pt_block=0, pt_slots=0):
         """shared: [(volume_desc, layout), ...] for one cache over several
-        volumes sharing the pool (vol/layout are then the first of them)."""
+        volumes sharing the pool (vol/layout are then the first of them).
+        pt_block, pt_slots: a two-level page directory (one word per
+        pt_block^3 bricks, a table pool of pt_slots blocks); 0: one level."""
         flags = (CACHE_SYNC_LOADER if sync_loader else 0) | (CACHE_STAGED_UPLOAD if staged_upload else 0)
-        self.desc = CacheDesc(vol, layout, u3(cache_size), max_requests, flags, gpu)
+        self.desc = CacheDesc(vol, layout, u3(cache_size), max_requests, flags, gpu, pt_block, pt_slots)
         self._h = vp()
         if shared:
             vols = (VolumeDesc * len(shared))(*[v for v, _ in shared])

@@ -59,7 +59,23 @@ __device__ __forceinline__ int gc_sample_normalized(const gc_cache_device_view *
     const uint32_t cz = (uint32_t)(pz * (float)v->level_bricks[level][2]);
     const uint64_t idx = (uint64_t)cx + (uint64_t)cy * v->mrpd_dims[0] +
                          (uint64_t)cz * v->mrpd_dims[0] * v->mrpd_dims[1];
-    const uint4 e = *reinterpret_cast<const uint4 *>(v->mrpd + 4 * idx);
+    uint4 e = make_uint4(0u, 0u, 0u, 0u);
+    if (v->pt_shift) {
+        /* two-level directory: the directory word of the brick's block, then
+         * the entry in the block (the table slot's usage word stamped); a
+         * word without a block reads as an unmapped entry */
+        const uint32_t s = v->pt_shift, m = (1u << s) - 1u, bx = cx - v->level_offset[level];
+        const uint32_t word = v->pt_level_offset[level] + (bx >> s) + (cy >> s) * v->pt_dims[0] +
+                              (cz >> s) * v->pt_dims[0] * v->pt_dims[1];
+        const uint32_t t = v->pt_top[word];
+        if (t & 1u) {
+            v->pt_usage[t >> 1] = v->timestamp;
+            const uint64_t j = ((uint64_t)(t >> 1) << (3u * s)) + ((bx & m) | ((cy & m) << s) | ((cz & m) << (2u * s)));
+            e = *reinterpret_cast<const uint4 *>(v->pt_pool + 4 * j);
+        }
+    } else {
+        e = *reinterpret_cast<const uint4 *>(v->mrpd + 4 * idx);
+    }
     if (e.w == 1u) {
         const uint32_t B = v->brick_size, c = v->covering, beff = B - 2u * c;
         const uint32_t slot = e.x / B + (e.y / B) * v->pool_slots[0] + (e.z / B) * v->pool_slots[0] * v->pool_slots[1];

@@ -203,6 +203,22 @@ typedef struct gc_cache_desc {
     uint32_t max_requests;    /* reference: 50 (CacheManager.hpp:263)              */
     uint32_t flags;           /* GC_CACHE_*                                        */
     int32_t gpu;              /* gpuID                                             */
+    /* Two-level page directory: the page-table hierarchy of CacheManager
+     * (CacheManager.hpp:151-236, CacheManagerKernels.hpp:148-357) with one
+     * page-table cache between the directory and the brick pool, i.e. a
+     * CacheConfiguration of two CacheSize / BlockSize entries.  pt_block = 0:
+     * one level (every configuration of the reference application).  Else
+     * a power of two from 2 to 16: the directory keeps one word per
+     * pt_block^3 bricks of a level, naming the block of pt_block^3 brick
+     * entries that holds them in a table pool of pt_slots blocks; the table
+     * pool has its own usage words and LRU order, and a block taken for new
+     * bricks evicts the least recently used one (its bricks become
+     * unreachable until requested again).  The flat directory of 16 bytes
+     * per brick is not allocated.  Not with the batched form's overlapped
+     * loads.  Brick entries, requests, samples and images are those of the
+     * one-level directory while no block in use is evicted. */
+    uint32_t pt_block;
+    uint32_t pt_slots;
 } gc_cache_desc;
 
 /* Brick source callback: copy the big brick (level, x, y, z) -- (BB*B)^3
@@ -305,6 +321,10 @@ typedef struct gc_cache_info {
     uint32_t slot_voxels;         /* B^3                                      */
     uint32_t level_offset[GC_MAX_LEVELS];
     uint64_t pool_bytes;
+    uint32_t pt_block;            /* 0: one-level directory                    */
+    uint32_t pt_slots;            /* table-pool blocks                         */
+    uint32_t pt_dims[3];          /* directory words per axis (two levels)     */
+    uint32_t pt_level_offset[GC_MAX_LEVELS];
 } gc_cache_info;
 int gc_cache_info_get(gc_cache_t cache, gc_cache_info *out);
 
@@ -345,6 +365,21 @@ int gc_cache_stats_get(gc_cache_t cache, gc_cache_stats *out);
 #define GC_DUMP_USAGE 2
 #define GC_DUMP_REQUESTS 3
 #define GC_DUMP_POOL 4
+/* Two-level directory (gc_cache_desc.pt_block > 0); GC_DUMP_MRPD then gives
+ * the brick entries as the flat directory would hold them (0 where the
+ * brick's table block is not resident):
+ *  GC_DUMP_PT_TOP   uint32 per directory word: table slot << 1 | 1, or 0
+ *  GC_DUMP_PT_POOL  uint32[4] per table entry, pt_block^3 entries per slot
+ *                   (x fastest inside the block)
+ *  GC_DUMP_PT_LRU   uint32 table slot ids in LRU order (most recent first)
+ *  GC_DUMP_PT_USAGE uint32 per table slot
+ *  GC_DUMP_PT_KEYS  uint32[4] per table slot: first brick (x, y, z) of its
+ *                   block in its level, and the level; all ones when free */
+#define GC_DUMP_PT_TOP 5
+#define GC_DUMP_PT_POOL 6
+#define GC_DUMP_PT_LRU 7
+#define GC_DUMP_PT_USAGE 8
+#define GC_DUMP_PT_KEYS 9
 int gc_cache_dump(gc_cache_t cache, int what, void *dst, size_t bytes);
 /* Miss list of the last request scan (coord_1D_to_3D output: x, y, z, level
  * per brick, CacheManagerKernels.cu:32-72), at most `max` entries; *total is
@@ -407,6 +442,13 @@ typedef struct gc_cache_device_view {
     uint32_t level_bricks[GC_MAX_LEVELS][3];       /* bricks per axis                                   */
     uint32_t level_voxels[GC_MAX_LEVELS][3];       /* virtualized voxels per axis (bricks x (B - 2c))  */
     float level_initial_over_real[GC_MAX_LEVELS][3]; /* initial / real level size                     */
+    /* two-level directory (pt_shift > 0; mrpd is then null): */
+    const uint32_t *pt_top;      /* directory word per pt_block^3 bricks: table slot << 1 | 1, or 0   */
+    const uint32_t *pt_pool;     /* table blocks: 4 words per brick entry, pt_block^3 entries a slot  */
+    uint32_t *pt_usage;          /* last-use word per table slot                                     */
+    uint32_t pt_shift;           /* log2(pt_block); 0 for the one-level directory                    */
+    uint32_t pt_dims[3];         /* directory words per axis, levels packed along x                  */
+    uint32_t pt_level_offset[GC_MAX_LEVELS];       /* directory x offset of each level               */
 } gc_cache_device_view;
 int gc_cache_device_view_get(gc_cache_t cache, uint32_t volume, gc_cache_device_view *out);
 

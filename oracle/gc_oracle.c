@@ -13,6 +13,19 @@
  *   orc_cache_*       CacheManager.hpp:135-670, CacheDevice.hpp:146-219,
  *                     CacheManagerKernels.cu:8-125, CacheManagerKernels.hpp:59-357,
  *                     RequestHandler.hpp:277-372
+ *   orc_cache_* with desc.pt_block > 0 (two-level directory)   the page-table
+ *                     hierarchy of CacheManager.hpp:151-236 and
+ *                     CacheManagerKernels.hpp:148-357 with one table cache,
+ *                     restated as this library defines it (see entry_of and
+ *                     load_new_bricks): the reference's own multi-level walk
+ *                     is used by no configuration and does not keep its
+ *                     directory consistent: downward writes stack entry 0
+ *                     only for a mapped directory word (CacheManagerKernels.hpp:
+ *                     193-198), so upward reads the previous brick's entry 0
+ *                     (:255) and files the brick into that brick's block; a
+ *                     block taken for an empty brick is flagged empty in the
+ *                     directory (:245-250); the eviction walk writes through
+ *                     an unmapped word (:130-138)
  *   orc_render        RayCasters.cu:35-349, 484-567; K_CacheManager.hpp:265-396;
  *                     K_CacheDevice.hpp:188-336; K_MultiResolutionPageDirectory.hpp:141-180;
  *                     VolumeRayCaster.cu:136-161
@@ -24,12 +37,12 @@
  *       sources (tests/golden/layout.json, bricker.json; oracle/build.py).
  *   bricks.xml format             PINNED: goldens written by the reference's
  *       MetaData::write_bricks_xml (tests/golden/bricks_xml/).
- *   orc_mip_level, orc_empty, orc_cache_*, orc_render   PARITY UNPINNED by
- *       reference execution: the reference implements them only as CUDA kernels
- *       (and its sources do not exist where the GPU runs), so they are literal
- *       restatements of the cited code, checked by closed-form properties and
- *       against the FP64 restatement (orc_render_f64), not against the
- *       reference's own outputs.  Two-channel rendering has no reference at all.
+ *   orc_mip_level, orc_empty, orc_cache_*, orc_render   the reference implements
+ *       them as CUDA kernels; they are pinned on the GPU, where the reference's
+ *       own CUDA build runs beside the CUDA path (oracle/ref_gpu_driver.cu,
+ *       tests/test_gpu_reference.py), and checked by closed-form properties
+ *       and the FP64 restatement (orc_render_f64) everywhere.  Two-channel
+ *       rendering and the two-level directory have no reference execution.
  *
  * Build with -ffp-contract=off: every float operation is rounded separately,
  * in source order, like the CUDA kernels built with -fmad=false; the fused
@@ -400,6 +413,11 @@ struct orc_cache {
     uint64_t level_off[GC_MAX_LEVELS];
     uint64_t *empty;
     size_t n_empty;
+    /* two-level directory (d.pt_block > 0): directory words, table pool,
+     * its usage words, LRU order (slot ids) and the block each slot holds */
+    uint32_t pts, pt_slots, ptx, pty, ptz, pt_off[GC_MAX_LEVELS];
+    uint64_t pt_words;
+    uint32_t *pt_top, *pt_table, *pt_usage, *pt_order, *pt_tmp, *pt_keys;
 };
 
 orc_cache *orc_cache_create(const gc_cache_desc *d) {
@@ -432,6 +450,30 @@ orc_cache *orc_cache_create(const gc_cache_desc *d) {
     c->big_bytes = c->brick_bytes * d->volume.big_brick_size[0] * d->volume.big_brick_size[1] *
                    d->volume.big_brick_size[2];
     c->mrpd = (uint32_t *)calloc(c->nentries * 4, sizeof(uint32_t));
+    if (d->pt_block) {
+        /* one directory word per P^3 bricks of a level: ceil(bricks / P) per
+         * axis (CacheManager.hpp:160-176), levels packed along x */
+        const uint32_t P = d->pt_block;
+        while ((1u << c->pts) < P) ++c->pts;
+        c->pt_slots = d->pt_slots;
+        uint32_t toff = 0;
+        for (uint32_t l = 0; l < c->nl; ++l) {
+            c->pt_off[l] = toff;
+            toff += (c->nb[l][0] + P - 1) / P;
+            if ((c->nb[l][1] + P - 1) / P > c->pty) c->pty = (c->nb[l][1] + P - 1) / P;
+            if ((c->nb[l][2] + P - 1) / P > c->ptz) c->ptz = (c->nb[l][2] + P - 1) / P;
+        }
+        c->ptx = toff;
+        c->pt_words = (uint64_t)c->ptx * c->pty * c->ptz;
+        c->pt_top = (uint32_t *)calloc(c->pt_words, sizeof(uint32_t));
+        c->pt_table = (uint32_t *)calloc(((uint64_t)c->pt_slots << (3 * c->pts)) * 4, sizeof(uint32_t));
+        c->pt_usage = (uint32_t *)calloc(c->pt_slots, sizeof(uint32_t));
+        c->pt_order = (uint32_t *)calloc(c->pt_slots, sizeof(uint32_t));
+        c->pt_tmp = (uint32_t *)calloc(c->pt_slots, sizeof(uint32_t));
+        c->pt_keys = (uint32_t *)malloc((size_t)c->pt_slots * 4 * sizeof(uint32_t));
+        for (uint32_t i = 0; i < c->pt_slots; ++i) c->pt_order[i] = i;
+        memset(c->pt_keys, 0xff, (size_t)c->pt_slots * 4 * sizeof(uint32_t));
+    }
     c->req = (uint32_t *)calloc(c->nentries, sizeof(uint32_t));
     c->usage = (uint32_t *)calloc(c->nslots, sizeof(uint32_t));
     c->lru = (orc_lru *)calloc(c->nslots, sizeof(orc_lru));
@@ -472,6 +514,12 @@ void orc_cache_destroy(orc_cache *c) {
     free(c->big_coord);
     free(c->staging);
     free(c->empty);
+    free(c->pt_top);
+    free(c->pt_table);
+    free(c->pt_usage);
+    free(c->pt_order);
+    free(c->pt_tmp);
+    free(c->pt_keys);
     free(c);
 }
 
@@ -485,7 +533,36 @@ void orc_cache_set_source(orc_cache *c, const void *bricks, const uint64_t *leve
     c->n_empty = n;
 }
 
-uint32_t *orc_mrpd(orc_cache *c) { return c->mrpd; }
+static uint32_t *entry_of(orc_cache *c, uint32_t l, uint32_t x, uint32_t y, uint32_t z, int stamp);
+
+/* With a two-level directory the flat entries are materialized from it (0
+ * where the brick's block is not resident). */
+uint32_t *orc_mrpd(orc_cache *c) {
+    if (c->pts) {
+        memset(c->mrpd, 0, c->nentries * 16);
+        for (uint32_t l = 0; l < c->nl; ++l)
+            for (uint32_t z = 0; z < c->nb[l][2]; ++z)
+                for (uint32_t y = 0; y < c->nb[l][1]; ++y)
+                    for (uint32_t x = 0; x < c->nb[l][0]; ++x) {
+                        const uint32_t *e = entry_of(c, l, x, y, z, 0);
+                        const uint64_t i = (uint64_t)(c->off[l] + x) + (uint64_t)y * c->mx + (uint64_t)z * c->mx * c->my;
+                        if (e) memcpy(&c->mrpd[4 * i], e, 16);
+                    }
+    }
+    return c->mrpd;
+}
+void orc_pt_dims(const orc_cache *c, uint32_t dims[3], uint32_t *slots, uint32_t *block) {
+    dims[0] = c->ptx;
+    dims[1] = c->pty;
+    dims[2] = c->ptz;
+    *slots = c->pt_slots;
+    *block = c->pts ? 1u << c->pts : 0u;
+}
+uint32_t *orc_pt_top(orc_cache *c) { return c->pt_top; }
+uint32_t *orc_pt_table(orc_cache *c) { return c->pt_table; }
+uint32_t *orc_pt_order(orc_cache *c) { return c->pt_order; }
+uint32_t *orc_pt_usage(orc_cache *c) { return c->pt_usage; }
+uint32_t *orc_pt_keys(orc_cache *c) { return c->pt_keys; }
 uint32_t *orc_requests(orc_cache *c) { return c->req; }
 uint32_t *orc_usage(orc_cache *c) { return c->usage; }
 orc_lru *orc_lru_records(orc_cache *c) { return c->lru; }
@@ -504,6 +581,27 @@ static uint32_t slot_of(const orc_cache *c, uint32_t cx, uint32_t cy, uint32_t c
     return cx / c->B + (cy / c->B) * c->sx + (cz / c->B) * c->sx * c->sy;
 }
 
+/* Two-level directory: the directory word of brick (x, y, z) of level l (x
+ * inside the level) and the place of its entry in the word's block. */
+static uint64_t pt_word_of(const orc_cache *c, uint32_t l, uint32_t x, uint32_t y, uint32_t z) {
+    return (uint64_t)(c->pt_off[l] + (x >> c->pts)) + (uint64_t)(y >> c->pts) * c->ptx +
+           (uint64_t)(z >> c->pts) * c->ptx * c->pty;
+}
+static uint32_t pt_local_of(const orc_cache *c, uint32_t x, uint32_t y, uint32_t z) {
+    const uint32_t m = (1u << c->pts) - 1u;
+    return (x & m) | ((y & m) << c->pts) | ((z & m) << (2 * c->pts));
+}
+/* The 4-word entry of a brick, or NULL when its table block is not resident
+ * (two levels).  stamp: a read of the page walk, which stamps the table
+ * slot's usage word (the reference's table-cache read, K_CacheDevice.hpp:314-336). */
+static uint32_t *entry_of(orc_cache *c, uint32_t l, uint32_t x, uint32_t y, uint32_t z, int stamp) {
+    if (!c->pts) return &c->mrpd[4 * ((uint64_t)(c->off[l] + x) + (uint64_t)y * c->mx + (uint64_t)z * c->mx * c->my)];
+    const uint32_t t = c->pt_top[pt_word_of(c, l, x, y, z)];
+    if (!(t & 1u)) return NULL;
+    if (stamp) __atomic_store_n(&c->pt_usage[t >> 1], c->ts, __ATOMIC_RELAXED);
+    return &c->pt_table[4 * (((uint64_t)(t >> 1) << (3 * c->pts)) + pt_local_of(c, x, y, z))];
+}
+
 /* create_mask + CacheDevice::update: stable partition, used first */
 void orc_lru_update(orc_cache *c) {
     uint32_t k = 0;
@@ -518,6 +616,16 @@ void orc_lru_update(orc_cache *c) {
     orc_lru *t = c->lru;
     c->lru = c->tmp;
     c->tmp = t;
+    if (c->pts) {  /* the table pool's LRU, the same stable partition */
+        k = 0;
+        for (uint32_t i = 0; i < c->pt_slots; ++i)
+            if (c->pt_usage[c->pt_order[i]] == c->ts) c->pt_tmp[k++] = c->pt_order[i];
+        for (uint32_t i = 0; i < c->pt_slots; ++i)
+            if (c->pt_usage[c->pt_order[i]] != c->ts) c->pt_tmp[k++] = c->pt_order[i];
+        uint32_t *u = c->pt_order;
+        c->pt_order = c->pt_tmp;
+        c->pt_tmp = u;
+    }
 }
 
 /* create_request_list: indexes in [0, size - 1) with req == ts, first max,
@@ -640,9 +748,21 @@ static void load_new_bricks(orc_cache *c) {
     if (n == 0) return;
     if (nne > c->nslots) nne = c->nslots;
     orc_lru *tail = c->lru + (c->nslots - nne);
-    /* dereference_old_bricks */
+    /* dereference_old_bricks; with two levels only an entry that still names
+     * the slot is cleared (after its block was evicted the brick may be
+     * unreachable, or resident again in another slot) */
     for (uint32_t i = 0; i < nne; ++i) {
         if (tail[i].vx < 0.f) continue;
+        if (c->pts) {
+            const uint32_t l = tail[i].level;
+            const uint32_t x = (uint32_t)(tail[i].vx * (float)c->nb[l][0]);
+            const uint32_t y = (uint32_t)(tail[i].vy * (float)c->nb[l][1]);
+            const uint32_t z = (uint32_t)(tail[i].vz * (float)c->nb[l][2]);
+            if (x >= c->nb[l][0] || y >= c->nb[l][1] || z >= c->nb[l][2]) continue;
+            uint32_t *e = entry_of(c, l, x, y, z, 0);
+            if (e && e[3] == 1 && e[0] == tail[i].cx && e[1] == tail[i].cy && e[2] == tail[i].cz) memset(e, 0, 16);
+            continue;
+        }
         uint64_t e = mrpd_coord(c, tail[i].level, tail[i].vx, tail[i].vy, tail[i].vz);
         memset(&c->mrpd[4 * e], 0, 16);
     }
@@ -679,20 +799,74 @@ static void load_new_bricks(orc_cache *c) {
                 memcpy(dst + ((uint64_t)(z * B + y) * B) * E,
                        src + (((uint64_t)(oz + z) * bvy + (oy + y)) * bvx + ox) * E, (uint64_t)B * E);
     }
+    if (c->pts) {
+        /* Two levels: table blocks for the new bricks.  The directory words
+         * without a block named by the list, in order of their first element,
+         * take the table slots at the LRU tail (the k-th of npt words the
+         * slot at position pt_slots - npt + k); a slot leaves the block it
+         * held (directory word cleared) and is cleared.  Words beyond the
+         * table pool's size get none: their bricks stay unmapped. */
+        uint64_t *words = (uint64_t *)malloc((n ? n : 1) * sizeof(uint64_t));
+        uint32_t *first = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+        uint32_t m = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            const uint32_t l = draft[i].level;
+            const uint32_t x = (uint32_t)(draft[i].vx * (float)c->nb[l][0]);
+            const uint32_t y = (uint32_t)(draft[i].vy * (float)c->nb[l][1]);
+            const uint32_t z = (uint32_t)(draft[i].vz * (float)c->nb[l][2]);
+            if (x >= c->nb[l][0] || y >= c->nb[l][1] || z >= c->nb[l][2]) continue;
+            const uint64_t w = pt_word_of(c, l, x, y, z);
+            if (c->pt_top[w] & 1u) continue;
+            uint32_t k = 0;
+            while (k < m && words[k] != w) ++k;
+            if (k == m) {
+                words[m] = w;
+                first[m++] = i;
+            }
+        }
+        const uint32_t npt = m < c->pt_slots ? m : c->pt_slots;
+        const uint32_t P = 1u << c->pts, msk = ~(P - 1u);
+        const uint64_t per = (uint64_t)1 << (3 * c->pts);
+        for (uint32_t k = 0; k < npt; ++k) {
+            const uint32_t slot = c->pt_order[c->pt_slots - npt + k];
+            uint32_t *key = &c->pt_keys[4 * slot];
+            if (key[3] != 0xffffffffu) c->pt_top[pt_word_of(c, key[3], key[0], key[1], key[2])] = 0;
+            memset(&c->pt_table[4 * ((uint64_t)slot * per)], 0, per * 16);
+            const orc_lru *d = &draft[first[k]];
+            key[0] = (uint32_t)(d->vx * (float)c->nb[d->level][0]) & msk;
+            key[1] = (uint32_t)(d->vy * (float)c->nb[d->level][1]) & msk;
+            key[2] = (uint32_t)(d->vz * (float)c->nb[d->level][2]) & msk;
+            key[3] = d->level;
+            c->pt_top[words[k]] = slot << 1 | 1u;
+        }
+        free(words);
+        free(first);
+    }
     /* reference_new_bricks: non-empty then empty, serially */
     for (uint32_t i = 0; i < n; ++i) {
-        uint64_t e = mrpd_coord(c, draft[i].level, draft[i].vx, draft[i].vy, draft[i].vz);
-        if (c->mrpd[4 * e + 3] >= 1) continue;
+        const uint32_t l = draft[i].level;
+        uint32_t *e;
+        if (c->pts) {
+            const uint32_t x = (uint32_t)(draft[i].vx * (float)c->nb[l][0]);
+            const uint32_t y = (uint32_t)(draft[i].vy * (float)c->nb[l][1]);
+            const uint32_t z = (uint32_t)(draft[i].vz * (float)c->nb[l][2]);
+            if (x >= c->nb[l][0] || y >= c->nb[l][1] || z >= c->nb[l][2]) continue;
+            e = entry_of(c, l, x, y, z, 0);
+            if (!e) continue;
+        } else {
+            e = &c->mrpd[4 * mrpd_coord(c, l, draft[i].vx, draft[i].vy, draft[i].vz)];
+        }
+        if (e[3] >= 1) continue;
         if (i < nne) {
-            c->mrpd[4 * e + 0] = tail[i].cx;
-            c->mrpd[4 * e + 1] = tail[i].cy;
-            c->mrpd[4 * e + 2] = tail[i].cz;
-            c->mrpd[4 * e + 3] = 1;
+            e[0] = tail[i].cx;
+            e[1] = tail[i].cy;
+            e[2] = tail[i].cz;
+            e[3] = 1;
         } else if (i >= c->n_nonempty) {
-            c->mrpd[4 * e + 0] = 0;
-            c->mrpd[4 * e + 1] = 0;
-            c->mrpd[4 * e + 2] = 0;
-            c->mrpd[4 * e + 3] = 2;
+            e[0] = 0;
+            e[1] = 0;
+            e[2] = 0;
+            e[3] = 2;
         }
     }
     free(draft);
@@ -901,7 +1075,11 @@ static int fetch32_at(orc_cache *c, uint32_t sampler, uint32_t lod, f3 np, walk 
     uint32_t cz = (uint32_t)(pz * (float)c->nb[lod][2]);
     uint64_t idx = (uint64_t)cx + (uint64_t)cy * c->mx + (uint64_t)cz * c->mx * c->my;
     if (cx != w->pcx || cy != w->pcy || cz != w->pcz) {
-        memcpy(w->e, &c->mrpd[4 * idx], 16);
+        const uint32_t *e = entry_of(c, lod, cx - c->off[lod], cy, cz, 1);
+        if (e)
+            memcpy(w->e, e, 16);
+        else
+            memset(w->e, 0, 16);
         w->pcx = cx;
         w->pcy = cy;
         w->pcz = cz;
@@ -1242,7 +1420,9 @@ static void march64(orc_cache *c, const gc_view *v, const float *tf, uint32_t x,
             uint32_t cx = c->off[lod] + (uint32_t)(px * c->nb[lod][0]), cy = (uint32_t)(py * c->nb[lod][1]),
                      cz = (uint32_t)(pz * c->nb[lod][2]);
             uint64_t idx = (uint64_t)cx + (uint64_t)cy * c->mx + (uint64_t)cz * c->mx * c->my;
-            const uint32_t *e = &c->mrpd[4 * idx];
+            static const uint32_t no_entry[4] = {0, 0, 0, 0};
+            const uint32_t *e = entry_of(c, lod, cx - c->off[lod], cy, cz, 0);
+            if (!e) e = no_entry;
             double sample = 0.0;
             if (e[3] == 0) {
                 __atomic_store_n(&req[idx], c->ts, __ATOMIC_RELAXED);

@@ -38,7 +38,7 @@ void orc_brick_level(const void *level, const uint32_t dims[3], const gc_volume_
 void orc_empty(const void *bricks, uint64_t nbig, uint64_t values_per_big, uint32_t cb, float threshold,
                uint8_t *flags);
 
-/* cache state machine (MRPD-only hierarchy) */
+/* cache state machine (one-level directory, or two levels: desc.pt_block) */
 typedef struct orc_lru {
     uint32_t cx, cy, cz, level;
     float vx, vy, vz;
@@ -64,6 +64,15 @@ uint32_t *orc_usage(orc_cache *c);
 orc_lru *orc_lru_records(orc_cache *c);
 uint8_t *orc_pool(orc_cache *c);
 void orc_cache_dims(const orc_cache *c, uint32_t mrpd_dims[3], uint32_t *nslots, uint64_t *pool_bytes);
+/* two-level directory (desc.pt_block > 0): dimensions and state, in the
+ * layouts of the GC_DUMP_PT_* dumps; orc_mrpd then returns the flat entries
+ * materialized from it */
+void orc_pt_dims(const orc_cache *c, uint32_t dims[3], uint32_t *slots, uint32_t *block);
+uint32_t *orc_pt_top(orc_cache *c);
+uint32_t *orc_pt_table(orc_cache *c);
+uint32_t *orc_pt_order(orc_cache *c);
+uint32_t *orc_pt_usage(orc_cache *c);
+uint32_t *orc_pt_keys(orc_cache *c);
 
 /* ray caster, FP32 mirror of the CUDA kernel's operation sequence
  * (threads = 0 -> all cores) */

@@ -40,7 +40,7 @@ class Generator(C.Structure):
 
 class CacheDesc(C.Structure):
     _fields_ = [("volume", VolumeDesc), ("layout", Layout), ("cache_size", U3), ("max_requests", C.c_uint32),
-                ("flags", C.c_uint32), ("gpu", C.c_int32)]
+                ("flags", C.c_uint32), ("gpu", C.c_int32), ("pt_block", C.c_uint32), ("pt_slots", C.c_uint32)]
 
 
 class View(C.Structure):
@@ -78,6 +78,9 @@ _SIGS = {
     "orc_mrpd": ([vp], vp), "orc_requests": ([vp], vp), "orc_usage": ([vp], vp),
     "orc_lru_records": ([vp], vp), "orc_pool": ([vp], vp),
     "orc_cache_dims": ([vp, P(C.c_uint32), P(C.c_uint32), P(C.c_uint64)], None),
+    "orc_pt_dims": ([vp, P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)], None),
+    "orc_pt_top": ([vp], vp), "orc_pt_table": ([vp], vp), "orc_pt_order": ([vp], vp),
+    "orc_pt_usage": ([vp], vp), "orc_pt_keys": ([vp], vp),
     "orc_render": ([vp, P(View), vp, vp, vp, vp, C.c_int], None),
     "orc_render_f64": ([vp, P(View), vp, vp, vp, vp, vp, vp, C.c_int], None),
     "orc_pow": ([C.c_float, C.c_float], C.c_float),
@@ -170,6 +173,10 @@ class Cache:
         self.nslots = ns.value
         self.pool_bytes = pb.value
         self.nentries = md[0] * md[1] * md[2]
+        td, ts_, tb = U3(), C.c_uint32(), C.c_uint32()
+        lib.orc_pt_dims(self.h, td, C.byref(ts_), C.byref(tb))
+        self.pt_dims, self.pt_slots, self.pt_block = tuple(td), ts_.value, tb.value
+        self.pt_words = td[0] * td[1] * td[2]
         self._keep = []
 
     def set_source(self, bricks, level_offsets, empty_keys=()):
@@ -219,6 +226,22 @@ class Cache:
 
     def pool(self):
         return self._arr(lib.orc_pool, np.uint8, self.pool_bytes)
+
+    # two-level directory state (the layouts of the GC_DUMP_PT_* dumps)
+    def pt_top(self):
+        return self._arr(lib.orc_pt_top, np.uint32, self.pt_words)
+
+    def pt_table(self):
+        return self._arr(lib.orc_pt_table, np.uint32, self.pt_slots * self.pt_block ** 3 * 4).reshape(-1, 4)
+
+    def pt_order(self):
+        return self._arr(lib.orc_pt_order, np.uint32, self.pt_slots)
+
+    def pt_usage(self):
+        return self._arr(lib.orc_pt_usage, np.uint32, self.pt_slots)
+
+    def pt_keys(self):
+        return self._arr(lib.orc_pt_keys, np.uint32, self.pt_slots * 4).reshape(-1, 4)
 
     def render(self, view, tf, rgba, tbuf, state, threads=0):
         v = conv(View, view)

@@ -1,0 +1,146 @@
+"""Two-level page directory on the GPU (gc_cache_desc.pt_block: the
+page-table hierarchy of CacheManager.hpp:151-236 with one table cache)
+against the oracle's restatement, frame by frame: images, t buffer, colour
+state, converged flags, brick entries (flattened), LRU, usage, requests,
+pool bytes and the table state (directory words, table blocks, table LRU,
+table usage, block keys), with a roomy table pool and with pools small
+enough that views evict each other's blocks.  A user kernel sampling through
+the device view of a two-level cache matches the oracle too."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import scenario
+from test_gpu_device_view import user_lib  # noqa: F401  (fixture)
+from test_gpu_render import RGBA_TOL_FP32, Scene, rgba_diff
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    # size, bpc, B, c, big brick, pool, maxreq, pt_block, pt_slots, W, H, tf, view kwargs
+    "roomy_p4": ((64, 48, 56), 1, 8, 1, (1, 1, 1), (6, 6, 5), 40, 4, 1000, 48, 40, "ramp", dict()),
+    "evicting_p2": ((96, 96, 96), 1, 8, 1, (1, 1, 1), (12, 12, 12), 100, 2, 300, 40, 32, "ramp", dict()),
+    "evicting_p4_u16_mop": ((96, 96, 96), 2, 8, 1, (2, 1, 1), (12, 12, 12), 100, 4, 60, 40, 32, "bumps",
+                            dict(mode=1, sampler=1, early_alpha=0.99)),
+}
+VIEWS = ((0, 10), (4, 10), (2, 60), (6, -40), (0, 10))
+
+
+def compare_tables(s, tag):
+    gc, oc, cm = s.gc, s.oc, s.cm
+    for what, ref in ((gc.DUMP_PT_TOP, oc.pt_top()), (gc.DUMP_PT_POOL, oc.pt_table()), (gc.DUMP_PT_LRU, oc.pt_order()),
+                      (gc.DUMP_PT_USAGE, oc.pt_usage()), (gc.DUMP_PT_KEYS, oc.pt_keys())):
+        got = cm.dump(what, np.zeros_like(ref))
+        assert np.array_equal(got, ref), (tag, what)
+
+
+def run_views(s, torch, tf, W, H, kw, frames_per_view, check):
+    tf_dev = torch.from_numpy(tf.reshape(-1).copy()).cuda()
+    g, o = s.buffers(W, H)
+    f = 0
+    for k, (az, el) in enumerate(VIEWS):
+        m = scenario.orbit_camera(s.gc, az, 8, 1.2, el)
+        for x in g:
+            x.zero_()
+        for x in o:
+            x[:] = 0
+        for _ in range(frames_per_view):
+            v = s.view(m, W, H, tf_dev, 256, g, **kw)
+            s.cm.render(v)
+            s.oc.render(v, tf, *o)
+            torch.cuda.synchronize()
+            d = rgba_diff(g[0].cpu().numpy(), o[0])
+            assert d.max() <= RGBA_TOL_FP32, f"frame {f}: RGBA off by {d.max()}"
+            assert np.array_equal(g[1].cpu().numpy(), o[1]), f"frame {f}: t buffer"
+            assert np.array_equal(g[2].cpu().numpy(), o[2]), f"frame {f}: colour state"
+            c1, c2 = s.cm.update(), s.oc.update()
+            assert c1 == c2, f"frame {f}"
+            if check:
+                s.compare_cache(f"frame {f}")
+                compare_tables(s, f"frame {f}")
+            f += 1
+            if c1:
+                break
+    return f
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_two_level_loop_matches_oracle(gc, orc, torch_cuda, case):
+    size, bpc, B, c, bb, pool, maxreq, P, slots, W, H, tfk, kw = CASES[case]
+    s = Scene(gc, orc, torch_cuda, size, bpc, B, c, bb, pool, maxreq, pt_block=P, pt_slots=slots)
+    assert s.cm.info.pt_block == P and s.cm.info.pt_slots == slots
+    assert tuple(s.cm.info.pt_dims) == s.oc.pt_dims
+    tf = scenario.ramp_tf() if tfk == "ramp" else scenario.bumps_tf(3)
+    frames = run_views(s, torch_cuda, tf, W, H, kw, 80, True)
+    assert frames > 20
+    keys = s.oc.pt_keys()
+    assert (keys[:, 3] != 0xFFFFFFFF).sum() > 0
+    st = s.cm.stats()
+    assert st.bricks_installed > 0 and st.device_error == 0
+
+
+@pytest.mark.parametrize("scheduler", [0, 1])
+def test_two_level_images_equal_one_level(gc, orc, torch_cuda, scheduler):
+    """A roomy table pool is transparent on the GPU: both ray-caster
+    schedulers render, frame by frame, what the one-level cache renders."""
+    torch = torch_cuda
+    size, bpc, B, c, bb, pool, maxreq = (64, 64, 64), 2, 16, 1, (1, 1, 1), (5, 5, 5), 60
+    a = Scene(gc, orc, torch, size, bpc, B, c, bb, pool, maxreq)
+    b = Scene(gc, orc, torch, size, bpc, B, c, bb, pool, maxreq, pt_block=2, pt_slots=4096)
+    old = gc.render_tuning()
+    try:
+        gc.render_tuning(scheduler, 8, 128, 0)
+        tf = scenario.bumps_tf(2)
+        tf_dev = torch.from_numpy(tf.reshape(-1).copy()).cuda()
+        W, H = 64, 48
+        ga, _ = a.buffers(W, H)
+        gb, _ = b.buffers(W, H)
+        for f in range(18):
+            m = scenario.orbit_camera(gc, f // 6, 6, 2.2)
+            if f % 6 == 0:
+                for x in ga + gb:
+                    x.zero_()
+            a.cm.render(a.view(m, W, H, tf_dev, 256, ga, sampler=1))
+            b.cm.render(b.view(m, W, H, tf_dev, 256, gb, sampler=1))
+            torch.cuda.synchronize()
+            for x, y in zip(ga, gb):
+                assert torch.equal(x, y), f"frame {f}"
+            assert a.cm.update() == b.cm.update(), f"frame {f}"
+    finally:
+        gc.render_tuning(*old)
+
+
+def test_user_kernel_two_level(gc, orc, torch_cuda, user_lib):  # noqa: F811
+    """gc_sample_normalized through the device view of a two-level cache
+    after an evicting run: statuses, values, usage stamps (pool and table)
+    and requests equal the oracle's samples of the same state."""
+    torch = torch_cuda
+    s = Scene(gc, orc, torch, (96, 96, 96), 1, 8, 1, (1, 1, 1), (12, 12, 12), 100, pt_block=2, pt_slots=300)
+    run_views(s, torch, scenario.ramp_tf(), 40, 32, {}, 6, False)
+    s.compare_cache("after the frames")
+    compare_tables(s, "after the frames")
+    oc, cm = s.oc, s.cm
+    v = cm.device_view()
+    assert v.pt_shift == 1 and v.timestamp == cm.timestamp() == oc.timestamp
+    rng = np.random.default_rng(9)
+    n = 20000
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, :3] = rng.uniform(0.0, 0.99, (n, 3))
+    pos[:, 3] = rng.integers(0, s.layout.nb_levels, n)
+    d_pos = torch.from_numpy(pos).cuda()
+    d_val = torch.zeros(n, dtype=torch.float32, device="cuda")
+    d_st = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    assert user_lib.user_sample(ctypes.addressof(v), d_pos.data_ptr(), n, d_val.data_ptr(), d_st.data_ptr()) == 0
+    want = [oc.sample_normalized(int(p[3]), float(p[0]), float(p[1]), float(p[2])) for p in pos]
+    st, val = d_st.cpu().numpy(), d_val.cpu().numpy()
+    want_st = np.array([w[0] for w in want])
+    want_val = np.array([w[1] for w in want], np.float32)
+    assert np.array_equal(st, want_st)
+    mapped = st == 0
+    assert mapped.any() and (st == 1).any(), "samples of resident and of missing bricks"
+    assert np.array_equal(val[mapped], want_val[mapped])
+    for what, ref in ((gc.DUMP_USAGE, oc.usage()), (gc.DUMP_REQUESTS, oc.requests()),
+                      (gc.DUMP_PT_USAGE, oc.pt_usage())):
+        got = cm.dump(what, np.zeros_like(ref))
+        assert np.array_equal(got, ref), what

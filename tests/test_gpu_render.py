@@ -20,7 +20,8 @@ FAST_OUTLIER_SHARE = 1e-3  # fast build vs FP64: pixels allowed beyond 1/255 (te
 
 
 class Scene:
-    def __init__(self, gc, orc, torch, size, bpc, B, c, bb, pool, maxreq, seed=21, nblobs=6, sync=True, channels=1):
+    def __init__(self, gc, orc, torch, size, bpc, B, c, bb, pool, maxreq, seed=21, nblobs=6, sync=True, channels=1,
+                 **cache_kw):
         self.gc, self.orc, self.torch = gc, orc, torch
         self.vol = gc.volume_desc(size, B, c, bpc * channels, channels, bb)
         self.layout = gc.compute_layout(self.vol)
@@ -30,7 +31,7 @@ class Scene:
         ref, roffs = scenario.orc_store(orc, gc, o.reshape(-1).view(np.uint8), self.vol, self.layout)
         assert np.array_equal(self.store.numpy(), ref)
         self.ref = ref
-        self.cm = gc.CacheManager(self.vol, self.layout, pool, max_requests=maxreq, sync_loader=sync)
+        self.cm = gc.CacheManager(self.vol, self.layout, pool, max_requests=maxreq, sync_loader=sync, **cache_kw)
         self.cm.set_source_host(self.store, self.offs)
         self.oc = orc.Cache(self.cm.desc)
         self.oc.set_source(ref, roffs)
