@@ -422,11 +422,11 @@ class Session:
     staged = False  # GC_CACHE_STAGED_UPLOAD for every session (--upload staged)
     brick_bins = False  # give the cache the value bins of every brick (--brick-bins)
 
-    def __init__(self, gc, torch, cfg, vol, layout, store, offs, max_requests, sync=True):
+    def __init__(self, gc, torch, cfg, vol, layout, store, offs, max_requests, sync=True, pt=(0, 0)):
         self.gc, self.torch, self.cfg = gc, torch, cfg
         self.pool = cfg["pool_slots"] or gc.pool_dims(vol, cfg["pool_bytes"])
         self.cm = gc.CacheManager(vol, layout, self.pool, max_requests=max_requests, sync_loader=sync,
-                                  staged_upload=Session.staged)
+                                  staged_upload=Session.staged, pt_block=pt[0], pt_slots=pt[1])
         self.cm.set_source_host(store, offs)
         if Session.brick_bins:
             self.cm.set_brick_bins(BRICK_BINS[store.data_ptr()])
@@ -758,6 +758,12 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(gc, S, cfg, last, args, images)
         out["parity_max_abs"] = out["cpu_baseline"]["parity"]["max_abs_rgba"]
+    if rank == 0:
+        try:
+            out["page_table"] = page_table_leg(gc, torch, cfg, vol, layout, store, offs, args, last, render_ms,
+                                               images["fast" if args.precision == "fast" else "exact"], S)
+        except Exception as e:  # a reported leg: its failure does not void the line
+            out["page_table"] = {"unavailable": f"{type(e).__name__}: {e}"[:300]}
     S.close()
     del store, S
     release_memory(torch)
@@ -787,6 +793,49 @@ def run_ours(args):
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+PT_BLOCK, PT_SLOTS = 8, 4096
+
+
+def page_table_leg(gc, torch, cfg, vol, layout, store, offs, args, spec, render_ms_one, image_one, S1):
+    """The roofline view through a two-level page directory (PT_BLOCK^3 bricks
+    per directory word, a table pool of PT_SLOTS blocks): rendered to
+    convergence from a cold cache over the same store, then re-rendered from
+    scratch after an L2 flush 5 times (CUDA events); the image must equal the
+    one-level cache's."""
+    S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests, pt=(PT_BLOCK, PT_SLOTS))
+    try:
+        it, conv = S.converge(spec, cap=cfg.get("cap", 64))
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        ev = []
+        for _ in range(5):
+            views, bufs = S.views(spec)
+            with torch.cuda.stream(S.stream):
+                bufs[0][1].zero_()
+                bufs[0][2].zero_()
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(S.stream)
+                S.cm.render(views[0], S.sp)
+                e1.record(S.stream)
+                ev.append((e0, e1))
+        torch.cuda.synchronize()
+        img = bufs[0][0].cpu().numpy().view(np.uint32)
+        info, info1 = S.cm.info, S1.cm.info
+        flat = info1.mrpd_dims[0] * info1.mrpd_dims[1] * info1.mrpd_dims[2] * 16
+        two = info.pt_dims[0] * info.pt_dims[1] * info.pt_dims[2] * 4 + PT_SLOTS * PT_BLOCK ** 3 * 16
+        ms = statistics.median([a.elapsed_time(b) for a, b in ev])
+        return {"pt_block": PT_BLOCK, "pt_slots": PT_SLOTS, "iterations_to_converge": it, "converged": bool(conv),
+                "launch_ms": round(ms, 4), "launch_ms_one_level": round(render_ms_one, 4),
+                "launch_ratio": round(ms / render_ms_one, 3),
+                "image_equal_to_one_level": bool(np.array_equal(img, image_one)),
+                "directory_bytes": {"one_level": int(flat), "two_level": int(two)},
+                "note": "the roofline view through the two-level page directory (directory word per "
+                        f"{PT_BLOCK}^3 bricks, table pool of {PT_SLOTS} blocks), converged from a cold cache, "
+                        "re-rendered after an L2 flush; launch_ms_one_level is the roofline launch above"}
+    finally:
+        S.close()
 
 
 def release_memory(torch):
@@ -1082,7 +1131,8 @@ def run_roofline_only(args):
     torch.cuda.synchronize()
     if args.tuning:
         gc.render_tuning(*[int(x) for x in args.tuning.split(",")])
-    cm = gc.CacheManager(vol, layout, pool_slots(cfg), max_requests=args.max_requests, sync_loader=True)
+    cm = gc.CacheManager(vol, layout, pool_slots(cfg), max_requests=args.max_requests, sync_loader=True,
+                         pt_block=args.pt_block, pt_slots=args.pt_slots if args.pt_block else 0)
     cm.set_source_device(pyr.data_ptr(), poffs, keep=pyr)
     tf = torch.from_numpy(tf_table(cfg["tf"]).reshape(-1).copy()).cuda()
     W, H = cfg["W"], cfg["H"]
@@ -1129,6 +1179,7 @@ def run_roofline_only(args):
                                         "launch_ms": [round(t, 4) for t in times],
                                         "samples_per_launch": (st.samples - s0) / max(1, args.steps),
                                         "tuning": list(gc.render_tuning()),
+                                        "pt_block": args.pt_block,
                                         "device_gb_reserved": round(torch.cuda.memory_reserved() / 1e9, 2)}}),
           flush=True)
     cm.close()
@@ -1751,6 +1802,9 @@ def main():
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip the reference's own CUDA build timed beside our plain path (c1 views)")
     ap.add_argument("--no-plain", action="store_true", help="c3: skip the plain loop over the same views")
+    ap.add_argument("--pt-block", type=int, default=0,
+                    help="--roofline-only: a two-level page directory with this block size (0: one level)")
+    ap.add_argument("--pt-slots", type=int, default=PT_SLOTS, help="--roofline-only: table-pool blocks")
     ap.add_argument("--roofline-only", action="store_true",
                     help="only the c2 roofline launch, --steps times, bricks from the device pyramid (for ncu)")
     ap.add_argument("--preprocess-only", action="store_true",
