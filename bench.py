@@ -806,7 +806,7 @@ def page_table_leg(gc, torch, cfg, vol, layout, store, offs, args, spec, render_
     one-level cache's."""
     S = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests, pt=(PT_BLOCK, PT_SLOTS))
     try:
-        it, conv = S.converge(spec, cap=cfg.get("cap", 64))
+        it, conv = S.converge(spec, cap=256)  # from a cold cache
         flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
         ev = []
         for _ in range(5):

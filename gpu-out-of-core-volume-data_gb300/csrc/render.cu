@@ -296,6 +296,9 @@ struct Walk {
     uint32_t flag;   // flag of the entry last read (0 unmapped, 1 mapped, 2 empty, 3 in flight)
     const uint8_t *base;  // pool slot of a mapped entry (decoded when the entry is read)
     bool invisible;  // the mapped brick holds no value the view's transfer function shows
+    // two-level directory: the directory word last read and its value (a ray
+    // crosses several bricks of one table block in a row)
+    uint32_t pword, ptop;
 };
 
 // Voxel sampling of one brick (slot base address), typed by T; MixedVoxel
@@ -425,11 +428,26 @@ __device__ __forceinline__ uint32_t entry_index(const CacheView &cv, const Level
 // two-level directory (the one-level kernels carry none of this).
 template <bool TL>
 __device__ __forceinline__ uint4 load_entry(const CacheView &cv, const LevelTables &lt, uint32_t lvl, uint32_t idx,
-                                            uint3 q) {
+                                            uint3 q, Walk *w) {
     if constexpr (!TL) return __ldg(cv.mrpd + idx);
-    const uint32_t t = __ldg(cv.pt.top + pt_word(cv.pt, lt, lvl, q.x, q.y, q.z));
+    const uint32_t word = pt_word(cv.pt, lt, lvl, q.x, q.y, q.z);
+    uint32_t t;
+    if (w && word == w->pword) {
+        t = w->ptop;  // same block as the entry before: read and stamped then
+    } else {
+        t = __ldg(cv.pt.top + word);
+        if (w) {
+            w->pword = word;
+            w->ptop = t;
+        }
+        if (t & 1u) {
+            // many rays share a table block: the stamp is stored only where the
+            // word does not hold it yet (a stale read only repeats the store)
+            uint32_t *u = cv.pt.usage + (t >> 1);
+            if (*u != cv.ts) *u = cv.ts;
+        }
+    }
     if (!(t & 1u)) return make_uint4(0u, 0u, 0u, 0u);
-    cv.pt.usage[t >> 1] = cv.ts;
     return __ldg(cv.pt.table + pt_entry(cv.pt, t >> 1, pt_local(cv.pt, q.x, q.y, q.z)));
 }
 
@@ -460,7 +478,7 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
         // A new entry: the entry and its value bins are read together (one
         // memory round trip); the usage stamp of a mapped brick is a plain
         // store (idempotent, like the reference's per-sample stamp).
-        const uint4 e = load_entry<TL>(cv, lt, lvl, idx, q);
+        const uint4 e = load_entry<TL>(cv, lt, lvl, idx, q, &w);
         const unsigned long long bins = __ldg(cv.entry_bins + idx);
         w.pidx = idx;
         w.flag = e.w;
@@ -496,7 +514,8 @@ __device__ __forceinline__ int fetch(const CacheView &cv, const LevelTables &lt,
             const uint3 q2 = make_uint3(static_cast<uint32_t>(qx * static_cast<float>(lt.nb[l2][0])),
                                         static_cast<uint32_t>(qy * static_cast<float>(lt.nb[l2][1])),
                                         static_cast<uint32_t>(qz * static_cast<float>(lt.nb[l2][2])));
-            const uint4 e2 = load_entry<TL>(cv, lt, l2, lt.off[l2] + q2.x + q2.y * cv.mx + q2.z * cv.mxy, q2);
+            const uint4 e2 =
+                load_entry<TL>(cv, lt, l2, lt.off[l2] + q2.x + q2.y * cv.mx + q2.z * cv.mxy, q2, nullptr);
             if (e2.w == 2u) return kEmpty;
             if (e2.w != 1u) continue;
             const uint32_t B = cv.B;
@@ -643,6 +662,7 @@ __device__ __forceinline__ bool ray_setup(const LevelTables &lt, const ViewParam
     r.sampler = vp.sampler;
     r.t_lo = lod_keep_bound(r.sL, r.sU, r.endX, r.endY, r.tfar, r.lvl + 1 >= r.lvl_end);
     r.w.pidx = UINT_MAX;
+    r.w.pword = UINT_MAX;
     r.w.flag = 0;
     r.w.base = nullptr;
     r.w.invisible = false;
@@ -829,7 +849,7 @@ __device__ __forceinline__ void retire_warp(uint32_t *queue, uint32_t nwarps) {
 // Tile scheduler: a warp takes one tile (tile_w x 32/tile_w pixels) at a time
 // from the queue and marches its 32 rays to completion.
 template <typename T, uint32_t BS, bool TL>
-__global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_kernel(const CacheView cv, const LevelTables lt,
+__global__ void __launch_bounds__(256, TL ? 3 : GC_RENDER_MIN_BLOCKS) render_kernel(const CacheView cv, const LevelTables lt,
                                                      const ViewParams *__restrict__ views, uint32_t nviews,
                                                      uint32_t total_tiles, uint32_t *queue, uint32_t nwarps) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -874,7 +894,7 @@ __global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_kernel(const
 // waits for its slowest ray.  Pixels are enumerated tile by tile, which keeps
 // consecutive grabs spatially close.
 template <typename T, uint32_t BS, bool TL>
-__global__ void __launch_bounds__(256, GC_RENDER_MIN_BLOCKS) render_pixels_kernel(const CacheView cv, const LevelTables lt,
+__global__ void __launch_bounds__(256, TL ? 3 : GC_RENDER_MIN_BLOCKS) render_pixels_kernel(const CacheView cv, const LevelTables lt,
                                                             const ViewParams *__restrict__ views, uint32_t nviews,
                                                             uint32_t total_tiles, uint32_t *queue, uint32_t nwarps) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -935,7 +955,8 @@ void *march_kernel_bs(uint32_t kind, bool pixels) {
     }
 }
 void *march_kernel(uint32_t kind, bool pixels, uint32_t brick_size, bool two_level) {
-    if (two_level) return march_kernel_bs<0, true>(kind, pixels);
+    if (two_level)
+        return brick_size == 16 ? march_kernel_bs<16, true>(kind, pixels) : march_kernel_bs<0, true>(kind, pixels);
     if (brick_size == 16) return march_kernel_bs<16, false>(kind, pixels);
     if (brick_size == 32) return march_kernel_bs<32, false>(kind, pixels);
     return march_kernel_bs<0, false>(kind, pixels);
@@ -1062,9 +1083,9 @@ static RenderLaunch render_launch_config(uint32_t eb, uint32_t brick_size, bool 
                               : exact::march_kernel(eb, pix, brick_size, two_level);
     if (!kernel) fail(GC_ERR_UNSUPPORTED, "the ray caster supports one channel of 1, 2 or 4 bytes");
     const int slot = eb == 1 ? 0 : eb == 2 ? 1 : eb == 4 ? 2 : eb == 0 ? 3 : 4;
-    static int occupancy[2][2][5][3][4] = {};
+    static int occupancy[2][2][5][3][5] = {};
     const int tslot = threads == 64 ? 0 : (threads == 128 ? 1 : 2);
-    const int bslot = two_level ? 3 : (brick_size == 16 ? 0 : (brick_size == 32 ? 1 : 2));
+    const int bslot = two_level ? (brick_size == 16 ? 3 : 4) : (brick_size == 16 ? 0 : (brick_size == 32 ? 1 : 2));
     int &occ = occupancy[fast_build ? 1 : 0][pix ? 1 : 0][slot][tslot][bslot];
     if (!occ) {
         int b = 0;
