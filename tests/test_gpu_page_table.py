@@ -144,3 +144,39 @@ def test_user_kernel_two_level(gc, orc, torch_cuda, user_lib):  # noqa: F811
                       (gc.DUMP_PT_USAGE, oc.pt_usage())):
         got = cm.dump(what, np.zeros_like(ref))
         assert np.array_equal(got, ref), what
+
+
+@pytest.mark.parametrize("sync", [True, False])
+def test_two_level_batch_matches_single_views(gc, orc, torch_cuda, sync):
+    """Continuous batching over a two-level cache (P = 2, a table pool for
+    every block) gives every view the image it gets rendered alone through a
+    one-level cache; overlapped loads are refused for a two-level cache."""
+    from test_gpu_render import single_view_images
+
+    specs = [((64, 48), 1), ((33, 17), 4), ((96, 80), 7), ((40, 40), 10), ((80, 24), 5)]
+    tf_dev = torch_cuda.from_numpy(scenario.ramp_tf().reshape(-1)).cuda()
+    single = single_view_images(gc, orc, torch_cuda, specs, tf_dev)
+    s2 = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 64, sync=sync, pt_block=2,
+               pt_slots=64)
+    if not sync:
+        with pytest.raises(gc.GcError, match="one-level page directory"):
+            gc.Batch(s2.cm, overlap_loads=True)
+    b = gc.Batch(s2.cm, max_views=3, max_pixels=96 * 80 + 64 * 48)
+    bufs = []
+    for i, ((W, H), cam) in enumerate(specs):
+        g, _ = s2.buffers(W, H)
+        bufs.append(g)
+        b.submit(s2.view(scenario.orbit_camera(gc, cam, 12, 3.0), W, H, tf_dev, 256, g), tag=100 + i)
+    results = []
+    for _ in range(4000):
+        b.tick()
+        results += b.poll()
+        if len(results) == len(specs):
+            break
+    assert sorted(r[0] for r in results) == [100 + i for i in range(len(specs))]
+    assert all(r[2] for r in results)
+    torch_cuda.cuda.synchronize()
+    for i in range(len(specs)):
+        assert np.array_equal(bufs[i][0].cpu().numpy(), single[i]), i
+    b.close()
+    assert s2.cm.stats().device_error == 0
