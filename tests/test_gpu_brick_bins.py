@@ -88,11 +88,11 @@ def converge(cm, v, st, cap=96):
     return False
 
 
-def render_views(gc, torch, built, specs, tf, use_bins, sync=True, mode=0, warm=False, cache=(6, 6, 6)):
+def render_views(gc, torch, built, specs, tf, use_bins, sync=True, mode=0, warm=False, cache=(6, 6, 6), **cache_kw):
     """Each view to convergence (plain frame loop); warm: then once more from
     cleared buffers, with every brick it needs resident (no ray pauses)."""
     vol, layout, store, offs, empty, bins = built
-    cm = gc.CacheManager(vol, layout, cache, max_requests=96, sync_loader=sync)
+    cm = gc.CacheManager(vol, layout, cache, max_requests=96, sync_loader=sync, **cache_kw)
     cm.set_source_host(store, offs, empty)
     if use_bins:
         cm.set_brick_bins(bins)

@@ -180,3 +180,24 @@ def test_two_level_batch_matches_single_views(gc, orc, torch_cuda, sync):
         assert np.array_equal(bufs[i][0].cpu().numpy(), single[i]), i
     b.close()
     assert s2.cm.stats().device_error == 0
+
+
+def test_two_level_with_brick_bins(gc, torch_cuda):
+    """Brick value bins over a two-level cache: with a table pool for every
+    block the warm images equal the one-level cache's without bins; with a
+    table pool that evicts (the bins of an evicted block's bricks revert to
+    the user's), each view still converges within the reference's own
+    resume spread of those images."""
+    from test_gpu_brick_bins import IN_CORE, RESUME_TOL, SPECS, build, render_views
+    from test_gpu_brick_bins import rgba_diff as bins_diff
+
+    built = build(gc, torch_cuda, (96, 96, 96), 1, 16, 1, (1, 1, 1), empty_threshold=30.0)
+    tf = scenario.ramp_tf()
+    ref, _ = render_views(gc, torch_cuda, built, SPECS, tf, False, warm=True, cache=IN_CORE)
+    roomy, sr = render_views(gc, torch_cuda, built, SPECS, tf, True, warm=True, cache=IN_CORE, pt_block=2,
+                             pt_slots=512)
+    small, ss = render_views(gc, torch_cuda, built, SPECS, tf, True, cache=IN_CORE, pt_block=2, pt_slots=16)
+    for i in range(len(SPECS)):
+        assert np.array_equal(ref[i], roomy[i]), i
+        assert bins_diff(ref[i], small[i]).max() <= RESUME_TOL, i
+    assert sr.device_error == 0 and ss.device_error == 0
