@@ -53,8 +53,11 @@ def run_batch(gc, cm, views, max_views):
     return results
 
 
-@pytest.mark.parametrize("sync", [True, False])
-def test_shared_pool_views_equal_single_volume_caches(gc, torch_cuda, sync):
+@pytest.mark.parametrize("sync,pt_block", [(True, 0), (False, 0), (True, 2), (False, 4)])
+def test_shared_pool_views_equal_single_volume_caches(gc, torch_cuda, sync, pt_block):
+    """pt_block > 0: the shared cache with a two-level page directory (one
+    directory word per pt_block^3 bricks of each volume's levels, a table pool
+    for every block)."""
     torch = torch_cuda
     built = [build(gc, torch, *v) for v in VOLUMES]
     tf_dev = torch.from_numpy(scenario.ramp_tf().reshape(-1)).cuda()
@@ -84,7 +87,8 @@ def test_shared_pool_views_equal_single_volume_caches(gc, torch_cuda, sync):
 
     # one shared pool; every view served in one mix (continuous batching)
     shared = [(vol, layout) for vol, layout, _, _ in built]
-    cm = gc.CacheManager(built[0][0], built[0][1], (9, 9, 9), max_requests=128, sync_loader=sync, shared=shared)
+    cm = gc.CacheManager(built[0][0], built[0][1], (9, 9, 9), max_requests=128, sync_loader=sync, shared=shared,
+                         pt_block=pt_block, pt_slots=1024 if pt_block else 0)
     for k, (_, _, store, offs) in enumerate(built):
         cm.set_source_host(store, offs, volume=k)
     bases = [cm.volume_levels(k) for k in range(len(built))]
