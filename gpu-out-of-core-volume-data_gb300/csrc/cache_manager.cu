@@ -179,7 +179,6 @@ struct gc_cache {
     ulonglong2 *h_src = nullptr;
     uint8_t *h_staging = nullptr;
     cudaStream_t side = nullptr;
-    cudaStream_t frame_stream = nullptr;  // stream of the update in progress (synchronous loader)
     cudaEvent_t ev_upload = nullptr, ev_upload_begin = nullptr;
     bool upload_timed = false;  // ev_upload_begin/ev_upload bracket an upload not yet counted
     int cur = 0;
@@ -441,16 +440,18 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     C->stats.loader_host_ns += static_cast<uint64_t>(
         std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t_begin).count());
     if (k == 0) return;
-    // With the synchronous loader a gather upload goes on the caller's stream,
-    // ahead of the next frame's render: on a side stream it can wait behind a
-    // persistent ray-caster launch that holds every SM.  Staged copies (copy
-    // engine) and the asynchronous loader use the high-priority side stream.
+    // The upload goes on the high-priority side stream, beside the next
+    // frame's render (the install of the next update waits for it): the
+    // gather kernel's small blocks fit next to a persistent ray-caster launch
+    // at its occupancy, so the bricks cross the host link while the frame
+    // renders.  The staging buffers are free: the install that read them is
+    // ahead of the scan this list came from.
     const bool gather = C->gather;
-    cudaStream_t s = C->sync_mode() && gather ? C->frame_stream : C->side;
+    cudaStream_t s = C->side;
     GC_CUDA(cudaEventRecord(C->ev_upload_begin, s));
     if (nhost && gather) {
         GC_CUDA(cudaMemcpyAsync(C->d_src, C->h_src, nbig * sizeof(ulonglong2), cudaMemcpyHostToDevice, s));
-        launch_gather_bricks(C->d_src, nbig, C->big_stride, C->d_staging, C->vec16, !C->sync_mode(), s);
+        launch_gather_bricks(C->d_src, nbig, C->big_stride, C->d_staging, C->vec16, true, s);
     } else if (nhost) {
         GC_CUDA(cudaMemcpyAsync(C->d_staging, C->h_staging, static_cast<size_t>(nbig) * C->big_stride,
                                 cudaMemcpyHostToDevice, s));
@@ -624,7 +625,6 @@ static void scan_requests(gc_cache *C, cudaStream_t s, int slot = 0, bool mark =
 
 static bool update(gc_cache *C, cudaStream_t s) {
     GC_CUDA(cudaSetDevice(C->device));
-    C->frame_stream = s;
     lru_update(C, s);
     bool converged = false;
     if (C->sync_mode()) {
@@ -1600,7 +1600,6 @@ static bool loader_idle(gc_cache *C) {
 // End of a rendered tick: LRU update and, with the loader idle, the scan.
 // Returns true when a scan was issued (its miss count lands in h_total).
 static bool batch_update(gc_cache *C, cudaStream_t s) {
-    C->frame_stream = s;
     lru_update(C, s);
     bool scanned = false;
     if (C->sync_mode()) {
@@ -1889,7 +1888,6 @@ static void batch_tick_overlapped(gc_batch *b, gc_cache *C, cudaStream_t s, uint
     lru_update(C, s);
     GC_CUDA(cudaMemcpyAsync(b->h_status + b->d.max_views, C->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     // 4. their requests into the free list, marked in flight
-    C->frame_stream = s;
     scan_requests(C, s, free_slot, true);
     const uint64_t serial = b->next_serial++;
     b->slot_state[free_slot] = 1;
