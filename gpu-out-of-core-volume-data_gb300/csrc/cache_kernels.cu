@@ -837,9 +837,11 @@ void launch_gather_bricks(const ulonglong2 *src, uint32_t n, uint64_t stride, ui
         // Next to a persistent ray-caster launch: at its occupancy each SM
         // sub-partition keeps 1024 registers free, room for one warp of 32
         // registers per thread -- 128-thread blocks (one warp per
-        // sub-partition), two per SM over the grid, run during the render
-        // instead of after it (two 16-byte loads in flight per thread).
-        const uint32_t grid = std::min<uint32_t>(n, 2 * sms);
+        // sub-partition), one per SM, run during the render instead of after
+        // it (two 16-byte loads in flight per thread).  A second block per
+        // SM, resident before the render's blocks arrive, would hold
+        // registers a ray-caster block needs.
+        const uint32_t grid = std::min<uint32_t>(n, sms);
         if (vec16)
             gather_bricks_beside_kernel<uint4><<<grid, 128, 0, s>>>(src, n, stride, dst);
         else
