@@ -57,7 +57,10 @@ extern "C" {
 
 /* cache flags */
 #define GC_CACHE_SYNC_LOADER 1u   /* loader completes inside update(): deterministic
-                                     request -> install alternation            */
+                                     request -> install alternation (the upload
+                                     it starts runs on the cache's side stream,
+                                     beside the next render; the next update's
+                                     install waits for it)                     */
 #define GC_CACHE_STAGED_UPLOAD 2u /* host-store bricks always go through the pinned
                                      staging buffer + cudaMemcpyAsync, even when
                                      the device can read the store directly     */
