@@ -154,39 +154,33 @@ struct gc_cache {
     uint64_t *status_lru = nullptr, *status_miss = nullptr;
     gc::ScanCtl *ctl_lru = nullptr, *ctl_miss = nullptr;
     uint32_t *d_count = nullptr, *d_misc = nullptr, *d_queue = nullptr;
+    uint4 *d_asked = nullptr, *d_big_coord = nullptr;
     uint32_t *d_owner = nullptr;   // install: lowest list index per page-directory entry (~0 between installs)
     uint64_t *d_coords = nullptr;  // install: page-directory entry per list element
+    uint32_t *d_big_index = nullptr;
+    ulonglong2 *d_src = nullptr;      // gather list: {host address, bytes} per big brick
+    uint8_t *d_staging = nullptr;
     gc::CutSources cut;               // device-resident pyramids of the volumes that have one
-    bool has_cut = false;             // some volume has one (load buffers carry cut jobs)
+    uint4 *d_cut = nullptr, *h_cut = nullptr;  // cut jobs of a load cycle (device-levels sources)
     ResolveScratch resolve;           // the loader's per-cycle scratch
     gc::ViewParams *d_views = nullptr;
     uint32_t max_views = 256;
-    uint32_t *h_misc = nullptr;
+    // pinned host buffers
+    uint4 *h_asked = nullptr, *h_big_coord = nullptr;
+    uint32_t *h_big_index = nullptr, *h_misc = nullptr;
     // Miss lists: the scan writes one, the loader serves one.  The plain frame
     // loop only uses list 0; the batched form's overlapped loads use both.
-    // Each list owns the buffers of the load made from it (the asked list,
-    // big-brick indexes, gather list, staging), so that the loader can load
-    // one list while the other list's load waits for its install.
     struct MissList {
         uint4 *d = nullptr, *h = nullptr;  // up to max_requests (x, y, z, level)
         uint32_t *total = nullptr;         // pinned: misses found (uncapped)
         cudaEvent_t ev = nullptr;          // the list and total are on the host
-        // the load (device / pinned host)
-        uint4 *d_asked = nullptr, *d_big_coord = nullptr, *d_cut = nullptr;
-        uint32_t *d_big_index = nullptr;
-        ulonglong2 *d_src = nullptr;       // gather list: {host address, bytes} per big brick
-        uint8_t *d_staging = nullptr;
-        uint4 *h_asked = nullptr, *h_big_coord = nullptr, *h_cut = nullptr;  // cut jobs: device-levels sources
-        uint32_t *h_big_index = nullptr;
-        ulonglong2 *h_src = nullptr;
-        uint8_t *h_staging = nullptr;
-        cudaEvent_t ev_upload = nullptr, ev_upload_begin = nullptr;
-        bool upload_timed = false;         // ev_upload_begin/ev_upload bracket an upload not yet counted
-        uint32_t pend_n = 0, pend_nonempty = 0;  // bricks to install (non-empty first)
-        bool loaded = false;               // the loader finished a load from this list, not installed yet
     } lists[2];
     int cur_load = 0;  // list the loader serves
+    ulonglong2 *h_src = nullptr;
+    uint8_t *h_staging = nullptr;
     cudaStream_t side = nullptr;
+    cudaEvent_t ev_upload = nullptr, ev_upload_begin = nullptr;
+    bool upload_timed = false;  // ev_upload_begin/ev_upload bracket an upload not yet counted
     int cur = 0;
     uint32_t ts = 1, epoch_lru = 0, epoch_miss = 0;
     // loader
@@ -196,6 +190,7 @@ struct gc_cache {
     std::mutex mu;
     std::condition_variable cv;
     bool stop = false, has_request = false, busy = false, done = false, last_converged = false;
+    uint32_t pend_n = 0, pend_nonempty = 0;
     std::string loader_error;
     gc_cache_stats stats;
 
@@ -267,7 +262,6 @@ static void build_tables(gc_cache *C) {
 // Returns the number of bricks to install (non-empty first), or 0.
 static void resolve_and_upload(gc_cache *C, uint32_t n) {
     const auto t_begin = std::chrono::steady_clock::now();
-    gc_cache::MissList &LB = C->lists[C->cur_load];  // the list and the buffers of its load
     ResolveScratch &R = C->resolve;
     R.kind.assign(n, 0);  // 0 non-empty, 1 empty, 2 unknown (dropped)
     std::vector<int> &kind = R.kind;
@@ -329,7 +323,7 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
         int status = GC_BRICK_UNKNOWN;
         bool on_device = false;
         const Source &src = V.src;
-        uint8_t *stage = LB.h_staging + static_cast<uint64_t>(nbig) * C->big_stride;
+        uint8_t *stage = C->h_staging + static_cast<uint64_t>(nbig) * C->big_stride;
         if (!src.empty.empty() && src.empty.count(gc_brick_key(lvl, gx, gy, gz))) {  // the volume's own keys
             status = GC_BRICK_EMPTY;
         } else if (src.kind == 1) {
@@ -340,7 +334,7 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
                     (static_cast<uint64_t>(gz) * L.nb_big_bricks[lvl][1] + gy) * L.nb_big_bricks[lvl][0] + gx;
                 const uint64_t off = src.level_off[lvl] + idx * V.big_bytes;  // inside the store (checked)
                 if (C->gather)
-                    LB.h_src[nbig] = make_ulonglong2(reinterpret_cast<uint64_t>(src.dev + off), V.big_bytes);
+                    C->h_src[nbig] = make_ulonglong2(reinterpret_cast<uint64_t>(src.dev + off), V.big_bytes);
                 else
                     copies.push_back({src.host + off, stage, V.big_bytes});
                 status = GC_BRICK_SUCCESS;
@@ -352,8 +346,8 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
             if (lvl < L.nb_levels && gx < L.nb_big_bricks[lvl][0] && gy < L.nb_big_bricks[lvl][1] &&
                 gz < L.nb_big_bricks[lvl][2]) {
                 const uint32_t vol = C->level_volume[b.w];
-                LB.h_cut[ncut++] = make_uint4(gx, gy, gz, (nbig << 8) | (vol << 6) | lvl);
-                if (C->gather) LB.h_src[nbig] = make_ulonglong2(0, 0);  // nothing to gather for this slot
+                C->h_cut[ncut++] = make_uint4(gx, gy, gz, (nbig << 8) | (vol << 6) | lvl);
+                if (C->gather) C->h_src[nbig] = make_ulonglong2(0, 0);  // nothing to gather for this slot
                 on_device = true;
                 status = GC_BRICK_SUCCESS;
             }
@@ -373,7 +367,7 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
                 ++nhost;
             }
             val = static_cast<int32_t>(nbig);
-            LB.h_big_coord[nbig] = make_uint4(gx, gy, gz, b.w);
+            C->h_big_coord[nbig] = make_uint4(gx, gy, gz, b.w);
             big_index.push_back(nbig);
             ++nbig;
             ++n_nonempty;
@@ -436,12 +430,12 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     // stable partition: non-empty first, then empty (RequestHandler.hpp:354-369)
     uint32_t k = 0;
     for (uint32_t i = 0; i < n; ++i)
-        if (kind[i] == 0) LB.h_asked[k++] = C->lists[C->cur_load].h[i];
+        if (kind[i] == 0) C->h_asked[k++] = C->lists[C->cur_load].h[i];
     for (uint32_t i = 0; i < n; ++i)
-        if (kind[i] == 1) LB.h_asked[k++] = C->lists[C->cur_load].h[i];
-    std::memcpy(LB.h_big_index, big_index.data(), big_index.size() * sizeof(uint32_t));
-    LB.pend_n = k;
-    LB.pend_nonempty = n_nonempty;
+        if (kind[i] == 1) C->h_asked[k++] = C->lists[C->cur_load].h[i];
+    std::memcpy(C->h_big_index, big_index.data(), big_index.size() * sizeof(uint32_t));
+    C->pend_n = k;
+    C->pend_nonempty = n_nonempty;
     C->stats.load_cycles++;
     C->stats.loader_host_ns += static_cast<uint64_t>(
         std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t_begin).count());
@@ -454,27 +448,27 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     // ahead of the scan this list came from.
     const bool gather = C->gather;
     cudaStream_t s = C->side;
-    GC_CUDA(cudaEventRecord(LB.ev_upload_begin, s));
+    GC_CUDA(cudaEventRecord(C->ev_upload_begin, s));
     if (nhost && gather) {
-        GC_CUDA(cudaMemcpyAsync(LB.d_src, LB.h_src, nbig * sizeof(ulonglong2), cudaMemcpyHostToDevice, s));
-        launch_gather_bricks(LB.d_src, nbig, C->big_stride, LB.d_staging, C->vec16, true, s);
+        GC_CUDA(cudaMemcpyAsync(C->d_src, C->h_src, nbig * sizeof(ulonglong2), cudaMemcpyHostToDevice, s));
+        launch_gather_bricks(C->d_src, nbig, C->big_stride, C->d_staging, C->vec16, true, s);
     } else if (nhost) {
-        GC_CUDA(cudaMemcpyAsync(LB.d_staging, LB.h_staging, static_cast<size_t>(nbig) * C->big_stride,
+        GC_CUDA(cudaMemcpyAsync(C->d_staging, C->h_staging, static_cast<size_t>(nbig) * C->big_stride,
                                 cudaMemcpyHostToDevice, s));
     }
     if (ncut) {  // after the host bricks: a staged copy covers every slot
-        GC_CUDA(cudaMemcpyAsync(LB.d_cut, LB.h_cut, ncut * sizeof(uint4), cudaMemcpyHostToDevice, s));
-        launch_cut_bricks(C->cut, LB.d_cut, ncut, LB.d_staging, C->big_stride, s);
+        GC_CUDA(cudaMemcpyAsync(C->d_cut, C->h_cut, ncut * sizeof(uint4), cudaMemcpyHostToDevice, s));
+        launch_cut_bricks(C->cut, C->d_cut, ncut, C->d_staging, C->big_stride, s);
     }
-    GC_CUDA(cudaMemcpyAsync(LB.d_asked, LB.h_asked, k * sizeof(uint4), cudaMemcpyHostToDevice, s));
+    GC_CUDA(cudaMemcpyAsync(C->d_asked, C->h_asked, k * sizeof(uint4), cudaMemcpyHostToDevice, s));
     if (n_nonempty) {
-        GC_CUDA(cudaMemcpyAsync(LB.d_big_index, LB.h_big_index, n_nonempty * sizeof(uint32_t),
+        GC_CUDA(cudaMemcpyAsync(C->d_big_index, C->h_big_index, n_nonempty * sizeof(uint32_t),
                                 cudaMemcpyHostToDevice, s));
-        GC_CUDA(cudaMemcpyAsync(LB.d_big_coord, LB.h_big_coord, std::max(1u, nbig) * sizeof(uint4),
+        GC_CUDA(cudaMemcpyAsync(C->d_big_coord, C->h_big_coord, std::max(1u, nbig) * sizeof(uint4),
                                 cudaMemcpyHostToDevice, s));
     }
-    GC_CUDA(cudaEventRecord(LB.ev_upload, s));
-    LB.upload_timed = true;
+    GC_CUDA(cudaEventRecord(C->ev_upload, s));
+    C->upload_timed = true;
     C->stats.bytes_h2d += bytes_up;
     C->stats.requests_served += n;
 }
@@ -483,18 +477,16 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
 // bricks are pending for install.
 static bool serve_request(gc_cache *C) {
     GC_CUDA(cudaSetDevice(C->device));
-    gc_cache::MissList &LB = C->lists[C->cur_load];
-    GC_CUDA(cudaEventSynchronize(LB.ev));
-    // The list's previous upload has normally completed (its install ran
-    // before this scan); waiting on it also keeps the staging buffers from
-    // being refilled under a copy when the caller switches streams between
-    // frames.
-    if (LB.upload_timed) {
-        GC_CUDA(cudaEventSynchronize(LB.ev_upload));
+    GC_CUDA(cudaEventSynchronize(C->lists[C->cur_load].ev));
+    // The previous upload has normally completed (its install ran before this
+    // scan); waiting on it also keeps the staging buffers from being refilled
+    // under a copy when the caller switches streams between frames.
+    if (C->upload_timed) {
+        GC_CUDA(cudaEventSynchronize(C->ev_upload));
         float ms = 0.f;
-        GC_CUDA(cudaEventElapsedTime(&ms, LB.ev_upload_begin, LB.ev_upload));
+        GC_CUDA(cudaEventElapsedTime(&ms, C->ev_upload_begin, C->ev_upload));
         C->stats.upload_ns += static_cast<uint64_t>(static_cast<double>(ms) * 1e6);
-        LB.upload_timed = false;
+        C->upload_timed = false;
     }
     const uint32_t total = *C->lists[C->cur_load].total;
     const uint32_t n = std::min(total, C->d.max_requests);
@@ -502,7 +494,7 @@ static bool serve_request(gc_cache *C) {
     C->stats.requests_raised += total;
     if (n == 0) return false;
     resolve_and_upload(C, n);
-    return LB.pend_n > 0;
+    return C->pend_n > 0;
 }
 
 static void loader_main(gc_cache *C) {
@@ -522,7 +514,6 @@ static void loader_main(gc_cache *C) {
         }
         lk.lock();
         C->done = pending;
-        C->lists[C->cur_load].loaded = pending;
         C->last_converged = converged;
         if (!err.empty()) C->loader_error = err;
         C->busy = false;
@@ -575,37 +566,9 @@ static void lru_update(gc_cache *C, cudaStream_t s) {
     }
 }
 
-// The buffers of the loads made from miss list k (list 1 only for the
-// batched form's overlapped loads); cut jobs where a volume has a
-// device-levels source.
-static void alloc_load_buffers(gc_cache *C, int k) {
-    gc_cache::MissList &L = C->lists[k];
-    const uint32_t maxr = C->d.max_requests;
-    if (!L.d_staging) {
-        L.d_asked = dalloc<uint4>(maxr, "asked list");
-        L.d_big_coord = dalloc<uint4>(maxr, "big brick coords");
-        L.d_big_index = dalloc<uint32_t>(maxr, "big brick indexes");
-        L.d_src = dalloc<ulonglong2>(maxr, "brick gather list");
-        L.d_staging = dalloc<uint8_t>(maxr * C->big_stride, "staging");
-        L.h_asked = halloc<uint4>(maxr);
-        L.h_big_coord = halloc<uint4>(maxr);
-        L.h_big_index = halloc<uint32_t>(maxr);
-        L.h_src = halloc<ulonglong2>(maxr);
-        L.h_staging = halloc<uint8_t>(maxr * C->big_stride);
-        GC_CUDA(cudaEventCreate(&L.ev_upload));
-        GC_CUDA(cudaEventCreate(&L.ev_upload_begin));
-    }
-    if (C->has_cut && !L.d_cut) {
-        L.d_cut = dalloc<uint4>(maxr, "cut jobs");
-        L.h_cut = halloc<uint4>(maxr);
-    }
-}
-
-// Installs the load made from miss list k (the plain loop: list 0).
-static void install(gc_cache *C, cudaStream_t s, int k = 0) {
-    gc_cache::MissList &LB = C->lists[k];
-    if (LB.pend_n == 0) return;
-    GC_CUDA(cudaStreamWaitEvent(s, LB.ev_upload, 0));
+static void install(gc_cache *C, cudaStream_t s) {
+    if (C->pend_n == 0) return;
+    GC_CUDA(cudaStreamWaitEvent(s, C->ev_upload, 0));
     InstallArgs a;
     a.mrpd = C->mrpd;
     a.pt = C->pt;
@@ -634,19 +597,19 @@ static void install(gc_cache *C, cudaStream_t s, int k = 0) {
     a.entry_bins = C->entry_bins;
     a.user_bins = C->user_bins;
     a.nc = C->nc;
-    a.asked = LB.d_asked;
+    a.asked = C->d_asked;
     a.owner = C->d_owner;
     a.coords = C->d_coords;
-    a.big_index = LB.d_big_index;
-    a.big_coord = LB.d_big_coord;
-    a.staging = LB.d_staging;
-    a.n = LB.pend_n;
-    a.n_nonempty = std::min(LB.pend_nonempty, C->nslots);
+    a.big_index = C->d_big_index;
+    a.big_coord = C->d_big_coord;
+    a.staging = C->d_staging;
+    a.n = C->pend_n;
+    a.n_nonempty = std::min(C->pend_nonempty, C->nslots);
     launch_install(a, C->lt, s);
     C->stats.bricks_installed += a.n_nonempty;
-    C->stats.bricks_empty += a.n - LB.pend_nonempty;
-    LB.pend_n = 0;
-    LB.pend_nonempty = 0;
+    C->stats.bricks_empty += a.n - C->pend_nonempty;
+    C->pend_n = 0;
+    C->pend_nonempty = 0;
 }
 
 // Miss scan into list `slot`; mark: flag the listed entries in flight (3).
@@ -721,20 +684,18 @@ static void destroy(gc_cache *C) {
     void *dev[] = {C->pt.top, C->pt.table, C->pt.usage, C->pt_order[0], C->pt_order[1], C->pt_keys, C->pt_claim,
                    C->pt_word_of, C->pt_jobs, C->pt_njobs, C->status_pt, C->ctl_pt, C->mrpd, C->req, C->usage, C->order[0], C->order[1], C->slot_level, C->slot_vpos, C->pool, C->slot_bins, C->entry_bins, C->user_bins, C->d_samples,
                    C->status_lru, C->status_miss, C->ctl_lru, C->ctl_miss, C->d_count, C->d_misc, C->d_queue,
-                   C->d_owner, C->d_coords, C->d_views};
+                   C->lists[0].d, C->lists[1].d, C->d_asked, C->d_owner, C->d_coords, C->d_big_coord, C->d_big_index, C->d_src,
+                   C->d_staging, C->d_views, C->d_cut};
     for (void *p : dev)
         if (p) cudaFree(p);
-    for (auto &L : C->lists) {
-        void *ld[] = {L.d, L.d_asked, L.d_big_coord, L.d_cut, L.d_big_index, L.d_src, L.d_staging};
-        for (void *p : ld)
-            if (p) cudaFree(p);
-        void *lh[] = {L.h, L.total, L.h_asked, L.h_big_coord, L.h_cut, L.h_big_index, L.h_src, L.h_staging};
-        for (void *p : lh)
-            if (p) cudaFreeHost(p);
-        for (cudaEvent_t e : {L.ev, L.ev_upload, L.ev_upload_begin})
-            if (e) cudaEventDestroy(e);
-    }
-    if (C->h_misc) cudaFreeHost(C->h_misc);
+    void *host[] = {C->lists[0].h, C->lists[1].h, C->lists[0].total, C->lists[1].total, C->h_asked, C->h_big_coord,
+                    C->h_big_index, C->h_misc, C->h_src, C->h_staging, C->h_cut};
+    for (void *p : host)
+        if (p) cudaFreeHost(p);
+    for (auto &L : C->lists)
+        if (L.ev) cudaEventDestroy(L.ev);
+    if (C->ev_upload) cudaEventDestroy(C->ev_upload);
+    if (C->ev_upload_begin) cudaEventDestroy(C->ev_upload_begin);
     if (C->side) cudaStreamDestroy(C->side);
     delete C;
 }
@@ -1099,17 +1060,26 @@ int gc_cache_create_shared(const gc_cache_desc *desc, const gc_volume_desc *volu
         C->d_misc = dalloc<uint32_t>(1, "counter");
         C->d_queue = dalloc<uint32_t>(4, "work queue");
         for (auto &L : C->lists) L.d = dalloc<uint4>(maxr, "miss list");
+        C->d_asked = dalloc<uint4>(maxr, "asked list");
         C->d_coords = dalloc<uint64_t>(maxr, "install entries");
         C->d_owner = dalloc<uint32_t>(C->nentries, "install owners");
         GC_CUDA(cudaMemset(C->d_owner, 0xff, C->nentries * sizeof(uint32_t)));
+        C->d_big_coord = dalloc<uint4>(maxr, "big brick coords");
+        C->d_big_index = dalloc<uint32_t>(maxr, "big brick indexes");
+        C->d_src = dalloc<ulonglong2>(maxr, "brick gather list");
+        C->d_staging = dalloc<uint8_t>(maxr * C->big_stride, "staging");
         C->d_views = dalloc<ViewParams>(C->max_views, "views");
         for (auto &L : C->lists) {
             L.h = halloc<uint4>(maxr);
             L.total = halloc<uint32_t>(1);
             *L.total = 0;
         }
-        alloc_load_buffers(C, 0);
+        C->h_asked = halloc<uint4>(maxr);
+        C->h_big_coord = halloc<uint4>(maxr);
+        C->h_big_index = halloc<uint32_t>(maxr);
+        C->h_src = halloc<ulonglong2>(maxr);
         C->h_misc = halloc<uint32_t>(1);
+        C->h_staging = halloc<uint8_t>(maxr * C->big_stride);
         *C->h_misc = 0;
         GC_CUDA(cudaMemset(C->req, 0, C->nentries * sizeof(uint32_t)));
         GC_CUDA(cudaMemset(C->usage, 0, C->nslots * sizeof(uint32_t)));
@@ -1127,6 +1097,8 @@ int gc_cache_create_shared(const gc_cache_desc *desc, const gc_volume_desc *volu
         GC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
         GC_CUDA(cudaStreamCreateWithPriority(&C->side, cudaStreamNonBlocking, greatest));
         for (auto &L : C->lists) GC_CUDA(cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming));
+        GC_CUDA(cudaEventCreate(&C->ev_upload));
+        GC_CUDA(cudaEventCreate(&C->ev_upload_begin));
         GC_CUDA(cudaDeviceSynchronize());
         if (!C->sync_mode()) C->th = std::thread(loader_main, C);
         *out = C;
@@ -1230,9 +1202,10 @@ int gc_cache_set_volume_source_device(gc_cache_t C, uint32_t volume, const void 
         }
         std::lock_guard<std::mutex> g(C->mu);
         GC_REQUIRE(!C->busy, "the loader is busy");
-        C->has_cut = true;
-        for (int k = 0; k < 2; ++k)
-            if (C->lists[k].d_staging) alloc_load_buffers(C, k);
+        if (!C->d_cut) {
+            C->d_cut = dalloc<uint4>(C->d.max_requests, "cut jobs");
+            GC_CUDA(cudaMallocHost(reinterpret_cast<void **>(&C->h_cut), C->d.max_requests * sizeof(uint4)));
+        }
         C->cut.vol[volume] = cs;
         Source &src = C->vols[volume].src;
         src = Source();
@@ -1597,7 +1570,7 @@ namespace gc {
 static bool batch_install(gc_cache *C, cudaStream_t s) {
     if (C->sync_mode()) {
         if (!C->done) return false;
-        const bool any = C->lists[0].pend_n > 0;
+        const bool any = C->pend_n > 0;
         install(C, s);
         C->done = false;
         return any;
@@ -1610,7 +1583,7 @@ static bool batch_install(gc_cache *C, cudaStream_t s) {
     }
     if (C->busy || !C->done) return false;
     lk.unlock();
-    const bool any = C->lists[0].pend_n > 0;
+    const bool any = C->pend_n > 0;
     install(C, s);
     lk.lock();
     C->done = false;
@@ -1716,18 +1689,15 @@ static void batch_drain_loads(gc_batch *b) {
     if (!b->d.overlap_loads || (b->slot_state[0] == 0 && b->slot_state[1] == 0)) return;
     cudaSetDevice(C->device);
     cudaStream_t s = b->stream;
+    bool installable = false;
     {
         std::unique_lock<std::mutex> lk(C->mu);
         C->cv.wait(lk, [&] { return !C->busy; });  // the loader's load is finite
+        installable = C->done && b->slot_state[C->cur_load] == 2;
         C->done = false;
         C->loader_error.clear();
     }
-    // the finished loads, oldest first
-    int first = 0;
-    if (b->slot_state[1] == 2 && (b->slot_state[0] != 2 || b->slot_serial[1] < b->slot_serial[0])) first = 1;
-    for (int k : {first, 1 - first})
-        if (b->slot_state[k] == 2 && C->lists[k].loaded) install(C, s, k);
-    for (auto &L : C->lists) L.loaded = false;
+    if (installable) install(C, s);
     for (int k = 0; k < 2; ++k) {
         if (b->slot_state[k] == 0) continue;
         const gc_cache::MissList &L = C->lists[k];
@@ -1820,20 +1790,16 @@ static void batch_admit(gc_batch *b, gc_cache *C, cudaStream_t s, bool all, doub
 static void batch_tick_overlapped(gc_batch *b, gc_cache *C, cudaStream_t s, uint32_t *n_active,
                                   uint32_t *n_queued) {
     b->stream = s;
-    // The oldest waiting list goes to the loader when it is idle, even while
-    // the other list's load waits for its install: each list has its own load
-    // buffers, so the next upload queues behind the current one on the side
-    // stream and the host link stays busy.
-    auto hand_to_loader = [&] {
+    auto hand_to_loader = [&] {  // the oldest waiting list, if the loader is idle
         std::unique_lock<std::mutex> lk(C->mu);
-        if (C->busy) return;
+        if (C->busy || C->done) return;
         int pick = -1;
         for (int k = 0; k < 2; ++k)
             if (b->slot_state[k] == 1 && (pick < 0 || b->slot_serial[k] < b->slot_serial[pick])) pick = k;
         if (pick < 0) return;
-        // the loader waits on this event: it covers the scan of the list, and
-        // so the install of the list's previous load, which read the staging
-        // buffers that this load refills
+        // the loader waits on this event: it covers the scan of the list and
+        // the install just enqueued, which reads the staging buffers that
+        // the load refills
         GC_CUDA(cudaEventRecord(C->lists[pick].ev, s));
         C->cur_load = pick;
         b->slot_state[pick] = 2;
@@ -1841,23 +1807,19 @@ static void batch_tick_overlapped(gc_batch *b, gc_cache *C, cudaStream_t s, uint
         C->has_request = true;
         C->cv.notify_all();
     };
-    {  // 1. the loads the loader finished, oldest first
+    {  // 1. the load the loader finished
         std::unique_lock<std::mutex> lk(C->mu);
         if (!C->loader_error.empty()) {
             std::string e = C->loader_error;
             C->loader_error.clear();
             fail(GC_ERR_IO, "brick loader: " + e);
         }
-        for (;;) {
-            int k = -1;
-            for (int j = 0; j < 2; ++j)
-                if (b->slot_state[j] == 2 && (k < 0 || b->slot_serial[j] < b->slot_serial[k])) k = j;
-            if (k < 0 || (C->busy && C->cur_load == k)) break;  // none, or still being resolved
-            const bool installable = C->lists[k].loaded;
-            C->lists[k].loaded = false;
+        const int k = C->cur_load;
+        if (!C->busy && b->slot_state[k] == 2) {
+            const bool installable = C->done;
             lk.unlock();
             if (installable) {
-                install(C, s, k);
+                install(C, s);
                 b->installs++;
                 b->st.install_ticks++;
             }
@@ -1865,10 +1827,10 @@ static void batch_tick_overlapped(gc_batch *b, gc_cache *C, cudaStream_t s, uint
             launch_unmark_in_flight(L.d, std::min(*L.total, C->d.max_requests), C->lt, C->mx, C->my, C->nentries,
                                     C->mrpd, s);
             lk.lock();
+            C->done = false;
             b->slot_state[k] = 0;
             b->completed.insert(b->slot_serial[k]);
         }
-        C->done = false;  // the plain loop's flag; an overlapped batch tracks its loads per list
     }
     hand_to_loader();
     int free_slot = b->slot_state[0] == 0 ? 0 : (b->slot_state[1] == 0 ? 1 : -1);
@@ -1991,10 +1953,6 @@ int gc_batch_create(gc_cache_t C, const gc_batch_desc *desc, gc_batch_t *out) {
         GC_REQUIRE(!desc->overlap_loads || !C->pt.shift, "overlapped loads need the one-level page directory");
         GC_REQUIRE(!desc->overlap_loads || !(desc->park_above > 0.f), "parking is not available with overlapped loads");
         GC_CUDA(cudaSetDevice(C->device));
-        if (desc->overlap_loads) {
-            std::lock_guard<std::mutex> g(C->mu);
-            alloc_load_buffers(C, 1);  // the second list's loads
-        }
         b = new gc_batch();
         b->cache = C;
         b->d = *desc;
