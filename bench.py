@@ -50,6 +50,7 @@ import argparse
 import json
 import math
 import os
+import platform
 import statistics
 import shutil
 import subprocess
@@ -1576,6 +1577,27 @@ def vol_bytes_per_voxel(cfg):
     return cfg["bpc"] * cfg.get("channels", 1)
 
 
+ARM_PARTS = {"0xd4f": "Neoverse-V2", "0xd40": "Neoverse-V1", "0xd0c": "Neoverse-N1", "0xd49": "Neoverse-N2"}
+
+
+def host_cpu():
+    """The host CPU's model name (x86: /proc/cpuinfo "model name"; Arm: the
+    implementer's part number) for the CPU baselines."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            info = f.read()
+    except OSError:
+        return platform.machine()
+    for line in info.splitlines():
+        if line.lower().startswith("model name"):
+            return line.split(":", 1)[1].strip()
+    for line in info.splitlines():
+        if line.startswith("CPU part"):
+            part = line.split(":", 1)[1].strip().lower()
+            return f"{platform.machine()} {ARM_PARTS.get(part, 'part ' + part)}"
+    return platform.machine()
+
+
 def cpu_baseline(gc, S, cfg, spec, args, images):
     """The oracle's FP32 ray-march (all host threads) on a bounded sample of
     converged c2 views, reading a snapshot of the GPU's cache state; its image
@@ -1645,6 +1667,7 @@ def cpu_baseline(gc, S, cfg, spec, args, images):
         reps += 1
     brick_cpu = reps * level.nbytes / (time.perf_counter() - t1) / 1e9
     return {"value": round(W * H * frames / el / 1e6, 4), "unit": "Mrays/s", "cores": os.cpu_count(),
+            "cpu_model": host_cpu(),
             "mip_cpu_gbs_1thread": round(mip_cpu, 2), "mip_cpu_gbs_all_cores": round(mip_cpu_all, 2),
             "bricking_cpu_gbs_1thread": round(brick_cpu, 3),
             "kind": "port", "sample": f"{frames} renders of one converged {W}x{H} {args.config} view from the GPU's cache "
@@ -1747,7 +1770,8 @@ def run_reference(args):
            "iterations_per_view": {"mean": round(statistics.mean(i for i, _ in info), 2),
                                    "max": max(i for i, _ in info)},
            "converged_views": f"{sum(1 for _, c in info if c)}/{len(views)}",
-           "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
+           "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": os.cpu_count(),
+                            "cpu_model": host_cpu(), "kind": "port",
                             "sample": sample},
            "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
