@@ -1585,16 +1585,16 @@ def host_cpu():
     implementer's part number) for the CPU baselines."""
     try:
         with open("/proc/cpuinfo") as f:
-            info = f.read()
-    except OSError:
-        return platform.machine()
-    for line in info.splitlines():
-        if line.lower().startswith("model name"):
-            return line.split(":", 1)[1].strip()
-    for line in info.splitlines():
-        if line.startswith("CPU part"):
-            part = line.split(":", 1)[1].strip().lower()
-            return f"{platform.machine()} {ARM_PARTS.get(part, 'part ' + part)}"
+            lines = f.read().splitlines()
+        for line in lines:
+            if line.lower().startswith("model name") and ":" in line:
+                return line.split(":", 1)[1].strip()
+        for line in lines:
+            if line.startswith("CPU part") and ":" in line:
+                part = line.split(":", 1)[1].strip().lower()
+                return f"{platform.machine()} {ARM_PARTS.get(part, 'part ' + part)}"
+    except Exception:  # a reported detail: never fails the line
+        pass
     return platform.machine()
 
 
