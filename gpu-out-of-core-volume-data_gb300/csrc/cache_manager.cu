@@ -191,7 +191,6 @@ struct gc_cache {
     std::condition_variable cv;
     bool stop = false, has_request = false, busy = false, done = false, last_converged = false;
     uint32_t pend_n = 0, pend_nonempty = 0;
-    uint32_t resolve_n = 0;  // synchronous loader: misses of the last scan, resolved by the next update
     std::string loader_error;
     gc_cache_stats stats;
 
@@ -474,9 +473,9 @@ static void resolve_and_upload(gc_cache *C, uint32_t n) {
     C->stats.requests_served += n;
 }
 
-// Waits for the miss list of the last scan; returns the number of its
-// entries to load (at most max_requests).
-static uint32_t scan_wait(gc_cache *C) {
+// Waits for the miss list of the last scan and resolves it.  Returns true when
+// bricks are pending for install.
+static bool serve_request(gc_cache *C) {
     GC_CUDA(cudaSetDevice(C->device));
     GC_CUDA(cudaEventSynchronize(C->lists[C->cur_load].ev));
     // The previous upload has normally completed (its install ran before this
@@ -490,15 +489,9 @@ static uint32_t scan_wait(gc_cache *C) {
         C->upload_timed = false;
     }
     const uint32_t total = *C->lists[C->cur_load].total;
+    const uint32_t n = std::min(total, C->d.max_requests);
     C->stats.last_requests = total;
     C->stats.requests_raised += total;
-    return std::min(total, C->d.max_requests);
-}
-
-// Waits for the miss list of the last scan and resolves it.  Returns true when
-// bricks are pending for install.
-static bool serve_request(gc_cache *C) {
-    const uint32_t n = scan_wait(C);
     if (n == 0) return false;
     resolve_and_upload(C, n);
     return C->pend_n > 0;
@@ -635,29 +628,13 @@ static bool update(gc_cache *C, cudaStream_t s) {
     lru_update(C, s);
     bool converged = false;
     if (C->sync_mode()) {
-        // The frame after a scan installs its misses.  They are resolved here,
-        // not in the scan's update: the scan's update only waits for the miss
-        // count (the converged flag), and the host resolves while the frame
-        // rendered since then still runs, so the device does not wait for it;
-        // the upload goes beside that frame and the install after it.
-        bool scan = true;
-        if (C->done) {  // a load a batched tick left
+        if (C->done) {
             install(C, s);
             C->done = false;
-            scan = false;
-        } else if (C->resolve_n) {
-            const uint32_t n = C->resolve_n;
-            C->resolve_n = 0;
-            resolve_and_upload(C, n);
-            if (C->pend_n > 0) {
-                install(C, s);
-                scan = false;
-            }
-        }
-        if (scan) {
+        } else {
             scan_requests(C, s);
             C->cur_load = 0;  // the loader serves list 0 (an overlapped batch may have left 1)
-            C->resolve_n = scan_wait(C);
+            C->done = serve_request(C);
             converged = (C->stats.last_requests == 0);
         }
     } else {
@@ -1592,12 +1569,6 @@ namespace gc {
 // Installs what the loader finished.  Returns true when bricks were installed.
 static bool batch_install(gc_cache *C, cudaStream_t s) {
     if (C->sync_mode()) {
-        if (C->resolve_n) {  // misses a plain update scanned: resolved now
-            const uint32_t n = C->resolve_n;
-            C->resolve_n = 0;
-            resolve_and_upload(C, n);
-            C->done = C->pend_n > 0;
-        }
         if (!C->done) return false;
         const bool any = C->pend_n > 0;
         install(C, s);
