@@ -598,14 +598,16 @@ def run_ours(args):
     # list under ncu serialises launches and slows the upload's host reads)
     render_events = []
 
+    # clock samples from here to the end of the timed passes (the sampler's
+    # start-up overlaps the autotuning, not a timed pass)
+    clocks = ClockSampler()
+    clocks.start()
     # launch configuration: autotuned once, on three views spread along the
     # path (near, middle, far), in a cache of its own
     T = Session(gc, torch, cfg, vol, layout, store, offs, args.max_requests)
     n = cfg.get("frames", 120)
     tuned = [autotune(gc, torch, T, [spec(f)[0] for f in (n // 6, n // 2, 5 * n // 6)], args, per_view=True)]
     T.close()
-    clocks = ClockSampler()
-    clocks.start()
     S_e, wall_e, lat_e, _, _, s0_e, s1_e = plain_pass(True)
     S_e.close()
     S, wall, lat, info, launches, s0, s1 = plain_pass(False)
