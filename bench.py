@@ -1329,7 +1329,7 @@ def c4_serve(gc, torch, cfg, vols, stores, args):
     return out
 
 
-SERVING_RATES = (25.0, 50.0, 100.0, 200.0)  # requests per second tried by the default run
+SERVING_RATES = (25.0, 50.0, 75.0, 100.0, 200.0)  # requests per second tried by the default run
 SERVING_SECONDS = 2.0
 SERVING_P99_MS = 1000.0  # a rate is sustained while the p99 latency stays below this
 SERVING_KEEP_UP = 0.95  # ... and the server keeps up with at least this share of the offered rays
