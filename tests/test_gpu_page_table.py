@@ -201,3 +201,17 @@ def test_two_level_with_brick_bins(gc, torch_cuda):
         assert np.array_equal(ref[i], roomy[i]), i
         assert bins_diff(ref[i], small[i]).max() <= RESUME_TOL, i
     assert sr.device_error == 0 and ss.device_error == 0
+
+
+def test_two_level_arguments_are_checked(gc, torch_cuda):
+    """pt_block must be 0 or a power of two from 2 to 16, pt_slots at least 1."""
+    vol = gc.volume_desc((64, 64, 64), 16, 1, 1, 1)
+    layout = gc.compute_layout(vol)
+    for blk, slots in ((3, 8), (32, 8), (1, 8)):
+        with pytest.raises(gc.GcError, match="pt_block must be 0 or a power of two"):
+            gc.CacheManager(vol, layout, (4, 4, 4), max_requests=16, pt_block=blk, pt_slots=slots)
+    with pytest.raises(gc.GcError, match="pt_slots must be in"):
+        gc.CacheManager(vol, layout, (4, 4, 4), max_requests=16, pt_block=4, pt_slots=0)
+    cm = gc.CacheManager(vol, layout, (4, 4, 4), max_requests=16, pt_block=16, pt_slots=2)
+    assert cm.info.pt_block == 16 and cm.info.pt_slots == 2
+    cm.close()
