@@ -406,16 +406,18 @@ def test_coarser_level_fallback_preview(gc, orc, torch_cuda):
     assert np.array_equal(ref, img2)
 
 
-@pytest.mark.parametrize("mode", [0, 1])
-def test_coarser_level_fallback_matches_oracle(gc, orc, torch_cuda, mode):
+@pytest.mark.parametrize("mode,pt_block", [(0, 0), (1, 0), (0, 2)])
+def test_coarser_level_fallback_matches_oracle(gc, orc, torch_cuda, mode, pt_block):
     """The preview mode against the oracle's restatement of the level walk of
     K_CacheManager::get (K_CacheManager.hpp:163-260): a missing brick is
     requested on the asked level only, the first mapped coarser level is
     sampled instead, an empty one ends the lookup.  Coarse levels are paged in
     by a far view, then a near view is previewed frame by frame (progressive
     buffers restarted each frame, as the mode requires): RGBA, t buffer,
-    colour state and the cache state after every update equal the oracle's."""
-    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 60)
+    colour state and the cache state after every update equal the oracle's,
+    with the one-level and the two-level page directory."""
+    s = Scene(gc, orc, torch_cuda, (64, 64, 64), 1, 16, 1, (1, 1, 1), (6, 6, 6), 60, pt_block=pt_block,
+              pt_slots=64 if pt_block else 0)
     tf = scenario.ramp_tf() if mode == 0 else scenario.bumps_tf(4)
     tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
     W, H = 72, 56
