@@ -107,14 +107,16 @@ def test_render_update_loop_matches_oracle(gc, orc, torch_cuda, case):
     assert st.bricks_installed > 0 and st.device_error == 0
 
 
-@pytest.mark.parametrize("mode,sampler", [(0, 0), (0, 1), (1, 0)])
-def test_two_channel_2d_tf_loop_matches_oracle(gc, orc, torch_cuda, mode, sampler):
+@pytest.mark.parametrize("mode,sampler,pt_block", [(0, 0, 0), (0, 1, 0), (1, 0, 0), (0, 1, 4)])
+def test_two_channel_2d_tf_loop_matches_oracle(gc, orc, torch_cuda, mode, sampler, pt_block):
     """Two 8-bit channels (blob field + independent noise field, interleaved)
     rendered with a 2D transfer function, covering 2 and big bricks 2^3 (the
     c5 brick layout): RGBA, t buffer and colour state bit-exact vs the FP32
-    oracle every frame, cache state bit-exact.  (No reference counterpart:
-    the reference ray caster reads one channel.)"""
-    s = Scene(gc, orc, torch_cuda, (72, 64, 56), 1, 16, 2, (2, 2, 2), (6, 6, 6), 100, channels=2, seed=33)
+    oracle every frame, cache state bit-exact; also through a two-level page
+    directory whose table pool holds 6 of its blocks.  (No reference
+    counterpart: the reference ray caster reads one channel.)"""
+    s = Scene(gc, orc, torch_cuda, (72, 64, 56), 1, 16, 2, (2, 2, 2), (6, 6, 6), 100, channels=2, seed=33,
+              pt_block=pt_block, pt_slots=6 if pt_block else 0)
     tf = scenario.tf2d(5)
     th, tw = tf.shape[:2]
     tf_dev = torch_cuda.from_numpy(tf.reshape(-1)).cuda()
