@@ -656,7 +656,10 @@ class CacheManager:
         return s
 
     def dump(self, what, buf):
-        """Copies one state buffer into a writable host buffer (numpy array)."""
+        """Copies one state buffer into a writable host buffer (numpy array):
+        DUMP_MRPD / LRU / USAGE / REQUESTS / POOL, and for a two-level page
+        directory DUMP_PT_TOP / PT_POOL / PT_LRU / PT_USAGE / PT_KEYS (sizes and
+        layouts in include/gc_gb300.h)."""
         check(lib.gc_cache_dump(self._h, what, vp(buf.ctypes.data), buf.nbytes))
         return buf
 

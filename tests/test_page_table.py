@@ -136,3 +136,23 @@ def test_two_level_directory_evicting(gc, orc, pt_block, pt_slots):
         for a, b in zip(*images):
             assert np.array_equal(a, b), f"view {k}"
     assert replaced > 0, "no table block was evicted"
+
+
+@pytest.mark.parametrize("size,B,c,P", [((64, 48, 56), 8, 1, 4), ((96, 96, 96), 16, 1, 2), ((200, 64, 33), 16, 2, 8),
+                                        ((256, 256, 256), 32, 1, 16)])
+def test_directory_geometry(gc, orc, size, B, c, P):
+    """The directory of a two-level cache holds ceil(bricks / P) words per
+    axis and level (CacheManager.hpp:160-176: realNumberOfEntries of the
+    table level), levels packed along x, like the one-level directory."""
+    vol = gc.volume_desc(size, B, c, 1, 1, (1, 1, 1))
+    layout = gc.compute_layout(vol)
+    d = gc.CacheDesc(vol, layout, gc.u3((4, 4, 4)), 16, gc.CACHE_SYNC_LOADER, 0, P, 8)
+    oc = orc.Cache(d)
+    nb = [tuple(layout.nb_bricks[l]) for l in range(layout.nb_levels)]
+    words = [tuple(-(-n // P) for n in b) for b in nb]
+    assert oc.pt_dims == (sum(w[0] for w in words), max(w[1] for w in words), max(w[2] for w in words))
+    assert oc.pt_block == P and oc.pt_slots == 8
+    assert oc.mrpd_dims == (sum(b[0] for b in nb), max(b[1] for b in nb), max(b[2] for b in nb))
+    assert (oc.pt_top() == 0).all() and (oc.pt_keys() == 0xFFFFFFFF).all()
+    assert list(oc.pt_order()) == list(range(8))
+    oc.close()
